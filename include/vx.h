@@ -1,0 +1,145 @@
+/*
+ * vx.h — C ABI of the GB300 Vlasov–Maxwell step (libvx_cuda.so).
+ *
+ * The reference (Veritas, C++14/OpenMP) has no plugin or FFI surface: its driver calls
+ * C++ class methods.  Each entry point below replaces one of those methods for the
+ * per-step path; the citation after each declaration names the reference interface it
+ * stands in for (file:line in the Veritas source tree).
+ *
+ * Conventions
+ *   - Every function returns 0 on success or a negative VX_ERR_* code; the message of
+ *     the last failure on the calling thread is available from vx_last_error().  No
+ *     function calls exit() (the reference exits on configuration errors,
+ *     Settings.cpp:35-50).
+ *   - A context owns one CUDA device and one stream; all device memory of its runs is
+ *     owned by the context.  Host pointers passed in are borrowed for the call only.
+ *   - Calls on one context must come from one thread at a time; different contexts are
+ *     independent.
+ */
+#ifndef VX_H_
+#define VX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VX_OK 0
+#define VX_ERR_INVALID -1   /* bad argument or configuration */
+#define VX_ERR_CUDA -2      /* CUDA runtime error */
+#define VX_ERR_STATE -3     /* operation not valid in the current state */
+#define VX_ERR_IO -4        /* file read/write failure */
+#define VX_ERR_NOMEM -5     /* device memory budget exceeded */
+#define VX_ERR_TIMEOUT -6   /* bounded device wait expired */
+#define VX_ERR_UNSUPPORTED -7
+
+typedef struct vx_ctx vx_ctx;
+typedef struct vx_run vx_run;
+
+/* Built-in synthetic laser / plasma-slab problem: the hooks a Veritas user writes in
+ * veritas.cpp (initialConditions :7, settingsOverride :36, InitialDistribution :107,
+ * GetBY/GetBZ :80/:93, RefinementOverride :76).  Lengths in laser wavelengths, momenta
+ * in m_e c, temperatures in keV. */
+typedef struct vx_problem {
+    double lambda;     /* laser wavelength [m] */
+    double L;          /* domain length [lambda] */
+    uint32_t nx, np, Lfinest, r;
+    double pmax;       /* p in [-pmax, pmax] */
+    double dens;       /* plateau density / n_c */
+    double x1, x2, x3, x4; /* up-ramp [x1,x2], plateau [x2,x3], down-ramp [x3,x4] */
+    double Te;         /* electron temperature [keV] */
+    double p0;         /* drift momentum */
+    double pert_amp, pert_k; /* density modulation amplitude and mode number */
+    double a0, fwhm, delay;  /* laser amplitude, field-envelope FWHM and delay [periods] */
+    double cfl, minEff, crit, sizeWeight;
+    int32_t quadDepth;
+    int32_t precision; /* 64: plain FP64 path; 32: FP32 precision form */
+} vx_problem;
+
+/* Fills *p with the defaults of the 2048 x 256 single-level laser/slab case. */
+void vx_problem_defaults(vx_problem *p);
+
+const char *vx_last_error(void);
+
+/* Context: one GPU + one stream. */
+int vx_ctx_create(int device, vx_ctx **out);
+int vx_ctx_destroy(vx_ctx *ctx);
+int vx_ctx_sync(vx_ctx *ctx);
+/* Kernels launched by this context so far (graph replays count their nodes). */
+int vx_ctx_kernel_launches(vx_ctx *ctx, uint64_t *out);
+
+/* SolverManager::SolverManager (SolverManager.cpp:8-26): Settings from the problem hooks
+ * (Settings.cpp:5-54), initial hierarchy and distribution (Mesh.cpp:8-50,
+ * Rectangle.cpp:616-665), field solver set-up (EMSolver.cpp:6-89) and charge
+ * neutralisation (EMSolver.cpp:621-629). */
+int vx_run_create(vx_ctx *ctx, const vx_problem *prob, vx_run **out);
+int vx_run_destroy(vx_run *run);
+
+/* SolverManager::CalculateDt (SolverManager.cpp:162-164 -> EMSolver.cpp:631-664). */
+int vx_run_calculate_dt(vx_run *run, double *dt);
+/* SolverManager::Advance (SolverManager.cpp:28-39): one six-stage RK step of every
+ * species and the fields.  Asynchronous on the context stream. */
+int vx_run_advance(vx_run *run, double dt);
+/* Advance several runs of one context together, one launch per sub-step for all of
+ * them (batched form).  dt[i] belongs to runs[i]. */
+int vx_runs_advance(vx_run *const *runs, const double *dt, int nruns);
+
+/* Simulation time (Settings::time, Settings.cpp:166-179). */
+int vx_run_time(vx_run *run, double *t);
+/* Total phase-space cells of all patches of all species and levels. */
+int vx_run_cell_count(vx_run *run, int64_t *cells);
+
+/* Checkpoint / parity exchange in the binary layout the parity harness writes
+ * ("VXST0001": time, dt, Ex0, field arrays with their 8 RK slots, then every patch's
+ * 3-slot f block in the reference's Index3 order, Rectangle.hpp:96). */
+int vx_run_load_state(vx_run *run, const char *path);
+int vx_run_save_state(vx_run *run, const char *path);
+
+/* Copy field arrays to host memory.  which: 0 By, 1 Bz, 2 Ey, 3 Ez, 4 Ay, 5 Az (slot 0,
+ * n+pre+post values), 6 a_squared (n+1), 7 phi (n), 8 charge (n), 9 J (n), 10 E_x on the
+ * finest grid (n).  *len receives the element count; out may be NULL to query it. */
+int vx_run_get_field(vx_run *run, int which, double *out, int64_t *len);
+
+/* ---- measurement and host-buffer entry points ------------------------------------ */
+
+/* Device time between two points on the context stream (CUDA events). */
+int vx_ctx_timer_begin(vx_ctx *ctx);
+int vx_ctx_timer_end(vx_ctx *ctx, double *ms);
+
+/* Time the run's Vlasov kernels in isolation: reps back-to-back launches per kernel on
+ * the context stream (after one untimed launch).  out_ms[k] receives the mean launch
+ * time of kernel k in the order gamma, faces, flux, ds_f2, limR, limC, update,
+ * moments (log table + ordered sums), assemble; *count is set to the number of entries
+ * written (<= cap).  Each timed kernel is idempotent, so the run's state is unchanged. */
+int vx_run_profile_kernels(vx_run *run, int reps, double *out_ms, int cap, int *count);
+
+/* Overwrite a device buffer larger than the L2 cache on the context stream, so the next
+ * timed region starts with a cold L2. */
+int vx_ctx_flush_l2(vx_ctx *ctx);
+
+/* Measured FP64 FMA throughput of this GPU in GFLOP/s (2 flops per FMA): a register-
+ * resident DFMA chain kernel timed with CUDA events on the context stream. */
+int vx_ctx_measure_fp64_peak(vx_ctx *ctx, double *gflops);
+
+/* Page-locked host memory for host-buffer calls. */
+int vx_host_alloc(size_t bytes, void **out);
+int vx_host_free(void *p);
+
+/* Packed host image of a run's state at a step boundary: every patch's f (slot 0,
+ * padded (n_x+4) x pitch block, patch order species -> level -> patch), then the six
+ * transverse field arrays (slot 0, n+pre+post each), a_squared (n+1) and Ex0.  *len
+ * receives the element count. */
+int vx_run_state_size(vx_run *run, int64_t *len);
+/* Copy the run's current state into a packed host image (D2H only). */
+int vx_run_state_to_host(vx_run *run, double *state_out);
+/* End-to-end step with host buffers (Veritas's driver loop calling
+ * SolverManager::Advance on state that lives in host memory): copy state_in to the
+ * device, run one RK step with dt, copy the new state to state_out. */
+int vx_run_step_host(vx_run *run, const double *state_in, double *state_out, double dt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VX_H_ */

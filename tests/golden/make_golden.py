@@ -1,0 +1,64 @@
+"""Generate the golden parity fixtures by running the reference Veritas build.
+
+The reference (its unmodified sources) is compiled by ``oracle/ref/build_ref.sh`` into
+``oracle/_ref/veritas_ref`` together with the harness problem file; this script runs it
+for each case below and stores the dumped states as compressed ``.npz`` files next to
+this script.  It needs the reference tree, so it only runs where that tree is mounted:
+
+    python tests/golden/make_golden.py [--ref /path/to/veritas/sources]
+
+Cases are small enough for the oracle to finish in seconds; every parameter is the
+harness's key=value argument.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+sys.path.insert(0, str(HERE.parent))
+import vxstate  # noqa: E402
+
+# name -> (harness args, steps, states to keep)
+CASES = {
+    # Plasma slab with a density modulation and a strong injected pulse on 64 x 32 cells.
+    "slab64": (["L=8", "nx=64", "np=32", "Te=50", "pmax=2", "x1=1.5", "x2=2", "x3=6", "x4=6.5", "pert_amp=0.2",
+                "pert_k=2", "a0=2", "fwhm=2", "delay=1", "levels=1"], 5, [0, 1, 2, 5]),
+    # Drifting plasma (net current) on 128 x 64 cells.
+    "drift128": (["L=16", "nx=128", "np=64", "Te=20", "pmax=1.5", "p0=0.15", "x1=3", "x2=4", "x3=12", "x4=13",
+                  "pert_amp=0.1", "pert_k=3", "a0=1.5", "fwhm=3", "delay=1.5", "levels=1"], 3, [0, 1, 3]),
+    # Plasma touching both x edges and both p edges: exercises the skipped domain-edge faces.
+    "edge64": (["L=4", "nx=64", "np=32", "Te=50", "pmax=0.5", "x1=-1", "x2=0", "x3=3", "x4=5", "pert_amp=0.3",
+                "pert_k=1", "a0=1", "fwhm=2", "delay=0.5", "levels=1"], 3, [0, 1, 3]),
+}
+
+
+def run_case(exe: Path, name: str, args: list[str], steps: int, keep: list[int]) -> None:
+    with tempfile.TemporaryDirectory() as td:
+        env = dict(os.environ, OMP_NUM_THREADS="4")
+        cmd = [str(exe), *args, f"steps={steps}", "dump_every=1", f"dumpdir={td}"]
+        subprocess.run(cmd, check=True, env=env, stdout=subprocess.DEVNULL)
+        for k in keep:
+            st = vxstate.read_state(Path(td) / f"state_{k:05d}.bin")
+            vxstate.to_npz(st, HERE / f"{name}_s{k}.npz")
+    (HERE / f"{name}.args").write_text(" ".join(args) + "\n")
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    a = ap.parse_args()
+    subprocess.run(["bash", str(REPO / "oracle" / "ref" / "build_ref.sh"), a.ref], check=True)
+    exe = REPO / "oracle" / "_ref" / "veritas_ref"
+    for name, (args, steps, keep) in CASES.items():
+        run_case(exe, name, args, steps, keep)
+        print("wrote", name)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,307 @@
+"""GB300-native Vlasov–Maxwell step (Veritas per-step path) — Python mirror of the C ABI.
+
+The classes follow the reference's driver interface: :class:`SolverManager` stands in for
+Veritas's ``SolverManager`` (SolverManager.hpp:5-19) with ``CalculateDt``, ``Advance``
+and the state exchange used for checkpoints and parity tests.  Every call goes through
+``libvx_cuda.so`` (declared in ``include/vx.h``); there is no CPU fallback — if the
+library cannot be loaded, importing this module raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, fields
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libvx_cuda.so"
+
+VX_ERRORS = {
+    -1: "invalid argument",
+    -2: "CUDA error",
+    -3: "invalid state",
+    -4: "I/O error",
+    -5: "out of device memory",
+    -6: "device wait timed out",
+    -7: "unsupported",
+}
+
+
+class VxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{VX_ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _Problem(ctypes.Structure):
+    _fields_ = [
+        ("lambda_", ctypes.c_double), ("L", ctypes.c_double),
+        ("nx", ctypes.c_uint32), ("np", ctypes.c_uint32), ("Lfinest", ctypes.c_uint32), ("r", ctypes.c_uint32),
+        ("pmax", ctypes.c_double), ("dens", ctypes.c_double),
+        ("x1", ctypes.c_double), ("x2", ctypes.c_double), ("x3", ctypes.c_double), ("x4", ctypes.c_double),
+        ("Te", ctypes.c_double), ("p0", ctypes.c_double), ("pert_amp", ctypes.c_double), ("pert_k", ctypes.c_double),
+        ("a0", ctypes.c_double), ("fwhm", ctypes.c_double), ("delay", ctypes.c_double),
+        ("cfl", ctypes.c_double), ("minEff", ctypes.c_double), ("crit", ctypes.c_double), ("sizeWeight", ctypes.c_double),
+        ("quadDepth", ctypes.c_int32), ("precision", ctypes.c_int32),
+    ]
+
+
+def _load() -> ctypes.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'` first")
+    lib = ctypes.CDLL(str(LIB_PATH))
+    P = ctypes.POINTER
+    vp = ctypes.c_void_p
+    sig = {
+        "vx_problem_defaults": (None, [P(_Problem)]),
+        "vx_last_error": (ctypes.c_char_p, []),
+        "vx_ctx_create": (ctypes.c_int, [ctypes.c_int, P(vp)]),
+        "vx_ctx_destroy": (ctypes.c_int, [vp]),
+        "vx_ctx_sync": (ctypes.c_int, [vp]),
+        "vx_ctx_kernel_launches": (ctypes.c_int, [vp, P(ctypes.c_uint64)]),
+        "vx_run_create": (ctypes.c_int, [vp, P(_Problem), P(vp)]),
+        "vx_run_destroy": (ctypes.c_int, [vp]),
+        "vx_run_calculate_dt": (ctypes.c_int, [vp, P(ctypes.c_double)]),
+        "vx_run_advance": (ctypes.c_int, [vp, ctypes.c_double]),
+        "vx_runs_advance": (ctypes.c_int, [P(vp), P(ctypes.c_double), ctypes.c_int]),
+        "vx_run_time": (ctypes.c_int, [vp, P(ctypes.c_double)]),
+        "vx_run_cell_count": (ctypes.c_int, [vp, P(ctypes.c_int64)]),
+        "vx_run_load_state": (ctypes.c_int, [vp, ctypes.c_char_p]),
+        "vx_run_save_state": (ctypes.c_int, [vp, ctypes.c_char_p]),
+        "vx_run_get_field": (ctypes.c_int, [vp, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_int64)]),
+        "vx_ctx_timer_begin": (ctypes.c_int, [vp]),
+        "vx_ctx_timer_end": (ctypes.c_int, [vp, P(ctypes.c_double)]),
+        "vx_run_profile_kernels": (ctypes.c_int, [vp, ctypes.c_int, P(ctypes.c_double), ctypes.c_int, P(ctypes.c_int)]),
+        "vx_ctx_flush_l2": (ctypes.c_int, [vp]),
+        "vx_ctx_measure_fp64_peak": (ctypes.c_int, [vp, P(ctypes.c_double)]),
+        "vx_host_alloc": (ctypes.c_int, [ctypes.c_size_t, P(vp)]),
+        "vx_host_free": (ctypes.c_int, [vp]),
+        "vx_run_state_size": (ctypes.c_int, [vp, P(ctypes.c_int64)]),
+        "vx_run_step_host": (ctypes.c_int, [vp, P(ctypes.c_double), P(ctypes.c_double), ctypes.c_double]),
+        "vx_run_state_to_host": (ctypes.c_int, [vp, P(ctypes.c_double)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+_lib = _load()
+
+
+def lib() -> ctypes.CDLL:
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise VxError(rc, (_lib.vx_last_error() or b"").decode())
+
+
+@dataclass
+class Problem:
+    """Synthetic laser / plasma-slab problem (the hooks of the reference's veritas.cpp)."""
+
+    lambda_: float = 1e-6
+    L: float = 100.0
+    nx: int = 2048
+    np: int = 256
+    Lfinest: int = 1
+    r: int = 2
+    pmax: float = 2.0
+    dens: float = 0.01
+    x1: float = 15.0
+    x2: float = 20.0
+    x3: float = 80.0
+    x4: float = 85.0
+    Te: float = 1.0
+    p0: float = 0.0
+    pert_amp: float = 0.0
+    pert_k: float = 1.0
+    a0: float = 1.0
+    fwhm: float = 10.0
+    delay: float = 10.0
+    cfl: float = 0.5
+    minEff: float = 0.75
+    crit: float = 1e-6
+    sizeWeight: float = 1.0
+    quadDepth: int = 2
+    precision: int = 64
+
+    def to_c(self) -> _Problem:
+        p = _Problem()
+        for f in fields(self):
+            setattr(p, f.name, getattr(self, f.name))
+        return p
+
+    def harness_args(self) -> list[str]:
+        """key=value arguments of the oracle harness for the same problem."""
+        keys = ["L", "nx", "np", "r", "pmax", "dens", "x1", "x2", "x3", "x4", "Te", "p0", "pert_amp", "pert_k",
+                "a0", "fwhm", "delay", "cfl", "minEff", "crit", "sizeWeight", "quadDepth"]
+        out = [f"{k}={getattr(self, k)!r}" for k in keys]
+        out.append(f"levels={self.Lfinest}")
+        return out
+
+
+class Context:
+    """One GPU and one CUDA stream (vx_ctx)."""
+
+    def __init__(self, device: int = 0):
+        h = ctypes.c_void_p()
+        _check(_lib.vx_ctx_create(device, ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def sync(self) -> None:
+        _check(_lib.vx_ctx_sync(self._h))
+
+    def kernel_launches(self) -> int:
+        v = ctypes.c_uint64()
+        _check(_lib.vx_ctx_kernel_launches(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    def timer_begin(self) -> None:
+        _check(_lib.vx_ctx_timer_begin(self._h))
+
+    def timer_end(self) -> float:
+        v = ctypes.c_double()
+        _check(_lib.vx_ctx_timer_end(self._h, ctypes.byref(v)))
+        return float(v.value)
+
+    def flush_l2(self) -> None:
+        _check(_lib.vx_ctx_flush_l2(self._h))
+
+    def measure_fp64_peak(self) -> float:
+        v = ctypes.c_double()
+        _check(_lib.vx_ctx_measure_fp64_peak(self._h, ctypes.byref(v)))
+        return float(v.value)
+
+    def close(self) -> None:
+        if self._h:
+            _check(_lib.vx_ctx_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+FIELD_IDS = {"By": 0, "Bz": 1, "Ey": 2, "Ez": 3, "Ay": 4, "Az": 5, "a_squared": 6, "phi": 7, "charge": 8, "J": 9,
+             "Ex": 10}
+
+
+class SolverManager:
+    """One independent solve on a context (the reference's SolverManager)."""
+
+    def __init__(self, ctx: Context, problem: Problem):
+        self.ctx = ctx
+        self.problem = problem
+        h = ctypes.c_void_p()
+        _check(_lib.vx_run_create(ctx.handle, ctypes.byref(problem.to_c()), ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def CalculateDt(self) -> float:
+        v = ctypes.c_double()
+        _check(_lib.vx_run_calculate_dt(self._h, ctypes.byref(v)))
+        return float(v.value)
+
+    def Advance(self, dt: float) -> None:
+        _check(_lib.vx_run_advance(self._h, float(dt)))
+
+    @property
+    def time(self) -> float:
+        v = ctypes.c_double()
+        _check(_lib.vx_run_time(self._h, ctypes.byref(v)))
+        return float(v.value)
+
+    def cell_count(self) -> int:
+        v = ctypes.c_int64()
+        _check(_lib.vx_run_cell_count(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    def load_state(self, path: str | os.PathLike) -> None:
+        _check(_lib.vx_run_load_state(self._h, str(path).encode()))
+
+    def save_state(self, path: str | os.PathLike) -> None:
+        _check(_lib.vx_run_save_state(self._h, str(path).encode()))
+
+    def field(self, name: str) -> np.ndarray:
+        n = ctypes.c_int64()
+        fid = FIELD_IDS[name]
+        _check(_lib.vx_run_get_field(self._h, fid, None, ctypes.byref(n)))
+        out = np.empty(n.value, dtype=np.float64)
+        _check(_lib.vx_run_get_field(self._h, fid, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(n)))
+        return out
+
+    PROFILE_KERNELS = ["gamma", "faces", "flux", "ds_f2", "limR", "limC", "update", "moments", "assemble"]
+
+    def profile_kernels(self, reps: int = 5) -> dict:
+        buf = (ctypes.c_double * 16)()
+        cnt = ctypes.c_int()
+        _check(_lib.vx_run_profile_kernels(self._h, reps, buf, 16, ctypes.byref(cnt)))
+        return {self.PROFILE_KERNELS[i]: float(buf[i]) for i in range(cnt.value)}
+
+    def state_size(self) -> int:
+        v = ctypes.c_int64()
+        _check(_lib.vx_run_state_size(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    def state_to_host(self, out: np.ndarray) -> None:
+        _check(_lib.vx_run_state_to_host(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+
+    def step_host(self, state_in: np.ndarray, state_out: np.ndarray, dt: float) -> None:
+        dp = ctypes.POINTER(ctypes.c_double)
+        _check(_lib.vx_run_step_host(self._h, state_in.ctypes.data_as(dp), state_out.ctypes.data_as(dp), float(dt)))
+
+    def close(self) -> None:
+        if self._h:
+            _check(_lib.vx_run_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PinnedArray:
+    """Page-locked float64 host buffer (cudaMallocHost through the C ABI)."""
+
+    def __init__(self, n: int):
+        p = ctypes.c_void_p()
+        _check(_lib.vx_host_alloc(max(8, 8 * n), ctypes.byref(p)))
+        self._p = p
+        buf = (ctypes.c_double * n).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=np.float64, count=n)
+
+    def close(self) -> None:
+        if self._p:
+            self.array = None
+            _check(_lib.vx_host_free(self._p))
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def advance_many(runs: list[SolverManager], dts: list[float]) -> None:
+    """Advance several runs of one context together (batched launch per sub-step)."""
+    arr = (ctypes.c_void_p * len(runs))(*[r.handle for r in runs])
+    d = (ctypes.c_double * len(runs))(*dts)
+    _check(_lib.vx_runs_advance(arr, d, len(runs)))

@@ -1,0 +1,286 @@
+// extern "C" entry points declared in include/vx.h.
+#include <cstring>
+#include <string>
+
+#include "../../include/vx.h"
+#include "engine.hpp"
+
+struct vx_ctx {
+    std::unique_ptr<vx::Engine> eng;
+};
+struct vx_run {
+    vx_ctx *ctx;
+    std::unique_ptr<vx::Run> run;
+};
+
+namespace {
+thread_local std::string g_err;
+
+template <class F>
+int guard(F &&f) {
+    try {
+        f();
+        return VX_OK;
+    } catch (const vx::CudaError &e) {
+        g_err = e.what();
+        return VX_ERR_CUDA;
+    } catch (const std::invalid_argument &e) {
+        g_err = e.what();
+        return VX_ERR_INVALID;
+    } catch (const std::bad_alloc &e) {
+        g_err = e.what();
+        return VX_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return VX_ERR_STATE;
+    }
+}
+
+vx::LaserSlabParams to_params(const vx_problem &p) {
+    vx::LaserSlabParams q;
+    q.lambda = p.lambda;
+    q.L = p.L;
+    q.nx = p.nx;
+    q.np = p.np;
+    q.Lfinest = p.Lfinest;
+    q.r = p.r;
+    q.pmax = p.pmax;
+    q.dens = p.dens;
+    q.x1 = p.x1;
+    q.x2 = p.x2;
+    q.x3 = p.x3;
+    q.x4 = p.x4;
+    q.Te = p.Te;
+    q.p0 = p.p0;
+    q.pert_amp = p.pert_amp;
+    q.pert_k = p.pert_k;
+    q.a0 = p.a0;
+    q.fwhm = p.fwhm;
+    q.delay = p.delay;
+    q.cfl = p.cfl;
+    q.minEff = p.minEff;
+    q.crit = p.crit;
+    q.sizeWeight = p.sizeWeight;
+    q.quadDepth = p.quadDepth;
+    return q;
+}
+}  // namespace
+
+extern "C" {
+
+void vx_problem_defaults(vx_problem *p) {
+    vx::LaserSlabParams d;
+    std::memset(p, 0, sizeof *p);
+    p->lambda = d.lambda;
+    p->L = d.L;
+    p->nx = d.nx;
+    p->np = d.np;
+    p->Lfinest = d.Lfinest;
+    p->r = d.r;
+    p->pmax = d.pmax;
+    p->dens = d.dens;
+    p->x1 = d.x1;
+    p->x2 = d.x2;
+    p->x3 = d.x3;
+    p->x4 = d.x4;
+    p->Te = d.Te;
+    p->p0 = d.p0;
+    p->pert_amp = d.pert_amp;
+    p->pert_k = d.pert_k;
+    p->a0 = d.a0;
+    p->fwhm = d.fwhm;
+    p->delay = d.delay;
+    p->cfl = d.cfl;
+    p->minEff = d.minEff;
+    p->crit = d.crit;
+    p->sizeWeight = d.sizeWeight;
+    p->quadDepth = d.quadDepth;
+    p->precision = 64;
+}
+
+const char *vx_last_error(void) { return g_err.c_str(); }
+
+int vx_ctx_create(int device, vx_ctx **out) {
+    if (!out) return VX_ERR_INVALID;
+    return guard([&] {
+        auto c = new vx_ctx;
+        try {
+            c->eng.reset(new vx::Engine(device));
+        } catch (...) {
+            delete c;
+            throw;
+        }
+        *out = c;
+    });
+}
+
+int vx_ctx_destroy(vx_ctx *ctx) {
+    if (!ctx) return VX_ERR_INVALID;
+    return guard([&] { delete ctx; });
+}
+
+int vx_ctx_sync(vx_ctx *ctx) {
+    if (!ctx) return VX_ERR_INVALID;
+    return guard([&] { ctx->eng->sync(); });
+}
+
+int vx_ctx_kernel_launches(vx_ctx *ctx, uint64_t *out) {
+    if (!ctx || !out) return VX_ERR_INVALID;
+    *out = ctx->eng->kernel_launches;
+    return VX_OK;
+}
+
+int vx_run_create(vx_ctx *ctx, const vx_problem *prob, vx_run **out) {
+    if (!ctx || !prob || !out) return VX_ERR_INVALID;
+    return guard([&] {
+        if (prob->precision != 64) throw std::invalid_argument("only precision 64 is available in this build");
+        auto r = std::make_unique<vx_run>();
+        r->ctx = ctx;
+        r->run.reset(new vx::Run(*ctx->eng, std::make_shared<vx::LaserSlab>(to_params(*prob))));
+        r->run->init();
+        ctx->eng->runs.push_back(r->run.get());
+        *out = r.release();
+    });
+}
+
+int vx_run_destroy(vx_run *run) {
+    if (!run) return VX_ERR_INVALID;
+    return guard([&] {
+        run->ctx->eng->sync();
+        delete run;
+    });
+}
+
+int vx_run_calculate_dt(vx_run *run, double *dt) {
+    if (!run || !dt) return VX_ERR_INVALID;
+    return guard([&] { *dt = run->run->calculate_dt(); });
+}
+
+int vx_run_advance(vx_run *run, double dt) {
+    if (!run || !(dt >= 0)) return VX_ERR_INVALID;
+    return guard([&] { run->run->advance(dt); });
+}
+
+int vx_runs_advance(vx_run *const *runs, const double *dt, int nruns) {
+    if (!runs || !dt || nruns <= 0) return VX_ERR_INVALID;
+    return guard([&] {
+        std::vector<vx::Run *> set;
+        std::vector<double> d;
+        vx_ctx *c = runs[0]->ctx;
+        for (int i = 0; i < nruns; i++) {
+            if (!runs[i] || runs[i]->ctx != c) throw std::invalid_argument("runs must belong to one context");
+            set.push_back(runs[i]->run.get());
+            d.push_back(dt[i]);
+        }
+        c->eng->advance(set, d);
+    });
+}
+
+int vx_run_time(vx_run *run, double *t) {
+    if (!run || !t) return VX_ERR_INVALID;
+    *t = run->run->S->time;
+    return VX_OK;
+}
+
+int vx_run_cell_count(vx_run *run, int64_t *cells) {
+    if (!run || !cells) return VX_ERR_INVALID;
+    *cells = run->run->cell_count();
+    return VX_OK;
+}
+
+int vx_run_load_state(vx_run *run, const char *path) {
+    if (!run || !path) return VX_ERR_INVALID;
+    int rc = guard([&] { run->run->load_state(path); });
+    return (rc == VX_ERR_STATE) ? VX_ERR_IO : rc;
+}
+
+int vx_run_save_state(vx_run *run, const char *path) {
+    if (!run || !path) return VX_ERR_INVALID;
+    int rc = guard([&] { run->run->save_state(path); });
+    return (rc == VX_ERR_STATE) ? VX_ERR_IO : rc;
+}
+
+int vx_run_get_field(vx_run *run, int which, double *out, int64_t *len) {
+    if (!run || !len) return VX_ERR_INVALID;
+    return guard([&] {
+        vx::Run &R = *run->run;
+        const double *src = nullptr;
+        int64_t n = 0;
+        switch (which) {
+            case 0: src = R.F.By; n = R.nf; break;
+            case 1: src = R.F.Bz; n = R.nf; break;
+            case 2: src = R.F.Ey; n = R.nf; break;
+            case 3: src = R.F.Ez; n = R.nf; break;
+            case 4: src = R.F.Ay; n = R.nf; break;
+            case 5: src = R.F.Az; n = R.nf; break;
+            case 6: src = R.F.asq; n = R.n + 1; break;
+            case 7: src = R.F.phi; n = R.n; break;
+            case 8: src = R.F.charge; n = R.n; break;
+            case 9: src = R.F.J; n = R.n; break;
+            case 10: src = R.F.efin; n = R.n; break;
+            default: throw std::invalid_argument("unknown field id");
+        }
+        *len = n;
+        if (out) {
+            R.eng.sync();
+            VX_CUDA(cudaMemcpy(out, src, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+        }
+    });
+}
+
+int vx_ctx_timer_begin(vx_ctx *ctx) {
+    if (!ctx) return VX_ERR_INVALID;
+    return guard([&] { ctx->eng->timer_begin(); });
+}
+
+int vx_ctx_timer_end(vx_ctx *ctx, double *ms) {
+    if (!ctx || !ms) return VX_ERR_INVALID;
+    return guard([&] { *ms = ctx->eng->timer_end(); });
+}
+
+int vx_run_profile_kernels(vx_run *run, int reps, double *out_ms, int cap, int *count) {
+    if (!run || !out_ms || !count || reps <= 0 || cap <= 0) return VX_ERR_INVALID;
+    return guard([&] {
+        auto v = run->ctx->eng->profile_kernels(*run->run, reps);
+        int k = 0;
+        for (; k < (int)v.size() && k < cap; k++) out_ms[k] = v[k];
+        *count = k;
+    });
+}
+
+int vx_ctx_flush_l2(vx_ctx *ctx) {
+    if (!ctx) return VX_ERR_INVALID;
+    return guard([&] { ctx->eng->flush_l2(); });
+}
+
+int vx_ctx_measure_fp64_peak(vx_ctx *ctx, double *gflops) {
+    if (!ctx || !gflops) return VX_ERR_INVALID;
+    return guard([&] { *gflops = ctx->eng->measure_fp64_peak(); });
+}
+
+int vx_host_alloc(size_t bytes, void **out) {
+    if (!out || bytes == 0) return VX_ERR_INVALID;
+    return guard([&] { VX_CUDA(cudaMallocHost(out, bytes)); });
+}
+
+int vx_host_free(void *p) {
+    if (!p) return VX_ERR_INVALID;
+    return guard([&] { VX_CUDA(cudaFreeHost(p)); });
+}
+
+int vx_run_state_size(vx_run *run, int64_t *len) {
+    if (!run || !len) return VX_ERR_INVALID;
+    return guard([&] { *len = run->run->state_size(); });
+}
+
+int vx_run_state_to_host(vx_run *run, double *state_out) {
+    if (!run || !state_out) return VX_ERR_INVALID;
+    return guard([&] { run->run->state_to_host(state_out); });
+}
+
+int vx_run_step_host(vx_run *run, const double *state_in, double *state_out, double dt) {
+    if (!run || !state_in || !state_out || !(dt >= 0)) return VX_ERR_INVALID;
+    return guard([&] { run->run->step_host(state_in, state_out, dt); });
+}
+
+}  // extern "C"

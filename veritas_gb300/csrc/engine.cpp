@@ -1,0 +1,730 @@
+#include "engine.hpp"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <thread>
+
+namespace vx {
+
+void cuda_check(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+DevBuf::DevBuf(size_t b) : bytes(b) {
+    if (b) {
+        VX_CUDA(cudaMalloc(&p, b));
+        VX_CUDA(cudaMemset(p, 0, b));
+    }
+}
+DevBuf::~DevBuf() {
+    if (p) cudaFree(p);
+}
+DevBuf &DevBuf::operator=(DevBuf &&o) noexcept {
+    if (this != &o) {
+        if (p) cudaFree(p);
+        p = o.p;
+        bytes = o.bytes;
+        o.p = nullptr;
+        o.bytes = 0;
+    }
+    return *this;
+}
+
+template <class T>
+static DevBuf upload(const std::vector<T> &v, cudaStream_t s) {
+    DevBuf b(std::max<size_t>(v.size() * sizeof(T), sizeof(T)));
+    if (!v.empty()) VX_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return b;
+}
+
+// ---------------------------------------------------------------- Run
+Run::Run(Engine &e, std::shared_ptr<Problem> prob) : eng(e) {
+    Input grid;
+    Particles particles;
+    Output output;
+    prob->initialConditions(grid, particles, output);
+    S.reset(new Settings(grid, particles, output, prob));
+    rects.resize(S->q.size());
+    for (auto &sp : rects) sp.resize(S->maxDepth + 1);
+}
+
+Run::~Run() {
+    auto &v = eng.runs;
+    v.erase(std::remove(v.begin(), v.end(), this), v.end());
+}
+
+long long Run::cell_count() const {
+    long long c = 0;
+    for (auto &sp : rects)
+        for (auto &lvl : sp)
+            for (auto &r : lvl) c += (long long)r->n_x * r->n_p;
+    return c;
+}
+
+static const int kPlanes = 28;
+
+void Run::allocate_rect(Rect &r) {
+    r.pitch = ((r.n_p + 4) + 7) / 8 * 8;
+    size_t pe = r.plane_elems();
+    r.slab = DevBuf(pe * kPlanes * sizeof(double));
+    r.cols = DevBuf((size_t)2 * r.n_x * (1 << std::max(0, r.depth)) * sizeof(double) + 64);
+    PatchT<double> &d = r.desc;
+    std::memset(&d, 0, sizeof d);
+    double *base = r.slab.as<double>();
+    int k = 0;
+    auto plane = [&]() { return base + pe * (k++); };
+    d.f0 = plane();
+    d.f1 = plane();
+    d.f2 = plane();
+    d.gam = plane();
+    d.ex = plane();
+    d.fx = plane();
+    d.ep = plane();
+    d.fp = plane();
+    for (int s = 0; s < 6; s++) d.FxH[s] = plane();
+    for (int s = 0; s < 6; s++) d.FpH[s] = plane();
+    d.FxL = plane();
+    d.FpL = plane();
+    d.FxDS = plane();
+    d.FpDS = plane();
+    d.Rp = plane();
+    d.Rm = plane();
+    d.Cx = plane();
+    d.Cp = plane();
+}
+
+// Fill the geometric / physical part of a patch descriptor (Rectangle.cpp:7-113).
+void Run::upload_rect_desc(Rect &r, int run_index) {
+    const Settings &s = *S;
+    PatchT<double> &d = r.desc;
+    int sp = r.species;
+    d.nx = r.n_x;
+    d.np = r.n_p;
+    d.x_pos = r.x_pos;
+    d.p_pos = r.p_pos;
+    d.depth = r.depth;
+    d.rtb = (int)std::pow(s.refinementRatio, r.depth);
+    d.pitch = r.pitch;
+    d.xm = r.left ? 1 : 0;
+    d.xp = r.right ? r.n_x : (r.n_x + 1);
+    d.pp = r.up ? r.n_p : (r.n_p + 1);
+    d.pm = r.down ? 1 : 0;
+    d.run = run_index;
+    d.species = sp;
+    d.dp = s.GetDp(r.depth, sp);
+    d.dx = s.GetDx(r.depth);
+    d.dx_inv = 1 / d.dx;
+    d.dp_inv = 1 / d.dp;
+    d.pmin = s.pmin[sp];
+    d.q = s.GetCharge(sp);
+    d.qq = d.q * d.q;
+    d.mass = s.GetMass(sp);
+    d.cc = kCs * kCs * s.GetMass(sp);
+    double m_inv = 1 / s.GetMass(sp);
+    d.g2 = (m_inv * kCInv) * (m_inv * kCInv);
+    double *cols = r.cols.as<double>();
+    d.chargeR = cols;
+    d.currentR = cols + (size_t)r.n_x * d.rtb;
+    d.relc = nullptr;
+}
+
+// Rectangle::InitializeDistribution, non-MKL quadrature (Rectangle.cpp:616-665), run on
+// host threads with the user's InitialDistribution hook.
+void Run::init_rect_distribution(Rect &r) {
+    const Settings &s = *S;
+    const int nvals = std::pow(s.refinementRatio, r.depth + s.quadratureDepth);
+    const double dx = s.GetDx(r.depth), dp = s.GetDp(r.depth, r.species);
+    const double pmin = s.pmin[r.species];
+    std::vector<double> host((size_t)(r.n_x + 4) * r.pitch, 0.0);
+    unsigned nth = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nth; t++) {
+        th.emplace_back([&, t]() {
+            for (int i = (int)t; i < r.n_x; i += (int)nth) {
+                for (int j = 0; j < r.n_p; j++) {
+                    double temp = 0.0, xp = 0.0, pp = 0.0;
+                    for (int k = 0; k < nvals; k++) {
+                        for (int l = 0; l < nvals; l++) {
+                            xp = ((0.5 + k) / nvals + i + r.x_pos) * dx;
+                            pp = pmin + dp * ((0.5 + l) / nvals + j + r.p_pos);
+                            temp += s.InitialDistribution(xp, pp, r.species);
+                        }
+                    }
+                    host[pidx(i, j, r.pitch)] = temp * (1 / std::pow(nvals, 2.0));
+                }
+            }
+        });
+    }
+    for (auto &x : th) x.join();
+    size_t bytes = host.size() * sizeof(double);
+    VX_CUDA(cudaMemcpyAsync(r.desc.f0, host.data(), bytes, cudaMemcpyHostToDevice, eng.stream));
+    VX_CUDA(cudaMemcpyAsync(r.desc.f1, host.data(), bytes, cudaMemcpyHostToDevice, eng.stream));
+    VX_CUDA(cudaStreamSynchronize(eng.stream));
+}
+
+void Run::alloc_fields() {
+    const Settings &s = *S;
+    n = s.x_size_finest;
+    pre = std::max(std::floor(s.preLength / s.GetDx(0)), 2.0);
+    post = std::max(std::floor(s.postLength / s.GetDx(0)), 2.0);
+    nf = n + pre + post;
+    dx0 = s.GetDx(0);
+    size_t fb = (size_t)nf * 8 * sizeof(double);
+    dBy = DevBuf(fb);
+    dBz = DevBuf(fb);
+    dEy = DevBuf(fb);
+    dEz = DevBuf(fb);
+    dAy = DevBuf(fb);
+    dAz = DevBuf(fb);
+    dasq = DevBuf((size_t)(n + 1) * sizeof(double));
+    dphi = DevBuf((size_t)n * sizeof(double));
+    dcharge = DevBuf((size_t)n * sizeof(double));
+    dJ = DevBuf((size_t)n * sizeof(double));
+    dneut = DevBuf((size_t)n * sizeof(double));
+    defin = DevBuf((size_t)n * sizeof(double));
+    dex0 = DevBuf(sizeof(double));
+    F.n = n;
+    F.pre = pre;
+    F.post = post;
+    F.nf = nf;
+    F.dx0 = dx0;
+    F.By = dBy.as<double>();
+    F.Bz = dBz.as<double>();
+    F.Ey = dEy.as<double>();
+    F.Ez = dEz.as<double>();
+    F.Ay = dAy.as<double>();
+    F.Az = dAz.as<double>();
+    F.asq = dasq.as<double>();
+    F.phi = dphi.as<double>();
+    F.charge = dcharge.as<double>();
+    F.J = dJ.as<double>();
+    F.neut = dneut.as<double>();
+    F.efin = defin.as<double>();
+    F.ex0 = dex0.as<double>();
+    F.asq_cell = nullptr;
+}
+
+void Run::upload_lu() {
+    cudaStream_t st = eng.stream;
+    dlu_ipiv = upload(lu.ipiv, st);
+    dlu_lptr = upload(lu.lptr, st);
+    dlu_lcol = upload(lu.lcol, st);
+    dlu_lval = upload(lu.lval, st);
+    dlu_uptr = upload(lu.uptr, st);
+    dlu_ucol = upload(lu.ucol, st);
+    dlu_uval = upload(lu.uval, st);
+    dlu_udiag = upload(lu.udiag, st);
+    ludev.n = lu.n;
+    ludev.ipiv = dlu_ipiv.as<int>();
+    ludev.lptr = dlu_lptr.as<int>();
+    ludev.lcol = dlu_lcol.as<int>();
+    ludev.lval = dlu_lval.as<double>();
+    ludev.uptr = dlu_uptr.as<int>();
+    ludev.ucol = dlu_ucol.as<int>();
+    ludev.uval = dlu_uval.as<double>();
+    ludev.udiag = dlu_udiag.as<double>();
+}
+
+// SolverManager::SolverManager (SolverManager.cpp:8-26) for a hierarchy that starts and
+// stays at the base level (the only case before regridding support is added).
+void Run::init() {
+    const Settings &s = *S;
+    if (s.maxDepth != 0) throw std::invalid_argument("multi-level runs need the AMR build (not available)");
+    for (size_t sp = 0; sp < rects.size(); sp++) {
+        auto r = std::make_unique<Rect>();
+        r->n_x = s.GetXSize(s.maxDepth);
+        r->n_p = s.GetPSize(s.maxDepth, (int)sp);
+        r->x_pos = 0;
+        r->p_pos = 0;
+        r->depth = s.maxDepth;
+        r->up = r->down = r->left = r->right = true;
+        r->species = (int)sp;
+        allocate_rect(*r);
+        upload_rect_desc(*r, 0);
+        init_rect_distribution(*r);
+        rects[sp][s.maxDepth].push_back(std::move(r));
+    }
+    alloc_fields();
+    int info = lu.build(n);
+    if (info) throw std::runtime_error("Poisson operator is singular");
+    upload_lu();
+    layout_version++;
+    enforce_neutralization();
+}
+
+// EMFieldSolver::EnforceChargeNeutralization (EMSolver.cpp:621-629):
+// neutralizationCharge = -rho(t=0), J = 0.
+void Run::enforce_neutralization() {
+    eng.moments_only({this});
+    launch_negate(F.neut, F.charge, n, eng.stream);
+    VX_CUDA(cudaMemsetAsync(F.J, 0, (size_t)n * sizeof(double), eng.stream));
+    eng.sync();
+}
+
+// Until coarse/fine machinery is present, every species must be one patch that covers
+// the whole domain, so that every ghost cell is a physical (zero) boundary cell
+// (BoundaryCondition.cpp:5-7).
+void Run::check_layout_supported() const {
+    for (auto &sp : rects) {
+        int count = 0;
+        for (auto &lvl : sp)
+            for (auto &r : lvl) {
+                count++;
+                if (!(r->up && r->down && r->left && r->right))
+                    throw std::invalid_argument("multi-patch layouts need the AMR build (not available)");
+            }
+        if (count != 1) throw std::invalid_argument("multi-patch layouts need the AMR build (not available)");
+    }
+}
+
+int64_t Run::state_size() const {
+    int64_t len = 0;
+    for (auto &sp : rects)
+        for (auto &lvl : sp)
+            for (auto &r : lvl) len += (int64_t)r->plane_elems();
+    return len + 6 * (int64_t)nf + (n + 1) + 1;
+}
+
+// Host-buffer step: H2D of the packed state, one RK step, D2H of the new state.
+void Run::step_host(const double *in, double *out, double dt) {
+    cudaStream_t st = eng.stream;
+    const double *p = in;
+    for (auto &sp : rects)
+        for (auto &lvl : sp)
+            for (auto &r : lvl) {
+                size_t b = r->plane_elems() * sizeof(double);
+                VX_CUDA(cudaMemcpyAsync(r->desc.f0, p, b, cudaMemcpyHostToDevice, st));
+                VX_CUDA(cudaMemcpyAsync(r->desc.f1, r->desc.f0, b, cudaMemcpyDeviceToDevice, st));
+                p += r->plane_elems();
+            }
+    for (double *X : {F.By, F.Bz, F.Ey, F.Ez, F.Ay, F.Az}) {
+        VX_CUDA(cudaMemcpyAsync(X, p, (size_t)nf * sizeof(double), cudaMemcpyHostToDevice, st));
+        VX_CUDA(cudaMemcpyAsync(X + nf, X, (size_t)nf * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        p += nf;
+    }
+    VX_CUDA(cudaMemcpyAsync(F.asq, p, (size_t)(n + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
+    p += n + 1;
+    VX_CUDA(cudaMemcpyAsync(F.ex0, p, sizeof(double), cudaMemcpyHostToDevice, st));
+    advance(dt);
+    state_to_host(out);
+}
+
+void Run::state_to_host(double *out) {
+    cudaStream_t st = eng.stream;
+    double *q = out;
+    for (auto &sp : rects)
+        for (auto &lvl : sp)
+            for (auto &r : lvl) {
+                VX_CUDA(cudaMemcpyAsync(q, r->desc.f0, r->plane_elems() * sizeof(double), cudaMemcpyDeviceToHost, st));
+                q += r->plane_elems();
+            }
+    for (double *X : {F.By, F.Bz, F.Ey, F.Ez, F.Ay, F.Az}) {
+        VX_CUDA(cudaMemcpyAsync(q, X, (size_t)nf * sizeof(double), cudaMemcpyDeviceToHost, st));
+        q += nf;
+    }
+    VX_CUDA(cudaMemcpyAsync(q, F.asq, (size_t)(n + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+    q += n + 1;
+    VX_CUDA(cudaMemcpyAsync(q, F.ex0, sizeof(double), cudaMemcpyDeviceToHost, st));
+    eng.sync();
+}
+
+double Run::calculate_dt() { return eng.calculate_dt({this})[0]; }
+
+void Run::advance(double dt) { eng.advance({this}, {dt}); }
+
+// ---------------------------------------------------------------- LaunchSet / Engine
+LaunchSet::~LaunchSet() {
+    if (graph) cudaGraphExecDestroy(graph);
+}
+
+Engine::Engine(int dev) : device(dev) {
+    VX_CUDA(cudaSetDevice(dev));
+    VX_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+}
+
+Engine::~Engine() {
+    sets_.clear();
+    if (ev0_) cudaEventDestroy(ev0_);
+    if (ev1_) cudaEventDestroy(ev1_);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+void Engine::timer_begin() {
+    if (!ev0_) {
+        VX_CUDA(cudaEventCreate(&ev0_));
+        VX_CUDA(cudaEventCreate(&ev1_));
+    }
+    VX_CUDA(cudaEventRecord(ev0_, stream));
+}
+
+double Engine::timer_end() {
+    if (!ev0_) throw std::logic_error("timer_end without timer_begin");
+    VX_CUDA(cudaEventRecord(ev1_, stream));
+    VX_CUDA(cudaEventSynchronize(ev1_));
+    float ms = 0;
+    VX_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+    return ms;
+}
+
+void Engine::flush_l2() {
+    if (!flush_.p) flush_ = DevBuf((size_t)512 << 20);
+    VX_CUDA(cudaMemsetAsync(flush_.p, (int)(kernel_launches & 0xff), flush_.bytes, stream));
+}
+
+double Engine::measure_fp64_peak() {
+    if (!flush_.p) flush_ = DevBuf((size_t)512 << 20);
+    int sms = 0;
+    VX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    const int iters = 4096;
+    int blocks = sms * 8, threads = 256;
+    launch_fp64_peak(flush_.as<double>(), blocks, threads, iters, stream);
+    timer_begin();
+    launch_fp64_peak(flush_.as<double>(), blocks, threads, iters, stream);
+    double ms = timer_end();
+    kernel_launches += 2;
+    double flops = 2.0 * 8.0 * (double)iters * blocks * threads;  // 8 independent FMA chains
+    return flops / (ms * 1e-3) / 1e9;
+}
+
+std::vector<double> Engine::profile_kernels(Run &run, int reps) {
+    LaunchSet &L = get_set({&run});
+    FctLaunch fl{};
+    fl.patches = L.dpatch.p;
+    fl.tiles = L.dtiles.as<TileRef>();
+    fl.ntiles = L.ntiles;
+    fl.fields = L.dfields.as<RunFields>();
+    fl.params = L.dparams.as<double>();
+    fl.step = 0;
+    fl.stream = stream;
+    std::vector<double> out;
+    auto time_it = [&](auto &&fn) {
+        fn();
+        timer_begin();
+        for (int r = 0; r < reps; r++) fn();
+        out.push_back(timer_end() / reps);
+        kernel_launches += reps + 1;
+    };
+    // stage-0 parameters with dt = 0 keep every kernel well defined
+    for (int sub : {kSubGamma, kSubFaces, kSubFlux, kSubDsF2, kSubLimR, kSubLimC, kSubUpdate})
+        time_it([&] { launch_fct64_substep(fl, sub); });
+    MomLaunch ml{};
+    ml.patches = L.dpatch.p;
+    ml.colpatch = L.dcolpatch.as<int>();
+    ml.colidx = L.dcolidx.as<int>();
+    ml.ncols = L.ncols;
+    ml.maxnp = L.maxnp;
+    ml.fields = L.dfields.as<RunFields>();
+    ml.Lbuf = L.dLbuf.as<double>();
+    ml.stream = stream;
+    time_it([&] { launch_moments64(ml); });
+    AsmLaunch al{};
+    al.patches = L.dpatch.p;
+    al.lvl_ptr = L.dlvl_ptr.as<int>();
+    al.lvl_off = L.dlvl_off.as<int>();
+    al.lvl_patch = L.dlvl_patch.as<int>();
+    al.run_n = L.drun_n.as<int>();
+    al.run_ns = L.drun_ns.as<int>();
+    al.run_nl = L.drun_nl.as<int>();
+    al.nruns = 1;
+    al.maxn = L.maxn;
+    al.fields = L.dfields.as<RunFields>();
+    al.stream = stream;
+    time_it([&] { launch_assemble(al); });
+    return out;
+}
+
+void Engine::sync() { VX_CUDA(cudaStreamSynchronize(stream)); }
+
+LaunchSet &Engine::get_set(const std::vector<Run *> &set) {
+    auto it = sets_.find(set);
+    uint64_t ver = 0;
+    for (Run *r : set) ver = ver * 1000003ull + r->layout_version;
+    if (it != sets_.end() && it->second->key_version == ver) return *it->second;
+    auto L = std::make_unique<LaunchSet>();
+    L->runs = set;
+    L->key_version = ver;
+    build_set(*L);
+    LaunchSet &ref = *L;
+    sets_[set] = std::move(L);
+    return ref;
+}
+
+void Engine::build_set(LaunchSet &L) {
+    std::vector<TileRef> tiles;
+    std::vector<int> colpatch, colidx, lvl_ptr, lvl_off, lvl_patch, run_n, run_ns, run_nl;
+    std::vector<RunFields> fields;
+    std::vector<LUDev> lus;
+    std::vector<double> dxinv, spec;
+    L.hpatch.clear();
+    L.maxnp = 0;
+    L.maxn = 0;
+    L.maxnf = 0;
+    for (size_t ri = 0; ri < L.runs.size(); ri++) {
+        Run &R = *L.runs[ri];
+        const Settings &s = *R.S;
+        int ns = (int)R.rects.size(), nl = s.maxDepth + 1;
+        lvl_off.push_back((int)lvl_ptr.size());
+        std::vector<int> ptr;
+        ptr.push_back(0);
+        for (int sp = 0; sp < ns; sp++) {
+            for (int l = 0; l < nl; l++) {
+                for (auto &rp : R.rects[sp][l]) {
+                    Rect &r = *rp;
+                    R.upload_rect_desc(r, (int)ri);
+                    int pi = (int)L.hpatch.size();
+                    L.hpatch.push_back(r.desc);
+                    lvl_patch.push_back(pi);
+                    for (int i0 = -2; i0 <= r.n_x + 1; i0 += 8)
+                        for (int j0 = -2; j0 <= r.n_p + 1; j0 += 32) tiles.push_back({pi, i0, j0});
+                    int rtb = r.desc.rtb;
+                    for (int c = 0; c < r.n_x * rtb; c++) {
+                        colpatch.push_back(pi);
+                        colidx.push_back(c);
+                    }
+                    L.maxnp = std::max(L.maxnp, r.n_p);
+                }
+                ptr.push_back((int)lvl_patch.size());
+            }
+        }
+        // lvl_ptr entries are absolute indices into lvl_patch
+        for (int v : ptr) lvl_ptr.push_back(v);
+        run_n.push_back(R.n);
+        run_ns.push_back(ns);
+        run_nl.push_back(nl);
+        fields.push_back(R.F);
+        lus.push_back(R.ludev);
+        dxinv.push_back(1 / s.GetDx(0));
+        L.w.push_back(std::pow(s.GetDx(0), 2.0));
+        L.fcoef.push_back(1.0 / (12 * s.GetDx(0)));
+        L.maxn = std::max(L.maxn, R.n);
+        L.maxnf = std::max(L.maxnf, R.nf);
+        // CFL species table (EMSolver.cpp:631-646)
+        std::vector<double> sp(25, 0.0);
+        double dpsMax(0.0);
+        for (int i = 0; i < ns && i < 8; i++) {
+            double dps = 1 / s.GetDp(0, i);
+            dpsMax = std::max(dpsMax, std::fabs(s.q[i]) * dps);
+            sp[3 * i] = std::fabs(s.q[i]);
+            sp[3 * i + 1] = s.m[i];
+            sp[3 * i + 2] = dps;
+        }
+        sp[24] = dpsMax;
+        spec.insert(spec.end(), sp.begin(), sp.end());
+    }
+    L.ntiles = (int)tiles.size();
+    L.ncols = (int)colpatch.size();
+    // lvl_ptr is absolute; lvl_off points at each run's block.
+    L.dpatch = upload(L.hpatch, stream);
+    L.dtiles = upload(tiles, stream);
+    L.dfields = upload(fields, stream);
+    L.dcolpatch = upload(colpatch, stream);
+    L.dcolidx = upload(colidx, stream);
+    L.dLbuf = DevBuf((size_t)std::max(1, L.ncols) * (L.maxnp + 2) * sizeof(double));
+    L.dlvl_ptr = upload(lvl_ptr, stream);
+    L.dlvl_off = upload(lvl_off, stream);
+    L.dlvl_patch = upload(lvl_patch, stream);
+    L.drun_n = upload(run_n, stream);
+    L.drun_ns = upload(run_ns, stream);
+    L.drun_nl = upload(run_nl, stream);
+    L.dlu = upload(lus, stream);
+    L.dw = upload(L.w, stream);
+    L.dfcoef = upload(L.fcoef, stream);
+    L.ddxinv = upload(dxinv, stream);
+    L.dcfl_spec = upload(spec, stream);
+    L.dns = upload(run_ns, stream);
+    L.dcfl_out = DevBuf(L.runs.size() * sizeof(double));
+    L.hparams.assign(L.runs.size() * 6 * kParamStride, 0.0);
+    L.dparams = DevBuf(L.hparams.size() * sizeof(double));
+    if (L.graph) {
+        cudaGraphExecDestroy(L.graph);
+        L.graph = nullptr;
+    }
+    sync();
+}
+
+// The kernel sequence of one full RK step (SolverManager.cpp:28-39 -> Mesh.cpp:64-89,
+// EMSolver.cpp:104-202) for every run of the set.
+void Engine::record_step(LaunchSet &L) {
+    int launches = 0;
+    FctLaunch fl{};
+    fl.patches = L.dpatch.p;
+    fl.tiles = L.dtiles.as<TileRef>();
+    fl.ntiles = L.ntiles;
+    fl.fields = L.dfields.as<RunFields>();
+    fl.params = L.dparams.as<double>();
+    fl.use_f0 = 0;
+    fl.stream = stream;
+    MomLaunch ml{};
+    ml.patches = L.dpatch.p;
+    ml.colpatch = L.dcolpatch.as<int>();
+    ml.colidx = L.dcolidx.as<int>();
+    ml.ncols = L.ncols;
+    ml.maxnp = L.maxnp;
+    ml.fields = L.dfields.as<RunFields>();
+    ml.Lbuf = L.dLbuf.as<double>();
+    ml.stream = stream;
+    AsmLaunch al{};
+    al.patches = L.dpatch.p;
+    al.lvl_ptr = L.dlvl_ptr.as<int>();
+    al.lvl_off = L.dlvl_off.as<int>();
+    al.lvl_patch = L.dlvl_patch.as<int>();
+    al.run_n = L.drun_n.as<int>();
+    al.run_ns = L.drun_ns.as<int>();
+    al.run_nl = L.drun_nl.as<int>();
+    al.nruns = (int)L.runs.size();
+    al.maxn = L.maxn;
+    al.fields = L.dfields.as<RunFields>();
+    al.stream = stream;
+    PoissonLaunch pl{};
+    pl.lu = L.dlu.as<LUDev>();
+    pl.fields = L.dfields.as<RunFields>();
+    pl.w = L.dw.as<double>();
+    pl.fcoef = L.dfcoef.as<double>();
+    pl.nruns = (int)L.runs.size();
+    pl.maxn = L.maxn;
+    pl.stream = stream;
+    MaxwellLaunch mx{};
+    mx.fields = L.dfields.as<RunFields>();
+    mx.nruns = (int)L.runs.size();
+    mx.maxnf = L.maxnf;
+    mx.params = L.dparams.as<double>();
+    mx.dxinv = L.ddxinv.as<double>();
+    mx.stream = stream;
+    for (int s = 0; s < 6; s++) {
+        launch_moments64(ml);
+        launch_assemble(al);
+        launch_poisson(pl);
+        launches += 4;
+        fl.step = s;
+        launch_fct64_substep(fl, kSubGamma);
+        launch_fct64_substep(fl, kSubFaces);
+        launch_fct64_substep(fl, kSubFlux);
+        launch_fct64_substep(fl, kSubDsF2);
+        launch_fct64_substep(fl, kSubLimR);
+        launch_fct64_substep(fl, kSubLimC);
+        launch_fct64_substep(fl, kSubUpdate);
+        launches += 7;
+        if (s == 5) {
+            launch_fct64_substep(fl, kSubCopy10);
+            launches += 1;
+        }
+        mx.step = s;
+        launch_maxwell(mx);
+        launches += 3;
+    }
+    launches_per_step_ = launches;
+}
+
+void Engine::advance(const std::vector<Run *> &set, const std::vector<double> &dt) {
+    LaunchSet &L = get_set(set);
+    // Host-side stage parameters (dt-scaled tableau, laser boundary values).
+    for (size_t ri = 0; ri < set.size(); ri++) {
+        Run &R = *set[ri];
+        Settings &s = *R.S;
+        double timestep = dt[ri];
+        for (int st = 0; st < 6; st++) {
+            double *p = &L.hparams[param_base((int)ri, st)];
+            for (int k = 0; k < kParamStride; k++) p[k] = 0.0;
+            if (st < 5) {
+                double sum = 0.0;
+                for (int k = 0; k <= st; k++) {
+                    p[k] = kRK[st][k] * timestep;
+                }
+                // aSum exactly as written in Rectangle.cpp (left-to-right sum of products)
+                sum = p[0];
+                for (int k = 1; k <= st; k++) sum = sum + p[k];
+                p[6] = sum;
+            } else {
+                for (int k = 0; k < 6; k++) p[k] = kRK[5][k] * timestep;
+                double sum = p[0];
+                for (int k = 1; k < 6; k++) sum = sum + p[k];
+                p[6] = sum;
+            }
+            // Maxwell weights (EMSolver.cpp:204-338)
+            if (st < 5) {
+                for (int k = 0; k <= st; k++) p[8 + k] = kRK[st][k] * timestep;
+            } else {
+                double a[6];
+                for (int k = 0; k < 5; k++) a[k] = kRK[4][k] * timestep;
+                a[5] = 0;
+                for (int k = 0; k < 6; k++) p[8 + k] = kRK[5][k] * timestep - a[k];
+            }
+            s.UpdateTime(st, timestep);
+            p[16] = s.GetBY(0, s.time);
+            p[17] = s.GetBZ(0, s.time);
+        }
+    }
+    VX_CUDA(cudaMemcpyAsync(L.dparams.p, L.hparams.data(), L.hparams.size() * sizeof(double), cudaMemcpyHostToDevice,
+                            stream));
+    if (use_graphs) {
+        if (!L.graph) {
+            cudaGraph_t g;
+            VX_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            record_step(L);
+            VX_CUDA(cudaStreamEndCapture(stream, &g));
+            VX_CUDA(cudaGraphInstantiate(&L.graph, g, 0));
+            cudaGraphDestroy(g);
+        }
+        VX_CUDA(cudaGraphLaunch(L.graph, stream));
+    } else {
+        record_step(L);
+    }
+    kernel_launches += launches_per_step_;
+    VX_CUDA(cudaGetLastError());
+}
+
+std::vector<double> Engine::calculate_dt(const std::vector<Run *> &set) {
+    LaunchSet &L = get_set(set);
+    CflLaunch cl{};
+    cl.fields = L.dfields.as<RunFields>();
+    cl.nruns = (int)set.size();
+    cl.maxn = L.maxn;
+    cl.spec = L.dcfl_spec.as<double>();
+    cl.run_ns = L.dns.as<int>();
+    cl.out = L.dcfl_out.as<double>();
+    cl.stream = stream;
+    launch_cfl(cl);
+    kernel_launches += 1;
+    std::vector<double> pc(set.size());
+    VX_CUDA(cudaMemcpyAsync(pc.data(), L.dcfl_out.p, pc.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    sync();
+    std::vector<double> dt(set.size());
+    for (size_t i = 0; i < set.size(); i++) {
+        const Settings &s = *set[i]->S;
+        double bound = 1.0 / std::max((kCs / s.GetDx(0) + pc[i]), 1e-40);
+        dt[i] = s.cfl * bound;
+    }
+    return dt;
+}
+
+// Moments and rho/J assembly only (used for EnforceChargeNeutralization).
+void Engine::moments_only(const std::vector<Run *> &set) {
+    LaunchSet &L = get_set(set);
+    MomLaunch ml{};
+    ml.patches = L.dpatch.p;
+    ml.colpatch = L.dcolpatch.as<int>();
+    ml.colidx = L.dcolidx.as<int>();
+    ml.ncols = L.ncols;
+    ml.maxnp = L.maxnp;
+    ml.fields = L.dfields.as<RunFields>();
+    ml.Lbuf = L.dLbuf.as<double>();
+    ml.stream = stream;
+    launch_moments64(ml);
+    AsmLaunch al{};
+    al.patches = L.dpatch.p;
+    al.lvl_ptr = L.dlvl_ptr.as<int>();
+    al.lvl_off = L.dlvl_off.as<int>();
+    al.lvl_patch = L.dlvl_patch.as<int>();
+    al.run_n = L.drun_n.as<int>();
+    al.run_ns = L.drun_ns.as<int>();
+    al.run_nl = L.drun_nl.as<int>();
+    al.nruns = (int)L.runs.size();
+    al.maxn = L.maxn;
+    al.fields = L.dfields.as<RunFields>();
+    al.stream = stream;
+    launch_assemble(al);
+    kernel_launches += 3;
+}
+
+}  // namespace vx

@@ -1,0 +1,149 @@
+// Device runtime: runs (one per SolverManager), their patches in HBM, and the launch
+// sets that advance a group of runs together with one launch per sub-step.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "poisson_lu.hpp"
+#include "settings.hpp"
+#include "vx_kernels.hpp"
+
+namespace vx {
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+void cuda_check(cudaError_t e, const char *what);
+#define VX_CUDA(x) ::vx::cuda_check((x), #x)
+
+// Owned device allocation.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t b);
+    ~DevBuf();
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), bytes(o.bytes) {
+        o.p = nullptr;
+        o.bytes = 0;
+    }
+    DevBuf &operator=(DevBuf &&o) noexcept;
+    template <class T>
+    T *as() const {
+        return (T *)p;
+    }
+};
+
+// Geometry of one Rectangle (Rectangle.hpp:20-23) plus its device storage.
+struct Rect {
+    int n_x = 0, n_p = 0, x_pos = 0, p_pos = 0, depth = 0;
+    bool up = false, down = false, left = false, right = false;
+    int species = 0;
+    int pitch = 0;
+    DevBuf slab;   // all per-patch planes
+    DevBuf cols;   // chargeR, currentR
+    DevBuf masks;  // nested, ifx, ifp (AMR only)
+    PatchT<double> desc{};
+    size_t plane_elems() const { return (size_t)(n_x + 4) * pitch; }
+};
+
+class Engine;
+
+// One independent solve: the state owned by the reference's SolverManager
+// (SolverManager.hpp:5-19): Settings, one mesh per species, the field solver.
+class Run {
+public:
+    Run(Engine &eng, std::shared_ptr<Problem> prob);
+    ~Run();
+    Engine &eng;
+    std::unique_ptr<Settings> S;
+    // rects[species][depth] -> patches of that level, in the reference's order.
+    std::vector<std::vector<std::vector<std::unique_ptr<Rect>>>> rects;
+    int n = 0, pre = 0, post = 0, nf = 0;
+    double dx0 = 0;
+    // fields
+    DevBuf dBy, dBz, dEy, dEz, dAy, dAz, dasq, dphi, dcharge, dJ, dneut, defin, dex0;
+    RunFields F{};
+    PoissonLU lu;
+    DevBuf dlu_ipiv, dlu_lptr, dlu_lcol, dlu_lval, dlu_uptr, dlu_ucol, dlu_uval, dlu_udiag;
+    LUDev ludev{};
+    uint64_t layout_version = 0;
+    int id = 0;
+
+    // SolverManager-level operations (SolverManager.cpp:8-164).
+    void init();                        // constructor path: hierarchy, f(t=0), fields, neutralisation
+    double calculate_dt();              // cfl * EstimateCFLBound
+    void advance(double dt);            // six RK stages
+    void advance_fields(double dt);     // Maxwell-only stages
+
+    // State exchange in the reference dump layout (see vx.h).
+    void load_state(const std::string &path);
+    void save_state(const std::string &path);
+
+    long long cell_count() const;
+    void allocate_rect(Rect &r);
+    void upload_rect_desc(Rect &r, int run_index_in_set);
+    void init_rect_distribution(Rect &r);  // Rectangle::InitializeDistribution on the host
+    void alloc_fields();
+    void upload_lu();
+    void enforce_neutralization();
+    void check_layout_supported() const;
+    int64_t state_size() const;
+    void step_host(const double *in, double *out, double dt);
+    void state_to_host(double *out);
+};
+
+// A set of runs advanced together: flattened descriptor and work tables.
+struct LaunchSet {
+    std::vector<Run *> runs;
+    uint64_t key_version = 0;
+    std::vector<PatchT<double>> hpatch;
+    DevBuf dpatch, dtiles, dfields, dcolpatch, dcolidx, dLbuf, dlvl_ptr, dlvl_off, dlvl_patch, drun_n, drun_ns,
+        drun_nl, dlu, dw, dfcoef, dparams, dcfl_spec, dcfl_out, dns, ddxinv;
+    int ntiles = 0, ncols = 0, maxnp = 0, maxn = 0, maxnf = 0;
+    std::vector<double> hparams;  // per run: 6 stages x (8 fct + 8 maxwell + 2 laser)
+    std::vector<double> w, fcoef;
+    cudaGraphExec_t graph = nullptr;
+    ~LaunchSet();
+};
+
+class Engine {
+public:
+    explicit Engine(int device);
+    ~Engine();
+    int device;
+    cudaStream_t stream = nullptr;
+    std::vector<Run *> runs;
+    bool use_graphs = true;
+    uint64_t kernel_launches = 0;  // launches issued by this engine (graph replays count their nodes)
+
+    void advance(const std::vector<Run *> &set, const std::vector<double> &dt);
+    std::vector<double> calculate_dt(const std::vector<Run *> &set);
+    void moments_only(const std::vector<Run *> &set);
+    // Mean device time per launch of each Vlasov kernel (see vx_run_profile_kernels).
+    std::vector<double> profile_kernels(Run &run, int reps);
+    void timer_begin();
+    double timer_end();
+    void flush_l2();
+    double measure_fp64_peak();
+    void sync();
+
+private:
+    std::map<std::vector<Run *>, std::unique_ptr<LaunchSet>> sets_;
+    LaunchSet &get_set(const std::vector<Run *> &set);
+    void build_set(LaunchSet &L);
+    void record_step(LaunchSet &L);
+    int launches_per_step_ = 0;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    DevBuf flush_;
+};
+
+}  // namespace vx

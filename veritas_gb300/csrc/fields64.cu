@@ -1,0 +1,430 @@
+// FP64 field-side kernels: momentum moments (Rectangle::CalculateRhoAndJ, MKL path
+// Rectangle.cpp:157-237), finest-grid assembly (Level.cpp:19-62, EMSolver.cpp:104-122),
+// Poisson solve with the precomputed LU factors (EMSolver.cpp:156-192), the transverse
+// Maxwell RK stage with face interpolation of A (EMSolver.cpp:194-619) and the CFL bound
+// (EMSolver.cpp:631-664).
+//
+// Compiled with --fmad=false so each double expression keeps the reference's operations
+// and evaluation order.
+#include <cuda_runtime.h>
+#include "vx_kernels.hpp"
+
+namespace vx {
+
+using P64 = PatchT<double>;
+
+// Interpolated value of f on finest sub-cell k of coarse cell (i, j), including the
+// conservative correction (Rectangle.cpp:139-155 and :183-204).  Fixed 12-entry
+// interpolation matrix of the reference (Rectangle.cpp:76-89).
+__device__ __forceinline__ double rel_value(const P64 &P, const double *f, int i, int j, int k) {
+    const int pit = P.pitch;
+    const double f3 = f[pidx(i, j, pit)];
+    // With one sub-cell every weight is exactly zero and the correction vanishes.
+    if (P.rtb == 1) return f3;
+    const double m0 = 0.104166666666667, m1 = -0.708333333333334, m2 = 0.708333333333334, m3 = -0.104166666666667;
+    const double m4 = 0.117647058823529, m5 = 0.029411764705882, m6 = 0.029411764705882, m7 = 0.117647058823529;
+    const double m8 = -0.083333333333333, m9 = 0.166666666666667, m10 = -0.166666666666667, m11 = 0.083333333333334;
+    double g1 = f[pidx(i - 2, j, pit)] - f3;
+    double g2 = f[pidx(i - 1, j, pit)] - f3;
+    double g4 = f[pidx(i + 1, j, pit)] - f3;
+    double g5 = f[pidx(i + 2, j, pit)] - f3;
+    double a1 = m0 * g1 + m1 * g2 + m2 * g4 + m3 * g5;
+    double a2 = m4 * g1 + m5 * g2 + m6 * g4 + m7 * g5;
+    double a3 = m8 * g1 + m9 * g2 + m10 * g4 + m11 * g5;
+    double te = 0.0, mine = 0.0;
+    for (int q = 0; q < P.rtb; q++) {
+        double v = P.relc[3 * q] * a1 + P.relc[3 * q + 1] * a2 + P.relc[3 * q + 2] * a3 + f3;
+        te += v;
+        if (q == k) mine = v;
+    }
+    double cor = f3 - (1.0 / (double)P.rtb) * te;
+    return mine + cor;
+}
+
+__device__ __forceinline__ double cell_asq(const RunFields &F, int x) {
+    int i = x + F.pre;
+    i = i > -1 ? i : 0;
+    i = i < F.nf ? i : F.nf - 1;
+    double ay = F.Ay[F.nf + i], az = F.Az[F.nf + i];
+    return (ay * ay) + (az * az);
+}
+
+// Log-ratio table L(j) = c2 * ln((g_{j+1} + c1 p_{j+1}) / (g_j + c1 p_j)) for j in
+// [-1, n_p] of every moment column; gm, gm1, gp1 of the reference are L(j), L(j-1),
+// L(j+1) (identical expressions evaluated at neighbouring j).
+__global__ void k64_mom_L(MomLaunch M) {
+    const int col = blockIdx.y * blockDim.y + threadIdx.y;
+    const int jj = blockIdx.x * blockDim.x + threadIdx.x;  // j + 1
+    if (col >= M.ncols) return;
+    const P64 &P = ((const P64 *)M.patches)[M.colpatch[col]];
+    if (jj > P.np + 1) return;
+    const int j = jj - 1;
+    const int c = M.colidx[col];
+    const int i = c / P.rtb, k = c - i * P.rtb;
+    const RunFields &F = M.fields[P.run];
+    const double a = P.qq * cell_asq(F, (i + P.x_pos) * P.rtb + k);
+    const double minv = 1 / P.mass;
+    const double c1 = minv * kCInv;
+    const double c2 = 1 / c1;
+    double p0 = P.pmin + P.dp * (double)(j + P.p_pos);
+    double p1 = P.pmin + P.dp * (double)(j + 1 + P.p_pos);
+    double g0 = sqrt(1.0 + ((p0 * p0) + a) * P.g2);
+    double g1 = sqrt(1.0 + ((p1 * p1) + a) * P.g2);
+    M.Lbuf[(size_t)col * (M.maxnp + 2) + jj] = c2 * log((g1 + c1 * p1) / (g0 + c1 * p0));
+}
+
+// Ordered accumulation over p of charge and current per moment column, in the exact
+// j order of the reference loop, skipping nested cells.
+__global__ void k64_mom_acc(MomLaunch M) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= M.ncols) return;
+    const P64 &P = ((const P64 *)M.patches)[M.colpatch[col]];
+    const int c = M.colidx[col];
+    const int i = c / P.rtb, k = c - i * P.rtb;
+    const double *L = M.Lbuf + (size_t)col * (M.maxnp + 2) + 1;  // L[j], j >= -1
+    const double *f = P.f1;
+    const double c3 = 1 / 48.0;
+    double vm1 = rel_value(P, f, i, -1, k);
+    double v0 = rel_value(P, f, i, 0, k);
+    double vp1 = rel_value(P, f, i, 1, k);
+    double ch = 0.0, cu = 0.0;
+    for (int j = 0; j < P.np; j++) {
+        if (!(P.nested && P.nested[pidx(i, j, P.pitch)])) {
+            ch += v0;
+            double gm = L[j], gm1 = L[j - 1], gp1 = L[j + 1];
+            cu += v0 * gm + c3 * (gp1 - gm1) * (vp1 - vm1);
+        }
+        vm1 = v0;
+        v0 = vp1;
+        vp1 = rel_value(P, f, i, j + 2, k);
+    }
+    const double q = P.q;
+    P.chargeR[c] = ch * (P.dp * q);
+    P.currentR[c] = cu * (-q * q / P.mass);
+}
+
+void launch_moments64(const MomLaunch &M) {
+    if (M.ncols == 0) return;
+    dim3 b1(64, 4);
+    dim3 g1((M.maxnp + 2 + 63) / 64, (M.ncols + 3) / 4);
+    k64_mom_L<<<g1, b1, 0, M.stream>>>(M);
+    k64_mom_acc<<<(M.ncols + 127) / 128, 128, 0, M.stream>>>(M);
+}
+
+// ---------------------------------------------------------------- assembly
+// Level::CollectRhoAndJ + EMFieldSolver::AssembleRhoAndJ (Level.cpp:19-62,
+// EMSolver.cpp:104-122): per level, chargeL[x] = 0 + (patch values in patch order);
+// charges_s[x] = 0 + level sums finest->coarsest; J sums species then levels;
+// charge[x] = 0 + species sums.
+__global__ void k_assemble(AsmLaunch A) {
+    const int run = blockIdx.y;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (run >= A.nruns) return;
+    const int n = A.run_n[run];
+    if (x >= n) return;
+    const int ns = A.run_ns[run], nl = A.run_nl[run];
+    const int *lp = A.lvl_ptr + A.lvl_off[run];
+    const P64 *patches = (const P64 *)A.patches;
+    double J = 0.0, charge = 0.0;
+    for (int s = 0; s < ns; s++) {
+        double cs = 0.0;
+        for (int l = 0; l < nl; l++) {
+            double lc = 0.0, lj = 0.0;
+            for (int e = lp[s * nl + l]; e < lp[s * nl + l + 1]; e++) {
+                const P64 &P = patches[A.lvl_patch[e]];
+                int c = x - P.x_pos * P.rtb;
+                if (c >= 0 && c < P.nx * P.rtb) {
+                    lc += P.chargeR[c];
+                    lj += P.currentR[c];
+                }
+            }
+            cs += lc;
+            J += lj;
+        }
+        charge += cs;
+    }
+    RunFields &F = A.fields[run];
+    F.charge[x] = charge;
+    F.J[x] = J;
+}
+
+void launch_assemble(const AsmLaunch &A) {
+    dim3 g((A.maxn + 255) / 256, A.nruns);
+    k_assemble<<<g, 256, 0, A.stream>>>(A);
+}
+
+// ---------------------------------------------------------------- Poisson
+__device__ __forceinline__ double efield_at(const double *phi, int n, double fcoef, double ex0, int i) {
+    int ip1 = i + 1, im1 = i - 1, ip2 = i + 2, im2 = i - 2;
+    ip1 = (ip1 > -1) ? ip1 : (ip1 + n);
+    im1 = (im1 > -1) ? im1 : (im1 + n);
+    ip2 = (ip2 > -1) ? ip2 : (ip2 + n);
+    im2 = (im2 > -1) ? im2 : (im2 + n);
+    ip1 = (ip1 < n) ? ip1 : (ip1 - n);
+    im1 = (im1 < n) ? im1 : (im1 - n);
+    ip2 = (ip2 < n) ? ip2 : (ip2 - n);
+    im2 = (im2 < n) ? im2 : (im2 - n);
+    return -fcoef * (8 * (phi[ip1] - phi[im1]) - phi[ip2] + phi[im2]) + ex0;
+}
+
+// One block per run.  The triangular solves are linear recurrences; to keep the
+// reference's rounding they run in a single thread, in the order of the column-oriented
+// dgetrs.  Entries within four rows of the diagonal come from a register window.
+__global__ void k_poisson(PoissonLaunch L) {
+    const int run = blockIdx.x;
+    RunFields &F = L.fields[run];
+    const LUDev &lu = L.lu[run];
+    const int n = F.n;
+    double *phi = F.phi;
+    const double te = kEps0Inv;
+    const double w = L.w[run];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double v = te * (F.charge[i] + F.neut[i]);
+        phi[i] = v * w;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < n; k++) {
+            int p = lu.ipiv[k];
+            if (p != k) {
+                double t = phi[k];
+                phi[k] = phi[p];
+                phi[p] = t;
+            }
+        }
+        double w1 = 0, w2 = 0, w3 = 0, w4 = 0;
+        for (int i = 0; i < n; i++) {
+            double s = phi[i];
+            for (int e = lu.lptr[i]; e < lu.lptr[i + 1]; e++) {
+                int c = lu.lcol[e];
+                int d = i - c;
+                double xc = d == 1 ? w1 : d == 2 ? w2 : d == 3 ? w3 : d == 4 ? w4 : phi[c];
+                s = s - xc * lu.lval[e];
+            }
+            phi[i] = s;
+            w4 = w3;
+            w3 = w2;
+            w2 = w1;
+            w1 = s;
+        }
+        w1 = w2 = w3 = w4 = 0;
+        for (int i = n - 1; i >= 0; i--) {
+            double s = phi[i];
+            for (int e = lu.uptr[i]; e < lu.uptr[i + 1]; e++) {
+                int c = lu.ucol[e];
+                int d = c - i;
+                double xc = d == 1 ? w1 : d == 2 ? w2 : d == 3 ? w3 : d == 4 ? w4 : phi[c];
+                s = s - xc * lu.uval[e];
+            }
+            s = s / lu.udiag[i];
+            phi[i] = s;
+            w4 = w3;
+            w3 = w2;
+            w2 = w1;
+            w1 = s;
+        }
+        double ex0 = *F.ex0;
+        double e_m1 = efield_at(phi, n, L.fcoef[run], ex0, -1);
+        double e_0 = efield_at(phi, n, L.fcoef[run], ex0, 0);
+        *F.ex0 = ex0 + -(e_m1 + e_0) * 0.5;
+    }
+    __syncthreads();
+    const double ex0 = *F.ex0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) F.efin[i] = efield_at(phi, n, L.fcoef[run], ex0, i);
+}
+
+void launch_poisson(const PoissonLaunch &L) {
+    k_poisson<<<L.nruns, 512, 0, L.stream>>>(L);
+}
+
+// ---------------------------------------------------------------- Maxwell
+// Right-hand side into slot step+2 from slot 1 (EMSolver.cpp:479-553).
+__global__ void k_mx_rhs(MaxwellLaunch L) {
+    const int run = blockIdx.y;
+    if (run >= L.nruns) return;
+    RunFields &F = L.fields[run];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nf = F.nf;
+    if (i >= nf) return;
+    const int s2 = (L.step + 2) * nf;
+    const double *By = F.By + nf, *Bz = F.Bz + nf, *Ey = F.Ey + nf, *Ez = F.Ez + nf, *Ay = F.Ay + nf, *Az = F.Az + nf;
+    const double dx_inv = L.dxinv[run];
+    const double eps0_inv = kEps0Inv, mu_inv = kMuInv;
+    double rBy = 0, rBz = 0, rEy = 0, rEz = 0, rAy = 0, rAz = 0;
+    const int pre = F.pre, n = F.n;
+    if (i == 0) {
+        const double *pb = L.params + param_base(run, L.step);
+        double by0 = pb[16], bz0 = pb[17];
+        rBy = dx_inv * (Ez[1] - Ez[0]);
+        rBz = -dx_inv * (Ey[1] - Ey[0]);
+        rEy = -dx_inv * (Bz[0] - bz0) * eps0_inv * mu_inv;
+        rEz = dx_inv * (By[0] - by0) * eps0_inv * mu_inv;
+        rAy = -Ey[0];
+        rAz = -Ez[0];
+    } else if (i < pre || (i >= pre + n && i < nf - 2)) {
+        rBy = dx_inv * (Ez[i + 1] - Ez[i]);
+        rBz = -dx_inv * (Ey[i + 1] - Ey[i]);
+        rEy = -dx_inv * (Bz[i] - Bz[i - 1]) * eps0_inv * mu_inv;
+        rEz = dx_inv * (By[i] - By[i - 1]) * eps0_inv * mu_inv;
+        rAy = -Ey[i];
+        rAz = -Ez[i];
+    } else if (i >= pre && i < pre + n) {
+        const double c1 = -1.0 / 24;
+        const double c2 = 9.0 / 8.0;
+        const double Jv = F.J[i - pre];
+        rBy = dx_inv * (c1 * (Ez[i + 2] - Ez[i - 1]) + c2 * (Ez[i + 1] - Ez[i]));
+        rBz = -dx_inv * (c1 * (Ey[i + 2] - Ey[i - 1]) + c2 * (Ey[i + 1] - Ey[i]));
+        rEy = -dx_inv * (c1 * (Bz[i + 1] - Bz[i - 2]) + c2 * (Bz[i] - Bz[i - 1])) * eps0_inv * mu_inv - eps0_inv * Jv * Ay[i];
+        rEz = dx_inv * (c1 * (By[i + 1] - By[i - 2]) + c2 * (By[i] - By[i - 1])) * eps0_inv * mu_inv - eps0_inv * Jv * Az[i];
+        rAy = -Ey[i];
+        rAz = -Ez[i];
+    }
+    F.By[s2 + i] = rBy;
+    F.Bz[s2 + i] = rBz;
+    F.Ey[s2 + i] = rEy;
+    F.Ez[s2 + i] = rEz;
+    F.Ay[s2 + i] = rAy;
+    F.Az[s2 + i] = rAz;
+}
+
+// Stage combination (EMSolver.cpp:204-338).  coef[0..5] are the dt-scaled weights of
+// slots 2..7; the last stage writes slot 0 from slot 1 and copies it back to slot 1.
+__device__ __forceinline__ void mx_combine(double *X, int nf, int i, int step, const double *c) {
+    if (step < 5) {
+        double v = X[i] + c[0] * X[2 * nf + i];
+        for (int k = 1; k <= step; k++) v = v + c[k] * X[(k + 2) * nf + i];
+        X[nf + i] = v;
+    } else {
+        double v = X[nf + i] + c[0] * X[2 * nf + i];
+        for (int k = 1; k <= 5; k++) v = v + c[k] * X[(k + 2) * nf + i];
+        X[i] = v;
+        X[nf + i] = v;
+    }
+}
+
+__global__ void k_mx_update(MaxwellLaunch L) {
+    const int run = blockIdx.y;
+    if (run >= L.nruns) return;
+    RunFields &F = L.fields[run];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.nf) return;
+    const double *c = L.params + param_base(run, L.step) + 8;
+    mx_combine(F.By, F.nf, i, L.step, c);
+    mx_combine(F.Bz, F.nf, i, L.step, c);
+    mx_combine(F.Ey, F.nf, i, L.step, c);
+    mx_combine(F.Ez, F.nf, i, L.step, c);
+    mx_combine(F.Ay, F.nf, i, L.step, c);
+    mx_combine(F.Az, F.nf, i, L.step, c);
+}
+
+// WENO-weighted (unmapped) face value of A (EMSolver.cpp:555-619).
+__device__ __forceinline__ double face_a(double f1, double f2, double f3, double f4) {
+    const double c6 = 1.0 / 6;
+    const double c43 = 4.0 / 3;
+    double fL = c6 * (-f1 + 5 * f2 + 2 * f3);
+    double fR = c6 * (2 * f2 + 5 * f3 - f4);
+    double AL = f1 - 2 * f2 + f3;
+    double BL = f3 - f1;
+    double AR = f2 - 2 * f3 + f4;
+    double BR = f4 - f2;
+    double bL = c43 * (AL * AL) + 0.5 * AL * BL + 0.25 * (BL * BL);
+    double bR = c43 * (AR * AR) - 0.5 * AR * BR + 0.25 * (BR * BR);
+    const double mm = 1.0e-10;
+    double oL = 0.5 / ((mm + bL) * (mm + bL));
+    double oR = 0.5 / ((mm + bR) * (mm + bR));
+    double wL = oL / (oL + oR);
+    double wR = oR / (oL + oR);
+    return wL * fL + wR * fR;
+}
+
+__global__ void k_mx_asq(MaxwellLaunch L) {
+    const int run = blockIdx.y;
+    if (run >= L.nruns) return;
+    RunFields &F = L.fields[run];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.n) return;
+    const double *Ay = F.Ay + F.nf + F.pre + i, *Az = F.Az + F.nf + F.pre + i;
+    double a_y = face_a(Ay[-2], Ay[-1], Ay[0], Ay[1]);
+    double a_z = face_a(Az[-2], Az[-1], Az[0], Az[1]);
+    F.asq[i] = (a_y * a_y) + (a_z * a_z);
+}
+
+void launch_maxwell(const MaxwellLaunch &L) {
+    dim3 g((L.maxnf + 255) / 256, L.nruns);
+    k_mx_rhs<<<g, 256, 0, L.stream>>>(L);
+    k_mx_update<<<g, 256, 0, L.stream>>>(L);
+    k_mx_asq<<<g, 256, 0, L.stream>>>(L);
+}
+
+// ---------------------------------------------------------------- CFL
+__global__ void k_cfl(CflLaunch L) {
+    const int run = blockIdx.x;
+    const RunFields &F = L.fields[run];
+    const int ns = L.run_ns[run];
+    const double *sp = L.spec + run * 25;  // up to 8 species x 3 + dpsMax
+    const double dpsMax = sp[24];
+    __shared__ double red[256];
+    double pc = 0.0;
+    for (int i = threadIdx.x; i < F.n; i += blockDim.x) {
+        double Azv = F.Az[i], Ayv = F.Ay[i];
+        double As = Ayv * Ayv + Azv * Azv;
+        double temp = 0.0;
+        for (int j = 0; j < ns; j++) {
+            double aq = sp[3 * j], m = sp[3 * j + 1], dps = sp[3 * j + 2];
+            double v = aq / m / sqrt(1 + As / ((m * kCs) * (m * kCs))) * dps;
+            temp = (temp < v) ? v : temp;
+        }
+        double v = temp * fabs(Ayv * F.Bz[i] - Azv * F.By[i]) + dpsMax * fabs(F.efin[i]);
+        pc = (pc < v) ? v : pc;
+    }
+    red[threadIdx.x] = pc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) {
+            double o = red[threadIdx.x + s];
+            red[threadIdx.x] = (red[threadIdx.x] < o) ? o : red[threadIdx.x];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) L.out[run] = red[0];
+}
+
+void launch_cfl(const CflLaunch &L) {
+    k_cfl<<<L.nruns, 256, 0, L.stream>>>(L);
+}
+
+__global__ void k_negate(double *dst, const double *src, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = -src[i];
+}
+
+void launch_negate(double *dst, const double *src, int n, cudaStream_t s) {
+    k_negate<<<(n + 255) / 256, 256, 0, s>>>(dst, src, n);
+}
+
+}  // namespace vx
+
+namespace vx {
+// Eight independent fused multiply-add chains per thread (register resident).  The
+// result is stored so the chains are not eliminated.
+__global__ void k_fp64_peak(double *out, int iters) {
+    double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+    double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+    const double b = 0.999999, c = 1e-7;
+    for (int k = 0; k < iters; k++) {
+        a0 = fma(a0, b, c);
+        a1 = fma(a1, b, c);
+        a2 = fma(a2, b, c);
+        a3 = fma(a3, b, c);
+        a4 = fma(a4, b, c);
+        a5 = fma(a5, b, c);
+        a6 = fma(a6, b, c);
+        a7 = fma(a7, b, c);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+void launch_fp64_peak(double *out, int blocks, int threads, int iters, cudaStream_t s) {
+    k_fp64_peak<<<blocks, threads, 0, s>>>(out, iters);
+}
+}  // namespace vx

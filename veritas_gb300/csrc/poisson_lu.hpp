@@ -1,0 +1,30 @@
+// Host set-up of the Poisson operator (EMFieldSolver::EMFieldSolver, EMSolver.cpp:28-88).
+//
+// The reference assembles a dense n x n column-major matrix (n = finest x size) and
+// factorises it once with LAPACK dgetrf; every RK stage then calls dgetrs.  The matrix
+// is a periodic 4th-order Laplacian stencil with row/column 0 replaced by a gauge
+// condition, so its LU factors with partial pivoting have O(n) nonzeros.  PoissonLU
+// builds only the nonzeros and runs the unblocked right-looking factorisation with
+// partial pivoting (first maximal |pivot|, full-row swaps, multipliers by division),
+// skipping only exact-zero operands — the same values the dense algorithm stores.  The
+// factors are uploaded once per run; the device applies the column-oriented triangular
+// solves in the same order (fields64.cu: k_poisson).
+#pragma once
+#include <utility>
+#include <vector>
+
+namespace vx {
+
+struct PoissonLU {
+    int n = 0;
+    std::vector<int> ipiv;                             // pivot row of step k (0-based)
+    std::vector<int> lptr, lcol, uptr, ucol;           // CSR rows: L ascending, U descending
+    std::vector<double> lval, uval, udiag;
+    // Factorise the Veritas Poisson matrix of size n (n >= 5).  Returns 0 or k+1 for a
+    // zero pivot at step k.
+    int build(int n);
+    // Host reference solve with the same operation order as the device (tests only).
+    void solve(double *b) const;
+};
+
+}  // namespace vx

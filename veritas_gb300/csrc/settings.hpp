@@ -1,0 +1,121 @@
+// Host-side configuration, mirroring the reference's Input / Particles / Output structs
+// and Settings class (Settings.hpp:4-67, Settings.cpp:5-195).  The user hooks the
+// reference expects in its problem file (veritas.cpp: settingsOverride,
+// InitialDistribution, GetBY/GetBZ, RefinementOverride) are virtual methods of
+// vx::Problem; vx::LaserSlab is the built-in synthetic laser / plasma-slab problem.
+#pragma once
+#include <cmath>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "vx_common.hpp"
+
+namespace vx {
+
+struct Input {  // Settings.hpp:4-11
+    double minEfficiency = 0.6, dx = 0.5, k = 0.01;
+    double refinementCriteria = 1e-8, cfl = 0.9, sizeWeight = 0.0;
+    double preLength = 2, postLength = 2;
+    unsigned int nx = 76 * 4, r = 2, Lfinest = 5;
+    double plasma_xl_bound = 3.0e-6, plasma_xr_bound = 7.0e-6;
+    std::vector<double> tempEM = {0.0};
+};
+
+struct Particles {  // Settings.hpp:13-20
+    std::vector<double> mass = {9.10938291e-31};
+    std::vector<double> charge = {-1.60217657e-19};
+    std::vector<std::vector<double>> misc = {{0.0, 0.01}};
+    std::vector<unsigned int> np = {50};
+    std::vector<double> dp = {0.1};
+    std::vector<double> pmin = {0.1};
+};
+
+struct Output {  // Settings.hpp:22-33 (file output itself is not part of the step)
+    bool time = true, rectangleData = true, charge = true, energy = true, potential = true;
+    bool EFieldLongitudinal = true, EFieldTransverse = true, BFieldTransverse = true, AFieldSquared = true;
+    int precision = 15;
+};
+
+class Settings;
+
+// The user's problem definition.  Default behaviour matches an empty override.
+class Problem {
+public:
+    virtual ~Problem() = default;
+    virtual void initialConditions(Input &grid, Particles &particles, Output &output) = 0;
+    virtual void settingsOverride(Settings &s) = 0;
+    virtual double InitialDistribution(const Settings &s, double x, double p, int particleType) const = 0;
+    virtual double GetBY(const Settings &s, double x, double t) const = 0;
+    virtual double GetBZ(const Settings &s, double x, double t) const = 0;
+    virtual bool RefinementOverride(const Settings &s, double x, double p, int depth, int particleType) const = 0;
+    virtual bool HasRefinementOverride() const { return true; }
+};
+
+// Parameters of the built-in laser / plasma-slab problem (lengths in laser wavelengths,
+// momenta in m_e c, temperatures in keV).  Field layout matches vx_problem in vx.h.
+struct LaserSlabParams {
+    double lambda = 1e-6;
+    double L = 100.0;
+    unsigned nx = 2048, np = 256, Lfinest = 1, r = 2;
+    double pmax = 2.0;
+    double dens = 0.01;
+    double x1 = 15, x2 = 20, x3 = 80, x4 = 85;
+    double Te = 1.0;
+    double p0 = 0.0;
+    double pert_amp = 0.0, pert_k = 1.0;
+    double a0 = 1.0, fwhm = 10.0, delay = 10.0;
+    double cfl = 0.5, minEff = 0.75, crit = 1e-6, sizeWeight = 1.0;
+    int quadDepth = 2;
+};
+
+class LaserSlab : public Problem {
+public:
+    explicit LaserSlab(const LaserSlabParams &p) : P(p) {}
+    void initialConditions(Input &grid, Particles &particles, Output &output) override;
+    void settingsOverride(Settings &s) override;
+    double InitialDistribution(const Settings &s, double x, double p, int particleType) const override;
+    double GetBY(const Settings &s, double x, double t) const override;
+    double GetBZ(const Settings &s, double x, double t) const override;
+    bool RefinementOverride(const Settings &s, double x, double p, int depth, int particleType) const override {
+        return false;
+    }
+    bool HasRefinementOverride() const override { return false; }
+    double slab_density(double xl) const;
+    LaserSlabParams P;
+};
+
+class Settings {  // Settings.hpp:35-65
+public:
+    Output output;
+    double dx, time, minEfficiency, preLength, postLength, refinementCriteria, cfl, sizeWeight, plasma_xl_bound,
+        plasma_xr_bound;
+    std::vector<double> m, q, m_inv, dp, fMax, tempEM, pmin;
+    std::vector<std::vector<double>> temp;
+    unsigned int x_size_finest, x_size, refinementRatio;
+    int maxDepth, quadratureDepth = 0;
+    std::vector<unsigned int> p_size, p_size_finest;
+    std::shared_ptr<Problem> problem;
+
+    // Throws std::invalid_argument where the reference exits (Settings.cpp:35-50).
+    Settings(const Input &grid, const Particles &particles, const Output &out, std::shared_ptr<Problem> problem);
+    double InitialDistribution(double x, double p, int particleType) const {
+        return problem->InitialDistribution(*this, x, p, particleType);
+    }
+    double GetDp(int level, int particleType) const;
+    double GetDx(int level) const;
+    int GetXSize(int level) const;
+    int GetPSize(int level, int particleType) const;
+    double GetMass(int i) const { return m.at(i); }
+    double GetCharge(int i) const { return q.at(i); }
+    double GetfMax(int i) const { return fMax.at(i); }
+    void UpdateTime(int step, double dt);
+    double GetBY(double x, double t) const { return problem->GetBY(*this, x, t); }
+    double GetBZ(double x, double t) const { return problem->GetBZ(*this, x, t); }
+    void DetermineMaximum();
+    bool RefinementOverride(double x, double p, int depth, int particleType) const {
+        return problem->RefinementOverride(*this, x, p, depth, particleType);
+    }
+};
+
+}  // namespace vx

@@ -1,0 +1,122 @@
+// Kernel launch interfaces shared by the CUDA translation units and the host runtime.
+#pragma once
+#include <cuda_runtime.h>
+#include "vx_common.hpp"
+
+namespace vx {
+
+// One 32(p) x 8(x) tile of a patch's padded block; (i0, j0) is its lower corner in
+// reference indices (>= -2).
+struct TileRef {
+    int patch, i0, j0;
+};
+
+// Per-run, per-stage parameter block in device memory (doubles):
+//   [0..5]  FCT RK weights a_{s,k} * dt (Rectangle.cpp:1396-1517), [6] their sum,
+//   [8..13] Maxwell stage weights (EMSolver.cpp:204-338),
+//   [16] GetBY(0, t_s), [17] GetBZ(0, t_s) with t_s the time after UpdateTime(s).
+constexpr int kParamStride = 18;
+VX_HD inline int param_base(int run, int step) { return (run * 6 + step) * kParamStride; }
+
+enum FctSub : int {
+    kSubGamma = 0,
+    kSubFaces,
+    kSubFlux,
+    kSubDsF2,
+    kSubLimR,
+    kSubLimC,
+    kSubUpdate,
+    kSubCopy10,
+};
+
+struct FctLaunch {
+    const void *patches;  // device array of PatchT<T>
+    const TileRef *tiles;
+    int ntiles;
+    const RunFields *fields;  // device array, one per run
+    const double *params;     // per-run stage parameter blocks
+    int step;
+    int use_f0;
+    cudaStream_t stream;
+};
+
+void launch_fct64_substep(const FctLaunch &L, int sub);
+
+// ---------------------------------------------------------------- moments
+struct MomLaunch {
+    const void *patches;
+    const int *colpatch;  // per moment column: patch index
+    const int *colidx;    // per moment column: local column index c = i*rtb + k
+    int ncols;
+    int maxnp;            // largest n_p over the patches
+    const RunFields *fields;
+    double *Lbuf;         // scratch: log-ratio table, ncols * (maxnp + 2)
+    cudaStream_t stream;
+};
+void launch_moments64(const MomLaunch &M);
+
+// Assembly of rho and J on the finest grid (EMSolver::AssembleRhoAndJ).
+struct AsmLaunch {
+    const void *patches;
+    const int *lvl_ptr;    // per run, (ns*nl + 1) offsets into lvl_patch (relative to run)
+    const int *lvl_off;    // per run: offset of its lvl_ptr block
+    const int *lvl_patch;  // patch indices level by level, in each level's patch order
+    const int *run_n;      // per run: n
+    const int *run_ns;     // per run: species count
+    const int *run_nl;     // per run: level count
+    int nruns, maxn;
+    RunFields *fields;
+    cudaStream_t stream;
+};
+void launch_assemble(const AsmLaunch &A);
+
+// Poisson solve with precomputed sparse LU factors (EMSolver::UpdatePotential).
+struct LUDev {
+    int n;
+    const int *ipiv;
+    const int *lptr, *lcol;
+    const double *lval;
+    const int *uptr, *ucol;
+    const double *uval;
+    const double *udiag;
+};
+struct PoissonLaunch {
+    const LUDev *lu;      // per run
+    RunFields *fields;    // per run (device array)
+    const double *w;      // per run: dx0^2
+    const double *fcoef;  // per run: 1/(12 dx0)
+    int nruns;
+    int maxn;
+    cudaStream_t stream;
+};
+void launch_poisson(const PoissonLaunch &L);
+
+// Maxwell RK stage + face interpolation of A (EMSolver::RGKStep).
+struct MaxwellLaunch {
+    RunFields *fields;  // device array
+    int nruns, maxnf;
+    int step;
+    const double *params;  // per-run stage parameter blocks
+    const double *dxinv;   // per run: 1/dx0
+    cudaStream_t stream;
+};
+void launch_maxwell(const MaxwellLaunch &L);
+
+// CFL bound (EMSolver::EstimateCFLBound), result per run into out[run].
+struct CflLaunch {
+    const RunFields *fields;
+    int nruns, maxn;
+    const double *spec;   // per run: [ns][3] = |q|, m, dps ; followed by dpsMax
+    const int *run_ns;
+    double *out;
+    cudaStream_t stream;
+};
+void launch_cfl(const CflLaunch &L);
+
+// FP64 FMA throughput probe: blocks x threads threads, iters x 8 independent DFMA each.
+void launch_fp64_peak(double *out, int blocks, int threads, int iters, cudaStream_t s);
+
+// dst[i] = -src[i]
+void launch_negate(double *dst, const double *src, int n, cudaStream_t s);
+
+}  // namespace vx
