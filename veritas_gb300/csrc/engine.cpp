@@ -52,6 +52,7 @@ Run::Run(Engine &e, std::shared_ptr<Problem> prob) : eng(e) {
 Run::~Run() {
     auto &v = eng.runs;
     v.erase(std::remove(v.begin(), v.end(), this), v.end());
+    eng.forget(this);
 }
 
 long long Run::cell_count() const {
@@ -68,7 +69,8 @@ void Run::allocate_rect(Rect &r) {
     r.pitch = ((r.n_p + 4) + 7) / 8 * 8;
     size_t pe = r.plane_elems();
     r.slab = DevBuf(pe * kPlanes * sizeof(double));
-    r.cols = DevBuf((size_t)2 * r.n_x * (1 << std::max(0, r.depth)) * sizeof(double) + 64);
+    const int rtb = (int)std::pow(S->refinementRatio, r.depth);
+    r.cols = DevBuf((size_t)2 * r.n_x * rtb * sizeof(double) + 64);
     PatchT<double> &d = r.desc;
     std::memset(&d, 0, sizeof d);
     double *base = r.slab.as<double>();
@@ -435,6 +437,15 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
 }
 
 void Engine::sync() { VX_CUDA(cudaStreamSynchronize(stream)); }
+
+// Drop every cached launch set that refers to a run being destroyed.
+void Engine::forget(Run *r) {
+    cudaStreamSynchronize(stream);
+    for (auto it = sets_.begin(); it != sets_.end();) {
+        if (std::find(it->first.begin(), it->first.end(), r) != it->first.end()) it = sets_.erase(it);
+        else ++it;
+    }
+}
 
 LaunchSet &Engine::get_set(const std::vector<Run *> &set) {
     auto it = sets_.find(set);

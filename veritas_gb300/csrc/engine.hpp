@@ -135,6 +135,7 @@ public:
     void flush_l2();
     double measure_fp64_peak();
     void sync();
+    void forget(Run *r);
 
 private:
     std::map<std::vector<Run *>, std::unique_ptr<LaunchSet>> sets_;
