@@ -150,6 +150,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lite", action="store_true",
+                    help="only the warm-up and timed steps (used under ncu); no e2e, kernel timing or CPU baseline")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -198,6 +200,12 @@ def main() -> None:
         dist.barrier()
     ms_step = total_ms / args.steps
     value = cells * world * args.steps / (total_ms * 1e-3)
+    if args.lite:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms_step, "lite": True}))
+        s.close()
+        ctx.close()
+        return
 
     # ---- end to end through the C ABI with pinned host buffers
     n = s.state_size()

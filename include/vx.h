@@ -129,7 +129,7 @@ int vx_host_free(void *p);
 
 /* Packed host image of a run's state at a step boundary: every patch's f (slot 0,
  * padded (n_x+4) x pitch block, patch order species -> level -> patch), then the six
- * transverse field arrays (slot 0, n+pre+post each), a_squared (n+1) and Ex0.  *len
+ * transverse field arrays (slot 0, n+pre+post each), a_squared (n+1), phi (n) and Ex0.  *len
  * receives the element count. */
 int vx_run_state_size(vx_run *run, int64_t *len);
 /* Copy the run's current state into a packed host image (D2H only). */

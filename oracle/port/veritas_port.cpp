@@ -1,0 +1,857 @@
+// ORACLE / TEST INFRASTRUCTURE — CPU restatement of the Veritas Vlasov–Maxwell step.
+//
+// Not part of the product: tests compare the CUDA path against it, and bench.py times
+// it on the host cores as the CPU baseline ("kind": "port").  It restates, in plain
+// C++/OpenMP, the per-step algorithm of the reference for a mesh whose every species is
+// one patch covering the domain (the single-level case):
+//   SolverManager::Advance            SolverManager.cpp:28-39
+//   EMFieldSolver::AssembleRhoAndJ     EMSolver.cpp:104-122
+//   Rectangle::CalculateRhoAndJ (MKL)  Rectangle.cpp:157-237, 276-281
+//   EMFieldSolver::UpdatePotential     EMSolver.cpp:156-192  (LU: oracle/lu_exact.hpp)
+//   Rectangle::FCTTimeStep             Rectangle.cpp:1255-1623
+//   EMFieldSolver::RGKStep             EMSolver.cpp:194-619
+//   EMFieldSolver::EstimateCFLBound    EMSolver.cpp:631-664
+//   Rectangle::InitializeDistribution  Rectangle.cpp:616-665
+//   Settings::UpdateTime               Settings.cpp:166-179
+// Each floating-point expression keeps the reference's operations and order, so with
+// -ffp-contract=off the results are bit-identical to the reference build (which links
+// the same LU restatement through its MKL header shim).  Pinned against the reference's
+// own dumps by tests/test_oracle_port.py.
+//
+// Command line: the parity harness's key=value problem arguments, plus
+//   load=<state file>  start from a VXST0001 state instead of t=0
+//   dts=a,b,c          use these step sizes instead of the CFL bound
+//   steps=N dump_every=K dumpdir=D time_steps=M
+#include <omp.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../lu_exact.hpp"
+
+namespace {
+
+// Constants as the reference defines them (veritas.hpp:22-30).
+const double eps0_inv = 1.1294e+11;
+const double eps0 = 8.854187817e-12;
+const double mu_inv = 795774.715482;
+const double cs = 299792458.0;
+const double c_inv = 3.33564095e-9;
+const double DPI = 6.28318530718;
+
+const double kMe = 9.10938291e-31;
+const double kQe = -1.60217657e-19;
+const double kKeV = 1.602176565e-16;
+
+struct Params {
+    double lambda = 1e-6, L = 100.0;
+    unsigned nx = 2048, np = 256, Lfinest = 1, r = 2;
+    double pmax = 2.0, dens = 0.01, x1 = 15, x2 = 20, x3 = 80, x4 = 85, Te = 1.0, p0 = 0.0;
+    double pert_amp = 0.0, pert_k = 1.0, a0 = 1.0, fwhm = 10.0, delay = 10.0;
+    double cfl = 0.5, minEff = 0.75, crit = 1e-6, sizeWeight = 1.0;
+    int quadDepth = 2;
+};
+
+// ------------------------------------------------------------------ problem hooks
+struct Problem {
+    Params P;
+    double m, q, dp, pmin, dx, n0, sigma, pdrift, A0;
+    int maxDepth, quadDepth;
+    unsigned x_size, p_size, r;
+
+    void setup() {
+        m = kMe;
+        q = kQe;
+        x_size = P.nx;
+        p_size = P.np;
+        r = P.r;
+        maxDepth = (int)P.Lfinest - 1;
+        double mc = m * cs;
+        dp = 2.0 * P.pmax * mc / p_size;
+        pmin = -P.pmax * mc;
+        dx = P.L * P.lambda / x_size;
+        quadDepth = P.quadDepth;
+        double T = P.lambda / cs;
+        double omega = DPI / T;
+        double Nc = omega * omega * m * eps0 / (q * q);
+        n0 = P.dens * Nc;
+        sigma = m * (P.Te * kKeV);
+        pdrift = P.p0 * mc;
+        A0 = P.a0 * mc / std::fabs(q);
+    }
+    double slab(double xl) const {
+        double s;
+        if (xl <= P.x1 || xl >= P.x4) s = 0.0;
+        else if (xl < P.x2) s = (xl - P.x1) / (P.x2 - P.x1);
+        else if (xl <= P.x3) s = 1.0;
+        else s = (P.x4 - xl) / (P.x4 - P.x3);
+        if (P.pert_amp != 0.0) s = s * (1.0 + P.pert_amp * std::sin(DPI * P.pert_k * xl / P.L));
+        return s;
+    }
+    double init_f(double x, double p) const {
+        double ne = n0 * slab(x / P.lambda);
+        double d = p - pdrift;
+        return ne * std::exp(-(d * d) / (2.0 * sigma)) / std::sqrt(DPI * sigma);
+    }
+    double BY(double, double) const { return 0.0; }
+    double BZ(double x, double t) const {
+        double T = P.lambda / cs;
+        double k = DPI / P.lambda;
+        double omega = cs * k;
+        double F = P.fwhm * T;
+        double tau = (t - x / cs) - P.delay * T;
+        double c4 = 4.0 * std::log(2.0) / (F * F);
+        double g = std::exp(-c4 * tau * tau);
+        double gp = -2.0 * c4 * tau * g;
+        double ph = omega * t - k * x;
+        return A0 * (k * g * std::sin(ph) - (gp / cs) * std::cos(ph));
+    }
+    double GetDx(int level) const { return std::pow(r, level - maxDepth) * dx; }
+    double GetDp(int level) const { return std::pow(r, level - maxDepth) * dp; }
+    int GetXSize(int level) const { return x_size * std::pow(r, -level + maxDepth); }
+    int GetPSize(int level) const { return p_size * std::pow(r, -level + maxDepth); }
+};
+
+// ------------------------------------------------------------------ patch
+// One patch: SoA planes of (nx+4) x (np+4) doubles, p fastest.
+struct Patch {
+    int nx, np, x_pos = 0, p_pos = 0, depth, rtb;
+    bool up = true, down = true, left = true, right = true;
+    int W;  // row width np + 4
+    std::vector<double> f[3], gam, ex, fx, ep, fp, FxH[6], FpH[6], FxL, FpL, FxDS, FpDS, Rp, Rm, Cx, Cp;
+    std::vector<double> chargeR, currentR, relc;
+    double dx, dp, dx_inv, dp_inv, pmin, q, m, cc, g2;
+    size_t id(int i, int j) const { return (size_t)(i + 2) * W + (j + 2); }
+    void alloc() {
+        W = np + 4;
+        size_t N = (size_t)(nx + 4) * W;
+        for (auto &v : f) v.assign(N, 0.0);
+        for (auto *v : {&gam, &ex, &fx, &ep, &fp, &FxL, &FpL, &FxDS, &FpDS, &Rp, &Rm, &Cx, &Cp}) v->assign(N, 0.0);
+        for (int s = 0; s < 6; s++) {
+            FxH[s].assign(N, 0.0);
+            FpH[s].assign(N, 0.0);
+        }
+        chargeR.assign((size_t)nx * rtb, 0.0);
+        currentR.assign((size_t)nx * rtb, 0.0);
+    }
+};
+
+struct Fields {
+    int n, pre, post, nf;
+    std::vector<double> By, Bz, Ey, Ez, Ay, Az, asq, phi, charge, J, neut;
+    double Ex0 = 0.0, fcoef;
+    size_t I(int i, int slot) const { return (size_t)slot * nf + i; }
+};
+
+// ------------------------------------------------------------------ numerics
+inline double vmax(double a, double b) { return (a > b) ? a : b; }
+inline double vmin(double a, double b) { return (a < b) ? a : b; }
+
+double weno(double f1, double f2, double f3, double f4, bool right) {
+    double fL = (1.0 / 6) * (-f1 + 5 * f2 + 2 * f3);
+    double fR = (1.0 / 6) * (2 * f2 + 5 * f3 - f4);
+    double AL = f1 - 2 * f2 + f3;
+    double BL = f3 - f1;
+    double AR = f2 - 2 * f3 + f4;
+    double BR = f4 - f2;
+    double bL = 4.0 / 3 * (AL * AL) + 0.5 * AL * BL + 0.25 * (BL * BL);
+    double bR = 4.0 / 3 * (AR * AR) - 0.5 * AR * BR + 0.25 * (BR * BR);
+    double mm = 1.0e-10;
+    double oL = 0.5 / ((mm + bL) * (mm + bL));
+    double oR = 0.5 / ((mm + bR) * (mm + bR));
+    double wL = oL / (oL + oR);
+    double wR = oR / (oL + oR);
+    double wL0 = wL * (0.75 + wL * (wL - 0.5));
+    double wR0 = wR * (0.75 + wR * (wR - 0.5));
+    double pick = right ? ((wL0 > wR0) ? wL0 : wR0) : ((wL0 < wR0) ? wL0 : wR0);
+    double fwl = pick / (wL0 + wR0);
+    double fwr = 1 - fwl;
+    return fwl * fL + fwr * fR;
+}
+
+double face_a(double f1, double f2, double f3, double f4) {
+    double fL = (1.0 / 6) * (-f1 + 5 * f2 + 2 * f3);
+    double fR = (1.0 / 6) * (2 * f2 + 5 * f3 - f4);
+    double AL = f1 - 2 * f2 + f3;
+    double BL = f3 - f1;
+    double AR = f2 - 2 * f3 + f4;
+    double BR = f4 - f2;
+    double bL = 4.0 / 3 * (AL * AL) + 0.5 * AL * BL + 0.25 * (BL * BL);
+    double bR = 4.0 / 3 * (AR * AR) - 0.5 * AR * BR + 0.25 * (BR * BR);
+    double mm(1.0e-10);
+    double oL = 0.5 / ((mm + bL) * (mm + bL));
+    double oR = 0.5 / ((mm + bR) * (mm + bR));
+    double wL = oL / (oL + oR);
+    double wR = oR / (oL + oR);
+    return wL * fL + wR * fR;
+}
+
+struct Solver {
+    Problem pr;
+    std::vector<Patch> patches;  // one per species
+    Fields F;
+    vxo::SparseLU lu;
+    double time = 0.0;
+
+    double asq_face(int x) const { return F.asq[std::min(std::max(x, 0), F.n)]; }
+    double efield(int i) const {
+        const int n = F.n;
+        int ip1 = i + 1, im1 = i - 1, ip2 = i + 2, im2 = i - 2;
+        ip1 = (ip1 > -1) ? ip1 : (ip1 + n);
+        im1 = (im1 > -1) ? im1 : (im1 + n);
+        ip2 = (ip2 > -1) ? ip2 : (ip2 + n);
+        im2 = (im2 > -1) ? im2 : (im2 + n);
+        ip1 = (ip1 < n) ? ip1 : (ip1 - n);
+        im1 = (im1 < n) ? im1 : (im1 - n);
+        ip2 = (ip2 < n) ? ip2 : (ip2 - n);
+        im2 = (im2 < n) ? im2 : (im2 - n);
+        const double *P = F.phi.data();
+        return -F.fcoef * (8 * (P[ip1] - P[im1]) - P[ip2] + P[im2]) + F.Ex0;
+    }
+    double patch_efield(const Patch &P, int i) const {
+        int x = P.rtb * (i + P.x_pos);
+        double t = 0.0;
+        for (int k = 0; k < P.rtb; k++) t += efield(x + k);
+        return t * (1.0 / P.rtb);
+    }
+    double cell_asq(int x) const {
+        int i = x + F.pre;
+        i = i > -1 ? i : 0;
+        i = i < F.nf ? i : F.nf - 1;
+        double ay = F.Ay[F.I(i, 1)], az = F.Az[F.I(i, 1)];
+        return (ay * ay) + (az * az);
+    }
+
+    void setup() {
+        pr.setup();
+        const int base = pr.maxDepth;
+        Patch P;
+        P.nx = pr.GetXSize(base);
+        P.np = pr.GetPSize(base);
+        P.depth = base;
+        P.rtb = (int)std::pow(pr.r, base);
+        P.dx = pr.GetDx(base);
+        P.dp = pr.GetDp(base);
+        P.dx_inv = 1 / P.dx;
+        P.dp_inv = 1 / P.dp;
+        P.pmin = pr.pmin;
+        P.q = pr.q;
+        P.m = pr.m;
+        P.cc = cs * cs * pr.m;
+        double m_inv = 1 / pr.m;
+        P.g2 = (m_inv * c_inv) * (m_inv * c_inv);
+        P.relc.assign(3 * P.rtb, 0.0);
+        for (int i = 0; i < P.rtb; i++) {
+            double rb = P.rtb;
+            double tl = -0.5 + i / rb;
+            double tr = -0.5 + (i + 1.0) / rb;
+            P.relc[3 * i] = (tl + tr) * 0.5;
+            P.relc[3 * i + 1] = (tl * tl + tl * tr + tr * tr) / 3.0 - (1.0 / 12);
+            P.relc[3 * i + 2] = (tl * tl * tl + tl * tl * tr + tl * tr * tr + tr * tr * tr) * 0.25;
+        }
+        P.alloc();
+        patches.push_back(std::move(P));
+        F.n = pr.x_size * std::pow(pr.r, pr.maxDepth);
+        F.pre = std::max(std::floor(0.0 / pr.GetDx(0)), 2.0);
+        F.post = std::max(std::floor(0.0 / pr.GetDx(0)), 2.0);
+        F.nf = F.n + F.pre + F.post;
+        for (auto *v : {&F.By, &F.Bz, &F.Ey, &F.Ez, &F.Ay, &F.Az}) v->assign((size_t)F.nf * 8, 0.0);
+        F.asq.assign(F.n + 1, 0.0);
+        for (auto *v : {&F.phi, &F.charge, &F.J, &F.neut}) v->assign(F.n, 0.0);
+        F.fcoef = 1.0 / (12 * pr.GetDx(0));
+        const int n = F.n;
+        const double w1 = -16.0 / 30.0 / 0.4, w2 = 1.0 / 30.0 / 0.4, w3 = 1 / 0.4;
+        std::vector<std::vector<std::pair<int, double>>> rows(n);
+        std::vector<std::map<int, double>> acc(n);
+        auto put = [&](int col, int row, double v) { acc[row][col] = v; };
+        for (int i = 2; i < n - 2; i++) {
+            put(i, i, w3);
+            put(i, i + 1, w1);
+            put(i, i - 1, w1);
+            put(i, i + 2, w2);
+            put(i, i - 2, w2);
+        }
+        put(0, 0, 1.0);
+        put(1, 1, w3), put(1, 2, w1), put(1, 0, w1), put(1, 3, w2), put(1, n - 1, w2);
+        put(n - 2, n - 2, w3), put(n - 2, n - 1, w1), put(n - 2, n - 3, w1), put(n - 2, 0, w2), put(n - 2, n - 4, w2);
+        put(n - 1, n - 1, w3), put(n - 1, 0, w1), put(n - 1, n - 2, w1), put(n - 1, 1, w2), put(n - 1, n - 3, w2);
+        for (int rr = 0; rr < n; rr++)
+            for (auto &kv : acc[rr]) rows[rr].push_back({kv.first, kv.second});
+        lu.factor_rows(rows);
+    }
+
+    void init_distribution() {
+        for (auto &P : patches) {
+            const int nvals = std::pow(pr.r, P.depth + pr.quadDepth);
+#pragma omp parallel for schedule(guided)
+            for (int i = 0; i < P.nx; i++)
+                for (int j = 0; j < P.np; j++) {
+                    double temp = 0.0;
+                    for (int k = 0; k < nvals; k++)
+                        for (int l = 0; l < nvals; l++) {
+                            double xp = ((0.5 + k) / nvals + i + P.x_pos) * P.dx;
+                            double pp = P.pmin + P.dp * ((0.5 + l) / nvals + j + P.p_pos);
+                            temp += pr.init_f(xp, pp);
+                        }
+                    P.f[0][P.id(i, j)] = temp * (1 / std::pow(nvals, 2.0));
+                    P.f[1][P.id(i, j)] = temp * (1 / std::pow(nvals, 2.0));
+                }
+        }
+        assemble();
+        for (int i = 0; i < F.n; i++) F.neut[i] = -F.charge[i];
+        std::fill(F.J.begin(), F.J.end(), 0.0);
+    }
+
+    // ---------------------------------------------------------------- moments
+    double rel_value(const Patch &P, int i, int j, int k) const {
+        const double *f = P.f[1].data();
+        const double f3 = f[P.id(i, j)];
+        if (P.rtb == 1) return f3;
+        double g1 = f[P.id(i - 2, j)] - f3, g2 = f[P.id(i - 1, j)] - f3;
+        double g4 = f[P.id(i + 1, j)] - f3, g5 = f[P.id(i + 2, j)] - f3;
+        double a1 = 0.104166666666667 * g1 + -0.708333333333334 * g2 + 0.708333333333334 * g4 + -0.104166666666667 * g5;
+        double a2 = 0.117647058823529 * g1 + 0.029411764705882 * g2 + 0.029411764705882 * g4 + 0.117647058823529 * g5;
+        double a3 = -0.083333333333333 * g1 + 0.166666666666667 * g2 + -0.166666666666667 * g4 + 0.083333333333334 * g5;
+        double te = 0.0, mine = 0.0;
+        for (int q = 0; q < P.rtb; q++) {
+            double v = P.relc[3 * q] * a1 + P.relc[3 * q + 1] * a2 + P.relc[3 * q + 2] * a3 + f3;
+            te += v;
+            if (q == k) mine = v;
+        }
+        double cor = f3 - (1.0 / (double)P.rtb) * te;
+        return mine + cor;
+    }
+
+    void moments(Patch &P) {
+        const double q = P.q, mass = P.m;
+        const double c1 = (1 / mass) * c_inv, c2 = 1 / c1, c3 = 1 / 48.0;
+        const int rtb = P.rtb;
+#pragma omp parallel for schedule(guided)
+        for (int i = 0; i < P.nx; i++) {
+            for (int k = 0; k < rtb; k++) {
+                const double a = (q * q) * cell_asq((i + P.x_pos) * rtb + k);
+                std::vector<double> Lr(P.np + 2);
+                for (int j = -1; j <= P.np; j++) {
+                    double p0 = P.pmin + P.dp * (double)(j + P.p_pos);
+                    double p1 = P.pmin + P.dp * (double)(j + 1 + P.p_pos);
+                    double g0 = std::sqrt(1.0 + ((p0 * p0) + a) * P.g2);
+                    double g1 = std::sqrt(1.0 + ((p1 * p1) + a) * P.g2);
+                    Lr[j + 1] = c2 * std::log((g1 + c1 * p1) / (g0 + c1 * p0));
+                }
+                double vm1 = rel_value(P, i, -1, k), v0 = rel_value(P, i, 0, k), vp1 = rel_value(P, i, 1, k);
+                double ch = 0.0, cu = 0.0;
+                for (int j = 0; j < P.np; j++) {
+                    ch += v0;
+                    double gm = Lr[j + 1], gm1 = Lr[j], gp1 = Lr[j + 2];
+                    cu += v0 * gm + c3 * (gp1 - gm1) * (vp1 - vm1);
+                    vm1 = v0;
+                    v0 = vp1;
+                    vp1 = rel_value(P, i, j + 2, k);
+                }
+                P.chargeR[i * rtb + k] = ch * (P.dp * q);
+                P.currentR[i * rtb + k] = cu * (-q * q / mass);
+            }
+        }
+    }
+
+    void assemble() {
+        for (auto &P : patches) moments(P);
+        for (int x = 0; x < F.n; x++) {
+            double J = 0.0, charge = 0.0;
+            for (auto &P : patches) {
+                double cs_ = 0.0;
+                for (int l = 0; l <= pr.maxDepth; l++) {
+                    double lc = 0.0, lj = 0.0;
+                    if (l == P.depth) {
+                        int c = x - P.x_pos * P.rtb;
+                        if (c >= 0 && c < P.nx * P.rtb) {
+                            lc += P.chargeR[c];
+                            lj += P.currentR[c];
+                        }
+                    }
+                    cs_ += lc;
+                    J += lj;
+                }
+                charge += cs_;
+            }
+            F.charge[x] = charge;
+            F.J[x] = J;
+        }
+    }
+
+    void poisson() {
+        const int n = F.n;
+        const double w = std::pow(pr.GetDx(0), 2.0);
+        for (int i = 0; i < n; i++) F.phi[i] = eps0_inv * (F.charge[i] + F.neut[i]);
+        for (int i = 0; i < n; i++) F.phi[i] *= w;
+        lu.solve(F.phi.data());
+        F.Ex0 += -(efield(-1) + efield(0)) * 0.5;
+    }
+
+    // ---------------------------------------------------------------- FCT sub-steps
+    void fct_sub0(Patch &P, int step, const double *a, double asum) {
+        const int nx = P.nx, np = P.np;
+        const double *f = P.f[1].data();
+        const double w3 = 1 / 48.0;
+#pragma omp parallel for schedule(guided)
+        for (int i = -1; i <= nx + 1; i++) {
+            double as = P.q * P.q * asq_face(P.rtb * (i + P.x_pos));
+            for (int j = -1; j <= np + 1; j++) {
+                double p = P.pmin + P.dp * (double)(j + P.p_pos);
+                P.gam[P.id(i, j)] = std::sqrt(1.0 + ((p * p) + as) * P.g2);
+            }
+        }
+#pragma omp parallel for schedule(guided)
+        for (int i = -1; i <= nx; i++) {
+            double Em = P.q * patch_efield(P, i);
+            for (int j = -1; j <= np; j++) {
+                if (i >= 0) {
+                    double am = P.dp_inv * P.cc * (P.gam[P.id(i, j + 1)] - P.gam[P.id(i, j)]);
+                    P.ex[P.id(i, j)] = am;
+                    P.fx[P.id(i, j)] = weno(f[P.id(i - 2, j)], f[P.id(i - 1, j)], f[P.id(i, j)], f[P.id(i + 1, j)], am > 0.0);
+                }
+                if (j >= 0) {
+                    double am = Em - P.cc * P.dx_inv * (P.gam[P.id(i + 1, j)] - P.gam[P.id(i, j)]);
+                    P.ep[P.id(i, j)] = am;
+                    P.fp[P.id(i, j)] = weno(f[P.id(i, j - 2)], f[P.id(i, j - 1)], f[P.id(i, j)], f[P.id(i, j + 1)], am > 0.0);
+                }
+            }
+        }
+#pragma omp parallel for schedule(guided)
+        for (int i = -1; i <= nx; i++) {
+            for (int j = -1; j <= np; j++) {
+                size_t d = P.id(i, j);
+                if (i >= 0) {
+                    double am = P.ex[d], ap1 = P.ex[d + 1], am1 = P.ex[d - 1];
+                    double fm = P.fx[d], fp1 = P.fx[d + 1], fm1 = P.fx[d - 1];
+                    P.FxH[step][d] = P.dx_inv * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
+                    if (step == 0) P.FxL[d] = P.dx_inv * ((am > 0.0 ? f[d - P.W] : f[d]) * am);
+                }
+                if (j >= 0) {
+                    double am = P.ep[d], ap1 = P.ep[d + P.W], am1 = P.ep[d - P.W];
+                    double fm = P.fp[d], fp1 = P.fp[d + P.W], fm1 = P.fp[d - P.W];
+                    P.FpH[step][d] = P.dp_inv * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
+                    if (step == 0) P.FpL[d] = P.dp_inv * ((am > 0.0 ? f[d - 1] : f[d]) * am);
+                }
+            }
+        }
+        const int xm = P.left ? 1 : 0, xp = P.right ? nx : nx + 1, pm = P.down ? 1 : 0, pp = P.up ? np : np + 1;
+        auto act = [&](int i, int j) { return i >= xm && i < xp && j >= pm && j < pp; };
+#pragma omp parallel for schedule(guided)
+        for (int i = -2; i <= nx + 1; i++) {
+            for (int j = -2; j <= np + 1; j++) {
+                size_t d = P.id(i, j);
+                double hx = a[0] * P.FxH[0][d], hp = a[0] * P.FpH[0][d];
+                for (int k = 1; k <= step; k++) {
+                    if (step == 5 && k == 1) continue;
+                    hx = hx + a[k] * P.FxH[k][d];
+                    hp = hp + a[k] * P.FpH[k][d];
+                }
+                double lsx = asum * P.FxL[d], lsp = asum * P.FpL[d];
+                P.FxDS[d] = hx - lsx;
+                P.FpDS[d] = hp - lsp;
+            }
+        }
+        double *f2 = P.f[2].data();
+        const double *f0 = P.f[0].data();
+#pragma omp parallel for schedule(guided)
+        for (int i = 0; i < nx; i++)
+            for (int j = 0; j < np; j++) {
+                size_t d = P.id(i, j);
+                double v = f0[d];
+                if (act(i, j)) v += asum * P.FxL[d];
+                if (act(i, j)) v += asum * P.FpL[d];
+                if (act(i, j + 1)) v -= asum * P.FpL[d + 1];
+                if (act(i + 1, j)) v -= asum * P.FxL[d + P.W];
+                f2[d] = v;
+            }
+    }
+
+    void fct_sub1(Patch &P) {
+        const int nx = P.nx, np = P.np, W = P.W;
+        const double *f0 = P.f[0].data(), *f2 = P.f[2].data();
+#pragma omp parallel for schedule(guided)
+        for (int i = -1; i <= nx; i++)
+            for (int j = -1; j <= np; j++) {
+                size_t d = P.id(i, j);
+                double dxi = P.FxDS[d], dxn = P.FxDS[d + W], dpi = P.FpDS[d], dpn = P.FpDS[d + 1];
+                double Pp = vmax(0.0, dxi) - vmin(0.0, dxn) + vmax(0.0, dpi) - vmin(0.0, dpn);
+                double Pm = vmax(0.0, dxn) - vmin(0.0, dxi) + vmax(0.0, dpn) - vmin(0.0, dpi);
+                double wMax = vmax(vmax(f0[d], f2[d]), vmax(vmax(f0[d + W], f2[d + W]),
+                                   vmax(vmax(f0[d - W], f2[d - W]), vmax(vmax(f0[d + 1], f2[d + 1]), vmax(f0[d - 1], f2[d - 1])))));
+                double wMin = vmin(vmin(f0[d], f2[d]), vmin(vmin(f0[d + W], f2[d + W]),
+                                   vmin(vmin(f0[d - W], f2[d - W]), vmin(vmin(f0[d + 1], f2[d + 1]), vmin(f0[d - 1], f2[d - 1])))));
+                double Qm = -wMin + f2[d], Qp = wMax - f2[d];
+                P.Rp[d] = Pp > 0.0 ? vmin(1.0, Qp / Pp) : 0.0;
+                P.Rm[d] = Pm > 0.0 ? vmin(1.0, Qm / Pm) : 0.0;
+            }
+        std::fill(P.Cx.begin(), P.Cx.end(), 1.0);
+        std::fill(P.Cp.begin(), P.Cp.end(), 1.0);
+#pragma omp parallel for schedule(guided)
+        for (int i = 1; i < nx; i++)
+            for (int j = 0; j < np; j++) {
+                size_t d = P.id(i, j);
+                P.Cx[d] = P.FxDS[d] > 0.0 ? vmin(P.Rp[d], P.Rm[d - W]) : vmin(P.Rp[d - W], P.Rm[d]);
+                P.Cp[d] = P.FpDS[d] > 0.0 ? vmin(P.Rp[d], P.Rm[d - 1]) : vmin(P.Rp[d - 1], P.Rm[d]);
+            }
+    }
+
+    void fct_sub2(Patch &P) {
+        const int nx = P.nx, np = P.np, W = P.W;
+        const int xm = P.left ? 1 : 0, xp = P.right ? nx : nx + 1, pm = P.down ? 1 : 0, pp = P.up ? np : np + 1;
+        auto act = [&](int i, int j) { return i >= xm && i < xp && j >= pm && j < pp; };
+        double *f1 = P.f[1].data();
+        const double *f2 = P.f[2].data();
+#pragma omp parallel for schedule(guided)
+        for (int i = 0; i < nx; i++)
+            for (int j = 0; j < np; j++) {
+                size_t d = P.id(i, j);
+                double v = f2[d];
+                if (act(i, j)) v += P.Cx[d] * P.FxDS[d];
+                if (act(i, j)) v += P.Cp[d] * P.FpDS[d];
+                if (act(i, j + 1)) v -= P.Cp[d + 1] * P.FpDS[d + 1];
+                if (act(i + 1, j)) v -= P.Cx[d + W] * P.FxDS[d + W];
+                f1[d] = v;
+            }
+    }
+
+    // ---------------------------------------------------------------- Maxwell
+    void maxwell(int step, double timestep) {
+        const int nf = F.nf, pre = F.pre, n = F.n;
+        const double dx_inv = 1 / pr.GetDx(0);
+        const double bz0 = pr.BZ(0, time), by0 = pr.BY(0, time);
+        auto S1 = [&](std::vector<double> &X, int i) { return X[F.I(i, 1)]; };
+        for (int i = 0; i < nf; i++) {
+            double rBy = 0, rBz = 0, rEy = 0, rEz = 0, rAy = 0, rAz = 0;
+            if (i == 0) {
+                rBy = dx_inv * (S1(F.Ez, 1) - S1(F.Ez, 0));
+                rBz = -dx_inv * (S1(F.Ey, 1) - S1(F.Ey, 0));
+                rEy = -dx_inv * (S1(F.Bz, 0) - bz0) * eps0_inv * mu_inv;
+                rEz = dx_inv * (S1(F.By, 0) - by0) * eps0_inv * mu_inv;
+                rAy = -S1(F.Ey, 0);
+                rAz = -S1(F.Ez, 0);
+            } else if (i < pre || (i >= pre + n && i < nf - 2)) {
+                rBy = dx_inv * (S1(F.Ez, i + 1) - S1(F.Ez, i));
+                rBz = -dx_inv * (S1(F.Ey, i + 1) - S1(F.Ey, i));
+                rEy = -dx_inv * (S1(F.Bz, i) - S1(F.Bz, i - 1)) * eps0_inv * mu_inv;
+                rEz = dx_inv * (S1(F.By, i) - S1(F.By, i - 1)) * eps0_inv * mu_inv;
+                rAy = -S1(F.Ey, i);
+                rAz = -S1(F.Ez, i);
+            } else if (i >= pre && i < pre + n) {
+                const double c1 = -1.0 / 24, c2 = 9.0 / 8.0;
+                const double Jv = F.J[i - pre];
+                rBy = dx_inv * (c1 * (S1(F.Ez, i + 2) - S1(F.Ez, i - 1)) + c2 * (S1(F.Ez, i + 1) - S1(F.Ez, i)));
+                rBz = -dx_inv * (c1 * (S1(F.Ey, i + 2) - S1(F.Ey, i - 1)) + c2 * (S1(F.Ey, i + 1) - S1(F.Ey, i)));
+                rEy = -dx_inv * (c1 * (S1(F.Bz, i + 1) - S1(F.Bz, i - 2)) + c2 * (S1(F.Bz, i) - S1(F.Bz, i - 1))) * eps0_inv * mu_inv -
+                      eps0_inv * Jv * S1(F.Ay, i);
+                rEz = dx_inv * (c1 * (S1(F.By, i + 1) - S1(F.By, i - 2)) + c2 * (S1(F.By, i) - S1(F.By, i - 1))) * eps0_inv * mu_inv -
+                      eps0_inv * Jv * S1(F.Az, i);
+                rAy = -S1(F.Ey, i);
+                rAz = -S1(F.Ez, i);
+            }
+            const int s2 = step + 2;
+            F.By[F.I(i, s2)] = rBy;
+            F.Bz[F.I(i, s2)] = rBz;
+            F.Ey[F.I(i, s2)] = rEy;
+            F.Ez[F.I(i, s2)] = rEz;
+            F.Ay[F.I(i, s2)] = rAy;
+            F.Az[F.I(i, s2)] = rAz;
+        }
+        double c[6] = {0, 0, 0, 0, 0, 0};
+        static const double R[6][6] = {
+            {0.5, 0, 0, 0, 0, 0},
+            {0.221776, 0.110224, 0, 0, 0, 0},
+            {-0.04884659515311857, -0.17772065232640102, 0.8465672474795197, 0, 0, 0},
+            {-0.15541685842491548, -0.3567050098221991, 1.0587258798684427, 0.30339598837867193, 0, 0},
+            {0.2014243506726763, 0.008742057842904185, 0.15993995707168115, 0.4038290605220775, 0.22606457389066084, 0},
+            {0.15791629516167136, 0.0, 0.18675894052400077, 0.6805652953093346, -0.27524053099500667, 0.25}};
+        if (step < 5) {
+            for (int k = 0; k <= step; k++) c[k] = R[step][k] * timestep;
+        } else {
+            double a[6];
+            for (int k = 0; k < 5; k++) a[k] = R[4][k] * timestep;
+            a[5] = 0;
+            for (int k = 0; k < 6; k++) c[k] = R[5][k] * timestep - a[k];
+        }
+        for (auto *Xp : {&F.By, &F.Bz, &F.Ey, &F.Ez, &F.Ay, &F.Az}) {
+            auto &X = *Xp;
+            for (int i = 0; i < nf; i++) {
+                if (step < 5) {
+                    double v = X[F.I(i, 0)] + c[0] * X[F.I(i, 2)];
+                    for (int k = 1; k <= step; k++) v = v + c[k] * X[F.I(i, k + 2)];
+                    X[F.I(i, 1)] = v;
+                } else {
+                    double v = X[F.I(i, 1)] + c[0] * X[F.I(i, 2)];
+                    for (int k = 1; k <= 5; k++) v = v + c[k] * X[F.I(i, k + 2)];
+                    X[F.I(i, 0)] = v;
+                    X[F.I(i, 1)] = v;
+                }
+            }
+        }
+        for (int i = 0; i < n; i++) {
+            const double *Ay = &F.Ay[F.I(pre + i, 1)], *Az = &F.Az[F.I(pre + i, 1)];
+            double a_y = face_a(Ay[-2], Ay[-1], Ay[0], Ay[1]);
+            double a_z = face_a(Az[-2], Az[-1], Az[0], Az[1]);
+            F.asq[i] = (a_y * a_y) + (a_z * a_z);
+        }
+    }
+
+    void update_time(int step, double dt) {
+        if (step == 1) time += (0.5 * dt);
+        else if (step == 2) time += (0.332 - 0.5) * dt;
+        else if (step == 3) time += (0.62 - 0.332) * dt;
+        else if (step == 4) time += (0.85 - 0.62) * dt;
+        else if (step == 5) time += (1.0 - 0.85) * dt;
+    }
+
+    void advance(double timestep) {
+        static const double R[6][6] = {
+            {0.5, 0, 0, 0, 0, 0},
+            {0.221776, 0.110224, 0, 0, 0, 0},
+            {-0.04884659515311857, -0.17772065232640102, 0.8465672474795197, 0, 0, 0},
+            {-0.15541685842491548, -0.3567050098221991, 1.0587258798684427, 0.30339598837867193, 0, 0},
+            {0.2014243506726763, 0.008742057842904185, 0.15993995707168115, 0.4038290605220775, 0.22606457389066084, 0},
+            {0.15791629516167136, 0.0, 0.18675894052400077, 0.6805652953093346, -0.27524053099500667, 0.25}};
+        for (int s = 0; s < 6; s++) {
+            assemble();
+            poisson();
+            double a[6] = {0, 0, 0, 0, 0, 0};
+            const int kmax = s;
+            for (int k = 0; k <= kmax; k++) a[k] = R[s][k] * timestep;
+            double asum = a[0];
+            for (int k = 1; k <= kmax; k++) asum = asum + a[k];
+            for (auto &P : patches) {
+                fct_sub0(P, s, a, asum);
+                fct_sub1(P);
+                fct_sub2(P);
+                if (s == 5) P.f[0] = P.f[1];
+            }
+            update_time(s, timestep);
+            maxwell(s, timestep);
+        }
+    }
+
+    double calculate_dt() {
+        const double dps = 1 / pr.GetDp(0);
+        const double dpsMax = std::max(0.0, std::fabs(pr.q) * dps);
+        double pc = 0.0;
+        for (int i = 0; i < F.n; i++) {
+            double Azv = F.Az[i], Ayv = F.Ay[i];
+            double As = Ayv * Ayv + Azv * Azv;
+            double temp = 0.0;
+            temp = std::max(temp, std::fabs(pr.q) / pr.m / std::sqrt(1 + As / ((pr.m * cs) * (pr.m * cs))) * dps);
+            pc = std::max(pc, temp * std::fabs(Ayv * F.Bz[i] - Azv * F.By[i]) + dpsMax * std::fabs(efield(i)));
+        }
+        return P_cfl() * (1.0 / std::max((cs / pr.GetDx(0) + pc), 1e-40));
+    }
+    double P_cfl() const { return pr.P.cfl; }
+
+    // ---------------------------------------------------------------- state files
+    void write_state(const std::string &path, double dt, long long step) {
+        FILE *fp = fopen(path.c_str(), "wb");
+        if (!fp) {
+            perror(path.c_str());
+            exit(2);
+        }
+        auto wi = [&](long long v) { fwrite(&v, 8, 1, fp); };
+        auto wd = [&](double v) { fwrite(&v, 8, 1, fp); };
+        auto wv = [&](const std::vector<double> &v) {
+            wi((long long)v.size());
+            fwrite(v.data(), 8, v.size(), fp);
+        };
+        fwrite("VXST0001", 1, 8, fp);
+        wi(step);
+        wd(time);
+        wd(dt);
+        wd(F.Ex0);
+        wi(F.n);
+        wi(F.pre);
+        wi(F.post);
+        for (auto *v : {&F.By, &F.Bz, &F.Ey, &F.Ez, &F.Ay, &F.Az, &F.asq, &F.phi, &F.charge, &F.J, &F.neut}) wv(*v);
+        wi((long long)patches.size());
+        for (auto &P : patches) {
+            wi(pr.maxDepth + 1);
+            for (int l = 0; l <= pr.maxDepth; l++) {
+                if (l != P.depth) {
+                    wi(0);
+                    continue;
+                }
+                wi(1);
+                for (long long v : {(long long)P.x_pos, (long long)P.p_pos, (long long)P.nx, (long long)P.np,
+                                    (long long)P.depth, (long long)P.up, (long long)P.down, (long long)P.left,
+                                    (long long)P.right})
+                    wi(v);
+                std::vector<double> fv((size_t)3 * (P.nx + 4) * P.W);
+                for (size_t c = 0; c < (size_t)(P.nx + 4) * P.W; c++)
+                    for (int s = 0; s < 3; s++) fv[3 * c + s] = P.f[s][c];
+                wv(fv);
+            }
+        }
+        fclose(fp);
+    }
+
+    void read_state(const std::string &path) {
+        FILE *fp = fopen(path.c_str(), "rb");
+        if (!fp) {
+            perror(path.c_str());
+            exit(2);
+        }
+        auto need = [&](void *p, size_t n) {
+            if (fread(p, 1, n, fp) != n) {
+                fprintf(stderr, "truncated state\n");
+                exit(2);
+            }
+        };
+        auto ri = [&]() {
+            long long v;
+            need(&v, 8);
+            return v;
+        };
+        auto rd = [&]() {
+            double v;
+            need(&v, 8);
+            return v;
+        };
+        auto rv = [&](std::vector<double> &v) {
+            long long n = ri();
+            if ((size_t)n != v.size()) {
+                fprintf(stderr, "state size mismatch\n");
+                exit(2);
+            }
+            need(v.data(), 8 * v.size());
+        };
+        char magic[8];
+        need(magic, 8);
+        ri();
+        time = rd();
+        rd();
+        F.Ex0 = rd();
+        if (ri() != F.n || ri() != F.pre || ri() != F.post) {
+            fprintf(stderr, "grid mismatch\n");
+            exit(2);
+        }
+        for (auto *v : {&F.By, &F.Bz, &F.Ey, &F.Ez, &F.Ay, &F.Az, &F.asq, &F.phi, &F.charge, &F.J, &F.neut}) rv(*v);
+        long long ns = ri();
+        if (ns != (long long)patches.size()) {
+            fprintf(stderr, "species mismatch\n");
+            exit(2);
+        }
+        for (auto &P : patches) {
+            long long nl = ri();
+            for (long long l = 0; l < nl; l++) {
+                long long nr = ri();
+                for (long long k = 0; k < nr; k++) {
+                    long long h[9];
+                    for (auto &x : h) x = ri();
+                    if (h[2] != P.nx || h[3] != P.np || h[0] != 0 || h[1] != 0) {
+                        fprintf(stderr, "the port handles one full-domain patch per species\n");
+                        exit(3);
+                    }
+                    std::vector<double> fv((size_t)3 * (P.nx + 4) * P.W);
+                    rv(fv);
+                    for (size_t c = 0; c < (size_t)(P.nx + 4) * P.W; c++)
+                        for (int s = 0; s < 3; s++) P.f[s][c] = fv[3 * c + s];
+                }
+            }
+        }
+        fclose(fp);
+    }
+};
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    std::map<std::string, std::string> kv;
+    for (int i = 1; i < argc; i++) {
+        std::string a = argv[i];
+        auto eq = a.find('=');
+        if (eq == std::string::npos) {
+            fprintf(stderr, "bad argument %s\n", a.c_str());
+            return 2;
+        }
+        kv[a.substr(0, eq)] = a.substr(eq + 1);
+    }
+    auto getd = [&](const char *k, double d) { return kv.count(k) ? std::stod(kv[k]) : d; };
+    auto geti = [&](const char *k, long long d) { return kv.count(k) ? std::stoll(kv[k]) : d; };
+    Solver S;
+    Params &P = S.pr.P;
+    P.L = getd("L", P.L);
+    P.nx = (unsigned)geti("nx", P.nx);
+    P.np = (unsigned)geti("np", P.np);
+    P.Lfinest = (unsigned)geti("levels", P.Lfinest);
+    P.r = (unsigned)geti("r", P.r);
+    P.pmax = getd("pmax", P.pmax);
+    P.dens = getd("dens", P.dens);
+    P.x1 = getd("x1", P.x1);
+    P.x2 = getd("x2", P.x2);
+    P.x3 = getd("x3", P.x3);
+    P.x4 = getd("x4", P.x4);
+    P.Te = getd("Te", P.Te);
+    P.p0 = getd("p0", P.p0);
+    P.pert_amp = getd("pert_amp", P.pert_amp);
+    P.pert_k = getd("pert_k", P.pert_k);
+    P.a0 = getd("a0", P.a0);
+    P.fwhm = getd("fwhm", P.fwhm);
+    P.delay = getd("delay", P.delay);
+    P.cfl = getd("cfl", P.cfl);
+    P.minEff = getd("minEff", P.minEff);
+    P.crit = getd("crit", P.crit);
+    P.sizeWeight = getd("sizeWeight", P.sizeWeight);
+    P.quadDepth = (int)geti("quadDepth", P.quadDepth);
+    if (P.Lfinest != 1) {
+        fprintf(stderr, "the port restates the single-level step (levels=1)\n");
+        return 3;
+    }
+    long long steps = geti("steps", 0), dump_every = geti("dump_every", 0), time_steps = geti("time_steps", 0);
+    std::string dumpdir = kv.count("dumpdir") ? kv["dumpdir"] : "";
+    std::vector<double> dts;
+    if (kv.count("dts")) {
+        std::stringstream ss(kv["dts"]);
+        std::string tok;
+        while (std::getline(ss, tok, ',')) dts.push_back(std::stod(tok));
+    }
+    S.setup();
+    auto t0 = std::chrono::steady_clock::now();
+    if (kv.count("load")) S.read_state(kv["load"]);
+    else S.init_distribution();
+    auto t1 = std::chrono::steady_clock::now();
+    char name[512];
+    if (!dumpdir.empty()) {
+        snprintf(name, sizeof name, "%s/state_%05lld.bin", dumpdir.c_str(), 0LL);
+        S.write_state(name, 0.0, 0);
+    }
+    for (long long s = 1; s <= steps; s++) {
+        double dt = (s - 1 < (long long)dts.size()) ? dts[s - 1] : S.calculate_dt();
+        S.advance(dt);
+        if (!dumpdir.empty() && dump_every > 0 && s % dump_every == 0) {
+            snprintf(name, sizeof name, "%s/state_%05lld.bin", dumpdir.c_str(), s);
+            S.write_state(name, dt, s);
+        }
+    }
+    if (time_steps > 0) {
+        S.advance(S.calculate_dt());
+        std::vector<double> per;
+        for (long long s = 0; s < time_steps; s++) {
+            double dt = S.calculate_dt();
+            auto a = std::chrono::steady_clock::now();
+            S.advance(dt);
+            auto b = std::chrono::steady_clock::now();
+            per.push_back(std::chrono::duration<double>(b - a).count());
+        }
+        std::sort(per.begin(), per.end());
+        long long cells = 0;
+        for (auto &p : S.patches) cells += (long long)p.nx * p.np;
+        printf("{\"cells\": %lld, \"steps\": %lld, \"best_s\": %.6f, \"median_s\": %.6f, \"threads\": %d, \"init_s\": %.3f}\n",
+               cells, time_steps, per.front(), per[per.size() / 2], omp_get_max_threads(),
+               std::chrono::duration<double>(t1 - t0).count());
+    }
+    return 0;
+}

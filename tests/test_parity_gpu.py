@@ -117,3 +117,32 @@ def test_full_size_conservation_and_fields():
     assert np.abs(st["Bz"]).max() > 0
     s.close()
     c.close()
+
+
+@pytest.mark.gpu
+def test_gpu_matches_port_at_512x128(tmp_path):
+    """Larger than the fixtures: GPU and oracle port from t=0 for 3 steps, own dt."""
+    import subprocess
+    from pathlib import Path
+    from veritas_gb300 import Context, Problem, SolverManager
+
+    root = Path(__file__).resolve().parent.parent
+    port = root / "oracle" / "_port" / "veritas_port"
+    if not port.exists():
+        subprocess.run(["bash", str(root / "oracle" / "port" / "build_port.sh")], check=True)
+    p = Problem(L=40.0, nx=512, np=128, Te=5.0, pmax=1.0, x1=5, x2=8, x3=30, x4=34, pert_amp=0.05, pert_k=4,
+                a0=1.5, fwhm=4, delay=2)
+    subprocess.run([str(port), *p.harness_args(), "steps=3", "dump_every=3", f"dumpdir={tmp_path}"], check=True)
+    ref = vxstate.read_state(tmp_path / "state_00003.bin")
+    c = Context(0)
+    s = SolverManager(c, p)
+    for _ in range(3):
+        s.Advance(s.CalculateDt())
+    s.save_state(tmp_path / "gpu.bin")
+    got = vxstate.read_state(tmp_path / "gpu.bin")
+    err = compare_states(got, ref, TOL)
+    print("512x128 vs port", {k: f"{v:.2e}" for k, v in err.items()})
+    for k, v in err.items():
+        assert v <= TOL, (k, v)
+    s.close()
+    c.close()

@@ -209,7 +209,7 @@ void Run::alloc_fields() {
 
 void Run::upload_lu() {
     cudaStream_t st = eng.stream;
-    dlu_ipiv = upload(lu.ipiv, st);
+    dlu_ipiv = upload(lu.perm, st);
     dlu_lptr = upload(lu.lptr, st);
     dlu_lcol = upload(lu.lcol, st);
     dlu_lval = upload(lu.lval, st);
@@ -218,7 +218,7 @@ void Run::upload_lu() {
     dlu_uval = upload(lu.uval, st);
     dlu_udiag = upload(lu.udiag, st);
     ludev.n = lu.n;
-    ludev.ipiv = dlu_ipiv.as<int>();
+    ludev.perm = dlu_ipiv.as<int>();
     ludev.lptr = dlu_lptr.as<int>();
     ludev.lcol = dlu_lcol.as<int>();
     ludev.lval = dlu_lval.as<double>();
@@ -285,7 +285,7 @@ int64_t Run::state_size() const {
     for (auto &sp : rects)
         for (auto &lvl : sp)
             for (auto &r : lvl) len += (int64_t)r->plane_elems();
-    return len + 6 * (int64_t)nf + (n + 1) + 1;
+    return len + 6 * (int64_t)nf + (n + 1) + n + 1;
 }
 
 // Host-buffer step: H2D of the packed state, one RK step, D2H of the new state.
@@ -307,7 +307,10 @@ void Run::step_host(const double *in, double *out, double dt) {
     }
     VX_CUDA(cudaMemcpyAsync(F.asq, p, (size_t)(n + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
     p += n + 1;
+    VX_CUDA(cudaMemcpyAsync(F.phi, p, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st));
+    p += n;
     VX_CUDA(cudaMemcpyAsync(F.ex0, p, sizeof(double), cudaMemcpyHostToDevice, st));
+    eng.refresh_efield(*this);
     advance(dt);
     state_to_host(out);
 }
@@ -327,6 +330,8 @@ void Run::state_to_host(double *out) {
     }
     VX_CUDA(cudaMemcpyAsync(q, F.asq, (size_t)(n + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
     q += n + 1;
+    VX_CUDA(cudaMemcpyAsync(q, F.phi, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    q += n;
     VX_CUDA(cudaMemcpyAsync(q, F.ex0, sizeof(double), cudaMemcpyDeviceToHost, st));
     eng.sync();
 }
@@ -707,6 +712,13 @@ std::vector<double> Engine::calculate_dt(const std::vector<Run *> &set) {
         dt[i] = s.cfl * bound;
     }
     return dt;
+}
+
+// E_x on the finest grid from the current phi and Ex0 (after a state was loaded).
+void Engine::refresh_efield(Run &run) {
+    LaunchSet &L = get_set({&run});
+    launch_efield(L.dfields.as<RunFields>(), L.dfcoef.as<double>(), 1, L.maxn, stream);
+    kernel_launches += 1;
 }
 
 // Moments and rho/J assembly only (used for EnforceChargeNeutralization).

@@ -128,6 +128,7 @@ public:
     void advance(const std::vector<Run *> &set, const std::vector<double> &dt);
     std::vector<double> calculate_dt(const std::vector<Run *> &set);
     void moments_only(const std::vector<Run *> &set);
+    void refresh_efield(Run &run);
     // Mean device time per launch of each Vlasov kernel (see vx_run_profile_kernels).
     std::vector<double> profile_kernels(Run &run, int reps);
     void timer_begin();

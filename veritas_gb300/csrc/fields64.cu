@@ -169,72 +169,196 @@ __device__ __forceinline__ double efield_at(const double *phi, int n, double fco
 
 // One block per run.  The triangular solves are linear recurrences; to keep the
 // reference's rounding they run in a single thread, in the order of the column-oriented
-// dgetrs.  Entries within four rows of the diagonal come from a register window.
+// dgetrs.  The block stages the factor rows of the next chunk into shared memory while
+// thread 0 consumes the current one, so the sequential thread only ever waits on shared
+// memory; solution entries within four rows of the diagonal come from registers.
+constexpr int kPoisChunk = 256;     // rows per chunk
+constexpr int kPoisMaxNnz = 2048;   // entries per chunk buffer
+
+struct PoisChunk {
+    int ptr[kPoisChunk + 1];
+    int col[kPoisMaxNnz];
+    double val[kPoisMaxNnz];
+};
+
+// Cooperative copy of rows [r0, r0+cnt) of a CSR factor into buffer B (relative ptrs).
+// Returns false when the rows do not fit (the caller then reads global memory).
+__device__ bool pois_stage(PoisChunk &B, const int *ptr, const int *col, const double *val, int r0, int cnt) {
+    const int e0 = ptr[r0], e1 = ptr[r0 + cnt];
+    const bool fits = (e1 - e0) <= kPoisMaxNnz;
+    for (int k = threadIdx.x; k <= cnt; k += blockDim.x) B.ptr[k] = ptr[r0 + k] - e0;
+    if (fits)
+        for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+            B.col[e - e0] = col[e];
+            B.val[e - e0] = val[e];
+        }
+    return fits;
+}
+
+constexpr int kPoisSmemMaxN = 16384;  // solution vector kept in shared memory up to this n
+
 __global__ void k_poisson(PoissonLaunch L) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PoisChunk *buf = (PoisChunk *)smem_raw;  // two chunk buffers, then the solution vector
     const int run = blockIdx.x;
     RunFields &F = L.fields[run];
     const LUDev &lu = L.lu[run];
     const int n = F.n;
-    double *phi = F.phi;
+    const bool in_smem = L.x_in_smem;
+    double *x = in_smem ? (double *)(smem_raw + 2 * sizeof(PoisChunk)) : F.phi;
+    double *tmp = F.efin;  // scratch until E_x is recomputed at the end
     const double te = kEps0Inv;
     const double w = L.w[run];
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double v = te * (F.charge[i] + F.neut[i]);
-        phi[i] = v * w;
+        tmp[i] = v * w;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < n; k++) {
-            int p = lu.ipiv[k];
-            if (p != k) {
-                double t = phi[k];
-                phi[k] = phi[p];
-                phi[p] = t;
-            }
-        }
+    // Row interchanges of dgetrs applied as one gather: b'[k] = b[perm[k]].
+    for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = tmp[lu.perm[k]];
+    __syncthreads();
+    const int nchunks = (n + kPoisChunk - 1) / kPoisChunk;
+    // ---- forward: rows ascending
+    {
         double w1 = 0, w2 = 0, w3 = 0, w4 = 0;
-        for (int i = 0; i < n; i++) {
-            double s = phi[i];
-            for (int e = lu.lptr[i]; e < lu.lptr[i + 1]; e++) {
-                int c = lu.lcol[e];
-                int d = i - c;
-                double xc = d == 1 ? w1 : d == 2 ? w2 : d == 3 ? w3 : d == 4 ? w4 : phi[c];
-                s = s - xc * lu.lval[e];
+        bool fit_cur = pois_stage(buf[0], lu.lptr, lu.lcol, lu.lval, 0, min(kPoisChunk, n));
+        __syncthreads();
+        for (int c = 0; c < nchunks; c++) {
+            const int r0 = c * kPoisChunk, cnt = min(kPoisChunk, n - r0);
+            PoisChunk &B = buf[c & 1];
+            bool fit_next = false;
+            if (c + 1 < nchunks) {
+                const int r1 = r0 + cnt, cnt1 = min(kPoisChunk, n - r1);
+                if (threadIdx.x >= 32) {
+                    // warps 1.. stage the next chunk while thread 0 solves this one
+                    PoisChunk &N = buf[(c + 1) & 1];
+                    const int e0 = lu.lptr[r1], e1 = lu.lptr[r1 + cnt1];
+                    const int t = threadIdx.x - 32, nt = blockDim.x - 32;
+                    fit_next = (e1 - e0) <= kPoisMaxNnz;
+                    for (int k = t; k <= cnt1; k += nt) N.ptr[k] = lu.lptr[r1 + k] - e0;
+                    if (fit_next)
+                        for (int e = e0 + t; e < e1; e += nt) {
+                            N.col[e - e0] = lu.lcol[e];
+                            N.val[e - e0] = lu.lval[e];
+                        }
+                } else {
+                    fit_next = (lu.lptr[r1 + cnt1] - lu.lptr[r1]) <= kPoisMaxNnz;
+                }
             }
-            phi[i] = s;
-            w4 = w3;
-            w3 = w2;
-            w2 = w1;
-            w1 = s;
-        }
-        w1 = w2 = w3 = w4 = 0;
-        for (int i = n - 1; i >= 0; i--) {
-            double s = phi[i];
-            for (int e = lu.uptr[i]; e < lu.uptr[i + 1]; e++) {
-                int c = lu.ucol[e];
-                int d = c - i;
-                double xc = d == 1 ? w1 : d == 2 ? w2 : d == 3 ? w3 : d == 4 ? w4 : phi[c];
-                s = s - xc * lu.uval[e];
+            if (threadIdx.x == 0) {
+                const int gbase = lu.lptr[r0];
+                for (int q = 0; q < cnt; q++) {
+                    const int i = r0 + q;
+                    double s = x[i];
+                    const int a = B.ptr[q], b = B.ptr[q + 1];
+                    for (int e = a; e < b; e++) {
+                        int col = fit_cur ? B.col[e] : lu.lcol[gbase + e];
+                        double v = fit_cur ? B.val[e] : lu.lval[gbase + e];
+                        int d = i - col;
+                        double xc = d == 1 ? w1 : d == 2 ? w2 : d == 3 ? w3 : d == 4 ? w4 : x[col];
+                        s = s - xc * v;
+                    }
+                    x[i] = s;
+                    w4 = w3;
+                    w3 = w2;
+                    w2 = w1;
+                    w1 = s;
+                }
             }
-            s = s / lu.udiag[i];
-            phi[i] = s;
-            w4 = w3;
-            w3 = w2;
-            w2 = w1;
-            w1 = s;
+            fit_cur = fit_next;
+            __syncthreads();
         }
+    }
+    // ---- backward: rows descending (chunk c holds rows [c*kPoisChunk, ...))
+    {
+        double w1 = 0, w2 = 0, w3 = 0, w4 = 0;
+        const int clast = nchunks - 1;
+        const int r0l = clast * kPoisChunk;
+        bool fit_cur = pois_stage(buf[0], lu.uptr, lu.ucol, lu.uval, r0l, n - r0l);
+        __syncthreads();
+        int parity = 0;
+        for (int c = clast; c >= 0; c--) {
+            const int r0 = c * kPoisChunk, cnt = min(kPoisChunk, n - r0);
+            PoisChunk &B = buf[parity];
+            bool fit_next = false;
+            if (c > 0) {
+                const int r1 = (c - 1) * kPoisChunk, cnt1 = kPoisChunk;
+                if (threadIdx.x >= 32) {
+                    PoisChunk &N = buf[parity ^ 1];
+                    const int e0 = lu.uptr[r1], e1 = lu.uptr[r1 + cnt1];
+                    const int t = threadIdx.x - 32, nt = blockDim.x - 32;
+                    fit_next = (e1 - e0) <= kPoisMaxNnz;
+                    for (int k = t; k <= cnt1; k += nt) N.ptr[k] = lu.uptr[r1 + k] - e0;
+                    if (fit_next)
+                        for (int e = e0 + t; e < e1; e += nt) {
+                            N.col[e - e0] = lu.ucol[e];
+                            N.val[e - e0] = lu.uval[e];
+                        }
+                } else {
+                    fit_next = (lu.uptr[r1 + cnt1] - lu.uptr[r1]) <= kPoisMaxNnz;
+                }
+            }
+            if (threadIdx.x == 0) {
+                const int gbase = lu.uptr[r0];
+                for (int q = cnt - 1; q >= 0; q--) {
+                    const int i = r0 + q;
+                    double s = x[i];
+                    const int a = B.ptr[q], b = B.ptr[q + 1];
+                    for (int e = a; e < b; e++) {
+                        int col = fit_cur ? B.col[e] : lu.ucol[gbase + e];
+                        double v = fit_cur ? B.val[e] : lu.uval[gbase + e];
+                        int d = col - i;
+                        double xc = d == 1 ? w1 : d == 2 ? w2 : d == 3 ? w3 : d == 4 ? w4 : x[col];
+                        s = s - xc * v;
+                    }
+                    s = s / lu.udiag[i];
+                    x[i] = s;
+                    w4 = w3;
+                    w3 = w2;
+                    w2 = w1;
+                    w1 = s;
+                }
+            }
+            fit_cur = fit_next;
+            parity ^= 1;
+            __syncthreads();
+        }
+    }
+    if (in_smem)
+        for (int i = threadIdx.x; i < n; i += blockDim.x) F.phi[i] = x[i];
+    if (threadIdx.x == 0) {
         double ex0 = *F.ex0;
-        double e_m1 = efield_at(phi, n, L.fcoef[run], ex0, -1);
-        double e_0 = efield_at(phi, n, L.fcoef[run], ex0, 0);
+        double e_m1 = efield_at(x, n, L.fcoef[run], ex0, -1);
+        double e_0 = efield_at(x, n, L.fcoef[run], ex0, 0);
         *F.ex0 = ex0 + -(e_m1 + e_0) * 0.5;
     }
     __syncthreads();
     const double ex0 = *F.ex0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) F.efin[i] = efield_at(phi, n, L.fcoef[run], ex0, i);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) F.efin[i] = efield_at(x, n, L.fcoef[run], ex0, i);
 }
 
 void launch_poisson(const PoissonLaunch &L) {
-    k_poisson<<<L.nruns, 512, 0, L.stream>>>(L);
+    PoissonLaunch P = L;
+    P.x_in_smem = L.maxn <= kPoisSmemMaxN ? 1 : 0;
+    const int smem = 2 * (int)sizeof(PoisChunk) + (P.x_in_smem ? 8 * L.maxn : 0);
+    cudaFuncSetAttribute(k_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    k_poisson<<<L.nruns, 512, smem, L.stream>>>(P);
+}
+
+// E_x on the finest grid from phi and Ex0 (EMSolver::GetEfield), for states loaded from
+// outside the step.
+__global__ void k_efield(RunFields *fields, const double *fcoef, int nruns) {
+    const int run = blockIdx.y;
+    if (run >= nruns) return;
+    RunFields &F = fields[run];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.n) return;
+    F.efin[i] = efield_at(F.phi, F.n, fcoef[run], *F.ex0, i);
+}
+
+void launch_efield(RunFields *fields, const double *fcoef, int nruns, int maxn, cudaStream_t s) {
+    dim3 g((maxn + 255) / 256, nruns);
+    k_efield<<<g, 256, 0, s>>>(fields, fcoef, nruns);
 }
 
 // ---------------------------------------------------------------- Maxwell

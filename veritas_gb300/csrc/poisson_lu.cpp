@@ -124,6 +124,10 @@ int PoissonLU::build(int N) {
         std::reverse(urow.begin(), urow.end());
         urows[k] = std::move(urow);
     }
+    perm.resize(n);
+    for (int i = 0; i < n; i++) perm[i] = i;
+    for (int k = 0; k < n; k++)
+        if (ipiv[k] != k) std::swap(perm[k], perm[ipiv[k]]);
     lptr.assign(1, 0);
     uptr.assign(1, 0);
     lcol.clear();

@@ -18,6 +18,7 @@ namespace vx {
 struct PoissonLU {
     int n = 0;
     std::vector<int> ipiv;                             // pivot row of step k (0-based)
+    std::vector<int> perm;                             // composed interchanges: b'[k] = b[perm[k]]
     std::vector<int> lptr, lcol, uptr, ucol;           // CSR rows: L ascending, U descending
     std::vector<double> lval, uval, udiag;
     // Factorise the Veritas Poisson matrix of size n (n >= 5).  Returns 0 or k+1 for a

@@ -132,6 +132,7 @@ void Run::load_state(const std::string &path) {
     rects = std::move(nr);
     check_layout_supported();
     layout_version++;
+    eng.refresh_efield(*this);
     eng.sync();
 }
 

@@ -73,7 +73,7 @@ void launch_assemble(const AsmLaunch &A);
 // Poisson solve with precomputed sparse LU factors (EMSolver::UpdatePotential).
 struct LUDev {
     int n;
-    const int *ipiv;
+    const int *perm;  // row interchanges composed into one gather b'[k] = b[perm[k]]
     const int *lptr, *lcol;
     const double *lval;
     const int *uptr, *ucol;
@@ -87,9 +87,11 @@ struct PoissonLaunch {
     const double *fcoef;  // per run: 1/(12 dx0)
     int nruns;
     int maxn;
+    int x_in_smem;  // set by launch_poisson
     cudaStream_t stream;
 };
 void launch_poisson(const PoissonLaunch &L);
+void launch_efield(RunFields *fields, const double *fcoef, int nruns, int maxn, cudaStream_t s);
 
 // Maxwell RK stage + face interpolation of A (EMSolver::RGKStep).
 struct MaxwellLaunch {
