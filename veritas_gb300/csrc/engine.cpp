@@ -14,7 +14,10 @@ void cuda_check(cudaError_t e, const char *what) {
 DevBuf::DevBuf(size_t b) : bytes(b) {
     if (b) {
         VX_CUDA(cudaMalloc(&p, b));
+        // Zero-fill and wait: later uploads run on a non-blocking stream that is not
+        // ordered after work on the legacy default stream.
         VX_CUDA(cudaMemset(p, 0, b));
+        VX_CUDA(cudaDeviceSynchronize());
     }
 }
 DevBuf::~DevBuf() {

@@ -179,6 +179,7 @@ struct PoisChunk {
     int ptr[kPoisChunk + 1];
     int col[kPoisMaxNnz];
     double val[kPoisMaxNnz];
+    double diag[kPoisChunk];  // U diagonal of the chunk's rows (backward pass)
 };
 
 // Cooperative copy of rows [r0, r0+cnt) of a CSR factor into buffer B (relative ptrs).
@@ -196,6 +197,41 @@ __device__ bool pois_stage(PoisChunk &B, const int *ptr, const int *col, const d
 }
 
 constexpr int kPoisSmemMaxN = 16384;  // solution vector kept in shared memory up to this n
+
+// Sequential substitution over the rows of one staged chunk.  FROM_SMEM selects where
+// the factor entries are read (a uniform branch per chunk, so the compiler never issues
+// both loads).  Window registers hold the four most recent solution values.
+template <bool FORWARD, bool FROM_SMEM>
+__device__ __forceinline__ void pois_rows(const PoisChunk &B, const int *gcol, const double *gval, int gbase, int r0,
+                                          int cnt, double *x, const double *udiag, double &w1, double &w2, double &w3,
+                                          double &w4) {
+    for (int qq = 0; qq < cnt; qq++) {
+        const int q = FORWARD ? qq : cnt - 1 - qq;
+        const int i = r0 + q;
+        double s = x[i];
+        const int a = B.ptr[q], b = B.ptr[q + 1];
+        for (int e = a; e < b; e++) {
+            int col;
+            double v;
+            if (FROM_SMEM) {
+                col = B.col[e];
+                v = B.val[e];
+            } else {
+                col = gcol[gbase + e];
+                v = gval[gbase + e];
+            }
+            int d = FORWARD ? i - col : col - i;
+            double xc = d == 1 ? w1 : d == 2 ? w2 : d == 3 ? w3 : d == 4 ? w4 : x[col];
+            s = s - xc * v;
+        }
+        if (!FORWARD) s = s / B.diag[q];
+        x[i] = s;
+        w4 = w3;
+        w3 = w2;
+        w2 = w1;
+        w1 = s;
+    }
+}
 
 __global__ void k_poisson(PoissonLaunch L) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -247,23 +283,8 @@ __global__ void k_poisson(PoissonLaunch L) {
             }
             if (threadIdx.x == 0) {
                 const int gbase = lu.lptr[r0];
-                for (int q = 0; q < cnt; q++) {
-                    const int i = r0 + q;
-                    double s = x[i];
-                    const int a = B.ptr[q], b = B.ptr[q + 1];
-                    for (int e = a; e < b; e++) {
-                        int col = fit_cur ? B.col[e] : lu.lcol[gbase + e];
-                        double v = fit_cur ? B.val[e] : lu.lval[gbase + e];
-                        int d = i - col;
-                        double xc = d == 1 ? w1 : d == 2 ? w2 : d == 3 ? w3 : d == 4 ? w4 : x[col];
-                        s = s - xc * v;
-                    }
-                    x[i] = s;
-                    w4 = w3;
-                    w3 = w2;
-                    w2 = w1;
-                    w1 = s;
-                }
+                if (fit_cur) pois_rows<true, true>(B, lu.lcol, lu.lval, gbase, r0, cnt, x, nullptr, w1, w2, w3, w4);
+                else pois_rows<true, false>(B, lu.lcol, lu.lval, gbase, r0, cnt, x, nullptr, w1, w2, w3, w4);
             }
             fit_cur = fit_next;
             __syncthreads();
@@ -275,6 +296,7 @@ __global__ void k_poisson(PoissonLaunch L) {
         const int clast = nchunks - 1;
         const int r0l = clast * kPoisChunk;
         bool fit_cur = pois_stage(buf[0], lu.uptr, lu.ucol, lu.uval, r0l, n - r0l);
+        for (int k = threadIdx.x; k < n - r0l; k += blockDim.x) buf[0].diag[k] = lu.udiag[r0l + k];
         __syncthreads();
         int parity = 0;
         for (int c = clast; c >= 0; c--) {
@@ -289,6 +311,7 @@ __global__ void k_poisson(PoissonLaunch L) {
                     const int t = threadIdx.x - 32, nt = blockDim.x - 32;
                     fit_next = (e1 - e0) <= kPoisMaxNnz;
                     for (int k = t; k <= cnt1; k += nt) N.ptr[k] = lu.uptr[r1 + k] - e0;
+                    for (int k = t; k < cnt1; k += nt) N.diag[k] = lu.udiag[r1 + k];
                     if (fit_next)
                         for (int e = e0 + t; e < e1; e += nt) {
                             N.col[e - e0] = lu.ucol[e];
@@ -300,24 +323,8 @@ __global__ void k_poisson(PoissonLaunch L) {
             }
             if (threadIdx.x == 0) {
                 const int gbase = lu.uptr[r0];
-                for (int q = cnt - 1; q >= 0; q--) {
-                    const int i = r0 + q;
-                    double s = x[i];
-                    const int a = B.ptr[q], b = B.ptr[q + 1];
-                    for (int e = a; e < b; e++) {
-                        int col = fit_cur ? B.col[e] : lu.ucol[gbase + e];
-                        double v = fit_cur ? B.val[e] : lu.uval[gbase + e];
-                        int d = col - i;
-                        double xc = d == 1 ? w1 : d == 2 ? w2 : d == 3 ? w3 : d == 4 ? w4 : x[col];
-                        s = s - xc * v;
-                    }
-                    s = s / lu.udiag[i];
-                    x[i] = s;
-                    w4 = w3;
-                    w3 = w2;
-                    w2 = w1;
-                    w1 = s;
-                }
+                if (fit_cur) pois_rows<false, true>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, lu.udiag, w1, w2, w3, w4);
+                else pois_rows<false, false>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, lu.udiag, w1, w2, w3, w4);
             }
             fit_cur = fit_next;
             parity ^= 1;
