@@ -220,6 +220,7 @@ void Run::upload_lu() {
     dlu_ucol = upload(lu.ucol, st);
     dlu_uval = upload(lu.uval, st);
     dlu_udiag = upload(lu.udiag, st);
+    dlu_urdiag = upload(lu.urdiag, st);
     ludev.n = lu.n;
     ludev.perm = dlu_ipiv.as<int>();
     ludev.lptr = dlu_lptr.as<int>();
@@ -229,6 +230,7 @@ void Run::upload_lu() {
     ludev.ucol = dlu_ucol.as<int>();
     ludev.uval = dlu_uval.as<double>();
     ludev.udiag = dlu_udiag.as<double>();
+    ludev.urdiag = dlu_urdiag.as<double>();
 }
 
 // SolverManager::SolverManager (SolverManager.cpp:8-26) for a hierarchy that starts and

@@ -49,66 +49,76 @@ __device__ __forceinline__ double cell_asq(const RunFields &F, int x) {
     return (ay * ay) + (az * az);
 }
 
-// Log-ratio table L(j) = c2 * ln((g_{j+1} + c1 p_{j+1}) / (g_j + c1 p_j)) for j in
-// [-1, n_p] of every moment column; gm, gm1, gp1 of the reference are L(j), L(j-1),
-// L(j+1) (identical expressions evaluated at neighbouring j).
-__global__ void k64_mom_L(MomLaunch M) {
-    const int col = blockIdx.y * blockDim.y + threadIdx.y;
-    const int jj = blockIdx.x * blockDim.x + threadIdx.x;  // j + 1
-    if (col >= M.ncols) return;
-    const P64 &P = ((const P64 *)M.patches)[M.colpatch[col]];
-    if (jj > P.np + 1) return;
-    const int j = jj - 1;
-    const int c = M.colidx[col];
+// One warp per moment column (coarse column i, finest sub-column k).  The warp walks p
+// in windows of 32 lanes covering j0-1 .. j0+30: every lane computes the Lorentz factor
+// at its p-face once (shared with the neighbouring face through shuffles instead of the
+// reference's four Gamma calls per cell), the log ratio
+//   L(j) = c2 * ln((g_{j+1} + c1 p_{j+1}) / (g_j + c1 p_j))
+// (the reference's gm; gm1 and gp1 are L(j-1) and L(j+1), the same expressions), the
+// interpolated f and the cell's charge/current contributions.  Lane 0 then adds the 29
+// contributions of the window in ascending j, which keeps the reference's accumulation
+// order (Rectangle.cpp:207-255) exactly.
+constexpr int kMomOut = 29;  // outputs per window: j0 .. j0+28
+
+__global__ void k64_moments(MomLaunch M) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= M.ncols) return;
+    const P64 &P = ((const P64 *)M.patches)[M.colpatch[warp]];
+    const int c = M.colidx[warp];
     const int i = c / P.rtb, k = c - i * P.rtb;
     const RunFields &F = M.fields[P.run];
     const double a = P.qq * cell_asq(F, (i + P.x_pos) * P.rtb + k);
     const double minv = 1 / P.mass;
     const double c1 = minv * kCInv;
     const double c2 = 1 / c1;
-    double p0 = P.pmin + P.dp * (double)(j + P.p_pos);
-    double p1 = P.pmin + P.dp * (double)(j + 1 + P.p_pos);
-    double g0 = sqrt(1.0 + ((p0 * p0) + a) * P.g2);
-    double g1 = sqrt(1.0 + ((p1 * p1) + a) * P.g2);
-    M.Lbuf[(size_t)col * (M.maxnp + 2) + jj] = c2 * log((g1 + c1 * p1) / (g0 + c1 * p0));
-}
-
-// Ordered accumulation over p of charge and current per moment column, in the exact
-// j order of the reference loop, skipping nested cells.
-__global__ void k64_mom_acc(MomLaunch M) {
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= M.ncols) return;
-    const P64 &P = ((const P64 *)M.patches)[M.colpatch[col]];
-    const int c = M.colidx[col];
-    const int i = c / P.rtb, k = c - i * P.rtb;
-    const double *L = M.Lbuf + (size_t)col * (M.maxnp + 2) + 1;  // L[j], j >= -1
-    const double *f = P.f1;
     const double c3 = 1 / 48.0;
-    double vm1 = rel_value(P, f, i, -1, k);
-    double v0 = rel_value(P, f, i, 0, k);
-    double vp1 = rel_value(P, f, i, 1, k);
+    const double *f = P.f1;
+    const unsigned full = 0xffffffffu;
     double ch = 0.0, cu = 0.0;
-    for (int j = 0; j < P.np; j++) {
-        if (!(P.nested && P.nested[pidx(i, j, P.pitch)])) {
-            ch += v0;
-            double gm = L[j], gm1 = L[j - 1], gp1 = L[j + 1];
-            cu += v0 * gm + c3 * (gp1 - gm1) * (vp1 - vm1);
+    for (int j0 = 0; j0 < P.np; j0 += kMomOut) {
+        const int j = j0 - 1 + lane;  // this lane's p index
+        double G = 0.0, V = 0.0;
+        if (j <= P.np + 1) {
+            double p = P.pmin + P.dp * (double)(j + P.p_pos);
+            double g = sqrt(1.0 + ((p * p) + a) * P.g2);
+            G = g + c1 * p;
         }
-        vm1 = v0;
-        v0 = vp1;
-        vp1 = rel_value(P, f, i, j + 2, k);
+        if (j <= P.np) V = rel_value(P, f, i, j, k);
+        const double Gn = __shfl_down_sync(full, G, 1);
+        const double L = c2 * log(Gn / G);  // valid for lanes 0..30
+        const double Lm = __shfl_up_sync(full, L, 1);
+        const double Lp = __shfl_down_sync(full, L, 1);
+        const double Vm = __shfl_up_sync(full, V, 1);
+        const double Vp = __shfl_down_sync(full, V, 1);
+        double cc = 0.0, cj = 0.0;
+        bool use = lane >= 1 && lane <= kMomOut && j < P.np && !(P.nested && P.nested[pidx(i, j, P.pitch)]);
+        if (use) {
+            cc = V;
+            cj = V * L + c3 * (Lp - Lm) * (Vp - Vm);
+        }
+        const unsigned usemask = __ballot_sync(full, use);
+        for (int t = 1; t <= kMomOut; t++) {
+            const double vc = __shfl_sync(full, cc, t);
+            const double vj = __shfl_sync(full, cj, t);
+            if ((usemask >> t) & 1u) {
+                ch += vc;
+                cu += vj;
+            }
+        }
     }
-    const double q = P.q;
-    P.chargeR[c] = ch * (P.dp * q);
-    P.currentR[c] = cu * (-q * q / P.mass);
+    if (lane == 0) {
+        const double q = P.q;
+        P.chargeR[c] = ch * (P.dp * q);
+        P.currentR[c] = cu * (-q * q / P.mass);
+    }
 }
 
 void launch_moments64(const MomLaunch &M) {
     if (M.ncols == 0) return;
-    dim3 b1(64, 4);
-    dim3 g1((M.maxnp + 2 + 63) / 64, (M.ncols + 3) / 4);
-    k64_mom_L<<<g1, b1, 0, M.stream>>>(M);
-    k64_mom_acc<<<(M.ncols + 127) / 128, 128, 0, M.stream>>>(M);
+    const int threads = 256;
+    const int blocks = (M.ncols * 32 + threads - 1) / threads;
+    k64_moments<<<blocks, threads, 0, M.stream>>>(M);
 }
 
 // ---------------------------------------------------------------- assembly
@@ -179,7 +189,9 @@ struct PoisChunk {
     int ptr[kPoisChunk + 1];
     int col[kPoisMaxNnz];
     double val[kPoisMaxNnz];
-    double diag[kPoisChunk];  // U diagonal of the chunk's rows (backward pass)
+    double diag[kPoisChunk];   // U diagonal of the chunk's rows (backward pass)
+    double rdiag[kPoisChunk];  // RN(1/u_ii)
+    double xin[kPoisChunk];    // right-hand sides of the chunk (to redo it exactly)
 };
 
 // Cooperative copy of rows [r0, r0+cnt) of a CSR factor into buffer B (relative ptrs).
@@ -201,10 +213,18 @@ constexpr int kPoisSmemMaxN = 16384;  // solution vector kept in shared memory u
 // Sequential substitution over the rows of one staged chunk.  FROM_SMEM selects where
 // the factor entries are read (a uniform branch per chunk, so the compiler never issues
 // both loads).  Window registers hold the four most recent solution values.
+//
+// Backward rows divide by the pivot u_ii.  An IEEE division costs ~550 cycles of
+// dependent FP64 latency on this part, so the chain uses Markstein's sequence with the
+// correctly rounded reciprocal y_i = RN(1/u_ii) from the host (q = s*y, r = s - q*u
+// exact by FMA, q' = q + r*y), and the true IEEE quotient s/u_ii is computed beside it,
+// off the critical path.  If any row of the chunk disagrees, the chunk is recomputed with
+// the IEEE quotients, so the result is always the column-oriented dgetrs rounding.
 template <bool FORWARD, bool FROM_SMEM>
-__device__ __forceinline__ void pois_rows(const PoisChunk &B, const int *gcol, const double *gval, int gbase, int r0,
-                                          int cnt, double *x, const double *udiag, double &w1, double &w2, double &w3,
-                                          double &w4) {
+__device__ __forceinline__ bool pois_rows(const PoisChunk &B, const int *gcol, const double *gval, int gbase, int r0,
+                                          int cnt, double *x, double &w1, double &w2, double &w3, double &w4,
+                                          bool exact_div) {
+    bool ok = true;
     for (int qq = 0; qq < cnt; qq++) {
         const int q = FORWARD ? qq : cnt - 1 - qq;
         const int i = r0 + q;
@@ -224,13 +244,26 @@ __device__ __forceinline__ void pois_rows(const PoisChunk &B, const int *gcol, c
             double xc = d == 1 ? w1 : d == 2 ? w2 : d == 3 ? w3 : d == 4 ? w4 : x[col];
             s = s - xc * v;
         }
-        if (!FORWARD) s = s / B.diag[q];
+        if (!FORWARD) {
+            const double u = B.diag[q], y = B.rdiag[q];
+            const double ieee = s / u;
+            if (exact_div) {
+                s = ieee;
+            } else {
+                double q0 = __dmul_rn(s, y);
+                double r = __fma_rn(-q0, u, s);
+                double q1 = __fma_rn(r, y, q0);
+                ok = ok && (__double_as_longlong(q1) == __double_as_longlong(ieee));
+                s = q1;
+            }
+        }
         x[i] = s;
         w4 = w3;
         w3 = w2;
         w2 = w1;
         w1 = s;
     }
+    return ok;
 }
 
 __global__ void k_poisson(PoissonLaunch L) {
@@ -283,8 +316,8 @@ __global__ void k_poisson(PoissonLaunch L) {
             }
             if (threadIdx.x == 0) {
                 const int gbase = lu.lptr[r0];
-                if (fit_cur) pois_rows<true, true>(B, lu.lcol, lu.lval, gbase, r0, cnt, x, nullptr, w1, w2, w3, w4);
-                else pois_rows<true, false>(B, lu.lcol, lu.lval, gbase, r0, cnt, x, nullptr, w1, w2, w3, w4);
+                if (fit_cur) pois_rows<true, true>(B, lu.lcol, lu.lval, gbase, r0, cnt, x, w1, w2, w3, w4, true);
+                else pois_rows<true, false>(B, lu.lcol, lu.lval, gbase, r0, cnt, x, w1, w2, w3, w4, true);
             }
             fit_cur = fit_next;
             __syncthreads();
@@ -296,7 +329,10 @@ __global__ void k_poisson(PoissonLaunch L) {
         const int clast = nchunks - 1;
         const int r0l = clast * kPoisChunk;
         bool fit_cur = pois_stage(buf[0], lu.uptr, lu.ucol, lu.uval, r0l, n - r0l);
-        for (int k = threadIdx.x; k < n - r0l; k += blockDim.x) buf[0].diag[k] = lu.udiag[r0l + k];
+        for (int k = threadIdx.x; k < n - r0l; k += blockDim.x) {
+            buf[0].diag[k] = lu.udiag[r0l + k];
+            buf[0].rdiag[k] = lu.urdiag[r0l + k];
+        }
         __syncthreads();
         int parity = 0;
         for (int c = clast; c >= 0; c--) {
@@ -311,7 +347,10 @@ __global__ void k_poisson(PoissonLaunch L) {
                     const int t = threadIdx.x - 32, nt = blockDim.x - 32;
                     fit_next = (e1 - e0) <= kPoisMaxNnz;
                     for (int k = t; k <= cnt1; k += nt) N.ptr[k] = lu.uptr[r1 + k] - e0;
-                    for (int k = t; k < cnt1; k += nt) N.diag[k] = lu.udiag[r1 + k];
+                    for (int k = t; k < cnt1; k += nt) {
+                        N.diag[k] = lu.udiag[r1 + k];
+                        N.rdiag[k] = lu.urdiag[r1 + k];
+                    }
                     if (fit_next)
                         for (int e = e0 + t; e < e1; e += nt) {
                             N.col[e - e0] = lu.ucol[e];
@@ -323,8 +362,18 @@ __global__ void k_poisson(PoissonLaunch L) {
             }
             if (threadIdx.x == 0) {
                 const int gbase = lu.uptr[r0];
-                if (fit_cur) pois_rows<false, true>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, lu.udiag, w1, w2, w3, w4);
-                else pois_rows<false, false>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, lu.udiag, w1, w2, w3, w4);
+                double *xin = B.xin;
+                for (int q = 0; q < cnt; q++) xin[q] = x[r0 + q];
+                // keep the chunk's inputs and window so that a mismatch can be redone exactly
+                const double s1 = w1, s2 = w2, s3 = w3, s4 = w4;
+                bool ok = fit_cur ? pois_rows<false, true>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, w1, w2, w3, w4, false)
+                                  : pois_rows<false, false>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, w1, w2, w3, w4, false);
+                if (!ok) {
+                    for (int q = 0; q < cnt; q++) x[r0 + q] = xin[q];
+                    w1 = s1, w2 = s2, w3 = s3, w4 = s4;
+                    if (fit_cur) pois_rows<false, true>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, w1, w2, w3, w4, true);
+                    else pois_rows<false, false>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, w1, w2, w3, w4, true);
+                }
             }
             fit_cur = fit_next;
             parity ^= 1;

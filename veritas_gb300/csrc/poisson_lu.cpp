@@ -124,6 +124,8 @@ int PoissonLU::build(int N) {
         std::reverse(urow.begin(), urow.end());
         urows[k] = std::move(urow);
     }
+    urdiag.resize(n);
+    for (int i = 0; i < n; i++) urdiag[i] = 1.0 / udiag[i];
     perm.resize(n);
     for (int i = 0; i < n; i++) perm[i] = i;
     for (int k = 0; k < n; k++)

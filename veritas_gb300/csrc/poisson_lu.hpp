@@ -20,7 +20,7 @@ struct PoissonLU {
     std::vector<int> ipiv;                             // pivot row of step k (0-based)
     std::vector<int> perm;                             // composed interchanges: b'[k] = b[perm[k]]
     std::vector<int> lptr, lcol, uptr, ucol;           // CSR rows: L ascending, U descending
-    std::vector<double> lval, uval, udiag;
+    std::vector<double> lval, uval, udiag, urdiag;  // urdiag = RN(1/u_ii)
     // Factorise the Veritas Poisson matrix of size n (n >= 5).  Returns 0 or k+1 for a
     // zero pivot at step k.
     int build(int n);

@@ -79,6 +79,7 @@ struct LUDev {
     const int *uptr, *ucol;
     const double *uval;
     const double *udiag;
+    const double *urdiag;  // RN(1/u_ii), computed on the host
 };
 struct PoissonLaunch {
     const LUDev *lu;      // per run
