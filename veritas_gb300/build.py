@@ -64,7 +64,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         for f in futs:
             f.result()
     tmp = LIB.with_suffix(".so.tmp")
-    _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for _, o in jobs], "-lcudart", "-lpthread"])
+    _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for _, o in jobs], "-lcudart", "-lpthread",
+          "-Xlinker", "--no-undefined"])
     os.replace(tmp, LIB)
     if verbose:
         print(f"built {LIB}")

@@ -212,25 +212,26 @@ void Run::alloc_fields() {
 
 void Run::upload_lu() {
     cudaStream_t st = eng.stream;
-    dlu_ipiv = upload(lu.perm, st);
-    dlu_lptr = upload(lu.lptr, st);
-    dlu_lcol = upload(lu.lcol, st);
-    dlu_lval = upload(lu.lval, st);
-    dlu_uptr = upload(lu.uptr, st);
-    dlu_ucol = upload(lu.ucol, st);
-    dlu_uval = upload(lu.uval, st);
-    dlu_udiag = upload(lu.udiag, st);
-    dlu_urdiag = upload(lu.urdiag, st);
+    auto Lb = lu.lower_band();
+    auto Ub = lu.upper_band();
+    dlu_perm = upload(lu.perm, st);
+    dlb_band = upload(Lb.band, st);
+    dlb_fptr = upload(Lb.fptr, st);
+    dlb_fcol = upload(Lb.fcol, st);
+    dlb_fval = upload(Lb.fval, st);
+    dub_band = upload(Ub.band, st);
+    dub_diag = upload(Ub.diag, st);
+    dub_rdiag = upload(Ub.rdiag, st);
+    dub_fptr = upload(Ub.fptr, st);
+    dub_fcol = upload(Ub.fcol, st);
+    dub_fval = upload(Ub.fval, st);
+    eng.sync();
     ludev.n = lu.n;
-    ludev.perm = dlu_ipiv.as<int>();
-    ludev.lptr = dlu_lptr.as<int>();
-    ludev.lcol = dlu_lcol.as<int>();
-    ludev.lval = dlu_lval.as<double>();
-    ludev.uptr = dlu_uptr.as<int>();
-    ludev.ucol = dlu_ucol.as<int>();
-    ludev.uval = dlu_uval.as<double>();
-    ludev.udiag = dlu_udiag.as<double>();
-    ludev.urdiag = dlu_urdiag.as<double>();
+    ludev.perm = dlu_perm.as<int>();
+    ludev.L = BandFactor{dlb_band.as<double>(), nullptr, nullptr, dlb_fptr.as<int>(), dlb_fcol.as<int>(),
+                         dlb_fval.as<double>()};
+    ludev.U = BandFactor{dub_band.as<double>(), dub_diag.as<double>(), dub_rdiag.as<double>(), dub_fptr.as<int>(),
+                         dub_fcol.as<int>(), dub_fval.as<double>()};
 }
 
 // SolverManager::SolverManager (SolverManager.cpp:8-26) for a hierarchy that starts and

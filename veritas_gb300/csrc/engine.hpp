@@ -73,7 +73,8 @@ public:
     DevBuf dBy, dBz, dEy, dEz, dAy, dAz, dasq, dphi, dcharge, dJ, dneut, defin, dex0;
     RunFields F{};
     PoissonLU lu;
-    DevBuf dlu_ipiv, dlu_lptr, dlu_lcol, dlu_lval, dlu_uptr, dlu_ucol, dlu_uval, dlu_udiag, dlu_urdiag;
+    DevBuf dlu_perm, dlb_band, dlb_fptr, dlb_fcol, dlb_fval, dub_band, dub_diag, dub_rdiag, dub_fptr, dub_fcol,
+        dub_fval;
     LUDev ludev{};
     uint64_t layout_version = 0;
     int id = 0;

@@ -178,103 +178,132 @@ __device__ __forceinline__ double efield_at(const double *phi, int n, double fco
 }
 
 // One block per run.  The triangular solves are linear recurrences; to keep the
-// reference's rounding they run in a single thread, in the order of the column-oriented
-// dgetrs.  The block stages the factor rows of the next chunk into shared memory while
-// thread 0 consumes the current one, so the sequential thread only ever waits on shared
-// memory; solution entries within four rows of the diagonal come from registers.
-constexpr int kPoisChunk = 256;     // rows per chunk
-constexpr int kPoisMaxNnz = 2048;   // entries per chunk buffer
+// reference's rounding they run in one thread in the order of the column-oriented
+// dgetrs (entries ascending in column for L, descending for U).  FP64 dependent latency
+// (~64 cycles per add/mul, ~550 per IEEE division on this part) makes the chain length
+// the cost, so the factors are stored in band form: four coefficients per row for the
+// columns next to the diagonal (exact zeros where the factor has none — subtracting a
+// zero product never changes a partial sum, which is never -0 here) plus a short list of
+// "far" entries that precede the band in the summation order.  Only the product with the
+// previous row's value sits on the critical path.  Back substitution divides with
+// Markstein's sequence (q = s*y, r = s - q*u exactly, q' = q + r*y with y = RN(1/u));
+// after each chunk the whole block checks every quotient against the IEEE quotient and
+// the chunk is redone with IEEE division if any differs, so the result is always the
+// dgetrs rounding.
+constexpr int kPoisRows = 256;   // rows per staged chunk
+constexpr int kPoisFar = 2048;   // far entries per staged chunk
 
-struct PoisChunk {
-    int ptr[kPoisChunk + 1];
-    int col[kPoisMaxNnz];
-    double val[kPoisMaxNnz];
-    double diag[kPoisChunk];   // U diagonal of the chunk's rows (backward pass)
-    double rdiag[kPoisChunk];  // RN(1/u_ii)
-    double xin[kPoisChunk];    // right-hand sides of the chunk (to redo it exactly)
+struct PoisBandChunk {
+    double c1[kPoisRows], c2[kPoisRows], c3[kPoisRows], c4[kPoisRows];  // band coefficients
+    double diag[kPoisRows], rdiag[kPoisRows], num[kPoisRows];           // U only
+    double rhs[kPoisRows];  // right-hand sides of a backward chunk, kept for an exact redo
+    int fptr[kPoisRows + 1];
+    int fcol[kPoisFar];
+    double fval[kPoisFar];
 };
 
-// Cooperative copy of rows [r0, r0+cnt) of a CSR factor into buffer B (relative ptrs).
-// Returns false when the rows do not fit (the caller then reads global memory).
-__device__ bool pois_stage(PoisChunk &B, const int *ptr, const int *col, const double *val, int r0, int cnt) {
-    const int e0 = ptr[r0], e1 = ptr[r0 + cnt];
-    const bool fits = (e1 - e0) <= kPoisMaxNnz;
-    for (int k = threadIdx.x; k <= cnt; k += blockDim.x) B.ptr[k] = ptr[r0 + k] - e0;
-    if (fits)
-        for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-            B.col[e - e0] = col[e];
-            B.val[e - e0] = val[e];
+// Stage rows [r0, r0+cnt) of a band factor into B with threads [t0, t0+nt).
+__device__ bool pois_stage_band(PoisBandChunk &B, const BandFactor &F, int r0, int cnt, int t0, int nt, bool upper) {
+    const int f0 = F.fptr[r0], f1 = F.fptr[r0 + cnt];
+    const bool fits = (f1 - f0) <= kPoisFar;
+    for (int k = (int)threadIdx.x - t0; k < cnt; k += nt) {
+        if (k < 0) continue;
+        const int r = r0 + k;
+        B.c1[k] = F.band[4 * r];
+        B.c2[k] = F.band[4 * r + 1];
+        B.c3[k] = F.band[4 * r + 2];
+        B.c4[k] = F.band[4 * r + 3];
+        if (upper) {
+            B.diag[k] = F.diag[r];
+            B.rdiag[k] = F.rdiag[r];
         }
+    }
+    for (int k = (int)threadIdx.x - t0; k <= cnt; k += nt)
+        if (k >= 0) B.fptr[k] = F.fptr[r0 + k] - f0;
+    if (fits)
+        for (int e = f0 + (int)threadIdx.x - t0; e < f1; e += nt)
+            if (e >= f0) {
+                B.fcol[e - f0] = F.fcol[e];
+                B.fval[e - f0] = F.fval[e];
+            }
     return fits;
 }
 
-constexpr int kPoisSmemMaxN = 16384;  // solution vector kept in shared memory up to this n
-
-// Sequential substitution over the rows of one staged chunk.  FROM_SMEM selects where
-// the factor entries are read (a uniform branch per chunk, so the compiler never issues
-// both loads).  Window registers hold the four most recent solution values.
-//
-// Backward rows divide by the pivot u_ii.  An IEEE division costs ~550 cycles of
-// dependent FP64 latency on this part, so the chain uses Markstein's sequence with the
-// correctly rounded reciprocal y_i = RN(1/u_ii) from the host (q = s*y, r = s - q*u
-// exact by FMA, q' = q + r*y), and the true IEEE quotient s/u_ii is computed beside it,
-// off the critical path.  If any row of the chunk disagrees, the chunk is recomputed with
-// the IEEE quotients, so the result is always the column-oriented dgetrs rounding.
-template <bool FORWARD, bool FROM_SMEM>
-__device__ __forceinline__ bool pois_rows(const PoisChunk &B, const int *gcol, const double *gval, int gbase, int r0,
-                                          int cnt, double *x, double &w1, double &w2, double &w3, double &w4,
-                                          bool exact_div) {
-    bool ok = true;
-    for (int qq = 0; qq < cnt; qq++) {
-        const int q = FORWARD ? qq : cnt - 1 - qq;
+// Forward rows of one chunk: x_i = b_i - sum (far, ascending) - x_{i-4}c4 - x_{i-3}c3
+// - x_{i-2}c2 - x_{i-1}c1.
+template <bool FAR_SMEM>
+__device__ __forceinline__ void pois_fwd(const PoisBandChunk &B, const BandFactor &F, int gbase, int r0, int cnt,
+                                         double *x, double &w1, double &w2, double &w3, double &w4) {
+#pragma unroll 2
+    for (int q = 0; q < cnt; q++) {
         const int i = r0 + q;
         double s = x[i];
-        const int a = B.ptr[q], b = B.ptr[q + 1];
-        for (int e = a; e < b; e++) {
-            int col;
-            double v;
-            if (FROM_SMEM) {
-                col = B.col[e];
-                v = B.val[e];
-            } else {
-                col = gcol[gbase + e];
-                v = gval[gbase + e];
-            }
-            int d = FORWARD ? i - col : col - i;
-            double xc = d == 1 ? w1 : d == 2 ? w2 : d == 3 ? w3 : d == 4 ? w4 : x[col];
-            s = s - xc * v;
+        for (int e = B.fptr[q]; e < B.fptr[q + 1]; e++) {
+            const int col = FAR_SMEM ? B.fcol[e] : F.fcol[gbase + e];
+            const double v = FAR_SMEM ? B.fval[e] : F.fval[gbase + e];
+            s = s - x[col] * v;
         }
-        if (!FORWARD) {
-            const double u = B.diag[q], y = B.rdiag[q];
-            const double ieee = s / u;
-            if (exact_div) {
-                s = ieee;
-            } else {
-                double q0 = __dmul_rn(s, y);
-                double r = __fma_rn(-q0, u, s);
-                double q1 = __fma_rn(r, y, q0);
-                ok = ok && (__double_as_longlong(q1) == __double_as_longlong(ieee));
-                s = q1;
-            }
-        }
+        s = s - w4 * B.c4[q];
+        s = s - w3 * B.c3[q];
+        s = s - w2 * B.c2[q];
+        s = s - w1 * B.c1[q];
         x[i] = s;
         w4 = w3;
         w3 = w2;
         w2 = w1;
         w1 = s;
     }
-    return ok;
 }
+
+// Backward rows of one chunk (descending): numerator as above with the far entries
+// (descending columns) first, then x_{i+4} .. x_{i+1}; quotient by Markstein or IEEE.
+template <bool FAR_SMEM, bool IEEE>
+__device__ __forceinline__ void pois_bwd(PoisBandChunk &B, const BandFactor &F, int gbase, int r0, int cnt,
+                                         double *x, double &w1, double &w2, double &w3, double &w4) {
+#pragma unroll 2
+    for (int qq = 0; qq < cnt; qq++) {
+        const int q = cnt - 1 - qq;
+        const int i = r0 + q;
+        double s = x[i];
+        for (int e = B.fptr[q]; e < B.fptr[q + 1]; e++) {
+            const int col = FAR_SMEM ? B.fcol[e] : F.fcol[gbase + e];
+            const double v = FAR_SMEM ? B.fval[e] : F.fval[gbase + e];
+            s = s - x[col] * v;
+        }
+        s = s - w4 * B.c4[q];
+        s = s - w3 * B.c3[q];
+        s = s - w2 * B.c2[q];
+        s = s - w1 * B.c1[q];
+        double out;
+        if (IEEE) {
+            out = s / B.diag[q];
+        } else {
+            B.num[q] = s;
+            const double y = B.rdiag[q];
+            const double q0 = __dmul_rn(s, y);
+            const double r = __fma_rn(-q0, B.diag[q], s);
+            out = __fma_rn(r, y, q0);
+        }
+        x[i] = out;
+        w4 = w3;
+        w3 = w2;
+        w2 = w1;
+        w1 = out;
+    }
+}
+
+constexpr int kPoisSmemMaxN = 16384;  // solution vector kept in shared memory up to this n
 
 __global__ void k_poisson(PoissonLaunch L) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    PoisChunk *buf = (PoisChunk *)smem_raw;  // two chunk buffers, then the solution vector
+    PoisBandChunk *buf = (PoisBandChunk *)smem_raw;  // two chunk buffers, then the solution vector
+    __shared__ int s_bad;
     const int run = blockIdx.x;
     RunFields &F = L.fields[run];
     const LUDev &lu = L.lu[run];
     const int n = F.n;
     const bool in_smem = L.x_in_smem;
-    double *x = in_smem ? (double *)(smem_raw + 2 * sizeof(PoisChunk)) : F.phi;
+    double *x = in_smem ? (double *)(smem_raw + 2 * sizeof(PoisBandChunk)) : F.phi;
     double *tmp = F.efin;  // scratch until E_x is recomputed at the end
     const double te = kEps0Inv;
     const double w = L.w[run];
@@ -285,95 +314,68 @@ __global__ void k_poisson(PoissonLaunch L) {
     __syncthreads();
     // Row interchanges of dgetrs applied as one gather: b'[k] = b[perm[k]].
     for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = tmp[lu.perm[k]];
-    __syncthreads();
-    const int nchunks = (n + kPoisChunk - 1) / kPoisChunk;
-    // ---- forward: rows ascending
+    const int nchunks = (n + kPoisRows - 1) / kPoisRows;
+    // ---- forward
     {
         double w1 = 0, w2 = 0, w3 = 0, w4 = 0;
-        bool fit_cur = pois_stage(buf[0], lu.lptr, lu.lcol, lu.lval, 0, min(kPoisChunk, n));
+        bool fit_cur = pois_stage_band(buf[0], lu.L, 0, min(kPoisRows, n), 0, blockDim.x, false);
         __syncthreads();
         for (int c = 0; c < nchunks; c++) {
-            const int r0 = c * kPoisChunk, cnt = min(kPoisChunk, n - r0);
-            PoisChunk &B = buf[c & 1];
+            const int r0 = c * kPoisRows, cnt = min(kPoisRows, n - r0);
+            PoisBandChunk &B = buf[c & 1];
             bool fit_next = false;
             if (c + 1 < nchunks) {
-                const int r1 = r0 + cnt, cnt1 = min(kPoisChunk, n - r1);
-                if (threadIdx.x >= 32) {
-                    // warps 1.. stage the next chunk while thread 0 solves this one
-                    PoisChunk &N = buf[(c + 1) & 1];
-                    const int e0 = lu.lptr[r1], e1 = lu.lptr[r1 + cnt1];
-                    const int t = threadIdx.x - 32, nt = blockDim.x - 32;
-                    fit_next = (e1 - e0) <= kPoisMaxNnz;
-                    for (int k = t; k <= cnt1; k += nt) N.ptr[k] = lu.lptr[r1 + k] - e0;
-                    if (fit_next)
-                        for (int e = e0 + t; e < e1; e += nt) {
-                            N.col[e - e0] = lu.lcol[e];
-                            N.val[e - e0] = lu.lval[e];
-                        }
-                } else {
-                    fit_next = (lu.lptr[r1 + cnt1] - lu.lptr[r1]) <= kPoisMaxNnz;
-                }
+                const int r1 = r0 + cnt, cnt1 = min(kPoisRows, n - r1);
+                if (threadIdx.x >= 32) fit_next = pois_stage_band(buf[(c + 1) & 1], lu.L, r1, cnt1, 32, blockDim.x - 32, false);
+                else fit_next = (lu.L.fptr[r1 + cnt1] - lu.L.fptr[r1]) <= kPoisFar;
             }
             if (threadIdx.x == 0) {
-                const int gbase = lu.lptr[r0];
-                if (fit_cur) pois_rows<true, true>(B, lu.lcol, lu.lval, gbase, r0, cnt, x, w1, w2, w3, w4, true);
-                else pois_rows<true, false>(B, lu.lcol, lu.lval, gbase, r0, cnt, x, w1, w2, w3, w4, true);
+                const int gbase = lu.L.fptr[r0];
+                if (fit_cur) pois_fwd<true>(B, lu.L, gbase, r0, cnt, x, w1, w2, w3, w4);
+                else pois_fwd<false>(B, lu.L, gbase, r0, cnt, x, w1, w2, w3, w4);
             }
             fit_cur = fit_next;
             __syncthreads();
         }
     }
-    // ---- backward: rows descending (chunk c holds rows [c*kPoisChunk, ...))
+    // ---- backward
     {
         double w1 = 0, w2 = 0, w3 = 0, w4 = 0;
         const int clast = nchunks - 1;
-        const int r0l = clast * kPoisChunk;
-        bool fit_cur = pois_stage(buf[0], lu.uptr, lu.ucol, lu.uval, r0l, n - r0l);
-        for (int k = threadIdx.x; k < n - r0l; k += blockDim.x) {
-            buf[0].diag[k] = lu.udiag[r0l + k];
-            buf[0].rdiag[k] = lu.urdiag[r0l + k];
-        }
-        __syncthreads();
         int parity = 0;
+        bool fit_cur = pois_stage_band(buf[0], lu.U, clast * kPoisRows, n - clast * kPoisRows, 0, blockDim.x, true);
+        __syncthreads();
         for (int c = clast; c >= 0; c--) {
-            const int r0 = c * kPoisChunk, cnt = min(kPoisChunk, n - r0);
-            PoisChunk &B = buf[parity];
+            const int r0 = c * kPoisRows, cnt = min(kPoisRows, n - r0);
+            PoisBandChunk &B = buf[parity];
             bool fit_next = false;
             if (c > 0) {
-                const int r1 = (c - 1) * kPoisChunk, cnt1 = kPoisChunk;
-                if (threadIdx.x >= 32) {
-                    PoisChunk &N = buf[parity ^ 1];
-                    const int e0 = lu.uptr[r1], e1 = lu.uptr[r1 + cnt1];
-                    const int t = threadIdx.x - 32, nt = blockDim.x - 32;
-                    fit_next = (e1 - e0) <= kPoisMaxNnz;
-                    for (int k = t; k <= cnt1; k += nt) N.ptr[k] = lu.uptr[r1 + k] - e0;
-                    for (int k = t; k < cnt1; k += nt) {
-                        N.diag[k] = lu.udiag[r1 + k];
-                        N.rdiag[k] = lu.urdiag[r1 + k];
-                    }
-                    if (fit_next)
-                        for (int e = e0 + t; e < e1; e += nt) {
-                            N.col[e - e0] = lu.ucol[e];
-                            N.val[e - e0] = lu.uval[e];
-                        }
-                } else {
-                    fit_next = (lu.uptr[r1 + cnt1] - lu.uptr[r1]) <= kPoisMaxNnz;
-                }
+                const int r1 = (c - 1) * kPoisRows;
+                if (threadIdx.x >= 32) fit_next = pois_stage_band(buf[parity ^ 1], lu.U, r1, kPoisRows, 32, blockDim.x - 32, true);
+                else fit_next = (lu.U.fptr[r1 + kPoisRows] - lu.U.fptr[r1]) <= kPoisFar;
             }
+            const double s1 = w1, s2 = w2, s3 = w3, s4 = w4;
             if (threadIdx.x == 0) {
-                const int gbase = lu.uptr[r0];
-                double *xin = B.xin;
-                for (int q = 0; q < cnt; q++) xin[q] = x[r0 + q];
-                // keep the chunk's inputs and window so that a mismatch can be redone exactly
-                const double s1 = w1, s2 = w2, s3 = w3, s4 = w4;
-                bool ok = fit_cur ? pois_rows<false, true>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, w1, w2, w3, w4, false)
-                                  : pois_rows<false, false>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, w1, w2, w3, w4, false);
-                if (!ok) {
-                    for (int q = 0; q < cnt; q++) x[r0 + q] = xin[q];
-                    w1 = s1, w2 = s2, w3 = s3, w4 = s4;
-                    if (fit_cur) pois_rows<false, true>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, w1, w2, w3, w4, true);
-                    else pois_rows<false, false>(B, lu.ucol, lu.uval, gbase, r0, cnt, x, w1, w2, w3, w4, true);
-                }
+                s_bad = 0;
+                const int gbase = lu.U.fptr[r0];
+                for (int q = 0; q < cnt; q++) B.rhs[q] = x[r0 + q];  // keep right-hand sides for a redo
+                if (fit_cur) pois_bwd<true, false>(B, lu.U, gbase, r0, cnt, x, w1, w2, w3, w4);
+                else pois_bwd<false, false>(B, lu.U, gbase, r0, cnt, x, w1, w2, w3, w4);
+            }
+            __syncthreads();
+            // every quotient of the chunk against the IEEE quotient of its numerator
+            for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+                const double ieee = B.num[q] / B.diag[q];
+                if (__double_as_longlong(ieee) != __double_as_longlong(x[r0 + q])) s_bad = 1;
+            }
+            __syncthreads();
+            if (s_bad && threadIdx.x == 0) {
+                // redo the chunk from its right-hand sides with IEEE division
+                for (int q = 0; q < cnt; q++) x[r0 + q] = B.rhs[q];
+                w1 = s1, w2 = s2, w3 = s3, w4 = s4;
+                const int gbase = lu.U.fptr[r0];
+                if (fit_cur) pois_bwd<true, true>(B, lu.U, gbase, r0, cnt, x, w1, w2, w3, w4);
+                else pois_bwd<false, true>(B, lu.U, gbase, r0, cnt, x, w1, w2, w3, w4);
             }
             fit_cur = fit_next;
             parity ^= 1;
@@ -396,7 +398,7 @@ __global__ void k_poisson(PoissonLaunch L) {
 void launch_poisson(const PoissonLaunch &L) {
     PoissonLaunch P = L;
     P.x_in_smem = L.maxn <= kPoisSmemMaxN ? 1 : 0;
-    const int smem = 2 * (int)sizeof(PoisChunk) + (P.x_in_smem ? 8 * L.maxn : 0);
+    const int smem = 2 * (int)sizeof(PoisBandChunk) + (P.x_in_smem ? 8 * L.maxn : 0);
     cudaFuncSetAttribute(k_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     k_poisson<<<L.nruns, 512, smem, L.stream>>>(P);
 }

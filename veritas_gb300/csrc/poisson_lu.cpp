@@ -151,6 +151,46 @@ int PoissonLU::build(int N) {
     return info;
 }
 
+PoissonLU::Band PoissonLU::lower_band() const {
+    Band B;
+    B.band.assign((size_t)4 * n, 0.0);
+    B.fptr.push_back(0);
+    for (int i = 0; i < n; i++) {
+        for (int e = lptr[i]; e < lptr[i + 1]; e++) {  // ascending columns
+            int d = i - lcol[e];
+            if (d >= 1 && d <= 4) {
+                B.band[4 * i + d - 1] = lval[e];
+            } else {
+                B.fcol.push_back(lcol[e]);
+                B.fval.push_back(lval[e]);
+            }
+        }
+        B.fptr.push_back((int)B.fcol.size());
+    }
+    return B;
+}
+
+PoissonLU::Band PoissonLU::upper_band() const {
+    Band B;
+    B.band.assign((size_t)4 * n, 0.0);
+    B.diag = udiag;
+    B.rdiag = urdiag;
+    B.fptr.push_back(0);
+    for (int i = 0; i < n; i++) {
+        for (int e = uptr[i]; e < uptr[i + 1]; e++) {  // descending columns
+            int d = ucol[e] - i;
+            if (d >= 1 && d <= 4) {
+                B.band[4 * i + d - 1] = uval[e];
+            } else {
+                B.fcol.push_back(ucol[e]);
+                B.fval.push_back(uval[e]);
+            }
+        }
+        B.fptr.push_back((int)B.fcol.size());
+    }
+    return B;
+}
+
 void PoissonLU::solve(double *b) const {
     for (int k = 0; k < n; k++)
         if (ipiv[k] != k) std::swap(b[k], b[ipiv[k]]);

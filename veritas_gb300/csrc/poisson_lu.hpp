@@ -26,6 +26,14 @@ struct PoissonLU {
     int build(int n);
     // Host reference solve with the same operation order as the device (tests only).
     void solve(double *b) const;
+    // Band form of the factors for the device (four columns either side of the
+    // diagonal, the rest as "far" entries in summation order).
+    struct Band {
+        std::vector<double> band, diag, rdiag, fval;
+        std::vector<int> fptr, fcol;
+    };
+    Band lower_band() const;
+    Band upper_band() const;
 };
 
 }  // namespace vx

@@ -71,15 +71,21 @@ struct AsmLaunch {
 void launch_assemble(const AsmLaunch &A);
 
 // Poisson solve with precomputed sparse LU factors (EMSolver::UpdatePotential).
+// One triangular factor in band form (see k_poisson): band[4*i + d - 1] is the
+// coefficient of column i-d (L) or i+d (U), exact zero where the factor has none; the
+// far entries of row i are fcol/fval[fptr[i] .. fptr[i+1]) in summation order.
+struct BandFactor {
+    const double *band;
+    const double *diag;   // U: u_ii
+    const double *rdiag;  // U: RN(1/u_ii)
+    const int *fptr, *fcol;
+    const double *fval;
+};
+
 struct LUDev {
     int n;
     const int *perm;  // row interchanges composed into one gather b'[k] = b[perm[k]]
-    const int *lptr, *lcol;
-    const double *lval;
-    const int *uptr, *ucol;
-    const double *uval;
-    const double *udiag;
-    const double *urdiag;  // RN(1/u_ii), computed on the host
+    BandFactor L, U;
 };
 struct PoissonLaunch {
     const LUDev *lu;      // per run
