@@ -190,25 +190,34 @@ __device__ __forceinline__ double efield_at(const double *phi, int n, double fco
 // after each chunk the whole block checks every quotient against the IEEE quotient and
 // the chunk is redone with IEEE division if any differs, so the result is always the
 // dgetrs rounding.
-constexpr int kPoisRows = 256;   // rows per staged chunk
-constexpr int kPoisFar = 2048;   // far entries per staged chunk
+constexpr int kPoisRows = 256;               // rows per chunk
+constexpr int kPoisLA = 3;                   // look-ahead rows staged with each chunk
+constexpr int kPoisBuf = kPoisRows + kPoisLA;
+constexpr int kPoisFar = 2048;               // far entries per staged chunk
 
 struct PoisBandChunk {
-    double c1[kPoisRows], c2[kPoisRows], c3[kPoisRows], c4[kPoisRows];  // band coefficients
-    double diag[kPoisRows], rdiag[kPoisRows], num[kPoisRows];           // U only
-    double rhs[kPoisRows];  // right-hand sides of a backward chunk, kept for an exact redo
-    int fptr[kPoisRows + 1];
+    int a;                                    // first staged row
+    double c1[kPoisBuf], c2[kPoisBuf], c3[kPoisBuf], c4[kPoisBuf];  // band coefficients
+    double diag[kPoisBuf], rdiag[kPoisBuf];   // U only
+    double num[kPoisRows], rhs[kPoisRows];    // backward: numerators, chunk right-hand sides
+    int fptr[kPoisBuf + 1];
     int fcol[kPoisFar];
     double fval[kPoisFar];
 };
 
-// Stage rows [r0, r0+cnt) of a band factor into B with threads [t0, t0+nt).
-__device__ bool pois_stage_band(PoisBandChunk &B, const BandFactor &F, int r0, int cnt, int t0, int nt, bool upper) {
-    const int f0 = F.fptr[r0], f1 = F.fptr[r0 + cnt];
+// Stage rows [a, b) (clamped to [0, n)) of a band factor into B with threads
+// [t0, t0+nt).  Returns whether the far entries fit.
+__device__ bool pois_stage_band(PoisBandChunk &B, const BandFactor &F, int a, int b, int n, int t0, int nt,
+                                bool upper) {
+    a = max(a, 0);
+    b = min(b, n);
+    const int cnt = b - a;
+    const int f0 = F.fptr[a], f1 = F.fptr[b];
     const bool fits = (f1 - f0) <= kPoisFar;
-    for (int k = (int)threadIdx.x - t0; k < cnt; k += nt) {
-        if (k < 0) continue;
-        const int r = r0 + k;
+    const int t = (int)threadIdx.x - t0;
+    if (t == 0) B.a = a;
+    for (int k = t; k < cnt; k += nt) {
+        const int r = a + k;
         B.c1[k] = F.band[4 * r];
         B.c2[k] = F.band[4 * r + 1];
         B.c3[k] = F.band[4 * r + 2];
@@ -218,77 +227,85 @@ __device__ bool pois_stage_band(PoisBandChunk &B, const BandFactor &F, int r0, i
             B.rdiag[k] = F.rdiag[r];
         }
     }
-    for (int k = (int)threadIdx.x - t0; k <= cnt; k += nt)
-        if (k >= 0) B.fptr[k] = F.fptr[r0 + k] - f0;
+    for (int k = t; k <= cnt; k += nt) B.fptr[k] = F.fptr[a + k] - f0;
     if (fits)
-        for (int e = f0 + (int)threadIdx.x - t0; e < f1; e += nt)
-            if (e >= f0) {
-                B.fcol[e - f0] = F.fcol[e];
-                B.fval[e - f0] = F.fval[e];
-            }
+        for (int e = f0 + t; e < f1; e += nt) {
+            B.fcol[e - f0] = F.fcol[e];
+            B.fval[e - f0] = F.fval[e];
+        }
     return fits;
 }
 
-// Forward rows of one chunk: x_i = b_i - sum (far, ascending) - x_{i-4}c4 - x_{i-3}c3
-// - x_{i-2}c2 - x_{i-1}c1.
+// Right-hand side of row r with its far entries subtracted in summation order.
 template <bool FAR_SMEM>
-__device__ __forceinline__ void pois_fwd(const PoisBandChunk &B, const BandFactor &F, int gbase, int r0, int cnt,
-                                         double *x, double &w1, double &w2, double &w3, double &w4) {
-#pragma unroll 2
+__device__ __forceinline__ double pois_far(const PoisBandChunk &B, const BandFactor &F, const double *x, int r) {
+    const int k = r - B.a;
+    double s = x[r];
+    const int gbase = FAR_SMEM ? 0 : F.fptr[B.a];
+    for (int e = B.fptr[k]; e < B.fptr[k + 1]; e++) {
+        const int col = FAR_SMEM ? B.fcol[e] : F.fcol[gbase + e];
+        const double v = FAR_SMEM ? B.fval[e] : F.fval[gbase + e];
+        s = s - x[col] * v;
+    }
+    return s;
+}
+
+// Software-pipelined substitution.  Row i's sum is ((((Fb - x4 c4) - x3 c3) - x2 c2) - x1 c1)
+// with x_d the solution d rows back (forward) or ahead (backward) and Fb the right-hand side
+// minus its far entries.  The partial sums of the next three rows are held in registers
+// (P1 for the next row after its c2 term, P2 after c3, P3 after c4), so when x_{i-1}
+// arrives the four products that use it are independent and only x_i's own
+// product-and-subtract is on the critical path.
+struct PoisPipe {
+    double w1, P1, P2, P3;
+};
+
+template <bool FAR_SMEM>
+__device__ void pois_fwd_chunk(const PoisBandChunk &B, const BandFactor &F, int r0, int cnt, int n, double *x,
+                               PoisPipe &st) {
     for (int q = 0; q < cnt; q++) {
         const int i = r0 + q;
-        double s = x[i];
-        for (int e = B.fptr[q]; e < B.fptr[q + 1]; e++) {
-            const int col = FAR_SMEM ? B.fcol[e] : F.fcol[gbase + e];
-            const double v = FAR_SMEM ? B.fval[e] : F.fval[gbase + e];
-            s = s - x[col] * v;
-        }
-        s = s - w4 * B.c4[q];
-        s = s - w3 * B.c3[q];
-        s = s - w2 * B.c2[q];
-        s = s - w1 * B.c1[q];
-        x[i] = s;
-        w4 = w3;
-        w3 = w2;
-        w2 = w1;
-        w1 = s;
+        const int k = i - B.a;
+        const double w1 = st.w1;
+        const double xi = st.P1 - w1 * B.c1[k];
+        double n1 = st.P2, n2 = st.P3, n3 = 0.0;
+        if (i + 1 < n) n1 = st.P2 - w1 * B.c2[k + 1];
+        if (i + 2 < n) n2 = st.P3 - w1 * B.c3[k + 2];
+        if (i + 3 < n) n3 = pois_far<FAR_SMEM>(B, F, x, i + 3) - w1 * B.c4[k + 3];
+        x[i] = xi;
+        st.w1 = xi;
+        st.P1 = n1;
+        st.P2 = n2;
+        st.P3 = n3;
     }
 }
 
-// Backward rows of one chunk (descending): numerator as above with the far entries
-// (descending columns) first, then x_{i+4} .. x_{i+1}; quotient by Markstein or IEEE.
 template <bool FAR_SMEM, bool IEEE>
-__device__ __forceinline__ void pois_bwd(PoisBandChunk &B, const BandFactor &F, int gbase, int r0, int cnt,
-                                         double *x, double &w1, double &w2, double &w3, double &w4) {
-#pragma unroll 2
-    for (int qq = 0; qq < cnt; qq++) {
-        const int q = cnt - 1 - qq;
-        const int i = r0 + q;
-        double s = x[i];
-        for (int e = B.fptr[q]; e < B.fptr[q + 1]; e++) {
-            const int col = FAR_SMEM ? B.fcol[e] : F.fcol[gbase + e];
-            const double v = FAR_SMEM ? B.fval[e] : F.fval[gbase + e];
-            s = s - x[col] * v;
-        }
-        s = s - w4 * B.c4[q];
-        s = s - w3 * B.c3[q];
-        s = s - w2 * B.c2[q];
-        s = s - w1 * B.c1[q];
-        double out;
+__device__ void pois_bwd_chunk(PoisBandChunk &B, const BandFactor &F, int r0, int cnt, double *x, PoisPipe &st) {
+    for (int qq = cnt - 1; qq >= 0; qq--) {
+        const int i = r0 + qq;
+        const int k = i - B.a;
+        const double w1 = st.w1;
+        const double num = st.P1 - w1 * B.c1[k];
+        double n1 = st.P2, n2 = st.P3, n3 = 0.0;
+        if (i - 1 >= 0) n1 = st.P2 - w1 * B.c2[k - 1];
+        if (i - 2 >= 0) n2 = st.P3 - w1 * B.c3[k - 2];
+        if (i - 3 >= 0) n3 = pois_far<FAR_SMEM>(B, F, x, i - 3) - w1 * B.c4[k - 3];
+        double xi;
         if (IEEE) {
-            out = s / B.diag[q];
+            xi = num / B.diag[k];
         } else {
-            B.num[q] = s;
-            const double y = B.rdiag[q];
-            const double q0 = __dmul_rn(s, y);
-            const double r = __fma_rn(-q0, B.diag[q], s);
-            out = __fma_rn(r, y, q0);
+            B.num[qq] = num;
+            const double y = B.rdiag[k];
+            const double q0 = __dmul_rn(num, y);
+            const double r = __fma_rn(-q0, B.diag[k], num);
+            xi = __fma_rn(r, y, q0);
         }
-        x[i] = out;
-        w4 = w3;
-        w3 = w2;
-        w2 = w1;
-        w1 = out;
+        x[i] = xi;
+        st.w1 = xi;
+        st.P1 = n1;
+        st.P2 = n2;
+        st.P3 = n3;
     }
 }
 
@@ -315,67 +332,78 @@ __global__ void k_poisson(PoissonLaunch L) {
     // Row interchanges of dgetrs applied as one gather: b'[k] = b[perm[k]].
     for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = tmp[lu.perm[k]];
     const int nchunks = (n + kPoisRows - 1) / kPoisRows;
-    // ---- forward
+    // ---- forward: rows ascending; chunk c stages rows [c*R, c*R + R + LA)
     {
-        double w1 = 0, w2 = 0, w3 = 0, w4 = 0;
-        bool fit_cur = pois_stage_band(buf[0], lu.L, 0, min(kPoisRows, n), 0, blockDim.x, false);
+        PoisPipe st{0.0, 0.0, 0.0, 0.0};
+        bool fit_cur = pois_stage_band(buf[0], lu.L, 0, kPoisBuf, n, 0, blockDim.x, false);
         __syncthreads();
+        if (threadIdx.x == 0) {
+            // pipeline start: partial sums of rows 0..2 (their band terms reach before row 0)
+            st.P1 = fit_cur ? pois_far<true>(buf[0], lu.L, x, 0) : pois_far<false>(buf[0], lu.L, x, 0);
+            if (n > 1) st.P2 = fit_cur ? pois_far<true>(buf[0], lu.L, x, 1) : pois_far<false>(buf[0], lu.L, x, 1);
+            if (n > 2) st.P3 = fit_cur ? pois_far<true>(buf[0], lu.L, x, 2) : pois_far<false>(buf[0], lu.L, x, 2);
+        }
         for (int c = 0; c < nchunks; c++) {
             const int r0 = c * kPoisRows, cnt = min(kPoisRows, n - r0);
             PoisBandChunk &B = buf[c & 1];
             bool fit_next = false;
             if (c + 1 < nchunks) {
-                const int r1 = r0 + cnt, cnt1 = min(kPoisRows, n - r1);
-                if (threadIdx.x >= 32) fit_next = pois_stage_band(buf[(c + 1) & 1], lu.L, r1, cnt1, 32, blockDim.x - 32, false);
-                else fit_next = (lu.L.fptr[r1 + cnt1] - lu.L.fptr[r1]) <= kPoisFar;
+                const int r1 = r0 + kPoisRows;
+                if (threadIdx.x >= 32)
+                    fit_next = pois_stage_band(buf[(c + 1) & 1], lu.L, r1, r1 + kPoisBuf, n, 32, blockDim.x - 32, false);
+                else
+                    fit_next = (lu.L.fptr[min(r1 + kPoisBuf, n)] - lu.L.fptr[r1]) <= kPoisFar;
             }
             if (threadIdx.x == 0) {
-                const int gbase = lu.L.fptr[r0];
-                if (fit_cur) pois_fwd<true>(B, lu.L, gbase, r0, cnt, x, w1, w2, w3, w4);
-                else pois_fwd<false>(B, lu.L, gbase, r0, cnt, x, w1, w2, w3, w4);
+                if (fit_cur) pois_fwd_chunk<true>(B, lu.L, r0, cnt, n, x, st);
+                else pois_fwd_chunk<false>(B, lu.L, r0, cnt, n, x, st);
             }
             fit_cur = fit_next;
             __syncthreads();
         }
     }
-    // ---- backward
+    // ---- backward: rows descending; chunk c stages rows [c*R - LA, c*R + R)
     {
-        double w1 = 0, w2 = 0, w3 = 0, w4 = 0;
+        PoisPipe st{0.0, 0.0, 0.0, 0.0};
         const int clast = nchunks - 1;
         int parity = 0;
-        bool fit_cur = pois_stage_band(buf[0], lu.U, clast * kPoisRows, n - clast * kPoisRows, 0, blockDim.x, true);
+        bool fit_cur = pois_stage_band(buf[0], lu.U, clast * kPoisRows - kPoisLA, n, n, 0, blockDim.x, true);
         __syncthreads();
+        if (threadIdx.x == 0) {
+            st.P1 = fit_cur ? pois_far<true>(buf[0], lu.U, x, n - 1) : pois_far<false>(buf[0], lu.U, x, n - 1);
+            if (n > 1) st.P2 = fit_cur ? pois_far<true>(buf[0], lu.U, x, n - 2) : pois_far<false>(buf[0], lu.U, x, n - 2);
+            if (n > 2) st.P3 = fit_cur ? pois_far<true>(buf[0], lu.U, x, n - 3) : pois_far<false>(buf[0], lu.U, x, n - 3);
+        }
         for (int c = clast; c >= 0; c--) {
             const int r0 = c * kPoisRows, cnt = min(kPoisRows, n - r0);
             PoisBandChunk &B = buf[parity];
             bool fit_next = false;
             if (c > 0) {
                 const int r1 = (c - 1) * kPoisRows;
-                if (threadIdx.x >= 32) fit_next = pois_stage_band(buf[parity ^ 1], lu.U, r1, kPoisRows, 32, blockDim.x - 32, true);
-                else fit_next = (lu.U.fptr[r1 + kPoisRows] - lu.U.fptr[r1]) <= kPoisFar;
+                if (threadIdx.x >= 32)
+                    fit_next = pois_stage_band(buf[parity ^ 1], lu.U, r1 - kPoisLA, r1 + kPoisRows, n, 32, blockDim.x - 32, true);
+                else
+                    fit_next = (lu.U.fptr[r1 + kPoisRows] - lu.U.fptr[max(r1 - kPoisLA, 0)]) <= kPoisFar;
             }
-            const double s1 = w1, s2 = w2, s3 = w3, s4 = w4;
+            PoisPipe saved = st;
             if (threadIdx.x == 0) {
                 s_bad = 0;
-                const int gbase = lu.U.fptr[r0];
-                for (int q = 0; q < cnt; q++) B.rhs[q] = x[r0 + q];  // keep right-hand sides for a redo
-                if (fit_cur) pois_bwd<true, false>(B, lu.U, gbase, r0, cnt, x, w1, w2, w3, w4);
-                else pois_bwd<false, false>(B, lu.U, gbase, r0, cnt, x, w1, w2, w3, w4);
+                for (int q = 0; q < cnt; q++) B.rhs[q] = x[r0 + q];
+                if (fit_cur) pois_bwd_chunk<true, false>(B, lu.U, r0, cnt, x, st);
+                else pois_bwd_chunk<false, false>(B, lu.U, r0, cnt, x, st);
             }
             __syncthreads();
-            // every quotient of the chunk against the IEEE quotient of its numerator
+            // every Markstein quotient of the chunk against the IEEE quotient of its numerator
             for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
-                const double ieee = B.num[q] / B.diag[q];
+                const double ieee = B.num[q] / B.diag[r0 + q - B.a];
                 if (__double_as_longlong(ieee) != __double_as_longlong(x[r0 + q])) s_bad = 1;
             }
             __syncthreads();
             if (s_bad && threadIdx.x == 0) {
-                // redo the chunk from its right-hand sides with IEEE division
                 for (int q = 0; q < cnt; q++) x[r0 + q] = B.rhs[q];
-                w1 = s1, w2 = s2, w3 = s3, w4 = s4;
-                const int gbase = lu.U.fptr[r0];
-                if (fit_cur) pois_bwd<true, true>(B, lu.U, gbase, r0, cnt, x, w1, w2, w3, w4);
-                else pois_bwd<false, true>(B, lu.U, gbase, r0, cnt, x, w1, w2, w3, w4);
+                st = saved;
+                if (fit_cur) pois_bwd_chunk<true, true>(B, lu.U, r0, cnt, x, st);
+                else pois_bwd_chunk<false, true>(B, lu.U, r0, cnt, x, st);
             }
             fit_cur = fit_next;
             parity ^= 1;
