@@ -191,13 +191,13 @@ __device__ __forceinline__ double efield_at(const double *phi, int n, double fco
 // the chunk is redone with IEEE division if any differs, so the result is always the
 // dgetrs rounding.
 constexpr int kPoisRows = 256;               // rows per chunk
-constexpr int kPoisLA = 3;                   // look-ahead rows staged with each chunk
+constexpr int kPoisLA = 4;                   // look-ahead rows staged with each chunk
 constexpr int kPoisBuf = kPoisRows + kPoisLA;
 constexpr int kPoisFar = 2048;               // far entries per staged chunk
 
 struct PoisBandChunk {
     int a;                                    // first staged row
-    double c1[kPoisBuf], c2[kPoisBuf], c3[kPoisBuf], c4[kPoisBuf];  // band coefficients
+    double c[4][kPoisBuf];                    // band coefficients, c[d-1][row - a]
     double diag[kPoisBuf], rdiag[kPoisBuf];   // U only
     double num[kPoisRows], rhs[kPoisRows];    // backward: numerators, chunk right-hand sides
     int fptr[kPoisBuf + 1];
@@ -218,10 +218,10 @@ __device__ bool pois_stage_band(PoisBandChunk &B, const BandFactor &F, int a, in
     if (t == 0) B.a = a;
     for (int k = t; k < cnt; k += nt) {
         const int r = a + k;
-        B.c1[k] = F.band[4 * r];
-        B.c2[k] = F.band[4 * r + 1];
-        B.c3[k] = F.band[4 * r + 2];
-        B.c4[k] = F.band[4 * r + 3];
+        B.c[0][k] = F.band[4 * r];
+        B.c[1][k] = F.band[4 * r + 1];
+        B.c[2][k] = F.band[4 * r + 2];
+        B.c[3][k] = F.band[4 * r + 3];
         if (upper) {
             B.diag[k] = F.diag[r];
             B.rdiag[k] = F.rdiag[r];
@@ -250,62 +250,69 @@ __device__ __forceinline__ double pois_far(const PoisBandChunk &B, const BandFac
     return s;
 }
 
-// Software-pipelined substitution.  Row i's sum is ((((Fb - x4 c4) - x3 c3) - x2 c2) - x1 c1)
-// with x_d the solution d rows back (forward) or ahead (backward) and Fb the right-hand side
-// minus its far entries.  The partial sums of the next three rows are held in registers
-// (P1 for the next row after its c2 term, P2 after c3, P3 after c4), so when x_{i-1}
-// arrives the four products that use it are independent and only x_i's own
-// product-and-subtract is on the critical path.
-struct PoisPipe {
-    double w1, P1, P2, P3;
-};
-
+// Software-pipelined substitution on lanes 0..3 of warp 0.  Row i's sum is
+// ((((Fb - x4 c4) - x3 c3) - x2 c2) - x1 c1), x_d the solution d rows back (forward) or
+// ahead (backward), Fb the right-hand side minus its far entries.  Lane L holds the
+// partial sum of row i+L (forward) / i-L (backward), already reduced by every term but
+// the one with x_{i-1} (x_{i+1}); when that value arrives, each lane subtracts its own
+// product in the same two warp instructions, lane 0's result is x_i (before the division
+// backward), and the partials shift down one lane while lane 3 takes up the next row's
+// right-hand side.  On this part each FP64 warp instruction occupies the sub-partition's
+// FP64 unit for tens of cycles whatever the number of active lanes, so the lanes carry
+// the independent work for free.
 template <bool FAR_SMEM>
 __device__ void pois_fwd_chunk(const PoisBandChunk &B, const BandFactor &F, int r0, int cnt, int n, double *x,
-                               PoisPipe &st) {
+                               double &V, double &w1) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int L = lane < 4 ? lane : 3;
     for (int q = 0; q < cnt; q++) {
         const int i = r0 + q;
         const int k = i - B.a;
-        const double w1 = st.w1;
-        const double xi = st.P1 - w1 * B.c1[k];
-        double n1 = st.P2, n2 = st.P3, n3 = 0.0;
-        if (i + 1 < n) n1 = st.P2 - w1 * B.c2[k + 1];
-        if (i + 2 < n) n2 = st.P3 - w1 * B.c3[k + 2];
-        if (i + 3 < n) n3 = pois_far<FAR_SMEM>(B, F, x, i + 3) - w1 * B.c4[k + 3];
-        x[i] = xi;
-        st.w1 = xi;
-        st.P1 = n1;
-        st.P2 = n2;
-        st.P3 = n3;
+        const double coef = (i + L < n) ? B.c[L][k + L] : 0.0;
+        double fb = 0.0;
+        if (lane == 3 && i + 4 < n) fb = pois_far<FAR_SMEM>(B, F, x, i + 4);
+        const double nv = V - w1 * coef;
+        const double xi = __shfl_sync(full, nv, 0);
+        const double up = __shfl_down_sync(full, nv, 1);
+        V = (lane == 3) ? fb : up;
+        if (lane == 0) x[i] = xi;
+        __syncwarp();  // x[i] is read by lane 3 when it gathers a later row's far entries
+        w1 = xi;
     }
 }
 
 template <bool FAR_SMEM, bool IEEE>
-__device__ void pois_bwd_chunk(PoisBandChunk &B, const BandFactor &F, int r0, int cnt, double *x, PoisPipe &st) {
+__device__ void pois_bwd_chunk(PoisBandChunk &B, const BandFactor &F, int r0, int cnt, double *x, double &V,
+                               double &w1) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int L = lane < 4 ? lane : 3;
     for (int qq = cnt - 1; qq >= 0; qq--) {
         const int i = r0 + qq;
         const int k = i - B.a;
-        const double w1 = st.w1;
-        const double num = st.P1 - w1 * B.c1[k];
-        double n1 = st.P2, n2 = st.P3, n3 = 0.0;
-        if (i - 1 >= 0) n1 = st.P2 - w1 * B.c2[k - 1];
-        if (i - 2 >= 0) n2 = st.P3 - w1 * B.c3[k - 2];
-        if (i - 3 >= 0) n3 = pois_far<FAR_SMEM>(B, F, x, i - 3) - w1 * B.c4[k - 3];
-        double xi;
-        if (IEEE) {
-            xi = num / B.diag[k];
-        } else {
-            B.num[qq] = num;
-            const double y = B.rdiag[k];
-            const double q0 = __dmul_rn(num, y);
-            const double r = __fma_rn(-q0, B.diag[k], num);
-            xi = __fma_rn(r, y, q0);
+        const double coef = (i - L >= 0) ? B.c[L][k - L] : 0.0;
+        double fb = 0.0;
+        if (lane == 3 && i - 4 >= 0) fb = pois_far<FAR_SMEM>(B, F, x, i - 4);
+        const double nv = V - w1 * coef;
+        const double up = __shfl_down_sync(full, nv, 1);
+        double xi = 0.0;
+        if (lane == 0) {
+            if (IEEE) {
+                xi = nv / B.diag[k];
+            } else {
+                B.num[qq] = nv;
+                const double y = B.rdiag[k];
+                const double q0 = __dmul_rn(nv, y);
+                const double r = __fma_rn(-q0, B.diag[k], nv);
+                xi = __fma_rn(r, y, q0);
+            }
+            x[i] = xi;
         }
-        x[i] = xi;
-        st.w1 = xi;
-        st.P1 = n1;
-        st.P2 = n2;
-        st.P3 = n3;
+        xi = __shfl_sync(full, xi, 0);
+        __syncwarp();  // x[i] is read by lane 3 when it gathers a later row's far entries
+        V = (lane == 3) ? fb : up;
+        w1 = xi;
     }
 }
 
@@ -332,17 +339,14 @@ __global__ void k_poisson(PoissonLaunch L) {
     // Row interchanges of dgetrs applied as one gather: b'[k] = b[perm[k]].
     for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = tmp[lu.perm[k]];
     const int nchunks = (n + kPoisRows - 1) / kPoisRows;
+    const int lane = threadIdx.x & 31;
     // ---- forward: rows ascending; chunk c stages rows [c*R, c*R + R + LA)
     {
-        PoisPipe st{0.0, 0.0, 0.0, 0.0};
+        double V = 0.0, w1 = 0.0;
         bool fit_cur = pois_stage_band(buf[0], lu.L, 0, kPoisBuf, n, 0, blockDim.x, false);
         __syncthreads();
-        if (threadIdx.x == 0) {
-            // pipeline start: partial sums of rows 0..2 (their band terms reach before row 0)
-            st.P1 = fit_cur ? pois_far<true>(buf[0], lu.L, x, 0) : pois_far<false>(buf[0], lu.L, x, 0);
-            if (n > 1) st.P2 = fit_cur ? pois_far<true>(buf[0], lu.L, x, 1) : pois_far<false>(buf[0], lu.L, x, 1);
-            if (n > 2) st.P3 = fit_cur ? pois_far<true>(buf[0], lu.L, x, 2) : pois_far<false>(buf[0], lu.L, x, 2);
-        }
+        if (threadIdx.x < 32 && lane < 4 && lane < n)
+            V = fit_cur ? pois_far<true>(buf[0], lu.L, x, lane) : pois_far<false>(buf[0], lu.L, x, lane);
         for (int c = 0; c < nchunks; c++) {
             const int r0 = c * kPoisRows, cnt = min(kPoisRows, n - r0);
             PoisBandChunk &B = buf[c & 1];
@@ -354,9 +358,9 @@ __global__ void k_poisson(PoissonLaunch L) {
                 else
                     fit_next = (lu.L.fptr[min(r1 + kPoisBuf, n)] - lu.L.fptr[r1]) <= kPoisFar;
             }
-            if (threadIdx.x == 0) {
-                if (fit_cur) pois_fwd_chunk<true>(B, lu.L, r0, cnt, n, x, st);
-                else pois_fwd_chunk<false>(B, lu.L, r0, cnt, n, x, st);
+            if (threadIdx.x < 32) {
+                if (fit_cur) pois_fwd_chunk<true>(B, lu.L, r0, cnt, n, x, V, w1);
+                else pois_fwd_chunk<false>(B, lu.L, r0, cnt, n, x, V, w1);
             }
             fit_cur = fit_next;
             __syncthreads();
@@ -364,16 +368,13 @@ __global__ void k_poisson(PoissonLaunch L) {
     }
     // ---- backward: rows descending; chunk c stages rows [c*R - LA, c*R + R)
     {
-        PoisPipe st{0.0, 0.0, 0.0, 0.0};
+        double V = 0.0, w1 = 0.0;
         const int clast = nchunks - 1;
         int parity = 0;
         bool fit_cur = pois_stage_band(buf[0], lu.U, clast * kPoisRows - kPoisLA, n, n, 0, blockDim.x, true);
         __syncthreads();
-        if (threadIdx.x == 0) {
-            st.P1 = fit_cur ? pois_far<true>(buf[0], lu.U, x, n - 1) : pois_far<false>(buf[0], lu.U, x, n - 1);
-            if (n > 1) st.P2 = fit_cur ? pois_far<true>(buf[0], lu.U, x, n - 2) : pois_far<false>(buf[0], lu.U, x, n - 2);
-            if (n > 2) st.P3 = fit_cur ? pois_far<true>(buf[0], lu.U, x, n - 3) : pois_far<false>(buf[0], lu.U, x, n - 3);
-        }
+        if (threadIdx.x < 32 && lane < 4 && n - 1 - lane >= 0)
+            V = fit_cur ? pois_far<true>(buf[0], lu.U, x, n - 1 - lane) : pois_far<false>(buf[0], lu.U, x, n - 1 - lane);
         for (int c = clast; c >= 0; c--) {
             const int r0 = c * kPoisRows, cnt = min(kPoisRows, n - r0);
             PoisBandChunk &B = buf[parity];
@@ -385,12 +386,13 @@ __global__ void k_poisson(PoissonLaunch L) {
                 else
                     fit_next = (lu.U.fptr[r1 + kPoisRows] - lu.U.fptr[max(r1 - kPoisLA, 0)]) <= kPoisFar;
             }
-            PoisPipe saved = st;
-            if (threadIdx.x == 0) {
-                s_bad = 0;
-                for (int q = 0; q < cnt; q++) B.rhs[q] = x[r0 + q];
-                if (fit_cur) pois_bwd_chunk<true, false>(B, lu.U, r0, cnt, x, st);
-                else pois_bwd_chunk<false, false>(B, lu.U, r0, cnt, x, st);
+            const double V0 = V, w10 = w1;
+            if (threadIdx.x < 32) {
+                if (threadIdx.x == 0) s_bad = 0;
+                for (int q = lane; q < cnt; q += 32) B.rhs[q] = x[r0 + q];
+                __syncwarp();
+                if (fit_cur) pois_bwd_chunk<true, false>(B, lu.U, r0, cnt, x, V, w1);
+                else pois_bwd_chunk<false, false>(B, lu.U, r0, cnt, x, V, w1);
             }
             __syncthreads();
             // every Markstein quotient of the chunk against the IEEE quotient of its numerator
@@ -399,11 +401,13 @@ __global__ void k_poisson(PoissonLaunch L) {
                 if (__double_as_longlong(ieee) != __double_as_longlong(x[r0 + q])) s_bad = 1;
             }
             __syncthreads();
-            if (s_bad && threadIdx.x == 0) {
-                for (int q = 0; q < cnt; q++) x[r0 + q] = B.rhs[q];
-                st = saved;
-                if (fit_cur) pois_bwd_chunk<true, true>(B, lu.U, r0, cnt, x, st);
-                else pois_bwd_chunk<false, true>(B, lu.U, r0, cnt, x, st);
+            if (s_bad && threadIdx.x < 32) {
+                for (int q = lane; q < cnt; q += 32) x[r0 + q] = B.rhs[q];
+                __syncwarp();
+                V = V0;
+                w1 = w10;
+                if (fit_cur) pois_bwd_chunk<true, true>(B, lu.U, r0, cnt, x, V, w1);
+                else pois_bwd_chunk<false, true>(B, lu.U, r0, cnt, x, V, w1);
             }
             fit_cur = fit_next;
             parity ^= 1;
