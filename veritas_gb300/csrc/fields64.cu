@@ -200,6 +200,7 @@ struct PoisBandChunk {
     double c[4][kPoisBuf];                    // band coefficients, c[d-1][row - a]
     double diag[kPoisBuf], rdiag[kPoisBuf];   // U only
     double num[kPoisRows], rhs[kPoisRows];    // backward: numerators, chunk right-hand sides
+    double slotc[2][kPoisBuf];                // forward: accumulator-lane coefficients per step
     int fptr[kPoisBuf + 1];
     int fcol[kPoisFar];
     double fval[kPoisFar];
@@ -226,6 +227,7 @@ __device__ bool pois_stage_band(PoisBandChunk &B, const BandFactor &F, int a, in
             B.diag[k] = F.diag[r];
             B.rdiag[k] = F.rdiag[r];
         }
+        for (int sl = 0; sl < F.nslots; sl++) B.slotc[sl][k] = F.slot_coef[(size_t)sl * n + r];
     }
     for (int k = t; k <= cnt; k += nt) B.fptr[k] = F.fptr[a + k] - f0;
     if (fits)
@@ -266,16 +268,25 @@ __device__ void pois_fwd_chunk(const PoisBandChunk &B, const BandFactor &F, int 
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int L = lane < 4 ? lane : 3;
+    const int slot = lane - 4;  // lanes 4, 5: accumulators of the long far rows
+    const bool is_slot = slot >= 0 && slot < F.nslots;
+    const int sr0 = F.nslots > 0 ? F.slot_row[0] : -1, sr1 = F.nslots > 1 ? F.slot_row[1] : -1;
     for (int q = 0; q < cnt; q++) {
         const int i = r0 + q;
         const int k = i - B.a;
-        const double coef = (i + L < n) ? B.c[L][k + L] : 0.0;
+        double coef = 0.0;
+        if (lane < 4) coef = (i + L < n) ? B.c[L][k + L] : 0.0;
+        else if (is_slot) coef = B.slotc[slot][k];
         double fb = 0.0;
-        if (lane == 3 && i + 4 < n) fb = pois_far<FAR_SMEM>(B, F, x, i + 4);
+        if (lane == 3 && i + 4 < n && i + 4 != sr0 && i + 4 != sr1) fb = pois_far<FAR_SMEM>(B, F, x, i + 4);
         const double nv = V - w1 * coef;
         const double xi = __shfl_sync(full, nv, 0);
         const double up = __shfl_down_sync(full, nv, 1);
-        V = (lane == 3) ? fb : up;
+        const double a0 = __shfl_sync(full, nv, 4);
+        const double a1 = __shfl_sync(full, nv, 5);
+        if (i + 4 == sr0) fb = a0;
+        else if (i + 4 == sr1) fb = a1;
+        V = (lane == 3) ? fb : (is_slot ? nv : up);
         if (lane == 0) x[i] = xi;
         __syncwarp();  // x[i] is read by lane 3 when it gathers a later row's far entries
         w1 = xi;
@@ -284,7 +295,7 @@ __device__ void pois_fwd_chunk(const PoisBandChunk &B, const BandFactor &F, int 
 
 template <bool FAR_SMEM, bool IEEE>
 __device__ void pois_bwd_chunk(PoisBandChunk &B, const BandFactor &F, int r0, int cnt, double *x, double &V,
-                               double &w1) {
+                               double &w1, bool far_done) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int L = lane < 4 ? lane : 3;
@@ -293,7 +304,7 @@ __device__ void pois_bwd_chunk(PoisBandChunk &B, const BandFactor &F, int r0, in
         const int k = i - B.a;
         const double coef = (i - L >= 0) ? B.c[L][k - L] : 0.0;
         double fb = 0.0;
-        if (lane == 3 && i - 4 >= 0) fb = pois_far<FAR_SMEM>(B, F, x, i - 4);
+        if (lane == 3 && i - 4 >= 0) fb = far_done ? x[i - 4] : pois_far<FAR_SMEM>(B, F, x, i - 4);
         const double nv = V - w1 * coef;
         const double up = __shfl_down_sync(full, nv, 1);
         double xi = 0.0;
@@ -347,6 +358,7 @@ __global__ void k_poisson(PoissonLaunch L) {
         __syncthreads();
         if (threadIdx.x < 32 && lane < 4 && lane < n)
             V = fit_cur ? pois_far<true>(buf[0], lu.L, x, lane) : pois_far<false>(buf[0], lu.L, x, lane);
+        if (threadIdx.x < 32 && lane >= 4 && lane - 4 < lu.L.nslots) V = x[lu.L.slot_row[lane - 4]];
         for (int c = 0; c < nchunks; c++) {
             const int r0 = c * kPoisRows, cnt = min(kPoisRows, n - r0);
             PoisBandChunk &B = buf[c & 1];
@@ -369,6 +381,7 @@ __global__ void k_poisson(PoissonLaunch L) {
     // ---- backward: rows descending; chunk c stages rows [c*R - LA, c*R + R)
     {
         double V = 0.0, w1 = 0.0;
+        bool far_done = false;
         const int clast = nchunks - 1;
         int parity = 0;
         bool fit_cur = pois_stage_band(buf[0], lu.U, clast * kPoisRows - kPoisLA, n, n, 0, blockDim.x, true);
@@ -391,8 +404,8 @@ __global__ void k_poisson(PoissonLaunch L) {
                 if (threadIdx.x == 0) s_bad = 0;
                 for (int q = lane; q < cnt; q += 32) B.rhs[q] = x[r0 + q];
                 __syncwarp();
-                if (fit_cur) pois_bwd_chunk<true, false>(B, lu.U, r0, cnt, x, V, w1);
-                else pois_bwd_chunk<false, false>(B, lu.U, r0, cnt, x, V, w1);
+                if (fit_cur) pois_bwd_chunk<true, false>(B, lu.U, r0, cnt, x, V, w1, far_done);
+                else pois_bwd_chunk<false, false>(B, lu.U, r0, cnt, x, V, w1, far_done);
             }
             __syncthreads();
             // every Markstein quotient of the chunk against the IEEE quotient of its numerator
@@ -406,8 +419,18 @@ __global__ void k_poisson(PoissonLaunch L) {
                 __syncwarp();
                 V = V0;
                 w1 = w10;
-                if (fit_cur) pois_bwd_chunk<true, true>(B, lu.U, r0, cnt, x, V, w1);
-                else pois_bwd_chunk<false, true>(B, lu.U, r0, cnt, x, V, w1);
+                if (fit_cur) pois_bwd_chunk<true, true>(B, lu.U, r0, cnt, x, V, w1, far_done);
+                else pois_bwd_chunk<false, true>(B, lu.U, r0, cnt, x, V, w1, far_done);
+            }
+            __syncthreads();
+            if (!far_done && c == clast && lu.U.far_pre_col == r0 && r0 > 4) {
+                // x_{r0..n-1} are final: subtract the far terms of every row below r0-4 at once
+                for (int r = threadIdx.x; r < r0 - 4; r += blockDim.x) {
+                    double v = x[r];
+                    for (int e = lu.U.fptr[r]; e < lu.U.fptr[r + 1]; e++) v = v - x[lu.U.fcol[e]] * lu.U.fval[e];
+                    x[r] = v;
+                }
+                far_done = true;
             }
             fit_cur = fit_next;
             parity ^= 1;

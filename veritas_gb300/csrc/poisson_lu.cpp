@@ -167,6 +167,36 @@ PoissonLU::Band PoissonLU::lower_band() const {
         }
         B.fptr.push_back((int)B.fcol.size());
     }
+    // Rows with long far lists (more than 64 entries) go to accumulator lanes, if at most
+    // two of them are open at any step.
+    std::vector<int> longrows;
+    for (int i = 0; i < n; i++)
+        if (B.fptr[i + 1] - B.fptr[i] > 64) longrows.push_back(i);
+    if (!longrows.empty() && longrows.size() <= 2) {
+        B.nslots = (int)longrows.size();
+        B.slot_coef.assign((size_t)2 * n, 0.0);
+        std::vector<double> nval;
+        std::vector<int> ncol, nptr(1, 0);
+        for (int i = 0; i < n; i++) {
+            int s = -1;
+            for (int k = 0; k < B.nslots; k++)
+                if (longrows[k] == i) s = k;
+            for (int e = B.fptr[i]; e < B.fptr[i + 1]; e++) {
+                if (s >= 0) {
+                    // column c is subtracted at step c+1, when x_c has just been produced
+                    B.slot_coef[(size_t)s * n + B.fcol[e] + 1] = B.fval[e];
+                } else {
+                    ncol.push_back(B.fcol[e]);
+                    nval.push_back(B.fval[e]);
+                }
+            }
+            nptr.push_back((int)ncol.size());
+        }
+        for (int k = 0; k < B.nslots; k++) B.slot_row[k] = longrows[k];
+        B.fptr = nptr;
+        B.fcol = ncol;
+        B.fval = nval;
+    }
     return B;
 }
 
@@ -188,6 +218,15 @@ PoissonLU::Band PoissonLU::upper_band() const {
         }
         B.fptr.push_back((int)B.fcol.size());
     }
+    // Far terms of the rows below the last 256-row chunk can be precomputed in parallel
+    // after that chunk when every such row's far columns lie inside it.
+    const int R = 256;
+    const int last = ((n + R - 1) / R - 1) * R;
+    bool ok = last > 4;
+    for (int i = 0; ok && i < last - 4; i++)
+        for (int e = B.fptr[i]; e < B.fptr[i + 1]; e++)
+            if (B.fcol[e] < last) ok = false;
+    B.far_pre_col = ok ? last : -1;
     return B;
 }
 

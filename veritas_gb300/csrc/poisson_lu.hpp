@@ -31,6 +31,16 @@ struct PoissonLU {
     struct Band {
         std::vector<double> band, diag, rdiag, fval;
         std::vector<int> fptr, fcol;
+        // Lower factor: up to two rows with long far lists are accumulated by dedicated
+        // lanes; slot_coef[s*n + i] is the coefficient of column i-1 in row slot_row[s]
+        // (0 where the row has none), and that row's far list is left empty.
+        int nslots = 0;
+        int slot_row[2] = {-1, -1};
+        std::vector<double> slot_coef;
+        // Upper factor: rows below far_pre_row have all their far columns at or above
+        // far_pre_col, so their far terms can be subtracted in one parallel pass once the
+        // solution is known from far_pre_col up (-1: not possible).
+        int far_pre_col = -1;
     };
     Band lower_band() const;
     Band upper_band() const;

@@ -80,6 +80,10 @@ struct BandFactor {
     const double *rdiag;  // U: RN(1/u_ii)
     const int *fptr, *fcol;
     const double *fval;
+    int nslots;                // L: rows accumulated by dedicated lanes (0..2)
+    int slot_row[2];
+    const double *slot_coef;   // L: [slot][step] coefficient of column step-1
+    int far_pre_col;           // U: see PoissonLU::Band (-1: none)
 };
 
 struct LUDev {
