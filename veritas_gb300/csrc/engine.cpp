@@ -220,6 +220,8 @@ void Run::upload_lu() {
     dlb_fcol = upload(Lb.fcol, st);
     dlb_fval = upload(Lb.fval, st);
     dlb_slot = upload(Lb.slot_coef, st);
+    dlb_sload = upload(Lb.slot_load, st);
+    dlb_take = upload(Lb.take, st);
     dub_band = upload(Ub.band, st);
     dub_diag = upload(Ub.diag, st);
     dub_rdiag = upload(Ub.rdiag, st);
@@ -230,10 +232,10 @@ void Run::upload_lu() {
     ludev.n = lu.n;
     ludev.perm = dlu_perm.as<int>();
     ludev.L = BandFactor{dlb_band.as<double>(), nullptr, nullptr, dlb_fptr.as<int>(), dlb_fcol.as<int>(),
-                         dlb_fval.as<double>(), Lb.nslots, {Lb.slot_row[0], Lb.slot_row[1]},
-                         dlb_slot.as<double>(), -1};
+                         dlb_fval.as<double>(), Lb.nslots, dlb_slot.as<double>(), dlb_sload.as<int>(),
+                         dlb_take.as<int>(), -1};
     ludev.U = BandFactor{dub_band.as<double>(), dub_diag.as<double>(), dub_rdiag.as<double>(), dub_fptr.as<int>(),
-                         dub_fcol.as<int>(), dub_fval.as<double>(), 0, {-1, -1}, nullptr, Ub.far_pre_col};
+                         dub_fcol.as<int>(), dub_fval.as<double>(), -1, nullptr, nullptr, nullptr, Ub.far_pre_col};
 }
 
 // SolverManager::SolverManager (SolverManager.cpp:8-26) for a hierarchy that starts and

@@ -200,7 +200,9 @@ struct PoisBandChunk {
     double c[4][kPoisBuf];                    // band coefficients, c[d-1][row - a]
     double diag[kPoisBuf], rdiag[kPoisBuf];   // U only
     double num[kPoisRows], rhs[kPoisRows];    // backward: numerators, chunk right-hand sides
-    double slotc[2][kPoisBuf];                // forward: accumulator-lane coefficients per step
+    double slotc[4][kPoisBuf];                // forward: accumulator-lane coefficients per step
+    int sload[4][kPoisBuf];                   // forward: row taken up by each slot at each step
+    int take[kPoisBuf];                       // forward: slot finishing row step+4
     int fptr[kPoisBuf + 1];
     int fcol[kPoisFar];
     double fval[kPoisFar];
@@ -227,7 +229,11 @@ __device__ bool pois_stage_band(PoisBandChunk &B, const BandFactor &F, int a, in
             B.diag[k] = F.diag[r];
             B.rdiag[k] = F.rdiag[r];
         }
-        for (int sl = 0; sl < F.nslots; sl++) B.slotc[sl][k] = F.slot_coef[(size_t)sl * n + r];
+        for (int sl = 0; sl < F.nslots; sl++) {
+            B.slotc[sl][k] = F.slot_coef[(size_t)sl * n + r];
+            B.sload[sl][k] = F.slot_load[(size_t)sl * n + r];
+        }
+        if (F.take) B.take[k] = F.take[r];
     }
     for (int k = t; k <= cnt; k += nt) B.fptr[k] = F.fptr[a + k] - f0;
     if (fits)
@@ -268,27 +274,32 @@ __device__ void pois_fwd_chunk(const PoisBandChunk &B, const BandFactor &F, int 
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int L = lane < 4 ? lane : 3;
-    const int slot = lane - 4;  // lanes 4, 5: accumulators of the long far rows
+    const int slot = lane - 4;  // lanes 4..7: accumulators of the rows with far terms
     const bool is_slot = slot >= 0 && slot < F.nslots;
-    const int sr0 = F.nslots > 0 ? F.slot_row[0] : -1, sr1 = F.nslots > 1 ? F.slot_row[1] : -1;
+    const bool slots = F.nslots >= 0;
     for (int q = 0; q < cnt; q++) {
         const int i = r0 + q;
         const int k = i - B.a;
         double coef = 0.0;
         if (lane < 4) coef = (i + L < n) ? B.c[L][k + L] : 0.0;
-        else if (is_slot) coef = B.slotc[slot][k];
+        else if (is_slot) {
+            const int ld = B.sload[slot][k];
+            if (ld >= 0) V = x[ld];  // take up a new row's right-hand side
+            coef = B.slotc[slot][k];
+        }
         double fb = 0.0;
-        if (lane == 3 && i + 4 < n && i + 4 != sr0 && i + 4 != sr1) fb = pois_far<FAR_SMEM>(B, F, x, i + 4);
+        if (lane == 3 && i + 4 < n) fb = slots ? x[i + 4] : pois_far<FAR_SMEM>(B, F, x, i + 4);
         const double nv = V - w1 * coef;
         const double xi = __shfl_sync(full, nv, 0);
         const double up = __shfl_down_sync(full, nv, 1);
-        const double a0 = __shfl_sync(full, nv, 4);
-        const double a1 = __shfl_sync(full, nv, 5);
-        if (i + 4 == sr0) fb = a0;
-        else if (i + 4 == sr1) fb = a1;
+        if (slots) {
+            const int tk = B.take[k];
+            const double fin = __shfl_sync(full, nv, 4 + (tk >= 0 ? tk : 0));
+            if (tk >= 0) fb = fin;
+        }
         V = (lane == 3) ? fb : (is_slot ? nv : up);
         if (lane == 0) x[i] = xi;
-        __syncwarp();  // x[i] is read by lane 3 when it gathers a later row's far entries
+        if (!slots) __syncwarp();  // lane 3 reads x[i] when it gathers a later row's far entries
         w1 = xi;
     }
 }
@@ -358,7 +369,7 @@ __global__ void k_poisson(PoissonLaunch L) {
         __syncthreads();
         if (threadIdx.x < 32 && lane < 4 && lane < n)
             V = fit_cur ? pois_far<true>(buf[0], lu.L, x, lane) : pois_far<false>(buf[0], lu.L, x, lane);
-        if (threadIdx.x < 32 && lane >= 4 && lane - 4 < lu.L.nslots) V = x[lu.L.slot_row[lane - 4]];
+
         for (int c = 0; c < nchunks; c++) {
             const int r0 = c * kPoisRows, cnt = min(kPoisRows, n - r0);
             PoisBandChunk &B = buf[c & 1];

@@ -167,35 +167,45 @@ PoissonLU::Band PoissonLU::lower_band() const {
         }
         B.fptr.push_back((int)B.fcol.size());
     }
-    // Rows with long far lists (more than 64 entries) go to accumulator lanes, if at most
-    // two of them are open at any step.
-    std::vector<int> longrows;
+    // Schedule every row with far terms on an accumulator lane: row r occupies a slot from
+    // step (first far column + 1) to step r - 4, when lane 3 takes its sum.
+    struct Iv {
+        int open, close, row;
+    };
+    std::vector<Iv> ivs;
     for (int i = 0; i < n; i++)
-        if (B.fptr[i + 1] - B.fptr[i] > 64) longrows.push_back(i);
-    if (!longrows.empty() && longrows.size() <= 2) {
-        B.nslots = (int)longrows.size();
-        B.slot_coef.assign((size_t)2 * n, 0.0);
-        std::vector<double> nval;
-        std::vector<int> ncol, nptr(1, 0);
-        for (int i = 0; i < n; i++) {
-            int s = -1;
-            for (int k = 0; k < B.nslots; k++)
-                if (longrows[k] == i) s = k;
-            for (int e = B.fptr[i]; e < B.fptr[i + 1]; e++) {
-                if (s >= 0) {
-                    // column c is subtracted at step c+1, when x_c has just been produced
-                    B.slot_coef[(size_t)s * n + B.fcol[e] + 1] = B.fval[e];
-                } else {
-                    ncol.push_back(B.fcol[e]);
-                    nval.push_back(B.fval[e]);
-                }
+        if (B.fptr[i + 1] > B.fptr[i]) ivs.push_back({B.fcol[B.fptr[i]] + 1, i - 4, i});
+    std::sort(ivs.begin(), ivs.end(), [](const Iv &x, const Iv &y) { return x.open < y.open; });
+    std::vector<int> slot_of(ivs.size(), -1), busy_until(Band::kMaxSlots, -1);
+    int used = 0;
+    bool ok = true;
+    for (size_t k = 0; k < ivs.size() && ok; k++) {
+        int s = -1;
+        for (int q = 0; q < Band::kMaxSlots; q++)
+            if (busy_until[q] < ivs[k].open) {
+                s = q;
+                break;
             }
-            nptr.push_back((int)ncol.size());
+        if (s < 0 || ivs[k].close < ivs[k].open) ok = false;
+        else {
+            slot_of[k] = s;
+            busy_until[s] = ivs[k].close;
+            used = std::max(used, s + 1);
         }
-        for (int k = 0; k < B.nslots; k++) B.slot_row[k] = longrows[k];
-        B.fptr = nptr;
-        B.fcol = ncol;
-        B.fval = nval;
+    }
+    if (!ok) {
+        B.nslots = -1;
+        return B;
+    }
+    B.nslots = used;
+    B.slot_coef.assign((size_t)Band::kMaxSlots * n, 0.0);
+    B.slot_load.assign((size_t)Band::kMaxSlots * n, -1);
+    B.take.assign(n, -1);
+    for (size_t k = 0; k < ivs.size(); k++) {
+        const int s = slot_of[k], r = ivs[k].row;
+        B.slot_load[(size_t)s * n + ivs[k].open] = r;
+        for (int e = B.fptr[r]; e < B.fptr[r + 1]; e++) B.slot_coef[(size_t)s * n + B.fcol[e] + 1] = B.fval[e];
+        B.take[r - 4] = s;
     }
     return B;
 }

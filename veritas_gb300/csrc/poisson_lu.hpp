@@ -31,12 +31,16 @@ struct PoissonLU {
     struct Band {
         std::vector<double> band, diag, rdiag, fval;
         std::vector<int> fptr, fcol;
-        // Lower factor: up to two rows with long far lists are accumulated by dedicated
-        // lanes; slot_coef[s*n + i] is the coefficient of column i-1 in row slot_row[s]
-        // (0 where the row has none), and that row's far list is left empty.
+        // Lower factor: the far terms of every row are accumulated by up to kMaxSlots
+        // dedicated lanes.  At step i (when x_{i-1} has just been produced) slot s
+        // subtracts slot_coef[s*n + i] * x_{i-1}; slot_load[s*n + i] >= 0 names the row
+        // whose right-hand side the slot takes up at the start of step i; take[i] is the
+        // slot holding row i+4's finished sum at step i (-1: that row has no far terms).
+        // nslots = -1 when the rows cannot be scheduled on the lanes.
+        static constexpr int kMaxSlots = 4;
         int nslots = 0;
-        int slot_row[2] = {-1, -1};
         std::vector<double> slot_coef;
+        std::vector<int> slot_load, take;
         // Upper factor: rows below far_pre_row have all their far columns at or above
         // far_pre_col, so their far terms can be subtracted in one parallel pass once the
         // solution is known from far_pre_col up (-1: not possible).

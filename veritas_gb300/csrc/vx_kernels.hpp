@@ -80,9 +80,10 @@ struct BandFactor {
     const double *rdiag;  // U: RN(1/u_ii)
     const int *fptr, *fcol;
     const double *fval;
-    int nslots;                // L: rows accumulated by dedicated lanes (0..2)
-    int slot_row[2];
+    int nslots;                // L: accumulator lanes in use (-1: far terms on lane 3)
     const double *slot_coef;   // L: [slot][step] coefficient of column step-1
+    const int *slot_load;      // L: [slot][step] row whose right-hand side the slot takes up, or -1
+    const int *take;           // L: [step] slot finishing row step+4, or -1
     int far_pre_col;           // U: see PoissonLU::Band (-1: none)
 };
 
