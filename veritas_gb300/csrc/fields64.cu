@@ -277,23 +277,36 @@ __device__ void pois_fwd_chunk(const PoisBandChunk &B, const BandFactor &F, int 
     const int slot = lane - 4;  // lanes 4..7: accumulators of the rows with far terms
     const bool is_slot = slot >= 0 && slot < F.nslots;
     const bool slots = F.nslots >= 0;
-    for (int q = 0; q < cnt; q++) {
+    // Operands of row r0 + q, loaded one row ahead so their shared-memory latency overlaps
+    // the previous row's multiply-subtract.
+    auto fetch = [&](int q, double &coef, int &ld, double &fb, int &tk) {
         const int i = r0 + q;
         const int k = i - B.a;
-        double coef = 0.0;
+        coef = 0.0;
+        ld = -1;
         if (lane < 4) coef = (i + L < n) ? B.c[L][k + L] : 0.0;
         else if (is_slot) {
-            const int ld = B.sload[slot][k];
-            if (ld >= 0) V = x[ld];  // take up a new row's right-hand side
+            ld = B.sload[slot][k];
             coef = B.slotc[slot][k];
         }
-        double fb = 0.0;
-        if (lane == 3 && i + 4 < n) fb = slots ? x[i + 4] : pois_far<FAR_SMEM>(B, F, x, i + 4);
+        fb = 0.0;
+        if (slots && lane == 3 && i + 4 < n) fb = x[i + 4];
+        tk = slots ? B.take[k] : -1;
+    };
+    double coef, fb;
+    int ld, tk;
+    fetch(0, coef, ld, fb, tk);
+    for (int q = 0; q < cnt; q++) {
+        const int i = r0 + q;
+        if (ld >= 0) V = x[ld];  // a slot takes up a new row's right-hand side
+        if (!slots && lane == 3 && i + 4 < n) fb = pois_far<FAR_SMEM>(B, F, x, i + 4);
         const double nv = V - w1 * coef;
+        double coef_n = 0.0, fb_n = 0.0;
+        int ld_n = -1, tk_n = -1;
+        if (q + 1 < cnt) fetch(q + 1, coef_n, ld_n, fb_n, tk_n);
         const double xi = __shfl_sync(full, nv, 0);
         const double up = __shfl_down_sync(full, nv, 1);
         if (slots) {
-            const int tk = B.take[k];
             const double fin = __shfl_sync(full, nv, 4 + (tk >= 0 ? tk : 0));
             if (tk >= 0) fb = fin;
         }
@@ -301,6 +314,10 @@ __device__ void pois_fwd_chunk(const PoisBandChunk &B, const BandFactor &F, int 
         if (lane == 0) x[i] = xi;
         if (!slots) __syncwarp();  // lane 3 reads x[i] when it gathers a later row's far entries
         w1 = xi;
+        coef = coef_n;
+        fb = fb_n;
+        ld = ld_n;
+        tk = tk_n;
     }
 }
 
@@ -310,31 +327,43 @@ __device__ void pois_bwd_chunk(PoisBandChunk &B, const BandFactor &F, int r0, in
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int L = lane < 4 ? lane : 3;
-    for (int qq = cnt - 1; qq >= 0; qq--) {
+    auto fetch = [&](int qq, double &coef, double &fb, double &u, double &y) {
         const int i = r0 + qq;
         const int k = i - B.a;
-        const double coef = (i - L >= 0) ? B.c[L][k - L] : 0.0;
-        double fb = 0.0;
-        if (lane == 3 && i - 4 >= 0) fb = far_done ? x[i - 4] : pois_far<FAR_SMEM>(B, F, x, i - 4);
+        coef = (i - L >= 0) ? B.c[L][k - L] : 0.0;
+        fb = (far_done && lane == 3 && i - 4 >= 0) ? x[i - 4] : 0.0;
+        u = B.diag[k];
+        y = B.rdiag[k];
+    };
+    double coef, fb, u, y;
+    fetch(cnt - 1, coef, fb, u, y);
+    for (int qq = cnt - 1; qq >= 0; qq--) {
+        const int i = r0 + qq;
+        if (!far_done && lane == 3 && i - 4 >= 0) fb = pois_far<FAR_SMEM>(B, F, x, i - 4);
         const double nv = V - w1 * coef;
+        double coef_n = 0.0, fb_n = 0.0, u_n = 1.0, y_n = 1.0;
+        if (qq > 0) fetch(qq - 1, coef_n, fb_n, u_n, y_n);
         const double up = __shfl_down_sync(full, nv, 1);
         double xi = 0.0;
         if (lane == 0) {
             if (IEEE) {
-                xi = nv / B.diag[k];
+                xi = nv / u;
             } else {
                 B.num[qq] = nv;
-                const double y = B.rdiag[k];
                 const double q0 = __dmul_rn(nv, y);
-                const double r = __fma_rn(-q0, B.diag[k], nv);
+                const double r = __fma_rn(-q0, u, nv);
                 xi = __fma_rn(r, y, q0);
             }
             x[i] = xi;
         }
         xi = __shfl_sync(full, xi, 0);
-        __syncwarp();  // x[i] is read by lane 3 when it gathers a later row's far entries
+        if (!far_done) __syncwarp();  // lane 3 reads x[i] when it gathers a later row's far entries
         V = (lane == 3) ? fb : up;
         w1 = xi;
+        coef = coef_n;
+        fb = fb_n;
+        u = u_n;
+        y = y_n;
     }
 }
 
