@@ -367,6 +367,85 @@ __device__ void pois_bwd_chunk(PoisBandChunk &B, const BandFactor &F, int r0, in
     }
 }
 
+// Steady-state forms of the two chunk loops (every far term handled by accumulator
+// lanes or by the parallel pass): each lane walks its own coefficient stream with a
+// pointer, the shift and the slot hand-over are one shuffle with a per-lane source, and
+// no branch depends on the lane, so a row costs about 25 warp instructions.
+__device__ void pois_fwd_fast(const PoisBandChunk &B, const BandFactor &F, int r0, int cnt, int n, double *x,
+                              double &V, double &w1) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int slot = lane - 4;
+    const bool is_slot = slot >= 0 && slot < F.nslots;
+    const int k0 = r0 - B.a;
+    // coefficient stream of this lane (zeros for lanes without a role)
+    __shared__ double zero_stream[1];
+    if (lane == 0) zero_stream[0] = 0.0;
+    __syncwarp();
+    const double *cp;
+    int cstep = 1;
+    if (lane < 4) cp = &B.c[lane][k0 + lane];
+    else if (is_slot) cp = &B.slotc[slot][k0];
+    else {
+        cp = zero_stream;
+        cstep = 0;
+    }
+    const int *lp = is_slot ? &B.sload[slot][k0] : nullptr;
+    const int base_src = lane < 3 ? lane + 1 : lane;
+    // rows past the end of the matrix get a zero coefficient
+    const int lim = lane < 4 ? n - 1 - lane - r0 : cnt;  // q > lim: row i+lane >= n
+    for (int q = 0; q < cnt; q++) {
+        const int i = r0 + q;
+        double coef = *cp;
+        cp += cstep;
+        if (q > lim) coef = 0.0;
+        if (lp) {
+            const int ld = *lp++;
+            if (ld >= 0) V = x[ld];
+        }
+        const int tk = B.take[k0 + q];
+        const double fb = (lane == 3 && i + 4 < n) ? x[i + 4] : 0.0;
+        const double nv = V - w1 * coef;
+        const double xi = __shfl_sync(full, nv, 0);
+        const int src = (lane == 3 && tk >= 0) ? 4 + tk : base_src;
+        const double sh = __shfl_sync(full, nv, src);
+        V = (lane == 3 && tk < 0) ? fb : sh;
+        if (lane == 0) x[i] = xi;
+        w1 = xi;
+    }
+}
+
+__device__ void pois_bwd_fast(PoisBandChunk &B, int r0, int cnt, double *x, double &V, double &w1) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int L = lane < 4 ? lane : 3;
+    const int kl = r0 + cnt - 1 - B.a;  // buffer row of the chunk's last (first processed) row
+    const double *cp = &B.c[L][kl - L];
+    const double *up_ = &B.diag[kl];
+    const double *yp = &B.rdiag[kl];
+    const int lim = r0 + cnt - 1 - L;  // row i - L < 0 when i < L
+    for (int qq = cnt - 1; qq >= 0; qq--) {
+        const int i = r0 + qq;
+        double coef = *cp--;
+        if (i - L < 0) coef = 0.0;
+        const double u = *up_--, y = *yp--;
+        const double fb = (lane == 3 && i - 4 >= 0) ? x[i - 4] : 0.0;
+        const double nv = V - w1 * coef;
+        const double up = __shfl_down_sync(full, nv, 1);
+        const double q0 = __dmul_rn(nv, y);
+        const double r = __fma_rn(-q0, u, nv);
+        const double q1 = __fma_rn(r, y, q0);
+        const double xi = __shfl_sync(full, q1, 0);
+        if (lane == 0) {
+            B.num[qq] = nv;
+            x[i] = xi;
+        }
+        V = (lane == 3) ? fb : up;
+        w1 = xi;
+    }
+    (void)lim;
+}
+
 constexpr int kPoisSmemMaxN = 16384;  // solution vector kept in shared memory up to this n
 
 __global__ void k_poisson(PoissonLaunch L) {
@@ -411,7 +490,8 @@ __global__ void k_poisson(PoissonLaunch L) {
                     fit_next = (lu.L.fptr[min(r1 + kPoisBuf, n)] - lu.L.fptr[r1]) <= kPoisFar;
             }
             if (threadIdx.x < 32) {
-                if (fit_cur) pois_fwd_chunk<true>(B, lu.L, r0, cnt, n, x, V, w1);
+                if (lu.L.nslots >= 0) pois_fwd_fast(B, lu.L, r0, cnt, n, x, V, w1);
+                else if (fit_cur) pois_fwd_chunk<true>(B, lu.L, r0, cnt, n, x, V, w1);
                 else pois_fwd_chunk<false>(B, lu.L, r0, cnt, n, x, V, w1);
             }
             fit_cur = fit_next;
@@ -444,7 +524,8 @@ __global__ void k_poisson(PoissonLaunch L) {
                 if (threadIdx.x == 0) s_bad = 0;
                 for (int q = lane; q < cnt; q += 32) B.rhs[q] = x[r0 + q];
                 __syncwarp();
-                if (fit_cur) pois_bwd_chunk<true, false>(B, lu.U, r0, cnt, x, V, w1, far_done);
+                if (far_done) pois_bwd_fast(B, r0, cnt, x, V, w1);
+                else if (fit_cur) pois_bwd_chunk<true, false>(B, lu.U, r0, cnt, x, V, w1, far_done);
                 else pois_bwd_chunk<false, false>(B, lu.U, r0, cnt, x, V, w1, far_done);
             }
             __syncthreads();
