@@ -225,16 +225,18 @@ void Run::upload_lu() {
     dub_band = upload(Ub.band, st);
     dub_diag = upload(Ub.diag, st);
     dub_rdiag = upload(Ub.rdiag, st);
+    dub_rdlo = upload(Ub.rdiag_lo, st);
     dub_fptr = upload(Ub.fptr, st);
     dub_fcol = upload(Ub.fcol, st);
     dub_fval = upload(Ub.fval, st);
     eng.sync();
     ludev.n = lu.n;
     ludev.perm = dlu_perm.as<int>();
-    ludev.L = BandFactor{dlb_band.as<double>(), nullptr, nullptr, dlb_fptr.as<int>(), dlb_fcol.as<int>(),
+    ludev.L = BandFactor{dlb_band.as<double>(), nullptr, nullptr, nullptr, dlb_fptr.as<int>(), dlb_fcol.as<int>(),
                          dlb_fval.as<double>(), Lb.nslots, dlb_slot.as<double>(), dlb_sload.as<int>(),
                          dlb_take.as<int>(), -1};
-    ludev.U = BandFactor{dub_band.as<double>(), dub_diag.as<double>(), dub_rdiag.as<double>(), dub_fptr.as<int>(),
+    ludev.U = BandFactor{dub_band.as<double>(), dub_diag.as<double>(), dub_rdiag.as<double>(), dub_rdlo.as<double>(),
+                         dub_fptr.as<int>(),
                          dub_fcol.as<int>(), dub_fval.as<double>(), -1, nullptr, nullptr, nullptr, Ub.far_pre_col};
 }
 

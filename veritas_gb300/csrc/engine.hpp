@@ -73,7 +73,7 @@ public:
     DevBuf dBy, dBz, dEy, dEz, dAy, dAz, dasq, dphi, dcharge, dJ, dneut, defin, dex0;
     RunFields F{};
     PoissonLU lu;
-    DevBuf dlu_perm, dlb_band, dlb_fptr, dlb_fcol, dlb_fval, dlb_slot, dlb_sload, dlb_take, dub_band, dub_diag, dub_rdiag, dub_fptr, dub_fcol,
+    DevBuf dlu_perm, dlb_band, dlb_fptr, dlb_fcol, dlb_fval, dlb_slot, dlb_sload, dlb_take, dub_band, dub_diag, dub_rdiag, dub_rdlo, dub_fptr, dub_fcol,
         dub_fval;
     LUDev ludev{};
     uint64_t layout_version = 0;

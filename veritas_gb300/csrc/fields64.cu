@@ -198,7 +198,7 @@ constexpr int kPoisFar = 2048;               // far entries per staged chunk
 struct PoisBandChunk {
     int a;                                    // first staged row
     double c[4][kPoisBuf];                    // band coefficients, c[d-1][row - a]
-    double diag[kPoisBuf], rdiag[kPoisBuf];   // U only
+    double diag[kPoisBuf], rdiag[kPoisBuf], rdlo[kPoisBuf];  // U only
     double num[kPoisRows], rhs[kPoisRows];    // backward: numerators, chunk right-hand sides
     double slotc[4][kPoisBuf];                // forward: accumulator-lane coefficients per step
     int sload[4][kPoisBuf];                   // forward: row taken up by each slot at each step
@@ -228,6 +228,7 @@ __device__ bool pois_stage_band(PoisBandChunk &B, const BandFactor &F, int a, in
         if (upper) {
             B.diag[k] = F.diag[r];
             B.rdiag[k] = F.rdiag[r];
+            B.rdlo[k] = F.rdiag_lo[r];
         }
         for (int sl = 0; sl < F.nslots; sl++) {
             B.slotc[sl][k] = F.slot_coef[(size_t)sl * n + r];
@@ -350,9 +351,7 @@ __device__ void pois_bwd_chunk(PoisBandChunk &B, const BandFactor &F, int r0, in
                 xi = nv / u;
             } else {
                 B.num[qq] = nv;
-                const double q0 = __dmul_rn(nv, y);
-                const double r = __fma_rn(-q0, u, nv);
-                xi = __fma_rn(r, y, q0);
+                xi = __fma_rn(nv, y, __dmul_rn(nv, B.rdlo[i - B.a]));
             }
             x[i] = xi;
         }
@@ -423,18 +422,20 @@ __device__ void pois_bwd_fast(PoisBandChunk &B, int r0, int cnt, double *x, doub
     const double *cp = &B.c[L][kl - L];
     const double *up_ = &B.diag[kl];
     const double *yp = &B.rdiag[kl];
+    const double *lp = &B.rdlo[kl];
     const int lim = r0 + cnt - 1 - L;  // row i - L < 0 when i < L
     for (int qq = cnt - 1; qq >= 0; qq--) {
         const int i = r0 + qq;
         double coef = *cp--;
         if (i - L < 0) coef = 0.0;
-        const double u = *up_--, y = *yp--;
+        const double y = *yp--, ylo = *lp--;
+        up_--;
         const double fb = (lane == 3 && i - 4 >= 0) ? x[i - 4] : 0.0;
         const double nv = V - w1 * coef;
         const double up = __shfl_down_sync(full, nv, 1);
-        const double q0 = __dmul_rn(nv, y);
-        const double r = __fma_rn(-q0, u, nv);
-        const double q1 = __fma_rn(r, y, q0);
+        // quotient from the reciprocal split into high and low parts: within 2^-105 of
+        // nv/u before the final rounding; the chunk check catches the rare wrong rounding
+        const double q1 = __fma_rn(nv, y, __dmul_rn(nv, ylo));
         const double xi = __shfl_sync(full, q1, 0);
         if (lane == 0) {
             B.num[qq] = nv;

@@ -125,7 +125,12 @@ int PoissonLU::build(int N) {
         urows[k] = std::move(urow);
     }
     urdiag.resize(n);
-    for (int i = 0; i < n; i++) urdiag[i] = 1.0 / udiag[i];
+    urdiag_lo.resize(n);
+    for (int i = 0; i < n; i++) {
+        urdiag[i] = 1.0 / udiag[i];
+        // low part of 1/u: (1 - u*y) is exact by FMA, scaled by y
+        urdiag_lo[i] = std::fma(-udiag[i], urdiag[i], 1.0) * urdiag[i];
+    }
     perm.resize(n);
     for (int i = 0; i < n; i++) perm[i] = i;
     for (int k = 0; k < n; k++)
@@ -215,6 +220,7 @@ PoissonLU::Band PoissonLU::upper_band() const {
     B.band.assign((size_t)4 * n, 0.0);
     B.diag = udiag;
     B.rdiag = urdiag;
+    B.rdiag_lo = urdiag_lo;
     B.fptr.push_back(0);
     for (int i = 0; i < n; i++) {
         for (int e = uptr[i]; e < uptr[i + 1]; e++) {  // descending columns

@@ -21,6 +21,7 @@ struct PoissonLU {
     std::vector<int> perm;                             // composed interchanges: b'[k] = b[perm[k]]
     std::vector<int> lptr, lcol, uptr, ucol;           // CSR rows: L ascending, U descending
     std::vector<double> lval, uval, udiag, urdiag;  // urdiag = RN(1/u_ii)
+    std::vector<double> urdiag_lo;                  // 1/u_ii - urdiag to double precision
     // Factorise the Veritas Poisson matrix of size n (n >= 5).  Returns 0 or k+1 for a
     // zero pivot at step k.
     int build(int n);
@@ -29,7 +30,7 @@ struct PoissonLU {
     // Band form of the factors for the device (four columns either side of the
     // diagonal, the rest as "far" entries in summation order).
     struct Band {
-        std::vector<double> band, diag, rdiag, fval;
+        std::vector<double> band, diag, rdiag, rdiag_lo, fval;
         std::vector<int> fptr, fcol;
         // Lower factor: the far terms of every row are accumulated by up to kMaxSlots
         // dedicated lanes.  At step i (when x_{i-1} has just been produced) slot s

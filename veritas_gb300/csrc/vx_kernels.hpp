@@ -78,6 +78,7 @@ struct BandFactor {
     const double *band;
     const double *diag;   // U: u_ii
     const double *rdiag;  // U: RN(1/u_ii)
+    const double *rdiag_lo;  // U: 1/u_ii - RN(1/u_ii)
     const int *fptr, *fcol;
     const double *fval;
     int nslots;                // L: accumulator lanes in use (-1: far terms on lane 3)
