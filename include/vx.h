@@ -56,6 +56,7 @@ typedef struct vx_problem {
     double cfl, minEff, crit, sizeWeight;
     int32_t quadDepth;
     int32_t precision; /* 64: plain FP64 path; 32: FP32 precision form */
+    double bdens, bp0, bTe; /* beam population: density fraction of the slab, drift, temperature [keV] */
 } vx_problem;
 
 /* Fills *p with the defaults of the 2048 x 256 single-level laser/slab case. */
@@ -65,6 +66,7 @@ const char *vx_last_error(void);
 
 /* Context: one GPU + one stream. */
 int vx_ctx_create(int device, vx_ctx **out);
+/* Fails (VX_ERR_INVALID) while runs created on the context are still alive. */
 int vx_ctx_destroy(vx_ctx *ctx);
 int vx_ctx_sync(vx_ctx *ctx);
 /* Kernels launched by this context so far (graph replays count their nodes). */

@@ -81,12 +81,14 @@ struct Problem {
     double x1 = 15, x2 = 20, x3 = 80, x4 = 85;      // ramp up [x1,x2], plateau, ramp down [x3,x4]
     double Te = 1.0;                                 // keV
     double p0 = 0.0;                                 // drift [m_e c]
+    double bdens = 0.0, bp0 = 0.0, bTe = 1.0;        // beam population: density fraction, drift, keV
     double pert_amp = 0.0, pert_k = 1.0;             // density modulation
     double a0 = 1.0, fwhm = 10.0, delay = 10.0;      // laser [periods]
     double cfl = 0.5, minEff = 0.75, crit = 1e-6, sizeWeight = 1.0;
     int quadDepth = 2;
 };
 static Problem P;
+static double beam_T = 0.0, beam_p = 0.0;
 
 static const double kMe = 9.10938291e-31;
 static const double kQe = -1.60217657e-19;
@@ -149,6 +151,8 @@ void Settings::settingsOverride() {
     tempEM.resize(2, 0.0);
     tempEM[0] = P.lambda;
     tempEM[1] = P.a0 * mc / std::fabs(q[0]);
+    beam_T = m[0] * (P.bTe * kKeV);
+    beam_p = P.bp0 * mc;
 }
 
 bool Settings::RefinementOverride(double x, double p, int depth, int particleType) {
@@ -175,7 +179,12 @@ double Settings::GetBZ(double x, double t) {
 double Settings::InitialDistribution(double x, double p, int particleType) {
     double ne = temp[particleType][0] * slab_density(x / P.lambda);
     double dpv = p - temp[particleType][2];
-    return ne * std::exp(-(dpv * dpv) / (2.0 * temp[particleType][1])) / std::sqrt(DPI * temp[particleType][1]);
+    double v = ne * std::exp(-(dpv * dpv) / (2.0 * temp[particleType][1])) / std::sqrt(DPI * temp[particleType][1]);
+    if (P.bdens != 0.0) {
+        double dbv = p - beam_p;
+        v += P.bdens * ne * std::exp(-(dbv * dbv) / (2.0 * beam_T)) / std::sqrt(DPI * beam_T);
+    }
+    return v;
 }
 
 bool LOUD = false, NOISY = false;
@@ -278,6 +287,9 @@ int main(int argc, char **argv) {
     P.x4 = getd("x4", P.x4);
     P.Te = getd("Te", P.Te);
     P.p0 = getd("p0", P.p0);
+    P.bdens = getd("bdens", P.bdens);
+    P.bp0 = getd("bp0", P.bp0);
+    P.bTe = getd("bTe", P.bTe);
     P.pert_amp = getd("pert_amp", P.pert_amp);
     P.pert_k = getd("pert_k", P.pert_k);
     P.a0 = getd("a0", P.a0);

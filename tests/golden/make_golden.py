@@ -35,6 +35,18 @@ CASES = {
     # Plasma touching both x edges and both p edges: exercises the skipped domain-edge faces.
     "edge64": (["L=4", "nx=64", "np=32", "Te=50", "pmax=0.5", "x1=-1", "x2=0", "x3=3", "x4=5", "pert_amp=0.3",
                 "pert_k=1", "a0=1", "fwhm=2", "delay=0.5", "levels=1"], 3, [0, 1, 3]),
+    # Two refinement levels, one fine patch over the slab.
+    "amr2": (["L=8", "nx=64", "np=32", "Te=50", "pmax=2", "x1=1.5", "x2=2", "x3=6", "x4=6.5", "pert_amp=0.2",
+              "pert_k=2", "a0=2", "fwhm=2", "delay=1", "levels=2"], 3, [0, 1, 3]),
+    # Slab plus a drifting beam: four fine patches, three of them side by side in x with
+    # staggered p extents (same-level ghost copies and limiter exchange between patches).
+    "beam2": (["L=8", "nx=64", "np=32", "Te=0.5", "pmax=2", "x1=1", "x2=1.5", "x3=3", "x4=3.5", "pert_amp=0.2",
+               "pert_k=2", "a0=2", "fwhm=2", "delay=1", "bdens=0.5", "bp0=1.2", "bTe=0.5", "crit=1e-3",
+               "minEff=0.9", "levels=2"], 3, [0, 1, 3]),
+    # Three levels: two finest patches inside one intermediate patch.
+    "beam3": (["L=8", "nx=64", "np=32", "Te=1", "pmax=2", "x1=1.5", "x2=2", "x3=6", "x4=6.5", "pert_amp=0.2",
+               "pert_k=2", "a0=2", "fwhm=2", "delay=1", "bdens=0.5", "bp0=-1.2", "bTe=1", "crit=1e-3",
+               "minEff=0.9", "levels=3"], 3, [0, 1, 3]),
 }
 
 

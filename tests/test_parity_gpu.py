@@ -13,7 +13,8 @@ import vxstate
 from helpers import compare_states, golden, problem_for, total_mass
 
 TOL = 1e-10
-ONE_STEP = [("slab64", 0), ("slab64", 1), ("drift128", 0), ("edge64", 0)]
+ONE_STEP = [("slab64", 0), ("slab64", 1), ("drift128", 0), ("edge64", 0),
+            ("amr2", 0), ("beam2", 0), ("beam3", 0)]
 
 
 @pytest.fixture(scope="module")
@@ -49,7 +50,8 @@ def test_one_step_from_reference_state(ctx, tmp_path, name, k):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name,k0,k1", [("slab64", 0, 5), ("drift128", 1, 3), ("edge64", 1, 3)])
+@pytest.mark.parametrize("name,k0,k1", [("slab64", 0, 5), ("drift128", 1, 3), ("edge64", 1, 3), ("amr2", 1, 3),
+                                        ("beam2", 1, 3), ("beam3", 0, 3)])
 def test_multi_step_with_own_dt(ctx, tmp_path, name, k0, k1):
     s = _solver(ctx, name)
     vxstate.write_state(golden(name, k0), tmp_path / "in.bin")

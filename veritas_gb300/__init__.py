@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 from dataclasses import dataclass, fields
 from pathlib import Path
 
@@ -45,6 +46,7 @@ class _Problem(ctypes.Structure):
         ("a0", ctypes.c_double), ("fwhm", ctypes.c_double), ("delay", ctypes.c_double),
         ("cfl", ctypes.c_double), ("minEff", ctypes.c_double), ("crit", ctypes.c_double), ("sizeWeight", ctypes.c_double),
         ("quadDepth", ctypes.c_int32), ("precision", ctypes.c_int32),
+        ("bdens", ctypes.c_double), ("bp0", ctypes.c_double), ("bTe", ctypes.c_double),
     ]
 
 
@@ -130,6 +132,9 @@ class Problem:
     sizeWeight: float = 1.0
     quadDepth: int = 2
     precision: int = 64
+    bdens: float = 0.0
+    bp0: float = 0.0
+    bTe: float = 1.0
 
     def to_c(self) -> _Problem:
         p = _Problem()
@@ -140,7 +145,7 @@ class Problem:
     def harness_args(self) -> list[str]:
         """key=value arguments of the oracle harness for the same problem."""
         keys = ["L", "nx", "np", "r", "pmax", "dens", "x1", "x2", "x3", "x4", "Te", "p0", "pert_amp", "pert_k",
-                "a0", "fwhm", "delay", "cfl", "minEff", "crit", "sizeWeight", "quadDepth"]
+                "a0", "fwhm", "delay", "cfl", "minEff", "crit", "sizeWeight", "quadDepth", "bdens", "bp0", "bTe"]
         out = [f"{k}={getattr(self, k)!r}" for k in keys]
         out.append(f"levels={self.Lfinest}")
         return out
@@ -153,6 +158,7 @@ class Context:
         h = ctypes.c_void_p()
         _check(_lib.vx_ctx_create(device, ctypes.byref(h)))
         self._h = h
+        self._runs = weakref.WeakSet()
 
     @property
     def handle(self) -> ctypes.c_void_p:
@@ -183,7 +189,10 @@ class Context:
         return float(v.value)
 
     def close(self) -> None:
+        """Destroys the context after every solve still open on it."""
         if self._h:
+            for r in list(self._runs):
+                r.close()
             _check(_lib.vx_ctx_destroy(self._h))
             self._h = None
 
@@ -207,6 +216,7 @@ class SolverManager:
         h = ctypes.c_void_p()
         _check(_lib.vx_run_create(ctx.handle, ctypes.byref(problem.to_c()), ctypes.byref(h)))
         self._h = h
+        ctx._runs.add(self)
 
     @property
     def handle(self) -> ctypes.c_void_p:

@@ -62,6 +62,9 @@ vx::LaserSlabParams to_params(const vx_problem &p) {
     q.crit = p.crit;
     q.sizeWeight = p.sizeWeight;
     q.quadDepth = p.quadDepth;
+    q.bdens = p.bdens;
+    q.bp0 = p.bp0;
+    q.bTe = p.bTe;
     return q;
 }
 }  // namespace
@@ -96,6 +99,9 @@ void vx_problem_defaults(vx_problem *p) {
     p->sizeWeight = d.sizeWeight;
     p->quadDepth = d.quadDepth;
     p->precision = 64;
+    p->bdens = d.bdens;
+    p->bp0 = d.bp0;
+    p->bTe = d.bTe;
 }
 
 const char *vx_last_error(void) { return g_err.c_str(); }
@@ -116,7 +122,12 @@ int vx_ctx_create(int device, vx_ctx **out) {
 
 int vx_ctx_destroy(vx_ctx *ctx) {
     if (!ctx) return VX_ERR_INVALID;
-    return guard([&] { delete ctx; });
+    return guard([&] {
+        if (!ctx->eng->runs.empty())
+            throw std::invalid_argument("context still has " + std::to_string(ctx->eng->runs.size()) +
+                                        " run(s): destroy them first");
+        delete ctx;
+    });
 }
 
 int vx_ctx_sync(vx_ctx *ctx) {

@@ -50,6 +50,18 @@ Run::Run(Engine &e, std::shared_ptr<Problem> prob) : eng(e) {
     S.reset(new Settings(grid, particles, output, prob));
     rects.resize(S->q.size());
     for (auto &sp : rects) sp.resize(S->maxDepth + 1);
+    // Rectangle.cpp:94-101: weights onto the r sub-cells of a coarse cell
+    const int r = S->refinementRatio;
+    std::vector<double> w;
+    for (int i = 0; i < r; i++) {
+        double tl = -0.5 + i / (double)r;
+        double tr = -0.5 + (i + 1.0) / (double)r;
+        w.push_back((tl + tr) * 0.5);
+        w.push_back((tl * tl + tl * tr + tr * tr) / 3.0 - (1.0 / 12));
+        w.push_back((tl * tl * tl + tl * tl * tr + tl * tr * tr + tr * tr * tr) * 0.25);
+    }
+    drefc = DevBuf(w.size() * sizeof(double));
+    VX_CUDA(cudaMemcpy(drefc.p, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice));
 }
 
 Run::~Run() {
@@ -131,7 +143,20 @@ void Run::upload_rect_desc(Rect &r, int run_index) {
     double *cols = r.cols.as<double>();
     d.chargeR = cols;
     d.currentR = cols + (size_t)r.n_x * d.rtb;
-    d.relc = nullptr;
+    d.r = (int)s.refinementRatio;
+    d.relc = drelc.p ? drelc.as<double>() + relc_off[r.depth] : nullptr;
+    d.refc = drefc.as<double>();
+    if (r.masks.p) {
+        const size_t pe = r.plane_elems();
+        uint8_t *m = r.masks.as<uint8_t>();
+        d.nested = m;
+        d.ifx = m + pe;
+        d.ifp = m + 2 * pe;
+        d.has_iface = 1;
+    } else {
+        d.nested = d.ifx = d.ifp = nullptr;
+        d.has_iface = 0;
+    }
 }
 
 // Rectangle::InitializeDistribution, non-MKL quadrature (Rectangle.cpp:616-665), run on
@@ -240,11 +265,10 @@ void Run::upload_lu() {
                          dub_fcol.as<int>(), dub_fval.as<double>(), -1, nullptr, nullptr, nullptr, Ub.far_pre_col};
 }
 
-// SolverManager::SolverManager (SolverManager.cpp:8-26) for a hierarchy that starts and
-// stays at the base level (the only case before regridding support is added).
+// SolverManager::SolverManager (SolverManager.cpp:8-26): the base-level patch of every
+// species covering the whole domain.
 void Run::init() {
     const Settings &s = *S;
-    if (s.maxDepth != 0) throw std::invalid_argument("multi-level runs need the AMR build (not available)");
     for (size_t sp = 0; sp < rects.size(); sp++) {
         auto r = std::make_unique<Rect>();
         r->n_x = s.GetXSize(s.maxDepth);
@@ -260,6 +284,7 @@ void Run::init() {
         rects[sp][s.maxDepth].push_back(std::move(r));
     }
     alloc_fields();
+    build_amr();
     int info = lu.build(n);
     if (info) throw std::runtime_error("Poisson operator is singular");
     upload_lu();
@@ -274,22 +299,6 @@ void Run::enforce_neutralization() {
     launch_negate(F.neut, F.charge, n, eng.stream);
     VX_CUDA(cudaMemsetAsync(F.J, 0, (size_t)n * sizeof(double), eng.stream));
     eng.sync();
-}
-
-// Until coarse/fine machinery is present, every species must be one patch that covers
-// the whole domain, so that every ghost cell is a physical (zero) boundary cell
-// (BoundaryCondition.cpp:5-7).
-void Run::check_layout_supported() const {
-    for (auto &sp : rects) {
-        int count = 0;
-        for (auto &lvl : sp)
-            for (auto &r : lvl) {
-                count++;
-                if (!(r->up && r->down && r->left && r->right))
-                    throw std::invalid_argument("multi-patch layouts need the AMR build (not available)");
-            }
-        if (count != 1) throw std::invalid_argument("multi-patch layouts need the AMR build (not available)");
-    }
 }
 
 int64_t Run::state_size() const {
@@ -540,6 +549,66 @@ void Engine::build_set(LaunchSet &L) {
         sp[24] = dpsMax;
         spec.insert(spec.end(), sp.begin(), sp.end());
     }
+    // AMR op tables: batch b of the set = batch b of every run, patch ids made global
+    {
+        std::vector<GhostOp> g;
+        std::vector<IfaceOp> fo;
+        std::vector<CSyncOp> c;
+        size_t nbg = 0, nbi = 0, nbc = 0;
+        for (Run *R : L.runs) {
+            nbg = std::max(nbg, R->ghost_b.ptr.empty() ? 0 : R->ghost_b.ptr.size() - 1);
+            nbi = std::max(nbi, R->iface_b.ptr.empty() ? 0 : R->iface_b.ptr.size() - 1);
+            nbc = std::max(nbc, R->csync_b.ptr.empty() ? 0 : R->csync_b.ptr.size() - 1);
+        }
+        L.ghost_ptr.assign(1, 0);
+        L.iface_ptr.assign(1, 0);
+        L.csync_ptr.assign(1, 0);
+        for (size_t b = 0; b < nbg; b++) {
+            int base = 0;
+            for (Run *R : L.runs) {
+                if (b + 1 < R->ghost_b.ptr.size())
+                    for (int k = R->ghost_b.ptr[b]; k < R->ghost_b.ptr[b + 1]; k++) {
+                        GhostOp op = R->ghost_ops[k];
+                        op.dst += base;
+                        if (op.src >= 0) op.src += base;
+                        g.push_back(op);
+                    }
+                base += (int)R->flat.size();
+            }
+            L.ghost_ptr.push_back((int)g.size());
+        }
+        for (size_t b = 0; b < nbi; b++) {
+            int base = 0;
+            for (Run *R : L.runs) {
+                if (b + 1 < R->iface_b.ptr.size())
+                    for (int k = R->iface_b.ptr[b]; k < R->iface_b.ptr[b + 1]; k++) {
+                        IfaceOp op = R->iface_ops[k];
+                        op.coarse += base;
+                        op.fine += base;
+                        fo.push_back(op);
+                    }
+                base += (int)R->flat.size();
+            }
+            L.iface_ptr.push_back((int)fo.size());
+        }
+        for (size_t b = 0; b < nbc; b++) {
+            int base = 0;
+            for (Run *R : L.runs) {
+                if (b + 1 < R->csync_b.ptr.size())
+                    for (int k = R->csync_b.ptr[b]; k < R->csync_b.ptr[b + 1]; k++) {
+                        CSyncOp op = R->csync_ops[k];
+                        op.nb += base;
+                        op.caller += base;
+                        c.push_back(op);
+                    }
+                base += (int)R->flat.size();
+            }
+            L.csync_ptr.push_back((int)c.size());
+        }
+        L.dghost = upload(g, stream);
+        L.diface = upload(fo, stream);
+        L.dcsync = upload(c, stream);
+    }
     L.ntiles = (int)tiles.size();
     L.ncols = (int)colpatch.size();
     // lvl_ptr is absolute; lvl_off points at each run's block.
@@ -628,11 +697,22 @@ void Engine::record_step(LaunchSet &L) {
         launch_fct64_substep(fl, kSubGamma);
         launch_fct64_substep(fl, kSubFaces);
         launch_fct64_substep(fl, kSubFlux);
+        launches += 3;
+        for (size_t b = 0; b + 1 < L.iface_ptr.size(); b++, launches++)
+            launch_iface(L.dpatch.p, L.diface.as<IfaceOp>() + L.iface_ptr[b], L.iface_ptr[b + 1] - L.iface_ptr[b], s, stream);
         launch_fct64_substep(fl, kSubDsF2);
+        launches += 1;
+        for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
+            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 2, stream);
         launch_fct64_substep(fl, kSubLimR);
         launch_fct64_substep(fl, kSubLimC);
+        launches += 2;
+        for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++, launches++)
+            launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], stream);
         launch_fct64_substep(fl, kSubUpdate);
-        launches += 7;
+        launches += 1;
+        for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
+            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, stream);
         if (s == 5) {
             launch_fct64_substep(fl, kSubCopy10);
             launches += 1;

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "amr.hpp"
 #include "poisson_lu.hpp"
 #include "settings.hpp"
 #include "vx_kernels.hpp"
@@ -53,6 +54,15 @@ struct Rect {
     DevBuf masks;  // nested, ifx, ifp (AMR only)
     PatchT<double> desc{};
     size_t plane_elems() const { return (size_t)(n_x + 4) * pitch; }
+    // Connectivity (Rectangle.hpp:8-12): neighbour patch ids (flat index within the run)
+    // or -1 for the domain boundary; "same level" flags; per-cell/face finer patch ids and
+    // the nested / interface masks, indexed (i+2)*(n_p+4) + (j+2) as IndexNS.
+    int id = -1;
+    std::vector<int> xm, xp, pm, pp;
+    std::vector<char> sxm, sxp, spm, spp;
+    std::vector<int> finer, finer_x, finer_p;
+    std::vector<uint8_t> nested, ifx, ifp;
+    int ns(int i, int j) const { return (i + 2) * (n_p + 4) + (j + 2); }
 };
 
 class Engine;
@@ -96,7 +106,20 @@ public:
     void alloc_fields();
     void upload_lu();
     void enforce_neutralization();
-    void check_layout_supported() const;
+    // AMR: flat patch list (species -> depth -> patch), connectivity and op lists.
+    std::vector<Rect *> flat;
+    std::vector<GhostOp> ghost_ops;
+    Batched ghost_b;
+    std::vector<CSyncOp> csync_ops;
+    Batched csync_b;
+    std::vector<IfaceOp> iface_ops;
+    Batched iface_b;
+    DevBuf drelc;                   // sub-cell interpolation weights per depth
+    DevBuf drefc;                   // coarse-to-fine interpolation weights (refinement ratio)
+    std::vector<int> relc_off;      // offset of depth d's weights in drelc
+    bool multi_patch = false;
+    void build_amr();               // connectivity + op lists + masks for the current layout
+    void validate_ops() const;      // bounds of every op against its patches
     int64_t state_size() const;
     void step_host(const double *in, double *out, double dt);
     void state_to_host(double *out);
@@ -112,6 +135,9 @@ struct LaunchSet {
     int ntiles = 0, ncols = 0, maxnp = 0, maxn = 0, maxnf = 0;
     std::vector<double> hparams;  // per run: 6 stages x (8 fct + 8 maxwell + 2 laser)
     std::vector<double> w, fcoef;
+    // AMR op tables of all runs, batch by batch (global patch ids)
+    DevBuf dghost, diface, dcsync;
+    std::vector<int> ghost_ptr, iface_ptr, csync_ptr;
     cudaGraphExec_t graph = nullptr;
     ~LaunchSet();
 };

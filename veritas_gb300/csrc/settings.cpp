@@ -115,6 +115,8 @@ void LaserSlab::settingsOverride(Settings &s) {
     s.tempEM.resize(2, 0.0);
     s.tempEM[0] = P.lambda;
     s.tempEM[1] = P.a0 * mc / std::fabs(s.q[0]);
+    beam_T = s.m[0] * (P.bTe * kKeV);
+    beam_p = P.bp0 * mc;
 }
 
 double LaserSlab::slab_density(double xl) const {
@@ -130,7 +132,12 @@ double LaserSlab::slab_density(double xl) const {
 double LaserSlab::InitialDistribution(const Settings &s, double x, double p, int particleType) const {
     double ne = s.temp[particleType][0] * slab_density(x / P.lambda);
     double dpv = p - s.temp[particleType][2];
-    return ne * std::exp(-(dpv * dpv) / (2.0 * s.temp[particleType][1])) / std::sqrt(kDPI * s.temp[particleType][1]);
+    double v = ne * std::exp(-(dpv * dpv) / (2.0 * s.temp[particleType][1])) / std::sqrt(kDPI * s.temp[particleType][1]);
+    if (P.bdens != 0.0) {  // second, drifting population with its own temperature
+        double dbv = p - beam_p;
+        v += P.bdens * ne * std::exp(-(dbv * dbv) / (2.0 * beam_T)) / std::sqrt(kDPI * beam_T);
+    }
+    return v;
 }
 
 double LaserSlab::GetBY(const Settings &s, double x, double t) const { return 0.0; }

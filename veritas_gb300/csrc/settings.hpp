@@ -67,6 +67,7 @@ struct LaserSlabParams {
     double a0 = 1.0, fwhm = 10.0, delay = 10.0;
     double cfl = 0.5, minEff = 0.75, crit = 1e-6, sizeWeight = 1.0;
     int quadDepth = 2;
+    double bdens = 0.0, bp0 = 0.0, bTe = 1.0;  // beam population: density fraction, drift, keV
 };
 
 class LaserSlab : public Problem {
@@ -83,6 +84,7 @@ public:
     bool HasRefinementOverride() const override { return false; }
     double slab_density(double xl) const;
     LaserSlabParams P;
+    double beam_T = 0.0, beam_p = 0.0;  // beam temperature [J] and drift [kg m/s]
 };
 
 class Settings {  // Settings.hpp:35-65

@@ -130,7 +130,10 @@ void Run::load_state(const std::string &path) {
         }
     }
     rects = std::move(nr);
-    check_layout_supported();
+    build_amr();
+    for (auto &sp : rects)
+        for (auto &lvl : sp)
+            for (auto &rp : lvl) upload_rect_desc(*rp, 0);
     layout_version++;
     eng.refresh_efield(*this);
     eng.sync();

@@ -49,6 +49,7 @@ struct PatchT {
     int xm, xp, pm, pp;     // active face window [xm,xp) x [pm,pp) (Rectangle.cpp:1257-1261)
     int run, species;
     int has_iface;          // any coarse/fine interface face on this patch
+    int r;                  // refinement ratio
     double dx, dp, dx_inv, dp_inv;
     double pmin, q, qq, mass, cc, g2;  // qq=q*q, cc=cs*cs*m, g2=(m_inv*c_inv)^2
     T *f0, *f1, *f2;
@@ -62,6 +63,7 @@ struct PatchT {
     uint8_t *ifx, *ifp;     // is_interrior_level_boundary_x / _p
     double *chargeR, *currentR;  // per finest column of this patch (n_x * rtb)
     const double *relc;     // interpolation weights onto the rtb finest sub-cells, 3*rtb
+    const double *refc;     // interpolation weights onto the r sub-cells of a coarse cell, 3*r
 };
 
 // Per-run field block on the device (EMSolver state, EMSolver.hpp:9-49).

@@ -131,6 +131,14 @@ void launch_cfl(const CflLaunch &L);
 // FP64 FMA throughput probe: blocks x threads threads, iters x 8 independent DFMA each.
 void launch_fp64_peak(double *out, int blocks, int threads, int iters, cudaStream_t s);
 
+// AMR op batches (amr.hpp, amr64.cu)
+struct GhostOp;
+struct IfaceOp;
+struct CSyncOp;
+void launch_ghost(const void *patches, const GhostOp *ops, int n, int slot, cudaStream_t s);
+void launch_iface(const void *patches, const IfaceOp *ops, int n, int step, cudaStream_t s);
+void launch_csync(const void *patches, const CSyncOp *ops, int n, cudaStream_t s);
+
 // dst[i] = -src[i]
 void launch_negate(double *dst, const double *src, int n, cudaStream_t s);
 
