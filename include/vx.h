@@ -84,6 +84,31 @@ int vx_run_calculate_dt(vx_run *run, double *dt);
 /* SolverManager::Advance (SolverManager.cpp:28-39): one six-stage RK step of every
  * species and the fields.  Asynchronous on the context stream. */
 int vx_run_advance(vx_run *run, double dt);
+/* SolverManager::AdvanceFields (SolverManager.cpp:41-46): the six Maxwell stages only
+ * (the reference driver's warm-up before the plasma is switched on). */
+int vx_run_advance_fields(vx_run *run, double dt);
+/* SolverManager::reGrid (SolverManager.cpp:48-57 -> Mesh::updateHierarchy,
+ * Mesh.cpp:132-208): flag cells, re-cluster every level, move f to the new patches. */
+int vx_run_regrid(vx_run *run);
+/* Patches of the current hierarchy: writes up to cap records of 6 ints
+ * (species, depth, x_pos, p_pos, n_x, n_p) in the reference's level order; *count
+ * receives the total. */
+int vx_run_layout(vx_run *run, int32_t *out, int cap, int *count);
+/* Rectangle error weights (Rectangle.cpp:68-74) of a patch at `depth` and the
+ * refinement criterion: a cell is flagged when
+ *   w[0]|f(i+1,j)-f(i-1,j)| + w[1]|f(i,j+1)-f(i,j-1)| + w[2]|f(i+1,j)-2f(i,j)+f(i-1,j)|
+ *   + w[3]|f(i,j+1)-2f(i,j)+f(i,j-1)| + w[4]|f(i,j)| > crit   (Rectangle.hpp:128-130).
+ * Host only. */
+int vx_error_weights(const vx_problem *prob, int species, int depth, double *w5, double *crit);
+/* Mesh::updateHierarchy's clustering and Mesh::promoteHierarchyToMesh's patch geometry
+ * (Mesh.cpp:132-208, 297-792, 803-826) on the host, without any device state.  patches:
+ * npatches records (depth, x_pos, p_pos, n_x, n_p) of one species in level order;
+ * flag_ptr[npatches + 1] / flag_ij: the flagged cells (i, j) of each patch in global
+ * level coordinates, in Rectangle::getError order.  out receives up to cap records
+ * (depth, x_pos, p_pos, n_x, n_p, up, down, left, right) of the new hierarchy; *count
+ * the total. */
+int vx_update_hierarchy(const vx_problem *prob, int species, const int32_t *patches, int npatches,
+                        const int32_t *flag_ptr, const int32_t *flag_ij, int32_t *out, int cap, int *count);
 /* Advance several runs of one context together, one launch per sub-step for all of
  * them (batched form).  dt[i] belongs to runs[i]. */
 int vx_runs_advance(vx_run *const *runs, const double *dt, int nruns);

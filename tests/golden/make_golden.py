@@ -50,6 +50,15 @@ CASES = {
 }
 
 
+# name -> regrid interval for the regrid fixtures of that case: the state just before
+# SolverManager::reGrid ("_pre"), just after it ("_post") and one step later ("_post1").
+REGRID = {
+    "amr2": 4,
+    "beam2": 4,
+    "beam3": 4,
+}
+
+
 def run_case(exe: Path, name: str, args: list[str], steps: int, keep: list[int]) -> None:
     with tempfile.TemporaryDirectory() as td:
         env = dict(os.environ, OMP_NUM_THREADS="4")
@@ -61,6 +70,16 @@ def run_case(exe: Path, name: str, args: list[str], steps: int, keep: list[int])
     (HERE / f"{name}.args").write_text(" ".join(args) + "\n")
 
 
+def run_regrid(exe: Path, name: str, args: list[str], every: int) -> None:
+    with tempfile.TemporaryDirectory() as td:
+        env = dict(os.environ, OMP_NUM_THREADS="4")
+        cmd = [str(exe), *args, f"steps={every + 1}", f"regrid_every={every}", "dump_every=1", f"dumpdir={td}"]
+        subprocess.run(cmd, check=True, env=env, stdout=subprocess.DEVNULL)
+        vxstate.to_npz(vxstate.read_state(Path(td) / f"state_{every:05d}.bin"), HERE / f"{name}_pre.npz")
+        vxstate.to_npz(vxstate.read_state(Path(td) / f"regrid_{every:05d}.bin"), HERE / f"{name}_post.npz")
+        vxstate.to_npz(vxstate.read_state(Path(td) / f"state_{every + 1:05d}.bin"), HERE / f"{name}_post1.npz")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -70,6 +89,9 @@ def main() -> None:
     for name, (args, steps, keep) in CASES.items():
         run_case(exe, name, args, steps, keep)
         print("wrote", name)
+    for name, every in REGRID.items():
+        run_regrid(exe, name, CASES[name][0], every)
+        print("wrote", name, "regrid")
 
 
 if __name__ == "__main__":

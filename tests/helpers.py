@@ -37,6 +37,10 @@ def golden(name: str, step: int) -> dict:
     return vxstate.from_npz(GOLDEN / f"{name}_s{step}.npz")
 
 
+def golden_named(name: str, tag: str) -> dict:
+    return vxstate.from_npz(GOLDEN / f"{name}_{tag}.npz")
+
+
 def compare_states(got: dict, ref: dict, tol: float) -> dict:
     """Relative L-inf errors of f (slots 0 and 1, whole padded block) and the fields."""
     err = {}
@@ -45,7 +49,7 @@ def compare_states(got: dict, ref: dict, tol: float) -> dict:
         for lg, lr in zip(sg, sr):
             assert len(lg) == len(lr)
             for rg, rr in zip(lg, lr):
-                for k in ("x_pos", "p_pos", "n_x", "n_p", "depth"):
+                for k in ("x_pos", "p_pos", "n_x", "n_p", "depth", "up", "down", "left", "right"):
                     assert rg[k] == rr[k], k
                 for slot in (0, 1):
                     e = vxstate.rel_linf(rg["f"][..., slot], rr["f"][..., slot])

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import vxstate
-from helpers import compare_states, golden, problem_for, total_mass
+from helpers import compare_states, golden, golden_named, problem_for, total_mass
 
 TOL = 1e-10
 ONE_STEP = [("slab64", 0), ("slab64", 1), ("drift128", 0), ("edge64", 0),
@@ -78,6 +78,42 @@ def test_initialisation_matches_reference(ctx, tmp_path):
     ref = golden("slab64", 0)
     assert np.array_equal(got["species"][0][0][0]["f"][..., :2], ref["species"][0][0][0]["f"][..., :2])
     assert vxstate.rel_linf(got["neut"], ref["neut"]) <= 1e-14
+    s.close()
+
+
+def _check(got, ref, label):
+    err = compare_states(got, ref, TOL)
+    print(label, {kk: f"{v:.2e}" for kk, v in err.items()})
+    for kk, v in err.items():
+        assert v <= TOL, (kk, v)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["amr2", "beam2", "beam3"])
+def test_initial_hierarchy_matches_reference(ctx, tmp_path, name):
+    """Mesh::Mesh: base level, maxDepth rounds of flagging / clustering with every patch
+    from the quadrature, then the ghost fill and the neutralising charge."""
+    s = _solver(ctx, name)
+    s.save_state(tmp_path / "init.bin")
+    _check(vxstate.read_state(tmp_path / "init.bin"), golden(name, 0), name + " init")
+    s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["amr2", "beam2", "beam3"])
+def test_regrid_matches_reference(ctx, tmp_path, name):
+    """SolverManager::reGrid on the reference's state: the new layout, the transferred
+    f (slots 0 and 1, ghosts included), then one step on the new layout."""
+    s = _solver(ctx, name)
+    vxstate.write_state(golden_named(name, "pre"), tmp_path / "pre.bin")
+    s.load_state(tmp_path / "pre.bin")
+    s.reGrid()
+    s.save_state(tmp_path / "post.bin")
+    _check(vxstate.read_state(tmp_path / "post.bin"), golden_named(name, "post"), name + " regrid")
+    ref1 = golden_named(name, "post1")
+    s.Advance(ref1["dt"])
+    s.save_state(tmp_path / "post1.bin")
+    _check(vxstate.read_state(tmp_path / "post1.bin"), ref1, name + " step after regrid")
     s.close()
 
 

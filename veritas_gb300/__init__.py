@@ -68,6 +68,14 @@ def _load() -> ctypes.CDLL:
         "vx_run_calculate_dt": (ctypes.c_int, [vp, P(ctypes.c_double)]),
         "vx_run_advance": (ctypes.c_int, [vp, ctypes.c_double]),
         "vx_runs_advance": (ctypes.c_int, [P(vp), P(ctypes.c_double), ctypes.c_int]),
+        "vx_run_advance_fields": (ctypes.c_int, [vp, ctypes.c_double]),
+        "vx_run_regrid": (ctypes.c_int, [vp]),
+        "vx_error_weights": (ctypes.c_int, [P(_Problem), ctypes.c_int, ctypes.c_int, P(ctypes.c_double),
+                                             P(ctypes.c_double)]),
+        "vx_update_hierarchy": (ctypes.c_int, [P(_Problem), ctypes.c_int, P(ctypes.c_int32), ctypes.c_int,
+                                                P(ctypes.c_int32), P(ctypes.c_int32), P(ctypes.c_int32), ctypes.c_int,
+                                                P(ctypes.c_int)]),
+        "vx_run_layout": (ctypes.c_int, [vp, P(ctypes.c_int32), ctypes.c_int, P(ctypes.c_int)]),
         "vx_run_time": (ctypes.c_int, [vp, P(ctypes.c_double)]),
         "vx_run_cell_count": (ctypes.c_int, [vp, P(ctypes.c_int64)]),
         "vx_run_load_state": (ctypes.c_int, [vp, ctypes.c_char_p]),
@@ -230,6 +238,20 @@ class SolverManager:
     def Advance(self, dt: float) -> None:
         _check(_lib.vx_run_advance(self._h, float(dt)))
 
+    def AdvanceFields(self, dt: float) -> None:
+        _check(_lib.vx_run_advance_fields(self._h, float(dt)))
+
+    def reGrid(self) -> None:
+        _check(_lib.vx_run_regrid(self._h))
+
+    def layout(self) -> list[tuple[int, int, int, int, int, int]]:
+        """(species, depth, x_pos, p_pos, n_x, n_p) of every patch, in level order."""
+        cnt = ctypes.c_int()
+        _check(_lib.vx_run_layout(self._h, None, 0, ctypes.byref(cnt)))
+        buf = (ctypes.c_int32 * max(1, 6 * cnt.value))()
+        _check(_lib.vx_run_layout(self._h, buf, cnt.value, ctypes.byref(cnt)))
+        return [tuple(buf[6 * k:6 * k + 6]) for k in range(cnt.value)]
+
     @property
     def time(self) -> float:
         v = ctypes.c_double()
@@ -285,6 +307,35 @@ class SolverManager:
             self.close()
         except Exception:
             pass
+
+
+def error_weights(problem: Problem, species: int, depth: int) -> tuple[list[float], float]:
+    """Rectangle error weights and refinement criterion (host only)."""
+    w = (ctypes.c_double * 5)()
+    crit = ctypes.c_double()
+    _check(_lib.vx_error_weights(ctypes.byref(problem.to_c()), species, depth, w, ctypes.byref(crit)))
+    return list(w), float(crit.value)
+
+
+def update_hierarchy(problem: Problem, species: int, patches: list, flags: list) -> list[tuple]:
+    """Mesh::updateHierarchy clustering on the host.
+
+    patches: [(depth, x_pos, p_pos, n_x, n_p)] in level order; flags: per patch a list of
+    flagged (i, j) in global level coordinates.  Returns the new patches as
+    (depth, x_pos, p_pos, n_x, n_p, up, down, left, right)."""
+    n = len(patches)
+    pa = (ctypes.c_int32 * (5 * n))(*[v for p in patches for v in p])
+    ptr = [0]
+    for f in flags:
+        ptr.append(ptr[-1] + len(f))
+    fp = (ctypes.c_int32 * (n + 1))(*ptr)
+    fij = (ctypes.c_int32 * max(1, 2 * ptr[-1]))(*[v for f in flags for c in f for v in c])
+    cnt = ctypes.c_int()
+    _check(_lib.vx_update_hierarchy(ctypes.byref(problem.to_c()), species, pa, n, fp, fij, None, 0, ctypes.byref(cnt)))
+    out = (ctypes.c_int32 * max(1, 9 * cnt.value))()
+    _check(_lib.vx_update_hierarchy(ctypes.byref(problem.to_c()), species, pa, n, fp, fij, out, cnt.value,
+                                    ctypes.byref(cnt)))
+    return [tuple(out[9 * k:9 * k + 9]) for k in range(cnt.value)]
 
 
 class PinnedArray:

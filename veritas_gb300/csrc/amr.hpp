@@ -51,6 +51,29 @@ struct IfaceOp {
     int fine, fi, fj;
 };
 
+// Error flags of one patch (Rectangle::getError): local cells [i0,i1) x [j0,j1) are
+// tested against crit with the patch's five error weights; out_off locates the patch's
+// n_x * n_p flag bytes.
+struct FlagPatch {
+    int patch;
+    int i0, i1, j0, j1;
+    long long out_off;
+    double w[5];
+    double crit;
+};
+
+// Regrid data transfer (Rectangle.cpp:892-1128) over the cells [i0,i1) x [j0,j1) of the
+// source's level (coarse cells for the interpolating kinds): new patch `dst`, source
+// patch `src`, (x2, p2) the dst position in source-level cells; mask_off locates dst's
+// is_interpolated bytes.
+enum XferKind : int { kXferInterp = 0, kXferCopy = 1, kXferInterpMissing = 2 };
+struct XferOp {
+    int kind, dst, src;
+    int i0, i1, j0, j1;
+    int x2, p2;
+    long long mask_off;
+};
+
 struct Batched {
     std::vector<int> ptr;  // batch b = ops[ptr[b] .. ptr[b+1])
 };

@@ -34,26 +34,29 @@ __device__ __forceinline__ void interp_ref(const double *c, int r, double f1, do
 
 constexpr int kMaxR = 8;
 
-// Rectangle::GetWenoValueFromCoarseLevel (Rectangle.cpp:343-415): entry `sub` of the
-// corrected r x r interpolants of coarse cell (ic, jc).
-__device__ double coarse_interp(const P64 &C, const double *f, int ic, int jc, int sub) {
+// Rectangle::GetWenoValueFromCoarseLevel (Rectangle.cpp:343-415): the corrected r x r
+// interpolants of coarse cell (ic, jc), out[kx * r + kp] for x sub-cell kx, p sub-cell kp.
+__device__ void interp_block(const P64 &C, const double *f, int ic, int jc, double *out) {
     const int r = C.r;
     const int pit = C.pitch;
     double temps[5][kMaxR];
     for (int k = -2; k < 3; k++)
         interp_ref(C.refc, r, f[pidx(ic - 2, jc + k, pit)], f[pidx(ic - 1, jc + k, pit)], f[pidx(ic, jc + k, pit)],
                    f[pidx(ic + 1, jc + k, pit)], f[pidx(ic + 2, jc + k, pit)], temps[k + 2]);
-    double sum = 0.0, want = 0.0;
+    double sum = 0.0;
     for (int k = 0; k < r; k++) {
-        double part[kMaxR];
-        interp_ref(C.refc, r, temps[0][k], temps[1][k], temps[2][k], temps[3][k], temps[4][k], part);
-        for (int l = 0; l < r; l++) {
-            sum += part[l];
-            if (k * r + l == sub) want = part[l];
-        }
+        interp_ref(C.refc, r, temps[0][k], temps[1][k], temps[2][k], temps[3][k], temps[4][k], out + k * r);
+        for (int l = 0; l < r; l++) sum += out[k * r + l];
     }
     double correction = f[pidx(ic, jc, pit)] - 1.0 / pow((double)r, 2.0) * sum;
-    return want + correction;
+    for (int q = 0; q < r * r; q++) out[q] += correction;
+}
+
+// Entry `sub` of interp_block.
+__device__ double coarse_interp(const P64 &C, const double *f, int ic, int jc, int sub) {
+    double out[kMaxR * kMaxR];
+    interp_block(C, f, ic, jc, out);
+    return out[sub];
 }
 
 __global__ void k_ghost(const P64 *patches, const GhostOp *ops, int n, int slot) {
@@ -177,6 +180,75 @@ __global__ void k_csync(const P64 *patches, const CSyncOp *ops, int n) {
         for (int q = 0; q < r; q++) RC[xf ? cid + q : cid + q * R.pitch] = v;
         NC[nid] = v;
     }
+}
+
+// Rectangle::getError (Rectangle.cpp:866-890) with ErrorEstimate (Rectangle.hpp:128-130)
+// on f slot 1; one flag byte per interior cell, zero outside the tested range.
+__global__ void k_flags(const P64 *patches, const FlagPatch *fps, uint8_t *out) {
+    const FlagPatch fp = fps[blockIdx.y];
+    const P64 &P = patches[fp.patch];
+    const int pit = P.pitch;
+    const double *f = P.f1;
+    const long long cells = (long long)P.nx * P.np;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < cells; c += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(c / P.np), j = (int)(c - (long long)i * P.np);
+        uint8_t flag = 0;
+        if (i >= fp.i0 && i < fp.i1 && j >= fp.j0 && j < fp.j1) {
+            const double c0 = f[pidx(i, j, pit)];
+            const double xp = f[pidx(i + 1, j, pit)], xm = f[pidx(i - 1, j, pit)];
+            const double pp = f[pidx(i, j + 1, pit)], pm = f[pidx(i, j - 1, pit)];
+            const double e = fp.w[0] * fabs(xp - xm) + fp.w[1] * fabs(pp - pm) + fp.w[2] * fabs(xp - 2 * c0 + xm) +
+                             fp.w[3] * fabs(pp - 2 * c0 + pm) + fp.w[4] * fabs(c0);
+            flag = e > fp.crit ? 1 : 0;
+        }
+        out[fp.out_off + c] = flag;
+    }
+}
+
+// Regrid transfer (Rectangle.cpp:892-941, 1100-1128): slots 0 and 1 of the new patch
+// from slot 1 of the source.
+__global__ void k_xfer(const P64 *patches, const XferOp *ops, uint8_t *mask) {
+    const XferOp op = ops[blockIdx.y];
+    const P64 &D = patches[op.dst];
+    const P64 &S = patches[op.src];
+    const int w = op.j1 - op.j0;
+    const long long cells = (long long)(op.i1 - op.i0) * w;
+    const int dpit = D.pitch;
+    const int mpit = D.np + 4;  // IndexNS pitch
+    uint8_t *m = mask + op.mask_off;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < cells; c += (long long)gridDim.x * blockDim.x) {
+        const int i = op.i0 + (int)(c / w), j = op.j0 + (int)(c % w);
+        if (op.kind == kXferCopy) {
+            const int di = i - op.x2, dj = j - op.p2;
+            const double v = S.f1[pidx(i - S.x_pos, j - S.p_pos, S.pitch)];
+            D.f0[pidx(di, dj, dpit)] = v;
+            D.f1[pidx(di, dj, dpit)] = v;
+            m[(di + 2) * mpit + (dj + 2)] = 1;
+            continue;
+        }
+        const int r = S.r;
+        const int bi = (i - op.x2) * r, bj = (j - op.p2) * r;
+        if (op.kind == kXferInterpMissing && m[(bi + 1 + 2) * mpit + (bj + 1 + 2)]) continue;
+        double out[kMaxR * kMaxR];
+        interp_block(S, S.f1, i - S.x_pos, j - S.p_pos, out);
+        for (int k = 0; k < r; k++)
+            for (int l = 0; l < r; l++) {
+                const int id = pidx(bi + k, bj + l, dpit);
+                D.f0[id] = out[l + r * k];
+                D.f1[id] = D.f0[id];
+                if (op.kind == kXferInterp) m[(bi + k + 2) * mpit + (bj + l + 2)] = 1;
+            }
+    }
+}
+
+void launch_flags(const void *patches, const FlagPatch *fp, int n, uint8_t *out, cudaStream_t s) {
+    if (n <= 0) return;
+    k_flags<<<dim3(64, n), 256, 0, s>>>((const P64 *)patches, fp, out);
+}
+
+void launch_xfer(const void *patches, const XferOp *ops, int n, uint8_t *mask, cudaStream_t s) {
+    if (n <= 0) return;
+    k_xfer<<<dim3(16, n), 256, 0, s>>>((const P64 *)patches, ops, mask);
 }
 
 void launch_ghost(const void *patches, const GhostOp *ops, int n, int slot, cudaStream_t s) {

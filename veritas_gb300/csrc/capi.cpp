@@ -67,6 +67,15 @@ vx::LaserSlabParams to_params(const vx_problem &p) {
     q.bTe = p.bTe;
     return q;
 }
+
+std::unique_ptr<vx::Settings> host_settings(const vx_problem &p) {
+    auto prob = std::make_shared<vx::LaserSlab>(to_params(p));
+    vx::Input grid;
+    vx::Particles particles;
+    vx::Output output;
+    prob->initialConditions(grid, particles, output);
+    return std::unique_ptr<vx::Settings>(new vx::Settings(grid, particles, output, prob));
+}
 }  // namespace
 
 extern "C" {
@@ -170,6 +179,99 @@ int vx_run_calculate_dt(vx_run *run, double *dt) {
 int vx_run_advance(vx_run *run, double dt) {
     if (!run || !(dt >= 0)) return VX_ERR_INVALID;
     return guard([&] { run->run->advance(dt); });
+}
+
+int vx_run_advance_fields(vx_run *run, double dt) {
+    if (!run || !(dt >= 0)) return VX_ERR_INVALID;
+    return guard([&] { run->run->advance_fields(dt); });
+}
+
+int vx_run_regrid(vx_run *run) {
+    if (!run) return VX_ERR_INVALID;
+    return guard([&] { run->run->regrid(false); });
+}
+
+int vx_run_layout(vx_run *run, int32_t *out, int cap, int *count) {
+    if (!run || !count || cap < 0 || (cap > 0 && !out)) return VX_ERR_INVALID;
+    return guard([&] {
+        int k = 0;
+        for (auto &sp : run->run->rects)
+            for (auto &lvl : sp)
+                for (auto &r : lvl) {
+                    if (k < cap) {
+                        int32_t *o = out + 6 * k;
+                        o[0] = r->species;
+                        o[1] = r->depth;
+                        o[2] = r->x_pos;
+                        o[3] = r->p_pos;
+                        o[4] = r->n_x;
+                        o[5] = r->n_p;
+                    }
+                    k++;
+                }
+        *count = k;
+    });
+}
+
+int vx_error_weights(const vx_problem *prob, int species, int depth, double *w5, double *crit) {
+    if (!prob || !w5 || !crit) return VX_ERR_INVALID;
+    return guard([&] {
+        auto S = host_settings(*prob);
+        if (species < 0 || species >= (int)S->q.size() || depth < 0 || depth > S->maxDepth)
+            throw std::invalid_argument("species or depth out of range");
+        vx::error_weights(*S, depth, species, w5);
+        *crit = S->refinementCriteria;
+    });
+}
+
+int vx_update_hierarchy(const vx_problem *prob, int species, const int32_t *patches, int npatches,
+                        const int32_t *flag_ptr, const int32_t *flag_ij, int32_t *out, int cap, int *count) {
+    if (!prob || !patches || npatches <= 0 || !flag_ptr || !count || cap < 0 || (cap > 0 && !out))
+        return VX_ERR_INVALID;
+    return guard([&] {
+        auto S = host_settings(*prob);
+        const vx::Settings &s = *S;
+        if (species < 0 || species >= (int)s.q.size()) throw std::invalid_argument("species out of range");
+        std::vector<vx::Run::BoxList> H;
+        std::vector<std::vector<int>> at_depth(s.maxDepth + 1);
+        for (int k = 0; k < npatches; k++) {
+            const int32_t *r = patches + 5 * k;
+            if (r[0] < 0 || r[0] > s.maxDepth) throw std::invalid_argument("patch depth out of range");
+            if (flag_ptr[k + 1] < flag_ptr[k]) throw std::invalid_argument("flag_ptr must not decrease");
+            at_depth[r[0]].push_back(k);
+        }
+        if (flag_ptr[0] != 0 || (flag_ptr[npatches] > 0 && !flag_ij)) throw std::invalid_argument("bad flag list");
+        for (int d = s.maxDepth; d >= 0 && !at_depth[d].empty(); d--) {
+            vx::Run::BoxList b;
+            for (int k : at_depth[d]) {
+                const int32_t *r = patches + 5 * k;
+                b.push_back({{r[1], r[2]}, {r[1] + r[3], r[2] + r[4]}});
+            }
+            H.push_back(b);
+        }
+        if (H.empty()) throw std::invalid_argument("no base-level patch");
+        auto level_flags = [&](int l) {
+            std::vector<std::pair<int, int>> f;
+            for (int k : at_depth[s.maxDepth - l])
+                for (int q = flag_ptr[k]; q < flag_ptr[k + 1]; q++) f.push_back({flag_ij[2 * q], flag_ij[2 * q + 1]});
+            return f;
+        };
+        auto geo = vx::promote_geometry(s, species, vx::update_hierarchy(s, species, H, level_flags));
+        for (size_t k = 0; k < geo.size() && (int)k < cap; k++) {
+            int32_t *o = out + 9 * k;
+            const vx::PatchGeom &g = geo[k];
+            o[0] = g.depth;
+            o[1] = g.x_pos;
+            o[2] = g.p_pos;
+            o[3] = g.n_x;
+            o[4] = g.n_p;
+            o[5] = g.up;
+            o[6] = g.down;
+            o[7] = g.left;
+            o[8] = g.right;
+        }
+        *count = (int)geo.size();
+    });
 }
 
 int vx_runs_advance(vx_run *const *runs, const double *dt, int nruns) {

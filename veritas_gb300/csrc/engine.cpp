@@ -34,13 +34,6 @@ DevBuf &DevBuf::operator=(DevBuf &&o) noexcept {
     return *this;
 }
 
-template <class T>
-static DevBuf upload(const std::vector<T> &v, cudaStream_t s) {
-    DevBuf b(std::max<size_t>(v.size() * sizeof(T), sizeof(T)));
-    if (!v.empty()) VX_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-    return b;
-}
-
 // ---------------------------------------------------------------- Run
 Run::Run(Engine &e, std::shared_ptr<Problem> prob) : eng(e) {
     Input grid;
@@ -265,26 +258,22 @@ void Run::upload_lu() {
                          dub_fcol.as<int>(), dub_fval.as<double>(), -1, nullptr, nullptr, nullptr, Ub.far_pre_col};
 }
 
-// SolverManager::SolverManager (SolverManager.cpp:8-26): the base-level patch of every
-// species covering the whole domain.
+// SolverManager::SolverManager (SolverManager.cpp:8-26).  Mesh::Mesh (Mesh.cpp:8-50):
+// the base level alone (the reference's initial flagging adds nothing here, its
+// non-MKL branch collects no cells), then maxDepth rounds of ghost fill + regrid with
+// every new patch set from the quadrature.  Then the field solver and neutralisation.
 void Run::init() {
     const Settings &s = *S;
-    for (size_t sp = 0; sp < rects.size(); sp++) {
-        auto r = std::make_unique<Rect>();
-        r->n_x = s.GetXSize(s.maxDepth);
-        r->n_p = s.GetPSize(s.maxDepth, (int)sp);
-        r->x_pos = 0;
-        r->p_pos = 0;
-        r->depth = s.maxDepth;
-        r->up = r->down = r->left = r->right = true;
-        r->species = (int)sp;
-        allocate_rect(*r);
-        upload_rect_desc(*r, 0);
-        init_rect_distribution(*r);
-        rects[sp][s.maxDepth].push_back(std::move(r));
+    std::vector<std::vector<BoxList>> hier(rects.size());
+    for (size_t sp = 0; sp < rects.size(); sp++)
+        hier[sp] = {BoxList{{{0, 0}, {s.GetXSize(s.maxDepth), s.GetPSize(s.maxDepth, (int)sp)}}}};
+    promote(hier, true);
+    for (int i = 0; i < s.maxDepth; i++) {
+        push_data(1);
+        regrid(true);
     }
     alloc_fields();
-    build_amr();
+    push_data(1);
     int info = lu.build(n);
     if (info) throw std::runtime_error("Poisson operator is singular");
     upload_lu();
@@ -360,6 +349,8 @@ void Run::state_to_host(double *out) {
 double Run::calculate_dt() { return eng.calculate_dt({this})[0]; }
 
 void Run::advance(double dt) { eng.advance({this}, {dt}); }
+
+void Run::advance_fields(double dt) { eng.advance_fields({this}, {dt}); }
 
 // ---------------------------------------------------------------- LaunchSet / Engine
 LaunchSet::~LaunchSet() {
@@ -724,9 +715,9 @@ void Engine::record_step(LaunchSet &L) {
     launches_per_step_ = launches;
 }
 
-void Engine::advance(const std::vector<Run *> &set, const std::vector<double> &dt) {
-    LaunchSet &L = get_set(set);
-    // Host-side stage parameters (dt-scaled tableau, laser boundary values).
+// Host-side stage parameters (dt-scaled tableau, laser boundary values) of one step of
+// every run of the set; advances each run's time through Settings::UpdateTime.
+void Engine::fill_params(LaunchSet &L, const std::vector<Run *> &set, const std::vector<double> &dt) {
     for (size_t ri = 0; ri < set.size(); ri++) {
         Run &R = *set[ri];
         Settings &s = *R.S;
@@ -765,6 +756,11 @@ void Engine::advance(const std::vector<Run *> &set, const std::vector<double> &d
     }
     VX_CUDA(cudaMemcpyAsync(L.dparams.p, L.hparams.data(), L.hparams.size() * sizeof(double), cudaMemcpyHostToDevice,
                             stream));
+}
+
+void Engine::advance(const std::vector<Run *> &set, const std::vector<double> &dt) {
+    LaunchSet &L = get_set(set);
+    fill_params(L, set, dt);
     if (use_graphs) {
         if (!L.graph) {
             cudaGraph_t g;
@@ -814,6 +810,26 @@ void Engine::refresh_efield(Run &run) {
 }
 
 // Moments and rho/J assembly only (used for EnforceChargeNeutralization).
+// SolverManager::AdvanceFields (SolverManager.cpp:41-46): the six Maxwell stages alone,
+// with the current density left as it is.
+void Engine::advance_fields(const std::vector<Run *> &set, const std::vector<double> &dt) {
+    LaunchSet &L = get_set(set);
+    fill_params(L, set, dt);
+    MaxwellLaunch mx{};
+    mx.fields = L.dfields.as<RunFields>();
+    mx.nruns = (int)L.runs.size();
+    mx.maxnf = L.maxnf;
+    mx.params = L.dparams.as<double>();
+    mx.dxinv = L.ddxinv.as<double>();
+    mx.stream = stream;
+    for (int s = 0; s < 6; s++) {
+        mx.step = s;
+        launch_maxwell(mx);
+    }
+    kernel_launches += 18;
+    VX_CUDA(cudaGetLastError());
+}
+
 void Engine::moments_only(const std::vector<Run *> &set) {
     LaunchSet &L = get_set(set);
     MomLaunch ml{};

@@ -3,7 +3,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -43,6 +45,14 @@ struct DevBuf {
     }
 };
 
+// Device copy of a host vector (at least one element's worth of storage).
+template <class T>
+DevBuf upload(const std::vector<T> &v, cudaStream_t s) {
+    DevBuf b(std::max<size_t>(v.size() * sizeof(T), sizeof(T)));
+    if (!v.empty()) VX_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return b;
+}
+
 // Geometry of one Rectangle (Rectangle.hpp:20-23) plus its device storage.
 struct Rect {
     int n_x = 0, n_p = 0, x_pos = 0, p_pos = 0, depth = 0;
@@ -66,6 +76,12 @@ struct Rect {
 };
 
 class Engine;
+
+// Geometry and boundary flags of one patch of a promoted hierarchy.
+struct PatchGeom {
+    int depth, x_pos, p_pos, n_x, n_p;
+    bool up, down, left, right;
+};
 
 // One independent solve: the state owned by the reference's SolverManager
 // (SolverManager.hpp:5-19): Settings, one mesh per species, the field solver.
@@ -120,10 +136,28 @@ public:
     bool multi_patch = false;
     void build_amr();               // connectivity + op lists + masks for the current layout
     void validate_ops() const;      // bounds of every op against its patches
+    // Hierarchy construction / regridding (regrid.cpp)
+    using BoxList = std::vector<std::pair<std::pair<int, int>, std::pair<int, int>>>;
+    std::vector<std::vector<std::pair<int, int>>> flag_cells();
+    std::vector<BoxList> hierarchy_of(int species) const;
+    void regrid(bool init);         // Mesh::updateHierarchy for every species
+    void promote(const std::vector<std::vector<BoxList>> &hier, bool init);
+    void transfer_from(std::vector<std::vector<std::vector<std::unique_ptr<Rect>>>> &old);
+    DevBuf flat_descs();
+    void push_data(int slot);       // Mesh::PushData(slot) for this run
+    void copy_slot(int from, int to);
     int64_t state_size() const;
     void step_host(const double *in, double *out, double dt);
     void state_to_host(double *out);
 };
+
+// Clustering of one species' hierarchy (Mesh::updateHierarchy without the promotion)
+// and the geometry of the promoted patches; host only (regrid.cpp).
+std::vector<Run::BoxList> update_hierarchy(const Settings &s, int sp, std::vector<Run::BoxList> H,
+                                           const std::function<std::vector<std::pair<int, int>>(int)> &level_flags);
+std::vector<PatchGeom> promote_geometry(const Settings &s, int sp, const std::vector<Run::BoxList> &H);
+// Rectangle error weights (Rectangle.cpp:68-74) of a patch of depth `depth`.
+void error_weights(const Settings &s, int depth, int sp, double *w);
 
 // A set of runs advanced together: flattened descriptor and work tables.
 struct LaunchSet {
@@ -153,6 +187,8 @@ public:
     uint64_t kernel_launches = 0;  // launches issued by this engine (graph replays count their nodes)
 
     void advance(const std::vector<Run *> &set, const std::vector<double> &dt);
+    void advance_fields(const std::vector<Run *> &set, const std::vector<double> &dt);
+    void fill_params(LaunchSet &L, const std::vector<Run *> &set, const std::vector<double> &dt);
     std::vector<double> calculate_dt(const std::vector<Run *> &set);
     void moments_only(const std::vector<Run *> &set);
     void refresh_efield(Run &run);

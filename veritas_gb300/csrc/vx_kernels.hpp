@@ -138,6 +138,10 @@ struct CSyncOp;
 void launch_ghost(const void *patches, const GhostOp *ops, int n, int slot, cudaStream_t s);
 void launch_iface(const void *patches, const IfaceOp *ops, int n, int step, cudaStream_t s);
 void launch_csync(const void *patches, const CSyncOp *ops, int n, cudaStream_t s);
+struct FlagPatch;
+struct XferOp;
+void launch_flags(const void *patches, const FlagPatch *fp, int n, uint8_t *out, cudaStream_t s);
+void launch_xfer(const void *patches, const XferOp *ops, int n, uint8_t *mask, cudaStream_t s);
 
 // dst[i] = -src[i]
 void launch_negate(double *dst, const double *src, int n, cudaStream_t s);
