@@ -58,12 +58,13 @@ struct Params {
     double pert_amp = 0.0, pert_k = 1.0, a0 = 1.0, fwhm = 10.0, delay = 10.0;
     double cfl = 0.5, minEff = 0.75, crit = 1e-6, sizeWeight = 1.0;
     int quadDepth = 2;
+    double bdens = 0.0, bp0 = 0.0, bTe = 1.0;
 };
 
 // ------------------------------------------------------------------ problem hooks
 struct Problem {
     Params P;
-    double m, q, dp, pmin, dx, n0, sigma, pdrift, A0;
+    double m, q, dp, pmin, dx, n0, sigma, pdrift, A0, bsigma, bdrift;
     int maxDepth, quadDepth;
     unsigned x_size, p_size, r;
 
@@ -86,6 +87,8 @@ struct Problem {
         sigma = m * (P.Te * kKeV);
         pdrift = P.p0 * mc;
         A0 = P.a0 * mc / std::fabs(q);
+        bsigma = m * (P.bTe * kKeV);
+        bdrift = P.bp0 * mc;
     }
     double slab(double xl) const {
         double s;
@@ -99,7 +102,12 @@ struct Problem {
     double init_f(double x, double p) const {
         double ne = n0 * slab(x / P.lambda);
         double d = p - pdrift;
-        return ne * std::exp(-(d * d) / (2.0 * sigma)) / std::sqrt(DPI * sigma);
+        double v = ne * std::exp(-(d * d) / (2.0 * sigma)) / std::sqrt(DPI * sigma);
+        if (P.bdens != 0.0) {
+            double db = p - bdrift;
+            v += P.bdens * ne * std::exp(-(db * db) / (2.0 * bsigma)) / std::sqrt(DPI * bsigma);
+        }
+        return v;
     }
     double BY(double, double) const { return 0.0; }
     double BZ(double x, double t) const {
@@ -123,16 +131,36 @@ struct Problem {
 // ------------------------------------------------------------------ patch
 // One patch: SoA planes of (nx+4) x (np+4) doubles, p fastest.
 struct Patch {
-    int nx, np, x_pos = 0, p_pos = 0, depth, rtb;
+    int nx, np, x_pos = 0, p_pos = 0, depth, rtb, r = 2, species = 0;
     bool up = true, down = true, left = true, right = true;
     int W;  // row width np + 4
     std::vector<double> f[3], gam, ex, fx, ep, fp, FxH[6], FpH[6], FxL, FpL, FxDS, FpDS, Rp, Rm, Cx, Cp;
-    std::vector<double> chargeR, currentR, relc;
+    std::vector<double> chargeR, currentR, relc, refc;
     double dx, dp, dx_inv, dp_inv, pmin, q, m, cc, g2;
+    // AMR connectivity (Rectangle.hpp:8-12): neighbour patch index per edge entry (-1:
+    // the domain boundary), "same level" flags, finer patch per cell / face, masks
+    std::vector<int> xm, xp, pm, pp;
+    std::vector<char> sxm, sxp, spm, spp;
+    std::vector<int> finer, finer_x, finer_p;
+    std::vector<char> nested, ifx, ifp;
     size_t id(int i, int j) const { return (size_t)(i + 2) * W + (j + 2); }
     void alloc() {
         W = np + 4;
         size_t N = (size_t)(nx + 4) * W;
+        xm.assign(np / r + 2, -1);
+        xp.assign(np / r + 2, -1);
+        pm.assign(nx / r, -1);
+        pp.assign(nx / r, -1);
+        sxm.assign(np / r + 2, 1);
+        sxp.assign(np / r + 2, 1);
+        spm.assign(nx / r, 1);
+        spp.assign(nx / r, 1);
+        finer.assign(N, -1);
+        finer_x.assign(N, -1);
+        finer_p.assign(N, -1);
+        nested.assign(N, 0);
+        ifx.assign(N, 0);
+        ifp.assign(N, 0);
         for (auto &v : f) v.assign(N, 0.0);
         for (auto *v : {&gam, &ex, &fx, &ep, &fp, &FxL, &FpL, &FxDS, &FpDS, &Rp, &Rm, &Cx, &Cp}) v->assign(N, 0.0);
         for (int s = 0; s < 6; s++) {
@@ -177,6 +205,34 @@ double weno(double f1, double f2, double f3, double f4, bool right) {
     return fwl * fL + fwr * fR;
 }
 
+// Rectangle::GetWenoEdgeValue (Rectangle.cpp:943-977), used by the fluxes a coarse
+// patch takes from a finer one.
+double weno_max(double f1, double f2, double f3, double f4, bool right) {
+    double fL = (1.0 / 6) * (-f1 + 5 * f2 + 2 * f3);
+    double fR = (1.0 / 6) * (2 * f2 + 5 * f3 - f4);
+    double AL = f1 - 2 * f2 + f3;
+    double BL = f3 - f1;
+    double AR = f2 - 2 * f3 + f4;
+    double BR = f4 - f2;
+    double bL = 4.0 / 3 * (AL * AL) + 0.5 * AL * BL + 0.25 * (BL * BL);
+    double bR = 4.0 / 3 * (AR * AR) - 0.5 * AR * BR + 0.25 * (BR * BR);
+    double mm(1.0e-10);
+    double oL = 0.5 / ((mm + bL) * (mm + bL));
+    double oR = 0.5 / ((mm + bR) * (mm + bR));
+    double wL = oL / (oL + oR);
+    double wR = oR / (oL + oR);
+    double wL0 = wL * (0.75 + wL * (wL - 0.5));
+    double wR0 = wR * (0.75 + wR * (wR - 0.5));
+    if (right) {
+        wL = std::max(wL0, wR0) / (wL0 + wR0);
+        wR = 1 - wL;
+    } else {
+        wL = std::min(wL0, wR0) / (wL0 + wR0);
+        wR = 1 - wL;
+    }
+    return (wL * (fL) + wR * (fR));
+}
+
 double face_a(double f1, double f2, double f3, double f4) {
     double fL = (1.0 / 6) * (-f1 + 5 * f2 + 2 * f3);
     double fR = (1.0 / 6) * (2 * f2 + 5 * f3 - f4);
@@ -196,7 +252,8 @@ double face_a(double f1, double f2, double f3, double f4) {
 
 struct Solver {
     Problem pr;
-    std::vector<Patch> patches;  // one per species
+    std::vector<Patch> patches;        // every patch of the (single) species
+    std::vector<std::vector<int>> lv;  // lv[depth]: patch indices in the reference's level order
     Fields F;
     vxo::SparseLU lu;
     double time = 0.0;
@@ -230,16 +287,17 @@ struct Solver {
         return (ay * ay) + (az * az);
     }
 
-    void setup() {
-        pr.setup();
-        const int base = pr.maxDepth;
+    Patch make_patch(int depth, int x_pos, int p_pos, int nx, int np) {
         Patch P;
-        P.nx = pr.GetXSize(base);
-        P.np = pr.GetPSize(base);
-        P.depth = base;
-        P.rtb = (int)std::pow(pr.r, base);
-        P.dx = pr.GetDx(base);
-        P.dp = pr.GetDp(base);
+        P.nx = nx;
+        P.np = np;
+        P.x_pos = x_pos;
+        P.p_pos = p_pos;
+        P.depth = depth;
+        P.r = (int)pr.r;
+        P.rtb = (int)std::pow(pr.r, depth);
+        P.dx = pr.GetDx(depth);
+        P.dp = pr.GetDp(depth);
         P.dx_inv = 1 / P.dx;
         P.dp_inv = 1 / P.dp;
         P.pmin = pr.pmin;
@@ -249,7 +307,7 @@ struct Solver {
         double m_inv = 1 / pr.m;
         P.g2 = (m_inv * c_inv) * (m_inv * c_inv);
         P.relc.assign(3 * P.rtb, 0.0);
-        for (int i = 0; i < P.rtb; i++) {
+        for (int i = 0; i < P.rtb; i++) {  // Rectangle.cpp:103-110
             double rb = P.rtb;
             double tl = -0.5 + i / rb;
             double tr = -0.5 + (i + 1.0) / rb;
@@ -257,8 +315,24 @@ struct Solver {
             P.relc[3 * i + 1] = (tl * tl + tl * tr + tr * tr) / 3.0 - (1.0 / 12);
             P.relc[3 * i + 2] = (tl * tl * tl + tl * tl * tr + tl * tr * tr + tr * tr * tr) * 0.25;
         }
+        P.refc.assign(3 * P.r, 0.0);
+        for (int i = 0; i < P.r; i++) {  // Rectangle.cpp:94-101
+            double tl = -0.5 + i / (double)P.r;
+            double tr = -0.5 + (i + 1.0) / (double)P.r;
+            P.refc[3 * i] = (tl + tr) * 0.5;
+            P.refc[3 * i + 1] = (tl * tl + tl * tr + tr * tr) / 3.0 - (1.0 / 12);
+            P.refc[3 * i + 2] = (tl * tl * tl + tl * tl * tr + tl * tr * tr + tr * tr * tr) * 0.25;
+        }
         P.alloc();
-        patches.push_back(std::move(P));
+        return P;
+    }
+
+    void setup() {
+        pr.setup();
+        const int base = pr.maxDepth;
+        patches.push_back(make_patch(base, 0, 0, pr.GetXSize(base), pr.GetPSize(base)));
+        lv.assign(pr.maxDepth + 1, {});
+        lv[base].push_back(0);
         F.n = pr.x_size * std::pow(pr.r, pr.maxDepth);
         F.pre = std::max(std::floor(0.0 / pr.GetDx(0)), 2.0);
         F.post = std::max(std::floor(0.0 / pr.GetDx(0)), 2.0);
@@ -310,6 +384,414 @@ struct Solver {
         std::fill(F.J.begin(), F.J.end(), 0.0);
     }
 
+    // ---------------------------------------------------------------- AMR connectivity
+    static bool on_line(int x, int y1, int y2) { return ((x - y1) > -1) && ((y2 - x) > -1); }
+
+    // Rectangle::CalculateConnectivityFromFiner (Rectangle.cpp:768-864): `c` is a patch,
+    // `fi` a patch one level finer.
+    void connect_finer(int ci, int fi) {
+        Patch &C = patches[ci], &Fp = patches[fi];
+        const int r = C.r;
+        const int x2 = Fp.x_pos / r - C.x_pos, p2 = Fp.p_pos / r - C.p_pos;
+        const int nx2 = Fp.nx / r, np2 = Fp.np / r;
+        const int lower_x = std::max(0, x2), upper_x = std::min(C.nx, x2 + nx2);
+        const int lower_p = std::max(0, p2), upper_p = std::min(C.np, p2 + np2);
+        for (int i = lower_x; i < upper_x; i++)
+            for (int j = lower_p; j < upper_p; j++) {
+                C.nested[C.id(i, j)] = 1;
+                C.finer[C.id(i, j)] = fi;
+            }
+        const int last = (int)Fp.xp.size() - 1;
+        if ((x2 + nx2) < (C.nx + 1) && (x2 + nx2) > -1)
+            for (int i = lower_p; i < upper_p; i++) {
+                C.finer_x[C.id(x2 + nx2, i)] = fi;
+                C.ifx[C.id(x2 + nx2, i)] = 1;
+            }
+        if ((x2 + nx2) < C.nx && (x2 + nx2) > -1) {
+            for (int i = lower_p; i < upper_p; i++) Fp.xp[i - p2 + 1] = ci, Fp.sxp[i - p2 + 1] = 0;
+            if (on_line(p2 - 1, 0, C.np - 1)) Fp.xp[0] = ci, Fp.sxp[0] = 0;
+            if (on_line(p2 + np2, 0, C.np - 1)) Fp.xp[last] = ci, Fp.sxp[last] = 0;
+        }
+        if (x2 < (C.nx + 1) && x2 > -1)
+            for (int i = lower_p; i < upper_p; i++) {
+                C.finer_x[C.id(x2, i)] = fi;
+                C.ifx[C.id(x2, i)] = 1;
+            }
+        if (x2 < (C.nx + 1) && x2 > 0) {
+            for (int i = lower_p; i < upper_p; i++) Fp.xm[i - p2 + 1] = ci, Fp.sxm[i - p2 + 1] = 0;
+            if (on_line(p2 - 1, 0, C.np - 1)) Fp.xm[0] = ci, Fp.sxm[0] = 0;
+            if (on_line(p2 + np2, 0, C.np - 1)) Fp.xm[last] = ci, Fp.sxm[last] = 0;
+        }
+        if ((p2 + np2) < (C.np + 1) && (p2 + np2) > -1)
+            for (int i = lower_x; i < upper_x; i++) {
+                C.finer_p[C.id(i, p2 + np2)] = fi;
+                C.ifp[C.id(i, p2 + np2)] = 1;
+            }
+        if ((p2 + np2) < C.np && (p2 + np2) > -1)
+            for (int i = lower_x; i < upper_x; i++) Fp.pp[i - x2] = ci, Fp.spp[i - x2] = 0;
+        if (p2 < (C.np + 1) && p2 > -1)
+            for (int i = lower_x; i < upper_x; i++) {
+                C.finer_p[C.id(i, p2)] = fi;
+                C.ifp[C.id(i, p2)] = 1;
+            }
+        if (p2 < (C.np + 1) && p2 > 0)
+            for (int i = lower_x; i < upper_x; i++) Fp.pm[i - x2] = ci, Fp.spm[i - x2] = 0;
+    }
+
+    // Rectangle::CalculateConnectivitySame (Rectangle.cpp:671-766)
+    void connect_same(int ai, int bi) {
+        Patch &A = patches[ai];
+        const Patch &B = patches[bi];
+        const int r = A.r;
+        const int xr = B.x_pos - A.x_pos, pr_ = B.p_pos - A.p_pos;
+        const int lx = (int)A.xm.size() - 1;
+        if (xr == A.nx) {
+            int lower = std::max(B.p_pos, A.p_pos), upper = std::min(A.p_pos + A.np, B.p_pos + B.np);
+            if (on_line(-1, pr_, pr_ + B.np - 1)) A.xp[0] = bi, A.sxp[0] = 1;
+            if (on_line(A.np, pr_, pr_ + B.np - 1)) A.xp[lx] = bi, A.sxp[lx] = 1;
+            for (; lower < upper; lower += r) A.xp.at((lower - A.p_pos) / r + 1) = bi, A.sxp.at((lower - A.p_pos) / r + 1) = 1;
+        }
+        if (xr == -B.nx) {
+            int lower = std::max(B.p_pos, A.p_pos), upper = std::min(A.p_pos + A.np, B.p_pos + B.np);
+            if (on_line(-1, pr_, pr_ + B.np - 1)) A.xm[0] = bi, A.sxm[0] = 1;
+            if (on_line(A.np, pr_, pr_ + B.np - 1)) A.xm[lx] = bi, A.sxm[lx] = 1;
+            for (; lower < upper; lower += r) A.xm.at((lower - A.p_pos) / r + 1) = bi, A.sxm.at((lower - A.p_pos) / r + 1) = 1;
+        }
+        if (pr_ == A.np) {
+            int lower = std::max(B.x_pos, A.x_pos), upper = std::min(A.x_pos + A.nx, B.x_pos + B.nx);
+            if (on_line(-1, xr, xr + B.nx - 1)) A.xm[lx] = bi, A.sxm[lx] = 1;
+            if (on_line(A.nx, xr, xr + B.nx - 1)) A.xp[lx] = bi, A.sxp[lx] = 1;
+            for (; lower < upper; lower += r) A.pp.at((lower - A.x_pos) / r) = bi, A.spp.at((lower - A.x_pos) / r) = 1;
+        }
+        if (pr_ == -B.np) {
+            int lower = std::max(B.x_pos, A.x_pos), upper = std::min(A.x_pos + A.nx, B.x_pos + B.nx);
+            if (on_line(-1, xr, xr + B.nx - 1)) A.xm[0] = bi, A.sxm[0] = 1;
+            if (on_line(A.nx, xr, xr + B.nx - 1)) A.xp[0] = bi, A.sxp[0] = 1;
+            for (; lower < upper; lower += r) A.pm.at((lower - A.x_pos) / r) = bi, A.spm.at((lower - A.x_pos) / r) = 1;
+        }
+    }
+
+    // Mesh::promoteHierarchyToMesh connectivity loops (Mesh.cpp:836-859) on patches whose
+    // connectivity is still the constructor's (every edge on the domain boundary).
+    void connect_keep_f() {
+        for (int l = 0; l <= pr.maxDepth; l++)
+            for (int rl : lv[l])
+                if (l > 0)
+                    for (int rf : lv[l - 1]) connect_finer(rl, rf);
+        for (int l = 0; l <= pr.maxDepth; l++)
+            for (int rl : lv[l])
+                for (int rr : lv[l])
+                    if (rl != rr) connect_same(rl, rr);
+    }
+
+    // ---------------------------------------------------------------- ghost fills
+    double same_value(int nb, int gi, int gj, int val) const {  // GetValueFromSameLevel; BC: 0
+        if (nb < 0) return 0.0;
+        const Patch &N = patches[nb];
+        return N.f[val][N.id(gi - N.x_pos, gj - N.p_pos)];
+    }
+    // Rectangle::GetInterpolantsREF (Rectangle.cpp:121-137)
+    static std::vector<double> interp_ref(const Patch &C, double f1, double f2, double f3, double f4, double f5) {
+        std::vector<double> t(C.r, 0.0);
+        f5 -= f3;
+        f4 -= f3;
+        f2 -= f3;
+        f1 -= f3;
+        double a1 = 0.104166666666667 * f1 + -0.708333333333334 * f2 + 0.708333333333334 * f4 + -0.104166666666667 * f5;
+        double a2 = 0.117647058823529 * f1 + 0.029411764705882 * f2 + 0.029411764705882 * f4 + 0.117647058823529 * f5;
+        double a3 = -0.083333333333333 * f1 + 0.166666666666667 * f2 + -0.166666666666667 * f4 + 0.083333333333334 * f5;
+        for (int i = 0; i < C.r; i++) t[i] = C.refc[3 * i] * a1 + C.refc[3 * i + 1] * a2 + C.refc[3 * i + 2] * a3 + f3;
+        return t;
+    }
+    // Rectangle::GetWenoValueFromCoarseLevel (Rectangle.cpp:343-415)
+    std::vector<double> weno_coarse(int ci, int gi, int gj, int d, int val) const {
+        const Patch &C = patches[ci];
+        const int r = C.r;
+        const int ic = gi / r - C.x_pos, jc = gj / r - C.p_pos;
+        const double *f = C.f[val].data();
+        std::vector<std::vector<double>> temps;
+        for (int k = -2; k < 3; k++)
+            temps.push_back(interp_ref(C, f[C.id(ic - 2, jc + k)], f[C.id(ic - 1, jc + k)], f[C.id(ic, jc + k)],
+                                       f[C.id(ic + 1, jc + k)], f[C.id(ic + 2, jc + k)]));
+        std::vector<double> it(r * r);
+        double sum(0.0);
+        for (int k = 0; k < r; k++) {
+            auto part = interp_ref(C, temps[0][k], temps[1][k], temps[2][k], temps[3][k], temps[4][k]);
+            for (int l = 0; l < r; l++) {
+                it[k * r + l] = part[l];
+                sum += part[l];
+            }
+        }
+        double correction = f[C.id(ic, jc)] - 1.0 / std::pow(r, 2) * sum;
+        for (auto &v : it) v += correction;
+        if (d < 0 || d > 3) return it;
+        std::vector<double> red(2 * r);
+        for (int k = 0; k < r; k++) {
+            if (d == 0) red[2 * k] = it[r * k + r - 1], red[2 * k + 1] = it[r * k + r - 2];
+            else if (d == 1) red[2 * k] = it[k], red[2 * k + 1] = it[r + k];
+            else if (d == 2) red[2 * k] = it[r * k], red[2 * k + 1] = it[r * k + 1];
+            else red[2 * k] = it[r * (r - 1) + k], red[2 * k + 1] = it[r * (r - 2) + k];
+        }
+        return red;
+    }
+    // Rectangle::UpdateInterriorPoints / GetValueFromFinerLevel (Rectangle.cpp:314-337)
+    void update_interior(Patch &R, int val) {
+        const int r = R.r;
+        for (int i = 0; i < R.nx; i++)
+            for (int j = 0; j < R.np; j++)
+                if (R.nested[R.id(i, j)]) {
+                    const Patch &Fp = patches[R.finer[R.id(i, j)]];
+                    const int fi = (R.x_pos + i) * r - Fp.x_pos, fj = (R.p_pos + j) * r - Fp.p_pos;
+                    double t(0.0);
+                    for (int k = 0; k < r; k++)
+                        for (int l = 0; l < r; l++) t += Fp.f[val][Fp.id(fi + k, fj + l)];
+                    t /= std::pow((double)r, 2.0);
+                    R.f[val][R.id(i, j)] = t;
+                }
+    }
+    // Rectangle::UpdateSameLevelBoundaries (Rectangle.cpp:562-614)
+    void update_same(Patch &R, int val) {
+        const int r = R.r;
+        double *f = R.f[val].data();
+        for (size_t e = 0; e + 2 < R.sxm.size(); e++)
+            if (R.sxm[e + 1])
+                for (int j = 0; j < r; j++) {
+                    const int i = (int)e;
+                    f[R.id(-1, i * r + j)] = same_value(R.xm[e + 1], R.x_pos - 1, R.p_pos + i * r + j, val);
+                    f[R.id(-2, i * r + j)] = same_value(R.xm[e + 1], R.x_pos - 2, R.p_pos + i * r + j, val);
+                }
+        for (size_t e = 0; e + 2 < R.sxp.size(); e++)
+            if (R.sxp[e + 1])
+                for (int j = 0; j < r; j++) {
+                    const int i = (int)e;
+                    f[R.id(R.nx, i * r + j)] = same_value(R.xp[e + 1], R.x_pos + R.nx, R.p_pos + i * r + j, val);
+                    f[R.id(R.nx + 1, i * r + j)] = same_value(R.xp[e + 1], R.x_pos + R.nx + 1, R.p_pos + i * r + j, val);
+                }
+        for (size_t e = 0; e < R.spm.size(); e++)
+            if (R.spm[e])
+                for (int j = 0; j < r; j++) {
+                    const int i = (int)e;
+                    f[R.id(i * r + j, -1)] = same_value(R.pm[e], R.x_pos + i * r + j, R.p_pos - 1, val);
+                    f[R.id(i * r + j, -2)] = same_value(R.pm[e], R.x_pos + i * r + j, R.p_pos - 2, val);
+                }
+        for (size_t e = 0; e < R.spp.size(); e++)
+            if (R.spp[e])
+                for (int j = 0; j < r; j++) {
+                    const int i = (int)e;
+                    f[R.id(i * r + j, R.np)] = same_value(R.pp[e], R.x_pos + i * r + j, R.p_pos + R.np, val);
+                    f[R.id(i * r + j, R.np + 1)] = same_value(R.pp[e], R.x_pos + i * r + j, R.p_pos + R.np + 1, val);
+                }
+    }
+    // Rectangle::UpdateCornerPoints (Rectangle.cpp:1130-1214)
+    void update_corners(Patch &R, int val) {
+        const int r = R.r;
+        double *f = R.f[val].data();
+        const int top = (int)R.sxm.size() - 2;
+        auto left = [&](int i, int j0, int j1) {
+            const int e = i + 1, nb = R.xm[e];
+            if (nb >= 0 && !R.sxm[e]) {
+                auto t = weno_coarse(nb, R.x_pos - 1, R.p_pos + i * r, 3, val);
+                for (int j = j0; j < j1; j++) {
+                    f[R.id(-1, i * r + j)] = t[2 * j];
+                    f[R.id(-2, i * r + j)] = t[2 * j + 1];
+                }
+            } else {
+                for (int j = j0; j < j1; j++) {
+                    f[R.id(-1, i * r + j)] = same_value(nb, R.x_pos - 1, R.p_pos + i * r + j, val);
+                    f[R.id(-2, i * r + j)] = same_value(nb, R.x_pos - 2, R.p_pos + i * r + j, val);
+                }
+            }
+        };
+        auto right = [&](int i, int j0, int j1) {
+            const int e = i + 1, nb = R.xp[e];
+            if (nb >= 0 && !R.sxp[e]) {
+                auto t = weno_coarse(nb, R.x_pos + R.nx, R.p_pos + i * r, 1, val);
+                for (int j = j0; j < j1; j++) {
+                    f[R.id(R.nx, i * r + j)] = t[2 * j];
+                    f[R.id(R.nx + 1, i * r + j)] = t[2 * j + 1];
+                }
+            } else {
+                for (int j = j0; j < j1; j++) {
+                    f[R.id(R.nx, i * r + j)] = same_value(nb, R.x_pos + R.nx, R.p_pos + i * r + j, val);
+                    f[R.id(R.nx + 1, i * r + j)] = same_value(nb, R.x_pos + R.nx + 1, R.p_pos + i * r + j, val);
+                }
+            }
+        };
+        left(-1, r - 2, r);
+        left(top, 0, 2);
+        right(-1, r - 2, r);
+        right(top, 0, 2);
+    }
+    // Rectangle::UpdateDifferentLevelBoundaries (Rectangle.cpp:416-560)
+    void update_diff(Patch &R, int val) {
+        const int r = R.r;
+        double *f = R.f[val].data();
+        for (size_t e = 0; e + 2 < R.sxm.size(); e++)
+            if (!R.sxm[e + 1] && R.xm[e + 1] >= 0) {
+                const int i = (int)e;
+                auto t = weno_coarse(R.xm[e + 1], R.x_pos - 1, R.p_pos + i * r, 3, val);
+                for (int j = 0; j < r; j++) {
+                    f[R.id(-1, i * r + j)] = t[2 * j];
+                    f[R.id(-2, i * r + j)] = t[2 * j + 1];
+                }
+            }
+        for (size_t e = 0; e + 2 < R.sxp.size(); e++)
+            if (!R.sxp[e + 1] && R.xp[e + 1] >= 0) {
+                const int i = (int)e;
+                auto t = weno_coarse(R.xp[e + 1], R.x_pos + R.nx, R.p_pos + i * r, 1, val);
+                for (int j = 0; j < r; j++) {
+                    f[R.id(R.nx, i * r + j)] = t[2 * j];
+                    f[R.id(R.nx + 1, i * r + j)] = t[2 * j + 1];
+                }
+            }
+        for (size_t e = 0; e < R.spm.size(); e++)
+            if (!R.spm[e] && R.pm[e] >= 0) {
+                const int i = (int)e;
+                auto t = weno_coarse(R.pm[e], R.x_pos + i * r, R.p_pos - 1, 0, val);
+                for (int j = 0; j < r; j++) {
+                    f[R.id(i * r + j, -1)] = t[2 * j];
+                    f[R.id(i * r + j, -2)] = t[2 * j + 1];
+                }
+            }
+        for (size_t e = 0; e < R.spp.size(); e++)
+            if (!R.spp[e] && R.pp[e] >= 0) {
+                const int i = (int)e;
+                auto t = weno_coarse(R.pp[e], R.x_pos + i * r, R.p_pos + R.np, 2, val);
+                for (int j = 0; j < r; j++) {
+                    f[R.id(i * r + j, R.np)] = t[2 * j];
+                    f[R.id(i * r + j, R.np + 1)] = t[2 * j + 1];
+                }
+            }
+        update_corners(R, val);
+    }
+    // Mesh::PushData (Mesh.cpp:91-106)
+    void push_data(int val) {
+        const int L = pr.maxDepth + 1;
+        for (int k : lv[0]) update_same(patches[k], val);
+        for (int i = 1; i < L; i++) {
+            for (int k : lv[i]) update_interior(patches[k], val);
+            for (int k : lv[i]) update_same(patches[k], val);
+        }
+        for (int k : lv[L - 1]) update_corners(patches[k], val);
+        for (int i = L - 1; i > 0; i--)
+            for (int k : lv[i - 1]) update_diff(patches[k], val);
+    }
+
+    // ---------------------------------------------------------------- fluxes to coarse
+    double gamma_p(const Patch &P, double mom, double as) const { return std::sqrt(1.0 + ((mom * mom) + as) * P.g2); }
+    double momentum(const Patch &P, double j) const { return P.pmin + P.dp * (j + P.p_pos); }
+    // Rectangle::RGKGetFluxX / RGKGetFluxXL / RGKGetFluxP / RGKGetFluxPL
+    // (Rectangle.cpp:1032-1098, 1216-1253) and CalculateFluxToCoarse* (Rectangle.hpp:132-178)
+    double rgk_flux(int pi, int i, int j, bool xdir, bool low) const {
+        const Patch &P = patches[pi];
+        const size_t d = P.id(i, j);
+        if (xdir && P.ifx[d]) return flux_to_coarse(P.finer_x[d], P.x_pos + i, P.p_pos + j, true, low);
+        if (!xdir && P.ifp[d]) return flux_to_coarse(P.finer_p[d], P.x_pos + i, P.p_pos + j, false, low);
+        const double *f = P.f[1].data();
+        const double w3 = 1.0 / 48.0;
+        const double q = P.q;
+        if (xdir) {
+            double as = q * q * asq_face(P.rtb * (i + P.x_pos));
+            double am = P.dp_inv * P.cc * (gamma_p(P, momentum(P, j + 1), as) - gamma_p(P, momentum(P, j), as));
+            if (low) return P.dx_inv * (am > 0.0 ? f[P.id(i - 1, j)] : f[P.id(i, j)]) * am;
+            double ap1 = P.dp_inv * P.cc * (gamma_p(P, momentum(P, j + 2.0), as) - gamma_p(P, momentum(P, j + 1.0), as));
+            double am1 = P.dp_inv * P.cc * (gamma_p(P, momentum(P, j), as) - gamma_p(P, momentum(P, j - 1.0), as));
+            double fm = weno_max(f[P.id(i - 2, j)], f[P.id(i - 1, j)], f[P.id(i, j)], f[P.id(i + 1, j)], am > 0.0);
+            double fp1 = weno_max(f[P.id(i - 2, j + 1)], f[P.id(i - 1, j + 1)], f[P.id(i, j + 1)], f[P.id(i + 1, j + 1)], ap1 > 0.0);
+            double fm1 = weno_max(f[P.id(i - 2, j - 1)], f[P.id(i - 1, j - 1)], f[P.id(i, j - 1)], f[P.id(i + 1, j - 1)], am1 > 0.0);
+            return P.dx_inv * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
+        }
+        double as_1 = q * q * asq_face(P.rtb * (i + P.x_pos));
+        double as_2 = q * q * asq_face(P.rtb * (i + 1 + P.x_pos));
+        double Em = q * patch_efield(P, i);
+        double mom = momentum(P, j);
+        double am = Em - P.cc * P.dx_inv * (gamma_p(P, mom, as_2) - gamma_p(P, mom, as_1));
+        if (low) return P.dp_inv * (am > 0.0 ? f[P.id(i, j - 1)] : f[P.id(i, j)]) * am;
+        double as_0 = q * q * asq_face(P.rtb * (i - 1 + P.x_pos));
+        double as_3 = q * q * asq_face(P.rtb * (i + 2 + P.x_pos));
+        double Ep1 = q * patch_efield(P, i + 1), Em1 = q * patch_efield(P, i - 1);
+        double ap1 = Ep1 - P.cc * P.dx_inv * (gamma_p(P, mom, as_3) - gamma_p(P, mom, as_2));
+        double am1 = Em1 - P.cc * P.dx_inv * (gamma_p(P, mom, as_1) - gamma_p(P, mom, as_0));
+        double fm = weno_max(f[P.id(i, j - 2)], f[P.id(i, j - 1)], f[P.id(i, j)], f[P.id(i, j + 1)], am > 0.0);
+        double fp1 = weno_max(f[P.id(i + 1, j - 2)], f[P.id(i + 1, j - 1)], f[P.id(i + 1, j)], f[P.id(i + 1, j + 1)], ap1 > 0.0);
+        double fm1 = weno_max(f[P.id(i - 1, j - 2)], f[P.id(i - 1, j - 1)], f[P.id(i - 1, j)], f[P.id(i - 1, j + 1)], am1 > 0.0);
+        return P.dp_inv * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
+    }
+    double flux_to_coarse(int fi, int ci, int cj, bool xdir, bool low) const {
+        const Patch &Fp = patches[fi];
+        const int r = Fp.r;
+        const int i = ci * r - Fp.x_pos, j = cj * r - Fp.p_pos;
+        double temp = 0.0;
+        for (int k = 0; k < r; k++) temp += xdir ? rgk_flux(fi, i, j + k, true, low) : rgk_flux(fi, i + k, j, false, low);
+        temp *= (1.0 / (r * r));
+        return temp;
+    }
+
+    // ---------------------------------------------------------------- limiter exchange
+    // Rectangle::SetCFromSameLevel / UpdateCFromSameLevel / SetCFromDifferentLevel
+    // (Rectangle.cpp:1625-1960); `N` is the neighbour, `R` the calling patch.
+    void c_same(Patch &N, Patch &R, int gi, int gj, int t, bool update) {
+        const int in = gi - N.x_pos, jn = gj - N.p_pos, ic = gi - R.x_pos, jc = gj - R.p_pos;
+        for (int k = 0; k < N.r; k++) {
+            const bool xf = t < 2;
+            const size_t dn = xf ? N.id(in, jn + k) : N.id(in + k, jn);
+            const size_t dc = xf ? R.id(ic, jc + k) : R.id(ic + k, jc);
+            std::vector<double> &NC = xf ? N.Cx : N.Cp, &RC = xf ? R.Cx : R.Cp;
+            const std::vector<double> &NDS = xf ? N.FxDS : N.FpDS;
+            const size_t np_ = xf ? dn - N.W : dn - 1, cp_ = xf ? dc - R.W : dc - 1;
+            double c;
+            if (update) c = std::min(NC[dn], RC[dc]);
+            else if (t == 0 || t == 2) c = NDS[dn] > 0.0 ? std::min(R.Rp[dc], N.Rm[np_]) : std::min(N.Rp[np_], R.Rm[dc]);
+            else c = NDS[dn] > 0.0 ? std::min(R.Rm[cp_], N.Rp[dn]) : std::min(N.Rm[dn], R.Rp[cp_]);
+            NC[dn] = c;
+            RC[dc] = c;
+        }
+    }
+    void c_diff(Patch &N, Patch &R, int gi, int gj, int t) {
+        const int r = N.r;
+        const int ic = gi - R.x_pos, jc = gj - R.p_pos;
+        const int i0 = gi / r - N.x_pos, j0 = gj / r - N.p_pos;
+        const bool xf = t < 2;
+        std::vector<double> &NC = xf ? N.Cx : N.Cp, &RC = xf ? R.Cx : R.Cp;
+        const std::vector<double> &NDS = xf ? N.FxDS : N.FpDS, &RDS = xf ? R.FxDS : R.FpDS;
+        const size_t dn = N.id(i0, j0), np_ = xf ? N.id(i0 - 1, j0) : N.id(i0, j0 - 1);
+        double c = NC[dn];
+        for (int k = 0; k < r; k++) {
+            const size_t dc = xf ? R.id(ic, jc + k) : R.id(ic + k, jc);
+            const size_t cp_ = xf ? R.id(ic - 1, jc + k) : R.id(ic + k, jc - 1);
+            if (t == 0 || t == 2) c = std::min(c, RDS[dc] > 0.0 ? R.Rp[dc] : R.Rm[dc]);
+            else c = std::min(c, RDS[dc] > 0.0 ? R.Rm[cp_] : R.Rp[cp_]);
+        }
+        if (t == 0 || t == 2) c = std::min(c, NDS[dn] > 0.0 ? N.Rm[np_] : N.Rp[np_]);
+        else c = std::min(c, NDS[dn] > 0.0 ? N.Rp[dn] : N.Rm[dn]);
+        for (int k = 0; k < r; k++) RC[xf ? R.id(ic, jc + k) : R.id(ic + k, jc)] = c;
+        NC[dn] = c;
+    }
+    // CalculateSameBoundaryC / CalculateDifferentBoundaryC / UpdateSameBoundaryC of one
+    // patch (kind 0 / 1 / 2); the domain boundary object does nothing.
+    void c_calls(int ri, int kind) {
+        Patch &R = patches[ri];
+        const int r = R.r;
+        auto one = [&](int nb, bool same, int gi, int gj, int t) {
+            if (nb < 0) return;
+            if (kind == 1) {
+                if (!same) c_diff(patches[nb], R, gi, gj, t);
+            } else if (same) {
+                c_same(patches[nb], R, gi, gj, t, kind == 2);
+            }
+        };
+        for (size_t e = 0; e + 2 < R.sxm.size(); e++) one(R.xm[e + 1], R.sxm[e + 1], R.x_pos, R.p_pos + (int)e * r, 0);
+        for (size_t e = 0; e + 2 < R.sxp.size(); e++) one(R.xp[e + 1], R.sxp[e + 1], R.x_pos + R.nx, R.p_pos + (int)e * r, 1);
+        for (size_t e = 0; e < R.spm.size(); e++) one(R.pm[e], R.spm[e], R.x_pos + (int)e * r, R.p_pos, 2);
+        for (size_t e = 0; e < R.spp.size(); e++) one(R.pp[e], R.spp[e], R.x_pos + (int)e * r, R.p_pos + R.np, 3);
+    }
+    // Mesh::PushBoundaryC (Mesh.cpp:904-917)
+    void push_boundary_c() {
+        for (int kind = 0; kind < 3; kind++)
+            for (int l = 0; l <= pr.maxDepth; l++)
+                for (int k : lv[l]) c_calls(k, kind);
+    }
+
     // ---------------------------------------------------------------- moments
     double rel_value(const Patch &P, int i, int j, int k) const {
         const double *f = P.f[1].data();
@@ -349,9 +831,11 @@ struct Solver {
                 double vm1 = rel_value(P, i, -1, k), v0 = rel_value(P, i, 0, k), vp1 = rel_value(P, i, 1, k);
                 double ch = 0.0, cu = 0.0;
                 for (int j = 0; j < P.np; j++) {
-                    ch += v0;
-                    double gm = Lr[j + 1], gm1 = Lr[j], gp1 = Lr[j + 2];
-                    cu += v0 * gm + c3 * (gp1 - gm1) * (vp1 - vm1);
+                    if (!P.nested[P.id(i, j)]) {
+                        ch += v0;
+                        double gm = Lr[j + 1], gm1 = Lr[j], gp1 = Lr[j + 2];
+                        cu += v0 * gm + c3 * (gp1 - gm1) * (vp1 - vm1);
+                    }
                     vm1 = v0;
                     v0 = vp1;
                     vp1 = rel_value(P, i, j + 2, k);
@@ -362,26 +846,26 @@ struct Solver {
         }
     }
 
+    // Level::CollectRhoAndJ + EMFieldSolver::AssembleRhoAndJ (Level.cpp:19-62,
+    // EMSolver.cpp:104-122): per level, patch sums in level order; levels finest first.
     void assemble() {
         for (auto &P : patches) moments(P);
         for (int x = 0; x < F.n; x++) {
-            double J = 0.0, charge = 0.0;
-            for (auto &P : patches) {
-                double cs_ = 0.0;
-                for (int l = 0; l <= pr.maxDepth; l++) {
-                    double lc = 0.0, lj = 0.0;
-                    if (l == P.depth) {
-                        int c = x - P.x_pos * P.rtb;
-                        if (c >= 0 && c < P.nx * P.rtb) {
-                            lc += P.chargeR[c];
-                            lj += P.currentR[c];
-                        }
+            double J = 0.0, charge = 0.0, cs_ = 0.0;
+            for (int l = 0; l <= pr.maxDepth; l++) {
+                double lc = 0.0, lj = 0.0;
+                for (int k : lv[l]) {
+                    const Patch &P = patches[k];
+                    int c = x - P.x_pos * P.rtb;
+                    if (c >= 0 && c < P.nx * P.rtb) {
+                        lc += P.chargeR[c];
+                        lj += P.currentR[c];
                     }
-                    cs_ += lc;
-                    J += lj;
                 }
-                charge += cs_;
+                cs_ += lc;
+                J += lj;
             }
+            charge += cs_;
             F.charge[x] = charge;
             F.J[x] = J;
         }
@@ -397,7 +881,8 @@ struct Solver {
     }
 
     // ---------------------------------------------------------------- FCT sub-steps
-    void fct_sub0(Patch &P, int step, const double *a, double asum) {
+    void fct_sub0(int pi, int step, const double *a, double asum) {
+        Patch &P = patches[pi];
         const int nx = P.nx, np = P.np;
         const double *f = P.f[1].data();
         const double w3 = 1 / 48.0;
@@ -429,13 +914,19 @@ struct Solver {
         for (int i = -1; i <= nx; i++) {
             for (int j = -1; j <= np; j++) {
                 size_t d = P.id(i, j);
-                if (i >= 0) {
+                if (i >= 0 && P.ifx[d]) {  // coarse/fine interface: the finer patch's mean flux
+                    P.FxH[step][d] = flux_to_coarse(P.finer_x[d], P.x_pos + i, P.p_pos + j, true, false);
+                    if (step == 0) P.FxL[d] = flux_to_coarse(P.finer_x[d], P.x_pos + i, P.p_pos + j, true, true);
+                } else if (i >= 0) {
                     double am = P.ex[d], ap1 = P.ex[d + 1], am1 = P.ex[d - 1];
                     double fm = P.fx[d], fp1 = P.fx[d + 1], fm1 = P.fx[d - 1];
                     P.FxH[step][d] = P.dx_inv * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
                     if (step == 0) P.FxL[d] = P.dx_inv * ((am > 0.0 ? f[d - P.W] : f[d]) * am);
                 }
-                if (j >= 0) {
+                if (j >= 0 && P.ifp[d]) {
+                    P.FpH[step][d] = flux_to_coarse(P.finer_p[d], P.x_pos + i, P.p_pos + j, false, false);
+                    if (step == 0) P.FpL[d] = flux_to_coarse(P.finer_p[d], P.x_pos + i, P.p_pos + j, false, true);
+                } else if (j >= 0) {
                     double am = P.ep[d], ap1 = P.ep[d + P.W], am1 = P.ep[d - P.W];
                     double fm = P.fp[d], fp1 = P.fp[d + P.W], fm1 = P.fp[d - P.W];
                     P.FpH[step][d] = P.dp_inv * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
@@ -628,12 +1119,19 @@ struct Solver {
             for (int k = 0; k <= kmax; k++) a[k] = R[s][k] * timestep;
             double asum = a[0];
             for (int k = 1; k <= kmax; k++) asum = asum + a[k];
-            for (auto &P : patches) {
-                fct_sub0(P, s, a, asum);
-                fct_sub1(P);
-                fct_sub2(P);
-                if (s == 5) P.f[0] = P.f[1];
-            }
+            // Mesh::Advance (Mesh.cpp:64-89): each sub-step over the levels coarsest first
+            const int L = pr.maxDepth + 1;
+            for (int l = L - 1; l > -1; l--)
+                for (int k : lv[l]) fct_sub0(k, s, a, asum);
+            push_data(2);
+            for (int l = L - 1; l > -1; l--)
+                for (int k : lv[l]) fct_sub1(patches[k]);
+            push_boundary_c();
+            for (int l = L - 1; l > -1; l--)
+                for (int k : lv[l]) fct_sub2(patches[k]);
+            push_data(1);
+            if (s == 5)
+                for (auto &P : patches) P.f[0] = P.f[1];
             update_time(s, timestep);
             maxwell(s, timestep);
         }
@@ -676,15 +1174,12 @@ struct Solver {
         wi(F.pre);
         wi(F.post);
         for (auto *v : {&F.By, &F.Bz, &F.Ey, &F.Ez, &F.Ay, &F.Az, &F.asq, &F.phi, &F.charge, &F.J, &F.neut}) wv(*v);
-        wi((long long)patches.size());
-        for (auto &P : patches) {
-            wi(pr.maxDepth + 1);
-            for (int l = 0; l <= pr.maxDepth; l++) {
-                if (l != P.depth) {
-                    wi(0);
-                    continue;
-                }
-                wi(1);
+        wi(1);  // species
+        wi(pr.maxDepth + 1);
+        for (int l = 0; l <= pr.maxDepth; l++) {
+            wi((long long)lv[l].size());
+            for (int k : lv[l]) {
+                const Patch &P = patches[k];
                 for (long long v : {(long long)P.x_pos, (long long)P.p_pos, (long long)P.nx, (long long)P.np,
                                     (long long)P.depth, (long long)P.up, (long long)P.down, (long long)P.left,
                                     (long long)P.right})
@@ -739,29 +1234,40 @@ struct Solver {
             exit(2);
         }
         for (auto *v : {&F.By, &F.Bz, &F.Ey, &F.Ez, &F.Ay, &F.Az, &F.asq, &F.phi, &F.charge, &F.J, &F.neut}) rv(*v);
-        long long ns = ri();
-        if (ns != (long long)patches.size()) {
-            fprintf(stderr, "species mismatch\n");
+        if (ri() != 1) {
+            fprintf(stderr, "the port handles one species\n");
+            exit(3);
+        }
+        long long nl = ri();
+        if (nl != pr.maxDepth + 1) {
+            fprintf(stderr, "level count mismatch\n");
             exit(2);
         }
-        for (auto &P : patches) {
-            long long nl = ri();
-            for (long long l = 0; l < nl; l++) {
-                long long nr = ri();
-                for (long long k = 0; k < nr; k++) {
-                    long long h[9];
-                    for (auto &x : h) x = ri();
-                    if (h[2] != P.nx || h[3] != P.np || h[0] != 0 || h[1] != 0) {
-                        fprintf(stderr, "the port handles one full-domain patch per species\n");
-                        exit(3);
-                    }
-                    std::vector<double> fv((size_t)3 * (P.nx + 4) * P.W);
-                    rv(fv);
-                    for (size_t c = 0; c < (size_t)(P.nx + 4) * P.W; c++)
-                        for (int s = 0; s < 3; s++) P.f[s][c] = fv[3 * c + s];
+        patches.clear();
+        lv.assign(nl, {});
+        for (long long l = 0; l < nl; l++) {
+            long long nr = ri();
+            for (long long k = 0; k < nr; k++) {
+                long long h[9];
+                for (auto &x : h) x = ri();
+                if (h[4] != l) {
+                    fprintf(stderr, "patch depth mismatch\n");
+                    exit(2);
                 }
+                Patch P = make_patch((int)h[4], (int)h[0], (int)h[1], (int)h[2], (int)h[3]);
+                P.up = h[5];
+                P.down = h[6];
+                P.left = h[7];
+                P.right = h[8];
+                std::vector<double> fv((size_t)3 * (P.nx + 4) * P.W);
+                rv(fv);
+                for (size_t c = 0; c < (size_t)(P.nx + 4) * P.W; c++)
+                    for (int s = 0; s < 3; s++) P.f[s][c] = fv[3 * c + s];
+                lv[l].push_back((int)patches.size());
+                patches.push_back(std::move(P));
             }
         }
+        connect_keep_f();
         fclose(fp);
     }
 };
@@ -806,8 +1312,12 @@ int main(int argc, char **argv) {
     P.crit = getd("crit", P.crit);
     P.sizeWeight = getd("sizeWeight", P.sizeWeight);
     P.quadDepth = (int)geti("quadDepth", P.quadDepth);
-    if (P.Lfinest != 1) {
-        fprintf(stderr, "the port restates the single-level step (levels=1)\n");
+    P.bdens = getd("bdens", P.bdens);
+    P.bp0 = getd("bp0", P.bp0);
+    P.bTe = getd("bTe", P.bTe);
+    if (P.Lfinest != 1 && !kv.count("load")) {
+        fprintf(stderr, "multi-level runs start from a state file (load=): the port restates the step, not the\n"
+                        "hierarchy construction\n");
         return 3;
     }
     long long steps = geti("steps", 0), dump_every = geti("dump_every", 0), time_steps = geti("time_steps", 0);
@@ -848,7 +1358,7 @@ int main(int argc, char **argv) {
         }
         std::sort(per.begin(), per.end());
         long long cells = 0;
-        for (auto &p : S.patches) cells += (long long)p.nx * p.np;
+        for (auto &p : S.patches) cells += (long long)p.nx * p.np;  // every level, covered cells included
         printf("{\"cells\": %lld, \"steps\": %lld, \"best_s\": %.6f, \"median_s\": %.6f, \"threads\": %d, \"init_s\": %.3f}\n",
                cells, time_steps, per.front(), per[per.size() / 2], omp_get_max_threads(),
                std::chrono::duration<double>(t1 - t0).count());

@@ -78,3 +78,31 @@ def test_port_detects_planted_error(port, tmp_path):
     got = vxstate.read_state(tmp_path / "state_00001.bin")
     err = compare_states(got, golden("slab64", 2), 0.0)
     assert err["f"] > 0.0
+
+
+@pytest.mark.parametrize("name,k0,k1", [("amr2", 0, 3), ("beam2", 1, 3), ("beam3", 0, 3)])
+def test_port_amr_steps_match_reference(port, tmp_path, name, k0, k1):
+    """Multi-level step (ghost fills, interface fluxes, limiter exchange, nested moments)
+    from a reference state with the port's own dt."""
+    vxstate.write_state(golden(name, k0), tmp_path / "in.bin")
+    subprocess.run([str(port), *_args(name), f"load={tmp_path / 'in.bin'}", f"steps={k1 - k0}", "dump_every=1",
+                    f"dumpdir={tmp_path}"], check=True, capture_output=True, env={"OMP_NUM_THREADS": "4"})
+    for k in range(k0 + 1, k1 + 1):
+        if not (GOLDEN / f"{name}_s{k}.npz").exists():
+            continue
+        got = vxstate.read_state(tmp_path / f"state_{k - k0:05d}.bin")
+        err = compare_states(got, golden(name, k), 0.0)
+        assert max(err.values()) == 0.0, (k, err)
+
+
+@pytest.mark.parametrize("name", ["amr2", "beam2", "beam3"])
+def test_port_amr_step_after_regrid(port, tmp_path, name):
+    from helpers import golden_named
+
+    vxstate.write_state(golden_named(name, "post"), tmp_path / "in.bin")
+    ref = golden_named(name, "post1")
+    subprocess.run([str(port), *_args(name), f"load={tmp_path / 'in.bin'}", "steps=1", "dump_every=1",
+                    f"dumpdir={tmp_path}", f"dts={ref['dt']!r}"], check=True, capture_output=True,
+                   env={"OMP_NUM_THREADS": "4"})
+    err = compare_states(vxstate.read_state(tmp_path / "state_00001.bin"), ref, 0.0)
+    assert max(err.values()) == 0.0, err

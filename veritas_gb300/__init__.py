@@ -277,7 +277,8 @@ class SolverManager:
         _check(_lib.vx_run_get_field(self._h, fid, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(n)))
         return out
 
-    PROFILE_KERNELS = ["gamma", "faces", "flux", "ds_f2", "limR", "limC", "update", "moments", "assemble"]
+    PROFILE_KERNELS = ["gamma", "faces", "flux", "ds_f2", "limR", "limC", "update", "moments", "assemble", "poisson",
+                       "maxwell", "ghost", "iface", "csync"]
 
     def profile_kernels(self, reps: int = 5) -> dict:
         buf = (ctypes.c_double * 16)()

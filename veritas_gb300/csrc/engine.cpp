@@ -450,6 +450,37 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     al.fields = L.dfields.as<RunFields>();
     al.stream = stream;
     time_it([&] { launch_assemble(al); });
+    PoissonLaunch pl{};
+    pl.lu = L.dlu.as<LUDev>();
+    pl.fields = L.dfields.as<RunFields>();
+    pl.w = L.dw.as<double>();
+    pl.fcoef = L.dfcoef.as<double>();
+    pl.nruns = 1;
+    pl.maxn = L.maxn;
+    pl.stream = stream;
+    time_it([&] { launch_poisson(pl); });
+    MaxwellLaunch mx{};
+    mx.fields = L.dfields.as<RunFields>();
+    mx.nruns = 1;
+    mx.maxnf = L.maxnf;
+    mx.params = L.dparams.as<double>();
+    mx.dxinv = L.ddxinv.as<double>();
+    mx.step = 0;
+    mx.stream = stream;
+    time_it([&] { launch_maxwell(mx); });
+    // the AMR op batches of one stage (each entry: all batches of that kind)
+    time_it([&] {
+        for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++)
+            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, stream);
+    });
+    time_it([&] {
+        for (size_t b = 0; b + 1 < L.iface_ptr.size(); b++)
+            launch_iface(L.dpatch.p, L.diface.as<IfaceOp>() + L.iface_ptr[b], L.iface_ptr[b + 1] - L.iface_ptr[b], 0, stream);
+    });
+    time_it([&] {
+        for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++)
+            launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], stream);
+    });
     return out;
 }
 
