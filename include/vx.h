@@ -55,7 +55,10 @@ typedef struct vx_problem {
     double a0, fwhm, delay;  /* laser amplitude, field-envelope FWHM and delay [periods] */
     double cfl, minEff, crit, sizeWeight;
     int32_t quadDepth;
-    int32_t precision; /* 64: plain FP64 path; 32: FP32 precision form */
+    int32_t precision; /* 64: plain FP64 path; 32: FP32 precision form (f, fluxes and
+                        * limiter in FP32 scaled by 1/peak of the initial f; moments
+                        * accumulated and fields advanced in FP64; Poisson by prefix
+                        * scans instead of the dense LU) */
     double bdens, bp0, bTe; /* beam population: density fraction of the slab, drift, temperature [keV] */
 } vx_problem;
 

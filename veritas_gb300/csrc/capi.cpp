@@ -153,10 +153,10 @@ int vx_ctx_kernel_launches(vx_ctx *ctx, uint64_t *out) {
 int vx_run_create(vx_ctx *ctx, const vx_problem *prob, vx_run **out) {
     if (!ctx || !prob || !out) return VX_ERR_INVALID;
     return guard([&] {
-        if (prob->precision != 64) throw std::invalid_argument("only precision 64 is available in this build");
+        if (prob->precision != 64 && prob->precision != 32) throw std::invalid_argument("precision must be 64 or 32");
         auto r = std::make_unique<vx_run>();
         r->ctx = ctx;
-        r->run.reset(new vx::Run(*ctx->eng, std::make_shared<vx::LaserSlab>(to_params(*prob))));
+        r->run.reset(new vx::Run(*ctx->eng, std::make_shared<vx::LaserSlab>(to_params(*prob)), prob->precision));
         r->run->init();
         ctx->eng->runs.push_back(r->run.get());
         *out = r.release();

@@ -35,7 +35,10 @@ DevBuf &DevBuf::operator=(DevBuf &&o) noexcept {
 }
 
 // ---------------------------------------------------------------- Run
-Run::Run(Engine &e, std::shared_ptr<Problem> prob) : eng(e) {
+static_assert(sizeof(PatchT<float>) == sizeof(PatchT<double>), "descriptor layouts must match");
+
+Run::Run(Engine &e, std::shared_ptr<Problem> prob, int prec) : eng(e), precision(prec) {
+    if (prec != kF64 && prec != kF32) throw std::invalid_argument("precision must be 64 or 32");
     Input grid;
     Particles particles;
     Output output;
@@ -43,6 +46,11 @@ Run::Run(Engine &e, std::shared_ptr<Problem> prob) : eng(e) {
     S.reset(new Settings(grid, particles, output, prob));
     rects.resize(S->q.size());
     for (auto &sp : rects) sp.resize(S->maxDepth + 1);
+    // the FP32 form stores f / (peak of the initial distribution)
+    fnorm.assign(S->q.size(), 1.0);
+    if (precision == kF32)
+        for (size_t sp = 0; sp < fnorm.size(); sp++)
+            if (S->fMax[sp] > 0) fnorm[sp] = 1.0 / S->fMax[sp];
     // Rectangle.cpp:94-101: weights onto the r sub-cells of a coarse cell
     const int r = S->refinementRatio;
     std::vector<double> w;
@@ -76,14 +84,15 @@ static const int kPlanes = 28;
 void Run::allocate_rect(Rect &r) {
     r.pitch = ((r.n_p + 4) + 7) / 8 * 8;
     size_t pe = r.plane_elems();
-    r.slab = DevBuf(pe * kPlanes * sizeof(double));
+    r.esize = precision == kF32 ? 4 : 8;
+    r.slab = DevBuf(pe * kPlanes * r.esize);
     const int rtb = (int)std::pow(S->refinementRatio, r.depth);
     r.cols = DevBuf((size_t)2 * r.n_x * rtb * sizeof(double) + 64);
     PatchT<double> &d = r.desc;
     std::memset(&d, 0, sizeof d);
-    double *base = r.slab.as<double>();
+    char *base = r.slab.as<char>();
     int k = 0;
-    auto plane = [&]() { return base + pe * (k++); };
+    auto plane = [&]() { return (double *)(base + pe * r.esize * (k++)); };
     d.f0 = plane();
     d.f1 = plane();
     d.f2 = plane();
@@ -133,6 +142,21 @@ void Run::upload_rect_desc(Rect &r, int run_index) {
     d.cc = kCs * kCs * s.GetMass(sp);
     double m_inv = 1 / s.GetMass(sp);
     d.g2 = (m_inv * kCInv) * (m_inv * kCInv);
+    d.fnorm = fnorm[sp];
+    d.pnorm = m_inv * kCInv;
+    d.dpn = d.dp * d.pnorm;
+    d.kx = d.dp_inv * d.cc;
+    d.kp = d.cc * d.dx_inv;
+    d.weno_eps = (float)std::max(1e-10 * d.fnorm * d.fnorm, 1e-30);
+    d.pminf = (float)(d.pmin * d.pnorm);
+    d.dpnf = (float)d.dpn;
+    d.kxf = (float)d.kx;
+    d.kpf = (float)d.kp;
+    d.dxif = (float)d.dx_inv;
+    d.dpif = (float)d.dp_inv;
+    d.qf = (float)d.q;
+    d.a2nf = (float)(d.qq * d.g2);
+    if (precision == kF32 && d.rtb > 8) throw std::invalid_argument("the FP32 form supports up to 8 finest cells per coarse cell");
     double *cols = r.cols.as<double>();
     d.chargeR = cols;
     d.currentR = cols + (size_t)r.n_x * d.rtb;
@@ -180,6 +204,15 @@ void Run::init_rect_distribution(Rect &r) {
         });
     }
     for (auto &x : th) x.join();
+    if (r.esize == 4) {
+        std::vector<float> h32(host.size());
+        const double fn = fnorm[r.species];
+        for (size_t q = 0; q < host.size(); q++) h32[q] = (float)(host[q] * fn);
+        VX_CUDA(cudaMemcpyAsync(r.desc.f0, h32.data(), r.plane_bytes(), cudaMemcpyHostToDevice, eng.stream));
+        VX_CUDA(cudaMemcpyAsync(r.desc.f1, h32.data(), r.plane_bytes(), cudaMemcpyHostToDevice, eng.stream));
+        VX_CUDA(cudaStreamSynchronize(eng.stream));
+        return;
+    }
     size_t bytes = host.size() * sizeof(double);
     VX_CUDA(cudaMemcpyAsync(r.desc.f0, host.data(), bytes, cudaMemcpyHostToDevice, eng.stream));
     VX_CUDA(cudaMemcpyAsync(r.desc.f1, host.data(), bytes, cudaMemcpyHostToDevice, eng.stream));
@@ -207,6 +240,8 @@ void Run::alloc_fields() {
     dneut = DevBuf((size_t)n * sizeof(double));
     defin = DevBuf((size_t)n * sizeof(double));
     dex0 = DevBuf(sizeof(double));
+    dasq32 = DevBuf((size_t)(n + 1) * sizeof(float));
+    defin32 = DevBuf((size_t)n * sizeof(float));
     F.n = n;
     F.pre = pre;
     F.post = post;
@@ -226,6 +261,8 @@ void Run::alloc_fields() {
     F.efin = defin.as<double>();
     F.ex0 = dex0.as<double>();
     F.asq_cell = nullptr;
+    F.asq32 = dasq32.as<float>();
+    F.efin32 = defin32.as<float>();
 }
 
 void Run::upload_lu() {
@@ -274,9 +311,13 @@ void Run::init() {
     }
     alloc_fields();
     push_data(1);
-    int info = lu.build(n);
-    if (info) throw std::runtime_error("Poisson operator is singular");
-    upload_lu();
+    if (precision == kF32) {
+        build_poisson_fast();
+    } else {
+        int info = lu.build(n);
+        if (info) throw std::runtime_error("Poisson operator is singular");
+        upload_lu();
+    }
     layout_version++;
     enforce_neutralization();
 }
@@ -294,7 +335,7 @@ int64_t Run::state_size() const {
     int64_t len = 0;
     for (auto &sp : rects)
         for (auto &lvl : sp)
-            for (auto &r : lvl) len += (int64_t)r->plane_elems();
+            for (auto &r : lvl) len += (int64_t)((r->plane_bytes() + 7) / 8);
     return len + 6 * (int64_t)nf + (n + 1) + n + 1;
 }
 
@@ -305,10 +346,11 @@ void Run::step_host(const double *in, double *out, double dt) {
     for (auto &sp : rects)
         for (auto &lvl : sp)
             for (auto &r : lvl) {
-                size_t b = r->plane_elems() * sizeof(double);
+                // FP32 runs pack the scaled float plane two values per double slot
+                size_t b = r->plane_bytes();
                 VX_CUDA(cudaMemcpyAsync(r->desc.f0, p, b, cudaMemcpyHostToDevice, st));
                 VX_CUDA(cudaMemcpyAsync(r->desc.f1, r->desc.f0, b, cudaMemcpyDeviceToDevice, st));
-                p += r->plane_elems();
+                p += (b + 7) / 8;
             }
     for (double *X : {F.By, F.Bz, F.Ey, F.Ez, F.Ay, F.Az}) {
         VX_CUDA(cudaMemcpyAsync(X, p, (size_t)nf * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -331,8 +373,8 @@ void Run::state_to_host(double *out) {
     for (auto &sp : rects)
         for (auto &lvl : sp)
             for (auto &r : lvl) {
-                VX_CUDA(cudaMemcpyAsync(q, r->desc.f0, r->plane_elems() * sizeof(double), cudaMemcpyDeviceToHost, st));
-                q += r->plane_elems();
+                VX_CUDA(cudaMemcpyAsync(q, r->desc.f0, r->plane_bytes(), cudaMemcpyDeviceToHost, st));
+                q += (r->plane_bytes() + 7) / 8;
             }
     for (double *X : {F.By, F.Bz, F.Ey, F.Ez, F.Ay, F.Az}) {
         VX_CUDA(cudaMemcpyAsync(q, X, (size_t)nf * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -406,6 +448,30 @@ double Engine::measure_fp64_peak() {
     return flops / (ms * 1e-3) / 1e9;
 }
 
+// Precision dispatch of the per-stage kernels of a launch set.
+static void fct_sub(const LaunchSet &L, const FctLaunch &fl, int sub) {
+    if (L.precision == kF32) launch_fct32_substep(fl, sub);
+    else launch_fct64_substep(fl, sub);
+}
+static void run_moments(const LaunchSet &L, const MomLaunch &ml) {
+    if (L.precision == kF32) launch_moments32(ml);
+    else launch_moments64(ml);
+}
+static void run_poisson(const LaunchSet &L, const PoissonLaunch &pl) {
+    if (L.precision == kF32) {
+        PoissonFastLaunch f{};
+        f.pf = L.dpf.as<PoissonFastDev>();
+        f.fields = pl.fields;
+        f.w = pl.w;
+        f.fcoef = pl.fcoef;
+        f.nruns = pl.nruns;
+        f.stream = pl.stream;
+        launch_poisson_fast(f);
+    } else {
+        launch_poisson(pl);
+    }
+}
+
 std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     LaunchSet &L = get_set({&run});
     FctLaunch fl{};
@@ -414,6 +480,7 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     fl.ntiles = L.ntiles;
     fl.fields = L.dfields.as<RunFields>();
     fl.params = L.dparams.as<double>();
+    fl.params32 = L.dparams32.as<float>();
     fl.step = 0;
     fl.stream = stream;
     std::vector<double> out;
@@ -426,7 +493,7 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     };
     // stage-0 parameters with dt = 0 keep every kernel well defined
     for (int sub : {kSubGamma, kSubFaces, kSubFlux, kSubDsF2, kSubLimR, kSubLimC, kSubUpdate})
-        time_it([&] { launch_fct64_substep(fl, sub); });
+        time_it([&] { fct_sub(L, fl, sub); });
     MomLaunch ml{};
     ml.patches = L.dpatch.p;
     ml.colpatch = L.dcolpatch.as<int>();
@@ -436,7 +503,7 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     ml.fields = L.dfields.as<RunFields>();
     ml.Lbuf = L.dLbuf.as<double>();
     ml.stream = stream;
-    time_it([&] { launch_moments64(ml); });
+    time_it([&] { run_moments(L, ml); });
     AsmLaunch al{};
     al.patches = L.dpatch.p;
     al.lvl_ptr = L.dlvl_ptr.as<int>();
@@ -458,7 +525,7 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     pl.nruns = 1;
     pl.maxn = L.maxn;
     pl.stream = stream;
-    time_it([&] { launch_poisson(pl); });
+    time_it([&] { run_poisson(L, pl); });
     MaxwellLaunch mx{};
     mx.fields = L.dfields.as<RunFields>();
     mx.nruns = 1;
@@ -471,15 +538,15 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     // the AMR op batches of one stage (each entry: all batches of that kind)
     time_it([&] {
         for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++)
-            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, stream);
+            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, L.precision, stream);
     });
     time_it([&] {
         for (size_t b = 0; b + 1 < L.iface_ptr.size(); b++)
-            launch_iface(L.dpatch.p, L.diface.as<IfaceOp>() + L.iface_ptr[b], L.iface_ptr[b + 1] - L.iface_ptr[b], 0, stream);
+            launch_iface(L.dpatch.p, L.diface.as<IfaceOp>() + L.iface_ptr[b], L.iface_ptr[b + 1] - L.iface_ptr[b], 0, L.precision, stream);
     });
     time_it([&] {
         for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++)
-            launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], stream);
+            launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], L.precision, stream);
     });
     return out;
 }
@@ -510,6 +577,13 @@ LaunchSet &Engine::get_set(const std::vector<Run *> &set) {
 }
 
 void Engine::build_set(LaunchSet &L) {
+    L.precision = L.runs.empty() ? kF64 : L.runs[0]->precision;
+    for (Run *R : L.runs)
+        if (R->precision != L.precision)
+            throw std::invalid_argument("runs advanced together must share one precision");
+    std::vector<PoissonFastDev> pfs;
+    for (Run *R : L.runs) pfs.push_back(R->pfdev);
+    L.dpf = upload(pfs, stream);
     std::vector<TileRef> tiles;
     std::vector<int> colpatch, colidx, lvl_ptr, lvl_off, lvl_patch, run_n, run_ns, run_nl;
     std::vector<RunFields> fields;
@@ -655,6 +729,8 @@ void Engine::build_set(LaunchSet &L) {
     L.dcfl_out = DevBuf(L.runs.size() * sizeof(double));
     L.hparams.assign(L.runs.size() * 6 * kParamStride, 0.0);
     L.dparams = DevBuf(L.hparams.size() * sizeof(double));
+    L.hparams32.assign(L.hparams.size(), 0.0f);
+    L.dparams32 = DevBuf(L.hparams32.size() * sizeof(float));
     if (L.graph) {
         cudaGraphExecDestroy(L.graph);
         L.graph = nullptr;
@@ -672,6 +748,7 @@ void Engine::record_step(LaunchSet &L) {
     fl.ntiles = L.ntiles;
     fl.fields = L.dfields.as<RunFields>();
     fl.params = L.dparams.as<double>();
+    fl.params32 = L.dparams32.as<float>();
     fl.use_f0 = 0;
     fl.stream = stream;
     MomLaunch ml{};
@@ -711,32 +788,36 @@ void Engine::record_step(LaunchSet &L) {
     mx.dxinv = L.ddxinv.as<double>();
     mx.stream = stream;
     for (int s = 0; s < 6; s++) {
-        launch_moments64(ml);
+        run_moments(L, ml);
         launch_assemble(al);
-        launch_poisson(pl);
+        run_poisson(L, pl);
+        if (L.precision == kF32) {
+            launch_fields_to_f32(L.dfields.as<RunFields>(), (int)L.runs.size(), L.maxn, stream);
+            launches++;
+        }
         launches += 4;
         fl.step = s;
-        launch_fct64_substep(fl, kSubGamma);
-        launch_fct64_substep(fl, kSubFaces);
-        launch_fct64_substep(fl, kSubFlux);
+        fct_sub(L, fl, kSubGamma);
+        fct_sub(L, fl, kSubFaces);
+        fct_sub(L, fl, kSubFlux);
         launches += 3;
         for (size_t b = 0; b + 1 < L.iface_ptr.size(); b++, launches++)
-            launch_iface(L.dpatch.p, L.diface.as<IfaceOp>() + L.iface_ptr[b], L.iface_ptr[b + 1] - L.iface_ptr[b], s, stream);
-        launch_fct64_substep(fl, kSubDsF2);
+            launch_iface(L.dpatch.p, L.diface.as<IfaceOp>() + L.iface_ptr[b], L.iface_ptr[b + 1] - L.iface_ptr[b], s, L.precision, stream);
+        fct_sub(L, fl, kSubDsF2);
         launches += 1;
         for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
-            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 2, stream);
-        launch_fct64_substep(fl, kSubLimR);
-        launch_fct64_substep(fl, kSubLimC);
+            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 2, L.precision, stream);
+        fct_sub(L, fl, kSubLimR);
+        fct_sub(L, fl, kSubLimC);
         launches += 2;
         for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++, launches++)
-            launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], stream);
-        launch_fct64_substep(fl, kSubUpdate);
+            launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], L.precision, stream);
+        fct_sub(L, fl, kSubUpdate);
         launches += 1;
         for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
-            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, stream);
+            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, L.precision, stream);
         if (s == 5) {
-            launch_fct64_substep(fl, kSubCopy10);
+            fct_sub(L, fl, kSubCopy10);
             launches += 1;
         }
         mx.step = s;
@@ -787,6 +868,11 @@ void Engine::fill_params(LaunchSet &L, const std::vector<Run *> &set, const std:
     }
     VX_CUDA(cudaMemcpyAsync(L.dparams.p, L.hparams.data(), L.hparams.size() * sizeof(double), cudaMemcpyHostToDevice,
                             stream));
+    if (L.precision == kF32) {
+        for (size_t q = 0; q < L.hparams.size(); q++) L.hparams32[q] = (float)L.hparams[q];
+        VX_CUDA(cudaMemcpyAsync(L.dparams32.p, L.hparams32.data(), L.hparams32.size() * sizeof(float),
+                                cudaMemcpyHostToDevice, stream));
+    }
 }
 
 void Engine::advance(const std::vector<Run *> &set, const std::vector<double> &dt) {
@@ -872,7 +958,7 @@ void Engine::moments_only(const std::vector<Run *> &set) {
     ml.fields = L.dfields.as<RunFields>();
     ml.Lbuf = L.dLbuf.as<double>();
     ml.stream = stream;
-    launch_moments64(ml);
+    run_moments(L, ml);
     AsmLaunch al{};
     al.patches = L.dpatch.p;
     al.lvl_ptr = L.dlvl_ptr.as<int>();

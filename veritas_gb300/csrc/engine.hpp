@@ -62,8 +62,13 @@ struct Rect {
     DevBuf slab;   // all per-patch planes
     DevBuf cols;   // chargeR, currentR
     DevBuf masks;  // nested, ifx, ifp (AMR only)
+    // Device descriptor.  For FP32 runs the plane pointers address float planes: the
+    // layout of PatchT<float> is identical (see the static_assert in engine.cpp), and the
+    // host never dereferences them.
     PatchT<double> desc{};
+    int esize = 8;  // bytes per element of the planes (8: FP64 path, 4: FP32 form)
     size_t plane_elems() const { return (size_t)(n_x + 4) * pitch; }
+    size_t plane_bytes() const { return plane_elems() * esize; }
     // Connectivity (Rectangle.hpp:8-12): neighbour patch ids (flat index within the run)
     // or -1 for the domain boundary; "same level" flags; per-cell/face finer patch ids and
     // the nested / interface masks, indexed (i+2)*(n_p+4) + (j+2) as IndexNS.
@@ -87,7 +92,7 @@ struct PatchGeom {
 // (SolverManager.hpp:5-19): Settings, one mesh per species, the field solver.
 class Run {
 public:
-    Run(Engine &eng, std::shared_ptr<Problem> prob);
+    Run(Engine &eng, std::shared_ptr<Problem> prob, int precision = kF64);
     ~Run();
     Engine &eng;
     std::unique_ptr<Settings> S;
@@ -96,7 +101,7 @@ public:
     int n = 0, pre = 0, post = 0, nf = 0;
     double dx0 = 0;
     // fields
-    DevBuf dBy, dBz, dEy, dEz, dAy, dAz, dasq, dphi, dcharge, dJ, dneut, defin, dex0;
+    DevBuf dBy, dBz, dEy, dEz, dAy, dAz, dasq, dphi, dcharge, dJ, dneut, defin, dex0, dasq32, defin32;
     RunFields F{};
     PoissonLU lu;
     DevBuf dlu_perm, dlb_band, dlb_fptr, dlb_fcol, dlb_fval, dlb_slot, dlb_sload, dlb_take, dub_band, dub_diag, dub_rdiag, dub_rdlo, dub_fptr, dub_fcol,
@@ -104,6 +109,14 @@ public:
     LUDev ludev{};
     uint64_t layout_version = 0;
     int id = 0;
+    int precision = kF64;            // kF64: plain path; kF32: precision form
+    std::vector<double> fnorm;       // per species: scale of the stored FP32 f (1 for FP64)
+    // fast Poisson of the precision form (Woodbury columns and capacitance)
+    std::vector<double> pf_Y;
+    PoissonFastDev pfdev{};
+    DevBuf dpf_Y;
+    void build_poisson_fast();
+    void rebase_neutralization(const std::vector<std::vector<double>> &f1_planes);
 
     // SolverManager-level operations (SolverManager.cpp:8-164).
     void init();                        // constructor path: hierarchy, f(t=0), fields, neutralisation
@@ -168,9 +181,13 @@ struct LaunchSet {
         drun_nl, dlu, dw, dfcoef, dparams, dcfl_spec, dcfl_out, dns, ddxinv;
     int ntiles = 0, ncols = 0, maxnp = 0, maxn = 0, maxnf = 0;
     std::vector<double> hparams;  // per run: 6 stages x (8 fct + 8 maxwell + 2 laser)
+    std::vector<float> hparams32;
+    DevBuf dparams32;
     std::vector<double> w, fcoef;
     // AMR op tables of all runs, batch by batch (global patch ids)
     DevBuf dghost, diface, dcsync;
+    int precision = kF64;
+    DevBuf dpf;  // per-run PoissonFastDev (FP32 sets)
     std::vector<int> ghost_ptr, iface_ptr, csync_ptr;
     cudaGraphExec_t graph = nullptr;
     ~LaunchSet();

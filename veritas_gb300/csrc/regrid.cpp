@@ -252,6 +252,9 @@ std::vector<std::vector<std::pair<int, int>>> Run::flag_cells() {
         f.j1 = std::min(R->p_pos + R->n_p, s.GetPSize(R->depth, R->species) - offset) - R->p_pos;
         f.out_off = (long long)total;
         error_weights(s, R->depth, R->species, f.w);
+        // FP32 form: f is stored times fnorm, so the weights (which carry 1/fMax) are
+        // divided by it and the criterion stays as it is
+        for (double &wq : f.w) wq /= fnorm[R->species];
         f.crit = s.refinementCriteria;
         total += (size_t)R->n_x * R->n_p;
         fp.push_back(f);
@@ -263,7 +266,7 @@ std::vector<std::vector<std::pair<int, int>>> Run::flag_cells() {
         DevBuf dd = upload(descs, eng.stream);
         DevBuf dfp = upload(fp, eng.stream);
         DevBuf dout(total);
-        launch_flags(dd.p, dfp.as<FlagPatch>(), (int)fp.size(), dout.as<uint8_t>(), eng.stream);
+        launch_flags(dd.p, dfp.as<FlagPatch>(), (int)fp.size(), dout.as<uint8_t>(), precision, eng.stream);
         VX_CUDA(cudaMemcpyAsync(flags.data(), dout.p, total, cudaMemcpyDeviceToHost, eng.stream));
         eng.sync();
     }
@@ -499,7 +502,7 @@ void Run::transfer_from(std::vector<std::vector<std::vector<std::unique_ptr<Rect
     auto run_ops = [&](const std::vector<XferOp> &ops) {
         if (ops.empty()) return;
         DevBuf d = upload(ops, eng.stream);
-        launch_xfer(dd.p, d.as<XferOp>(), (int)ops.size(), dmask.as<uint8_t>(), eng.stream);
+        launch_xfer(dd.p, d.as<XferOp>(), (int)ops.size(), dmask.as<uint8_t>(), precision, eng.stream);
         eng.sync();
     };
     for (size_t sp = 0; sp < old.size(); sp++) {
@@ -543,7 +546,8 @@ void Run::push_data(int slot) {
     DevBuf dd = flat_descs();
     DevBuf dops = upload(ghost_ops, eng.stream);
     for (size_t b = 0; b + 1 < ghost_b.ptr.size(); b++)
-        launch_ghost(dd.p, dops.as<GhostOp>() + ghost_b.ptr[b], ghost_b.ptr[b + 1] - ghost_b.ptr[b], slot, eng.stream);
+        launch_ghost(dd.p, dops.as<GhostOp>() + ghost_b.ptr[b], ghost_b.ptr[b + 1] - ghost_b.ptr[b], slot, precision,
+                     eng.stream);
     eng.sync();
 }
 
@@ -552,7 +556,7 @@ void Run::copy_slot(int from, int to) {
     for (Rect *R : flat) {
         const double *src = from == 0 ? R->desc.f0 : (from == 1 ? R->desc.f1 : R->desc.f2);
         double *dst = to == 0 ? R->desc.f0 : (to == 1 ? R->desc.f1 : R->desc.f2);
-        VX_CUDA(cudaMemcpyAsync(dst, src, R->plane_elems() * sizeof(double), cudaMemcpyDeviceToDevice, eng.stream));
+        VX_CUDA(cudaMemcpyAsync(dst, src, R->plane_bytes(), cudaMemcpyDeviceToDevice, eng.stream));
     }
     eng.sync();
 }

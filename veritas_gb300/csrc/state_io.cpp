@@ -2,6 +2,7 @@
 // fields as EMFieldSolver stores them (8 RK slots per array, EMSolver.cpp:20-26) and
 // each patch's f as the reference's interleaved 3-slot block (Index3, Rectangle.hpp:96).
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 
 #include "engine.hpp"
@@ -57,6 +58,28 @@ std::vector<double> d2h(const double *d, size_t n, cudaStream_t s) {
 void h2d(double *d, const std::vector<double> &h, cudaStream_t s) {
     VX_CUDA(cudaMemcpyAsync(d, h.data(), h.size() * 8, cudaMemcpyHostToDevice, s));
 }
+// A patch plane in SI units: FP64 planes as they are, FP32 planes (scaled by fnorm)
+// converted back.
+std::vector<double> plane_to_host(const Rect &r, const double *d, double fnorm, cudaStream_t s) {
+    if (r.esize == 8) return d2h(d, r.plane_elems(), s);
+    std::vector<float> h(r.plane_elems());
+    VX_CUDA(cudaMemcpyAsync(h.data(), d, r.plane_bytes(), cudaMemcpyDeviceToHost, s));
+    VX_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> out(h.size());
+    for (size_t q = 0; q < h.size(); q++) out[q] = (double)h[q] / fnorm;
+    return out;
+}
+void plane_to_device(const Rect &r, double *d, const std::vector<double> &h, double fnorm, cudaStream_t s) {
+    if (r.esize == 8) {
+        h2d(d, h, s);
+        VX_CUDA(cudaStreamSynchronize(s));
+        return;
+    }
+    std::vector<float> h32(h.size());
+    for (size_t q = 0; q < h.size(); q++) h32[q] = (float)(h[q] * fnorm);
+    VX_CUDA(cudaMemcpyAsync(d, h32.data(), r.plane_bytes(), cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaStreamSynchronize(s));
+}
 }  // namespace
 
 void Run::load_state(const std::string &path) {
@@ -93,6 +116,8 @@ void Run::load_state(const std::string &path) {
     long long ns = f.ri();
     if (ns != (long long)rects.size()) throw std::invalid_argument("state file species count mismatch");
     std::vector<std::vector<std::vector<std::unique_ptr<Rect>>>> nr(ns);
+    std::vector<std::vector<double>> f1_host;  // FP32 runs: the loaded FP64 slot-1 planes
+    bool fp32_exact = true;                     // every loaded f is an FP32-form value
     for (long long sp = 0; sp < ns; sp++) {
         long long nl = f.ri();
         if (nl != S->maxDepth + 1) throw std::invalid_argument("state file level count mismatch");
@@ -122,8 +147,16 @@ void Run::load_state(const std::string &path) {
                         for (int j = -2; j < r->n_p + 2; j++)
                             plane[pidx(i, j, r->pitch)] = fv[3 * ((size_t)(r->n_p + 4) * (i + 2) + 2 + j) + slot];
                     double *dst = slot == 0 ? r->desc.f0 : (slot == 1 ? r->desc.f1 : r->desc.f2);
-                    h2d(dst, plane, st);
-                    eng.sync();
+                    plane_to_device(*r, dst, plane, fnorm[sp], st);
+                    if (slot == 1 && precision == kF32) {
+                        const double fn = fnorm[sp];
+                        for (double v : plane)
+                            if ((double)(float)(v * fn) / fn != v) {
+                                fp32_exact = false;
+                                break;
+                            }
+                        f1_host.push_back(plane);
+                    }
                 }
                 nr[sp][l].push_back(std::move(r));
             }
@@ -135,7 +168,90 @@ void Run::load_state(const std::string &path) {
         for (auto &lvl : sp)
             for (auto &rp : lvl) upload_rect_desc(*rp, 0);
     layout_version++;
+    // a state written by an FP32 run holds FP32-form values already: nothing to rebase
+    if (precision == kF32 && !fp32_exact) rebase_neutralization(f1_host);
     eng.refresh_efield(*this);
+    eng.sync();
+}
+
+// The FP32 form represents f rounded to FP32, whose charge density differs from the
+// FP64 state's by the rounding; the net charge of a plasma near neutrality is a small
+// difference of large numbers, so that offset would show up as a spurious E_x.  After
+// loading an FP64 state (one whose f values are not all FP32-form values), the
+// neutralising background is shifted by
+// (FP64 charge of the loaded f) - (FP32 charge of the rounded f), which makes the net
+// charge of the loaded state the same in both forms.  The FP64 charge follows the
+// column sums of Rectangle::CalculateRhoAndJ (Rectangle.cpp:157-282) and the level
+// assembly (Level.cpp:19-62, EMSolver.cpp:104-122) on the host.
+void Run::rebase_neutralization(const std::vector<std::vector<double>> &f1) {
+    const Settings &s = *S;
+    std::vector<std::vector<double>> colq(flat.size());
+    for (size_t k = 0; k < flat.size(); k++) {
+        const Rect &R = *flat[k];
+        const int rtb = (int)std::pow(s.refinementRatio, R.depth);
+        const double *f = f1[k].data();
+        std::vector<double> w(3 * rtb);
+        for (int i = 0; i < rtb; i++) {  // Rectangle.cpp:103-110
+            double tl = -0.5 + i / (double)rtb, tr = -0.5 + (i + 1.0) / (double)rtb;
+            w[3 * i] = (tl + tr) * 0.5;
+            w[3 * i + 1] = (tl * tl + tl * tr + tr * tr) / 3.0 - (1.0 / 12);
+            w[3 * i + 2] = (tl * tl * tl + tl * tl * tr + tl * tr * tr + tr * tr * tr) * 0.25;
+        }
+        auto rel = [&](int i, int j, int kk) {
+            const double f3 = f[pidx(i, j, R.pitch)];
+            if (rtb == 1) return f3;
+            double g1 = f[pidx(i - 2, j, R.pitch)] - f3, g2 = f[pidx(i - 1, j, R.pitch)] - f3;
+            double g4 = f[pidx(i + 1, j, R.pitch)] - f3, g5 = f[pidx(i + 2, j, R.pitch)] - f3;
+            double a1 = 0.104166666666667 * g1 + -0.708333333333334 * g2 + 0.708333333333334 * g4 + -0.104166666666667 * g5;
+            double a2 = 0.117647058823529 * g1 + 0.029411764705882 * g2 + 0.029411764705882 * g4 + 0.117647058823529 * g5;
+            double a3 = -0.083333333333333 * g1 + 0.166666666666667 * g2 + -0.166666666666667 * g4 + 0.083333333333334 * g5;
+            double te = 0.0, mine = 0.0;
+            for (int q = 0; q < rtb; q++) {
+                double v = w[3 * q] * a1 + w[3 * q + 1] * a2 + w[3 * q + 2] * a3 + f3;
+                te += v;
+                if (q == kk) mine = v;
+            }
+            return mine + (f3 - (1.0 / (double)rtb) * te);
+        };
+        const double dpq = s.GetDp(R.depth, R.species) * s.GetCharge(R.species);
+        colq[k].assign((size_t)R.n_x * rtb, 0.0);
+        for (int i = 0; i < R.n_x; i++)
+            for (int kk = 0; kk < rtb; kk++) {
+                double ch = 0.0;
+                for (int j = 0; j < R.n_p; j++)
+                    if (!R.nested[R.ns(i, j)]) ch += rel(i, j, kk);
+                colq[k][(size_t)i * rtb + kk] = ch * dpq;
+            }
+    }
+    std::vector<double> q64(n, 0.0);
+    for (int x = 0; x < n; x++) {
+        double charge = 0.0;
+        for (auto &sp : rects) {
+            double cs = 0.0;
+            for (auto &lvl : sp) {
+                double lc = 0.0;
+                for (auto &rp : lvl) {
+                    const Rect &R = *rp;
+                    const int rtb = (int)std::pow(s.refinementRatio, R.depth);
+                    int c = x - R.x_pos * rtb;
+                    if (c >= 0 && c < R.n_x * rtb) lc += colq[R.id][c];
+                }
+                cs += lc;
+            }
+            charge += cs;
+        }
+        q64[x] = charge;
+    }
+    cudaStream_t st = eng.stream;
+    auto keep_charge = d2h(F.charge, (size_t)n, st);
+    auto keep_J = d2h(F.J, (size_t)n, st);
+    auto neut = d2h(F.neut, (size_t)n, st);
+    eng.moments_only({this});
+    auto q32 = d2h(F.charge, (size_t)n, st);
+    for (int x = 0; x < n; x++) neut[x] += q64[x] - q32[x];
+    h2d(F.neut, neut, st);
+    h2d(F.charge, keep_charge, st);
+    h2d(F.J, keep_J, st);
     eng.sync();
 }
 
@@ -185,7 +301,7 @@ void Run::save_state(const std::string &path) {
                 std::vector<double> fv(3 * cells, 0.0);
                 for (int slot = 0; slot < 3; slot++) {
                     const double *src = slot == 0 ? r.desc.f0 : (slot == 1 ? r.desc.f1 : r.desc.f2);
-                    auto plane = d2h(src, r.plane_elems(), st);
+                    auto plane = plane_to_host(r, src, fnorm[r.species], st);
                     for (int i = -2; i < r.n_x + 2; i++)
                         for (int j = -2; j < r.n_p + 2; j++)
                             fv[3 * ((size_t)(r.n_p + 4) * (i + 2) + 2 + j) + slot] = plane[pidx(i, j, r.pitch)];

@@ -52,6 +52,15 @@ struct PatchT {
     int r;                  // refinement ratio
     double dx, dp, dx_inv, dp_inv;
     double pmin, q, qq, mass, cc, g2;  // qq=q*q, cc=cs*cs*m, g2=(m_inv*c_inv)^2
+    // FP32 precision form: f is stored as f * fnorm; pnorm = 1/(m c) makes momenta
+    // dimensionless (dpn = dp * pnorm); kx = c^2 m / dp and kp = c^2 m / dx scale the
+    // rationalised Lorentz-factor differences into face velocities; weno_eps is the WENO
+    // regulariser in the scaled units.
+    double fnorm, pnorm, dpn, kx, kp;
+    float weno_eps;
+    // FP32 copies of the scalars the FP32 kernels use (no FP64 arithmetic in their
+    // loops): p_min / (m c), dp / (m c), kx, kp, 1/dx, 1/dp, q, q^2 / (m c)^2
+    float pminf, dpnf, kxf, kpf, dxif, dpif, qf, a2nf;
     T *f0, *f1, *f2;
     T *gam;                 // gamma at (x-face i, p-face j), i in [-1,nx+1], j in [-1,np+1]
     T *ex, *fx, *ep, *fp;   // face velocities and reconstructed face values
@@ -79,6 +88,8 @@ struct RunFields {
     double *efin;       // E_x at finest cells, n (recomputed after every Poisson solve)
     double *ex0;        // scalar
     double *asq_cell;   // cell-average A^2 at finest cells (Ay/Az slot 1), n
+    float *asq32;       // FP32 copies of asq (n+1) and efin (n) for the FP32 form
+    float *efin32;
 };
 
 VX_HD inline int pidx(int i, int j, int pitch) { return (i + 2) * pitch + (j + 2); }

@@ -35,12 +35,14 @@ struct FctLaunch {
     int ntiles;
     const RunFields *fields;  // device array, one per run
     const double *params;     // per-run stage parameter blocks
+    const float *params32;    // the same blocks in FP32 (FP32 form)
     int step;
     int use_f0;
     cudaStream_t stream;
 };
 
 void launch_fct64_substep(const FctLaunch &L, int sub);
+void launch_fct32_substep(const FctLaunch &L, int sub);
 
 // ---------------------------------------------------------------- moments
 struct MomLaunch {
@@ -54,6 +56,7 @@ struct MomLaunch {
     cudaStream_t stream;
 };
 void launch_moments64(const MomLaunch &M);
+void launch_moments32(const MomLaunch &M);
 
 // Assembly of rho and J on the finest grid (EMSolver::AssembleRhoAndJ).
 struct AsmLaunch {
@@ -104,6 +107,26 @@ struct PoissonLaunch {
     cudaStream_t stream;
 };
 void launch_poisson(const PoissonLaunch &L);
+
+// Poisson solve of the FP32 precision form by prefix scans (fields32.cu).  Y holds the
+// m x 3 Woodbury columns (row-major), K the 3x3 capacitance factor.
+constexpr int kPfMaxSeg = 64;  // elements per thread: n - 1 <= 1024 * kPfMaxSeg
+struct PoissonFastDev {
+    const double *Y;
+    double K[9];
+    double rho, c_inv, w1, w2;
+};
+struct PoissonFastLaunch {
+    const PoissonFastDev *pf;  // per run
+    RunFields *fields;         // per run (device array)
+    const double *w;           // per run: dx0^2
+    const double *fcoef;       // per run: 1/(12 dx0)
+    int nruns;
+    cudaStream_t stream;
+};
+void launch_poisson_fast(const PoissonFastLaunch &L);
+// FP32 copies of a^2 and E_x of every run of a set (the FP32 form reads these).
+void launch_fields_to_f32(RunFields *fields, int nruns, int maxn, cudaStream_t s);
 void launch_efield(RunFields *fields, const double *fcoef, int nruns, int maxn, cudaStream_t s);
 
 // Maxwell RK stage + face interpolation of A (EMSolver::RGKStep).
@@ -135,13 +158,14 @@ void launch_fp64_peak(double *out, int blocks, int threads, int iters, cudaStrea
 struct GhostOp;
 struct IfaceOp;
 struct CSyncOp;
-void launch_ghost(const void *patches, const GhostOp *ops, int n, int slot, cudaStream_t s);
-void launch_iface(const void *patches, const IfaceOp *ops, int n, int step, cudaStream_t s);
-void launch_csync(const void *patches, const CSyncOp *ops, int n, cudaStream_t s);
+// `prec` selects the patch storage type (kF64 or kF32) of the descriptor array.
+void launch_ghost(const void *patches, const GhostOp *ops, int n, int slot, int prec, cudaStream_t s);
+void launch_iface(const void *patches, const IfaceOp *ops, int n, int step, int prec, cudaStream_t s);
+void launch_csync(const void *patches, const CSyncOp *ops, int n, int prec, cudaStream_t s);
 struct FlagPatch;
 struct XferOp;
-void launch_flags(const void *patches, const FlagPatch *fp, int n, uint8_t *out, cudaStream_t s);
-void launch_xfer(const void *patches, const XferOp *ops, int n, uint8_t *mask, cudaStream_t s);
+void launch_flags(const void *patches, const FlagPatch *fp, int n, uint8_t *out, int prec, cudaStream_t s);
+void launch_xfer(const void *patches, const XferOp *ops, int n, uint8_t *mask, int prec, cudaStream_t s);
 
 // dst[i] = -src[i]
 void launch_negate(double *dst, const double *src, int n, cudaStream_t s);
