@@ -115,6 +115,8 @@ int vx_update_hierarchy(const vx_problem *prob, int species, const int32_t *patc
 /* Advance several runs of one context together, one launch per sub-step for all of
  * them (batched form).  dt[i] belongs to runs[i]. */
 int vx_runs_advance(vx_run *const *runs, const double *dt, int nruns);
+/* CalculateDt of several runs of one context in one launch; dt[i] belongs to runs[i]. */
+int vx_runs_calculate_dt(vx_run *const *runs, double *dt, int nruns);
 
 /* Simulation time (Settings::time, Settings.cpp:166-179). */
 int vx_run_time(vx_run *run, double *t);
@@ -168,6 +170,30 @@ int vx_run_state_to_host(vx_run *run, double *state_out);
  * SolverManager::Advance on state that lives in host memory): copy state_in to the
  * device, run one RK step with dt, copy the new state to state_out. */
 int vx_run_step_host(vx_run *run, const double *state_in, double *state_out, double dt);
+
+/* ---------------------------------------------------------------- serving loop
+ * No reference counterpart (the reference runs one solve per process): continuous
+ * batching of independent solves on one context under a device-memory budget.
+ * submit() queues a solve of `steps` RK steps (arrival on the server's clock, seconds);
+ * step() admits, in arrival order, the waiting solves that fit in the budget, advances
+ * every live solve one step in one batched launch set and retires the finished ones
+ * (writing their final state to state_path when one was given). */
+typedef struct vx_server vx_server;
+typedef struct vx_request_result {
+    int32_t finished;
+    int64_t steps_done;
+    double arrival, admitted, finish; /* server clock, seconds; -1 until reached */
+    double sim_time;                  /* simulated time at the end of the solve */
+    int64_t cells;                    /* phase-space cells of the final hierarchy */
+    uint64_t device_bytes;            /* device memory the solve held */
+} vx_request_result;
+int vx_server_create(vx_ctx *ctx, uint64_t hbm_budget_bytes, int max_live, vx_server **out);
+int vx_server_destroy(vx_server *s);
+int vx_server_clock(vx_server *s, double *now);
+int vx_server_submit(vx_server *s, const vx_problem *p, int64_t steps, double arrival, const char *state_path,
+                     int64_t *id);
+int vx_server_step(vx_server *s, int *live, int *waiting);
+int vx_server_result(vx_server *s, int64_t id, vx_request_result *out);
 
 #ifdef __cplusplus
 }

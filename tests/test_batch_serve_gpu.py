@@ -1,0 +1,98 @@
+"""Batched and served forms: every solve's result is the same alone and in a mix.
+
+The batched launch set runs one kernel per sub-step over all patches of all runs, and
+the serving loop admits and retires solves between steps; neither lets one run's data
+reach another's arithmetic, so the states must match bit for bit (both precisions).
+"""
+import dataclasses
+
+import pytest
+
+import vxstate
+from helpers import golden, problem_for
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from veritas_gb300 import Context
+
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def _bytes(s, path):
+    s.save_state(path)
+    return path.read_bytes()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [64, 32])
+def test_batched_equals_separate(ctx, tmp_path, precision):
+    from veritas_gb300 import SolverManager, advance_many, calculate_dt_many
+
+    names = ["slab64", "amr2", "drift128", "beam2"]
+    probs = [dataclasses.replace(problem_for(n), precision=precision) for n in names]
+    alone = [SolverManager(ctx, p) for p in probs]
+    mixed = [SolverManager(ctx, p) for p in probs]
+    for step in range(3):
+        dts = calculate_dt_many(mixed)
+        for s, dt in zip(alone, dts):
+            assert s.CalculateDt() == dt
+            s.Advance(dt)
+        advance_many(mixed, dts)
+    for k, (a, m) in enumerate(zip(alone, mixed)):
+        assert _bytes(a, tmp_path / f"a{k}.bin") == _bytes(m, tmp_path / f"m{k}.bin"), names[k]
+    for s in alone + mixed:
+        s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [64, 32])
+def test_served_result_same_alone_and_in_mix(ctx, tmp_path, precision):
+    from veritas_gb300 import Server
+
+    X = dataclasses.replace(problem_for("amr2"), precision=precision)
+    Y = dataclasses.replace(problem_for("drift128"), precision=precision)
+    Z = dataclasses.replace(problem_for("beam3"), precision=precision)
+    srv = Server(ctx, 8 << 30)
+    rid = srv.submit(X, 3, state_path=tmp_path / "alone.bin")
+    while srv.step() != (0, 0):
+        pass
+    assert srv.result(rid)["finished"] == 1
+    srv.close()
+
+    srv = Server(ctx, 8 << 30)
+    ry = srv.submit(Y, 4)
+    srv.step()  # Y runs alone for one step
+    rx = srv.submit(X, 3, state_path=tmp_path / "mix.bin")  # joins while Y is live
+    rz = srv.submit(Z, 2)
+    while srv.step() != (0, 0):
+        pass
+    for r in (rx, ry, rz):
+        assert srv.result(r)["finished"] == 1
+    assert srv.result(rx)["admitted"] >= srv.result(ry)["admitted"]
+    assert (tmp_path / "alone.bin").read_bytes() == (tmp_path / "mix.bin").read_bytes()
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_server_admits_by_memory_budget(ctx):
+    """A budget that holds one solve at a time: the second waits for the first to retire."""
+    from veritas_gb300 import Server
+
+    P = problem_for("slab64")
+    srv = Server(ctx, 1 << 30)
+    a = srv.submit(P, 2)
+    srv.step()
+    used = srv.result(a)["device_bytes"]
+    srv.close()
+    srv = Server(ctx, int(used * 1.5))
+    a = srv.submit(P, 2)
+    b = srv.submit(P, 2)
+    while srv.step() != (0, 0):
+        pass
+    ra, rb = srv.result(a), srv.result(b)
+    assert ra["finished"] and rb["finished"]
+    assert rb["admitted"] >= ra["finish"]
+    srv.close()

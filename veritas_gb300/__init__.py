@@ -50,6 +50,14 @@ class _Problem(ctypes.Structure):
     ]
 
 
+class _RequestResult(ctypes.Structure):
+    _fields_ = [
+        ("finished", ctypes.c_int32), ("steps_done", ctypes.c_int64), ("arrival", ctypes.c_double),
+        ("admitted", ctypes.c_double), ("finish", ctypes.c_double), ("sim_time", ctypes.c_double),
+        ("cells", ctypes.c_int64), ("device_bytes", ctypes.c_uint64),
+    ]
+
+
 def _load() -> ctypes.CDLL:
     if not LIB_PATH.exists():
         raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'` first")
@@ -68,6 +76,14 @@ def _load() -> ctypes.CDLL:
         "vx_run_calculate_dt": (ctypes.c_int, [vp, P(ctypes.c_double)]),
         "vx_run_advance": (ctypes.c_int, [vp, ctypes.c_double]),
         "vx_runs_advance": (ctypes.c_int, [P(vp), P(ctypes.c_double), ctypes.c_int]),
+        "vx_runs_calculate_dt": (ctypes.c_int, [P(vp), P(ctypes.c_double), ctypes.c_int]),
+        "vx_server_create": (ctypes.c_int, [vp, ctypes.c_uint64, ctypes.c_int, P(vp)]),
+        "vx_server_destroy": (ctypes.c_int, [vp]),
+        "vx_server_clock": (ctypes.c_int, [vp, P(ctypes.c_double)]),
+        "vx_server_submit": (ctypes.c_int, [vp, P(_Problem), ctypes.c_int64, ctypes.c_double, ctypes.c_char_p,
+                                             P(ctypes.c_int64)]),
+        "vx_server_step": (ctypes.c_int, [vp, P(ctypes.c_int), P(ctypes.c_int)]),
+        "vx_server_result": (ctypes.c_int, [vp, ctypes.c_int64, P(_RequestResult)]),
         "vx_run_advance_fields": (ctypes.c_int, [vp, ctypes.c_double]),
         "vx_run_regrid": (ctypes.c_int, [vp]),
         "vx_error_weights": (ctypes.c_int, [P(_Problem), ctypes.c_int, ctypes.c_int, P(ctypes.c_double),
@@ -367,3 +383,55 @@ def advance_many(runs: list[SolverManager], dts: list[float]) -> None:
     arr = (ctypes.c_void_p * len(runs))(*[r.handle for r in runs])
     d = (ctypes.c_double * len(runs))(*dts)
     _check(_lib.vx_runs_advance(arr, d, len(runs)))
+
+
+def calculate_dt_many(runs: list[SolverManager]) -> list[float]:
+    """CalculateDt of several runs of one context in one launch."""
+    arr = (ctypes.c_void_p * len(runs))(*[r.handle for r in runs])
+    out = (ctypes.c_double * len(runs))()
+    _check(_lib.vx_runs_calculate_dt(arr, out, len(runs)))
+    return list(out)
+
+
+class Server:
+    """Continuous-batching serving loop on one context (vx_server)."""
+
+    def __init__(self, ctx: Context, hbm_budget_bytes: int, max_live: int = 64):
+        h = ctypes.c_void_p()
+        _check(_lib.vx_server_create(ctx.handle, int(hbm_budget_bytes), int(max_live), ctypes.byref(h)))
+        self.ctx = ctx
+        self._h = h
+        ctx._runs.add(self)  # closed with the context, before it
+
+    def clock(self) -> float:
+        v = ctypes.c_double()
+        _check(_lib.vx_server_clock(self._h, ctypes.byref(v)))
+        return float(v.value)
+
+    def submit(self, problem: Problem, steps: int, arrival: float | None = None, state_path=None) -> int:
+        rid = ctypes.c_int64()
+        t = self.clock() if arrival is None else float(arrival)
+        path = None if state_path is None else str(state_path).encode()
+        _check(_lib.vx_server_submit(self._h, ctypes.byref(problem.to_c()), int(steps), t, path, ctypes.byref(rid)))
+        return int(rid.value)
+
+    def step(self) -> tuple[int, int]:
+        live, waiting = ctypes.c_int(), ctypes.c_int()
+        _check(_lib.vx_server_step(self._h, ctypes.byref(live), ctypes.byref(waiting)))
+        return int(live.value), int(waiting.value)
+
+    def result(self, rid: int) -> dict:
+        r = _RequestResult()
+        _check(_lib.vx_server_result(self._h, rid, ctypes.byref(r)))
+        return {k: getattr(r, k) for k, _ in r._fields_}
+
+    def close(self) -> None:
+        if self._h:
+            _check(_lib.vx_server_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -4,6 +4,7 @@
 
 #include "../../include/vx.h"
 #include "engine.hpp"
+#include "serve.hpp"
 
 struct vx_ctx {
     std::unique_ptr<vx::Engine> eng;
@@ -11,6 +12,10 @@ struct vx_ctx {
 struct vx_run {
     vx_ctx *ctx;
     std::unique_ptr<vx::Run> run;
+};
+struct vx_server {
+    vx_ctx *ctx;
+    std::unique_ptr<vx::Server> srv;
 };
 
 namespace {
@@ -274,6 +279,20 @@ int vx_update_hierarchy(const vx_problem *prob, int species, const int32_t *patc
     });
 }
 
+int vx_runs_calculate_dt(vx_run *const *runs, double *dt, int nruns) {
+    if (!runs || !dt || nruns <= 0) return VX_ERR_INVALID;
+    return guard([&] {
+        std::vector<vx::Run *> set;
+        vx_ctx *c = runs[0]->ctx;
+        for (int i = 0; i < nruns; i++) {
+            if (!runs[i] || runs[i]->ctx != c) throw std::invalid_argument("runs must belong to one context");
+            set.push_back(runs[i]->run.get());
+        }
+        auto v = c->eng->calculate_dt(set);
+        for (int i = 0; i < nruns; i++) dt[i] = v[i];
+    });
+}
+
 int vx_runs_advance(vx_run *const *runs, const double *dt, int nruns) {
     if (!runs || !dt || nruns <= 0) return VX_ERR_INVALID;
     return guard([&] {
@@ -394,6 +413,60 @@ int vx_run_state_to_host(vx_run *run, double *state_out) {
 int vx_run_step_host(vx_run *run, const double *state_in, double *state_out, double dt) {
     if (!run || !state_in || !state_out || !(dt >= 0)) return VX_ERR_INVALID;
     return guard([&] { run->run->step_host(state_in, state_out, dt); });
+}
+
+int vx_server_create(vx_ctx *ctx, uint64_t hbm_budget_bytes, int max_live, vx_server **out) {
+    if (!ctx || !out || hbm_budget_bytes == 0 || max_live <= 0) return VX_ERR_INVALID;
+    return guard([&] {
+        auto s = std::make_unique<vx_server>();
+        s->ctx = ctx;
+        s->srv.reset(new vx::Server(*ctx->eng, (size_t)hbm_budget_bytes, max_live));
+        *out = s.release();
+    });
+}
+
+int vx_server_destroy(vx_server *s) {
+    if (!s) return VX_ERR_INVALID;
+    return guard([&] {
+        s->ctx->eng->sync();
+        delete s;
+    });
+}
+
+int vx_server_clock(vx_server *s, double *now) {
+    if (!s || !now) return VX_ERR_INVALID;
+    *now = s->srv->clock();
+    return VX_OK;
+}
+
+int vx_server_submit(vx_server *s, const vx_problem *p, int64_t steps, double arrival, const char *state_path,
+                     int64_t *id) {
+    if (!s || !p || !id) return VX_ERR_INVALID;
+    return guard([&] { *id = s->srv->submit(to_params(*p), p->precision, steps, arrival, state_path ? state_path : ""); });
+}
+
+int vx_server_step(vx_server *s, int *live, int *waiting) {
+    if (!s) return VX_ERR_INVALID;
+    return guard([&] {
+        int l = s->srv->step(s->srv->clock());
+        if (live) *live = l;
+        if (waiting) *waiting = s->srv->waiting();
+    });
+}
+
+int vx_server_result(vx_server *s, int64_t id, vx_request_result *out) {
+    if (!s || !out) return VX_ERR_INVALID;
+    return guard([&] {
+        const auto &r = s->srv->request(id);
+        out->finished = r.finished ? 1 : 0;
+        out->steps_done = r.done_steps;
+        out->arrival = r.arrival;
+        out->admitted = r.admitted;
+        out->finish = r.finish;
+        out->sim_time = r.sim_time;
+        out->cells = r.cells;
+        out->device_bytes = r.bytes;
+    });
 }
 
 }  // extern "C"

@@ -184,6 +184,25 @@ void Run::init_rect_distribution(Rect &r) {
     const double dx = s.GetDx(r.depth), dp = s.GetDp(r.depth, r.species);
     const double pmin = s.pmin[r.species];
     std::vector<double> host((size_t)(r.n_x + 4) * r.pitch, 0.0);
+    if (precision == kF32 && s.problem->Separable()) {
+        // same sample points, summed as (sum_k density)(sum_l profile)
+        std::vector<double> dx_sum(r.n_x, 0.0), dp_sum(r.n_p, 0.0);
+        for (int i = 0; i < r.n_x; i++)
+            for (int k = 0; k < nvals; k++) dx_sum[i] += s.problem->Density(s, ((0.5 + k) / nvals + i + r.x_pos) * dx);
+        for (int j = 0; j < r.n_p; j++)
+            for (int l = 0; l < nvals; l++)
+                dp_sum[j] += s.problem->Profile(s, pmin + dp * ((0.5 + l) / nvals + j + r.p_pos), r.species);
+        const double inv = 1 / std::pow(nvals, 2.0);
+        for (int i = 0; i < r.n_x; i++)
+            for (int j = 0; j < r.n_p; j++) host[pidx(i, j, r.pitch)] = dx_sum[i] * dp_sum[j] * inv;
+        std::vector<float> h32(host.size());
+        const double fn = fnorm[r.species];
+        for (size_t q = 0; q < host.size(); q++) h32[q] = (float)(host[q] * fn);
+        VX_CUDA(cudaMemcpyAsync(r.desc.f0, h32.data(), r.plane_bytes(), cudaMemcpyHostToDevice, eng.stream));
+        VX_CUDA(cudaMemcpyAsync(r.desc.f1, h32.data(), r.plane_bytes(), cudaMemcpyHostToDevice, eng.stream));
+        VX_CUDA(cudaStreamSynchronize(eng.stream));
+        return;
+    }
     unsigned nth = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
     std::vector<std::thread> th;
     for (unsigned t = 0; t < nth; t++) {
@@ -501,7 +520,6 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     ml.ncols = L.ncols;
     ml.maxnp = L.maxnp;
     ml.fields = L.dfields.as<RunFields>();
-    ml.Lbuf = L.dLbuf.as<double>();
     ml.stream = stream;
     time_it([&] { run_moments(L, ml); });
     AsmLaunch al{};
@@ -599,7 +617,7 @@ void Engine::build_set(LaunchSet &L) {
         int ns = (int)R.rects.size(), nl = s.maxDepth + 1;
         lvl_off.push_back((int)lvl_ptr.size());
         std::vector<int> ptr;
-        ptr.push_back(0);
+        ptr.push_back((int)lvl_patch.size());  // absolute: this run's first patch
         for (int sp = 0; sp < ns; sp++) {
             for (int l = 0; l < nl; l++) {
                 for (auto &rp : R.rects[sp][l]) {
@@ -713,7 +731,6 @@ void Engine::build_set(LaunchSet &L) {
     L.dfields = upload(fields, stream);
     L.dcolpatch = upload(colpatch, stream);
     L.dcolidx = upload(colidx, stream);
-    L.dLbuf = DevBuf((size_t)std::max(1, L.ncols) * (L.maxnp + 2) * sizeof(double));
     L.dlvl_ptr = upload(lvl_ptr, stream);
     L.dlvl_off = upload(lvl_off, stream);
     L.dlvl_patch = upload(lvl_patch, stream);
@@ -758,7 +775,6 @@ void Engine::record_step(LaunchSet &L) {
     ml.ncols = L.ncols;
     ml.maxnp = L.maxnp;
     ml.fields = L.dfields.as<RunFields>();
-    ml.Lbuf = L.dLbuf.as<double>();
     ml.stream = stream;
     AsmLaunch al{};
     al.patches = L.dpatch.p;
@@ -956,7 +972,6 @@ void Engine::moments_only(const std::vector<Run *> &set) {
     ml.ncols = L.ncols;
     ml.maxnp = L.maxnp;
     ml.fields = L.dfields.as<RunFields>();
-    ml.Lbuf = L.dLbuf.as<double>();
     ml.stream = stream;
     run_moments(L, ml);
     AsmLaunch al{};

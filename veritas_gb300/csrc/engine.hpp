@@ -117,6 +117,7 @@ public:
     DevBuf dpf_Y;
     void build_poisson_fast();
     void rebase_neutralization(const std::vector<std::vector<double>> &f1_planes);
+    size_t device_bytes() const;     // device memory held by this run
 
     // SolverManager-level operations (SolverManager.cpp:8-164).
     void init();                        // constructor path: hierarchy, f(t=0), fields, neutralisation
@@ -177,7 +178,7 @@ struct LaunchSet {
     std::vector<Run *> runs;
     uint64_t key_version = 0;
     std::vector<PatchT<double>> hpatch;
-    DevBuf dpatch, dtiles, dfields, dcolpatch, dcolidx, dLbuf, dlvl_ptr, dlvl_off, dlvl_patch, drun_n, drun_ns,
+    DevBuf dpatch, dtiles, dfields, dcolpatch, dcolidx, dlvl_ptr, dlvl_off, dlvl_patch, drun_n, drun_ns,
         drun_nl, dlu, dw, dfcoef, dparams, dcfl_spec, dcfl_out, dns, ddxinv;
     int ntiles = 0, ncols = 0, maxnp = 0, maxn = 0, maxnf = 0;
     std::vector<double> hparams;  // per run: 6 stages x (8 fct + 8 maxwell + 2 laser)

@@ -140,6 +140,18 @@ double LaserSlab::InitialDistribution(const Settings &s, double x, double p, int
     return v;
 }
 
+double LaserSlab::Density(const Settings &s, double x) const { return s.temp[0][0] * slab_density(x / P.lambda); }
+
+double LaserSlab::Profile(const Settings &s, double p, int particleType) const {
+    double dpv = p - s.temp[particleType][2];
+    double v = std::exp(-(dpv * dpv) / (2.0 * s.temp[particleType][1])) / std::sqrt(kDPI * s.temp[particleType][1]);
+    if (P.bdens != 0.0) {
+        double dbv = p - beam_p;
+        v += P.bdens * std::exp(-(dbv * dbv) / (2.0 * beam_T)) / std::sqrt(kDPI * beam_T);
+    }
+    return v;
+}
+
 double LaserSlab::GetBY(const Settings &s, double x, double t) const { return 0.0; }
 
 // Linearly polarised pulse A_y = A0 g(t - x/c) cos(w t - k x) with a Gaussian field

@@ -50,6 +50,11 @@ public:
     virtual double GetBZ(const Settings &s, double x, double t) const = 0;
     virtual bool RefinementOverride(const Settings &s, double x, double p, int depth, int particleType) const = 0;
     virtual bool HasRefinementOverride() const { return true; }
+    // Optional: f(x, p) = density(x) * profile(p).  A problem that says so lets the FP32
+    // form integrate the initial cell averages as a product of two 1-D quadratures.
+    virtual bool Separable() const { return false; }
+    virtual double Density(const Settings &, double) const { return 0.0; }
+    virtual double Profile(const Settings &, double, int) const { return 0.0; }
 };
 
 // Parameters of the built-in laser / plasma-slab problem (lengths in laser wavelengths,
@@ -82,6 +87,9 @@ public:
         return false;
     }
     bool HasRefinementOverride() const override { return false; }
+    bool Separable() const override { return true; }
+    double Density(const Settings &s, double x) const override;
+    double Profile(const Settings &s, double p, int particleType) const override;
     double slab_density(double xl) const;
     LaserSlabParams P;
     double beam_T = 0.0, beam_p = 0.0;  // beam temperature [J] and drift [kg m/s]

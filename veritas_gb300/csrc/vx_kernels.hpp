@@ -52,7 +52,6 @@ struct MomLaunch {
     int ncols;
     int maxnp;            // largest n_p over the patches
     const RunFields *fields;
-    double *Lbuf;         // scratch: log-ratio table, ncols * (maxnp + 2)
     cudaStream_t stream;
 };
 void launch_moments64(const MomLaunch &M);
@@ -61,7 +60,7 @@ void launch_moments32(const MomLaunch &M);
 // Assembly of rho and J on the finest grid (EMSolver::AssembleRhoAndJ).
 struct AsmLaunch {
     const void *patches;
-    const int *lvl_ptr;    // per run, (ns*nl + 1) offsets into lvl_patch (relative to run)
+    const int *lvl_ptr;    // per run, (ns*nl + 1) absolute offsets into lvl_patch
     const int *lvl_off;    // per run: offset of its lvl_ptr block
     const int *lvl_patch;  // patch indices level by level, in each level's patch order
     const int *run_n;      // per run: n
