@@ -1,19 +1,24 @@
 #!/usr/bin/env python3
 """Benchmark: phase-space cell-updates/s of the Vlasov–Maxwell RK step on GB300.
 
-Workload: the single-level FP64 laser / plasma-slab case (Nx=2048, Np=256, x in [0,100]
-lambda, p in [-2,2] m_e c, 0.01 n_c slab on [20,80] with 5-lambda ramps, T=1 keV,
-a0=1 Gaussian pulse of FWHM 10 periods, CFL 0.5) on synthetic seeded inputs.
-One step = CalculateDt + one full six-stage RK step (moments, Poisson, Vlasov FCT stage,
-Maxwell stage, six times).  The metric counts every phase-space cell of every patch
-once per step.
+Workload: the block-structured AMR FP64 laser / plasma-slab case — base grid Nx=4096,
+Np=512, two levels with refinement ratio 2, refinement criterion 1e-6 with size weight 1
+(x in [0,100] lambda, p in [-2,2] m_e c, 0.01 n_c slab on [20,80] with 5-lambda ramps,
+T=1 keV, a0=1 Gaussian pulse of FWHM 10 periods, CFL 0.5), the hierarchy built by the
+initial flagging / clustering.  Inputs are synthetic (the analytic initial plasma).
+One step = CalculateDt + one full six-stage RK step (moments, Poisson, Vlasov FCT stage
+of every patch of every level with the ghost fills, interface fluxes and limiter
+exchange, Maxwell stage, six times); regridding is outside the timed region, as in the
+reference's own timing of SolverManager::Advance.  The metric counts every phase-space
+cell of every patch of every level (covered coarse cells included) once per step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 N>1 (torchrun) runs N independent replicas, one per GPU ("replicas only": a single solve
 has no sharded data path here); value sums the replicas' cells over the max-over-ranks
 time.  --impl reference times the reference algorithm on the host cores instead: the
-oracle port (C++ restatement pinned to the reference build), with all host threads.
+oracle port (C++ restatement pinned bit-exact to the reference build), with all host
+threads, from the same initial hierarchy.
 """
 from __future__ import annotations
 
@@ -32,7 +37,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "phase-space cell-updates/s"
 UNIT = "cell-updates/s"
-WORKLOAD = "laser_slab_Nx2048_Np256_1level_fp64"
+WORKLOAD = "laser_slab_amr_Nx4096_Np512_2level_r2_fp64"
 MEASURED = ROOT / "MEASURED_PEAKS.json"
 
 # Compulsory DRAM bytes per padded cell of each profiled kernel (each plane read or
@@ -42,6 +47,10 @@ KERNEL_BYTES = {"gamma": 8, "faces": 48, "flux": 72, "ds_f2": 64, "limR": 48, "l
 # Algorithmic FP64 operations per padded cell (a division counts as one operation).
 KERNEL_FLOPS = {"gamma": 6, "faces": 125, "flux": 20, "ds_f2": 8, "limR": 34, "limC": 4, "update": 8,
                 "moments": 30, "assemble": 0}
+KERNEL_NAMES = {"gamma": "k64_gamma", "faces": "k64_faces", "flux": "k64_flux", "ds_f2": "k64_ds_f2",
+                "limR": "k64_limR", "limC": "k64_limC", "update": "k64_update", "moments": "k64_moments",
+                "assemble": "k_assemble", "poisson": "k_poisson", "maxwell": "k_maxwell*", "ghost": "k_ghost",
+                "iface": "k_iface", "csync": "k_csync"}
 
 
 def problem_config1():
@@ -49,6 +58,14 @@ def problem_config1():
 
     return Problem(L=100.0, nx=2048, np=256, Lfinest=1, pmax=2.0, dens=0.01, x1=15, x2=20, x3=80, x4=85, Te=1.0,
                    a0=1.0, fwhm=10.0, delay=10.0, cfl=0.5, quadDepth=2, precision=64)
+
+
+def problem_config2():
+    """Two-level AMR laser / slab case: base 4096 x 512, refinement ratio 2."""
+    p = problem_config1()
+    p.nx, p.np, p.Lfinest, p.r = 4096, 512, 2, 2
+    p.crit, p.sizeWeight = 1e-6, 1.0
+    return p
 
 
 class ClockSampler:
@@ -107,40 +124,202 @@ def dist_info():
     return world, rank, local
 
 
-def cpu_reference(args, cells_per_step_full: int, sample_steps: int, threads: int, nx: int, np_: int) -> dict:
-    """Time the oracle port (reference algorithm, C++ OpenMP) on the host cores."""
+def cpu_reference(state_path: Path, sample_steps: int, threads: int) -> dict:
+    """Time the oracle port (reference algorithm, C++ OpenMP) on the host cores, from the
+    state in `state_path` (the initial hierarchy of the workload)."""
     exe = ROOT / "oracle" / "_port" / "veritas_port"
     if not exe.exists():
         return {"unavailable": "oracle port not built (run __graft_entry__.build())"}
-    p = problem_config1()
-    p.nx, p.np = nx, np_
+    p = problem_config2()
     env = dict(os.environ, OMP_NUM_THREADS=str(threads))
-    cmd = [str(exe), *p.harness_args(), f"time_steps={sample_steps}"]
+    cmd = [str(exe), *p.harness_args(), f"load={state_path}", f"time_steps={sample_steps}"]
     out = subprocess.run(cmd, capture_output=True, text=True, env=env, check=True).stdout
     rec = json.loads(out.strip().splitlines()[-1])
     return {"value": rec["cells"] / rec["median_s"], "best": rec["cells"] / rec["best_s"], "cells": rec["cells"],
             "median_s": rec["median_s"], "threads": rec["threads"]}
 
 
+def initial_state(path: Path, device: int) -> int:
+    """Builds the workload's initial hierarchy (flagging / clustering / quadrature) and
+    writes it as a state file; returns the cell count."""
+    from veritas_gb300 import Context, SolverManager
+
+    ctx = Context(device)
+    s = SolverManager(ctx, problem_config2())
+    s.save_state(path)
+    cells = s.cell_count()
+    s.close()
+    ctx.close()
+    return cells
+
+
 def run_reference(args) -> None:
-    world, rank, _ = dist_info()
+    world, rank, local = dist_info()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     steps = max(1, args.steps)
-    rec = cpu_reference(args, 0, steps, threads, 2048, 256)
+    with tempfile.TemporaryDirectory() as td:
+        st = Path(td) / "init.bin"
+        initial_state(st, local)
+        rec = cpu_reference(st, steps, threads)
     if "unavailable" in rec:
         print(json.dumps({"impl": "reference", "unavailable": rec["unavailable"]}))
         return
     v = rec["value"]
+    sample = (f"{steps} timed RK steps (median) of the full workload ({rec['cells']} cells) after 1 warm-up, "
+              "from its initial hierarchy")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": steps,
             "warmup": 1, "ms_per_step": rec["median_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "cells_per_step": rec["cells"]},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": rec["threads"], "kind": "port",
-                             "sample": f"{steps} timed RK steps (median) of the full 2048x256 case after 1 warm-up"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": rec["threads"], "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+EPS0, MU0 = 8.854187817e-12, 1.0 / 795774.715482
+
+
+def field_energy(s):
+    import numpy as np
+
+    nf = s.field("Ey").size // 8
+    Ey, Ez, By, Bz = (s.field(k)[:nf] for k in ("Ey", "Ez", "By", "Bz"))
+    Ex = s.field("Ex")
+    return 0.5 * EPS0 * float(np.sum(Ey * Ey) + np.sum(Ez * Ez) + np.sum(Ex * Ex)) + \
+        0.5 / MU0 * float(np.sum(By * By) + np.sum(Bz * Bz))
+
+
+def measure_fp32_form(ctx, init_path: Path, steps: int, warmup: int) -> dict:
+    """The FP32 precision form on the same workload: throughput, and its error against
+    the FP64 path over `steps` steps from the same state with the same dt sequence."""
+    import dataclasses
+
+    import numpy as np
+
+    from veritas_gb300 import SolverManager
+
+    sys.path.insert(0, str(ROOT / "tests"))
+    import vxstate
+
+    p32 = dataclasses.replace(problem_config2(), precision=32)
+    s = SolverManager(ctx, p32)
+    cells = s.cell_count()
+    for _ in range(warmup):
+        s.Advance(s.CalculateDt())
+    ctx.sync()
+    times = []
+    for _ in range(steps):
+        ctx.flush_l2()
+        ctx.timer_begin()
+        s.Advance(s.CalculateDt())
+        times.append(ctx.timer_end())
+    prof = s.profile_kernels(reps=5)
+    s.close()
+    ms = sum(times) / len(times)
+    # error against the FP64 path from the FP64 initial state
+    a, b = SolverManager(ctx, problem_config2()), SolverManager(ctx, p32)
+    a.load_state(init_path)
+    b.load_state(init_path)
+    # E_x is normalised by the laser's field amplitude a0 m c omega / |q| (near t = 0 the
+    # plasma is neutral and E_x itself is rounding noise, so a relative error means nothing)
+    e0 = p32.a0 * 9.10938291e-31 * 299792458.0 * (2 * np.pi * 299792458.0 / p32.lambda_) / 1.60217657e-19
+    ew = ee = ey = 0.0
+    for _ in range(steps):
+        dt = a.CalculateDt()
+        a.Advance(dt)
+        b.Advance(dt)
+        wa, wb = field_energy(a), field_energy(b)
+        ew = max(ew, abs(wb - wa) / max(abs(wa), 1e-300))
+        xa, xb = a.field("Ex"), b.field("Ex")
+        ee = max(ee, float(np.max(np.abs(xb - xa))) / e0)
+        ya, yb = a.field("Ey"), b.field("Ey")
+        ey = max(ey, float(np.max(np.abs(yb - ya))) / e0)
+    with tempfile.TemporaryDirectory() as td:
+        a.save_state(Path(td) / "a.bin")
+        b.save_state(Path(td) / "b.bin")
+        sa, sb = vxstate.read_state(Path(td) / "a.bin"), vxstate.read_state(Path(td) / "b.bin")
+    num = den = 0.0
+    for la, lb in zip(sa["species"][0], sb["species"][0]):
+        for ra, rb in zip(la, lb):
+            fa, fb = ra["f"][2:-2, 2:-2, 0], rb["f"][2:-2, 2:-2, 0]
+            num = max(num, float(np.max(np.abs(fb - fa))))
+            den = max(den, float(np.max(np.abs(fa))))
+    a.close()
+    b.close()
+    return {"value": cells / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "dtype": "f32 (moments, fields, Poisson f64)",
+            "error_vs_fp64": {"steps": steps, "from": "the FP64 run's initial hierarchy (t = 0), same dt sequence",
+                              "f_rel_linf": num / den, "field_energy_rel_max": ew,
+                              "Ex_abs_max_over_laser_E0": ee, "Ey_abs_max_over_laser_E0": ey},
+            "kernel_ms": prof}
+
+
+def measure_batched(ctx, count: int, steps: int, warmup: int, precision: int) -> dict:
+    """The seeded ensemble of `count` independent runs advanced together: one launch per
+    sub-step for all runs (captured in one CUDA graph per step)."""
+    from veritas_gb300 import SolverManager, advance_many, calculate_dt_many
+    from veritas_gb300.ensemble import ensemble_problems
+
+    t0 = time.perf_counter()
+    runs = [SolverManager(ctx, p) for p in ensemble_problems(count, precision=precision)]
+    init_s = time.perf_counter() - t0
+    cells = sum(r.cell_count() for r in runs)
+    for _ in range(warmup):
+        advance_many(runs, calculate_dt_many(runs))
+    ctx.sync()
+    times = []
+    for _ in range(steps):
+        ctx.timer_begin()
+        advance_many(runs, calculate_dt_many(runs))
+        times.append(ctx.timer_end())
+    for r in runs:
+        r.close()
+    ms = sum(times) / len(times)
+    return {"value": cells / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "runs": count, "cells_per_step": cells,
+            "init_s": init_s, "precision": precision,
+            "sampler": "splitmix64 seed 0x5EED0004, stream r = run r (veritas_gb300/ensemble.py)"}
+
+
+def measure_serving(ctx, count: int, steps: int, precision: int, budget_gb: float = 150.0) -> dict:
+    """Serving loop: Poisson arrivals at 20 solves/s (seed 0x5EED0005) of ensemble-sampled
+    problems, each run for `steps` RK steps, admitted under the HBM budget and batched
+    with whatever else is live."""
+    import dataclasses
+
+    import numpy as np
+
+    from veritas_gb300 import Server
+    from veritas_gb300.ensemble import arrival_times, ensemble_problems
+
+    probs = [dataclasses.replace(p, precision=precision) for p in ensemble_problems(count)]
+    arr = arrival_times(count)
+    srv = Server(ctx, int(budget_gb * (1 << 30)), max_live=count)
+    start = srv.clock()
+    ids, nxt = [], 0
+    done_cells = 0
+    while True:
+        now = srv.clock() - start
+        while nxt < count and arr[nxt] <= now:
+            ids.append(srv.submit(probs[nxt], steps, arrival=start + arr[nxt]))
+            nxt += 1
+        live, waiting = srv.step()
+        if nxt >= count and live == 0 and waiting == 0:
+            break
+        if live == 0 and waiting == 0 and nxt < count:
+            time.sleep(max(0.0, arr[nxt] - (srv.clock() - start)))
+    end = srv.clock()
+    res = [srv.result(i) for i in ids]
+    srv.close()
+    lat = np.array([r["finish"] - r["arrival"] for r in res])
+    cells = sum(r["cells"] for r in res) * steps
+    return {"solves": count, "steps_per_solve": steps, "precision": precision,
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "mean": float(lat.mean())},
+            "solves_per_s": count / (end - start), "cell_updates_per_s": cells / (end - start),
+            "arrivals": "Poisson, 20 solves/s, splitmix64 seed 0x5EED0005", "hbm_budget_gb": budget_gb,
+            "note": "each solve is scaled to a fixed step count (the full 50-period solves of this size mix "
+                    "exceed one GPU's throughput at this arrival rate by two orders of magnitude)"}
 
 
 def main() -> None:
@@ -150,6 +329,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the FP32 / batched / served forms (FP64 headline line only)")
     ap.add_argument("--lite", action="store_true",
                     help="only the warm-up and timed steps (used under ncu); no e2e, kernel timing or CPU baseline")
     args = ap.parse_args()
@@ -170,8 +351,11 @@ def main() -> None:
     from veritas_gb300 import Context, PinnedArray, SolverManager
 
     ctx = Context(local)
-    s = SolverManager(ctx, problem_config1())
+    s = SolverManager(ctx, problem_config2())
     cells = s.cell_count()
+    init_path = Path(tempfile.mkdtemp()) / "init.bin"
+    if rank == 0 and not args.lite and not (args.no_cpu_baseline and args.no_forms):
+        s.save_state(init_path)  # the CPU baseline and the FP32 error check start from it
     for _ in range(warmup):
         s.Advance(s.CalculateDt())
     ctx.sync()
@@ -221,48 +405,81 @@ def main() -> None:
     e2e = {"value": cells * world * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n,
            "d2h_bytes_per_step": 8 * n + 8}
 
-    # ---- dominant kernel, live CUDA-event timing
+    # ---- per-kernel live CUDA-event timing (context stream); shares per step
     prof = s.profile_kernels(reps=5)
-    padded = (2048 + 4) * (256 + 4)
-    launches_per_step = {"gamma": 6, "faces": 6, "flux": 6, "ds_f2": 6, "limR": 6, "limC": 6, "update": 6,
-                         "moments": 6, "assemble": 6}
-    share = {k: prof[k] * launches_per_step[k] for k in prof}
+    layout = s.layout()
+    padded = sum((l[4] + 4) * (l[5] + 4) for l in layout)
+    per_step = {k: 6 for k in prof}
+    per_step["ghost"] = 12  # two fills (slots 2 and 1) per stage
+    share = {k: prof[k] * per_step[k] for k in prof}
+    tot = sum(share.values())
     dom = max(share, key=share.get)
     peaks = json.loads(MEASURED.read_text()) if MEASURED.exists() else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    ach = KERNEL_BYTES[dom] * padded / (prof[dom] * 1e-3) / 1e9
     fp64_peak = ctx.measure_fp64_peak()
-    fp64_ach = KERNEL_FLOPS[dom] * padded / (prof[dom] * 1e-3) / 1e9
-    traffic = _read_traffic(dom)
-    roofline = {"kernel": f"k64_{dom}", "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                "frac": ach / hbm_peak, "traffic": traffic, "peak_source": "measured" if peaks else "fallback",
-                "algorithmic_bytes_per_launch": KERNEL_BYTES[dom] * padded,
-                "fp64": {"achieved_gflops": fp64_ach, "peak_gflops": fp64_peak, "frac": fp64_ach / fp64_peak,
-                         "note": "FP64 issue rate is the binding roofline of the plain path; peak measured live "
-                                 "with a DFMA chain kernel"},
-                "kernel_ms": prof}
+    n_fine = s.field("phi").size
+
+    def kernel_roofline(k):
+        if k == "poisson":
+            # the two band factors (4 coefficients per row each), the diagonal and its
+            # two-word reciprocal, the permutation, the right-hand side and the result
+            bpl = n_fine * (8 * 8 + 3 * 8 + 4 + 8 + 8)
+            flops = n_fine * 20
+        else:
+            bpl = KERNEL_BYTES.get(k, 0) * padded
+            flops = KERNEL_FLOPS.get(k, 0) * padded
+        ach = bpl / (prof[k] * 1e-3) / 1e9
+        return {"kernel": k, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                "frac": ach / hbm_peak, "algorithmic_bytes_per_launch": bpl, "ms_per_launch": prof[k],
+                "fp64": {"achieved_gflops": flops / (prof[k] * 1e-3) / 1e9, "peak_gflops": fp64_peak,
+                         "frac": flops / (prof[k] * 1e-3) / 1e9 / fp64_peak}}
+
+    roofline = kernel_roofline(dom)
+    roofline.update({"kernel": KERNEL_NAMES.get(dom, dom), "traffic": _read_traffic(dom),
+                     "peak_source": "measured" if peaks else "fallback",
+                     "share_of_step": share[dom] / tot,
+                     "note": ("the exact Poisson solve is two serial triangular recurrences in the reference's "
+                              "rounding order: one thread's FP64 latency chain, not bandwidth, bounds it"
+                              if dom == "poisson" else "FP64 issue rate is the binding roofline of the plain path"),
+                     "kernel_ms": prof, "kernel_share": {k: share[k] / tot for k in share}})
+    stencil = max((k for k in share if k in KERNEL_BYTES and KERNEL_BYTES[k] > 0), key=share.get)
+    roofline["stencil"] = kernel_roofline(stencil)
+    roofline["stencil"]["kernel"] = KERNEL_NAMES.get(stencil, stencil)
+
+    forms = None
+    if rank == 0 and not args.no_forms:
+        forms = {"fp32": measure_fp32_form(ctx, init_path, args.steps, warmup),
+                 "batched_fp32": measure_batched(ctx, 64, 5, 3, 32),
+                 "served_fp32": measure_serving(ctx, 24, 16, 32),
+                 "served_fp64": measure_serving(ctx, 24, 16, 64)}
+        forms["fp32_speedup_vs_fp64"] = forms["fp32"]["value"] / value
+        forms["batched_fp32_speedup_vs_fp64"] = forms["batched_fp32"]["value"] / value
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        rec = cpu_reference(args, cells, 3, os.cpu_count() or 1, 2048, 256)
+        rec = cpu_reference(init_path, 3, os.cpu_count() or 1)
         if "unavailable" not in rec:
             cpu = {"value": rec["value"], "unit": UNIT, "cores": rec["threads"], "kind": "port",
-                   "sample": "3 timed RK steps (median) of the full 2048x256 case after 1 warm-up"}
+                   "sample": f"3 timed RK steps (median) of the full workload ({rec['cells']} cells) after 1 "
+                             "warm-up, from the same initial hierarchy"}
         else:
             cpu = {"value": None, "unavailable": rec["unavailable"]}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "cells_per_step": cells, "l2": "flushed before every timed step",
+                "config": {"workload": WORKLOAD, "cells_per_step": cells, "levels": 2, "patches": len(layout),
+                           "l2": "flushed before every timed step",
                            "parallelism": f"replicas{world}"},
                 "clocks": clk.summary(), "gpu_launches": launches, "e2e": e2e, "roofline": roofline,
-                "cpu_baseline": cpu}
+                "cpu_baseline": cpu, "forms": forms}
         print(json.dumps(line))
     hin.close()
     hout.close()
     s.close()
     ctx.close()
+    if init_path.exists():
+        init_path.unlink()
     if dist:
         dist.destroy_process_group()
 

@@ -574,8 +574,16 @@ __global__ void k_poisson(PoissonLaunch L) {
 
 void launch_poisson(const PoissonLaunch &L) {
     PoissonLaunch P = L;
-    P.x_in_smem = L.maxn <= kPoisSmemMaxN ? 1 : 0;
-    const int smem = 2 * (int)sizeof(PoisBandChunk) + (P.x_in_smem ? 8 * L.maxn : 0);
+    static int max_smem = 0;
+    if (!max_smem) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    // the solution vector joins the two chunk buffers in shared memory when it fits
+    const int base = 2 * (int)sizeof(PoisBandChunk);
+    P.x_in_smem = (L.maxn <= kPoisSmemMaxN && base + 8 * L.maxn <= max_smem) ? 1 : 0;
+    const int smem = base + (P.x_in_smem ? 8 * L.maxn : 0);
     cudaFuncSetAttribute(k_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     k_poisson<<<L.nruns, 512, smem, L.stream>>>(P);
 }
