@@ -329,6 +329,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", type=int, default=64, choices=[64, 32],
+                    help="precision of the headline workload (64, the plain path, unless profiling the FP32 form)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the FP32 / batched / served forms (FP64 headline line only)")
     ap.add_argument("--lite", action="store_true",
@@ -351,7 +353,9 @@ def main() -> None:
     from veritas_gb300 import Context, PinnedArray, SolverManager
 
     ctx = Context(local)
-    s = SolverManager(ctx, problem_config2())
+    import dataclasses
+
+    s = SolverManager(ctx, dataclasses.replace(problem_config2(), precision=args.precision))
     cells = s.cell_count()
     init_path = Path(tempfile.mkdtemp()) / "init.bin"
     if rank == 0 and not args.lite and not (args.no_cpu_baseline and args.no_forms):

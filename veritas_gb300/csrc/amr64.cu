@@ -54,7 +54,8 @@ __device__ void interp_block(const PatchT<T> &C, const T *f, int ic, int jc, T *
         interp_ref(C.refc, r, temps[0][k], temps[1][k], temps[2][k], temps[3][k], temps[4][k], out + k * r);
         for (int l = 0; l < r; l++) sum += out[k * r + l];
     }
-    T correction = f[pidx(ic, jc, pit)] - (T)(1.0 / pow((double)r, 2.0)) * sum;
+    // 1 / r^2: r^2 is an exact small integer (the reference's std::pow(r, 2) gives it)
+    T correction = f[pidx(ic, jc, pit)] - (T)1 / (T)(r * r) * sum;
     for (int q = 0; q < r * r; q++) out[q] += correction;
 }
 
@@ -83,7 +84,7 @@ __global__ void k_ghost(const PatchT<T> *patches, const GhostOp *ops, int n, int
         T t = 0;
         for (int a = 0; a < r; a++)
             for (int b = 0; b < r; b++) t += f[pidx(op.si + a, op.sj + b, S.pitch)];
-        t /= (T)pow((double)r, 2.0);
+        t /= (T)(r * r);  // std::pow(r, 2.0) of the reference, an exact integer
         v = t;
     } else if (op.kind == kGhostInterp) {
         const PatchT<T> &S = patches[op.src];

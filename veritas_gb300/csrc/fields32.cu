@@ -2,7 +2,8 @@
 //
 //  * k32_moments — momentum moments (Rectangle::CalculateRhoAndJ, Rectangle.cpp:157-282)
 //    of FP32 (scaled) f: the per-cell weights are evaluated in FP32 in a cancellation-free
-//    form and every sum is accumulated in FP64.
+//    form; each lane keeps compensated (Kahan) FP32 sums and the lanes are combined in
+//    FP64.
 //  * k_poisson_fast — the Poisson solve (EMFieldSolver::UpdatePotential,
 //    EMSolver.cpp:156-192) in FP64 by an O(n) scan algorithm instead of the dense LU.
 //
@@ -64,7 +65,8 @@ __global__ void k32_moments(MomLaunch M) {
     const float c3 = 1.0f / 48.0f;
     const float *f = P.f1;
     const unsigned full = 0xffffffffu;
-    double ch = 0.0, cu = 0.0;
+    // per-lane compensated FP32 sums (Kahan); FP64 only for the final warp reduction
+    float chs = 0.0f, chc = 0.0f, cus = 0.0f, cuc = 0.0f;
     for (int j0 = 0; j0 < P.np; j0 += kMom32Out) {
         const int j = j0 - 1 + lane;
         const float p = fmaf(dpn, (float)(j + P.p_pos), pmin);
@@ -79,10 +81,17 @@ __global__ void k32_moments(MomLaunch M) {
         const float Vm = __shfl_up_sync(full, V, 1), Vp = __shfl_down_sync(full, V, 1);
         const bool use = lane >= 1 && lane <= kMom32Out && j < P.np && !(P.nested && P.nested[pidx(i, j, P.pitch)]);
         if (use) {
-            ch += (double)V;
-            cu += (double)(V * l + c3 * (lp - lm) * (Vp - Vm));
+            float y = V - chc;
+            float t = chs + y;
+            chc = (t - chs) - y;
+            chs = t;
+            y = (V * l + c3 * (lp - lm) * (Vp - Vm)) - cuc;
+            t = cus + y;
+            cuc = (t - cus) - y;
+            cus = t;
         }
     }
+    double ch = (double)chs - (double)chc, cu = (double)cus - (double)cuc;
     for (int o = 16; o > 0; o >>= 1) {
         ch += __shfl_down_sync(full, ch, o);
         cu += __shfl_down_sync(full, cu, o);
@@ -113,58 +122,40 @@ void launch_moments32(const MomLaunch &M) {
 // G = (I - S)(I - rho S), c = w2 / rho.  Hence
 //   B^{-1} v = z - Y K (z_0, z_1, z_{m-1}),   z = (1/c) G^{-T} G^{-1} v,
 // with Y = (1/c) G^{-T} G^{-1} [e_0 e_1 e_{m-1}] and the 3x3 K precomputed on the host
-// (Woodbury).  G^{-1} and G^{-T} are two prefix sums and two first-order recurrences,
-// each done as a block scan of affine maps.
+// (Woodbury).  G^{-1} and G^{-T} are two prefix sums (block scans) and two decaying
+// first-order recurrences (segment-local with a short carry gather).
 constexpr int kPfThreads = 1024;
 
-// Exclusive block scan of affine maps y -> a y + b (composition in thread order).
-__device__ void block_scan_affine(double &a, double &b, double *sa, double *sb) {
+// Exclusive block scan of sums (prefix sums of one value per thread).
+__device__ double block_exclusive_sum(double v, double *sb) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const unsigned full = 0xffffffffu;
-    // inclusive warp scan
+    double x = v;
     for (int o = 1; o < 32; o <<= 1) {
-        double pa = __shfl_up_sync(full, a, o), pb = __shfl_up_sync(full, b, o);
-        if (lane >= o) {
-            b = a * pb + b;
-            a = a * pa;
-        }
+        double p = __shfl_up_sync(full, x, o);
+        if (lane >= o) x += p;
     }
-    if (lane == 31) {
-        sa[wid] = a;
-        sb[wid] = b;
-    }
+    if (lane == 31) sb[wid] = x;
     __syncthreads();
     if (wid == 0) {
-        double wa = (lane < (int)(blockDim.x >> 5)) ? sa[lane] : 1.0;
-        double wb = (lane < (int)(blockDim.x >> 5)) ? sb[lane] : 0.0;
+        double w = (lane < (int)(blockDim.x >> 5)) ? sb[lane] : 0.0;
         for (int o = 1; o < 32; o <<= 1) {
-            double pa = __shfl_up_sync(full, wa, o), pb = __shfl_up_sync(full, wb, o);
-            if (lane >= o) {
-                wb = wa * pb + wb;
-                wa = wa * pa;
-            }
+            double p = __shfl_up_sync(full, w, o);
+            if (lane >= o) w += p;
         }
-        sa[lane] = wa;
-        sb[lane] = wb;
+        sb[lane] = w;
     }
     __syncthreads();
-    // exclusive: previous thread's inclusive map composed with the previous warps' map
-    double pa = __shfl_up_sync(full, a, 1), pb = __shfl_up_sync(full, b, 1);
-    if (lane == 0) {
-        pa = 1.0;
-        pb = 0.0;
-    }
-    if (wid > 0) {
-        const double wa = sa[wid - 1], wb = sb[wid - 1];
-        pb = pa * wb + pb;
-        pa = pa * wa;
-    }
-    a = pa;
-    b = pb;
+    double ex = x - v;
+    if (wid > 0) ex += sb[wid - 1];
     __syncthreads();
+    return ex;
 }
 
 // y_k = v_k + mult * y_{k-1} over v[0..m) in scan order (reversed when REV), in place.
+// mult = 1: prefix sums.  mult = rho (< 0.072): the carry into a segment is
+// sum_q rho^{(q-1)L} y_end(segment - q), and rho^{qL} drops below 1e-20 after a few
+// segments (three for L >= 8), so a short gather replaces the scan.
 template <bool REV>
 __device__ void recurrence_pass(double *v, int m, double mult, const double *powtab, double *sa, double *sb) {
     const int T = blockDim.x;
@@ -176,11 +167,22 @@ __device__ void recurrence_pass(double *v, int m, double mult, const double *pow
         y = v[idx] + mult * y;
         v[idx] = y;
     }
-    const int len = max(0, k1 - k0);
-    double a = len > 0 ? powtab[len - 1] : 1.0;  // mult^len
-    double b = y;
-    block_scan_affine(a, b, sa, sb);
-    const double carry = b;  // y just before this thread's segment
+    double carry;
+    if (mult == 1.0) {
+        carry = block_exclusive_sum(y, sb);
+    } else {
+        sa[threadIdx.x] = y;  // segment end without carry (sa holds blockDim doubles)
+        __syncthreads();
+        const int t = threadIdx.x;
+        const double aL = powtab[L - 1];  // mult^L
+        carry = 0.0;
+        double wgt = 1.0;
+        for (int q = 1; q <= t && wgt > 1e-20; q++) {
+            carry += wgt * sa[t - q];
+            wgt *= aL;
+        }
+        __syncthreads();
+    }
     for (int k = k0; k < k1; k++) {
         const int idx = REV ? m - 1 - k : k;
         v[idx] += powtab[k - k0] * carry;  // mult^(k-k0+1)
@@ -202,7 +204,7 @@ __device__ __forceinline__ double efield_fast(const double *phi, int n, double f
 }
 
 __global__ void __launch_bounds__(kPfThreads) k_poisson_fast(PoissonFastLaunch L) {
-    __shared__ double sa[32], sb[32];
+    __shared__ double sa[kPfThreads], sb[32];
     __shared__ double pw_one[kPfMaxSeg], pw_rho[kPfMaxSeg];
     __shared__ double tvec[3];
     const int run = blockIdx.x;

@@ -7,6 +7,7 @@
 // Compiled with --fmad=false so each double expression keeps the reference's operations
 // and evaluation order.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include "vx_kernels.hpp"
 
 namespace vx {
@@ -724,15 +725,17 @@ void launch_maxwell(const MaxwellLaunch &L) {
 }
 
 // ---------------------------------------------------------------- CFL
+// The maximum runs over non-negative doubles, so it is taken on their bit patterns:
+// each block reduces its slice and folds it into out[run] with an integer atomicMax.
 __global__ void k_cfl(CflLaunch L) {
-    const int run = blockIdx.x;
+    const int run = blockIdx.y;
     const RunFields &F = L.fields[run];
     const int ns = L.run_ns[run];
     const double *sp = L.spec + run * 25;  // up to 8 species x 3 + dpsMax
     const double dpsMax = sp[24];
     __shared__ double red[256];
     double pc = 0.0;
-    for (int i = threadIdx.x; i < F.n; i += blockDim.x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < F.n; i += gridDim.x * blockDim.x) {
         double Azv = F.Az[i], Ayv = F.Ay[i];
         double As = Ayv * Ayv + Azv * Azv;
         double temp = 0.0;
@@ -753,11 +756,14 @@ __global__ void k_cfl(CflLaunch L) {
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) L.out[run] = red[0];
+    if (threadIdx.x == 0)
+        atomicMax((unsigned long long *)&L.out[run], (unsigned long long)__double_as_longlong(red[0]));
 }
 
 void launch_cfl(const CflLaunch &L) {
-    k_cfl<<<L.nruns, 256, 0, L.stream>>>(L);
+    cudaMemsetAsync(L.out, 0, (size_t)L.nruns * sizeof(double), L.stream);
+    dim3 g(std::min(32, std::max(1, (L.maxn + 255) / 256)), L.nruns);
+    k_cfl<<<g, 256, 0, L.stream>>>(L);
 }
 
 __global__ void k_negate(double *dst, const double *src, int n) {
