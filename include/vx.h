@@ -171,6 +171,22 @@ int vx_run_state_to_host(vx_run *run, double *state_out);
  * device, run one RK step with dt, copy the new state to state_out. */
 int vx_run_step_host(vx_run *run, const double *state_in, double *state_out, double dt);
 
+/* ---------------------------------------------------------------- no-allocation CFL bound
+ * No counterpart in the reference.  For callers that must not allocate device memory
+ * (a time-step controller beside solves whose memory is committed up front, or one that
+ * must not cause the synchronisation cudaMalloc / cudaFree may imply): the bound of
+ * vx_run_calculate_dt (EMFieldSolver::EstimateCFLBound) from device field arrays the
+ * caller owns — Ay, Az, By, Bz (their first n entries, slot 0) and E_x (n) — with the
+ * species' charge q, mass m and finest-level dp0 given on the host.  Its scratch is a
+ * fixed device array of VX_CFL_NOALLOC_MAX_CELLS / 256 doubles, looked up on the first
+ * call on each device (make that first call before any stream capture); larger n is
+ * rejected with VX_ERR_INVALID.  Calls that overlap on the GPU share the scratch and race.
+ * `stream` is a cudaStream_t (NULL: the default stream); the call waits for its result. */
+#define VX_CFL_NOALLOC_MAX_CELLS (1 << 20)
+int vx_cfl_bound_noalloc(const double *Ay, const double *Az, const double *By, const double *Bz, const double *Ex,
+                         int n, const double *q, const double *m, const double *dp0, int nspecies, double dx0,
+                         double cfl, void *stream, double *dt);
+
 /* ---------------------------------------------------------------- serving loop
  * No reference counterpart (the reference runs one solve per process): continuous
  * batching of independent solves on one context under a device-memory budget.

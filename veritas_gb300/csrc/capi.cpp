@@ -83,6 +83,12 @@ std::unique_ptr<vx::Settings> host_settings(const vx_problem &p) {
 }
 }  // namespace
 
+namespace vx {
+// Error message for entry points defined outside this file.
+void set_last_error(const std::string &msg) { g_err = msg; }
+}  // namespace vx
+
+
 extern "C" {
 
 void vx_problem_defaults(vx_problem *p) {
