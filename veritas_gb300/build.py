@@ -39,8 +39,9 @@ def sources() -> list[Path]:
 
 def build(force: bool = False, verbose: bool = False) -> Path:
     srcs = sources()
-    deps = srcs + list(CSRC.glob("*.hpp")) + [HERE.parent / "include" / "vx.h", Path(__file__)]
-    if LIB.exists() and not force:
+    deps = srcs + list(CSRC.glob("*.hpp")) + [HERE.parent / "include" / "vx.h", HERE.parent / "include" / "veritas_gb300.hpp",
+                                              HERE / "driver" / "veritas_gb300_run.cpp", Path(__file__)]
+    if LIB.exists() and (HERE / "veritas_gb300_run").exists() and not force:
         t = LIB.stat().st_mtime
         if all(p.stat().st_mtime <= t for p in deps):
             return LIB
@@ -67,6 +68,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for _, o in jobs], "-lcudart", "-lpthread",
           "-Xlinker", "--no-undefined"])
     os.replace(tmp, LIB)
+    # the stand-alone C++ driver over include/veritas_gb300.hpp, found next to the library
+    drv = HERE / "veritas_gb300_run"
+    _run(["g++", "-O2", "-std=c++17", "-I", str(HERE.parent / "include"), str(HERE / "driver" / "veritas_gb300_run.cpp"),
+          "-L", str(HERE), "-lvx_cuda", "-Wl,-rpath,$ORIGIN", "-o", str(drv)])
     if verbose:
         print(f"built {LIB}")
     return LIB

@@ -421,12 +421,18 @@ LaunchSet::~LaunchSet() {
 Engine::Engine(int dev) : device(dev) {
     VX_CUDA(cudaSetDevice(dev));
     VX_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    VX_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    VX_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    VX_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
 }
 
 Engine::~Engine() {
     sets_.clear();
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -806,17 +812,31 @@ void Engine::record_step(LaunchSet &L) {
     for (int s = 0; s < 6; s++) {
         run_moments(L, ml);
         launch_assemble(al);
+        launches += 2;
+        // the Poisson solve (and E_x) runs beside the x-direction face work, which does
+        // not read E_x; the p-direction faces wait for both
+        VX_CUDA(cudaEventRecord(ev_fork, stream));
+        VX_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+        pl.stream = side;
         run_poisson(L, pl);
+        launches += 1;
         if (L.precision == kF32) {
-            launch_fields_to_f32(L.dfields.as<RunFields>(), (int)L.runs.size(), L.maxn, stream);
-            launches++;
+            launch_fields_to_f32(L.dfields.as<RunFields>(), (int)L.runs.size(), L.maxn, 2, side);
+            launch_fields_to_f32(L.dfields.as<RunFields>(), (int)L.runs.size(), L.maxn, 1, stream);
+            launches += 2;
         }
-        launches += 4;
         fl.step = s;
         fct_sub(L, fl, kSubGamma);
+        fl.part = 1;
         fct_sub(L, fl, kSubFaces);
         fct_sub(L, fl, kSubFlux);
-        launches += 3;
+        VX_CUDA(cudaEventRecord(ev_join, side));
+        VX_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
+        fl.part = 2;
+        fct_sub(L, fl, kSubFaces);
+        fct_sub(L, fl, kSubFlux);
+        fl.part = 0;
+        launches += 6;
         for (size_t b = 0; b + 1 < L.iface_ptr.size(); b++, launches++)
             launch_iface(L.dpatch.p, L.diface.as<IfaceOp>() + L.iface_ptr[b], L.iface_ptr[b + 1] - L.iface_ptr[b], s, L.precision, stream);
         fct_sub(L, fl, kSubDsF2);

@@ -200,6 +200,8 @@ public:
     ~Engine();
     int device;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;       // Poisson solve beside the E-independent x-direction work
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::vector<Run *> runs;
     bool use_graphs = true;
     uint64_t kernel_launches = 0;  // launches issued by this engine (graph replays count their nodes)

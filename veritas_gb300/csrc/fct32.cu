@@ -86,19 +86,19 @@ __global__ void k32_gamma(const P32 *patches, const TileRef *tiles, const RunFie
     P.gam[id] = sqrtf(1.0f + p * p + a);
 }
 
-__global__ void k32_faces(const P32 *patches, const TileRef *tiles, const RunFields *fields, int use_f0) {
+__global__ void k32_faces(const P32 *patches, const TileRef *tiles, const RunFields *fields, int use_f0, int part) {
     VX_TILE32
     const float *f = use_f0 ? P.f0 : P.f1;
     const float *g = P.gam;
     const float mm = P.weno_eps;
-    if (i >= 0 && i <= P.nx && j >= -1 && j <= P.np) {
+    if ((part & 1) && i >= 0 && i <= P.nx && j >= -1 && j <= P.np) {
         const float p0 = mom32(P, j), p1 = mom32(P, j + 1);
         const float dg = P.dpnf * (p1 + p0) / (g[pidx(i, j + 1, pit)] + g[id]);
         const float am = P.kxf * dg;
         P.ex[id] = am;
         P.fx[id] = weno32(f[pidx(i - 2, j, pit)], f[pidx(i - 1, j, pit)], f[id], f[pidx(i + 1, j, pit)], am > 0.0f, mm);
     }
-    if (i >= -1 && i <= P.nx && j >= 0 && j <= P.np) {
+    if ((part & 2) && i >= -1 && i <= P.nx && j >= 0 && j <= P.np) {
         const RunFields &F = fields[P.run];
         const float Em = qefield32(P, F, i);
         const float a0 = asq32(P, F, i), a1 = asq32(P, F, i + 1);
@@ -109,18 +109,18 @@ __global__ void k32_faces(const P32 *patches, const TileRef *tiles, const RunFie
     }
 }
 
-__global__ void k32_flux(const P32 *patches, const TileRef *tiles, int step, int use_f0) {
+__global__ void k32_flux(const P32 *patches, const TileRef *tiles, int step, int use_f0, int part) {
     VX_TILE32
     const float *f = use_f0 ? P.f0 : P.f1;
     const float w3 = 1.0f / 48.0f;
     const float dxi = P.dxif, dpi = P.dpif;
-    if (i >= 0 && i <= P.nx && j >= -1 && j <= P.np && !(P.ifx && P.ifx[id])) {
+    if ((part & 1) && i >= 0 && i <= P.nx && j >= -1 && j <= P.np && !(P.ifx && P.ifx[id])) {
         float am = P.ex[id], ap1 = P.ex[id + 1], am1 = P.ex[id - 1];
         float fm = P.fx[id], fp1 = P.fx[id + 1], fm1 = P.fx[id - 1];
         P.FxH[step][id] = dxi * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
         if (step == 0) P.FxL[id] = dxi * ((am > 0.0f ? f[id - pit] : f[id]) * am);
     }
-    if (i >= -1 && i <= P.nx && j >= 0 && j <= P.np && !(P.ifp && P.ifp[id])) {
+    if ((part & 2) && i >= -1 && i <= P.nx && j >= 0 && j <= P.np && !(P.ifp && P.ifp[id])) {
         float am = P.ep[id], ap1 = P.ep[id + pit], am1 = P.ep[id - pit];
         float fm = P.fp[id], fp1 = P.fp[id + pit], fm1 = P.fp[id - pit];
         P.FpH[step][id] = dpi * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
@@ -215,10 +215,10 @@ void launch_fct32_substep(const FctLaunch &L, int sub) {
             k32_gamma<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.fields);
             break;
         case kSubFaces:
-            k32_faces<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.fields, L.use_f0);
+            k32_faces<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.fields, L.use_f0, L.part ? L.part : 3);
             break;
         case kSubFlux:
-            k32_flux<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.step, L.use_f0);
+            k32_flux<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.step, L.use_f0, L.part ? L.part : 3);
             break;
         case kSubDsF2:
             k32_ds_f2<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.params32, L.step);

@@ -90,16 +90,16 @@ __global__ void k64_gamma(const P64 *patches, const TileRef *tiles, const RunFie
 }
 
 // Face velocities and reconstructed face values (Rectangle.cpp:1278-1312).
-__global__ void k64_faces(const P64 *patches, const TileRef *tiles, const RunFields *fields, int use_f0) {
+__global__ void k64_faces(const P64 *patches, const TileRef *tiles, const RunFields *fields, int use_f0, int part) {
     VX_TILE_PROLOGUE
     const double *f = use_f0 ? P.f0 : P.f1;
     const double *g = P.gam;
-    if (i >= 0 && i <= P.nx && j >= -1 && j <= P.np) {
+    if ((part & 1) && i >= 0 && i <= P.nx && j >= -1 && j <= P.np) {
         double am = P.dp_inv * P.cc * (g[pidx(i, j + 1, pit)] - g[id]);
         P.ex[id] = am;
         P.fx[id] = weno_face(f[pidx(i - 2, j, pit)], f[pidx(i - 1, j, pit)], f[id], f[pidx(i + 1, j, pit)], am > 0.0);
     }
-    if (i >= -1 && i <= P.nx && j >= 0 && j <= P.np) {
+    if ((part & 2) && i >= -1 && i <= P.nx && j >= 0 && j <= P.np) {
         const RunFields &F = fields[P.run];
         double Em = P.q * patch_efield(P, F, i);
         double am = Em - P.cc * P.dx_inv * (g[pidx(i + 1, j, pit)] - g[id]);
@@ -111,17 +111,17 @@ __global__ void k64_faces(const P64 *patches, const TileRef *tiles, const RunFie
 // High-order fluxes for stage `step` and, on stage 0, the donor-cell low-order fluxes
 // (Rectangle.cpp:1313-1394).  Coarse faces on a coarse/fine interface are skipped here
 // and written by the interface kernel.
-__global__ void k64_flux(const P64 *patches, const TileRef *tiles, int step, int use_f0) {
+__global__ void k64_flux(const P64 *patches, const TileRef *tiles, int step, int use_f0, int part) {
     VX_TILE_PROLOGUE
     const double *f = use_f0 ? P.f0 : P.f1;
     const double w3 = 1 / 48.0;
-    if (i >= 0 && i <= P.nx && j >= -1 && j <= P.np && !(P.ifx && P.ifx[id])) {
+    if ((part & 1) && i >= 0 && i <= P.nx && j >= -1 && j <= P.np && !(P.ifx && P.ifx[id])) {
         double am = P.ex[id], ap1 = P.ex[id + 1], am1 = P.ex[id - 1];
         double fm = P.fx[id], fp1 = P.fx[id + 1], fm1 = P.fx[id - 1];
         P.FxH[step][id] = P.dx_inv * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
         if (step == 0) P.FxL[id] = P.dx_inv * ((am > 0.0 ? f[id - pit] : f[id]) * am);
     }
-    if (i >= -1 && i <= P.nx && j >= 0 && j <= P.np && !(P.ifp && P.ifp[id])) {
+    if ((part & 2) && i >= -1 && i <= P.nx && j >= 0 && j <= P.np && !(P.ifp && P.ifp[id])) {
         double am = P.ep[id], ap1 = P.ep[id + pit], am1 = P.ep[id - pit];
         double fm = P.fp[id], fp1 = P.fp[id + pit], fm1 = P.fp[id - pit];
         P.FpH[step][id] = P.dp_inv * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
@@ -233,10 +233,10 @@ void launch_fct64_substep(const FctLaunch &L, int sub) {
             k64_gamma<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.fields);
             break;
         case kSubFaces:
-            k64_faces<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.fields, L.use_f0);
+            k64_faces<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.fields, L.use_f0, L.part ? L.part : 3);
             break;
         case kSubFlux:
-            k64_flux<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.step, L.use_f0);
+            k64_flux<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.step, L.use_f0, L.part ? L.part : 3);
             break;
         case kSubDsF2:
             k64_ds_f2<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.params, L.step);

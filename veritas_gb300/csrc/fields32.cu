@@ -252,19 +252,19 @@ __global__ void __launch_bounds__(kPfThreads) k_poisson_fast(PoissonFastLaunch L
     for (int i = threadIdx.x; i < n; i += blockDim.x) F.efin[i] = efield_fast(phi, n, L.fcoef[run], ex0, i);
 }
 
-__global__ void k_fields_to_f32(RunFields *fields, int nruns) {
+__global__ void k_fields_to_f32(RunFields *fields, int nruns, int which) {
     const int run = blockIdx.y;
     if (run >= nruns) return;
     RunFields &F = fields[run];
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x <= F.n) F.asq32[x] = (float)F.asq[x];
-    if (x < F.n) F.efin32[x] = (float)F.efin[x];
+    if ((which & 1) && x <= F.n) F.asq32[x] = (float)F.asq[x];
+    if ((which & 2) && x < F.n) F.efin32[x] = (float)F.efin[x];
 }
 
-void launch_fields_to_f32(RunFields *fields, int nruns, int maxn, cudaStream_t s) {
+void launch_fields_to_f32(RunFields *fields, int nruns, int maxn, int which, cudaStream_t s) {
     if (nruns == 0) return;
     dim3 g((maxn + 1 + 255) / 256, nruns);
-    k_fields_to_f32<<<g, 256, 0, s>>>(fields, nruns);
+    k_fields_to_f32<<<g, 256, 0, s>>>(fields, nruns, which);
 }
 
 void launch_poisson_fast(const PoissonFastLaunch &L) {

@@ -38,6 +38,7 @@ struct FctLaunch {
     const float *params32;    // the same blocks in FP32 (FP32 form)
     int step;
     int use_f0;
+    int part;  // faces / flux: 1 x faces only, 2 p faces only, 0 both
     cudaStream_t stream;
 };
 
@@ -124,8 +125,9 @@ struct PoissonFastLaunch {
     cudaStream_t stream;
 };
 void launch_poisson_fast(const PoissonFastLaunch &L);
-// FP32 copies of a^2 and E_x of every run of a set (the FP32 form reads these).
-void launch_fields_to_f32(RunFields *fields, int nruns, int maxn, cudaStream_t s);
+// FP32 copies of a^2 (which & 1) and E_x (which & 2) of every run of a set (the FP32 form
+// reads these).
+void launch_fields_to_f32(RunFields *fields, int nruns, int maxn, int which, cudaStream_t s);
 void launch_efield(RunFields *fields, const double *fcoef, int nruns, int maxn, cudaStream_t s);
 
 // Maxwell RK stage + face interpolation of A (EMSolver::RGKStep).
