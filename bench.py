@@ -60,6 +60,79 @@ def problem_config1():
                    a0=1.0, fwhm=10.0, delay=10.0, cfl=0.5, quadDepth=2, precision=64)
 
 
+def problem_config3():
+    """Larger wakefield case: base 16384 x 1024, three levels, 0.005 n_c, a0 = 2, 0.5 keV."""
+    p = problem_config1()
+    p.nx, p.np, p.Lfinest, p.r = 16384, 1024, 3, 2
+    p.dens, p.a0, p.Te = 0.005, 2.0, 0.5
+    p.crit, p.sizeWeight = 1e-6, 1.0
+    return p
+
+
+def run_config3(args) -> None:
+    """The precision form on the larger case: FP32 throughput, and the error of f, E_x,
+    E_y and the field energy against the FP64 path over the same steps from the same
+    initial hierarchy.  One JSON line."""
+    import dataclasses
+
+    import numpy as np
+
+    from veritas_gb300 import Context, SolverManager
+
+    sys.path.insert(0, str(ROOT / "tests"))
+    import vxstate
+
+    ctx = Context(0)
+    t0 = time.perf_counter()
+    s32 = SolverManager(ctx, dataclasses.replace(problem_config3(), precision=32))
+    init32 = time.perf_counter() - t0
+    cells = s32.cell_count()
+    layout = s32.layout()
+    with tempfile.TemporaryDirectory() as td:
+        t0 = time.perf_counter()
+        s64 = SolverManager(ctx, problem_config3())
+        init64 = time.perf_counter() - t0
+        s64.save_state(Path(td) / "init.bin")
+        s32.load_state(Path(td) / "init.bin")  # the same initial f (FP64 values, rounded)
+        p = problem_config3()
+        e0 = p.a0 * 9.10938291e-31 * 299792458.0 * (2 * np.pi * 299792458.0 / p.lambda_) / 1.60217657e-19
+        ew = ee = ey = 0.0
+        t64 = t32 = 0.0
+        for _ in range(args.steps):
+            dt = s64.CalculateDt()
+            ctx.timer_begin()
+            s64.Advance(dt)
+            t64 += ctx.timer_end()
+            ctx.timer_begin()
+            s32.Advance(dt)
+            t32 += ctx.timer_end()
+            wa, wb = field_energy(s64), field_energy(s32)
+            ew = max(ew, abs(wb - wa) / max(abs(wa), 1e-300))
+            ee = max(ee, float(np.max(np.abs(s32.field("Ex") - s64.field("Ex")))) / e0)
+            ey = max(ey, float(np.max(np.abs(s32.field("Ey") - s64.field("Ey")))) / e0)
+        s64.save_state(Path(td) / "a.bin")
+        s32.save_state(Path(td) / "b.bin")
+        sa, sb = vxstate.read_state(Path(td) / "a.bin"), vxstate.read_state(Path(td) / "b.bin")
+    num = den = 0.0
+    for la, lb in zip(sa["species"][0], sb["species"][0]):
+        for ra, rb in zip(la, lb):
+            fa, fb = ra["f"][2:-2, 2:-2, 0], rb["f"][2:-2, 2:-2, 0]
+            num = max(num, float(np.max(np.abs(fb - fa))))
+            den = max(den, float(np.max(np.abs(fa))))
+    line = {"form": "precision", "workload": "laser_wakefield_amr_Nx16384_Np1024_3level_r2",
+            "cells_per_step": cells, "patches": len(layout), "steps": args.steps,
+            "fp32": {"value": cells * args.steps / (t32 * 1e-3), "unit": UNIT, "ms_per_step": t32 / args.steps},
+            "fp64": {"value": cells * args.steps / (t64 * 1e-3), "unit": UNIT, "ms_per_step": t64 / args.steps},
+            "init_s": {"fp32": init32, "fp64": init64},
+            "error_vs_fp64": {"from": "the FP64 run's initial hierarchy (t = 0), same dt sequence",
+                              "f_rel_linf": num / den, "field_energy_rel_max": ew,
+                              "Ex_abs_max_over_laser_E0": ee, "Ey_abs_max_over_laser_E0": ey}}
+    print(json.dumps(line))
+    s32.close()
+    s64.close()
+    ctx.close()
+
+
 def problem_config2():
     """Two-level AMR laser / slab case: base 4096 x 512, refinement ratio 2."""
     p = problem_config1()
@@ -331,6 +404,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32],
                     help="precision of the headline workload (64, the plain path, unless profiling the FP32 form)")
+    ap.add_argument("--form", default="", choices=["", "config3"],
+                    help="config3: the precision form on the larger three-level case (its own JSON line)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the FP32 / batched / served forms (FP64 headline line only)")
     ap.add_argument("--lite", action="store_true",
@@ -338,6 +413,9 @@ def main() -> None:
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.form == "config3":
+        run_config3(args)
         return
     world, rank, local = dist_info()
     dist = None
