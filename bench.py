@@ -279,6 +279,9 @@ def measure_fp32_form(ctx, init_path: Path, steps: int, warmup: int) -> dict:
     p32 = dataclasses.replace(problem_config2(), precision=32)
     s = SolverManager(ctx, p32)
     cells = s.cell_count()
+    from veritas_gb300 import autotune_many
+
+    tile = autotune_many([s])
     for _ in range(warmup):
         s.Advance(s.CalculateDt())
     ctx.sync()
@@ -322,6 +325,7 @@ def measure_fp32_form(ctx, init_path: Path, steps: int, warmup: int) -> dict:
     a.close()
     b.close()
     return {"value": cells / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "dtype": "f32 (moments, fields, Poisson f64)",
+            "tile_p_x": list(tile),
             "error_vs_fp64": {"steps": steps, "from": "the FP64 run's initial hierarchy (t = 0), same dt sequence",
                               "f_rel_linf": num / den, "field_energy_rel_max": ew,
                               "Ex_abs_max_over_laser_E0": ee, "Ey_abs_max_over_laser_E0": ey},
@@ -338,6 +342,9 @@ def measure_batched(ctx, count: int, steps: int, warmup: int, precision: int) ->
     runs = [SolverManager(ctx, p) for p in ensemble_problems(count, precision=precision)]
     init_s = time.perf_counter() - t0
     cells = sum(r.cell_count() for r in runs)
+    from veritas_gb300 import autotune_many
+
+    tile = autotune_many(runs)
     for _ in range(warmup):
         advance_many(runs, calculate_dt_many(runs))
     ctx.sync()
@@ -350,7 +357,7 @@ def measure_batched(ctx, count: int, steps: int, warmup: int, precision: int) ->
         r.close()
     ms = sum(times) / len(times)
     return {"value": cells / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "runs": count, "cells_per_step": cells,
-            "init_s": init_s, "precision": precision,
+            "init_s": init_s, "precision": precision, "tile_p_x": list(tile),
             "sampler": "splitmix64 seed 0x5EED0004, stream r = run r (veritas_gb300/ensemble.py)"}
 
 

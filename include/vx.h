@@ -115,6 +115,11 @@ int vx_update_hierarchy(const vx_problem *prob, int species, const int32_t *patc
 /* Advance several runs of one context together, one launch per sub-step for all of
  * them (batched form).  dt[i] belongs to runs[i]. */
 int vx_runs_advance(vx_run *const *runs, const double *dt, int nruns);
+/* No reference counterpart.  Tile-shape autotuner: times the FCT sub-step kernels of the
+ * runs' launch set for each candidate tile (p x x cells = one thread block) and keeps the
+ * fastest for the set and for later sets of that precision.  Call between steps; the
+ * solution is unchanged.  The chosen shape is returned in *tile_j, *tile_i. */
+int vx_runs_autotune(vx_run *const *runs, int nruns, int *tile_j, int *tile_i);
 /* CalculateDt of several runs of one context in one launch; dt[i] belongs to runs[i]. */
 int vx_runs_calculate_dt(vx_run *const *runs, double *dt, int nruns);
 

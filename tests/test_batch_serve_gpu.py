@@ -96,3 +96,23 @@ def test_server_admits_by_memory_budget(ctx):
     assert ra["finished"] and rb["finished"]
     assert rb["admitted"] >= ra["finish"]
     srv.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [64, 32])
+def test_autotuned_tiles_change_nothing(ctx, tmp_path, precision):
+    """The tile shape the autotuner picks changes no arithmetic: results are identical to
+    the default 32 x 8 tiles."""
+    from veritas_gb300 import SolverManager, advance_many, autotune_many
+
+    P = dataclasses.replace(problem_for("beam3"), precision=precision)
+    a, b = SolverManager(ctx, P), SolverManager(ctx, P)
+    for _ in range(2):
+        a.Advance(a.CalculateDt())
+    shape = autotune_many([b])
+    assert shape[0] * shape[1] <= 1024
+    for _ in range(2):
+        b.Advance(b.CalculateDt())
+    assert _bytes(a, tmp_path / "a.bin") == _bytes(b, tmp_path / "b.bin")
+    a.close()
+    b.close()

@@ -77,6 +77,7 @@ def _load() -> ctypes.CDLL:
         "vx_run_advance": (ctypes.c_int, [vp, ctypes.c_double]),
         "vx_runs_advance": (ctypes.c_int, [P(vp), P(ctypes.c_double), ctypes.c_int]),
         "vx_runs_calculate_dt": (ctypes.c_int, [P(vp), P(ctypes.c_double), ctypes.c_int]),
+        "vx_runs_autotune": (ctypes.c_int, [P(vp), ctypes.c_int, P(ctypes.c_int), P(ctypes.c_int)]),
         "vx_server_create": (ctypes.c_int, [vp, ctypes.c_uint64, ctypes.c_int, P(vp)]),
         "vx_server_destroy": (ctypes.c_int, [vp]),
         "vx_server_clock": (ctypes.c_int, [vp, P(ctypes.c_double)]),
@@ -435,3 +436,11 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def autotune_many(runs: list[SolverManager]) -> tuple[int, int]:
+    """Picks the FCT tile shape (p x x) for these runs' launch set; returns it."""
+    arr = (ctypes.c_void_p * len(runs))(*[r.handle for r in runs])
+    tj, ti = ctypes.c_int(), ctypes.c_int()
+    _check(_lib.vx_runs_autotune(arr, len(runs), ctypes.byref(tj), ctypes.byref(ti)))
+    return int(tj.value), int(ti.value)

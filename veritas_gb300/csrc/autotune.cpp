@@ -1,0 +1,66 @@
+// Tile-shape autotuner for the FCT sub-step kernels.
+//
+// Every FCT kernel walks a list of tiles, one thread block per tile of tile_j (p, the
+// coalesced axis) x tile_i (x) cells.  The best shape depends on the patch sizes of the
+// set (ragged edges, occupancy, register pressure of the precision's kernels), so the
+// engine measures it: for each candidate the tile list is rebuilt and the sub-steps that
+// leave the solution unchanged between steps (gamma, faces, fluxes, ds/f2, limiter R and
+// C — their outputs are recomputed before being read in the next step) are timed with CUDA
+// events on the engine's stream; the fastest shape is kept for the set and becomes the
+// default for new sets of the same precision.  The tile shape changes no arithmetic.
+#include "engine.hpp"
+
+namespace vx {
+
+std::pair<int, int> Engine::autotune(const std::vector<Run *> &set, int reps) {
+    static const int kShapes[][2] = {{32, 4}, {32, 8}, {32, 16}, {64, 4}, {64, 8}, {128, 2}, {128, 4}};
+    LaunchSet &L = get_set(set);
+    FctLaunch fl{};
+    fl.patches = L.dpatch.p;
+    fl.fields = L.dfields.as<RunFields>();
+    fl.params = L.dparams.as<double>();
+    fl.params32 = L.dparams32.as<float>();
+    fl.step = 0;
+    fl.stream = stream;
+    auto run_subs = [&]() {
+        for (int sub : {kSubGamma, kSubFaces, kSubFlux, kSubDsF2, kSubLimR, kSubLimC}) {
+            if (L.precision == kF32) launch_fct32_substep(fl, sub);
+            else launch_fct64_substep(fl, sub);
+        }
+    };
+    double best_ms = 1e300;
+    int best[2] = {L.tile_j, L.tile_i};
+    for (auto &sh : kShapes) {
+        L.tile_j = sh[0];
+        L.tile_i = sh[1];
+        build_tiles(L);
+        fl.tiles = L.dtiles.as<TileRef>();
+        fl.ntiles = L.ntiles;
+        fl.tile_j = L.tile_j;
+        fl.tile_i = L.tile_i;
+        run_subs();  // warm-up
+        if (cudaGetLastError() != cudaSuccess) continue;  // shape not launchable here
+        timer_begin();
+        for (int r = 0; r < reps; r++) run_subs();
+        const double ms = timer_end() / reps;
+        kernel_launches += 6 * (reps + 1);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best[0] = sh[0];
+            best[1] = sh[1];
+        }
+    }
+    L.tile_j = best[0];
+    L.tile_i = best[1];
+    build_tiles(L);
+    if (L.graph) {  // the captured step holds the old tile list
+        cudaGraphExecDestroy(L.graph);
+        L.graph = nullptr;
+    }
+    tile_pref[L.precision == kF32][0] = best[0];
+    tile_pref[L.precision == kF32][1] = best[1];
+    sync();
+    return {best[0], best[1]};
+}
+
+}  // namespace vx

@@ -299,6 +299,21 @@ int vx_runs_calculate_dt(vx_run *const *runs, double *dt, int nruns) {
     });
 }
 
+int vx_runs_autotune(vx_run *const *runs, int nruns, int *tile_j, int *tile_i) {
+    if (!runs || nruns <= 0) return VX_ERR_INVALID;
+    return guard([&] {
+        std::vector<vx::Run *> set;
+        vx_ctx *c = runs[0]->ctx;
+        for (int i = 0; i < nruns; i++) {
+            if (!runs[i] || runs[i]->ctx != c) throw std::invalid_argument("runs must belong to one context");
+            set.push_back(runs[i]->run.get());
+        }
+        auto best = c->eng->autotune(set, 5);
+        if (tile_j) *tile_j = best.first;
+        if (tile_i) *tile_i = best.second;
+    });
+}
+
 int vx_runs_advance(vx_run *const *runs, const double *dt, int nruns) {
     if (!runs || !dt || nruns <= 0) return VX_ERR_INVALID;
     return guard([&] {

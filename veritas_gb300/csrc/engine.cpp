@@ -503,6 +503,8 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     fl.patches = L.dpatch.p;
     fl.tiles = L.dtiles.as<TileRef>();
     fl.ntiles = L.ntiles;
+    fl.tile_j = L.tile_j;
+    fl.tile_i = L.tile_i;
     fl.fields = L.dfields.as<RunFields>();
     fl.params = L.dparams.as<double>();
     fl.params32 = L.dparams32.as<float>();
@@ -600,15 +602,32 @@ LaunchSet &Engine::get_set(const std::vector<Run *> &set) {
     return ref;
 }
 
+// Tile list covering every patch's padded block with tile_j (p) x tile_i (x) tiles.
+void Engine::build_tiles(LaunchSet &L) {
+    std::vector<TileRef> tiles;
+    int pi = 0;
+    for (Run *R : L.runs)
+        for (auto &sp : R->rects)
+            for (auto &lvl : sp)
+                for (auto &rp : lvl) {
+                    for (int i0 = -2; i0 <= rp->n_x + 1; i0 += L.tile_i)
+                        for (int j0 = -2; j0 <= rp->n_p + 1; j0 += L.tile_j) tiles.push_back({pi, i0, j0});
+                    pi++;
+                }
+    L.ntiles = (int)tiles.size();
+    L.dtiles = upload(tiles, stream);
+}
+
 void Engine::build_set(LaunchSet &L) {
     L.precision = L.runs.empty() ? kF64 : L.runs[0]->precision;
+    L.tile_j = tile_pref[L.precision == kF32][0];
+    L.tile_i = tile_pref[L.precision == kF32][1];
     for (Run *R : L.runs)
         if (R->precision != L.precision)
             throw std::invalid_argument("runs advanced together must share one precision");
     std::vector<PoissonFastDev> pfs;
     for (Run *R : L.runs) pfs.push_back(R->pfdev);
     L.dpf = upload(pfs, stream);
-    std::vector<TileRef> tiles;
     std::vector<int> colpatch, colidx, lvl_ptr, lvl_off, lvl_patch, run_n, run_ns, run_nl;
     std::vector<RunFields> fields;
     std::vector<LUDev> lus;
@@ -632,8 +651,6 @@ void Engine::build_set(LaunchSet &L) {
                     int pi = (int)L.hpatch.size();
                     L.hpatch.push_back(r.desc);
                     lvl_patch.push_back(pi);
-                    for (int i0 = -2; i0 <= r.n_x + 1; i0 += 8)
-                        for (int j0 = -2; j0 <= r.n_p + 1; j0 += 32) tiles.push_back({pi, i0, j0});
                     int rtb = r.desc.rtb;
                     for (int c = 0; c < r.n_x * rtb; c++) {
                         colpatch.push_back(pi);
@@ -729,11 +746,10 @@ void Engine::build_set(LaunchSet &L) {
         L.diface = upload(fo, stream);
         L.dcsync = upload(c, stream);
     }
-    L.ntiles = (int)tiles.size();
     L.ncols = (int)colpatch.size();
     // lvl_ptr is absolute; lvl_off points at each run's block.
     L.dpatch = upload(L.hpatch, stream);
-    L.dtiles = upload(tiles, stream);
+    build_tiles(L);
     L.dfields = upload(fields, stream);
     L.dcolpatch = upload(colpatch, stream);
     L.dcolidx = upload(colidx, stream);
@@ -769,6 +785,8 @@ void Engine::record_step(LaunchSet &L) {
     fl.patches = L.dpatch.p;
     fl.tiles = L.dtiles.as<TileRef>();
     fl.ntiles = L.ntiles;
+    fl.tile_j = L.tile_j;
+    fl.tile_i = L.tile_i;
     fl.fields = L.dfields.as<RunFields>();
     fl.params = L.dparams.as<double>();
     fl.params32 = L.dparams32.as<float>();

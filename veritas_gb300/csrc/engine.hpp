@@ -188,6 +188,7 @@ struct LaunchSet {
     // AMR op tables of all runs, batch by batch (global patch ids)
     DevBuf dghost, diface, dcsync;
     int precision = kF64;
+    int tile_j = 32, tile_i = 8;  // FCT tile (p x x) = thread block of the sub-step kernels
     DevBuf dpf;  // per-run PoissonFastDev (FP32 sets)
     std::vector<int> ghost_ptr, iface_ptr, csync_ptr;
     cudaGraphExec_t graph = nullptr;
@@ -220,11 +221,16 @@ public:
     double measure_fp64_peak();
     void sync();
     void forget(Run *r);
+    // Times the FCT sub-step kernels of the set for each candidate tile shape and keeps
+    // the fastest for this precision (autotune.cpp).  Leaves the solution unchanged.
+    std::pair<int, int> autotune(const std::vector<Run *> &set, int reps);
+    int tile_pref[2][2] = {{32, 8}, {32, 8}};  // [precision 64, 32] -> (tile_j, tile_i)
 
 private:
     std::map<std::vector<Run *>, std::unique_ptr<LaunchSet>> sets_;
     LaunchSet &get_set(const std::vector<Run *> &set);
     void build_set(LaunchSet &L);
+    void build_tiles(LaunchSet &L);
     void record_step(LaunchSet &L);
     int launches_per_step_ = 0;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;

@@ -225,7 +225,7 @@ __global__ void k64_copy10(const P64 *patches, const TileRef *tiles) {
 
 // --------------------------------------------------------------------------------
 void launch_fct64_substep(const FctLaunch &L, int sub) {
-    dim3 blk(32, 8);
+    dim3 blk(L.tile_j ? L.tile_j : 32, L.tile_i ? L.tile_i : 8);
     const P64 *pp = (const P64 *)L.patches;
     if (L.ntiles == 0) return;
     switch (sub) {

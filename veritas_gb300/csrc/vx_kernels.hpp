@@ -39,6 +39,7 @@ struct FctLaunch {
     int step;
     int use_f0;
     int part;  // faces / flux: 1 x faces only, 2 p faces only, 0 both
+    int tile_j, tile_i;  // thread block = one tile of tile_j (p) x tile_i (x) cells
     cudaStream_t stream;
 };
 
