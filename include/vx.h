@@ -60,6 +60,11 @@ typedef struct vx_problem {
                         * accumulated and fields advanced in FP64; Poisson by prefix
                         * scans instead of the dense LU) */
     double bdens, bp0, bTe; /* beam population: density fraction of the slab, drift, temperature [keV] */
+    int32_t poisson;   /* Poisson solver of precision-64 runs: 0 (default) the reference's
+                        * dense LU in its rounding order; 1 the O(n) prefix-scan solve on a
+                        * thread-block cluster (not the LU's rounding: about 4e-11 relative
+                        * from it at n = 8192, growing as n^2 with the LU's own error).
+                        * Precision-32 runs always use 1. */
 } vx_problem;
 
 /* Fills *p with the defaults of the 2048 x 256 single-level laser/slab case. */

@@ -47,6 +47,7 @@ class _Problem(ctypes.Structure):
         ("cfl", ctypes.c_double), ("minEff", ctypes.c_double), ("crit", ctypes.c_double), ("sizeWeight", ctypes.c_double),
         ("quadDepth", ctypes.c_int32), ("precision", ctypes.c_int32),
         ("bdens", ctypes.c_double), ("bp0", ctypes.c_double), ("bTe", ctypes.c_double),
+        ("poisson", ctypes.c_int32),
     ]
 
 
@@ -160,6 +161,7 @@ class Problem:
     bdens: float = 0.0
     bp0: float = 0.0
     bTe: float = 1.0
+    poisson: int = 0  # precision-64 runs: 0 the reference's LU rounding order, 1 the O(n) scan solve
 
     def to_c(self) -> _Problem:
         p = _Problem()

@@ -118,7 +118,8 @@ __global__ void k_iface(const PatchT<T> *patches, const IfaceOp *ops, int n, int
             for (int q = 0; q < r; q++) {
                 const int fid = pidx(op.fi, op.fj + q, F.pitch);
                 T lo;
-                if (F.ifx && F.ifx[fid]) lo = F.FxL[fid];
+                // the FP32 form keeps no face-velocity plane; its FxL is this value
+                if (sizeof(T) == 4 || (F.ifx && F.ifx[fid])) lo = F.FxL[fid];
                 else {
                     const T am = F.ex[fid];
                     lo = dxi * (am > (T)0 ? f[fid - F.pitch] : f[fid]) * am;
@@ -136,7 +137,7 @@ __global__ void k_iface(const PatchT<T> *patches, const IfaceOp *ops, int n, int
             for (int q = 0; q < r; q++) {
                 const int fid = pidx(op.fi + q, op.fj, F.pitch);
                 T lo;
-                if (F.ifp && F.ifp[fid]) lo = F.FpL[fid];
+                if (sizeof(T) == 4 || (F.ifp && F.ifp[fid])) lo = F.FpL[fid];
                 else {
                     const T am = F.ep[fid];
                     lo = dpi * (am > (T)0 ? f[fid - 1] : f[fid]) * am;

@@ -22,11 +22,15 @@ std::pair<int, int> Engine::autotune(const std::vector<Run *> &set, int reps) {
     fl.params32 = L.dparams32.as<float>();
     fl.step = 0;
     fl.stream = stream;
+    fl.xtiles = L.dxtiles.as<TileRef>();
+    fl.ptiles = L.dptiles.as<TileRef>();
+    fl.nxtiles = L.nxtiles;
+    fl.nptiles = L.nptiles;
     auto run_subs = [&]() {
-        for (int sub : {kSubGamma, kSubFaces, kSubFlux, kSubDsF2, kSubLimR, kSubLimC}) {
-            if (L.precision == kF32) launch_fct32_substep(fl, sub);
-            else launch_fct64_substep(fl, sub);
-        }
+        if (L.precision == kF32)
+            for (int sub : {kSubXFlux, kSubPFlux, kSubDsF2, kSubLimR, kSubLimC}) launch_fct32_substep(fl, sub);
+        else
+            for (int sub : {kSubGamma, kSubFaces, kSubFlux, kSubDsF2, kSubLimR, kSubLimC}) launch_fct64_substep(fl, sub);
     };
     double best_ms = 1e300;
     int best[2] = {L.tile_j, L.tile_i};

@@ -122,6 +122,7 @@ void vx_problem_defaults(vx_problem *p) {
     p->bdens = d.bdens;
     p->bp0 = d.bp0;
     p->bTe = d.bTe;
+    p->poisson = 0;
 }
 
 const char *vx_last_error(void) { return g_err.c_str(); }
@@ -167,7 +168,10 @@ int vx_run_create(vx_ctx *ctx, const vx_problem *prob, vx_run **out) {
         if (prob->precision != 64 && prob->precision != 32) throw std::invalid_argument("precision must be 64 or 32");
         auto r = std::make_unique<vx_run>();
         r->ctx = ctx;
+        if (prob->poisson != vx::kPoissonLU && prob->poisson != vx::kPoissonScan)
+            throw std::invalid_argument("poisson must be 0 (LU) or 1 (scan)");
         r->run.reset(new vx::Run(*ctx->eng, std::make_shared<vx::LaserSlab>(to_params(*prob)), prob->precision));
+        r->run->poisson = prob->poisson;
         r->run->init();
         ctx->eng->runs.push_back(r->run.get());
         *out = r.release();
@@ -463,7 +467,7 @@ int vx_server_clock(vx_server *s, double *now) {
 int vx_server_submit(vx_server *s, const vx_problem *p, int64_t steps, double arrival, const char *state_path,
                      int64_t *id) {
     if (!s || !p || !id) return VX_ERR_INVALID;
-    return guard([&] { *id = s->srv->submit(to_params(*p), p->precision, steps, arrival, state_path ? state_path : ""); });
+    return guard([&] { *id = s->srv->submit(to_params(*p), p->precision, steps, arrival, state_path ? state_path : "", p->poisson); });
 }
 
 int vx_server_step(vx_server *s, int *live, int *waiting) {

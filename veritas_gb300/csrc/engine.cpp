@@ -330,7 +330,8 @@ void Run::init() {
     }
     alloc_fields();
     push_data(1);
-    if (precision == kF32) {
+    if (precision == kF32) poisson = kPoissonScan;
+    if (poisson == kPoissonScan) {
         build_poisson_fast();
     } else {
         int info = lu.build(n);
@@ -424,6 +425,8 @@ Engine::Engine(int dev) : device(dev) {
     VX_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     VX_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     VX_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    VX_CUDA(cudaEventCreateWithFlags(&ev_gamma, cudaEventDisableTiming));
+    VX_CUDA(cudaEventCreateWithFlags(&ev_mx, cudaEventDisableTiming));
 }
 
 Engine::~Engine() {
@@ -432,6 +435,8 @@ Engine::~Engine() {
     if (ev1_) cudaEventDestroy(ev1_);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
+    if (ev_gamma) cudaEventDestroy(ev_gamma);
+    if (ev_mx) cudaEventDestroy(ev_mx);
     if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
 }
@@ -483,13 +488,14 @@ static void run_moments(const LaunchSet &L, const MomLaunch &ml) {
     else launch_moments64(ml);
 }
 static void run_poisson(const LaunchSet &L, const PoissonLaunch &pl) {
-    if (L.precision == kF32) {
+    if (L.poisson == kPoissonScan) {
         PoissonFastLaunch f{};
         f.pf = L.dpf.as<PoissonFastDev>();
         f.fields = pl.fields;
         f.w = pl.w;
         f.fcoef = pl.fcoef;
         f.nruns = pl.nruns;
+        f.maxn = pl.maxn;
         f.stream = pl.stream;
         launch_poisson_fast(f);
     } else {
@@ -505,6 +511,10 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     fl.ntiles = L.ntiles;
     fl.tile_j = L.tile_j;
     fl.tile_i = L.tile_i;
+    fl.xtiles = L.dxtiles.as<TileRef>();
+    fl.ptiles = L.dptiles.as<TileRef>();
+    fl.nxtiles = L.nxtiles;
+    fl.nptiles = L.nptiles;
     fl.fields = L.dfields.as<RunFields>();
     fl.params = L.dparams.as<double>();
     fl.params32 = L.dparams32.as<float>();
@@ -519,8 +529,18 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
         kernel_launches += reps + 1;
     };
     // stage-0 parameters with dt = 0 keep every kernel well defined
-    for (int sub : {kSubGamma, kSubFaces, kSubFlux, kSubDsF2, kSubLimR, kSubLimC, kSubUpdate})
-        time_it([&] { fct_sub(L, fl, sub); });
+    // FP32 sets run the fused face + flux kernels: "faces" and "flux" time the x and p
+    // ones, "gamma" (folded into them) reads 0
+    for (int sub : {kSubGamma, kSubFaces, kSubFlux, kSubDsF2, kSubLimR, kSubLimC, kSubUpdate}) {
+        if (L.precision == kF32 && sub == kSubGamma) {
+            out.push_back(0.0);
+            continue;
+        }
+        const int run = L.precision == kF32 && sub == kSubFaces ? kSubXFlux
+                        : L.precision == kF32 && sub == kSubFlux ? kSubPFlux
+                                                                  : sub;
+        time_it([&] { fct_sub(L, fl, run); });
+    }
     MomLaunch ml{};
     ml.patches = L.dpatch.p;
     ml.colpatch = L.dcolpatch.as<int>();
@@ -616,15 +636,37 @@ void Engine::build_tiles(LaunchSet &L) {
                 }
     L.ntiles = (int)tiles.size();
     L.dtiles = upload(tiles, stream);
+    if (L.precision == kF32) {  // strip tiles of the fused face + flux kernels
+        std::vector<TileRef> xt, pt;
+        pi = 0;
+        for (Run *R : L.runs)
+            for (auto &sp : R->rects)
+                for (auto &lvl : sp)
+                    for (auto &rp : lvl) {
+                        for (int i0 = 0; i0 <= rp->n_x; i0 += kStripRows)
+                            for (int j0 = -1; j0 <= rp->n_p; j0 += kXCols) xt.push_back({pi, i0, j0});
+                        for (int i0 = -1; i0 <= rp->n_x; i0 += kStripRows)
+                            for (int j0 = 0; j0 <= rp->n_p; j0 += 32) pt.push_back({pi, i0, j0});
+                        pi++;
+                    }
+        L.nxtiles = (int)xt.size();
+        L.nptiles = (int)pt.size();
+        L.dxtiles = upload(xt, stream);
+        L.dptiles = upload(pt, stream);
+    }
 }
 
 void Engine::build_set(LaunchSet &L) {
     L.precision = L.runs.empty() ? kF64 : L.runs[0]->precision;
     L.tile_j = tile_pref[L.precision == kF32][0];
     L.tile_i = tile_pref[L.precision == kF32][1];
-    for (Run *R : L.runs)
+    L.poisson = L.runs.empty() ? kPoissonLU : L.runs[0]->poisson;
+    for (Run *R : L.runs) {
         if (R->precision != L.precision)
             throw std::invalid_argument("runs advanced together must share one precision");
+        if (R->poisson != L.poisson)
+            throw std::invalid_argument("runs advanced together must share one Poisson solver");
+    }
     std::vector<PoissonFastDev> pfs;
     for (Run *R : L.runs) pfs.push_back(R->pfdev);
     L.dpf = upload(pfs, stream);
@@ -787,6 +829,10 @@ void Engine::record_step(LaunchSet &L) {
     fl.ntiles = L.ntiles;
     fl.tile_j = L.tile_j;
     fl.tile_i = L.tile_i;
+    fl.xtiles = L.dxtiles.as<TileRef>();
+    fl.ptiles = L.dptiles.as<TileRef>();
+    fl.nxtiles = L.nxtiles;
+    fl.nptiles = L.nptiles;
     fl.fields = L.dfields.as<RunFields>();
     fl.params = L.dparams.as<double>();
     fl.params32 = L.dparams32.as<float>();
@@ -837,24 +883,45 @@ void Engine::record_step(LaunchSet &L) {
         VX_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
         pl.stream = side;
         run_poisson(L, pl);
-        launches += 1;
+        launches += L.poisson == kPoissonScan ? 2 : 1;
         if (L.precision == kF32) {
             launch_fields_to_f32(L.dfields.as<RunFields>(), (int)L.runs.size(), L.maxn, 2, side);
             launch_fields_to_f32(L.dfields.as<RunFields>(), (int)L.runs.size(), L.maxn, 1, stream);
             launches += 2;
         }
         fl.step = s;
-        fct_sub(L, fl, kSubGamma);
-        fl.part = 1;
-        fct_sub(L, fl, kSubFaces);
-        fct_sub(L, fl, kSubFlux);
+        // The Maxwell stage (EMFieldSolver::RGKStep) writes A and a^2, which the Vlasov
+        // stage reads only in the gamma kernel (FP64) or the FP32 copy of a^2 made above;
+        // it runs on the side stream after the Poisson solve, beside the rest of the FCT
+        // chain, and joins before the next stage's moments.
+        if (L.precision == kF64) {
+            fct_sub(L, fl, kSubGamma);
+            launches += 1;
+        }
         VX_CUDA(cudaEventRecord(ev_join, side));
-        VX_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
-        fl.part = 2;
-        fct_sub(L, fl, kSubFaces);
-        fct_sub(L, fl, kSubFlux);
-        fl.part = 0;
-        launches += 6;
+        VX_CUDA(cudaEventRecord(ev_gamma, stream));
+        VX_CUDA(cudaStreamWaitEvent(side, ev_gamma, 0));
+        mx.step = s;
+        mx.stream = side;
+        launch_maxwell(mx);
+        launches += 3;
+        VX_CUDA(cudaEventRecord(ev_mx, side));
+        if (L.precision == kF32) {  // fused face + flux kernels per direction
+            fct_sub(L, fl, kSubXFlux);
+            VX_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
+            fct_sub(L, fl, kSubPFlux);
+            launches += 2;
+        } else {
+            fl.part = 1;
+            fct_sub(L, fl, kSubFaces);
+            fct_sub(L, fl, kSubFlux);
+            VX_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
+            fl.part = 2;
+            fct_sub(L, fl, kSubFaces);
+            fct_sub(L, fl, kSubFlux);
+            fl.part = 0;
+            launches += 4;
+        }
         for (size_t b = 0; b + 1 < L.iface_ptr.size(); b++, launches++)
             launch_iface(L.dpatch.p, L.diface.as<IfaceOp>() + L.iface_ptr[b], L.iface_ptr[b + 1] - L.iface_ptr[b], s, L.precision, stream);
         fct_sub(L, fl, kSubDsF2);
@@ -874,9 +941,7 @@ void Engine::record_step(LaunchSet &L) {
             fct_sub(L, fl, kSubCopy10);
             launches += 1;
         }
-        mx.step = s;
-        launch_maxwell(mx);
-        launches += 3;
+        VX_CUDA(cudaStreamWaitEvent(stream, ev_mx, 0));
     }
     launches_per_step_ = launches;
 }

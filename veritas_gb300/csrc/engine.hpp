@@ -110,6 +110,7 @@ public:
     uint64_t layout_version = 0;
     int id = 0;
     int precision = kF64;            // kF64: plain path; kF32: precision form
+    int poisson = kPoissonLU;        // Poisson solver (kF32 runs always use kPoissonScan)
     std::vector<double> fnorm;       // per species: scale of the stored FP32 f (1 for FP64)
     // fast Poisson of the precision form (Woodbury columns and capacitance)
     std::vector<double> pf_Y;
@@ -189,7 +190,10 @@ struct LaunchSet {
     DevBuf dghost, diface, dcsync;
     int precision = kF64;
     int tile_j = 32, tile_i = 8;  // FCT tile (p x x) = thread block of the sub-step kernels
-    DevBuf dpf;  // per-run PoissonFastDev (FP32 sets)
+    DevBuf dxtiles, dptiles;      // FP32: strip tiles of the fused face + flux kernels
+    int nxtiles = 0, nptiles = 0;
+    int poisson = kPoissonLU;
+    DevBuf dpf;  // per-run PoissonFastDev (scan Poisson sets)
     std::vector<int> ghost_ptr, iface_ptr, csync_ptr;
     cudaGraphExec_t graph = nullptr;
     ~LaunchSet();
@@ -203,6 +207,7 @@ public:
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;       // Poisson solve beside the E-independent x-direction work
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_gamma = nullptr, ev_mx = nullptr;  // Maxwell stage beside the FCT chain
     std::vector<Run *> runs;
     bool use_graphs = true;
     uint64_t kernel_launches = 0;  // launches issued by this engine (graph replays count their nodes)

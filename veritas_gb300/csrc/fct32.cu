@@ -206,6 +206,99 @@ __global__ void k32_copy10(const P32 *patches, const TileRef *tiles) {
     P.f0[id] = P.f1[id];
 }
 
+
+// ---------------------------------------------------------------- fused face + flux
+// One warp per strip tile: Lorentz factors, face velocities and WENO values are formed in
+// registers and consumed there (neighbours through shuffles), so neither gamma nor the
+// face planes go to HBM.  The fluxes are those of k32_faces / k32_flux; face values
+// outside the ranges the separate kernels write (x: i in [0, nx], j in [-1, np];
+// p: i in [-1, nx], j in [0, np]) are zero, as the planes they read are.
+
+// x direction: a warp covers kXCols output columns j0 .. j0+29 (its 32 lanes hold the
+// face values of j0-1 .. j0+30) over kStripRows rows; rows are independent in x.
+__global__ void k32_xflux(const P32 *patches, const TileRef *tiles, int ntiles, const RunFields *fields, int step,
+                          int use_f0) {
+    const int wt = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (wt >= ntiles) return;
+    const int lane = threadIdx.x & 31;
+    const TileRef t = tiles[wt];
+    const P32 &P = patches[t.patch];
+    const int pit = P.pitch;
+    const float *f = use_f0 ? P.f0 : P.f1;
+    const RunFields &F = fields[P.run];
+    const int jj = t.j0 - 1 + lane;
+    const bool col_ok = jj >= -1 && jj <= P.np;
+    const float p0 = mom32(P, jj), p1 = mom32(P, jj + 1);
+    const float w3 = 1.0f / 48.0f;
+    const unsigned full = 0xffffffffu;
+    for (int r = 0; r < kStripRows; r++) {
+        const int i = t.i0 + r;
+        if (i > P.nx) break;  // warp-uniform
+        float am = 0.0f, fv = 0.0f;
+        if (col_ok) {
+            const float a = asq32(P, F, i);
+            const float g0 = sqrtf(1.0f + p0 * p0 + a), g1 = sqrtf(1.0f + p1 * p1 + a);
+            am = P.kxf * (P.dpnf * (p1 + p0) / (g1 + g0));
+            const int id = pidx(i, jj, pit);
+            fv = weno32(f[id - 2 * pit], f[id - pit], f[id], f[id + pit], am > 0.0f, P.weno_eps);
+        }
+        const float am1 = __shfl_up_sync(full, am, 1), ap1 = __shfl_down_sync(full, am, 1);
+        const float fm1 = __shfl_up_sync(full, fv, 1), fp1 = __shfl_down_sync(full, fv, 1);
+        if (lane < 1 || lane > kXCols || !col_ok) continue;
+        const int id = pidx(i, jj, pit);
+        if (P.ifx && P.ifx[id]) continue;
+        P.FxH[step][id] = P.dxif * (fv * am + w3 * (fp1 - fm1) * (ap1 - am1));
+        if (step == 0) P.FxL[id] = P.dxif * ((am > 0.0f ? f[id - pit] : f[id]) * am);
+    }
+}
+
+// p direction: a warp covers 32 columns over kStripRows output rows, walking down with
+// the face values of the previous and next rows in registers.
+__device__ __forceinline__ void pface32(const P32 &P, const RunFields &F, const float *f, int i, int j, float p,
+                                        bool col_ok, float &am, float &fv) {
+    am = 0.0f;
+    fv = 0.0f;
+    if (!col_ok || i < -1 || i > P.nx) return;
+    const float a0 = asq32(P, F, i), a1 = asq32(P, F, i + 1);
+    const float g0 = sqrtf(1.0f + p * p + a0), g1 = sqrtf(1.0f + p * p + a1);
+    am = qefield32(P, F, i) - P.kpf * ((a1 - a0) / (g1 + g0));
+    const int id = pidx(i, j, P.pitch);
+    fv = weno32(f[id - 2], f[id - 1], f[id], f[id + 1], am > 0.0f, P.weno_eps);
+}
+
+__global__ void k32_pflux(const P32 *patches, const TileRef *tiles, int ntiles, const RunFields *fields, int step,
+                          int use_f0) {
+    const int wt = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (wt >= ntiles) return;
+    const int lane = threadIdx.x & 31;
+    const TileRef t = tiles[wt];
+    const P32 &P = patches[t.patch];
+    const float *f = use_f0 ? P.f0 : P.f1;
+    const RunFields &F = fields[P.run];
+    const int j = t.j0 + lane;
+    const bool col_ok = j >= 0 && j <= P.np;
+    const float p = mom32(P, j);
+    const float w3 = 1.0f / 48.0f;
+    float amA, fvA, amB, fvB;  // rows i-1 and i
+    pface32(P, F, f, t.i0 - 1, j, p, col_ok, amA, fvA);
+    pface32(P, F, f, t.i0, j, p, col_ok, amB, fvB);
+    for (int r = 0; r < kStripRows; r++) {
+        const int i = t.i0 + r;
+        if (i > P.nx) break;
+        float amC, fvC;  // row i+1
+        pface32(P, F, f, i + 1, j, p, col_ok, amC, fvC);
+        if (col_ok && !(P.ifp && P.ifp[pidx(i, j, P.pitch)])) {
+            const int id = pidx(i, j, P.pitch);
+            P.FpH[step][id] = P.dpif * (fvB * amB + w3 * (fvC - fvA) * (amC - amA));
+            if (step == 0) P.FpL[id] = P.dpif * ((amB > 0.0f ? f[id - 1] : f[id]) * amB);
+        }
+        amA = amB;
+        fvA = fvB;
+        amB = amC;
+        fvB = fvC;
+    }
+}
+
 void launch_fct32_substep(const FctLaunch &L, int sub) {
     dim3 blk(L.tile_j ? L.tile_j : 32, L.tile_i ? L.tile_i : 8);
     const P32 *pp = (const P32 *)L.patches;
@@ -234,6 +327,12 @@ void launch_fct32_substep(const FctLaunch &L, int sub) {
             break;
         case kSubCopy10:
             k32_copy10<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles);
+            break;
+        case kSubXFlux:
+            if (L.nxtiles) k32_xflux<<<(L.nxtiles + 3) / 4, 128, 0, L.stream>>>(pp, L.xtiles, L.nxtiles, L.fields, L.step, L.use_f0);
+            break;
+        case kSubPFlux:
+            if (L.nptiles) k32_pflux<<<(L.nptiles + 3) / 4, 128, 0, L.stream>>>(pp, L.ptiles, L.nptiles, L.fields, L.step, L.use_f0);
             break;
     }
 }

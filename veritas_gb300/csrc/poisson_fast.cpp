@@ -1,9 +1,10 @@
-// Host set-up of the scan-based Poisson solve of the FP32 precision form (the device
-// part, k_poisson_fast, documents the algorithm): the Woodbury columns
+// Host set-up of the scan-based Poisson solve (the device part, poisson_scan64.cu,
+// documents the algorithm): the Woodbury columns
 // Y = (1/c) G^{-T} G^{-1} [e_0 e_1 e_{m-1}] and the 3x3 factor K = (I + C U^T Y)^{-1} C,
 // where C holds the top-left correction of T - c G G^T and the corner coupling of B.
 #include <cmath>
 #include <stdexcept>
+#include <string>
 
 #include "engine.hpp"
 
@@ -31,7 +32,9 @@ void Run::build_poisson_fast() {
     const double w1 = -16.0 / 30.0 / 0.4, w2 = 1.0 / 30.0 / 0.4;  // EMSolver.cpp:28
     const int m = n - 1;
     if (m < 4) throw std::invalid_argument("grid too small for the fast Poisson solve");
-    if (m > 1024 * kPfMaxSeg) throw std::invalid_argument("grid too large for the fast Poisson solve");
+    if (m > kPsMaxUnknowns)
+        throw std::invalid_argument("grid too large for the scan Poisson solve (n - 1 > " +
+                                    std::to_string(kPsMaxUnknowns) + ")");
     const double rho = 7.0 - 4.0 * std::sqrt(3.0);
     const double c = w2 / rho;
     const double g1 = -(1.0 + rho);

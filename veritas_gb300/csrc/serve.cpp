@@ -46,13 +46,15 @@ Server::Server(Engine &e, size_t budget, int max_live) : eng(e), budget_(budget)
 Server::~Server() = default;
 
 int64_t Server::submit(const LaserSlabParams &p, int precision, int64_t steps, double arrival,
-                       const std::string &state_path) {
+                       const std::string &state_path, int poisson) {
     if (steps <= 0) throw std::invalid_argument("a request needs at least one step");
     if (precision != kF64 && precision != kF32) throw std::invalid_argument("precision must be 64 or 32");
+    if (poisson != kPoissonLU && poisson != kPoissonScan) throw std::invalid_argument("poisson must be 0 or 1");
     Request r;
     r.id = next_id_++;
     r.params = p;
     r.precision = precision;
+    r.poisson = precision == kF32 ? kPoissonScan : poisson;
     r.steps = steps;
     r.arrival = arrival;
     r.state_path = state_path;
@@ -70,6 +72,7 @@ void Server::admit(double now) {
         waiting_.pop_front();
         r.admitted = now;
         r.run.reset(new Run(eng, std::make_shared<LaserSlab>(r.params), r.precision));
+        r.run->poisson = r.poisson;
         r.run->init();
         r.bytes = r.run->device_bytes();
         used_ += r.bytes;
@@ -82,15 +85,16 @@ int Server::step(double now) {
     if (live_.empty()) return 0;
     std::vector<Run *> set;
     for (int64_t id : live_) set.push_back(reqs_.at(id).run.get());
-    // one launch set per precision (the FP32 and FP64 kernels are different launches)
-    for (int prec : {kF64, kF32}) {
-        std::vector<Run *> part;
-        for (Run *r : set)
-            if (r->precision == prec) part.push_back(r);
-        if (part.empty()) continue;
-        auto dt = eng.calculate_dt(part);
-        eng.advance(part, dt);
-    }
+    // one launch set per precision and Poisson solver (different kernels)
+    for (int prec : {kF64, kF32})
+        for (int pois : {kPoissonLU, kPoissonScan}) {
+            std::vector<Run *> part;
+            for (Run *r : set)
+                if (r->precision == prec && r->poisson == pois) part.push_back(r);
+            if (part.empty()) continue;
+            auto dt = eng.calculate_dt(part);
+            eng.advance(part, dt);
+        }
     eng.sync();
     std::vector<int64_t> still;
     for (int64_t id : live_) {

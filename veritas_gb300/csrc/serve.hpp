@@ -17,6 +17,7 @@ public:
         int64_t id = 0;
         LaserSlabParams params;
         int precision = kF64;
+        int poisson = kPoissonLU;
         int64_t steps = 0, done_steps = 0;
         double arrival = 0, admitted = -1, finish = -1, sim_time = 0;
         size_t estimate = 0, bytes = 0;
@@ -30,7 +31,7 @@ public:
     ~Server();
     // Queue a solve of `steps` RK steps that arrived at `arrival` (seconds on clock()).
     int64_t submit(const LaserSlabParams &p, int precision, int64_t steps, double arrival,
-                   const std::string &state_path);
+                   const std::string &state_path, int poisson = kPoissonLU);
     // Admit what fits, advance every live solve one step, retire the finished ones.
     // Returns the number of solves still live.
     int step(double now);

@@ -39,6 +39,8 @@ constexpr double kRK[6][6] = {
 };
 
 enum Precision : int { kF64 = 64, kF32 = 32 };
+// Poisson solver: the reference's LU in its rounding order, or the O(n) prefix-scan solve
+enum PoissonSolver : int { kPoissonLU = 0, kPoissonScan = 1 };
 
 // Device view of one patch.  T is the storage type of f / fluxes / limiter planes.
 template <class T>

@@ -27,6 +27,9 @@ enum FctSub : int {
     kSubLimC,
     kSubUpdate,
     kSubCopy10,
+    // FP32 form only: gamma + x faces + x fluxes, and p faces + p fluxes, each fused
+    kSubXFlux,
+    kSubPFlux,
 };
 
 struct FctLaunch {
@@ -40,8 +43,13 @@ struct FctLaunch {
     int use_f0;
     int part;  // faces / flux: 1 x faces only, 2 p faces only, 0 both
     int tile_j, tile_i;  // thread block = one tile of tile_j (p) x tile_i (x) cells
+    // FP32 fused face + flux kernels: one warp per strip tile
+    const TileRef *xtiles, *ptiles;
+    int nxtiles, nptiles;
     cudaStream_t stream;
 };
+constexpr int kStripRows = 16;  // rows per strip tile of the fused FP32 face + flux kernels
+constexpr int kXCols = 30;      // output columns per x strip (32 lanes hold j0-1 .. j0+30)
 
 void launch_fct64_substep(const FctLaunch &L, int sub);
 void launch_fct32_substep(const FctLaunch &L, int sub);
@@ -109,9 +117,11 @@ struct PoissonLaunch {
 };
 void launch_poisson(const PoissonLaunch &L);
 
-// Poisson solve of the FP32 precision form by prefix scans (fields32.cu).  Y holds the
-// m x 3 Woodbury columns (row-major), K the 3x3 capacitance factor.
-constexpr int kPfMaxSeg = 64;  // elements per thread: n - 1 <= 1024 * kPfMaxSeg
+// O(n) Poisson solve by prefix scans, one thread-block cluster per run (poisson_scan64.cu).
+// Y holds the m x 3 Woodbury columns (row-major), K the 3x3 capacitance factor.
+constexpr int kPsThreads = 512, kPsCluster = 8;
+constexpr int kPsMaxSeg = 48;                                           // elements per thread
+constexpr int kPsMaxUnknowns = kPsThreads * kPsCluster * kPsMaxSeg;     // n - 1 <= this
 struct PoissonFastDev {
     const double *Y;
     double K[9];
@@ -123,9 +133,11 @@ struct PoissonFastLaunch {
     const double *w;           // per run: dx0^2
     const double *fcoef;       // per run: 1/(12 dx0)
     int nruns;
+    int maxn;                  // largest n of the runs
     cudaStream_t stream;
 };
 void launch_poisson_fast(const PoissonFastLaunch &L);
+size_t poisson_scan_smem(int maxn);  // dynamic shared memory of one block
 // FP32 copies of a^2 (which & 1) and E_x (which & 2) of every run of a set (the FP32 form
 // reads these).
 void launch_fields_to_f32(RunFields *fields, int nruns, int maxn, int which, cudaStream_t s);
