@@ -264,9 +264,11 @@ def field_energy(s):
         0.5 / MU0 * float(np.sum(By * By) + np.sum(Bz * Bz))
 
 
-def measure_fp32_form(ctx, init_path: Path, steps: int, warmup: int) -> dict:
-    """The FP32 precision form on the same workload: throughput, and its error against
-    the FP64 path over `steps` steps from the same state with the same dt sequence."""
+def measure_form(ctx, init_path: Path, steps: int, warmup: int, variant: dict, dtype: str) -> dict:
+    """A variant of the plain path (`variant` overrides Problem fields: the FP32 precision
+    form, or FP64 with the scan Poisson solve) on the same workload: throughput, and its
+    error against the plain FP64 path over `steps` steps from the same state with the same
+    dt sequence."""
     import dataclasses
 
     import numpy as np
@@ -276,7 +278,7 @@ def measure_fp32_form(ctx, init_path: Path, steps: int, warmup: int) -> dict:
     sys.path.insert(0, str(ROOT / "tests"))
     import vxstate
 
-    p32 = dataclasses.replace(problem_config2(), precision=32)
+    p32 = dataclasses.replace(problem_config2(), **variant)
     s = SolverManager(ctx, p32)
     cells = s.cell_count()
     from veritas_gb300 import autotune_many
@@ -324,8 +326,8 @@ def measure_fp32_form(ctx, init_path: Path, steps: int, warmup: int) -> dict:
             den = max(den, float(np.max(np.abs(fa))))
     a.close()
     b.close()
-    return {"value": cells / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "dtype": "f32 (moments, fields, Poisson f64)",
-            "tile_p_x": list(tile),
+    return {"value": cells / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "dtype": dtype,
+            "variant": variant, "tile_p_x": list(tile),
             "error_vs_fp64": {"steps": steps, "from": "the FP64 run's initial hierarchy (t = 0), same dt sequence",
                               "f_rel_linf": num / den, "field_energy_rel_max": ew,
                               "Ex_abs_max_over_laser_E0": ee, "Ey_abs_max_over_laser_E0": ey},
@@ -537,11 +539,15 @@ def main() -> None:
 
     forms = None
     if rank == 0 and not args.no_forms:
-        forms = {"fp32": measure_fp32_form(ctx, init_path, args.steps, warmup),
+        forms = {"fp32": measure_form(ctx, init_path, args.steps, warmup, {"precision": 32},
+                                      "f32 (moments, fields, Poisson f64)"),
+                 "fp64_scan_poisson": measure_form(ctx, init_path, args.steps, warmup, {"poisson": 1},
+                                                   "f64 (O(n) scan Poisson instead of the LU's rounding order)"),
                  "batched_fp32": measure_batched(ctx, 64, 5, 3, 32),
                  "served_fp32": measure_serving(ctx, 24, 16, 32),
                  "served_fp64": measure_serving(ctx, 24, 16, 64)}
         forms["fp32_speedup_vs_fp64"] = forms["fp32"]["value"] / value
+        forms["fp64_scan_poisson_speedup_vs_fp64"] = forms["fp64_scan_poisson"]["value"] / value
         forms["batched_fp32_speedup_vs_fp64"] = forms["batched_fp32"]["value"] / value
 
     cpu = None

@@ -552,6 +552,20 @@ void Run::build_amr() {
     }
     drelc = DevBuf(w.size() * sizeof(double));
     VX_CUDA(cudaMemcpy(drelc.p, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<float> w32;
+    relc32_off.assign(L, 0);
+    for (int d = 0; d < L; d++) {
+        relc32_off[d] = (int)w32.size();
+        const int rtb = (int)std::pow(r, d);
+        double sum[3] = {0, 0, 0};
+        for (int q = 0; q < 3 * rtb; q++) {
+            w32.push_back((float)w[relc_off[d] + q]);
+            sum[q % 3] += w[relc_off[d] + q];
+        }
+        for (double v : sum) w32.push_back((float)v);
+    }
+    drelc32 = DevBuf(w32.size() * sizeof(float));
+    VX_CUDA(cudaMemcpy(drelc32.p, w32.data(), w32.size() * sizeof(float), cudaMemcpyHostToDevice));
 }
 
 }  // namespace vx

@@ -22,10 +22,6 @@ std::pair<int, int> Engine::autotune(const std::vector<Run *> &set, int reps) {
     fl.params32 = L.dparams32.as<float>();
     fl.step = 0;
     fl.stream = stream;
-    fl.xtiles = L.dxtiles.as<TileRef>();
-    fl.ptiles = L.dptiles.as<TileRef>();
-    fl.nxtiles = L.nxtiles;
-    fl.nptiles = L.nptiles;
     auto run_subs = [&]() {
         if (L.precision == kF32)
             for (int sub : {kSubXFlux, kSubPFlux, kSubDsF2, kSubLimR, kSubLimC}) launch_fct32_substep(fl, sub);
@@ -37,9 +33,13 @@ std::pair<int, int> Engine::autotune(const std::vector<Run *> &set, int reps) {
     for (auto &sh : kShapes) {
         L.tile_j = sh[0];
         L.tile_i = sh[1];
-        build_tiles(L);
+        build_tiles(L);  // reallocates every tile list: take the pointers afresh
         fl.tiles = L.dtiles.as<TileRef>();
         fl.ntiles = L.ntiles;
+        fl.xtiles = L.dxtiles.as<TileRef>();
+        fl.ptiles = L.dptiles.as<TileRef>();
+        fl.nxtiles = L.nxtiles;
+        fl.nptiles = L.nptiles;
         fl.tile_j = L.tile_j;
         fl.tile_i = L.tile_i;
         run_subs();  // warm-up

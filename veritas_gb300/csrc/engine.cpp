@@ -156,6 +156,8 @@ void Run::upload_rect_desc(Rect &r, int run_index) {
     d.dpif = (float)d.dp_inv;
     d.qf = (float)d.q;
     d.a2nf = (float)(d.qq * d.g2);
+    d.msc_rho = (1.0 / d.fnorm) * (d.dp * d.q);
+    d.msc_j = (1.0 / d.fnorm) * (1.0 / ((1.0 / d.mass) * kCInv)) * (-d.q * d.q / d.mass);
     if (precision == kF32 && d.rtb > 8) throw std::invalid_argument("the FP32 form supports up to 8 finest cells per coarse cell");
     double *cols = r.cols.as<double>();
     d.chargeR = cols;
@@ -163,6 +165,7 @@ void Run::upload_rect_desc(Rect &r, int run_index) {
     d.r = (int)s.refinementRatio;
     d.relc = drelc.p ? drelc.as<double>() + relc_off[r.depth] : nullptr;
     d.refc = drefc.as<double>();
+    d.relc32 = drelc32.p ? drelc32.as<float>() + relc32_off[r.depth] : nullptr;
     if (r.masks.p) {
         const size_t pe = r.plane_elems();
         uint8_t *m = r.masks.as<uint8_t>();
@@ -261,6 +264,7 @@ void Run::alloc_fields() {
     dex0 = DevBuf(sizeof(double));
     dasq32 = DevBuf((size_t)(n + 1) * sizeof(float));
     defin32 = DevBuf((size_t)n * sizeof(float));
+    dacell32 = DevBuf((size_t)nf * sizeof(float));
     F.n = n;
     F.pre = pre;
     F.post = post;
@@ -279,7 +283,7 @@ void Run::alloc_fields() {
     F.neut = dneut.as<double>();
     F.efin = defin.as<double>();
     F.ex0 = dex0.as<double>();
-    F.asq_cell = nullptr;
+    F.acell32 = dacell32.as<float>();
     F.asq32 = dasq32.as<float>();
     F.efin32 = defin32.as<float>();
 }
@@ -548,6 +552,8 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     ml.ncols = L.ncols;
     ml.maxnp = L.maxnp;
     ml.fields = L.dfields.as<RunFields>();
+    ml.nruns = (int)L.runs.size();
+    ml.maxnf = L.maxnf;
     ml.stream = stream;
     time_it([&] { run_moments(L, ml); });
     AsmLaunch al{};
@@ -845,6 +851,8 @@ void Engine::record_step(LaunchSet &L) {
     ml.ncols = L.ncols;
     ml.maxnp = L.maxnp;
     ml.fields = L.dfields.as<RunFields>();
+    ml.nruns = (int)L.runs.size();
+    ml.maxnf = L.maxnf;
     ml.stream = stream;
     AsmLaunch al{};
     al.patches = L.dpatch.p;
@@ -876,7 +884,7 @@ void Engine::record_step(LaunchSet &L) {
     for (int s = 0; s < 6; s++) {
         run_moments(L, ml);
         launch_assemble(al);
-        launches += 2;
+        launches += L.precision == kF32 ? 3 : 2;
         // the Poisson solve (and E_x) runs beside the x-direction face work, which does
         // not read E_x; the p-direction faces wait for both
         VX_CUDA(cudaEventRecord(ev_fork, stream));
@@ -1075,6 +1083,8 @@ void Engine::moments_only(const std::vector<Run *> &set) {
     ml.ncols = L.ncols;
     ml.maxnp = L.maxnp;
     ml.fields = L.dfields.as<RunFields>();
+    ml.nruns = (int)L.runs.size();
+    ml.maxnf = L.maxnf;
     ml.stream = stream;
     run_moments(L, ml);
     AsmLaunch al{};

@@ -101,7 +101,7 @@ public:
     int n = 0, pre = 0, post = 0, nf = 0;
     double dx0 = 0;
     // fields
-    DevBuf dBy, dBz, dEy, dEz, dAy, dAz, dasq, dphi, dcharge, dJ, dneut, defin, dex0, dasq32, defin32;
+    DevBuf dBy, dBz, dEy, dEz, dAy, dAz, dasq, dphi, dcharge, dJ, dneut, defin, dex0, dasq32, defin32, dacell32;
     RunFields F{};
     PoissonLU lu;
     DevBuf dlu_perm, dlb_band, dlb_fptr, dlb_fcol, dlb_fval, dlb_slot, dlb_sload, dlb_take, dub_band, dub_diag, dub_rdiag, dub_rdlo, dub_fptr, dub_fcol,
@@ -148,6 +148,8 @@ public:
     DevBuf drelc;                   // sub-cell interpolation weights per depth
     DevBuf drefc;                   // coarse-to-fine interpolation weights (refinement ratio)
     std::vector<int> relc_off;      // offset of depth d's weights in drelc
+    DevBuf drelc32;                 // FP32 copy: per depth 3*rtb weights, then their 3 sums
+    std::vector<int> relc32_off;
     bool multi_patch = false;
     void build_amr();               // connectivity + op lists + masks for the current layout
     void validate_ops() const;      // bounds of every op against its patches

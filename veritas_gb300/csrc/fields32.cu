@@ -2,8 +2,8 @@
 //
 //  * k32_moments — momentum moments (Rectangle::CalculateRhoAndJ, Rectangle.cpp:157-282)
 //    of FP32 (scaled) f: the per-cell weights are evaluated in FP32 in a cancellation-free
-//    form; each lane keeps compensated (Kahan) FP32 sums and the lanes are combined in
-//    FP64.
+//    form; each lane keeps compensated (Kahan) FP32 sums, the lanes are combined as
+//    compensated FP32 pairs and the column sum is formed in FP64.
 //
 // It does not reproduce the reference's rounding; the precision form states its error
 // against the FP64 path instead.
@@ -31,7 +31,8 @@ struct RelWeights {
     float k0, k1, k2, s0, s1, s2;
 };
 
-__device__ __forceinline__ float rel_value32(const P32 &P, const float *f, int i, int j, const RelWeights &w) {
+__device__ __forceinline__ float rel_value32(const P32 &P, const float *f, int i, int j, const RelWeights &w,
+                                             float inv_rtb) {
     const int pit = P.pitch;
     const float f3 = f[pidx(i, j, pit)];
     if (P.rtb == 1) return f3;
@@ -41,10 +42,33 @@ __device__ __forceinline__ float rel_value32(const P32 &P, const float *f, int i
     const float a2 = 0.117647058823529f * g1 + 0.029411764705882f * g2 + 0.029411764705882f * g4 + 0.117647058823529f * g5;
     const float a3 = -0.083333333333333f * g1 + 0.166666666666667f * g2 - 0.166666666666667f * g4 + 0.083333333333334f * g5;
     const float mine = w.k0 * a1 + w.k1 * a2 + w.k2 * a3 + f3;
-    const float mean = (w.s0 * a1 + w.s1 * a2 + w.s2 * a3) / (float)P.rtb + f3;
+    const float mean = (w.s0 * a1 + w.s1 * a2 + w.s2 * a3) * inv_rtb + f3;
     return mine + (f3 - mean);
 }
 
+// Compensated FP32 pair (value = hi + lo): TwoSum (Knuth) and FastTwoSum (Dekker)
+// additions for the warp reduction of the lanes' Kahan sums.
+struct F2 {
+    float hi, lo;
+};
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    const float e = (a.hi - (s - bb)) + (b.hi - bb) + (a.lo + b.lo);
+    const float h = s + e;
+    return {h, e - (h - s)};
+}
+__device__ __forceinline__ F2 f2_warp_sum(F2 v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const F2 w{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+        v = f2_add(v, w);
+    }
+    return v;
+}
+
+// No FP64 instruction per cell or per lane: the A^2 of the column comes from the FP32
+// per-cell copy, the weights and the final scales from the patch descriptor; one lane
+// converts the two reduced pairs to FP64.
 __global__ void k32_moments(MomLaunch M) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -58,28 +82,19 @@ __global__ void k32_moments(MomLaunch M) {
     int xc = (i + P.x_pos) * P.rtb + k + F.pre;
     xc = xc > -1 ? xc : 0;
     xc = xc < F.nf ? xc : F.nf - 1;
-    const double ay = F.Ay[F.nf + xc], az = F.Az[F.nf + xc];
-    const float a = (float)(P.qq * ((ay * ay) + (az * az)) * P.g2);
+    const float a = P.a2nf * F.acell32[xc];
     RelWeights w{0, 0, 0, 0, 0, 0};
+    float inv_rtb = 1.0f;
     if (P.rtb > 1) {
-        w.k0 = (float)P.relc[3 * k];
-        w.k1 = (float)P.relc[3 * k + 1];
-        w.k2 = (float)P.relc[3 * k + 2];
-        double s0 = 0, s1 = 0, s2 = 0;
-        for (int q = 0; q < P.rtb; q++) {
-            s0 += P.relc[3 * q];
-            s1 += P.relc[3 * q + 1];
-            s2 += P.relc[3 * q + 2];
-        }
-        w.s0 = (float)s0;
-        w.s1 = (float)s1;
-        w.s2 = (float)s2;
+        const float *rw = P.relc32;
+        w = {rw[3 * k], rw[3 * k + 1], rw[3 * k + 2], rw[3 * P.rtb], rw[3 * P.rtb + 1], rw[3 * P.rtb + 2]};
+        inv_rtb = 1.0f / (float)P.rtb;
     }
     const float pmin = P.pminf, dpn = P.dpnf;
     const float c3 = 1.0f / 48.0f;
     const float *f = P.f1;
     const unsigned full = 0xffffffffu;
-    // per-lane compensated FP32 sums (Kahan); FP64 only for the final warp reduction
+    // per-lane compensated FP32 sums (Kahan)
     float chs = 0.0f, chc = 0.0f, cus = 0.0f, cuc = 0.0f;
     auto kahan = [](float v, float &sum, float &comp) {
         float y = v - comp;
@@ -103,7 +118,7 @@ __global__ void k32_moments(MomLaunch M) {
         const float y1 = 1.0f + u;
         const float l = (y1 == 1.0f) ? u : logf(y1) * (u / (y1 - 1.0f));  // valid on lanes 0..30
         float V = 0.0f;
-        if (j <= P.np) V = rel_value32(P, f, i, j, w);
+        if (j <= P.np) V = rel_value32(P, f, i, j, w, inv_rtb);
         const float lm = __shfl_up_sync(full, l, 1), lp = __shfl_down_sync(full, l, 1);
         const float Vm = __shfl_up_sync(full, V, 1), Vp = __shfl_down_sync(full, V, 1);
         const bool use = lane >= 1 && lane <= kMom32Out && j < P.np && !(P.nested && P.nested[pidx(i, j, P.pitch)]);
@@ -119,22 +134,28 @@ __global__ void k32_moments(MomLaunch M) {
         kahan(c1, chs, chc);
         kahan(j1v, cus, cuc);
     }
-    double ch = (double)chs - (double)chc, cu = (double)cus - (double)cuc;
-    for (int o = 16; o > 0; o >>= 1) {
-        ch += __shfl_down_sync(full, ch, o);
-        cu += __shfl_down_sync(full, cu, o);
-    }
+    const F2 ch = f2_warp_sum(F2{chs, -chc});
+    const F2 cu = f2_warp_sum(F2{cus, -cuc});
     if (lane == 0) {
-        const double q = P.q;
-        const double c2 = 1.0 / ((1.0 / P.mass) * kCInv);  // m c, the reference's c2
-        const double inv = 1.0 / P.fnorm;
-        P.chargeR[c] = ch * inv * (P.dp * q);
-        P.currentR[c] = cu * inv * c2 * (-q * q / P.mass);
+        P.chargeR[c] = ((double)ch.hi + (double)ch.lo) * P.msc_rho;
+        P.currentR[c] = ((double)cu.hi + (double)cu.lo) * P.msc_j;
     }
+}
+
+// FP32 copy of Ay^2 + Az^2 (slot 1) over every run's field grid, read by k32_moments.
+__global__ void k_acell32(const RunFields *fields, int nruns) {
+    const int run = blockIdx.y;
+    if (run >= nruns) return;
+    const RunFields &F = fields[run];
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= F.nf) return;
+    const double ay = F.Ay[F.nf + x], az = F.Az[F.nf + x];
+    F.acell32[x] = (float)((ay * ay) + (az * az));
 }
 
 void launch_moments32(const MomLaunch &M) {
     if (M.ncols == 0) return;
+    k_acell32<<<dim3((M.maxnf + 255) / 256, M.nruns), 256, 0, M.stream>>>(M.fields, M.nruns);
     const int threads = 256;
     const int blocks = (M.ncols * 32 + threads - 1) / threads;
     k32_moments<<<blocks, threads, 0, M.stream>>>(M);

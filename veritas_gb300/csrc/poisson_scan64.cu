@@ -14,13 +14,14 @@
 // first-order recurrences.
 //
 // One thread-block cluster per run: the kPsCluster blocks of a cluster hold consecutive
-// chunks of the vector in shared memory (kPsThreads segments of L elements each, stored
+// chunks of the vector in shared memory (T segments of L elements each, stored
 // segment-minor so that a warp's threads walk their segments on different banks).  A
 // pass runs every segment serially, then fixes the segments up with their carry: the
 // prefix sum of the preceding segment sums (a block scan plus the preceding blocks' totals
 // read through distributed shared memory), or for the decaying recurrences the sum over
 // preceding segment ends weighted by rho^{L (q-1)}, which drops below 1e-20 after a few
-// segments.  The cluster barriers are hardware barriers of co-scheduled blocks.
+// segments (three for L >= 8, which the block size is chosen for).  The cluster barriers
+// are hardware barriers of co-scheduled blocks.
 //
 // FP64 throughout (compiled with --fmad=false like the other FP64 files, so the
 // right-hand side and E_x round as the reference's do).  The result is not the LU's
@@ -38,7 +39,7 @@ namespace {
 
 namespace cg = cooperative_groups;
 
-constexpr int kPsStride = kPsThreads + 1;  // shared-memory row of one element offset
+constexpr int kPsMaxTerms = 24;  // carry-gather terms of a decaying pass (rho^24 < 1e-27)
 
 // E_x at cell i (EMSolver::GetEfield order); phi read past L1, since other blocks of the
 // cluster wrote it in this launch.
@@ -59,7 +60,7 @@ __device__ __forceinline__ double efield_at(const double *phi, int n, double fco
 __device__ double block_exclusive_sum(double v, double *sb, double *tot) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    constexpr int nw = kPsThreads / 32;
+    const int nw = blockDim.x >> 5;
     double x = v;
     for (int o = 1; o < 32; o <<= 1) {
         const double p = __shfl_up_sync(full, x, o);
@@ -80,65 +81,79 @@ __device__ double block_exclusive_sum(double v, double *sb, double *tot) {
     double ex = __shfl_up_sync(full, x, 1);
     if (lane == 0) ex = 0.0;
     if (wid > 0) ex = sb[wid - 1] + ex;
-    __syncthreads();
     return ex;
 }
+
+// Per-block scratch of a pass.
+struct ScanScratch {
+    double *sa;     // [T] segment ends without carry (read across the cluster)
+    double *sb;     // [32] warp totals
+    double *pw;     // [L] mult^(s+1) of the decaying passes
+    double *wt;     // [kPsMaxTerms] rho^(L q) carry weights
+    double *s_tot;  // block total of a prefix-sum pass (read across the cluster)
+    double *s_pre;  // preceding blocks' totals
+    int nterms;     // carry terms of a decaying pass
+};
 
 // y_k = v_k + mult y_{k-1} over the run's m unknowns, in place, ascending (or descending
 // when REV); mult = 1 when UNIT.  Thread t owns segment t (REV: segment T-1-t, so thread
 // order is scan order either way); blocks are in scan order by rank (REV: reversed).
-// pw[s] = mult^(s+1).  Segments past the end of the vector are short or empty; in scan
-// order they come last (REV: first), so no full-length weight ever crosses one.
+// Segments past the end of the vector are short or empty; in scan order they come last
+// (REV: first), so no full-length weight ever crosses one.
 template <bool REV, bool UNIT>
-__device__ void scan_pass(cg::cluster_group &cl, double *xs, int L, int m, int g0, double mult, const double *pw,
-                          double *sa, double *sb, double *s_tot) {
-    constexpr int T = kPsThreads, C = kPsCluster;
+__device__ void scan_pass(cg::cluster_group &cl, double *xs, int L, int m, int g0, double mult, const ScanScratch &W) {
+    constexpr int C = kPsCluster;
+    const int T = blockDim.x, stride = T + 1;
     const int rank = (int)cl.block_rank();
     const int tid = threadIdx.x;
     const int seg = REV ? T - 1 - tid : tid;
     const int len = max(0, min(L, m - (g0 + seg * L)));
     double y = 0.0;
     for (int s = 0; s < len; s++) {
-        double *p = &xs[(REV ? len - 1 - s : s) * kPsStride + seg];
+        double *p = &xs[(REV ? len - 1 - s : s) * stride + seg];
         y = UNIT ? (*p + y) : (*p + mult * y);
         *p = y;
     }
     const int cpos = REV ? C - 1 - rank : rank;  // this block's place in scan order
     double carry;
     if (UNIT) {
-        const double ex = block_exclusive_sum(y, sb, s_tot);
+        const double ex = block_exclusive_sum(y, W.sb, W.s_tot);
         cl.sync();
-        double pre = 0.0;
-        for (int q = 0; q < cpos; q++) pre = pre + *cl.map_shared_rank(s_tot, REV ? C - 1 - q : q);
-        carry = pre + ex;
+        if (tid == 0) {
+            double pre = 0.0;
+            for (int q = 0; q < cpos; q++) pre = pre + *cl.map_shared_rank(W.s_tot, REV ? C - 1 - q : q);
+            *W.s_pre = pre;
+        }
+        __syncthreads();
+        carry = *W.s_pre + ex;
     } else {
-        sa[tid] = y;  // segment end without carry
+        W.sa[tid] = y;
         cl.sync();
+        // carry = sum_q rho^{L (q-1)} y_end(sp - q): terms below 1e-20 relative are dropped
         const int sp = cpos * T + tid;
-        const double aL = pw[L - 1];
+        const int nq = min(W.nterms, sp);
         carry = 0.0;
-        double wgt = 1.0;
-        for (int q = 1; q <= sp && wgt > 1e-20; q++) {
+        for (int q = 1; q <= nq; q++) {
             const int src = sp - q;
             const int r = REV ? C - 1 - src / T : src / T;
-            carry = carry + wgt * cl.map_shared_rank(sa, r)[src % T];
-            wgt = wgt * aL;
+            carry = carry + W.wt[q - 1] * cl.map_shared_rank(W.sa, r)[src % T];
         }
     }
     cl.sync();  // every remote read of sa / s_tot is done before the next pass rewrites them
     for (int s = 0; s < len; s++) {
-        double *p = &xs[(REV ? len - 1 - s : s) * kPsStride + seg];
-        *p = *p + (UNIT ? carry : pw[s] * carry);
+        double *p = &xs[(REV ? len - 1 - s : s) * stride + seg];
+        *p = *p + (UNIT ? carry : W.pw[s] * carry);
     }
     __syncthreads();
 }
 
-__global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads)
+__global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsMaxThreads)
     k_poisson_scan(PoissonFastLaunch P) {
-    extern __shared__ double xs[];  // [L][kPsStride]: element (segment s, offset o) at o * kPsStride + s
-    __shared__ double sa[kPsThreads], sb[32], pw[kPsMaxSeg], s_tot, s_u[3];
+    extern __shared__ double xs[];  // [L][T + 1]: element (segment s, offset o) at o (T + 1) + s
+    __shared__ double sa[kPsMaxThreads], sb[32], pw[kPsMaxSeg], wt[kPsMaxTerms], s_tot, s_pre, s_u[3];
+    __shared__ int s_nterms;
     cg::cluster_group cl = cg::this_cluster();
-    constexpr int T = kPsThreads;
+    const int T = blockDim.x, stride = T + 1;
     const int run = blockIdx.x / kPsCluster;
     const int rank = (int)cl.block_rank();
     RunFields &F = P.fields[run];
@@ -155,19 +170,30 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads)
             const double r = te * (F.charge[g + 1] + F.neut[g + 1]);
             v = r * w;
         }
-        xs[(l % L) * kPsStride + l / L] = v;
+        xs[(l % L) * stride + l / L] = v;
     }
     for (int q = threadIdx.x; q < L; q += T) pw[q] = pow(D.rho, (double)(q + 1));
+    if (threadIdx.x == 0) {
+        const double aL = pow(D.rho, (double)L);
+        double x = 1.0;
+        int q = 0;
+        while (q < kPsMaxTerms && x > 1e-20) {
+            wt[q++] = x;
+            x = x * aL;
+        }
+        s_nterms = q;
+    }
     __syncthreads();
-    scan_pass<false, true>(cl, xs, L, m, g0, 1.0, pw, sa, sb, &s_tot);    // (I - S)^{-1}
-    scan_pass<false, false>(cl, xs, L, m, g0, D.rho, pw, sa, sb, &s_tot);  // (I - rho S)^{-1}
-    scan_pass<true, false>(cl, xs, L, m, g0, D.rho, pw, sa, sb, &s_tot);   // (I - rho S^T)^{-1}
-    scan_pass<true, true>(cl, xs, L, m, g0, 1.0, pw, sa, sb, &s_tot);     // (I - S^T)^{-1}
+    const ScanScratch W{sa, sb, pw, wt, &s_tot, &s_pre, s_nterms};
+    scan_pass<false, true>(cl, xs, L, m, g0, 1.0, W);    // (I - S)^{-1}
+    scan_pass<false, false>(cl, xs, L, m, g0, D.rho, W);  // (I - rho S)^{-1}
+    scan_pass<true, false>(cl, xs, L, m, g0, D.rho, W);   // (I - rho S^T)^{-1}
+    scan_pass<true, true>(cl, xs, L, m, g0, 1.0, W);     // (I - S^T)^{-1}
     cl.sync();  // every chunk final before the Woodbury entries are read across blocks
     if (threadIdx.x < 3) {
         const int g = threadIdx.x == 2 ? m - 1 : threadIdx.x;
         const int r = g / (T * L), l = g - r * T * L;
-        s_u[threadIdx.x] = cl.map_shared_rank(xs, r)[(l % L) * kPsStride + l / L] * D.c_inv;
+        s_u[threadIdx.x] = cl.map_shared_rank(xs, r)[(l % L) * stride + l / L] * D.c_inv;
     }
     __syncthreads();
     double t[3];
@@ -175,7 +201,7 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads)
     for (int l = threadIdx.x; l < T * L; l += T) {
         const int g = g0 + l;
         if (g >= m) break;
-        const double z = xs[(l % L) * kPsStride + l / L] * D.c_inv;
+        const double z = xs[(l % L) * stride + l / L] * D.c_inv;
         F.phi[g + 1] = z - (D.Y[3 * g] * t[0] + D.Y[3 * g + 1] * t[1] + D.Y[3 * g + 2] * t[2]);
     }
     __threadfence();
@@ -194,19 +220,28 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads)
     // E_x on the finest grid follows in k_efield (all blocks of the device)
 }
 
+// Threads per block: segments of about 8 elements (a decaying pass then gathers three
+// carry terms), 32 to kPsMaxThreads threads.
+int scan_threads(int maxn) {
+    const int m = maxn - 1;
+    int t = 32;
+    while (t < kPsMaxThreads && (long long)t * kPsCluster * 8 < m) t *= 2;
+    return t;
+}
+
 }  // namespace
 
 size_t poisson_scan_smem(int maxn) {
-    const int m = maxn - 1;
-    const int L = (m + kPsThreads * kPsCluster - 1) / (kPsThreads * kPsCluster);
-    return (size_t)L * kPsStride * sizeof(double);
+    const int m = maxn - 1, T = scan_threads(maxn);
+    const int L = (m + T * kPsCluster - 1) / (T * kPsCluster);
+    return (size_t)L * (T + 1) * sizeof(double);
 }
 
 void launch_poisson_fast(const PoissonFastLaunch &L) {
     if (L.nruns == 0) return;
     const size_t smem = poisson_scan_smem(L.maxn);
     cudaFuncSetAttribute(k_poisson_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_poisson_scan<<<L.nruns * kPsCluster, kPsThreads, smem, L.stream>>>(L);
+    k_poisson_scan<<<L.nruns * kPsCluster, scan_threads(L.maxn), smem, L.stream>>>(L);
     launch_efield(L.fields, L.fcoef, L.nruns, L.maxn, L.stream);
 }
 

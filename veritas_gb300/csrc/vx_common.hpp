@@ -63,6 +63,8 @@ struct PatchT {
     // FP32 copies of the scalars the FP32 kernels use (no FP64 arithmetic in their
     // loops): p_min / (m c), dp / (m c), kx, kp, 1/dx, 1/dp, q, q^2 / (m c)^2
     float pminf, dpnf, kxf, kpf, dxif, dpif, qf, a2nf;
+    // FP32 moments: final scales of the rho and J column sums (1/fnorm folded in)
+    double msc_rho, msc_j;
     T *f0, *f1, *f2;
     T *gam;                 // gamma at (x-face i, p-face j), i in [-1,nx+1], j in [-1,np+1]
     T *ex, *fx, *ep, *fp;   // face velocities and reconstructed face values
@@ -75,6 +77,7 @@ struct PatchT {
     double *chargeR, *currentR;  // per finest column of this patch (n_x * rtb)
     const double *relc;     // interpolation weights onto the rtb finest sub-cells, 3*rtb
     const double *refc;     // interpolation weights onto the r sub-cells of a coarse cell, 3*r
+    const float *relc32;    // FP32 relc, then the three weights summed over the sub-cells
 };
 
 // Per-run field block on the device (EMSolver state, EMSolver.hpp:9-49).
@@ -89,7 +92,7 @@ struct RunFields {
     double *charge, *J, *neut;  // n
     double *efin;       // E_x at finest cells, n (recomputed after every Poisson solve)
     double *ex0;        // scalar
-    double *asq_cell;   // cell-average A^2 at finest cells (Ay/Az slot 1), n
+    float *acell32;     // FP32 Ay^2 + Az^2 (slot 1) at every cell of the field grid, nf
     float *asq32;       // FP32 copies of asq (n+1) and efin (n) for the FP32 form
     float *efin32;
 };

@@ -62,6 +62,7 @@ struct MomLaunch {
     int ncols;
     int maxnp;            // largest n_p over the patches
     const RunFields *fields;
+    int nruns, maxnf;     // FP32: the per-cell A^2 copy covers every run's field grid
     cudaStream_t stream;
 };
 void launch_moments64(const MomLaunch &M);
@@ -119,9 +120,9 @@ void launch_poisson(const PoissonLaunch &L);
 
 // O(n) Poisson solve by prefix scans, one thread-block cluster per run (poisson_scan64.cu).
 // Y holds the m x 3 Woodbury columns (row-major), K the 3x3 capacitance factor.
-constexpr int kPsThreads = 512, kPsCluster = 8;
-constexpr int kPsMaxSeg = 48;                                           // elements per thread
-constexpr int kPsMaxUnknowns = kPsThreads * kPsCluster * kPsMaxSeg;     // n - 1 <= this
+constexpr int kPsMaxThreads = 512, kPsCluster = 8;
+constexpr int kPsMaxSeg = 48;                                              // elements per thread
+constexpr int kPsMaxUnknowns = kPsMaxThreads * kPsCluster * kPsMaxSeg;     // n - 1 <= this
 struct PoissonFastDev {
     const double *Y;
     double K[9];
