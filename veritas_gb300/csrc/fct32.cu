@@ -21,6 +21,11 @@ namespace vx {
 
 using P32 = PatchT<float>;
 
+// Quotients and square roots of the FP32 kernels use the hardware approximations
+// (__fdividef: within 2 ulp for divisors below 2^126, which every divisor here is; and
+// s * rsqrtf(s) for s >= 1); the precision form's stated error includes them.
+__device__ __forceinline__ float sqrt_ge1(float s) { return s * rsqrtf(s); }
+
 // WENO-type face value (Rectangle.cpp:980-1030) with the regulariser `mm`: the
 // reference's 1e-10 carried into the scaled units of the smoothness indicators, floored
 // at 1e-30 so that it stays a normal FP32 number (it only matters where f vanishes).
@@ -36,13 +41,13 @@ __device__ __forceinline__ float weno32(float f1, float f2, float f3, float f4, 
     float bL = c43 * (AL * AL) + 0.5f * AL * BL + 0.25f * (BL * BL);
     float bR = c43 * (AR * AR) - 0.5f * AR * BR + 0.25f * (BR * BR);
     // oL / (oL + oR) with o = 0.5 / (mm + b)^2, as a ratio that cannot underflow
-    float rr = (mm + bL) / (mm + bR);
-    float wL = 1.0f / (1.0f + rr * rr);
+    float rr = __fdividef(mm + bL, mm + bR);
+    float wL = __fdividef(1.0f, 1.0f + rr * rr);  // rr^2 = inf gives wL = 0, its limit
     float wR = 1.0f - wL;
     float wL0 = wL * (0.75f + wL * (wL - 0.5f));
     float wR0 = wR * (0.75f + wR * (wR - 0.5f));
     float pick = right ? fmaxf(wL0, wR0) : fminf(wL0, wR0);
-    float fwl = pick / (wL0 + wR0);
+    float fwl = __fdividef(pick, wL0 + wR0);  // wL0 + wR0 >= 0.75
     return fwl * fL + (1.0f - fwl) * fR;
 }
 
@@ -64,7 +69,7 @@ __device__ __forceinline__ float qefield32(const P32 &P, const RunFields &F, int
         y = (y < F.n) ? y : (y - F.n);
         t += F.efin32[y];
     }
-    return P.qf * (t / (float)P.rtb);
+    return P.qf * (t * (1.0f / (float)P.rtb));  // rtb is a power of two
 }
 
 #define VX_TILE32                                         \
@@ -237,8 +242,8 @@ __global__ void k32_xflux(const P32 *patches, const TileRef *tiles, int ntiles, 
         float am = 0.0f, fv = 0.0f;
         if (col_ok) {
             const float a = asq32(P, F, i);
-            const float g0 = sqrtf(1.0f + p0 * p0 + a), g1 = sqrtf(1.0f + p1 * p1 + a);
-            am = P.kxf * (P.dpnf * (p1 + p0) / (g1 + g0));
+            const float g0 = sqrt_ge1(1.0f + p0 * p0 + a), g1 = sqrt_ge1(1.0f + p1 * p1 + a);
+            am = P.kxf * __fdividef(P.dpnf * (p1 + p0), g1 + g0);
             const int id = pidx(i, jj, pit);
             fv = weno32(f[id - 2 * pit], f[id - pit], f[id], f[id + pit], am > 0.0f, P.weno_eps);
         }
@@ -260,8 +265,8 @@ __device__ __forceinline__ void pface32(const P32 &P, const RunFields &F, const 
     fv = 0.0f;
     if (!col_ok || i < -1 || i > P.nx) return;
     const float a0 = asq32(P, F, i), a1 = asq32(P, F, i + 1);
-    const float g0 = sqrtf(1.0f + p * p + a0), g1 = sqrtf(1.0f + p * p + a1);
-    am = qefield32(P, F, i) - P.kpf * ((a1 - a0) / (g1 + g0));
+    const float g0 = sqrt_ge1(1.0f + p * p + a0), g1 = sqrt_ge1(1.0f + p * p + a1);
+    am = qefield32(P, F, i) - P.kpf * __fdividef(a1 - a0, g1 + g0);
     const int id = pidx(i, j, P.pitch);
     fv = weno32(f[id - 2], f[id - 1], f[id], f[id + 1], am > 0.0f, P.weno_eps);
 }

@@ -18,9 +18,12 @@ using P32 = PatchT<float>;
 // One warp per moment column (coarse column i, finest sub-column k).  Windows of 29
 // outputs: lane l holds p index j = j0 - 1 + l; l_j needs G of the next lane, so lanes
 // 0..30 have it and lanes 1..29 produce.
-//   G_j = gamma_j + p_j (dimensionless, p in units of m c),
-//   l_j = ln(G_{j+1} / G_j) = log1p(dG / G_j),
-//   dG  = dp (1 + (p_{j+1} + p_j) / (gamma_{j+1} + gamma_j))   (no cancellation),
+//   G_j = gamma_j + p_j = (1 + a) / (gamma_j - p_j)   (dimensionless, p in units of m c;
+//         the second form where p_j < 0, free of cancellation),
+//   dG  = G_{j+1} - G_j = dp (1 + (p_{j+1} + p_j) / (gamma_{j+1} + gamma_j)),
+//   l_j = ln(G_{j+1} / G_j) = 2 atanh(z),  z = dG / (2 G_j + dG)
+//       = 2 z (1 + z^2/3 + z^4/5 + z^6/7)  (Taylor series; for z <= 1/16 the next term
+//         is below 3e-10 relative), ln(1 + u) otherwise,
 //   rho_k += f_j,  J_k += f_j l_j + (1/48)(l_{j+1} - l_{j-1})(f_{j+1} - f_{j-1}).
 constexpr int kMom32Out = 29;
 
@@ -107,16 +110,23 @@ __global__ void k32_moments(MomLaunch M) {
     auto window = [&](int j0, float &vc, float &vj) {
         const int j = j0 - 1 + lane;
         const float p = fmaf(dpn, (float)(j + P.p_pos), pmin);
-        const float g = sqrtf(1.0f + p * p + a);
+        const float g = (1.0f + p * p + a) * rsqrtf(1.0f + p * p + a);
         const float gn = __shfl_down_sync(full, g, 1);
         const float pn = __shfl_down_sync(full, p, 1);
-        const float dG = dpn * (1.0f + (pn + p) / (gn + g));
-        // ln(1 + u) for small u as logf(y) u / (y - 1), y = 1 + u rounded (Goldberg,
-        // "What every computer scientist should know about floating-point arithmetic",
-        // 1991): FP32 throughout, a few ulp
-        const float u = dG / (g + p);
-        const float y1 = 1.0f + u;
-        const float l = (y1 == 1.0f) ? u : logf(y1) * (u / (y1 - 1.0f));  // valid on lanes 0..30
+        const float dG = dpn * (1.0f + __fdividef(pn + p, gn + g));
+        const float G = p >= 0.0f ? g + p : __fdividef(1.0f + a, g - p);
+        const float z = __fdividef(dG, 2.0f * G + dG);
+        float l;  // valid on lanes 0..30
+        if (z <= 0.0625f) {
+            const float z2 = z * z;
+            l = 2.0f * z * fmaf(z2, fmaf(z2, fmaf(z2, 1.0f / 7.0f, 0.2f), 1.0f / 3.0f), 1.0f);
+        } else {
+            // ln(1 + u) as logf(y) u / (y - 1), y = 1 + u rounded (Goldberg, "What every
+            // computer scientist should know about floating-point arithmetic", 1991)
+            const float u = __fdividef(dG, G);
+            const float y1 = 1.0f + u;
+            l = logf(y1) * __fdividef(u, y1 - 1.0f);
+        }
         float V = 0.0f;
         if (j <= P.np) V = rel_value32(P, f, i, j, w, inv_rtb);
         const float lm = __shfl_up_sync(full, l, 1), lp = __shfl_down_sync(full, l, 1);
