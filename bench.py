@@ -411,6 +411,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--poisson", type=int, default=0, choices=[0, 1],
+                    help="Poisson solver of the headline run: 0 the LU's rounding order, 1 the O(n) scan solve")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32],
                     help="precision of the headline workload (64, the plain path, unless profiling the FP32 form)")
     ap.add_argument("--form", default="", choices=["", "config3"],
@@ -442,7 +444,7 @@ def main() -> None:
     ctx = Context(local)
     import dataclasses
 
-    s = SolverManager(ctx, dataclasses.replace(problem_config2(), precision=args.precision))
+    s = SolverManager(ctx, dataclasses.replace(problem_config2(), precision=args.precision, poisson=args.poisson))
     cells = s.cell_count()
     init_path = Path(tempfile.mkdtemp()) / "init.bin"
     if rank == 0 and not args.lite and not (args.no_cpu_baseline and args.no_forms):

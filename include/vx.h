@@ -76,6 +76,11 @@ const char *vx_last_error(void);
 int vx_ctx_create(int device, vx_ctx **out);
 /* Fails (VX_ERR_INVALID) while runs created on the context are still alive. */
 int vx_ctx_destroy(vx_ctx *ctx);
+/* Launch mode (no reference counterpart; both on by default): graphs != 0 replays each
+ * step as one captured CUDA graph, pdl != 0 launches every kernel with programmatic
+ * dependent launch (process-wide).  For debugging and timing; results do not depend on
+ * it. */
+int vx_ctx_set_launch_mode(vx_ctx *ctx, int graphs, int pdl);
 int vx_ctx_sync(vx_ctx *ctx);
 /* Kernels launched by this context so far (graph replays count their nodes). */
 int vx_ctx_kernel_launches(vx_ctx *ctx, uint64_t *out);

@@ -116,3 +116,23 @@ def test_autotuned_tiles_change_nothing(ctx, tmp_path, precision):
     assert _bytes(a, tmp_path / "a.bin") == _bytes(b, tmp_path / "b.bin")
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [64, 32])
+def test_launch_mode_changes_nothing(ctx, tmp_path, precision):
+    """Steps with and without the CUDA graph and programmatic dependent launch give the
+    same bits (every kernel waits for its predecessor before touching memory)."""
+    from veritas_gb300 import Problem, SolverManager
+
+    out = []
+    for graphs, pdl in ((True, True), (False, False), (True, False)):
+        ctx.set_launch_mode(graphs=graphs, pdl=pdl)
+        s = SolverManager(ctx, Problem(nx=512, np=64, Lfinest=2, precision=precision))
+        for _ in range(3):
+            s.Advance(s.CalculateDt())
+        s.save_state(tmp_path / f"s{len(out)}.bin")
+        out.append((tmp_path / f"s{len(out)}.bin").read_bytes())
+        s.close()
+    ctx.set_launch_mode(graphs=True, pdl=True)
+    assert out[0] == out[1] == out[2]

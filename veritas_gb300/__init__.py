@@ -71,6 +71,7 @@ def _load() -> ctypes.CDLL:
         "vx_ctx_create": (ctypes.c_int, [ctypes.c_int, P(vp)]),
         "vx_ctx_destroy": (ctypes.c_int, [vp]),
         "vx_ctx_sync": (ctypes.c_int, [vp]),
+        "vx_ctx_set_launch_mode": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
         "vx_ctx_kernel_launches": (ctypes.c_int, [vp, P(ctypes.c_uint64)]),
         "vx_run_create": (ctypes.c_int, [vp, P(_Problem), P(vp)]),
         "vx_run_destroy": (ctypes.c_int, [vp]),
@@ -193,6 +194,10 @@ class Context:
 
     def sync(self) -> None:
         _check(_lib.vx_ctx_sync(self._h))
+
+    def set_launch_mode(self, graphs: bool = True, pdl: bool = True) -> None:
+        """CUDA graph per step and programmatic dependent launch (both on by default)."""
+        _check(_lib.vx_ctx_set_launch_mode(self._h, int(graphs), int(pdl)))
 
     def kernel_launches(self) -> int:
         v = ctypes.c_uint64()

@@ -69,6 +69,7 @@ __device__ T coarse_interp(const PatchT<T> &C, const T *f, int ic, int jc, int s
 
 template <class T>
 __global__ void k_ghost(const PatchT<T> *patches, const GhostOp *ops, int n, int slot) {
+    VX_PDL_WAIT();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const GhostOp op = ops[k];
@@ -99,6 +100,7 @@ __global__ void k_ghost(const PatchT<T> *patches, const GhostOp *ops, int n, int
 // donor-cell flux the way RGKGetFluxXL/PL do, (dx_inv * f) * a (Rectangle.cpp:1216-1253).
 template <class T>
 __global__ void k_iface(const PatchT<T> *patches, const IfaceOp *ops, int n, int step) {
+    VX_PDL_WAIT();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const IfaceOp op = ops[k];
@@ -152,6 +154,7 @@ __global__ void k_iface(const PatchT<T> *patches, const IfaceOp *ops, int n, int
 // Limiter coefficient exchange (Rectangle.cpp:1625-1917).
 template <class T>
 __global__ void k_csync(const PatchT<T> *patches, const CSyncOp *ops, int n) {
+    VX_PDL_WAIT();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const CSyncOp op = ops[k];
@@ -200,6 +203,7 @@ __global__ void k_csync(const PatchT<T> *patches, const CSyncOp *ops, int n) {
 // on f slot 1; one flag byte per interior cell, zero outside the tested range.
 template <class T>
 __global__ void k_flags(const PatchT<T> *patches, const FlagPatch *fps, uint8_t *out) {
+    VX_PDL_WAIT();
     const FlagPatch fp = fps[blockIdx.y];
     const PatchT<T> &P = patches[fp.patch];
     const int pit = P.pitch;
@@ -225,6 +229,7 @@ __global__ void k_flags(const PatchT<T> *patches, const FlagPatch *fps, uint8_t 
 // from slot 1 of the source.
 template <class T>
 __global__ void k_xfer(const PatchT<T> *patches, const XferOp *ops, uint8_t *mask) {
+    VX_PDL_WAIT();
     const XferOp op = ops[blockIdx.y];
     const PatchT<T> &D = patches[op.dst];
     const PatchT<T> &S = patches[op.src];
@@ -260,32 +265,32 @@ __global__ void k_xfer(const PatchT<T> *patches, const XferOp *ops, uint8_t *mas
 
 void launch_flags(const void *patches, const FlagPatch *fp, int n, uint8_t *out, int prec, cudaStream_t s) {
     if (n <= 0) return;
-    if (prec == kF32) k_flags<<<dim3(64, n), 256, 0, s>>>((const PatchT<float> *)patches, fp, out);
-    else k_flags<<<dim3(64, n), 256, 0, s>>>((const PatchT<double> *)patches, fp, out);
+    if (prec == kF32) vx_launch(k_flags<float>, dim3(64, n), 256, 0, s, (const PatchT<float> *)patches, fp, out);
+    else vx_launch(k_flags<double>, dim3(64, n), 256, 0, s, (const PatchT<double> *)patches, fp, out);
 }
 
 void launch_xfer(const void *patches, const XferOp *ops, int n, uint8_t *mask, int prec, cudaStream_t s) {
     if (n <= 0) return;
-    if (prec == kF32) k_xfer<<<dim3(16, n), 256, 0, s>>>((const PatchT<float> *)patches, ops, mask);
-    else k_xfer<<<dim3(16, n), 256, 0, s>>>((const PatchT<double> *)patches, ops, mask);
+    if (prec == kF32) vx_launch(k_xfer<float>, dim3(16, n), 256, 0, s, (const PatchT<float> *)patches, ops, mask);
+    else vx_launch(k_xfer<double>, dim3(16, n), 256, 0, s, (const PatchT<double> *)patches, ops, mask);
 }
 
 void launch_ghost(const void *patches, const GhostOp *ops, int n, int slot, int prec, cudaStream_t s) {
     if (n <= 0) return;
-    if (prec == kF32) k_ghost<<<(n + 127) / 128, 128, 0, s>>>((const PatchT<float> *)patches, ops, n, slot);
-    else k_ghost<<<(n + 127) / 128, 128, 0, s>>>((const PatchT<double> *)patches, ops, n, slot);
+    if (prec == kF32) vx_launch(k_ghost<float>, (n + 127) / 128, 128, 0, s, (const PatchT<float> *)patches, ops, n, slot);
+    else vx_launch(k_ghost<double>, (n + 127) / 128, 128, 0, s, (const PatchT<double> *)patches, ops, n, slot);
 }
 
 void launch_iface(const void *patches, const IfaceOp *ops, int n, int step, int prec, cudaStream_t s) {
     if (n <= 0) return;
-    if (prec == kF32) k_iface<<<(n + 127) / 128, 128, 0, s>>>((const PatchT<float> *)patches, ops, n, step);
-    else k_iface<<<(n + 127) / 128, 128, 0, s>>>((const PatchT<double> *)patches, ops, n, step);
+    if (prec == kF32) vx_launch(k_iface<float>, (n + 127) / 128, 128, 0, s, (const PatchT<float> *)patches, ops, n, step);
+    else vx_launch(k_iface<double>, (n + 127) / 128, 128, 0, s, (const PatchT<double> *)patches, ops, n, step);
 }
 
 void launch_csync(const void *patches, const CSyncOp *ops, int n, int prec, cudaStream_t s) {
     if (n <= 0) return;
-    if (prec == kF32) k_csync<<<(n + 127) / 128, 128, 0, s>>>((const PatchT<float> *)patches, ops, n);
-    else k_csync<<<(n + 127) / 128, 128, 0, s>>>((const PatchT<double> *)patches, ops, n);
+    if (prec == kF32) vx_launch(k_csync<float>, (n + 127) / 128, 128, 0, s, (const PatchT<float> *)patches, ops, n);
+    else vx_launch(k_csync<double>, (n + 127) / 128, 128, 0, s, (const PatchT<double> *)patches, ops, n);
 }
 
 }  // namespace vx

@@ -156,6 +156,11 @@ int vx_ctx_sync(vx_ctx *ctx) {
     return guard([&] { ctx->eng->sync(); });
 }
 
+int vx_ctx_set_launch_mode(vx_ctx *ctx, int graphs, int pdl) {
+    if (!ctx) return VX_ERR_INVALID;
+    return guard([&] { ctx->eng->set_launch_mode(graphs != 0, pdl != 0); });
+}
+
 int vx_ctx_kernel_launches(vx_ctx *ctx, uint64_t *out) {
     if (!ctx || !out) return VX_ERR_INVALID;
     *out = ctx->eng->kernel_launches;

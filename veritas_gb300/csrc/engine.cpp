@@ -7,6 +7,8 @@
 
 namespace vx {
 
+bool g_launch_pdl = true;
+
 void cuda_check(cudaError_t e, const char *what) {
     if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -612,6 +614,17 @@ void Engine::forget(Run *r) {
         if (std::find(it->first.begin(), it->first.end(), r) != it->first.end()) it = sets_.erase(it);
         else ++it;
     }
+}
+
+void Engine::set_launch_mode(bool graphs, bool pdl) {
+    sync();
+    use_graphs = graphs;
+    g_launch_pdl = pdl;
+    for (auto &kv : sets_)
+        if (kv.second->graph) {
+            cudaGraphExecDestroy(kv.second->graph);
+            kv.second->graph = nullptr;
+        }
 }
 
 LaunchSet &Engine::get_set(const std::vector<Run *> &set) {

@@ -231,6 +231,9 @@ public:
     // Times the FCT sub-step kernels of the set for each candidate tile shape and keeps
     // the fastest for this precision (autotune.cpp).  Leaves the solution unchanged.
     std::pair<int, int> autotune(const std::vector<Run *> &set, int reps);
+    // CUDA graph per step and programmatic dependent launch on or off; drops the
+    // captured graphs (they hold the old launch attributes).
+    void set_launch_mode(bool graphs, bool pdl);
     int tile_pref[2][2] = {{32, 8}, {32, 8}};  // [precision 64, 32] -> (tile_j, tile_i)
 
 private:

@@ -83,6 +83,7 @@ __device__ __forceinline__ float qefield32(const P32 &P, const RunFields &F, int
 
 // Lorentz factor at (x-face i, p-face j), i in [-1,nx+1], j in [-1,np+1].
 __global__ void k32_gamma(const P32 *patches, const TileRef *tiles, const RunFields *fields) {
+    VX_PDL_WAIT();
     VX_TILE32
     if (i < -1 || j < -1) return;
     const RunFields &F = fields[P.run];
@@ -92,6 +93,7 @@ __global__ void k32_gamma(const P32 *patches, const TileRef *tiles, const RunFie
 }
 
 __global__ void k32_faces(const P32 *patches, const TileRef *tiles, const RunFields *fields, int use_f0, int part) {
+    VX_PDL_WAIT();
     VX_TILE32
     const float *f = use_f0 ? P.f0 : P.f1;
     const float *g = P.gam;
@@ -115,6 +117,7 @@ __global__ void k32_faces(const P32 *patches, const TileRef *tiles, const RunFie
 }
 
 __global__ void k32_flux(const P32 *patches, const TileRef *tiles, int step, int use_f0, int part) {
+    VX_PDL_WAIT();
     VX_TILE32
     const float *f = use_f0 ? P.f0 : P.f1;
     const float w3 = 1.0f / 48.0f;
@@ -138,6 +141,7 @@ __device__ __forceinline__ bool active32(const P32 &P, int i, int j) {
 }
 
 __global__ void k32_ds_f2(const P32 *patches, const TileRef *tiles, const float *params, int s) {
+    VX_PDL_WAIT();
     VX_TILE32
     if (i < -2 || j < -2) return;
     const float *a = params + param_base(P.run, s);
@@ -164,6 +168,7 @@ __global__ void k32_ds_f2(const P32 *patches, const TileRef *tiles, const float 
 }
 
 __global__ void k32_limR(const P32 *patches, const TileRef *tiles) {
+    VX_PDL_WAIT();
     VX_TILE32
     if (i < -1 || i > P.nx || j < -1 || j > P.np) return;
     const float *DX = P.FxDS, *DP = P.FpDS, *f0 = P.f0, *f2 = P.f2;
@@ -182,6 +187,7 @@ __global__ void k32_limR(const P32 *patches, const TileRef *tiles) {
 }
 
 __global__ void k32_limC(const P32 *patches, const TileRef *tiles) {
+    VX_PDL_WAIT();
     VX_TILE32
     if (i < -2 || j < -2) return;
     float cx = 1.0f, cp = 1.0f;
@@ -195,6 +201,7 @@ __global__ void k32_limC(const P32 *patches, const TileRef *tiles) {
 }
 
 __global__ void k32_update(const P32 *patches, const TileRef *tiles) {
+    VX_PDL_WAIT();
     VX_TILE32
     if (i < 0 || i >= P.nx || j < 0 || j >= P.np) return;
     float v = P.f2[id];
@@ -206,6 +213,7 @@ __global__ void k32_update(const P32 *patches, const TileRef *tiles) {
 }
 
 __global__ void k32_copy10(const P32 *patches, const TileRef *tiles) {
+    VX_PDL_WAIT();
     VX_TILE32
     if (i < -2 || j < -2) return;
     P.f0[id] = P.f1[id];
@@ -223,6 +231,7 @@ __global__ void k32_copy10(const P32 *patches, const TileRef *tiles) {
 // face values of j0-1 .. j0+30) over kStripRows rows; rows are independent in x.
 __global__ void k32_xflux(const P32 *patches, const TileRef *tiles, int ntiles, const RunFields *fields, int step,
                           int use_f0) {
+    VX_PDL_WAIT();
     const int wt = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (wt >= ntiles) return;
     const int lane = threadIdx.x & 31;
@@ -273,6 +282,7 @@ __device__ __forceinline__ void pface32(const P32 &P, const RunFields &F, const 
 
 __global__ void k32_pflux(const P32 *patches, const TileRef *tiles, int ntiles, const RunFields *fields, int step,
                           int use_f0) {
+    VX_PDL_WAIT();
     const int wt = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (wt >= ntiles) return;
     const int lane = threadIdx.x & 31;
@@ -310,34 +320,34 @@ void launch_fct32_substep(const FctLaunch &L, int sub) {
     if (L.ntiles == 0) return;
     switch (sub) {
         case kSubGamma:
-            k32_gamma<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.fields);
+            vx_launch(k32_gamma, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.fields);
             break;
         case kSubFaces:
-            k32_faces<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.fields, L.use_f0, L.part ? L.part : 3);
+            vx_launch(k32_faces, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.fields, L.use_f0, L.part ? L.part : 3);
             break;
         case kSubFlux:
-            k32_flux<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.step, L.use_f0, L.part ? L.part : 3);
+            vx_launch(k32_flux, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.step, L.use_f0, L.part ? L.part : 3);
             break;
         case kSubDsF2:
-            k32_ds_f2<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.params32, L.step);
+            vx_launch(k32_ds_f2, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.params32, L.step);
             break;
         case kSubLimR:
-            k32_limR<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles);
+            vx_launch(k32_limR, L.ntiles, blk, 0, L.stream, pp, L.tiles);
             break;
         case kSubLimC:
-            k32_limC<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles);
+            vx_launch(k32_limC, L.ntiles, blk, 0, L.stream, pp, L.tiles);
             break;
         case kSubUpdate:
-            k32_update<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles);
+            vx_launch(k32_update, L.ntiles, blk, 0, L.stream, pp, L.tiles);
             break;
         case kSubCopy10:
-            k32_copy10<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles);
+            vx_launch(k32_copy10, L.ntiles, blk, 0, L.stream, pp, L.tiles);
             break;
         case kSubXFlux:
-            if (L.nxtiles) k32_xflux<<<(L.nxtiles + 3) / 4, 128, 0, L.stream>>>(pp, L.xtiles, L.nxtiles, L.fields, L.step, L.use_f0);
+            if (L.nxtiles) vx_launch(k32_xflux, (L.nxtiles + 3) / 4, 128, 0, L.stream, pp, L.xtiles, L.nxtiles, L.fields, L.step, L.use_f0);
             break;
         case kSubPFlux:
-            if (L.nptiles) k32_pflux<<<(L.nptiles + 3) / 4, 128, 0, L.stream>>>(pp, L.ptiles, L.nptiles, L.fields, L.step, L.use_f0);
+            if (L.nptiles) vx_launch(k32_pflux, (L.nptiles + 3) / 4, 128, 0, L.stream, pp, L.ptiles, L.nptiles, L.fields, L.step, L.use_f0);
             break;
     }
 }

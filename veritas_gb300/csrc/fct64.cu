@@ -81,6 +81,7 @@ __device__ __forceinline__ double a_sq_face(const P64 &P, const RunFields &F, in
 // Rectangle::Gamma (Rectangle.hpp:181) with A^2 at the finest face under x-face i
 // (EMSolver::GetASquared, EMSolver.cpp:133) and p_j = Momentum(j) (Rectangle.hpp:86).
 __global__ void k64_gamma(const P64 *patches, const TileRef *tiles, const RunFields *fields) {
+    VX_PDL_WAIT();
     VX_TILE_PROLOGUE
     if (i < -1 || j < -1) return;
     const RunFields &F = fields[P.run];
@@ -91,6 +92,7 @@ __global__ void k64_gamma(const P64 *patches, const TileRef *tiles, const RunFie
 
 // Face velocities and reconstructed face values (Rectangle.cpp:1278-1312).
 __global__ void k64_faces(const P64 *patches, const TileRef *tiles, const RunFields *fields, int use_f0, int part) {
+    VX_PDL_WAIT();
     VX_TILE_PROLOGUE
     const double *f = use_f0 ? P.f0 : P.f1;
     const double *g = P.gam;
@@ -112,6 +114,7 @@ __global__ void k64_faces(const P64 *patches, const TileRef *tiles, const RunFie
 // (Rectangle.cpp:1313-1394).  Coarse faces on a coarse/fine interface are skipped here
 // and written by the interface kernel.
 __global__ void k64_flux(const P64 *patches, const TileRef *tiles, int step, int use_f0, int part) {
+    VX_PDL_WAIT();
     VX_TILE_PROLOGUE
     const double *f = use_f0 ? P.f0 : P.f1;
     const double w3 = 1 / 48.0;
@@ -137,6 +140,7 @@ __device__ __forceinline__ bool active_face(const P64 &P, int i, int j) {
 // low-order solution f2 = f0 + div(LS) on the interior in the reference's accumulation
 // order (Rectangle.cpp:1518-1534).  RK coefficients arrive pre-multiplied by dt.
 __global__ void k64_ds_f2(const P64 *patches, const TileRef *tiles, const double *params, int s) {
+    VX_PDL_WAIT();
     VX_TILE_PROLOGUE
     if (i < -2 || j < -2) return;
     const double *a = params + param_base(P.run, s);
@@ -165,6 +169,7 @@ __global__ void k64_ds_f2(const P64 *patches, const TileRef *tiles, const double
 
 // Zalesak R+/R- on i in [-1,nx], j in [-1,np] (Rectangle.cpp:1536-1579).
 __global__ void k64_limR(const P64 *patches, const TileRef *tiles) {
+    VX_PDL_WAIT();
     VX_TILE_PROLOGUE
     if (i < -1 || i > P.nx || j < -1 || j > P.np) return;
     const double *DX = P.FxDS, *DP = P.FpDS, *f0 = P.f0, *f2 = P.f2;
@@ -192,6 +197,7 @@ __global__ void k64_limR(const P64 *patches, const TileRef *tiles) {
 
 // Limiter coefficients on interior faces, 1 elsewhere (Rectangle.cpp:1581-1594).
 __global__ void k64_limC(const P64 *patches, const TileRef *tiles) {
+    VX_PDL_WAIT();
     VX_TILE_PROLOGUE
     if (i < -2 || j < -2) return;
     double cx = 1.0, cp = 1.0;
@@ -206,6 +212,7 @@ __global__ void k64_limC(const P64 *patches, const TileRef *tiles) {
 
 // Antidiffusive update f1 = f2 + div(C * DS) (Rectangle.cpp:1595-1612).
 __global__ void k64_update(const P64 *patches, const TileRef *tiles) {
+    VX_PDL_WAIT();
     VX_TILE_PROLOGUE
     if (i < 0 || i >= P.nx || j < 0 || j >= P.np) return;
     double v = P.f2[id];
@@ -218,6 +225,7 @@ __global__ void k64_update(const P64 *patches, const TileRef *tiles) {
 
 // Last stage: f0 = f1 over the padded block (Rectangle.cpp:1614-1621).
 __global__ void k64_copy10(const P64 *patches, const TileRef *tiles) {
+    VX_PDL_WAIT();
     VX_TILE_PROLOGUE
     if (i < -2 || j < -2) return;
     P.f0[id] = P.f1[id];
@@ -230,28 +238,28 @@ void launch_fct64_substep(const FctLaunch &L, int sub) {
     if (L.ntiles == 0) return;
     switch (sub) {
         case kSubGamma:
-            k64_gamma<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.fields);
+            vx_launch(k64_gamma, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.fields);
             break;
         case kSubFaces:
-            k64_faces<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.fields, L.use_f0, L.part ? L.part : 3);
+            vx_launch(k64_faces, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.fields, L.use_f0, L.part ? L.part : 3);
             break;
         case kSubFlux:
-            k64_flux<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.step, L.use_f0, L.part ? L.part : 3);
+            vx_launch(k64_flux, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.step, L.use_f0, L.part ? L.part : 3);
             break;
         case kSubDsF2:
-            k64_ds_f2<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles, L.params, L.step);
+            vx_launch(k64_ds_f2, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.params, L.step);
             break;
         case kSubLimR:
-            k64_limR<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles);
+            vx_launch(k64_limR, L.ntiles, blk, 0, L.stream, pp, L.tiles);
             break;
         case kSubLimC:
-            k64_limC<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles);
+            vx_launch(k64_limC, L.ntiles, blk, 0, L.stream, pp, L.tiles);
             break;
         case kSubUpdate:
-            k64_update<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles);
+            vx_launch(k64_update, L.ntiles, blk, 0, L.stream, pp, L.tiles);
             break;
         case kSubCopy10:
-            k64_copy10<<<L.ntiles, blk, 0, L.stream>>>(pp, L.tiles);
+            vx_launch(k64_copy10, L.ntiles, blk, 0, L.stream, pp, L.tiles);
             break;
     }
 }

@@ -73,6 +73,7 @@ __device__ __forceinline__ F2 f2_warp_sum(F2 v) {
 // per-cell copy, the weights and the final scales from the patch descriptor; one lane
 // converts the two reduced pairs to FP64.
 __global__ void k32_moments(MomLaunch M) {
+    VX_PDL_WAIT();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= M.ncols) return;
@@ -154,6 +155,7 @@ __global__ void k32_moments(MomLaunch M) {
 
 // FP32 copy of Ay^2 + Az^2 (slot 1) over every run's field grid, read by k32_moments.
 __global__ void k_acell32(const RunFields *fields, int nruns) {
+    VX_PDL_WAIT();
     const int run = blockIdx.y;
     if (run >= nruns) return;
     const RunFields &F = fields[run];
@@ -165,13 +167,14 @@ __global__ void k_acell32(const RunFields *fields, int nruns) {
 
 void launch_moments32(const MomLaunch &M) {
     if (M.ncols == 0) return;
-    k_acell32<<<dim3((M.maxnf + 255) / 256, M.nruns), 256, 0, M.stream>>>(M.fields, M.nruns);
+    vx_launch(k_acell32, dim3((M.maxnf + 255) / 256, M.nruns), 256, 0, M.stream, M.fields, M.nruns);
     const int threads = 256;
     const int blocks = (M.ncols * 32 + threads - 1) / threads;
-    k32_moments<<<blocks, threads, 0, M.stream>>>(M);
+    vx_launch(k32_moments, blocks, threads, 0, M.stream, M);
 }
 
 __global__ void k_fields_to_f32(RunFields *fields, int nruns, int which) {
+    VX_PDL_WAIT();
     const int run = blockIdx.y;
     if (run >= nruns) return;
     RunFields &F = fields[run];
@@ -183,7 +186,7 @@ __global__ void k_fields_to_f32(RunFields *fields, int nruns, int which) {
 void launch_fields_to_f32(RunFields *fields, int nruns, int maxn, int which, cudaStream_t s) {
     if (nruns == 0) return;
     dim3 g((maxn + 1 + 255) / 256, nruns);
-    k_fields_to_f32<<<g, 256, 0, s>>>(fields, nruns, which);
+    vx_launch(k_fields_to_f32, g, 256, 0, s, fields, nruns, which);
 }
 
 }  // namespace vx

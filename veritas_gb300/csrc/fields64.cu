@@ -62,6 +62,7 @@ __device__ __forceinline__ double cell_asq(const RunFields &F, int x) {
 constexpr int kMomOut = 29;  // outputs per window: j0 .. j0+28
 
 __global__ void k64_moments(MomLaunch M) {
+    VX_PDL_WAIT();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= M.ncols) return;
@@ -119,7 +120,7 @@ void launch_moments64(const MomLaunch &M) {
     if (M.ncols == 0) return;
     const int threads = 256;
     const int blocks = (M.ncols * 32 + threads - 1) / threads;
-    k64_moments<<<blocks, threads, 0, M.stream>>>(M);
+    vx_launch(k64_moments, blocks, threads, 0, M.stream, M);
 }
 
 // ---------------------------------------------------------------- assembly
@@ -128,6 +129,7 @@ void launch_moments64(const MomLaunch &M) {
 // charges_s[x] = 0 + level sums finest->coarsest; J sums species then levels;
 // charge[x] = 0 + species sums.
 __global__ void k_assemble(AsmLaunch A) {
+    VX_PDL_WAIT();
     const int run = blockIdx.y;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (run >= A.nruns) return;
@@ -161,7 +163,7 @@ __global__ void k_assemble(AsmLaunch A) {
 
 void launch_assemble(const AsmLaunch &A) {
     dim3 g((A.maxn + 255) / 256, A.nruns);
-    k_assemble<<<g, 256, 0, A.stream>>>(A);
+    vx_launch(k_assemble, g, 256, 0, A.stream, A);
 }
 
 // ---------------------------------------------------------------- Poisson
@@ -451,6 +453,7 @@ __device__ void pois_bwd_fast(PoisBandChunk &B, int r0, int cnt, double *x, doub
 constexpr int kPoisSmemMaxN = 16384;  // solution vector kept in shared memory up to this n
 
 __global__ void k_poisson(PoissonLaunch L) {
+    VX_PDL_WAIT();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PoisBandChunk *buf = (PoisBandChunk *)smem_raw;  // two chunk buffers, then the solution vector
     __shared__ int s_bad;
@@ -586,12 +589,13 @@ void launch_poisson(const PoissonLaunch &L) {
     P.x_in_smem = (L.maxn <= kPoisSmemMaxN && base + 8 * L.maxn <= max_smem) ? 1 : 0;
     const int smem = base + (P.x_in_smem ? 8 * L.maxn : 0);
     cudaFuncSetAttribute(k_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    k_poisson<<<L.nruns, 512, smem, L.stream>>>(P);
+    vx_launch(k_poisson, L.nruns, 512, smem, L.stream, P);
 }
 
 // E_x on the finest grid from phi and Ex0 (EMSolver::GetEfield), for states loaded from
 // outside the step.
 __global__ void k_efield(RunFields *fields, const double *fcoef, int nruns) {
+    VX_PDL_WAIT();
     const int run = blockIdx.y;
     if (run >= nruns) return;
     RunFields &F = fields[run];
@@ -602,12 +606,13 @@ __global__ void k_efield(RunFields *fields, const double *fcoef, int nruns) {
 
 void launch_efield(RunFields *fields, const double *fcoef, int nruns, int maxn, cudaStream_t s) {
     dim3 g((maxn + 255) / 256, nruns);
-    k_efield<<<g, 256, 0, s>>>(fields, fcoef, nruns);
+    vx_launch(k_efield, g, 256, 0, s, fields, fcoef, nruns);
 }
 
 // ---------------------------------------------------------------- Maxwell
 // Right-hand side into slot step+2 from slot 1 (EMSolver.cpp:479-553).
 __global__ void k_mx_rhs(MaxwellLaunch L) {
+    VX_PDL_WAIT();
     const int run = blockIdx.y;
     if (run >= L.nruns) return;
     RunFields &F = L.fields[run];
@@ -671,6 +676,7 @@ __device__ __forceinline__ void mx_combine(double *X, int nf, int i, int step, c
 }
 
 __global__ void k_mx_update(MaxwellLaunch L) {
+    VX_PDL_WAIT();
     const int run = blockIdx.y;
     if (run >= L.nruns) return;
     RunFields &F = L.fields[run];
@@ -706,6 +712,7 @@ __device__ __forceinline__ double face_a(double f1, double f2, double f3, double
 }
 
 __global__ void k_mx_asq(MaxwellLaunch L) {
+    VX_PDL_WAIT();
     const int run = blockIdx.y;
     if (run >= L.nruns) return;
     RunFields &F = L.fields[run];
@@ -719,15 +726,16 @@ __global__ void k_mx_asq(MaxwellLaunch L) {
 
 void launch_maxwell(const MaxwellLaunch &L) {
     dim3 g((L.maxnf + 255) / 256, L.nruns);
-    k_mx_rhs<<<g, 256, 0, L.stream>>>(L);
-    k_mx_update<<<g, 256, 0, L.stream>>>(L);
-    k_mx_asq<<<g, 256, 0, L.stream>>>(L);
+    vx_launch(k_mx_rhs, g, 256, 0, L.stream, L);
+    vx_launch(k_mx_update, g, 256, 0, L.stream, L);
+    vx_launch(k_mx_asq, g, 256, 0, L.stream, L);
 }
 
 // ---------------------------------------------------------------- CFL
 // The maximum runs over non-negative doubles, so it is taken on their bit patterns:
 // each block reduces its slice and folds it into out[run] with an integer atomicMax.
 __global__ void k_cfl(CflLaunch L) {
+    VX_PDL_WAIT();
     const int run = blockIdx.y;
     const RunFields &F = L.fields[run];
     const int ns = L.run_ns[run];
@@ -763,16 +771,17 @@ __global__ void k_cfl(CflLaunch L) {
 void launch_cfl(const CflLaunch &L) {
     cudaMemsetAsync(L.out, 0, (size_t)L.nruns * sizeof(double), L.stream);
     dim3 g(std::min(32, std::max(1, (L.maxn + 255) / 256)), L.nruns);
-    k_cfl<<<g, 256, 0, L.stream>>>(L);
+    vx_launch(k_cfl, g, 256, 0, L.stream, L);
 }
 
 __global__ void k_negate(double *dst, const double *src, int n) {
+    VX_PDL_WAIT();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dst[i] = -src[i];
 }
 
 void launch_negate(double *dst, const double *src, int n, cudaStream_t s) {
-    k_negate<<<(n + 255) / 256, 256, 0, s>>>(dst, src, n);
+    vx_launch(k_negate, (n + 255) / 256, 256, 0, s, dst, src, n);
 }
 
 }  // namespace vx
@@ -781,6 +790,7 @@ namespace vx {
 // Eight independent fused multiply-add chains per thread (register resident).  The
 // result is stored so the chains are not eliminated.
 __global__ void k_fp64_peak(double *out, int iters) {
+    VX_PDL_WAIT();
     double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
     double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
     const double b = 0.999999, c = 1e-7;
@@ -798,6 +808,6 @@ __global__ void k_fp64_peak(double *out, int iters) {
 }
 
 void launch_fp64_peak(double *out, int blocks, int threads, int iters, cudaStream_t s) {
-    k_fp64_peak<<<blocks, threads, 0, s>>>(out, iters);
+    vx_launch(k_fp64_peak, blocks, threads, 0, s, out, iters);
 }
 }  // namespace vx

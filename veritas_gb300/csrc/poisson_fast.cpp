@@ -1,4 +1,4 @@
-// Host set-up of the scan-based Poisson solve (the device part, poisson_scan64.cu,
+// Host set-up of the scan-based Poisson solve (the device part, poisson_scan.cu,
 // documents the algorithm): the Woodbury columns
 // Y = (1/c) G^{-T} G^{-1} [e_0 e_1 e_{m-1}] and the 3x3 factor K = (I + C U^T Y)^{-1} C,
 // where C holds the top-left correction of T - c G G^T and the corner coupling of B.

@@ -23,11 +23,10 @@
 // segments (three for L >= 8, which the block size is chosen for).  The cluster barriers
 // are hardware barriers of co-scheduled blocks.
 //
-// FP64 throughout (compiled with --fmad=false like the other FP64 files, so the
-// right-hand side and E_x round as the reference's do).  The result is not the LU's
-// rounding: against an extended-precision solve its error is about 1e-13 relative at
-// n = 8192, where the dense LU's own is about 4e-11 (it grows with the condition number,
-// roughly n^2).
+// FP64 throughout, with fused multiply-adds (E_x itself comes from k_efield, which keeps
+// the reference's rounding).  The result is not the LU's rounding order; both have the
+// error the discrete system's conditioning (~n^2) allows, about 1e-11 relative at
+// n = 2048 and 1e-9 at n = 8192 against the exact solution.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -149,6 +148,7 @@ __device__ void scan_pass(cg::cluster_group &cl, double *xs, int L, int m, int g
 
 __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsMaxThreads)
     k_poisson_scan(PoissonFastLaunch P) {
+    VX_PDL_WAIT();
     extern __shared__ double xs[];  // [L][T + 1]: element (segment s, offset o) at o (T + 1) + s
     __shared__ double sa[kPsMaxThreads], sb[32], pw[kPsMaxSeg], wt[kPsMaxTerms], s_tot, s_pre, s_u[3];
     __shared__ int s_nterms;
@@ -172,10 +172,14 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsMaxThrea
         }
         xs[(l % L) * stride + l / L] = v;
     }
-    for (int q = threadIdx.x; q < L; q += T) pw[q] = pow(D.rho, (double)(q + 1));
-    if (threadIdx.x == 0) {
-        const double aL = pow(D.rho, (double)L);
-        double x = 1.0;
+    if (threadIdx.x == 0) {  // powers by repeated products (a library pow is a long FP64 chain here)
+        double x = D.rho;
+        for (int q = 0; q < L; q++) {
+            pw[q] = x;
+            x = x * D.rho;
+        }
+        const double aL = pw[L - 1];
+        x = 1.0;
         int q = 0;
         while (q < kPsMaxTerms && x > 1e-20) {
             wt[q++] = x;
@@ -241,7 +245,7 @@ void launch_poisson_fast(const PoissonFastLaunch &L) {
     if (L.nruns == 0) return;
     const size_t smem = poisson_scan_smem(L.maxn);
     cudaFuncSetAttribute(k_poisson_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_poisson_scan<<<L.nruns * kPsCluster, scan_threads(L.maxn), smem, L.stream>>>(L);
+    vx_launch(k_poisson_scan, L.nruns * kPsCluster, scan_threads(L.maxn), smem, L.stream, L);
     launch_efield(L.fields, L.fcoef, L.nruns, L.maxn, L.stream);
 }
 

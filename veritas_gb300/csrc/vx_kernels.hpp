@@ -1,9 +1,36 @@
 // Kernel launch interfaces shared by the CUDA translation units and the host runtime.
 #pragma once
 #include <cuda_runtime.h>
+
+#include <utility>
+
 #include "vx_common.hpp"
 
 namespace vx {
+
+// Programmatic dependent launch.  Every kernel is launched with programmatic stream
+// serialisation, so the next kernel on a stream is scheduled while the current one
+// drains (the launch latency between the many short kernels of a stage overlaps the
+// previous kernel's tail instead of following it).  Correctness rests on every kernel
+// beginning with VX_PDL_WAIT: griddepcontrol.wait returns once the preceding grid has
+// completed and its memory operations are visible (and at once for a kernel launched
+// without the attribute), before the kernel reads or writes anything.
+#define VX_PDL_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+extern bool g_launch_pdl;  // cleared by vx_ctx_set_launch_mode (debugging, timing)
+template <typename... KP, typename... A>
+inline void vx_launch(void (*kernel)(KP...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream, A &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = g_launch_pdl ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);  // errors surface through cudaGetLastError
+}
 
 // One 32(p) x 8(x) tile of a patch's padded block; (i0, j0) is its lower corner in
 // reference indices (>= -2).
@@ -118,7 +145,7 @@ struct PoissonLaunch {
 };
 void launch_poisson(const PoissonLaunch &L);
 
-// O(n) Poisson solve by prefix scans, one thread-block cluster per run (poisson_scan64.cu).
+// O(n) Poisson solve by prefix scans, one thread-block cluster per run (poisson_scan.cu).
 // Y holds the m x 3 Woodbury columns (row-major), K the 3x3 capacitance factor.
 constexpr int kPsMaxThreads = 512, kPsCluster = 8;
 constexpr int kPsMaxSeg = 48;                                              // elements per thread
