@@ -8,12 +8,16 @@
 // C — their outputs are recomputed before being read in the next step) are timed with CUDA
 // events on the engine's stream; the fastest shape is kept for the set and becomes the
 // default for new sets of the same precision.  The tile shape changes no arithmetic.
+#include <array>
+
 #include "engine.hpp"
 
 namespace vx {
 
 std::pair<int, int> Engine::autotune(const std::vector<Run *> &set, int reps) {
-    static const int kShapes[][2] = {{32, 4}, {32, 8}, {32, 16}, {64, 4}, {64, 8}, {128, 2}, {128, 4}};
+    static const int kShapes64[][2] = {{32, 4}, {32, 8}, {32, 16}, {64, 4}, {64, 8}, {128, 2}, {128, 4}};
+    // FP32: 128 p cells (four per thread) by 1 .. 16 rows
+    static const int kShapes32[][2] = {{128, 1}, {128, 2}, {128, 4}, {128, 8}, {128, 16}};
     LaunchSet &L = get_set(set);
     FctLaunch fl{};
     fl.patches = L.dpatch.p;
@@ -30,7 +34,12 @@ std::pair<int, int> Engine::autotune(const std::vector<Run *> &set, int reps) {
     };
     double best_ms = 1e300;
     int best[2] = {L.tile_j, L.tile_i};
-    for (auto &sh : kShapes) {
+    std::vector<std::array<int, 2>> shapes;
+    if (L.precision == kF32)
+        for (auto &sh : kShapes32) shapes.push_back({sh[0], sh[1]});
+    else
+        for (auto &sh : kShapes64) shapes.push_back({sh[0], sh[1]});
+    for (auto &sh : shapes) {
         L.tile_j = sh[0];
         L.tile_i = sh[1];
         build_tiles(L);  // reallocates every tile list: take the pointers afresh
@@ -47,7 +56,7 @@ std::pair<int, int> Engine::autotune(const std::vector<Run *> &set, int reps) {
         timer_begin();
         for (int r = 0; r < reps; r++) run_subs();
         const double ms = timer_end() / reps;
-        kernel_launches += 6 * (reps + 1);
+        kernel_launches += (L.precision == kF32 ? 5 : 6) * (reps + 1);
         if (ms < best_ms) {
             best_ms = ms;
             best[0] = sh[0];

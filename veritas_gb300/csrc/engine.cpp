@@ -643,6 +643,9 @@ LaunchSet &Engine::get_set(const std::vector<Run *> &set) {
 
 // Tile list covering every patch's padded block with tile_j (p) x tile_i (x) tiles.
 void Engine::build_tiles(LaunchSet &L) {
+    // FP32 streaming kernels own four p cells per thread: 128-cell tiles starting at
+    // j0 = -2 + 128 k keep every thread's cells one aligned float4
+    if (L.precision == kF32) L.tile_j = 128;
     std::vector<TileRef> tiles;
     int pi = 0;
     for (Run *R : L.runs)

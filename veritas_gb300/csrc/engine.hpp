@@ -234,7 +234,7 @@ public:
     // CUDA graph per step and programmatic dependent launch on or off; drops the
     // captured graphs (they hold the old launch attributes).
     void set_launch_mode(bool graphs, bool pdl);
-    int tile_pref[2][2] = {{32, 8}, {32, 8}};  // [precision 64, 32] -> (tile_j, tile_i)
+    int tile_pref[2][2] = {{32, 8}, {128, 8}};  // [precision 64, 32] -> (tile_j, tile_i)
 
 private:
     std::map<std::vector<Run *>, std::unique_ptr<LaunchSet>> sets_;

@@ -72,153 +72,185 @@ __device__ __forceinline__ float qefield32(const P32 &P, const RunFields &F, int
     return P.qf * (t * (1.0f / (float)P.rtb));  // rtb is a power of two
 }
 
-#define VX_TILE32                                         \
-    const TileRef t = tiles[blockIdx.x];                  \
-    const P32 &P = patches[t.patch];                      \
-    const int i = t.i0 + (int)threadIdx.y;                \
-    const int j = t.j0 + (int)threadIdx.x;                \
-    if (i > P.nx + 1 || j > P.np + 1) return;             \
-    const int pit = P.pitch;                              \
-    const int id = pidx(i, j, pit);
-
-// Lorentz factor at (x-face i, p-face j), i in [-1,nx+1], j in [-1,np+1].
-__global__ void k32_gamma(const P32 *patches, const TileRef *tiles, const RunFields *fields) {
-    VX_PDL_WAIT();
-    VX_TILE32
-    if (i < -1 || j < -1) return;
-    const RunFields &F = fields[P.run];
-    const float a = asq32(P, F, i);
-    const float p = mom32(P, j);
-    P.gam[id] = sqrtf(1.0f + p * p + a);
-}
-
-__global__ void k32_faces(const P32 *patches, const TileRef *tiles, const RunFields *fields, int use_f0, int part) {
-    VX_PDL_WAIT();
-    VX_TILE32
-    const float *f = use_f0 ? P.f0 : P.f1;
-    const float *g = P.gam;
-    const float mm = P.weno_eps;
-    if ((part & 1) && i >= 0 && i <= P.nx && j >= -1 && j <= P.np) {
-        const float p0 = mom32(P, j), p1 = mom32(P, j + 1);
-        const float dg = P.dpnf * (p1 + p0) / (g[pidx(i, j + 1, pit)] + g[id]);
-        const float am = P.kxf * dg;
-        P.ex[id] = am;
-        P.fx[id] = weno32(f[pidx(i - 2, j, pit)], f[pidx(i - 1, j, pit)], f[id], f[pidx(i + 1, j, pit)], am > 0.0f, mm);
-    }
-    if ((part & 2) && i >= -1 && i <= P.nx && j >= 0 && j <= P.np) {
-        const RunFields &F = fields[P.run];
-        const float Em = qefield32(P, F, i);
-        const float a0 = asq32(P, F, i), a1 = asq32(P, F, i + 1);
-        const float dg = (a1 - a0) / (g[pidx(i + 1, j, pit)] + g[id]);
-        const float am = Em - P.kpf * dg;
-        P.ep[id] = am;
-        P.fp[id] = weno32(f[pidx(i, j - 2, pit)], f[pidx(i, j - 1, pit)], f[id], f[pidx(i, j + 1, pit)], am > 0.0f, mm);
-    }
-}
-
-__global__ void k32_flux(const P32 *patches, const TileRef *tiles, int step, int use_f0, int part) {
-    VX_PDL_WAIT();
-    VX_TILE32
-    const float *f = use_f0 ? P.f0 : P.f1;
-    const float w3 = 1.0f / 48.0f;
-    const float dxi = P.dxif, dpi = P.dpif;
-    if ((part & 1) && i >= 0 && i <= P.nx && j >= -1 && j <= P.np && !(P.ifx && P.ifx[id])) {
-        float am = P.ex[id], ap1 = P.ex[id + 1], am1 = P.ex[id - 1];
-        float fm = P.fx[id], fp1 = P.fx[id + 1], fm1 = P.fx[id - 1];
-        P.FxH[step][id] = dxi * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
-        if (step == 0) P.FxL[id] = dxi * ((am > 0.0f ? f[id - pit] : f[id]) * am);
-    }
-    if ((part & 2) && i >= -1 && i <= P.nx && j >= 0 && j <= P.np && !(P.ifp && P.ifp[id])) {
-        float am = P.ep[id], ap1 = P.ep[id + pit], am1 = P.ep[id - pit];
-        float fm = P.fp[id], fp1 = P.fp[id + pit], fm1 = P.fp[id - pit];
-        P.FpH[step][id] = dpi * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
-        if (step == 0) P.FpL[id] = dpi * ((am > 0.0f ? f[id - 1] : f[id]) * am);
-    }
-}
-
 __device__ __forceinline__ bool active32(const P32 &P, int i, int j) {
     return i >= P.xm && i < P.xp && j >= P.pm && j < P.pp;
 }
 
+// ---------------------------------------------------------------- streaming kernels
+// The cell-wise sub-steps move whole planes with 128-bit accesses: a thread owns four
+// consecutive p cells (j .. j+3) of one row, a tile is tile_i rows by 128 p cells
+// (blockDim = (32, tile_i)).  Tiles start at j0 = -2 + 128 k, so j + 2 is a multiple of
+// 4 and, with the pitch a multiple of 8 and every plane 16-byte aligned, each thread's
+// four cells are one aligned float4.  The p neighbours past the four (j - 1, j + 4) are
+// scalar loads, made only when a valid cell needs them (they are then inside the row).
+#define VX_VTILE32                                        \
+    const TileRef t = tiles[blockIdx.x];                  \
+    const P32 &P = patches[t.patch];                      \
+    const int i = t.i0 + (int)threadIdx.y;                \
+    const int j = t.j0 + 4 * (int)threadIdx.x;            \
+    if (i > P.nx + 1 || j > P.np + 1) return;             \
+    const int pit = P.pitch;                              \
+    const int id = pidx(i, j, pit);
+
+struct V4 {
+    float v[4];
+};
+__device__ __forceinline__ V4 ld4(const float *p) {
+    const float4 q = *reinterpret_cast<const float4 *>(p);
+    return {{q.x, q.y, q.z, q.w}};
+}
+// Stores the elements e with lo <= j + e < hi (one 128-bit store when all four are).
+__device__ __forceinline__ void st4(float *p, const V4 &x, int j, int lo, int hi) {
+    if (j >= lo && j + 3 < hi) {
+        *reinterpret_cast<float4 *>(p) = make_float4(x.v[0], x.v[1], x.v[2], x.v[3]);
+        return;
+    }
+#pragma unroll
+    for (int e = 0; e < 4; e++)
+        if (j + e >= lo && j + e < hi) p[e] = x.v[e];
+}
+
+// RK flux combination and low-order solution (Rectangle.cpp:1396-1534): DS over the
+// padded block, f2 over the interior.
 __global__ void k32_ds_f2(const P32 *patches, const TileRef *tiles, const float *params, int s) {
     VX_PDL_WAIT();
-    VX_TILE32
-    if (i < -2 || j < -2) return;
+    VX_VTILE32
     const float *a = params + param_base(P.run, s);
     const float asum = a[6];
-    float hx = a[0] * P.FxH[0][id];
-    float hp = a[0] * P.FpH[0][id];
+    V4 hx = ld4(P.FxH[0] + id), hp = ld4(P.FpH[0] + id);
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        hx.v[e] = a[0] * hx.v[e];
+        hp.v[e] = a[0] * hp.v[e];
+    }
     for (int k = 1; k <= s; k++) {
         if (s == 5 && k == 1) continue;  // b_1 = 0 (Rectangle.cpp:1494)
-        hx += a[k] * P.FxH[k][id];
-        hp += a[k] * P.FpH[k][id];
+        const V4 gx = ld4(P.FxH[k] + id), gp = ld4(P.FpH[k] + id);
+        const float ak = a[k];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            hx.v[e] += ak * gx.v[e];
+            hp.v[e] += ak * gp.v[e];
+        }
     }
-    const float lsx = asum * P.FxL[id];
-    const float lsp = asum * P.FpL[id];
-    P.FxDS[id] = hx - lsx;
-    P.FpDS[id] = hp - lsp;
-    if (i >= 0 && i < P.nx && j >= 0 && j < P.np) {
-        float v = P.f0[id];
-        if (active32(P, i, j)) v += lsx;
-        if (active32(P, i, j)) v += lsp;
-        if (active32(P, i, j + 1)) v -= asum * P.FpL[id + 1];
-        if (active32(P, i + 1, j)) v -= asum * P.FxL[id + pit];
-        P.f2[id] = v;
+    const V4 lx = ld4(P.FxL + id), lp = ld4(P.FpL + id);
+    V4 dx, dp, lsx, lsp;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        lsx.v[e] = asum * lx.v[e];
+        lsp.v[e] = asum * lp.v[e];
+        dx.v[e] = hx.v[e] - lsx.v[e];
+        dp.v[e] = hp.v[e] - lsp.v[e];
     }
+    st4(P.FxDS + id, dx, j, -2, P.np + 2);
+    st4(P.FpDS + id, dp, j, -2, P.np + 2);
+    if (i < 0 || i >= P.nx || j + 3 < 0 || j >= P.np) return;
+    const V4 f0 = ld4(P.f0 + id), lxn = ld4(P.FxL + id + pit);
+    const float lp4 = (j + 3 < P.np) ? P.FpL[id + 4] : 0.0f;  // j + 4 <= np
+    V4 f2;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const int je = j + e;
+        float v = f0.v[e];
+        if (active32(P, i, je)) v += lsx.v[e];
+        if (active32(P, i, je)) v += lsp.v[e];
+        if (active32(P, i, je + 1)) v -= asum * (e < 3 ? lp.v[e + 1] : lp4);
+        if (active32(P, i + 1, je)) v -= asum * lxn.v[e];
+        f2.v[e] = v;
+    }
+    st4(P.f2 + id, f2, j, 0, P.np);
 }
 
+// Zalesak R+ and R- (Rectangle.cpp:1536-1582), cells i in [-1, nx], j in [-1, np].
 __global__ void k32_limR(const P32 *patches, const TileRef *tiles) {
     VX_PDL_WAIT();
-    VX_TILE32
-    if (i < -1 || i > P.nx || j < -1 || j > P.np) return;
+    VX_VTILE32
+    if (i < -1 || i > P.nx || j + 3 < -1 || j > P.np) return;
     const float *DX = P.FxDS, *DP = P.FpDS, *f0 = P.f0, *f2 = P.f2;
-    float dxi = DX[id], dxn = DX[id + pit], dpi = DP[id], dpn = DP[id + 1];
-    float Pp = fmaxf(0.0f, dxi) - fminf(0.0f, dxn) + fmaxf(0.0f, dpi) - fminf(0.0f, dpn);
-    float Pm = fmaxf(0.0f, dxn) - fminf(0.0f, dxi) + fmaxf(0.0f, dpn) - fminf(0.0f, dpi);
-    float c0 = f0[id], c2 = f2[id];
-    float wMax = fmaxf(fmaxf(c0, c2), fmaxf(fmaxf(f0[id + pit], f2[id + pit]),
-                 fmaxf(fmaxf(f0[id - pit], f2[id - pit]), fmaxf(fmaxf(f0[id + 1], f2[id + 1]), fmaxf(f0[id - 1], f2[id - 1])))));
-    float wMin = fminf(fminf(c0, c2), fminf(fminf(f0[id + pit], f2[id + pit]),
-                 fminf(fminf(f0[id - pit], f2[id - pit]), fminf(fminf(f0[id + 1], f2[id + 1]), fminf(f0[id - 1], f2[id - 1])))));
-    float Qm = -wMin + c2;
-    float Qp = wMax - c2;
-    P.Rp[id] = Pp > 0.0f ? fminf(1.0f, Qp / Pp) : 0.0f;
-    P.Rm[id] = Pm > 0.0f ? fminf(1.0f, Qm / Pm) : 0.0f;
+    const V4 dxi = ld4(DX + id), dxn = ld4(DX + id + pit), dpi = ld4(DP + id);
+    const V4 a0 = ld4(f0 + id), a2 = ld4(f2 + id);
+    const V4 u0 = ld4(f0 + id + pit), u2 = ld4(f2 + id + pit);
+    const V4 d0 = ld4(f0 + id - pit), d2 = ld4(f2 + id - pit);
+    const bool lo_ok = j >= -1, hi_ok = j + 3 <= P.np;  // element 0 / element 3 valid
+    const float l0 = lo_ok ? f0[id - 1] : 0.0f, l2 = lo_ok ? f2[id - 1] : 0.0f;
+    const float r0 = hi_ok ? f0[id + 4] : 0.0f, r2 = hi_ok ? f2[id + 4] : 0.0f;
+    const float dp4 = hi_ok ? DP[id + 4] : 0.0f;
+    V4 rp, rm;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const float dpn = e < 3 ? dpi.v[e + 1] : dp4;
+        const float Pp = fmaxf(0.0f, dxi.v[e]) - fminf(0.0f, dxn.v[e]) + fmaxf(0.0f, dpi.v[e]) - fminf(0.0f, dpn);
+        const float Pm = fmaxf(0.0f, dxn.v[e]) - fminf(0.0f, dxi.v[e]) + fmaxf(0.0f, dpn) - fminf(0.0f, dpi.v[e]);
+        const float c0 = a0.v[e], c2 = a2.v[e];
+        const float lf0 = e > 0 ? a0.v[e - 1] : l0, lf2 = e > 0 ? a2.v[e - 1] : l2;
+        const float rf0 = e < 3 ? a0.v[e + 1] : r0, rf2 = e < 3 ? a2.v[e + 1] : r2;
+        const float wMax = fmaxf(fmaxf(c0, c2), fmaxf(fmaxf(u0.v[e], u2.v[e]),
+                           fmaxf(fmaxf(d0.v[e], d2.v[e]), fmaxf(fmaxf(rf0, rf2), fmaxf(lf0, lf2)))));
+        const float wMin = fminf(fminf(c0, c2), fminf(fminf(u0.v[e], u2.v[e]),
+                           fminf(fminf(d0.v[e], d2.v[e]), fminf(fminf(rf0, rf2), fminf(lf0, lf2)))));
+        const float Qm = -wMin + c2;
+        const float Qp = wMax - c2;
+        rp.v[e] = Pp > 0.0f ? fminf(1.0f, Qp / Pp) : 0.0f;
+        rm.v[e] = Pm > 0.0f ? fminf(1.0f, Qm / Pm) : 0.0f;
+    }
+    st4(P.Rp + id, rp, j, -1, P.np + 1);
+    st4(P.Rm + id, rm, j, -1, P.np + 1);
 }
 
+// Face coefficients C (Rectangle.cpp:1583-1594) over the padded block: 1 outside
+// i in [1, nx), j in [0, np).
 __global__ void k32_limC(const P32 *patches, const TileRef *tiles) {
     VX_PDL_WAIT();
-    VX_TILE32
-    if (i < -2 || j < -2) return;
-    float cx = 1.0f, cp = 1.0f;
-    if (i >= 1 && i < P.nx && j >= 0 && j < P.np) {
+    VX_VTILE32
+    V4 cx{{1.0f, 1.0f, 1.0f, 1.0f}}, cp{{1.0f, 1.0f, 1.0f, 1.0f}};
+    if (i >= 1 && i < P.nx && j + 3 >= 0 && j < P.np) {
         const float *Rp = P.Rp, *Rm = P.Rm;
-        cx = P.FxDS[id] > 0.0f ? fminf(Rp[id], Rm[id - pit]) : fminf(Rp[id - pit], Rm[id]);
-        cp = P.FpDS[id] > 0.0f ? fminf(Rp[id], Rm[id - 1]) : fminf(Rp[id - 1], Rm[id]);
+        const V4 rpi = ld4(Rp + id), rmi = ld4(Rm + id), rpd = ld4(Rp + id - pit), rmd = ld4(Rm + id - pit);
+        const V4 dx = ld4(P.FxDS + id), dp = ld4(P.FpDS + id);
+        const bool lo_ok = j >= 0;
+        const float rpl = lo_ok ? Rp[id - 1] : 0.0f, rml = lo_ok ? Rm[id - 1] : 0.0f;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            if (j + e < 0 || j + e >= P.np) continue;
+            const float rpm = e > 0 ? rpi.v[e - 1] : rpl, rmm = e > 0 ? rmi.v[e - 1] : rml;
+            cx.v[e] = dx.v[e] > 0.0f ? fminf(rpi.v[e], rmd.v[e]) : fminf(rpd.v[e], rmi.v[e]);
+            cp.v[e] = dp.v[e] > 0.0f ? fminf(rpi.v[e], rmm) : fminf(rpm, rmi.v[e]);
+        }
     }
-    P.Cx[id] = cx;
-    P.Cp[id] = cp;
+    st4(P.Cx + id, cx, j, -2, P.np + 2);
+    st4(P.Cp + id, cp, j, -2, P.np + 2);
 }
 
+// Antidiffusive update (Rectangle.cpp:1595-1612), interior cells.
 __global__ void k32_update(const P32 *patches, const TileRef *tiles) {
     VX_PDL_WAIT();
-    VX_TILE32
-    if (i < 0 || i >= P.nx || j < 0 || j >= P.np) return;
-    float v = P.f2[id];
-    if (active32(P, i, j)) v += P.Cx[id] * P.FxDS[id];
-    if (active32(P, i, j)) v += P.Cp[id] * P.FpDS[id];
-    if (active32(P, i, j + 1)) v -= P.Cp[id + 1] * P.FpDS[id + 1];
-    if (active32(P, i + 1, j)) v -= P.Cx[id + pit] * P.FxDS[id + pit];
-    P.f1[id] = v;
+    VX_VTILE32
+    if (i < 0 || i >= P.nx || j + 3 < 0 || j >= P.np) return;
+    const V4 f2 = ld4(P.f2 + id), cx = ld4(P.Cx + id), dx = ld4(P.FxDS + id), cp = ld4(P.Cp + id),
+             dp = ld4(P.FpDS + id);
+    const V4 cxn = ld4(P.Cx + id + pit), dxn = ld4(P.FxDS + id + pit);
+    const bool hi_ok = j + 3 < P.np;  // element 3 valid: j + 4 <= np
+    const float cp4 = hi_ok ? P.Cp[id + 4] : 0.0f, dp4 = hi_ok ? P.FpDS[id + 4] : 0.0f;
+    V4 out;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const int je = j + e;
+        float v = f2.v[e];
+        if (active32(P, i, je)) v += cx.v[e] * dx.v[e];
+        if (active32(P, i, je)) v += cp.v[e] * dp.v[e];
+        if (active32(P, i, je + 1)) v -= (e < 3 ? cp.v[e + 1] : cp4) * (e < 3 ? dp.v[e + 1] : dp4);
+        if (active32(P, i + 1, je)) v -= cxn.v[e] * dxn.v[e];
+        out.v[e] = v;
+    }
+    st4(P.f1 + id, out, j, 0, P.np);
 }
 
+// f0 = f1 over the padded block (Rectangle.cpp:1614-1621).
 __global__ void k32_copy10(const P32 *patches, const TileRef *tiles) {
     VX_PDL_WAIT();
-    VX_TILE32
-    if (i < -2 || j < -2) return;
-    P.f0[id] = P.f1[id];
+    VX_VTILE32
+    st4(P.f0 + id, ld4(P.f1 + id), j, -2, P.np + 2);
 }
-
 
 // ---------------------------------------------------------------- fused face + flux
 // One warp per strip tile: Lorentz factors, face velocities and WENO values are formed in
@@ -315,19 +347,11 @@ __global__ void k32_pflux(const P32 *patches, const TileRef *tiles, int ntiles, 
 }
 
 void launch_fct32_substep(const FctLaunch &L, int sub) {
-    dim3 blk(L.tile_j ? L.tile_j : 32, L.tile_i ? L.tile_i : 8);
+    // streaming kernels: tiles of tile_i rows x 128 p cells, four cells per thread
+    dim3 blk(32, L.tile_i ? L.tile_i : 8);
     const P32 *pp = (const P32 *)L.patches;
     if (L.ntiles == 0) return;
     switch (sub) {
-        case kSubGamma:
-            vx_launch(k32_gamma, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.fields);
-            break;
-        case kSubFaces:
-            vx_launch(k32_faces, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.fields, L.use_f0, L.part ? L.part : 3);
-            break;
-        case kSubFlux:
-            vx_launch(k32_flux, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.step, L.use_f0, L.part ? L.part : 3);
-            break;
         case kSubDsF2:
             vx_launch(k32_ds_f2, L.ntiles, blk, 0, L.stream, pp, L.tiles, L.params32, L.step);
             break;
@@ -348,6 +372,8 @@ void launch_fct32_substep(const FctLaunch &L, int sub) {
             break;
         case kSubPFlux:
             if (L.nptiles) vx_launch(k32_pflux, (L.nptiles + 3) / 4, 128, 0, L.stream, pp, L.ptiles, L.nptiles, L.fields, L.step, L.use_f0);
+            break;
+        default:  // the FP32 form has no separate gamma / face / flux sub-steps (fused above)
             break;
     }
 }
