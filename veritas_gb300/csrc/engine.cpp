@@ -160,7 +160,8 @@ void Run::upload_rect_desc(Rect &r, int run_index) {
     d.a2nf = (float)(d.qq * d.g2);
     d.msc_rho = (1.0 / d.fnorm) * (d.dp * d.q);
     d.msc_j = (1.0 / d.fnorm) * (1.0 / ((1.0 / d.mass) * kCInv)) * (-d.q * d.q / d.mass);
-    if (precision == kF32 && d.rtb > 8) throw std::invalid_argument("the FP32 form supports up to 8 finest cells per coarse cell");
+    if (precision == kF32 && d.rtb != 1 && d.rtb != 2 && d.rtb != 4 && d.rtb != 8)
+        throw std::invalid_argument("the FP32 form supports 1, 2, 4 or 8 finest cells per coarse cell");
     double *cols = r.cols.as<double>();
     d.chargeR = cols;
     d.currentR = cols + (size_t)r.n_x * d.rtb;
@@ -716,7 +717,10 @@ void Engine::build_set(LaunchSet &L) {
                     L.hpatch.push_back(r.desc);
                     lvl_patch.push_back(pi);
                     int rtb = r.desc.rtb;
-                    for (int c = 0; c < r.n_x * rtb; c++) {
+                    // FP64: one moment column per finest sub-column; FP32: per coarse
+                    // column (its kernel forms all rtb sub-columns from shared loads)
+                    const int cstep = L.precision == kF32 ? rtb : 1;
+                    for (int c = 0; c < r.n_x * rtb; c += cstep) {
                         colpatch.push_back(pi);
                         colidx.push_back(c);
                     }

@@ -15,7 +15,7 @@ namespace vx {
 using P32 = PatchT<float>;
 
 // ---------------------------------------------------------------- moments
-// One warp per moment column (coarse column i, finest sub-column k).  Windows of 29
+// One warp per coarse column i, all its finest sub-columns k at once.  Windows of 29
 // outputs: lane l holds p index j = j0 - 1 + l; l_j needs G of the next lane, so lanes
 // 0..30 have it and lanes 1..29 produce.
 //   G_j = gamma_j + p_j = (1 + a) / (gamma_j - p_j)   (dimensionless, p in units of m c;
@@ -26,28 +26,6 @@ using P32 = PatchT<float>;
 //         is below 3e-10 relative), ln(1 + u) otherwise,
 //   rho_k += f_j,  J_k += f_j l_j + (1/48)(l_{j+1} - l_{j-1})(f_{j+1} - f_{j-1}).
 constexpr int kMom32Out = 29;
-
-// Interpolated value on finest sub-cell k of coarse cell (i, j) (Rectangle.cpp:139-155,
-// 183-204): wk = weights of sub-cell k, ws = the weights summed over all sub-cells, so
-// the conservative correction needs no loop over the sub-cells.
-struct RelWeights {
-    float k0, k1, k2, s0, s1, s2;
-};
-
-__device__ __forceinline__ float rel_value32(const P32 &P, const float *f, int i, int j, const RelWeights &w,
-                                             float inv_rtb) {
-    const int pit = P.pitch;
-    const float f3 = f[pidx(i, j, pit)];
-    if (P.rtb == 1) return f3;
-    const float g1 = f[pidx(i - 2, j, pit)] - f3, g2 = f[pidx(i - 1, j, pit)] - f3;
-    const float g4 = f[pidx(i + 1, j, pit)] - f3, g5 = f[pidx(i + 2, j, pit)] - f3;
-    const float a1 = 0.104166666666667f * g1 - 0.708333333333334f * g2 + 0.708333333333334f * g4 - 0.104166666666667f * g5;
-    const float a2 = 0.117647058823529f * g1 + 0.029411764705882f * g2 + 0.029411764705882f * g4 + 0.117647058823529f * g5;
-    const float a3 = -0.083333333333333f * g1 + 0.166666666666667f * g2 - 0.166666666666667f * g4 + 0.083333333333334f * g5;
-    const float mine = w.k0 * a1 + w.k1 * a2 + w.k2 * a3 + f3;
-    const float mean = (w.s0 * a1 + w.s1 * a2 + w.s2 * a3) * inv_rtb + f3;
-    return mine + (f3 - mean);
-}
 
 // Compensated FP32 pair (value = hi + lo): TwoSum (Knuth) and FastTwoSum (Dekker)
 // additions for the warp reduction of the lanes' Kahan sums.
@@ -69,88 +47,131 @@ __device__ __forceinline__ F2 f2_warp_sum(F2 v) {
     return v;
 }
 
-// No FP64 instruction per cell or per lane: the A^2 of the column comes from the FP32
-// per-cell copy, the weights and the final scales from the patch descriptor; one lane
-// converts the two reduced pairs to FP64.
+// l_j = ln(G_{j+1} / G_j) for a lane's p_j (see the table above); valid on lanes 0..30.
+__device__ __forceinline__ float log_ratio32(float p, float pn, float g, float gn, float a, float dpn) {
+    const float dG = dpn * (1.0f + __fdividef(pn + p, gn + g));
+    const float G = p >= 0.0f ? g + p : __fdividef(1.0f + a, g - p);
+    const float z = __fdividef(dG, 2.0f * G + dG);
+    if (z <= 0.0625f) {
+        const float z2 = z * z;
+        return 2.0f * z * fmaf(z2, fmaf(z2, fmaf(z2, 1.0f / 7.0f, 0.2f), 1.0f / 3.0f), 1.0f);
+    }
+    // ln(1 + u) as logf(y) u / (y - 1), y = 1 + u rounded (Goldberg, "What every computer
+    // scientist should know about floating-point arithmetic", 1991)
+    const float u = __fdividef(dG, G);
+    const float y1 = 1.0f + u;
+    return logf(y1) * __fdividef(u, y1 - 1.0f);
+}
+
+__device__ __forceinline__ void kahan_add(float v, float &sum, float &comp) {
+    const float y = v - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
+// Sub-columns k0 .. k0+KG-1 of coarse column i (rtb finest sub-columns): the f stencil
+// and the interpolation's shared part are loaded and formed once per cell for the group.
+// KG = 1 (rtb = 1) runs two windows per iteration to have two chains in flight; wider
+// columns go through in groups of two, re-reading f from L1.
+template <int KG>
+__device__ __forceinline__ void moments_group(const P32 &P, const RunFields &F, int i, int k0, int lane) {
+    constexpr int NW = KG == 1 ? 2 : 1;
+    const unsigned full = 0xffffffffu;
+    const int rtb = P.rtb;
+    float a[KG], wk0[KG], wk1[KG], wk2[KG];
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+#pragma unroll
+    for (int q = 0; q < KG; q++) {
+        const int k = k0 + q;
+        // cell-average A^2 at the finest cell (EMSolver::GetCellAverageASquared), made
+        // dimensionless
+        int xc = (i + P.x_pos) * rtb + k + F.pre;
+        xc = xc > -1 ? xc : 0;
+        xc = xc < F.nf ? xc : F.nf - 1;
+        a[q] = P.a2nf * F.acell32[xc];
+        wk0[q] = wk1[q] = wk2[q] = 0.0f;
+        if (rtb > 1) {
+            wk0[q] = P.relc32[3 * k];
+            wk1[q] = P.relc32[3 * k + 1];
+            wk2[q] = P.relc32[3 * k + 2];
+        }
+    }
+    if (rtb > 1) {
+        s0 = P.relc32[3 * rtb];
+        s1 = P.relc32[3 * rtb + 1];
+        s2 = P.relc32[3 * rtb + 2];
+    }
+    const float pmin = P.pminf, dpn = P.dpnf;
+    const float c3 = 1.0f / 48.0f, inv_rtb = 1.0f / (float)rtb;  // rtb is a power of two
+    const float *f = P.f1;
+    const int pit = P.pitch;
+    float chs[KG], chc[KG], cus[KG], cuc[KG];
+#pragma unroll
+    for (int q = 0; q < KG; q++) chs[q] = chc[q] = cus[q] = cuc[q] = 0.0f;
+    for (int j0 = 0; j0 < P.np; j0 += NW * kMom32Out) {
+#pragma unroll
+        for (int w = 0; w < NW; w++) {
+            const int jw = j0 + w * kMom32Out;
+            if (w > 0 && jw >= P.np) break;  // warp-uniform
+            const int j = jw - 1 + lane;
+            const float p = fmaf(dpn, (float)(j + P.p_pos), pmin);
+            const float pn = fmaf(dpn, (float)(j + 1 + P.p_pos), pmin);
+            // interpolation's shared part (Rectangle.cpp:139-155, 183-204)
+            float f3 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f, fmean = 0.0f;
+            if (j <= P.np) {
+                f3 = f[pidx(i, j, pit)];
+                if (rtb > 1) {
+                    const float g1 = f[pidx(i - 2, j, pit)] - f3, g2 = f[pidx(i - 1, j, pit)] - f3;
+                    const float g4 = f[pidx(i + 1, j, pit)] - f3, g5 = f[pidx(i + 2, j, pit)] - f3;
+                    a1 = 0.104166666666667f * g1 - 0.708333333333334f * g2 + 0.708333333333334f * g4 - 0.104166666666667f * g5;
+                    a2 = 0.117647058823529f * g1 + 0.029411764705882f * g2 + 0.029411764705882f * g4 + 0.117647058823529f * g5;
+                    a3 = -0.083333333333333f * g1 + 0.166666666666667f * g2 - 0.166666666666667f * g4 + 0.083333333333334f * g5;
+                    fmean = (s0 * a1 + s1 * a2 + s2 * a3) * inv_rtb + f3;
+                }
+            }
+            const bool use = lane >= 1 && lane <= kMom32Out && j < P.np && !(P.nested && P.nested[pidx(i, j, pit)]);
+#pragma unroll
+            for (int q = 0; q < KG; q++) {
+                const float s = 1.0f + p * p + a[q];
+                const float g = s * rsqrtf(s);
+                const float gn = __shfl_down_sync(full, g, 1);
+                const float l = log_ratio32(p, pn, g, gn, a[q], dpn);
+                const float V = rtb == 1 ? f3 : (wk0[q] * a1 + wk1[q] * a2 + wk2[q] * a3 + f3) + (f3 - fmean);
+                const float lm = __shfl_up_sync(full, l, 1), lp = __shfl_down_sync(full, l, 1);
+                const float Vm = __shfl_up_sync(full, V, 1), Vp = __shfl_down_sync(full, V, 1);
+                kahan_add(use ? V : 0.0f, chs[q], chc[q]);
+                kahan_add(use ? (V * l + c3 * (lp - lm) * (Vp - Vm)) : 0.0f, cus[q], cuc[q]);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < KG; q++) {
+        const F2 ch = f2_warp_sum(F2{chs[q], -chc[q]});
+        const F2 cu = f2_warp_sum(F2{cus[q], -cuc[q]});
+        if (lane == 0) {
+            const int c = i * rtb + k0 + q;
+            P.chargeR[c] = ((double)ch.hi + (double)ch.lo) * P.msc_rho;
+            P.currentR[c] = ((double)cu.hi + (double)cu.lo) * P.msc_j;
+        }
+    }
+}
+
+// One warp per coarse column (M.colidx holds i * rtb, the column's first finest
+// sub-column).  No FP64 instruction per cell or per lane: the A^2 of each sub-column comes
+// from the FP32 per-cell copy, the weights and the final scales from the patch
+// descriptor; one lane converts the reduced pairs to FP64.
 __global__ void k32_moments(MomLaunch M) {
     VX_PDL_WAIT();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= M.ncols) return;
     const P32 &P = ((const P32 *)M.patches)[M.colpatch[warp]];
-    const int c = M.colidx[warp];
-    const int i = c / P.rtb, k = c - i * P.rtb;
+    const int i = M.colidx[warp] / P.rtb;
     const RunFields &F = M.fields[P.run];
-    // cell-average A^2 at the finest cell (EMSolver::GetCellAverageASquared), made
-    // dimensionless
-    int xc = (i + P.x_pos) * P.rtb + k + F.pre;
-    xc = xc > -1 ? xc : 0;
-    xc = xc < F.nf ? xc : F.nf - 1;
-    const float a = P.a2nf * F.acell32[xc];
-    RelWeights w{0, 0, 0, 0, 0, 0};
-    float inv_rtb = 1.0f;
-    if (P.rtb > 1) {
-        const float *rw = P.relc32;
-        w = {rw[3 * k], rw[3 * k + 1], rw[3 * k + 2], rw[3 * P.rtb], rw[3 * P.rtb + 1], rw[3 * P.rtb + 2]};
-        inv_rtb = 1.0f / (float)P.rtb;
-    }
-    const float pmin = P.pminf, dpn = P.dpnf;
-    const float c3 = 1.0f / 48.0f;
-    const float *f = P.f1;
-    const unsigned full = 0xffffffffu;
-    // per-lane compensated FP32 sums (Kahan)
-    float chs = 0.0f, chc = 0.0f, cus = 0.0f, cuc = 0.0f;
-    auto kahan = [](float v, float &sum, float &comp) {
-        float y = v - comp;
-        float t = sum + y;
-        comp = (t - sum) - y;
-        sum = t;
-    };
-    // contributions of the window starting at p index j0 (zero on lanes that produce
-    // nothing); warp-uniform, so two windows can be in flight per iteration
-    auto window = [&](int j0, float &vc, float &vj) {
-        const int j = j0 - 1 + lane;
-        const float p = fmaf(dpn, (float)(j + P.p_pos), pmin);
-        const float g = (1.0f + p * p + a) * rsqrtf(1.0f + p * p + a);
-        const float gn = __shfl_down_sync(full, g, 1);
-        const float pn = __shfl_down_sync(full, p, 1);
-        const float dG = dpn * (1.0f + __fdividef(pn + p, gn + g));
-        const float G = p >= 0.0f ? g + p : __fdividef(1.0f + a, g - p);
-        const float z = __fdividef(dG, 2.0f * G + dG);
-        float l;  // valid on lanes 0..30
-        if (z <= 0.0625f) {
-            const float z2 = z * z;
-            l = 2.0f * z * fmaf(z2, fmaf(z2, fmaf(z2, 1.0f / 7.0f, 0.2f), 1.0f / 3.0f), 1.0f);
-        } else {
-            // ln(1 + u) as logf(y) u / (y - 1), y = 1 + u rounded (Goldberg, "What every
-            // computer scientist should know about floating-point arithmetic", 1991)
-            const float u = __fdividef(dG, G);
-            const float y1 = 1.0f + u;
-            l = logf(y1) * __fdividef(u, y1 - 1.0f);
-        }
-        float V = 0.0f;
-        if (j <= P.np) V = rel_value32(P, f, i, j, w, inv_rtb);
-        const float lm = __shfl_up_sync(full, l, 1), lp = __shfl_down_sync(full, l, 1);
-        const float Vm = __shfl_up_sync(full, V, 1), Vp = __shfl_down_sync(full, V, 1);
-        const bool use = lane >= 1 && lane <= kMom32Out && j < P.np && !(P.nested && P.nested[pidx(i, j, P.pitch)]);
-        vc = use ? V : 0.0f;
-        vj = use ? (V * l + c3 * (lp - lm) * (Vp - Vm)) : 0.0f;
-    };
-    for (int j0 = 0; j0 < P.np; j0 += 2 * kMom32Out) {
-        float c0, j0v, c1 = 0.0f, j1v = 0.0f;
-        window(j0, c0, j0v);
-        if (j0 + kMom32Out < P.np) window(j0 + kMom32Out, c1, j1v);
-        kahan(c0, chs, chc);
-        kahan(j0v, cus, cuc);
-        kahan(c1, chs, chc);
-        kahan(j1v, cus, cuc);
-    }
-    const F2 ch = f2_warp_sum(F2{chs, -chc});
-    const F2 cu = f2_warp_sum(F2{cus, -cuc});
-    if (lane == 0) {
-        P.chargeR[c] = ((double)ch.hi + (double)ch.lo) * P.msc_rho;
-        P.currentR[c] = ((double)cu.hi + (double)cu.lo) * P.msc_j;
-    }
+    if (P.rtb == 1) moments_group<1>(P, F, i, 0, lane);
+    else  // rtb is even (2, 4 or 8 in the FP32 form)
+        for (int k0 = 0; k0 < P.rtb; k0 += 2) moments_group<2>(P, F, i, k0, lane);
 }
 
 // FP32 copy of Ay^2 + Az^2 (slot 1) over every run's field grid, read by k32_moments.
