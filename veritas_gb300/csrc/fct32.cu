@@ -260,7 +260,8 @@ __global__ void k32_copy10(const P32 *patches, const TileRef *tiles) {
 // p: i in [-1, nx], j in [0, np]) are zero, as the planes they read are.
 
 // x direction: a warp covers kXCols output columns j0 .. j0+29 (its 32 lanes hold the
-// face values of j0-1 .. j0+30) over kStripRows rows; rows are independent in x.
+// face values of j0-1 .. j0+30) over kStripRows rows; rows are independent in x, and the
+// four rows of f a face reads (i-2 .. i+1) slide down the strip, one new load per row.
 __global__ void k32_xflux(const P32 *patches, const TileRef *tiles, int ntiles, const RunFields *fields, int step,
                           int use_f0) {
     VX_PDL_WAIT();
@@ -277,37 +278,54 @@ __global__ void k32_xflux(const P32 *patches, const TileRef *tiles, int ntiles, 
     const float p0 = mom32(P, jj), p1 = mom32(P, jj + 1);
     const float w3 = 1.0f / 48.0f;
     const unsigned full = 0xffffffffu;
+    // f at rows i-2, i-1, i of the first row (i0 >= 0, so all inside the padded block)
+    float fa = 0.0f, fb = 0.0f, fc = 0.0f;
+    if (col_ok) {
+        const int id = pidx(t.i0, jj, pit);
+        fa = f[id - 2 * pit];
+        fb = f[id - pit];
+        fc = f[id];
+    }
     for (int r = 0; r < kStripRows; r++) {
         const int i = t.i0 + r;
         if (i > P.nx) break;  // warp-uniform
-        float am = 0.0f, fv = 0.0f;
+        const int id = pidx(i, jj, pit);
+        float am = 0.0f, fv = 0.0f, fd = 0.0f;
         if (col_ok) {
+            fd = f[id + pit];  // row i+1 <= nx+1
             const float a = asq32(P, F, i);
             const float g0 = sqrt_ge1(1.0f + p0 * p0 + a), g1 = sqrt_ge1(1.0f + p1 * p1 + a);
             am = P.kxf * __fdividef(P.dpnf * (p1 + p0), g1 + g0);
-            const int id = pidx(i, jj, pit);
-            fv = weno32(f[id - 2 * pit], f[id - pit], f[id], f[id + pit], am > 0.0f, P.weno_eps);
+            fv = weno32(fa, fb, fc, fd, am > 0.0f, P.weno_eps);
         }
         const float am1 = __shfl_up_sync(full, am, 1), ap1 = __shfl_down_sync(full, am, 1);
         const float fm1 = __shfl_up_sync(full, fv, 1), fp1 = __shfl_down_sync(full, fv, 1);
-        if (lane < 1 || lane > kXCols || !col_ok) continue;
-        const int id = pidx(i, jj, pit);
-        if (P.ifx && P.ifx[id]) continue;
-        P.FxH[step][id] = P.dxif * (fv * am + w3 * (fp1 - fm1) * (ap1 - am1));
-        if (step == 0) P.FxL[id] = P.dxif * ((am > 0.0f ? f[id - pit] : f[id]) * am);
+        if (lane >= 1 && lane <= kXCols && col_ok && !(P.ifx && P.ifx[id])) {
+            P.FxH[step][id] = P.dxif * (fv * am + w3 * (fp1 - fm1) * (ap1 - am1));
+            if (step == 0) P.FxL[id] = P.dxif * ((am > 0.0f ? fb : fc) * am);  // f[i-1] or f[i]
+        }
+        fa = fb;
+        fb = fc;
+        fc = fd;
     }
 }
 
 // p direction: a warp covers 32 columns over kStripRows output rows, walking down with
-// the face values of the previous and next rows in registers.
-__device__ __forceinline__ void pface32(const P32 &P, const RunFields &F, const float *f, int i, int j, float p,
-                                        bool col_ok, float &am, float &fv) {
+// the face values of the previous and next rows in registers.  Face row i reads a^2 and
+// gamma at x-faces i and i+1; the i+1 pair is the next row's i pair, so it is carried.
+struct PRow {
+    float a, g;  // q^2 A^2 / (m c)^2 and gamma at the row's lower x-face
+};
+__device__ __forceinline__ PRow prow32(const P32 &P, const RunFields &F, int i, float p) {
+    const float a = asq32(P, F, i);
+    return {a, sqrt_ge1(1.0f + p * p + a)};
+}
+__device__ __forceinline__ void pface32(const P32 &P, const RunFields &F, const float *f, int i, int j,
+                                        bool col_ok, const PRow &lo, const PRow &hi, float &am, float &fv) {
     am = 0.0f;
     fv = 0.0f;
     if (!col_ok || i < -1 || i > P.nx) return;
-    const float a0 = asq32(P, F, i), a1 = asq32(P, F, i + 1);
-    const float g0 = sqrt_ge1(1.0f + p * p + a0), g1 = sqrt_ge1(1.0f + p * p + a1);
-    am = qefield32(P, F, i) - P.kpf * __fdividef(a1 - a0, g1 + g0);
+    am = qefield32(P, F, i) - P.kpf * __fdividef(hi.a - lo.a, hi.g + lo.g);
     const int id = pidx(i, j, P.pitch);
     fv = weno32(f[id - 2], f[id - 1], f[id], f[id + 1], am > 0.0f, P.weno_eps);
 }
@@ -326,14 +344,16 @@ __global__ void k32_pflux(const P32 *patches, const TileRef *tiles, int ntiles, 
     const bool col_ok = j >= 0 && j <= P.np;
     const float p = mom32(P, j);
     const float w3 = 1.0f / 48.0f;
+    PRow r0 = prow32(P, F, t.i0 - 1, p), r1 = prow32(P, F, t.i0, p), r2 = prow32(P, F, t.i0 + 1, p);
     float amA, fvA, amB, fvB;  // rows i-1 and i
-    pface32(P, F, f, t.i0 - 1, j, p, col_ok, amA, fvA);
-    pface32(P, F, f, t.i0, j, p, col_ok, amB, fvB);
+    pface32(P, F, f, t.i0 - 1, j, col_ok, r0, r1, amA, fvA);
+    pface32(P, F, f, t.i0, j, col_ok, r1, r2, amB, fvB);
     for (int r = 0; r < kStripRows; r++) {
         const int i = t.i0 + r;
         if (i > P.nx) break;
+        const PRow r3 = prow32(P, F, i + 2, p);
         float amC, fvC;  // row i+1
-        pface32(P, F, f, i + 1, j, p, col_ok, amC, fvC);
+        pface32(P, F, f, i + 1, j, col_ok, r2, r3, amC, fvC);
         if (col_ok && !(P.ifp && P.ifp[pidx(i, j, P.pitch)])) {
             const int id = pidx(i, j, P.pitch);
             P.FpH[step][id] = P.dpif * (fvB * amB + w3 * (fvC - fvA) * (amC - amA));
@@ -343,6 +363,7 @@ __global__ void k32_pflux(const P32 *patches, const TileRef *tiles, int ntiles, 
         fvA = fvB;
         amB = amC;
         fvB = fvC;
+        r2 = r3;
     }
 }
 
