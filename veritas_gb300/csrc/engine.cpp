@@ -724,6 +724,12 @@ void Engine::build_set(LaunchSet &L) {
                         colpatch.push_back(pi);
                         colidx.push_back(c);
                     }
+                    // FP64: blocks of kMomCols columns of one patch (padding: patch -1)
+                    if (L.precision == kF64)
+                        while (colpatch.size() % kMomCols) {
+                            colpatch.push_back(-1);
+                            colidx.push_back(0);
+                        }
                     L.maxnp = std::max(L.maxnp, r.n_p);
                 }
                 ptr.push_back((int)lvl_patch.size());

@@ -50,77 +50,94 @@ __device__ __forceinline__ double cell_asq(const RunFields &F, int x) {
     return (ay * ay) + (az * az);
 }
 
-// One warp per moment column (coarse column i, finest sub-column k).  The warp walks p
-// in windows of 32 lanes covering j0-1 .. j0+30: every lane computes the Lorentz factor
-// at its p-face once (shared with the neighbouring face through shuffles instead of the
-// reference's four Gamma calls per cell), the log ratio
+// One warp per moment column (coarse column i, finest sub-column k), kMomCols columns of
+// one patch per block.  A warp walks p in windows of 32 lanes covering j0-1 .. j0+30:
+// every lane computes the Lorentz factor at its p-face once (shared with the
+// neighbouring face through shuffles instead of the reference's four Gamma calls per
+// cell), the log ratio
 //   L(j) = c2 * ln((g_{j+1} + c1 p_{j+1}) / (g_j + c1 p_j))
 // (the reference's gm; gm1 and gp1 are L(j-1) and L(j+1), the same expressions), the
-// interpolated f and the cell's charge/current contributions.  Lane 0 then adds the 29
-// contributions of the window in ascending j, which keeps the reference's accumulation
-// order (Rectangle.cpp:207-255) exactly.
+// interpolated f and the cell's charge/current contributions.  The window's 29
+// contributions per column then go through shared memory to warp 0, whose lane w adds
+// column w's in ascending j, which keeps the reference's accumulation order
+// (Rectangle.cpp:207-255) exactly.  The serial sums thus take one FP64 warp instruction
+// per cell for kMomCols columns at once (an FP64 warp instruction occupies the
+// sub-partition's FP64 unit for tens of cycles whatever the number of active lanes).
+// The column list is padded per patch to a multiple of kMomCols (padding: patch -1), so
+// the warps of a block share n_p and step through the windows together.
 constexpr int kMomOut = 29;  // outputs per window: j0 .. j0+28
 
-__global__ void k64_moments(MomLaunch M) {
+__global__ void __launch_bounds__(kMomCols * 32) k64_moments(MomLaunch M) {
     VX_PDL_WAIT();
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (warp >= M.ncols) return;
-    const P64 &P = ((const P64 *)M.patches)[M.colpatch[warp]];
-    const int c = M.colidx[warp];
+    __shared__ double s_cc[kMomCols][32], s_cj[kMomCols][32];
+    __shared__ unsigned s_use[kMomCols];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int col0 = blockIdx.x * kMomCols;
+    const int cp = M.colpatch[col0 + wid];  // -1: padding
+    const P64 &P = ((const P64 *)M.patches)[M.colpatch[col0]];  // the block's patch
+    const int np = P.np;
+    const int c = M.colidx[col0 + wid];
     const int i = c / P.rtb, k = c - i * P.rtb;
     const RunFields &F = M.fields[P.run];
-    const double a = P.qq * cell_asq(F, (i + P.x_pos) * P.rtb + k);
+    const double a = cp >= 0 ? P.qq * cell_asq(F, (i + P.x_pos) * P.rtb + k) : 0.0;
     const double minv = 1 / P.mass;
     const double c1 = minv * kCInv;
     const double c2 = 1 / c1;
     const double c3 = 1 / 48.0;
     const double *f = P.f1;
     const unsigned full = 0xffffffffu;
-    double ch = 0.0, cu = 0.0;
-    for (int j0 = 0; j0 < P.np; j0 += kMomOut) {
-        const int j = j0 - 1 + lane;  // this lane's p index
-        double G = 0.0, V = 0.0;
-        if (j <= P.np + 1) {
-            double p = P.pmin + P.dp * (double)(j + P.p_pos);
-            double g = sqrt(1.0 + ((p * p) + a) * P.g2);
-            G = g + c1 * p;
-        }
-        if (j <= P.np) V = rel_value(P, f, i, j, k);
-        const double Gn = __shfl_down_sync(full, G, 1);
-        const double L = c2 * log(Gn / G);  // valid for lanes 0..30
-        const double Lm = __shfl_up_sync(full, L, 1);
-        const double Lp = __shfl_down_sync(full, L, 1);
-        const double Vm = __shfl_up_sync(full, V, 1);
-        const double Vp = __shfl_down_sync(full, V, 1);
+    double ch = 0.0, cu = 0.0;  // warp 0, lane w: column w of the block
+    for (int j0 = 0; j0 < np; j0 += kMomOut) {
         double cc = 0.0, cj = 0.0;
-        bool use = lane >= 1 && lane <= kMomOut && j < P.np && !(P.nested && P.nested[pidx(i, j, P.pitch)]);
-        if (use) {
-            cc = V;
-            cj = V * L + c3 * (Lp - Lm) * (Vp - Vm);
-        }
-        const unsigned usemask = __ballot_sync(full, use);
-        for (int t = 1; t <= kMomOut; t++) {
-            const double vc = __shfl_sync(full, cc, t);
-            const double vj = __shfl_sync(full, cj, t);
-            if ((usemask >> t) & 1u) {
-                ch += vc;
-                cu += vj;
+        bool use = false;
+        if (cp >= 0) {  // warp-uniform
+            const int j = j0 - 1 + lane;  // this lane's p index
+            double G = 0.0, V = 0.0;
+            if (j <= np + 1) {
+                double p = P.pmin + P.dp * (double)(j + P.p_pos);
+                double g = sqrt(1.0 + ((p * p) + a) * P.g2);
+                G = g + c1 * p;
+            }
+            if (j <= np) V = rel_value(P, f, i, j, k);
+            const double Gn = __shfl_down_sync(full, G, 1);
+            const double L = c2 * log(Gn / G);  // valid for lanes 0..30
+            const double Lm = __shfl_up_sync(full, L, 1);
+            const double Lp = __shfl_down_sync(full, L, 1);
+            const double Vm = __shfl_up_sync(full, V, 1);
+            const double Vp = __shfl_down_sync(full, V, 1);
+            use = lane >= 1 && lane <= kMomOut && j < np && !(P.nested && P.nested[pidx(i, j, P.pitch)]);
+            if (use) {
+                cc = V;
+                cj = V * L + c3 * (Lp - Lm) * (Vp - Vm);
             }
         }
+        const unsigned usemask = __ballot_sync(full, use);
+        s_cc[wid][lane] = cc;
+        s_cj[wid][lane] = cj;
+        if (lane == 0) s_use[wid] = usemask;
+        __syncthreads();
+        if (wid == 0 && lane < kMomCols) {
+            const unsigned um = s_use[lane];
+            for (int t = 1; t <= kMomOut; t++)
+                if ((um >> t) & 1u) {
+                    ch += s_cc[lane][t];
+                    cu += s_cj[lane][t];
+                }
+        }
+        __syncthreads();
     }
-    if (lane == 0) {
+    if (wid == 0 && lane < kMomCols && M.colpatch[col0 + lane] >= 0) {
+        const int cl = M.colidx[col0 + lane];
         const double q = P.q;
-        P.chargeR[c] = ch * (P.dp * q);
-        P.currentR[c] = cu * (-q * q / P.mass);
+        P.chargeR[cl] = ch * (P.dp * q);
+        P.currentR[cl] = cu * (-q * q / P.mass);
     }
 }
 
 void launch_moments64(const MomLaunch &M) {
     if (M.ncols == 0) return;
-    const int threads = 256;
-    const int blocks = (M.ncols * 32 + threads - 1) / threads;
-    vx_launch(k64_moments, blocks, threads, 0, M.stream, M);
+    // M.ncols is a multiple of kMomCols (the list is padded per patch)
+    vx_launch(k64_moments, M.ncols / kMomCols, kMomCols * 32, 0, M.stream, M);
 }
 
 // ---------------------------------------------------------------- assembly

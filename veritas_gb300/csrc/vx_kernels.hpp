@@ -92,6 +92,7 @@ struct MomLaunch {
     int nruns, maxnf;     // FP32: the per-cell A^2 copy covers every run's field grid
     cudaStream_t stream;
 };
+constexpr int kMomCols = 16;  // FP64 moment columns per block (padded per patch)
 void launch_moments64(const MomLaunch &M);
 void launch_moments32(const MomLaunch &M);
 
