@@ -717,10 +717,9 @@ void Engine::build_set(LaunchSet &L) {
                     L.hpatch.push_back(r.desc);
                     lvl_patch.push_back(pi);
                     int rtb = r.desc.rtb;
-                    // FP64: one moment column per finest sub-column; FP32: per coarse
-                    // column (its kernel forms all rtb sub-columns from shared loads)
-                    const int cstep = L.precision == kF32 ? rtb : 1;
-                    for (int c = 0; c < r.n_x * rtb; c += cstep) {
+                    // one moment column per coarse column (the kernels form its rtb
+                    // finest sub-columns from shared loads); c = i * rtb
+                    for (int c = 0; c < r.n_x * rtb; c += rtb) {
                         colpatch.push_back(pi);
                         colidx.push_back(c);
                     }

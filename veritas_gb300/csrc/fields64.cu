@@ -14,14 +14,16 @@ namespace vx {
 
 using P64 = PatchT<double>;
 
-// Interpolated value of f on finest sub-cell k of coarse cell (i, j), including the
-// conservative correction (Rectangle.cpp:139-155 and :183-204).  Fixed 12-entry
-// interpolation matrix of the reference (Rectangle.cpp:76-89).
-__device__ __forceinline__ double rel_value(const P64 &P, const double *f, int i, int j, int k) {
+// Interpolated value of f on the finest sub-cells of coarse cell (i, j), rtb > 1, with the
+// conservative correction (Rectangle.cpp:139-155 and :183-204; the reference's fixed
+// 12-entry interpolation matrix, Rectangle.cpp:76-89).  rel_shared forms what all
+// sub-cells share — f3, the interpolation coefficients, the correction cor from the sum
+// over every sub-cell's value — and sub-cell k's value is rel_pick(k) + cor, in the
+// reference's operations and order.
+__device__ __forceinline__ void rel_shared(const P64 &P, const double *f, int i, int j, double &f3, double &a1,
+                                           double &a2, double &a3, double &cor) {
     const int pit = P.pitch;
-    const double f3 = f[pidx(i, j, pit)];
-    // With one sub-cell every weight is exactly zero and the correction vanishes.
-    if (P.rtb == 1) return f3;
+    f3 = f[pidx(i, j, pit)];
     const double m0 = 0.104166666666667, m1 = -0.708333333333334, m2 = 0.708333333333334, m3 = -0.104166666666667;
     const double m4 = 0.117647058823529, m5 = 0.029411764705882, m6 = 0.029411764705882, m7 = 0.117647058823529;
     const double m8 = -0.083333333333333, m9 = 0.166666666666667, m10 = -0.166666666666667, m11 = 0.083333333333334;
@@ -29,17 +31,18 @@ __device__ __forceinline__ double rel_value(const P64 &P, const double *f, int i
     double g2 = f[pidx(i - 1, j, pit)] - f3;
     double g4 = f[pidx(i + 1, j, pit)] - f3;
     double g5 = f[pidx(i + 2, j, pit)] - f3;
-    double a1 = m0 * g1 + m1 * g2 + m2 * g4 + m3 * g5;
-    double a2 = m4 * g1 + m5 * g2 + m6 * g4 + m7 * g5;
-    double a3 = m8 * g1 + m9 * g2 + m10 * g4 + m11 * g5;
-    double te = 0.0, mine = 0.0;
+    a1 = m0 * g1 + m1 * g2 + m2 * g4 + m3 * g5;
+    a2 = m4 * g1 + m5 * g2 + m6 * g4 + m7 * g5;
+    a3 = m8 * g1 + m9 * g2 + m10 * g4 + m11 * g5;
+    double te = 0.0;
     for (int q = 0; q < P.rtb; q++) {
         double v = P.relc[3 * q] * a1 + P.relc[3 * q + 1] * a2 + P.relc[3 * q + 2] * a3 + f3;
         te += v;
-        if (q == k) mine = v;
     }
-    double cor = f3 - (1.0 / (double)P.rtb) * te;
-    return mine + cor;
+    cor = f3 - (1.0 / (double)P.rtb) * te;
+}
+__device__ __forceinline__ double rel_pick(const P64 &P, int k, double a1, double a2, double a3, double f3) {
+    return P.relc[3 * k] * a1 + P.relc[3 * k + 1] * a2 + P.relc[3 * k + 2] * a3 + f3;
 }
 
 __device__ __forceinline__ double cell_asq(const RunFields &F, int x) {
@@ -50,87 +53,105 @@ __device__ __forceinline__ double cell_asq(const RunFields &F, int x) {
     return (ay * ay) + (az * az);
 }
 
-// One warp per moment column (coarse column i, finest sub-column k), kMomCols columns of
-// one patch per block.  A warp walks p in windows of 32 lanes covering j0-1 .. j0+30:
-// every lane computes the Lorentz factor at its p-face once (shared with the
-// neighbouring face through shuffles instead of the reference's four Gamma calls per
-// cell), the log ratio
+// One warp per coarse column i, kMomCols columns of one patch per block; a warp forms
+// its column's finest sub-columns k in pairs, the f stencil and the interpolation's
+// shared part once per cell for the pair.  The warp walks p in windows of 32 lanes
+// covering j0-1 .. j0+30: every lane computes the Lorentz factor at its p-face once
+// (shared with the neighbouring face through shuffles instead of the reference's four
+// Gamma calls per cell), the log ratio
 //   L(j) = c2 * ln((g_{j+1} + c1 p_{j+1}) / (g_j + c1 p_j))
 // (the reference's gm; gm1 and gp1 are L(j-1) and L(j+1), the same expressions), the
 // interpolated f and the cell's charge/current contributions.  The window's 29
-// contributions per column then go through shared memory to warp 0, whose lane w adds
-// column w's in ascending j, which keeps the reference's accumulation order
+// contributions per sub-column then go through shared memory to warp 0, whose lanes each
+// add one sub-column's in ascending j, which keeps the reference's accumulation order
 // (Rectangle.cpp:207-255) exactly.  The serial sums thus take one FP64 warp instruction
-// per cell for kMomCols columns at once (an FP64 warp instruction occupies the
+// per cell for up to 32 sub-columns at once (an FP64 warp instruction occupies the
 // sub-partition's FP64 unit for tens of cycles whatever the number of active lanes).
-// The column list is padded per patch to a multiple of kMomCols (padding: patch -1), so
-// the warps of a block share n_p and step through the windows together.
+// The coarse-column list is padded per patch to a multiple of kMomCols (padding: patch
+// -1), so the warps of a block share n_p and rtb and step through the windows together.
 constexpr int kMomOut = 29;  // outputs per window: j0 .. j0+28
 
 __global__ void __launch_bounds__(kMomCols * 32) k64_moments(MomLaunch M) {
     VX_PDL_WAIT();
-    __shared__ double s_cc[kMomCols][32], s_cj[kMomCols][32];
+    __shared__ double s_cc[kMomCols][2][32], s_cj[kMomCols][2][32];
     __shared__ unsigned s_use[kMomCols];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int col0 = blockIdx.x * kMomCols;
-    const int cp = M.colpatch[col0 + wid];  // -1: padding
+    const bool real = M.colpatch[col0 + wid] >= 0;  // warp-uniform
     const P64 &P = ((const P64 *)M.patches)[M.colpatch[col0]];  // the block's patch
-    const int np = P.np;
-    const int c = M.colidx[col0 + wid];
-    const int i = c / P.rtb, k = c - i * P.rtb;
+    const int np = P.np, rtb = P.rtb, pit = P.pitch;
+    const int i = M.colidx[col0 + wid] / rtb;
     const RunFields &F = M.fields[P.run];
-    const double a = cp >= 0 ? P.qq * cell_asq(F, (i + P.x_pos) * P.rtb + k) : 0.0;
     const double minv = 1 / P.mass;
     const double c1 = minv * kCInv;
     const double c2 = 1 / c1;
     const double c3 = 1 / 48.0;
     const double *f = P.f1;
     const unsigned full = 0xffffffffu;
-    double ch = 0.0, cu = 0.0;  // warp 0, lane w: column w of the block
-    for (int j0 = 0; j0 < np; j0 += kMomOut) {
-        double cc = 0.0, cj = 0.0;
-        bool use = false;
-        if (cp >= 0) {  // warp-uniform
+    for (int k0 = 0; k0 < rtb; k0 += 2) {  // block-uniform
+        const int kg = rtb - k0 < 2 ? rtb - k0 : 2;
+        double a[2] = {0.0, 0.0};
+        for (int q = 0; q < kg; q++)
+            if (real) a[q] = P.qq * cell_asq(F, (i + P.x_pos) * rtb + k0 + q);
+        double ch = 0.0, cu = 0.0;  // warp 0, lane t < kMomCols * kg: sub-column t % kg of column t / kg
+        for (int j0 = 0; j0 < np; j0 += kMomOut) {
             const int j = j0 - 1 + lane;  // this lane's p index
-            double G = 0.0, V = 0.0;
-            if (j <= np + 1) {
-                double p = P.pmin + P.dp * (double)(j + P.p_pos);
-                double g = sqrt(1.0 + ((p * p) + a) * P.g2);
-                G = g + c1 * p;
-            }
-            if (j <= np) V = rel_value(P, f, i, j, k);
-            const double Gn = __shfl_down_sync(full, G, 1);
-            const double L = c2 * log(Gn / G);  // valid for lanes 0..30
-            const double Lm = __shfl_up_sync(full, L, 1);
-            const double Lp = __shfl_down_sync(full, L, 1);
-            const double Vm = __shfl_up_sync(full, V, 1);
-            const double Vp = __shfl_down_sync(full, V, 1);
-            use = lane >= 1 && lane <= kMomOut && j < np && !(P.nested && P.nested[pidx(i, j, P.pitch)]);
-            if (use) {
-                cc = V;
-                cj = V * L + c3 * (Lp - Lm) * (Vp - Vm);
-            }
-        }
-        const unsigned usemask = __ballot_sync(full, use);
-        s_cc[wid][lane] = cc;
-        s_cj[wid][lane] = cj;
-        if (lane == 0) s_use[wid] = usemask;
-        __syncthreads();
-        if (wid == 0 && lane < kMomCols) {
-            const unsigned um = s_use[lane];
-            for (int t = 1; t <= kMomOut; t++)
-                if ((um >> t) & 1u) {
-                    ch += s_cc[lane][t];
-                    cu += s_cj[lane][t];
+            double p = 0.0, f3 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0, cor = 0.0;
+            bool use = false;
+            if (real) {
+                p = P.pmin + P.dp * (double)(j + P.p_pos);
+                if (j <= np) {
+                    if (rtb == 1) f3 = f[pidx(i, j, pit)];
+                    else rel_shared(P, f, i, j, f3, a1, a2, a3, cor);
                 }
+                use = lane >= 1 && lane <= kMomOut && j < np && !(P.nested && P.nested[pidx(i, j, pit)]);
+            }
+            for (int q = 0; q < kg; q++) {
+                double cc = 0.0, cj = 0.0;
+                if (real) {
+                    double G = 0.0, V = 0.0;
+                    if (j <= np + 1) {
+                        double g = sqrt(1.0 + ((p * p) + a[q]) * P.g2);
+                        G = g + c1 * p;
+                    }
+                    if (j <= np) V = rtb == 1 ? f3 : rel_pick(P, k0 + q, a1, a2, a3, f3) + cor;
+                    const double Gn = __shfl_down_sync(full, G, 1);
+                    const double L = c2 * log(Gn / G);  // valid for lanes 0..30
+                    const double Lm = __shfl_up_sync(full, L, 1);
+                    const double Lp = __shfl_down_sync(full, L, 1);
+                    const double Vm = __shfl_up_sync(full, V, 1);
+                    const double Vp = __shfl_down_sync(full, V, 1);
+                    if (use) {
+                        cc = V;
+                        cj = V * L + c3 * (Lp - Lm) * (Vp - Vm);
+                    }
+                }
+                s_cc[wid][q][lane] = cc;
+                s_cj[wid][q][lane] = cj;
+            }
+            const unsigned usemask = __ballot_sync(full, use);
+            if (lane == 0) s_use[wid] = usemask;
+            __syncthreads();
+            if (wid == 0 && lane < kMomCols * kg) {
+                const int w = lane / kg, q = lane - w * kg;
+                const unsigned um = s_use[w];
+                for (int t = 1; t <= kMomOut; t++)
+                    if ((um >> t) & 1u) {
+                        ch += s_cc[w][q][t];
+                        cu += s_cj[w][q][t];
+                    }
+            }
+            __syncthreads();
         }
-        __syncthreads();
-    }
-    if (wid == 0 && lane < kMomCols && M.colpatch[col0 + lane] >= 0) {
-        const int cl = M.colidx[col0 + lane];
-        const double q = P.q;
-        P.chargeR[cl] = ch * (P.dp * q);
-        P.currentR[cl] = cu * (-q * q / P.mass);
+        if (wid == 0 && lane < kMomCols * kg) {
+            const int w = lane / kg, q = lane - w * kg;
+            if (M.colpatch[col0 + w] >= 0) {
+                const int cl = M.colidx[col0 + w] + k0 + q;  // i_w * rtb + k
+                const double qc = P.q;
+                P.chargeR[cl] = ch * (P.dp * qc);
+                P.currentR[cl] = cu * (-qc * qc / P.mass);
+            }
+        }
     }
 }
 
