@@ -3,6 +3,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <unordered_map>
 
 #include "engine.hpp"
@@ -154,6 +157,50 @@ struct Scheduler {
     }
 };
 
+// The same schedule for ghost-fill ops, with the last write / read batch of each cell
+// kept in dense per-patch planes (allocated when a patch is first touched) instead of a
+// hash map: the restriction ops of large nested regions number in the millions.
+struct PlaneScheduler {
+    explicit PlaneScheduler(const std::vector<Rect *> &patches) : flat(patches), last_w(patches.size()), last_r(patches.size()) {}
+    const std::vector<Rect *> &flat;
+    std::vector<std::vector<int16_t>> last_w, last_r;
+    std::vector<int> batch;
+    int nbatches = 0;
+    size_t slot(int patch, int i, int j) {
+        if (patch < 0 || patch >= (int)flat.size()) throw std::invalid_argument("AMR layout: ghost op on no patch");
+        const Rect &R = *flat[patch];
+        if (i < -2 || i >= R.n_x + 2 || j < -2 || j >= R.n_p + 2)
+            throw std::invalid_argument("AMR layout: ghost op cell outside its patch");
+        if (last_w[patch].empty()) {
+            const size_t cells = (size_t)(R.n_x + 4) * (R.n_p + 4);
+            last_w[patch].assign(cells, (int16_t)-1);
+            last_r[patch].assign(cells, (int16_t)-1);
+        }
+        return (size_t)(i + 2) * (R.n_p + 4) + (j + 2);
+    }
+    // cells as (patch, i, j) triples
+    void add(const int (*reads)[3], int nr, const int (*writes)[3], int nw) {
+        int b = 0;
+        for (int q = 0; q < nr; q++) {
+            const size_t c = slot(reads[q][0], reads[q][1], reads[q][2]);
+            b = std::max(b, last_w[reads[q][0]][c] + 1);
+        }
+        for (int q = 0; q < nw; q++) {
+            const size_t c = slot(writes[q][0], writes[q][1], writes[q][2]);
+            b = std::max(b, last_w[writes[q][0]][c] + 1);
+            b = std::max(b, last_r[writes[q][0]][c] + 1);
+        }
+        if (b > 32000) throw std::runtime_error("ghost-fill schedule too deep");
+        for (int q = 0; q < nr; q++) {
+            int16_t &v = last_r[reads[q][0]][slot(reads[q][0], reads[q][1], reads[q][2])];
+            v = (int16_t)std::max<int>(v, b);
+        }
+        for (int q = 0; q < nw; q++) last_w[writes[q][0]][slot(writes[q][0], writes[q][1], writes[q][2])] = (int16_t)b;
+        batch.push_back(b);
+        nbatches = std::max(nbatches, b + 1);
+    }
+};
+
 template <class Op>
 void sort_by_batch(std::vector<Op> &ops, const std::vector<int> &batch, int nb, Batched &out) {
     std::vector<Op> sorted;
@@ -212,6 +259,14 @@ void Run::validate_ops() const {
 void Run::build_amr() {
     const int r = S->refinementRatio;
     const int L = S->maxDepth + 1;
+    static const bool trace = std::getenv("VX_TRACE_INIT") != nullptr;
+    auto t0 = std::chrono::steady_clock::now();
+    auto lap = [&](const char *what) {
+        if (!trace) return;
+        auto t1 = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "vx amr %-15s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(t1 - t0).count());
+        t0 = t1;
+    };
     flat.clear();
     int nrect = 0;
     for (auto &sp : rects)
@@ -237,6 +292,7 @@ void Run::build_amr() {
                 R.ifp.assign(cells, 0);
             }
     multi_patch = nrect > (int)rects.size();
+    lap("cell arrays");
     // Mesh::promoteHierarchyToMesh (Mesh.cpp:839-859): finer links first, then same level.
     for (auto &sp : rects) {
         for (int l = 0; l < L; l++)
@@ -249,21 +305,23 @@ void Run::build_amr() {
                     if (rl != rr) conn_same(*rl, *rr, r);
     }
 
+    lap("links");
     // ------------------------------------------------------------ ghost fills
     ghost_ops.clear();
-    Scheduler gs;
-    auto cellkey = [&](int patch, int i, int j) { return Scheduler::key(patch, 0, i, j); };
+    PlaneScheduler gs(flat);
     auto emit = [&](const GhostOp &op) {
-        std::vector<uint64_t> reads, writes{cellkey(op.dst, op.di, op.dj)};
-        if (op.kind == kGhostCopy) reads.push_back(cellkey(op.src, op.si, op.sj));
-        else if (op.kind == kGhostRestrict) {
+        int reads[64][3], writes[1][3] = {{op.dst, op.di, op.dj}};  // r <= 8: at most 64 reads
+        int nr = 0;
+        if (op.kind == kGhostCopy) {
+            reads[nr][0] = op.src, reads[nr][1] = op.si, reads[nr][2] = op.sj, nr++;
+        } else if (op.kind == kGhostRestrict) {
             for (int a = 0; a < r; a++)
-                for (int b = 0; b < r; b++) reads.push_back(cellkey(op.src, op.si + a, op.sj + b));
+                for (int b = 0; b < r; b++) reads[nr][0] = op.src, reads[nr][1] = op.si + a, reads[nr][2] = op.sj + b, nr++;
         } else if (op.kind == kGhostInterp) {
             for (int a = -2; a <= 2; a++)
-                for (int b = -2; b <= 2; b++) reads.push_back(cellkey(op.src, op.si + a, op.sj + b));
+                for (int b = -2; b <= 2; b++) reads[nr][0] = op.src, reads[nr][1] = op.si + a, reads[nr][2] = op.sj + b, nr++;
         }
-        gs.add(reads, writes);
+        gs.add(reads, nr, writes, 1);
         ghost_ops.push_back(op);
     };
     // value of global cell (gx, gp) of same-level patch `id` (BoundaryCondition: zero)
@@ -430,6 +488,7 @@ void Run::build_amr() {
         for (int i = L - 1; i > 0; i--) type2(sp[i - 1]);
     }
     sort_by_batch(ghost_ops, gs.batch, gs.nbatches, ghost_b);
+    lap("ghost ops");
 
     // ------------------------------------------------------------ interface fluxes
     iface_ops.clear();
@@ -455,6 +514,7 @@ void Run::build_amr() {
                     }
             }
     sort_by_batch(iface_ops, ib, inb, iface_b);
+    lap("iface ops");
 
     // ------------------------------------------------------------ limiter C exchange
     csync_ops.clear();
@@ -521,6 +581,7 @@ void Run::build_amr() {
     }
     sort_by_batch(csync_ops, cs.batch, cs.nbatches, csync_b);
     validate_ops();
+    lap("csync ops");
 
     // ------------------------------------------------------------ device masks, weights
     for (Rect *R : flat) {
@@ -536,6 +597,7 @@ void Run::build_amr() {
         R->masks = DevBuf(m.size());
         VX_CUDA(cudaMemcpy(R->masks.p, m.data(), m.size(), cudaMemcpyHostToDevice));
     }
+    lap("masks");
     std::vector<double> w;
     relc_off.assign(L, 0);
     for (int d = 0; d < L; d++) {

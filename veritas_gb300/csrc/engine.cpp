@@ -1,3 +1,7 @@
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+
 #include "engine.hpp"
 
 #include <algorithm>
@@ -327,16 +331,29 @@ void Run::upload_lu() {
 // every new patch set from the quadrature.  Then the field solver and neutralisation.
 void Run::init() {
     const Settings &s = *S;
+    // VX_TRACE_INIT=1: wall time of each phase on stderr (serving diagnostics)
+    static const bool trace = std::getenv("VX_TRACE_INIT") != nullptr;
+    auto t0 = std::chrono::steady_clock::now();
+    auto lap = [&](const char *what) {
+        if (!trace) return;
+        eng.sync();
+        auto t1 = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "vx init %-14s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(t1 - t0).count());
+        t0 = t1;
+    };
     std::vector<std::vector<BoxList>> hier(rects.size());
     for (size_t sp = 0; sp < rects.size(); sp++)
         hier[sp] = {BoxList{{{0, 0}, {s.GetXSize(s.maxDepth), s.GetPSize(s.maxDepth, (int)sp)}}}};
     promote(hier, true);
+    lap("base patch");
     for (int i = 0; i < s.maxDepth; i++) {
         push_data(1);
         regrid(true);
+        lap("regrid round");
     }
     alloc_fields();
     push_data(1);
+    lap("fields");
     if (precision == kF32) poisson = kPoissonScan;
     if (poisson == kPoissonScan) {
         build_poisson_fast();
@@ -345,8 +362,10 @@ void Run::init() {
         if (info) throw std::runtime_error("Poisson operator is singular");
         upload_lu();
     }
+    lap("poisson setup");
     layout_version++;
     enforce_neutralization();
+    lap("neutralisation");
 }
 
 // EMFieldSolver::EnforceChargeNeutralization (EMSolver.cpp:621-629):

@@ -14,6 +14,10 @@
 #include <iterator>
 #include <tuple>
 
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+
 #include "engine.hpp"
 
 namespace vx {
@@ -369,7 +373,16 @@ std::vector<Run::BoxList> Run::hierarchy_of(int sp) const {
 void Run::regrid(bool init) {
     const Settings &s = *S;
     if (s.maxDepth == 0) return;
+    static const bool trace = std::getenv("VX_TRACE_INIT") != nullptr;
+    auto t0 = std::chrono::steady_clock::now();
+    auto lap = [&](const char *what) {
+        if (!trace) return;
+        auto t1 = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "vx regrid %-12s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(t1 - t0).count());
+        t0 = t1;
+    };
     auto flags = flag_cells();
+    lap("flags");
     std::vector<std::vector<BoxList>> hier(rects.size());
     for (size_t sp = 0; sp < rects.size(); sp++) {
         auto level_flags = [&](int l) {  // Mesh::getError(l, false)
@@ -382,7 +395,9 @@ void Run::regrid(bool init) {
         };
         hier[sp] = update_hierarchy(s, (int)sp, hierarchy_of((int)sp), level_flags);
     }
+    lap("clustering");
     promote(hier, init);
+    lap("promote");
 }
 
 // Mesh::promoteHierarchyToMesh (Mesh.cpp:792-880) for all species at once (the species
@@ -391,6 +406,15 @@ void Run::regrid(bool init) {
 // and f0 = f1.
 void Run::promote(const std::vector<std::vector<BoxList>> &hier, bool init) {
     const Settings &s = *S;
+    static const bool trace = std::getenv("VX_TRACE_INIT") != nullptr;
+    auto t0 = std::chrono::steady_clock::now();
+    auto lap = [&](const char *what) {
+        if (!trace) return;
+        eng.sync();
+        auto t1 = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "vx promote %-11s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(t1 - t0).count());
+        t0 = t1;
+    };
     auto old = std::move(rects);
     rects.clear();
     rects.resize(old.size());
@@ -415,15 +439,19 @@ void Run::promote(const std::vector<std::vector<BoxList>> &hier, bool init) {
             rects[sp][g.depth].push_back(std::move(r));
         }
     }
+    lap("allocate");
     build_amr();
+    lap("connectivity");
     for (Rect *R : flat) upload_rect_desc(*R, 0);
     if (init) {
         for (Rect *R : flat) init_rect_distribution(*R);
     } else {
         transfer_from(old);
     }
+    lap(init ? "quadrature" : "transfer");
     push_data(1);
     copy_slot(1, 0);
+    lap("ghosts");
     layout_version++;
 }
 
