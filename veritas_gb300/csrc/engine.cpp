@@ -655,7 +655,14 @@ LaunchSet &Engine::get_set(const std::vector<Run *> &set) {
     auto L = std::make_unique<LaunchSet>();
     L->runs = set;
     L->key_version = ver;
+    static const bool trace = std::getenv("VX_TRACE_INIT") != nullptr;
+    const auto t0 = std::chrono::steady_clock::now();
     build_set(*L);
+    if (trace) {
+        sync();
+        std::fprintf(stderr, "vx launch set of %zu runs: %8.2f ms\n", set.size(),
+                     std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+    }
     LaunchSet &ref = *L;
     sets_[set] = std::move(L);
     return ref;
