@@ -600,6 +600,20 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     pl.maxn = L.maxn;
     pl.stream = stream;
     time_it([&] { run_poisson(L, pl); });
+    // VX_TRACE_POISSON=1 (LU solve): clock64 at each chunk end of both sweeps, on stderr
+    if (std::getenv("VX_TRACE_POISSON") && L.poisson == kPoissonLU) {
+        const int nch = (L.maxn + kPoisRowsHost - 1) / kPoisRowsHost;
+        DevBuf tr((size_t)(2 * nch + 2) * sizeof(unsigned long long));
+        pl.trace = tr.as<unsigned long long>();
+        run_poisson(L, pl);
+        sync();
+        std::vector<unsigned long long> h(2 * nch + 1);
+        VX_CUDA(cudaMemcpy(h.data(), tr.p, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        std::fprintf(stderr, "vx poisson n=%d chunks=%d forward %llu cycles, backward %llu cycles\n", L.maxn, nch,
+                     h[nch] - h[0], h[2 * nch] - h[nch]);
+        for (int c = 0; c < 2 * nch; c++) std::fprintf(stderr, "  chunk %d: %llu\n", c, h[c + 1] - h[c]);
+        pl.trace = nullptr;
+    }
     MaxwellLaunch mx{};
     mx.fields = L.dfields.as<RunFields>();
     mx.nruns = 1;

@@ -231,7 +231,7 @@ __device__ __forceinline__ double efield_at(const double *phi, int n, double fco
 // after each chunk the whole block checks every quotient against the IEEE quotient and
 // the chunk is redone with IEEE division if any differs, so the result is always the
 // dgetrs rounding.
-constexpr int kPoisRows = 256;               // rows per chunk
+constexpr int kPoisRows = kPoisRowsHost;     // rows per chunk
 constexpr int kPoisLA = 4;                   // look-ahead rows staged with each chunk
 constexpr int kPoisBuf = kPoisRows + kPoisLA;
 constexpr int kPoisFar = 2048;               // far entries per staged chunk
@@ -413,7 +413,10 @@ __device__ void pois_bwd_chunk(PoisBandChunk &B, const BandFactor &F, int r0, in
 // no branch depends on the lane, so a row costs about 25 warp instructions.
 __device__ void pois_fwd_fast(const PoisBandChunk &B, const BandFactor &F, int r0, int cnt, int n, double *x,
                               double &V, double &w1) {
-    const unsigned full = 0xffffffffu;
+    // Only lanes 0..7 (band lanes 0..3, accumulator lanes 4..7) run the recurrence: the
+    // dependent latency of an FP64 warp instruction grows with its active lanes on this
+    // part, so the chain's multiply-subtract runs on eight lanes, not 32.
+    constexpr unsigned act = 0xffu;
     const int lane = threadIdx.x & 31;
     const int slot = lane - 4;
     const bool is_slot = slot >= 0 && slot < F.nslots;
@@ -422,6 +425,7 @@ __device__ void pois_fwd_fast(const PoisBandChunk &B, const BandFactor &F, int r
     __shared__ double zero_stream[1];
     if (lane == 0) zero_stream[0] = 0.0;
     __syncwarp();
+    if (lane >= 8) return;
     const double *cp;
     int cstep = 1;
     if (lane < 4) cp = &B.c[lane][k0 + lane];
@@ -446,9 +450,9 @@ __device__ void pois_fwd_fast(const PoisBandChunk &B, const BandFactor &F, int r
         const int tk = B.take[k0 + q];
         const double fb = (lane == 3 && i + 4 < n) ? x[i + 4] : 0.0;
         const double nv = V - w1 * coef;
-        const double xi = __shfl_sync(full, nv, 0);
-        const int src = (lane == 3 && tk >= 0) ? 4 + tk : base_src;
-        const double sh = __shfl_sync(full, nv, src);
+        const double xi = __shfl_sync(act, nv, 0, 8);
+        const int src = (lane == 3 && tk >= 0) ? 4 + tk : base_src;  // tk < kMaxSlots = 4
+        const double sh = __shfl_sync(act, nv, src, 8);
         V = (lane == 3 && tk < 0) ? fb : sh;
         if (lane == 0) x[i] = xi;
         w1 = xi;
@@ -456,36 +460,36 @@ __device__ void pois_fwd_fast(const PoisBandChunk &B, const BandFactor &F, int r
 }
 
 __device__ void pois_bwd_fast(PoisBandChunk &B, int r0, int cnt, double *x, double &V, double &w1) {
-    const unsigned full = 0xffffffffu;
+    // Lanes 0..3 run the multiply-subtract and lane 0 alone the quotient (see
+    // pois_fwd_fast on active lanes); the other lanes leave V and w1 unused.
+    constexpr unsigned act = 0xfu;
     const int lane = threadIdx.x & 31;
-    const int L = lane < 4 ? lane : 3;
+    if (lane >= 4) return;
+    const int L = lane;
     const int kl = r0 + cnt - 1 - B.a;  // buffer row of the chunk's last (first processed) row
     const double *cp = &B.c[L][kl - L];
-    const double *up_ = &B.diag[kl];
     const double *yp = &B.rdiag[kl];
     const double *lp = &B.rdlo[kl];
-    const int lim = r0 + cnt - 1 - L;  // row i - L < 0 when i < L
     for (int qq = cnt - 1; qq >= 0; qq--) {
         const int i = r0 + qq;
         double coef = *cp--;
         if (i - L < 0) coef = 0.0;
         const double y = *yp--, ylo = *lp--;
-        up_--;
         const double fb = (lane == 3 && i - 4 >= 0) ? x[i - 4] : 0.0;
         const double nv = V - w1 * coef;
-        const double up = __shfl_down_sync(full, nv, 1);
+        const double up = __shfl_down_sync(act, nv, 1, 4);
         // quotient from the reciprocal split into high and low parts: within 2^-105 of
         // nv/u before the final rounding; the chunk check catches the rare wrong rounding
-        const double q1 = __fma_rn(nv, y, __dmul_rn(nv, ylo));
-        const double xi = __shfl_sync(full, q1, 0);
+        double q1 = 0.0;
         if (lane == 0) {
+            q1 = __fma_rn(nv, y, __dmul_rn(nv, ylo));
             B.num[qq] = nv;
-            x[i] = xi;
+            x[i] = q1;
         }
+        const double xi = __shfl_sync(act, q1, 0, 4);
         V = (lane == 3) ? fb : up;
         w1 = xi;
     }
-    (void)lim;
 }
 
 constexpr int kPoisSmemMaxN = 16384;  // solution vector kept in shared memory up to this n
@@ -512,6 +516,8 @@ __global__ void k_poisson(PoissonLaunch L) {
     // Row interchanges of dgetrs applied as one gather: b'[k] = b[perm[k]].
     for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = tmp[lu.perm[k]];
     const int nchunks = (n + kPoisRows - 1) / kPoisRows;
+    unsigned long long *trace = (L.trace && run == 0 && threadIdx.x == 0) ? L.trace : nullptr;
+    if (trace) trace[0] = clock64();
     const int lane = threadIdx.x & 31;
     // ---- forward: rows ascending; chunk c stages rows [c*R, c*R + R + LA)
     {
@@ -539,6 +545,7 @@ __global__ void k_poisson(PoissonLaunch L) {
             }
             fit_cur = fit_next;
             __syncthreads();
+            if (trace) trace[1 + c] = clock64();
         }
     }
     // ---- backward: rows descending; chunk c stages rows [c*R - LA, c*R + R)
@@ -599,6 +606,7 @@ __global__ void k_poisson(PoissonLaunch L) {
             fit_cur = fit_next;
             parity ^= 1;
             __syncthreads();
+            if (trace) trace[1 + nchunks + (clast - c)] = clock64();
         }
     }
     if (in_smem)

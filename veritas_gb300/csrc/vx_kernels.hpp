@@ -142,9 +142,11 @@ struct PoissonLaunch {
     int nruns;
     int maxn;
     int x_in_smem;  // set by launch_poisson
+    unsigned long long *trace;  // optional: clock64 at the solve's phase and chunk ends (run 0)
     cudaStream_t stream;
 };
 void launch_poisson(const PoissonLaunch &L);
+constexpr int kPoisRowsHost = 256;  // rows per chunk of k_poisson (fields64.cu kPoisRows)
 
 // O(n) Poisson solve by prefix scans, one thread-block cluster per run (poisson_scan.cu).
 // Y holds the m x 3 Woodbury columns (row-major), K the 3x3 capacitance factor.
