@@ -65,6 +65,9 @@ typedef struct vx_problem {
                         * thread-block cluster (not the LU's rounding: about 4e-11 relative
                         * from it at n = 8192, growing as n^2 with the LU's own error).
                         * Precision-32 runs always use 1. */
+    double mi, iTe, ipmax; /* mobile ions (second species) when mi > 0: mass mi m_e, charge
+                            * +e, the electrons' density, temperature iTe [keV], momenta in
+                            * [-ipmax, ipmax] m_i c */
 } vx_problem;
 
 /* Fills *p with the defaults of the 2048 x 256 single-level laser/slab case. */

@@ -86,6 +86,7 @@ struct Problem {
     double a0 = 1.0, fwhm = 10.0, delay = 10.0;      // laser [periods]
     double cfl = 0.5, minEff = 0.75, crit = 1e-6, sizeWeight = 1.0;
     int quadDepth = 2;
+    double mi = 0.0, iTe = 1.0, ipmax = 0.1;          // mobile ions when mi > 0 (mass / m_e, keV, m_i c)
 };
 static Problem P;
 static double beam_T = 0.0, beam_p = 0.0;
@@ -123,6 +124,14 @@ void initialConditions(Input &grid, Particles &particles, Output &output) {
     particles.np = {P.np};
     particles.dp = {0.1};
     particles.pmin = {0.0};
+    if (P.mi > 0.0) {  // mobile ions: second species
+        particles.mass.push_back(P.mi * kMe);
+        particles.charge.push_back(-kQe);
+        particles.misc.push_back({0.0, 0.0});
+        particles.np.push_back(P.np);
+        particles.dp.push_back(0.1);
+        particles.pmin.push_back(0.0);
+    }
     output.time = false;
     output.rectangleData = false;
     output.charge = false;
@@ -153,6 +162,15 @@ void Settings::settingsOverride() {
     tempEM[1] = P.a0 * mc / std::fabs(q[0]);
     beam_T = m[0] * (P.bTe * kKeV);
     beam_p = P.bp0 * mc;
+    if (m.size() > 1) {
+        double mci = m[1] * cs;
+        dp[1] = 2.0 * P.ipmax * mci / p_size[1];
+        pmin[1] = -P.ipmax * mci;
+        temp[1].resize(3, 0.0);
+        temp[1][0] = P.dens * Nc;
+        temp[1][1] = m[1] * (P.iTe * kKeV);
+        temp[1][2] = 0.0;
+    }
 }
 
 bool Settings::RefinementOverride(double x, double p, int depth, int particleType) {
@@ -180,7 +198,7 @@ double Settings::InitialDistribution(double x, double p, int particleType) {
     double ne = temp[particleType][0] * slab_density(x / P.lambda);
     double dpv = p - temp[particleType][2];
     double v = ne * std::exp(-(dpv * dpv) / (2.0 * temp[particleType][1])) / std::sqrt(DPI * temp[particleType][1]);
-    if (P.bdens != 0.0) {
+    if (P.bdens != 0.0 && particleType == 0) {  // drifting electron population
         double dbv = p - beam_p;
         v += P.bdens * ne * std::exp(-(dbv * dbv) / (2.0 * beam_T)) / std::sqrt(DPI * beam_T);
     }
@@ -300,6 +318,9 @@ int main(int argc, char **argv) {
     P.crit = getd("crit", P.crit);
     P.sizeWeight = getd("sizeWeight", P.sizeWeight);
     P.quadDepth = (int)geti("quadDepth", P.quadDepth);
+    P.mi = getd("mi", P.mi);
+    P.iTe = getd("iTe", P.iTe);
+    P.ipmax = getd("ipmax", P.ipmax);
     long long steps = geti("steps", 0);
     long long dump_every = geti("dump_every", 0);
     long long regrid_every = geti("regrid_every", 0);

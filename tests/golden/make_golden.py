@@ -47,6 +47,10 @@ CASES = {
     "beam3": (["L=8", "nx=64", "np=32", "Te=1", "pmax=2", "x1=1.5", "x2=2", "x3=6", "x4=6.5", "pert_amp=0.2",
                "pert_k=2", "a0=2", "fwhm=2", "delay=1", "bdens=0.5", "bp0=-1.2", "bTe=1", "crit=1e-3",
                "minEff=0.9", "levels=3"], 3, [0, 1, 3]),
+    # Electrons and mobile ions (mass 4 m_e, charge +e): two species, each with its own
+    # two-level hierarchy; moments, Poisson and CFL sum over both.
+    "ions2": (["L=8", "nx=64", "np=32", "Te=50", "pmax=2", "x1=1.5", "x2=2", "x3=6", "x4=6.5", "pert_amp=0.2",
+               "pert_k=2", "a0=2", "fwhm=2", "delay=1", "mi=4", "iTe=50", "ipmax=0.6", "levels=2"], 3, [0, 1, 3]),
 }
 
 
@@ -54,6 +58,7 @@ CASES = {
 # SolverManager::reGrid ("_pre"), just after it ("_post") and one step later ("_post1").
 REGRID = {
     "amr2": 4,
+    "ions2": 4,
     "beam2": 4,
     "beam3": 4,
 }
@@ -83,13 +88,18 @@ def run_regrid(exe: Path, name: str, args: list[str], every: int) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", action="append", default=[], help="regenerate only these cases")
     a = ap.parse_args()
     subprocess.run(["bash", str(REPO / "oracle" / "ref" / "build_ref.sh"), a.ref], check=True)
     exe = REPO / "oracle" / "_ref" / "veritas_ref"
     for name, (args, steps, keep) in CASES.items():
+        if a.only and name not in a.only:
+            continue
         run_case(exe, name, args, steps, keep)
         print("wrote", name)
     for name, every in REGRID.items():
+        if a.only and name not in a.only:
+            continue
         run_regrid(exe, name, CASES[name][0], every)
         print("wrote", name, "regrid")
 

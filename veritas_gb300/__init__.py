@@ -48,6 +48,7 @@ class _Problem(ctypes.Structure):
         ("quadDepth", ctypes.c_int32), ("precision", ctypes.c_int32),
         ("bdens", ctypes.c_double), ("bp0", ctypes.c_double), ("bTe", ctypes.c_double),
         ("poisson", ctypes.c_int32),
+        ("mi", ctypes.c_double), ("iTe", ctypes.c_double), ("ipmax", ctypes.c_double),
     ]
 
 
@@ -163,6 +164,9 @@ class Problem:
     bp0: float = 0.0
     bTe: float = 1.0
     poisson: int = 0  # precision-64 runs: 0 the reference's LU rounding order, 1 the O(n) scan solve
+    mi: float = 0.0     # mobile ions (second species) when > 0: mass / m_e
+    iTe: float = 1.0    # ion temperature [keV]
+    ipmax: float = 0.1  # ion momenta in [-ipmax, ipmax] m_i c
 
     def to_c(self) -> _Problem:
         p = _Problem()
@@ -173,7 +177,8 @@ class Problem:
     def harness_args(self) -> list[str]:
         """key=value arguments of the oracle harness for the same problem."""
         keys = ["L", "nx", "np", "r", "pmax", "dens", "x1", "x2", "x3", "x4", "Te", "p0", "pert_amp", "pert_k",
-                "a0", "fwhm", "delay", "cfl", "minEff", "crit", "sizeWeight", "quadDepth", "bdens", "bp0", "bTe"]
+                "a0", "fwhm", "delay", "cfl", "minEff", "crit", "sizeWeight", "quadDepth", "bdens", "bp0", "bTe",
+                "mi", "iTe", "ipmax"]
         out = [f"{k}={getattr(self, k)!r}" for k in keys]
         out.append(f"levels={self.Lfinest}")
         return out

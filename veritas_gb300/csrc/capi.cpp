@@ -70,6 +70,9 @@ vx::LaserSlabParams to_params(const vx_problem &p) {
     q.bdens = p.bdens;
     q.bp0 = p.bp0;
     q.bTe = p.bTe;
+    q.mi = p.mi;
+    q.iTe = p.iTe;
+    q.ipmax = p.ipmax;
     return q;
 }
 
@@ -123,6 +126,9 @@ void vx_problem_defaults(vx_problem *p) {
     p->bp0 = d.bp0;
     p->bTe = d.bTe;
     p->poisson = 0;
+    p->mi = d.mi;
+    p->iTe = d.iTe;
+    p->ipmax = d.ipmax;
 }
 
 const char *vx_last_error(void) { return g_err.c_str(); }

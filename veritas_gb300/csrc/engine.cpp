@@ -198,7 +198,7 @@ void Run::init_rect_distribution(Rect &r) {
         // same sample points, summed as (sum_k density)(sum_l profile)
         std::vector<double> dx_sum(r.n_x, 0.0), dp_sum(r.n_p, 0.0);
         for (int i = 0; i < r.n_x; i++)
-            for (int k = 0; k < nvals; k++) dx_sum[i] += s.problem->Density(s, ((0.5 + k) / nvals + i + r.x_pos) * dx);
+            for (int k = 0; k < nvals; k++) dx_sum[i] += s.problem->Density(s, ((0.5 + k) / nvals + i + r.x_pos) * dx, r.species);
         for (int j = 0; j < r.n_p; j++)
             for (int l = 0; l < nvals; l++)
                 dp_sum[j] += s.problem->Profile(s, pmin + dp * ((0.5 + l) / nvals + j + r.p_pos), r.species);

@@ -96,6 +96,14 @@ void LaserSlab::initialConditions(Input &grid, Particles &particles, Output &out
     particles.np = {P.np};
     particles.dp = {0.1};
     particles.pmin = {0.0};
+    if (P.mi > 0.0) {  // mobile ions
+        particles.mass.push_back(P.mi * kMe);
+        particles.charge.push_back(-kQe);
+        particles.misc.push_back({0.0, 0.0});
+        particles.np.push_back(P.np);
+        particles.dp.push_back(0.1);
+        particles.pmin.push_back(0.0);
+    }
     output = Output();
 }
 
@@ -117,6 +125,15 @@ void LaserSlab::settingsOverride(Settings &s) {
     s.tempEM[1] = P.a0 * mc / std::fabs(s.q[0]);
     beam_T = s.m[0] * (P.bTe * kKeV);
     beam_p = P.bp0 * mc;
+    if (s.m.size() > 1) {  // ions: same density, own temperature and momentum range
+        double mci = s.m[1] * kCs;
+        s.dp[1] = 2.0 * P.ipmax * mci / s.p_size[1];
+        s.pmin[1] = -P.ipmax * mci;
+        s.temp[1].resize(3, 0.0);
+        s.temp[1][0] = P.dens * Nc;
+        s.temp[1][1] = s.m[1] * (P.iTe * kKeV);
+        s.temp[1][2] = 0.0;
+    }
 }
 
 double LaserSlab::slab_density(double xl) const {
@@ -133,19 +150,21 @@ double LaserSlab::InitialDistribution(const Settings &s, double x, double p, int
     double ne = s.temp[particleType][0] * slab_density(x / P.lambda);
     double dpv = p - s.temp[particleType][2];
     double v = ne * std::exp(-(dpv * dpv) / (2.0 * s.temp[particleType][1])) / std::sqrt(kDPI * s.temp[particleType][1]);
-    if (P.bdens != 0.0) {  // second, drifting population with its own temperature
+    if (P.bdens != 0.0 && particleType == 0) {  // drifting electron population, own temperature
         double dbv = p - beam_p;
         v += P.bdens * ne * std::exp(-(dbv * dbv) / (2.0 * beam_T)) / std::sqrt(kDPI * beam_T);
     }
     return v;
 }
 
-double LaserSlab::Density(const Settings &s, double x) const { return s.temp[0][0] * slab_density(x / P.lambda); }
+double LaserSlab::Density(const Settings &s, double x, int particleType) const {
+    return s.temp[particleType][0] * slab_density(x / P.lambda);
+}
 
 double LaserSlab::Profile(const Settings &s, double p, int particleType) const {
     double dpv = p - s.temp[particleType][2];
     double v = std::exp(-(dpv * dpv) / (2.0 * s.temp[particleType][1])) / std::sqrt(kDPI * s.temp[particleType][1]);
-    if (P.bdens != 0.0) {
+    if (P.bdens != 0.0 && particleType == 0) {
         double dbv = p - beam_p;
         v += P.bdens * std::exp(-(dbv * dbv) / (2.0 * beam_T)) / std::sqrt(kDPI * beam_T);
     }

@@ -53,7 +53,7 @@ public:
     // Optional: f(x, p) = density(x) * profile(p).  A problem that says so lets the FP32
     // form integrate the initial cell averages as a product of two 1-D quadratures.
     virtual bool Separable() const { return false; }
-    virtual double Density(const Settings &, double) const { return 0.0; }
+    virtual double Density(const Settings &, double, int) const { return 0.0; }
     virtual double Profile(const Settings &, double, int) const { return 0.0; }
 };
 
@@ -73,6 +73,9 @@ struct LaserSlabParams {
     double cfl = 0.5, minEff = 0.75, crit = 1e-6, sizeWeight = 1.0;
     int quadDepth = 2;
     double bdens = 0.0, bp0 = 0.0, bTe = 1.0;  // beam population: density fraction, drift, keV
+    // mobile ions (second species) when mi > 0: charge +e, mass mi m_e, the electrons'
+    // density profile, temperature iTe [keV], p in [-ipmax, ipmax] m_i c
+    double mi = 0.0, iTe = 1.0, ipmax = 0.1;
 };
 
 class LaserSlab : public Problem {
@@ -88,7 +91,7 @@ public:
     }
     bool HasRefinementOverride() const override { return false; }
     bool Separable() const override { return true; }
-    double Density(const Settings &s, double x) const override;
+    double Density(const Settings &s, double x, int particleType) const override;
     double Profile(const Settings &s, double p, int particleType) const override;
     double slab_density(double xl) const;
     LaserSlabParams P;
