@@ -85,7 +85,10 @@ __global__ void k_ghost(const PatchT<T> *patches, const GhostOp *ops, int n, int
         T t = 0;
         for (int a = 0; a < r; a++)
             for (int b = 0; b < r; b++) t += f[pidx(op.si + a, op.sj + b, S.pitch)];
-        t /= (T)(r * r);  // std::pow(r, 2.0) of the reference, an exact integer
+        // std::pow(r, 2.0) of the reference, an exact integer; for a power of two the
+        // product with its exact reciprocal is the same correctly rounded value
+        if ((r & (r - 1)) == 0) t *= (T)(1.0 / (double)(r * r));
+        else t /= (T)(r * r);
         v = t;
     } else if (op.kind == kGhostInterp) {
         const PatchT<T> &S = patches[op.src];

@@ -588,6 +588,7 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     al.run_nl = L.drun_nl.as<int>();
     al.nruns = 1;
     al.maxn = L.maxn;
+    al.pairs = L.precision == kF32 ? 1 : 0;
     al.fields = L.dfields.as<RunFields>();
     al.stream = stream;
     time_it([&] { launch_assemble(al); });
@@ -929,6 +930,7 @@ void Engine::record_step(LaunchSet &L) {
     al.run_nl = L.drun_nl.as<int>();
     al.nruns = (int)L.runs.size();
     al.maxn = L.maxn;
+    al.pairs = L.precision == kF32 ? 1 : 0;
     al.fields = L.dfields.as<RunFields>();
     al.stream = stream;
     PoissonLaunch pl{};
@@ -1162,6 +1164,7 @@ void Engine::moments_only(const std::vector<Run *> &set) {
     al.run_nl = L.drun_nl.as<int>();
     al.nruns = (int)L.runs.size();
     al.maxn = L.maxn;
+    al.pairs = L.precision == kF32 ? 1 : 0;
     al.fields = L.dfields.as<RunFields>();
     al.stream = stream;
     launch_assemble(al);

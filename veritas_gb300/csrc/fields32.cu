@@ -151,16 +151,18 @@ __device__ __forceinline__ void moments_group(const P32 &P, const RunFields &F, 
         const F2 cu = f2_warp_sum(F2{cus[q], -cuc[q]});
         if (lane == 0) {
             const int c = i * rtb + k0 + q;
-            P.chargeR[c] = ((double)ch.hi + (double)ch.lo) * P.msc_rho;
-            P.currentR[c] = ((double)cu.hi + (double)cu.lo) * P.msc_j;
+            // the column sum as an FP32 pair in the column's double slot; k_assemble forms
+            // the FP64 value and applies the scale (no FP64 instruction here)
+            reinterpret_cast<float2 *>(P.chargeR)[c] = make_float2(ch.hi, ch.lo);
+            reinterpret_cast<float2 *>(P.currentR)[c] = make_float2(cu.hi, cu.lo);
         }
     }
 }
 
 // One warp per coarse column (M.colidx holds i * rtb, the column's first finest
-// sub-column).  No FP64 instruction per cell or per lane: the A^2 of each sub-column comes
-// from the FP32 per-cell copy, the weights and the final scales from the patch
-// descriptor; one lane converts the reduced pairs to FP64.
+// sub-column).  No FP64 instruction: the A^2 of each sub-column comes from the FP32
+// per-cell copy, the weights from the patch descriptor; the reduced pairs go to the
+// assembly, which scales them in FP64.
 __global__ void k32_moments(MomLaunch M) {
     VX_PDL_WAIT();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;

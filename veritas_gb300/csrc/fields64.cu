@@ -185,8 +185,15 @@ __global__ void k_assemble(AsmLaunch A) {
                 const P64 &P = patches[A.lvl_patch[e]];
                 int c = x - P.x_pos * P.rtb;
                 if (c >= 0 && c < P.nx * P.rtb) {
-                    lc += P.chargeR[c];
-                    lj += P.currentR[c];
+                    if (A.pairs) {  // FP32 moments: (hi, lo) of the column sum, then its scale
+                        const float2 qc = reinterpret_cast<const float2 *>(P.chargeR)[c];
+                        const float2 qj = reinterpret_cast<const float2 *>(P.currentR)[c];
+                        lc += ((double)qc.x + (double)qc.y) * P.msc_rho;
+                        lj += ((double)qj.x + (double)qj.y) * P.msc_j;
+                    } else {
+                        lc += P.chargeR[c];
+                        lj += P.currentR[c];
+                    }
                 }
             }
             cs += lc;

@@ -106,6 +106,7 @@ struct AsmLaunch {
     const int *run_ns;     // per run: species count
     const int *run_nl;     // per run: level count
     int nruns, maxn;
+    int pairs;             // FP32 sets: a column holds its unscaled sum as an FP32 pair
     RunFields *fields;
     cudaStream_t stream;
 };
