@@ -21,7 +21,7 @@
 // Command line: the parity harness's key=value problem arguments, plus
 //   load=<state file>  start from a VXST0001 state instead of t=0
 //   dts=a,b,c          use these step sizes instead of the CFL bound
-//   steps=N dump_every=K dumpdir=D time_steps=M
+//   steps=N dump_every=K dumpdir=D time_steps=M warmup=W
 #include <omp.h>
 
 #include <algorithm>
@@ -1347,7 +1347,8 @@ int main(int argc, char **argv) {
         }
     }
     if (time_steps > 0) {
-        S.advance(S.calculate_dt());
+        const long long warmup = std::max(1LL, geti("warmup", 1));
+        for (long long w = 0; w < warmup; w++) S.advance(S.calculate_dt());
         std::vector<double> per;
         for (long long s = 0; s < time_steps; s++) {
             double dt = S.calculate_dt();
