@@ -161,6 +161,15 @@ __global__ void k32_ds_f2(const P32 *patches, const TileRef *tiles, const float 
     st4(P.f2 + id, f2, j, 0, P.np);
 }
 
+// min(1, Q / P) for P > 0, else 0 (Q >= 0: a stencil extremum minus the centre value).
+// Q >= P gives 1 without a quotient; otherwise the hardware reciprocal (within 2 ulp),
+// except for a subnormal P, where it is not defined and IEEE division is used.
+__device__ __forceinline__ float limiter_ratio(float Q, float P) {
+    if (!(P > 0.0f)) return 0.0f;
+    if (Q >= P) return 1.0f;
+    return fminf(1.0f, P >= 1.17549435e-38f ? __fdividef(Q, P) : Q / P);
+}
+
 // Zalesak R+ and R- (Rectangle.cpp:1536-1582), cells i in [-1, nx], j in [-1, np].
 __global__ void k32_limR(const P32 *patches, const TileRef *tiles) {
     VX_PDL_WAIT();
@@ -190,8 +199,8 @@ __global__ void k32_limR(const P32 *patches, const TileRef *tiles) {
                            fminf(fminf(d0.v[e], d2.v[e]), fminf(fminf(rf0, rf2), fminf(lf0, lf2)))));
         const float Qm = -wMin + c2;
         const float Qp = wMax - c2;
-        rp.v[e] = Pp > 0.0f ? fminf(1.0f, Qp / Pp) : 0.0f;
-        rm.v[e] = Pm > 0.0f ? fminf(1.0f, Qm / Pm) : 0.0f;
+        rp.v[e] = limiter_ratio(Qp, Pp);
+        rm.v[e] = limiter_ratio(Qm, Pm);
     }
     st4(P.Rp + id, rp, j, -1, P.np + 1);
     st4(P.Rm + id, rm, j, -1, P.np + 1);
