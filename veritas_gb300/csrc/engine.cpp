@@ -91,7 +91,10 @@ void Run::allocate_rect(Rect &r) {
     r.pitch = ((r.n_p + 4) + 7) / 8 * 8;
     size_t pe = r.plane_elems();
     r.esize = precision == kF32 ? 4 : 8;
-    r.slab = DevBuf(pe * kPlanes * r.esize);
+    // the FP32 form forms gamma and the face values in registers (fused face + flux
+    // kernels): its patches have no planes for them
+    const bool faces = precision != kF32;
+    r.slab = DevBuf(pe * (faces ? kPlanes : kPlanes - 5) * r.esize);
     const int rtb = (int)std::pow(S->refinementRatio, r.depth);
     r.cols = DevBuf((size_t)2 * r.n_x * rtb * sizeof(double) + 64);
     PatchT<double> &d = r.desc;
@@ -102,11 +105,13 @@ void Run::allocate_rect(Rect &r) {
     d.f0 = plane();
     d.f1 = plane();
     d.f2 = plane();
-    d.gam = plane();
-    d.ex = plane();
-    d.fx = plane();
-    d.ep = plane();
-    d.fp = plane();
+    if (faces) {
+        d.gam = plane();
+        d.ex = plane();
+        d.fx = plane();
+        d.ep = plane();
+        d.fp = plane();
+    }
     for (int s = 0; s < 6; s++) d.FxH[s] = plane();
     for (int s = 0; s < 6; s++) d.FpH[s] = plane();
     d.FxL = plane();

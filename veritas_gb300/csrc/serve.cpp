@@ -35,7 +35,7 @@ size_t Server::estimate_bytes(const LaserSlabParams &p, int precision) {
     const double levels = std::max(1u, p.Lfinest);
     const double cells = (double)(p.nx + 4) * (p.np / 8 * 8 + 8 + 4);
     const double esize = precision == kF32 ? 4.0 : 8.0;
-    const double planes = 28.0;
+    const double planes = precision == kF32 ? 23.0 : 28.0;  // FP32: no gamma / face planes
     const double nfine = p.nx * std::pow((double)p.r, levels - 1);
     const double fields = nfine * (8.0 * 6 + 16) * 8.0 + nfine * 24.0 * (precision == kF32 ? 1.0 : 2.0);
     return (size_t)(cells * planes * esize * levels + fields);
