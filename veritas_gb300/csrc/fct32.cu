@@ -1,8 +1,9 @@
 // FP32 precision form of the per-patch FCT Runge-Kutta sub-steps
 // (Rectangle::FCTTimeStep, Rectangle.cpp:1255-1623).
 //
-// Same sub-step decomposition, tile walk and face windows as the FP64 kernels; the
-// arithmetic differs where FP32 needs it:
+// Same sub-steps and face windows as the FP64 kernels (gamma, faces and fluxes fused per
+// direction; the cell-wise sub-steps with 128-bit accesses); the arithmetic differs where
+// FP32 needs it:
 //   * f is stored scaled by the run's fnorm (1 / the peak of the initial distribution),
 //     so every plane stays far inside FP32 range; the FCT update is linear in f and its
 //     limiter is scale free, so nothing else changes;
@@ -263,10 +264,10 @@ __global__ void k32_copy10(const P32 *patches, const TileRef *tiles) {
 
 // ---------------------------------------------------------------- fused face + flux
 // One warp per strip tile: Lorentz factors, face velocities and WENO values are formed in
-// registers and consumed there (neighbours through shuffles), so neither gamma nor the
-// face planes go to HBM.  The fluxes are those of k32_faces / k32_flux; face values
-// outside the ranges the separate kernels write (x: i in [0, nx], j in [-1, np];
-// p: i in [-1, nx], j in [0, np]) are zero, as the planes they read are.
+// registers and consumed there (neighbours through shuffles), so the FP32 form has no
+// gamma or face planes at all.  The fluxes are the FP64 path's (k64_faces + k64_flux) in
+// FP32; face values outside the reference's face ranges (x: i in [0, nx], j in [-1, np];
+// p: i in [-1, nx], j in [0, np]) count as zero.
 
 // The descriptor and field-block values the p-direction kernel uses, read once into
 // registers: its row loop stores to global memory, after which the compiler would
