@@ -991,7 +991,22 @@ void Engine::record_step(LaunchSet &L) {
             VX_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
             fct_sub(L, fl, kSubPFlux);
             launches += 2;
-        } else {
+        } else if (L.poisson == kPoissonLU) {
+            // x faces and fluxes, and the E_x-independent half of the p faces, beside the
+            // exact Poisson solve; then the p-face velocities (E_x) and the p fluxes
+            fl.part = 1;
+            fct_sub(L, fl, kSubFaces);
+            fct_sub(L, fl, kSubFlux);
+            fl.part = 4;
+            fct_sub(L, fl, kSubFaces);
+            VX_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
+            fl.part = 8;
+            fct_sub(L, fl, kSubFaces);
+            fl.part = 2;
+            fct_sub(L, fl, kSubFlux);
+            fl.part = 0;
+            launches += 5;
+        } else {  // the scan solve is short: the p faces in one pass after it
             fl.part = 1;
             fct_sub(L, fl, kSubFaces);
             fct_sub(L, fl, kSubFlux);

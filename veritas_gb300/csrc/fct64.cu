@@ -45,6 +45,35 @@ __device__ __forceinline__ double weno_face(double f1, double f2, double f3, dou
     return fwl * fL + fwr * fR;
 }
 
+// Both upwind choices of weno_face at once (the smoothness weights do not depend on the
+// velocity): out_right / out_left are weno_face(..., true) / weno_face(..., false), bit
+// for bit.
+__device__ __forceinline__ void weno_face_both(double f1, double f2, double f3, double f4, double &out_right,
+                                               double &out_left) {
+    const double c6 = 1.0 / 6;
+    const double c43 = 4.0 / 3;
+    double fL = c6 * (-f1 + 5 * f2 + 2 * f3);
+    double fR = c6 * (2 * f2 + 5 * f3 - f4);
+    double AL = f1 - 2 * f2 + f3;
+    double BL = f3 - f1;
+    double AR = f2 - 2 * f3 + f4;
+    double BR = f4 - f2;
+    double bL = c43 * (AL * AL) + 0.5 * AL * BL + 0.25 * (BL * BL);
+    double bR = c43 * (AR * AR) - 0.5 * AR * BR + 0.25 * (BR * BR);
+    const double mm = 1.0e-10;
+    double oL = 0.5 / ((mm + bL) * (mm + bL));
+    double oR = 0.5 / ((mm + bR) * (mm + bR));
+    double wL = oL / (oL + oR);
+    double wR = oR / (oL + oR);
+    double wL0 = wL * (0.75 + wL * (wL - 0.5));
+    double wR0 = wR * (0.75 + wR * (wR - 0.5));
+    const double pr = (wL0 > wR0) ? wL0 : wR0, pl = (wL0 < wR0) ? wL0 : wR0;
+    double fwl = pr / (wL0 + wR0);
+    out_right = fwl * fL + (1 - fwl) * fR;
+    fwl = pl / (wL0 + wR0);
+    out_left = fwl * fL + (1 - fwl) * fR;
+}
+
 __device__ __forceinline__ double vmax(double a, double b) { return (a > b) ? a : b; }
 __device__ __forceinline__ double vmin(double a, double b) { return (a < b) ? a : b; }
 
@@ -107,6 +136,23 @@ __global__ void k64_faces(const P64 *patches, const TileRef *tiles, const RunFie
         double am = Em - P.cc * P.dx_inv * (g[pidx(i + 1, j, pit)] - g[id]);
         P.ep[id] = am;
         P.fp[id] = weno_face(f[pidx(i, j - 2, pit)], f[pidx(i, j - 1, pit)], f[id], f[pidx(i, j + 1, pit)], am > 0.0);
+    }
+    // The p faces in two halves, so that the E_x-independent one runs beside the Poisson
+    // solve: part 4 forms both upwind candidates (fp and, as scratch, Rp, which the
+    // limiter rewrites later in the stage); part 8, once E_x is known, the velocity and the
+    // choice.
+    if ((part & 4) && i >= -1 && i <= P.nx && j >= 0 && j <= P.np) {
+        double vr, vl;
+        weno_face_both(f[pidx(i, j - 2, pit)], f[pidx(i, j - 1, pit)], f[id], f[pidx(i, j + 1, pit)], vr, vl);
+        P.fp[id] = vr;
+        P.Rp[id] = vl;
+    }
+    if ((part & 8) && i >= -1 && i <= P.nx && j >= 0 && j <= P.np) {
+        const RunFields &F = fields[P.run];
+        double Em = P.q * patch_efield(P, F, i);
+        double am = Em - P.cc * P.dx_inv * (g[pidx(i + 1, j, pit)] - g[id]);
+        P.ep[id] = am;
+        if (!(am > 0.0)) P.fp[id] = P.Rp[id];
     }
 }
 
