@@ -278,6 +278,40 @@ void launch_xfer(const void *patches, const XferOp *ops, int n, uint8_t *mask, i
     else vx_launch(k_xfer<double>, dim3(16, n), 256, 0, s, (const PatchT<double> *)patches, ops, mask);
 }
 
+// One block per segment: copy its ops and make their patch ids global to the set.
+__device__ __forceinline__ void rebase(GhostOp &op, int b) {
+    op.dst += b;
+    if (op.src >= 0) op.src += b;
+}
+__device__ __forceinline__ void rebase(IfaceOp &op, int b) {
+    op.coarse += b;
+    op.fine += b;
+}
+__device__ __forceinline__ void rebase(CSyncOp &op, int b) {
+    op.nb += b;
+    op.caller += b;
+}
+template <class Op>
+__global__ void k_merge_ops(const OpSegment *segs, Op *dst) {
+    VX_PDL_WAIT();
+    const OpSegment sg = segs[blockIdx.x];
+    const Op *src = (const Op *)sg.src;
+    for (int k = threadIdx.x; k < sg.count; k += blockDim.x) {
+        Op op = src[k];
+        rebase(op, sg.base);
+        dst[sg.dst_off + k] = op;
+    }
+}
+void merge_ghost_ops(const OpSegment *segs, int nseg, GhostOp *dst, cudaStream_t s) {
+    if (nseg > 0) vx_launch(k_merge_ops<GhostOp>, nseg, 256, 0, s, segs, dst);
+}
+void merge_iface_ops(const OpSegment *segs, int nseg, IfaceOp *dst, cudaStream_t s) {
+    if (nseg > 0) vx_launch(k_merge_ops<IfaceOp>, nseg, 256, 0, s, segs, dst);
+}
+void merge_csync_ops(const OpSegment *segs, int nseg, CSyncOp *dst, cudaStream_t s) {
+    if (nseg > 0) vx_launch(k_merge_ops<CSyncOp>, nseg, 256, 0, s, segs, dst);
+}
+
 void launch_ghost(const void *patches, const GhostOp *ops, int n, int slot, int prec, cudaStream_t s) {
     if (n <= 0) return;
     if (prec == kF32) vx_launch(k_ghost<float>, (n + 127) / 128, 128, 0, s, (const PatchT<float> *)patches, ops, n, slot);

@@ -805,65 +805,46 @@ void Engine::build_set(LaunchSet &L) {
         sp[24] = dpsMax;
         spec.insert(spec.end(), sp.begin(), sp.end());
     }
-    // AMR op tables: batch b of the set = batch b of every run, patch ids made global
+    // AMR op tables: batch b of the set = batch b of every run, patch ids made global.
+    // Each run's sorted lists already sit on the device; the set's tables are gathered
+    // there, one segment per (batch, run), so a new set costs no host-side op copies.
     {
-        std::vector<GhostOp> g;
-        std::vector<IfaceOp> fo;
-        std::vector<CSyncOp> c;
-        size_t nbg = 0, nbi = 0, nbc = 0;
-        for (Run *R : L.runs) {
-            nbg = std::max(nbg, R->ghost_b.ptr.empty() ? 0 : R->ghost_b.ptr.size() - 1);
-            nbi = std::max(nbi, R->iface_b.ptr.empty() ? 0 : R->iface_b.ptr.size() - 1);
-            nbc = std::max(nbc, R->csync_b.ptr.empty() ? 0 : R->csync_b.ptr.size() - 1);
-        }
-        L.ghost_ptr.assign(1, 0);
-        L.iface_ptr.assign(1, 0);
-        L.csync_ptr.assign(1, 0);
-        for (size_t b = 0; b < nbg; b++) {
-            int base = 0;
-            for (Run *R : L.runs) {
-                if (b + 1 < R->ghost_b.ptr.size())
-                    for (int k = R->ghost_b.ptr[b]; k < R->ghost_b.ptr[b + 1]; k++) {
-                        GhostOp op = R->ghost_ops[k];
-                        op.dst += base;
-                        if (op.src >= 0) op.src += base;
-                        g.push_back(op);
+        auto gather = [&](auto dummy, auto table_of, auto ptr_of, auto merge, DevBuf &out, std::vector<int> &optr) {
+            using Op = decltype(dummy);
+            size_t nb = 0;
+            for (Run *R : L.runs) nb = std::max(nb, ptr_of(*R).empty() ? (size_t)0 : ptr_of(*R).size() - 1);
+            std::vector<OpSegment> segs;
+            optr.assign(1, 0);
+            long long total = 0;
+            for (size_t bt = 0; bt < nb; bt++) {
+                int base = 0;
+                for (Run *R : L.runs) {
+                    const std::vector<int> &p = ptr_of(*R);
+                    if (bt + 1 < p.size() && p[bt + 1] > p[bt]) {
+                        const int cnt = p[bt + 1] - p[bt];
+                        segs.push_back({table_of(*R).template as<Op>() + p[bt], total, cnt, base});
+                        total += cnt;
                     }
-                base += (int)R->flat.size();
+                    base += (int)R->flat.size();
+                }
+                optr.push_back((int)total);
             }
-            L.ghost_ptr.push_back((int)g.size());
-        }
-        for (size_t b = 0; b < nbi; b++) {
-            int base = 0;
-            for (Run *R : L.runs) {
-                if (b + 1 < R->iface_b.ptr.size())
-                    for (int k = R->iface_b.ptr[b]; k < R->iface_b.ptr[b + 1]; k++) {
-                        IfaceOp op = R->iface_ops[k];
-                        op.coarse += base;
-                        op.fine += base;
-                        fo.push_back(op);
-                    }
-                base += (int)R->flat.size();
+            out = DevBuf((size_t)std::max<long long>(total, 1) * sizeof(Op));
+            if (!segs.empty()) {
+                DevBuf dsegs = upload(segs, stream);
+                merge(dsegs.as<OpSegment>(), (int)segs.size(), out.as<Op>(), stream);
+                sync();  // dsegs is released at the end of this scope
             }
-            L.iface_ptr.push_back((int)fo.size());
-        }
-        for (size_t b = 0; b < nbc; b++) {
-            int base = 0;
-            for (Run *R : L.runs) {
-                if (b + 1 < R->csync_b.ptr.size())
-                    for (int k = R->csync_b.ptr[b]; k < R->csync_b.ptr[b + 1]; k++) {
-                        CSyncOp op = R->csync_ops[k];
-                        op.nb += base;
-                        op.caller += base;
-                        c.push_back(op);
-                    }
-                base += (int)R->flat.size();
-            }
-            L.csync_ptr.push_back((int)c.size());
-        }
-        L.dghost = upload(g, stream);
-        L.diface = upload(fo, stream);
-        L.dcsync = upload(c, stream);
+        };
+        gather(GhostOp{}, [](Run &R) -> DevBuf & { return R.dghost_ops; },
+               [](Run &R) -> const std::vector<int> & { return R.ghost_b.ptr; }, merge_ghost_ops, L.dghost,
+               L.ghost_ptr);
+        gather(IfaceOp{}, [](Run &R) -> DevBuf & { return R.diface_ops; },
+               [](Run &R) -> const std::vector<int> & { return R.iface_b.ptr; }, merge_iface_ops, L.diface,
+               L.iface_ptr);
+        gather(CSyncOp{}, [](Run &R) -> DevBuf & { return R.dcsync_ops; },
+               [](Run &R) -> const std::vector<int> & { return R.csync_b.ptr; }, merge_csync_ops, L.dcsync,
+               L.csync_ptr);
     }
     L.ncols = (int)colpatch.size();
     // lvl_ptr is absolute; lvl_off points at each run's block.

@@ -145,6 +145,7 @@ public:
     Batched csync_b;
     std::vector<IfaceOp> iface_ops;
     Batched iface_b;
+    DevBuf dghost_ops, dcsync_ops, diface_ops;  // the op lists on the device (set tables gather them)
     DevBuf drelc;                   // sub-cell interpolation weights per depth
     DevBuf drefc;                   // coarse-to-fine interpolation weights (refinement ratio)
     std::vector<int> relc_off;      // offset of depth d's weights in drelc

@@ -23,7 +23,7 @@ size_t Run::device_bytes() const {
     for (const DevBuf *d : {&dBy, &dBz, &dEy, &dEz, &dAy, &dAz, &dasq, &dphi, &dcharge, &dJ, &dneut, &defin, &dex0,
                             &dasq32, &defin32, &dacell32, &drelc32, &dlu_perm, &dlb_band, &dlb_fptr, &dlb_fcol, &dlb_fval, &dlb_slot,
                             &dlb_sload, &dlb_take, &dub_band, &dub_diag, &dub_rdiag, &dub_rdlo, &dub_fptr, &dub_fcol,
-                            &dub_fval, &dpf_Y, &drelc, &drefc})
+                            &dub_fval, &dpf_Y, &drelc, &drefc, &dghost_ops, &diface_ops, &dcsync_ops})
         b += d->bytes;
     return b;
 }
