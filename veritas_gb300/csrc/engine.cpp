@@ -198,7 +198,6 @@ void Run::init_rect_distribution(Rect &r) {
     const int nvals = std::pow(s.refinementRatio, r.depth + s.quadratureDepth);
     const double dx = s.GetDx(r.depth), dp = s.GetDp(r.depth, r.species);
     const double pmin = s.pmin[r.species];
-    std::vector<double> host((size_t)(r.n_x + 4) * r.pitch, 0.0);
     if (precision == kF32 && s.problem->Separable()) {
         // same sample points, summed as (sum_k density)(sum_l profile)
         std::vector<double> dx_sum(r.n_x, 0.0), dp_sum(r.n_p, 0.0);
@@ -207,17 +206,15 @@ void Run::init_rect_distribution(Rect &r) {
         for (int j = 0; j < r.n_p; j++)
             for (int l = 0; l < nvals; l++)
                 dp_sum[j] += s.problem->Profile(s, pmin + dp * ((0.5 + l) / nvals + j + r.p_pos), r.species);
+        // the product on the device (the planes of a new patch are zero: ghosts stay 0)
         const double inv = 1 / std::pow(nvals, 2.0);
-        for (int i = 0; i < r.n_x; i++)
-            for (int j = 0; j < r.n_p; j++) host[pidx(i, j, r.pitch)] = dx_sum[i] * dp_sum[j] * inv;
-        std::vector<float> h32(host.size());
-        const double fn = fnorm[r.species];
-        for (size_t q = 0; q < host.size(); q++) h32[q] = (float)(host[q] * fn);
-        VX_CUDA(cudaMemcpyAsync(r.desc.f0, h32.data(), r.plane_bytes(), cudaMemcpyHostToDevice, eng.stream));
-        VX_CUDA(cudaMemcpyAsync(r.desc.f1, h32.data(), r.plane_bytes(), cudaMemcpyHostToDevice, eng.stream));
+        DevBuf dxs = upload(dx_sum, eng.stream), dps = upload(dp_sum, eng.stream);
+        launch_fill_separable((float *)r.desc.f0, (float *)r.desc.f1, r.pitch, r.n_x, r.n_p, dxs.as<double>(),
+                              dps.as<double>(), inv, fnorm[r.species], eng.stream);
         VX_CUDA(cudaStreamSynchronize(eng.stream));
         return;
     }
+    std::vector<double> host((size_t)(r.n_x + 4) * r.pitch, 0.0);
     unsigned nth = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
     std::vector<std::thread> th;
     for (unsigned t = 0; t < nth; t++) {

@@ -161,6 +161,26 @@ void launch_moments64(const MomLaunch &M) {
     vx_launch(k64_moments, M.ncols / kMomCols, kMomCols * 32, 0, M.stream, M);
 }
 
+// ---------------------------------------------------------------- separable initial f
+// Interior cells of an FP32 patch's slots 0 and 1: (float)(((dx_sum[i] dp_sum[j]) inv) fn),
+// the host quadrature's product in its order (this file keeps IEEE multiplies unfused).
+__global__ void k_fill_separable(float *f0, float *f1, int pitch, int nx, int np, const double *dx_sum,
+                                 const double *dp_sum, double inv, double fn) {
+    VX_PDL_WAIT();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (j >= np || i >= nx) return;
+    const double v = dx_sum[i] * dp_sum[j] * inv;
+    const float x = (float)(v * fn);
+    const int id = pidx(i, j, pitch);
+    f0[id] = x;
+    f1[id] = x;
+}
+
+void launch_fill_separable(float *f0, float *f1, int pitch, int nx, int np, const double *dx_sum,
+                           const double *dp_sum, double inv, double fn, cudaStream_t s) {
+    vx_launch(k_fill_separable, dim3((np + 255) / 256, nx), 256, 0, s, f0, f1, pitch, nx, np, dx_sum, dp_sum, inv, fn);
+}
+
 // ---------------------------------------------------------------- assembly
 // Level::CollectRhoAndJ + EMFieldSolver::AssembleRhoAndJ (Level.cpp:19-62,
 // EMSolver.cpp:104-122): per level, chargeL[x] = 0 + (patch values in patch order);

@@ -197,6 +197,9 @@ struct CflLaunch {
 };
 void launch_cfl(const CflLaunch &L);
 
+// Interior of a fresh (zeroed) FP32 patch from the separable quadrature's 1-D sums.
+void launch_fill_separable(float *f0, float *f1, int pitch, int nx, int np, const double *dx_sum,
+                           const double *dp_sum, double inv, double fn, cudaStream_t s);
 // FP64 FMA throughput probe: blocks x threads threads, iters x 8 independent DFMA each.
 void launch_fp64_peak(double *out, int blocks, int threads, int iters, cudaStream_t s);
 
