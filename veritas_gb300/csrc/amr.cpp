@@ -590,13 +590,14 @@ void Run::build_amr() {
     for (Rect *R : flat) {
         const size_t pe = R->plane_elems();
         std::vector<uint8_t> m(3 * pe, 0);
-        for (int i = -2; i < R->n_x + 2; i++)
-            for (int j = -2; j < R->n_p + 2; j++) {
-                const size_t d = (size_t)pidx(i, j, R->pitch);
-                m[d] = R->nested[R->ns(i, j)];
-                m[pe + d] = R->ifx[R->ns(i, j)];
-                m[2 * pe + d] = R->ifp[R->ns(i, j)];
-            }
+        // rows of (n_p + 4) cells in the reference's index order become pitched rows
+        const size_t w = (size_t)R->n_p + 4;
+        for (int i = -2; i < R->n_x + 2; i++) {
+            const size_t d = (size_t)pidx(i, -2, R->pitch), q = (size_t)R->ns(i, -2);
+            std::memcpy(&m[d], &R->nested[q], w);
+            std::memcpy(&m[pe + d], &R->ifx[q], w);
+            std::memcpy(&m[2 * pe + d], &R->ifp[q], w);
+        }
         R->masks = DevBuf(m.size());
         VX_CUDA(cudaMemcpy(R->masks.p, m.data(), m.size(), cudaMemcpyHostToDevice));
     }
