@@ -199,6 +199,31 @@ struct PlaneScheduler {
         batch.push_back(b);
         nbatches = std::max(nbatches, b + 1);
     }
+    // add() for a restriction: reads the r x r block at (si, sj) of patch src, writes
+    // (di, dj) of patch dst; the same batch, with the block's bounds checked once.
+    void add_restrict(int dst, int di, int dj, int src, int si, int sj, int r) {
+        slot(src, si, sj);
+        slot(src, si + r - 1, sj + r - 1);  // bounds of the whole block
+        const size_t cw = slot(dst, di, dj);
+        const int wp = flat[src]->n_p + 4;
+        const size_t s0 = slot(src, si, sj);
+        const int16_t *lw = last_w[src].data();
+        int b = 0;
+        for (int a = 0; a < r; a++)
+            for (int q = 0; q < r; q++) b = std::max(b, lw[s0 + (size_t)a * wp + q] + 1);
+        b = std::max(b, last_w[dst][cw] + 1);
+        b = std::max(b, last_r[dst][cw] + 1);
+        if (b > 32000) throw std::runtime_error("ghost-fill schedule too deep");
+        int16_t *lr = last_r[src].data();
+        for (int a = 0; a < r; a++)
+            for (int q = 0; q < r; q++) {
+                int16_t &v = lr[s0 + (size_t)a * wp + q];
+                v = (int16_t)std::max<int>(v, b);
+            }
+        last_w[dst][cw] = (int16_t)b;
+        batch.push_back(b);
+        nbatches = std::max(nbatches, b + 1);
+    }
 };
 
 template <class Op>
@@ -397,8 +422,10 @@ void Run::build_amr() {
                 for (int j = 0; j < R.n_p; j++)
                     if (R.nested[R.ns(i, j)]) {
                         const Rect &F = *flat[R.finer[R.ns(i, j)]];
-                        emit({kGhostRestrict, R.id, i, j, F.id, (R.x_pos + i) * r - F.x_pos,
-                              (R.p_pos + j) * r - F.p_pos, 0});
+                        const GhostOp op{kGhostRestrict, R.id, i, j, F.id, (R.x_pos + i) * r - F.x_pos,
+                                         (R.p_pos + j) * r - F.p_pos, 0};
+                        gs.add_restrict(op.dst, op.di, op.dj, op.src, op.si, op.sj, r);
+                        ghost_ops.push_back(op);
                     }
         }
     };
