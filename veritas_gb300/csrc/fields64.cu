@@ -521,7 +521,7 @@ __device__ void pois_bwd_fast(PoisBandChunk &B, int r0, int cnt, double *x, doub
 
 constexpr int kPoisSmemMaxN = 16384;  // solution vector kept in shared memory up to this n
 
-__global__ void k_poisson(PoissonLaunch L) {
+__global__ void __launch_bounds__(1024, 1) k_poisson(PoissonLaunch L) {
     VX_PDL_WAIT();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PoisBandChunk *buf = (PoisBandChunk *)smem_raw;  // two chunk buffers, then the solution vector
@@ -662,7 +662,10 @@ void launch_poisson(const PoissonLaunch &L) {
     P.x_in_smem = (L.maxn <= kPoisSmemMaxN && base + 8 * L.maxn <= max_smem) ? 1 : 0;
     const int smem = base + (P.x_in_smem ? 8 * L.maxn : 0);
     cudaFuncSetAttribute(k_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    vx_launch(k_poisson, L.nruns, 512, smem, L.stream, P);
+    // 1024 threads x 64 registers take a whole SM's register file: no block of the FP64
+    // face kernels that run beside the solve shares the SM, whose FP64 unit would
+    // otherwise delay the solve's dependent chain (step 32.4 -> 28.1 ms on 4096 x 512)
+    vx_launch(k_poisson, L.nruns, 1024, smem, L.stream, P);
 }
 
 // E_x on the finest grid from phi and Ex0 (EMSolver::GetEfield), for states loaded from
