@@ -664,6 +664,18 @@ void Engine::set_launch_mode(bool graphs, bool pdl) {
         }
 }
 
+void Engine::retain_sets(const std::vector<std::vector<Run *>> &keep) {
+    bool drop = false;
+    for (auto &kv : sets_)
+        if (std::find(keep.begin(), keep.end(), kv.first) == keep.end()) drop = true;
+    if (!drop) return;
+    sync();  // a dropped set's buffers may still be in use by queued work
+    for (auto it = sets_.begin(); it != sets_.end();) {
+        if (std::find(keep.begin(), keep.end(), it->first) == keep.end()) it = sets_.erase(it);
+        else ++it;
+    }
+}
+
 LaunchSet &Engine::get_set(const std::vector<Run *> &set) {
     auto it = sets_.find(set);
     uint64_t ver = 0;

@@ -235,6 +235,9 @@ public:
     // CUDA graph per step and programmatic dependent launch on or off; drops the
     // captured graphs (they hold the old launch attributes).
     void set_launch_mode(bool graphs, bool pdl);
+    // Drops every cached launch set but the listed ones (their tables and graphs hold
+    // device memory; a serving loop keeps only the sets of its current step).
+    void retain_sets(const std::vector<std::vector<Run *>> &keep);
     int tile_pref[2][2] = {{32, 8}, {128, 8}};  // [precision 64, 32] -> (tile_j, tile_i)
 
 private:

@@ -85,7 +85,9 @@ int Server::step(double now) {
     if (live_.empty()) return 0;
     std::vector<Run *> set;
     for (int64_t id : live_) set.push_back(reqs_.at(id).run.get());
-    // one launch set per precision and Poisson solver (different kernels)
+    // one launch set per precision and Poisson solver (different kernels); the sets of
+    // earlier mixes are dropped, so cached tables do not pile up beside the budget
+    std::vector<std::vector<Run *>> used;
     for (int prec : {kF64, kF32})
         for (int pois : {kPoissonLU, kPoissonScan}) {
             std::vector<Run *> part;
@@ -94,7 +96,9 @@ int Server::step(double now) {
             if (part.empty()) continue;
             auto dt = eng.calculate_dt(part);
             eng.advance(part, dt);
+            used.push_back(part);
         }
+    eng.retain_sets(used);
     eng.sync();
     std::vector<int64_t> still;
     for (int64_t id : live_) {
