@@ -152,6 +152,34 @@ int vx_run_save_state(vx_run *run, const char *path);
  * finest grid (n).  *len receives the element count; out may be NULL to query it. */
 int vx_run_get_field(vx_run *run, int which, double *out, int64_t *len);
 
+/* ---- diagnostics in the reference's text formats --------------------------------- */
+
+/* Files of SolverManager::fileOutput (SolverManager.cpp:102-159), one bit each for the
+ * flags of Output (Settings.hpp:22-33); VX_OUT_ALL is Output's defaults (all on, with
+ * precision 15). */
+#define VX_OUT_CHARGE 0x01        /* charge.txt, one line per species (EMSolver.cpp:340-358) */
+#define VX_OUT_ENERGY 0x02        /* dNdP_<species>.txt (EMSolver.cpp:361-378) */
+#define VX_OUT_POTENTIAL 0x04     /* potential.txt (EMSolver.cpp:417-430) */
+#define VX_OUT_EFIELD_LONG 0x08   /* EFieldLong.txt (EMSolver.cpp:381-394) */
+#define VX_OUT_EFIELD_TRANS 0x10  /* EFieldTrans.txt (EMSolver.cpp:396-415) */
+#define VX_OUT_BFIELD_TRANS 0x20  /* BFieldTrans.txt (EMSolver.cpp:432-451) */
+#define VX_OUT_ASQUARED 0x40      /* ASquared.txt (EMSolver.cpp:453-466) */
+#define VX_OUT_TIME 0x80          /* time.txt (EMSolver.cpp:468-477) */
+#define VX_OUT_ALL 0xff
+
+/* Replaces SolverManager::fileOutput(t) (SolverManager.cpp:102).  Appends one record to
+ * each selected file under dir (the reference writes under "output/"); a run creates its
+ * files on its first call and appends afterwards, as the reference's streams do.  digits
+ * is Output::precision (std::setprecision of the scientific values); t is written to
+ * time.txt.  Values are formatted as the reference does, so an FP64 run's files compare
+ * line by line with the reference's. */
+int vx_run_write_fields(vx_run *run, const char *dir, uint32_t mask, int digits, double t);
+/* Replaces SolverManager::OutputRectangles(t) / Mesh::outputRectangleData
+ * (SolverManager.cpp:64-70, Mesh.cpp:877-902): writes
+ * dir/rectangleData_p<species>_l<level>_t<t in scientific>.txt for every non-empty level
+ * (the reference's dir is "output/rectangleData"). */
+int vx_run_write_rectangles(vx_run *run, const char *dir, double t);
+
 /* ---- measurement and host-buffer entry points ------------------------------------ */
 
 /* Device time between two points on the context stream (CUDA events). */

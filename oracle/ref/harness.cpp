@@ -87,6 +87,7 @@ struct Problem {
     double cfl = 0.5, minEff = 0.75, crit = 1e-6, sizeWeight = 1.0;
     int quadDepth = 2;
     double mi = 0.0, iTe = 1.0, ipmax = 0.1;          // mobile ions when mi > 0 (mass / m_e, keV, m_i c)
+    bool diag = false;                               // enable the reference's text outputs
 };
 static Problem P;
 static double beam_T = 0.0, beam_p = 0.0;
@@ -132,15 +133,9 @@ void initialConditions(Input &grid, Particles &particles, Output &output) {
         particles.dp.push_back(0.1);
         particles.pmin.push_back(0.0);
     }
-    output.time = false;
-    output.rectangleData = false;
-    output.charge = false;
-    output.energy = false;
-    output.potential = false;
-    output.EFieldLongitudinal = false;
-    output.EFieldTransverse = false;
-    output.BFieldTransverse = false;
-    output.AFieldSquared = false;
+    // the reference's text outputs only in the diag_every mode
+    output.time = output.rectangleData = output.charge = output.energy = output.potential = P.diag;
+    output.EFieldLongitudinal = output.EFieldTransverse = output.BFieldTransverse = output.AFieldSquared = P.diag;
     output.precision = 15;
 }
 
@@ -325,6 +320,10 @@ int main(int argc, char **argv) {
     long long dump_every = geti("dump_every", 0);
     long long regrid_every = geti("regrid_every", 0);
     long long time_steps = geti("time_steps", 0);
+    // diag_every=K: SolverManager::fileOutput and OutputRectangles at t = 0 and after every
+    // K-th step, into output/ and output/rectangleData/ of the working directory.
+    long long diag_every = geti("diag_every", 0);
+    P.diag = diag_every > 0;
     std::string dumpdir = kv.count("dumpdir") ? kv["dumpdir"] : "";
 
     Input grid;
@@ -345,6 +344,11 @@ int main(int argc, char **argv) {
         snprintf(name, sizeof name, "%s/state_%05lld.bin", dumpdir.c_str(), 0LL);
         dump_state(SM, settings, name, 0.0, 0);
     }
+    auto diag = [&] {
+        SM.fileOutput(settings.time);
+        SM.OutputRectangles(settings.time);
+    };
+    if (diag_every > 0) diag();
     for (long long s = 1; s <= steps; s++) {
         double dt = SM.CalculateDt(settings.cfl);
         SM.Advance(dt);
@@ -353,6 +357,7 @@ int main(int argc, char **argv) {
             snprintf(name, sizeof name, "%s/state_%05lld.bin", dumpdir.c_str(), s);
             dump_state(SM, settings, name, dt, s);
         }
+        if (diag_every > 0 && s % diag_every == 0) diag();
         if (regrid) {
             std::cout.rdbuf(sink.rdbuf());
             SM.reGrid(settings.time);

@@ -64,6 +64,30 @@ REGRID = {
 }
 
 
+# name -> (steps, interval) of the text-output fixtures: the files SolverManager::fileOutput
+# and OutputRectangles write at t = 0 and after every interval-th step, stored byte for
+# byte (one-thread run: Rectangle::CalculateEnergy's OpenMP loop adds into shared bins).
+DIAG = {
+    "ions2": (2, 2),
+    "beam3": (2, 2),
+}
+
+
+def run_diag(exe: Path, name: str, args: list[str], steps: int, every: int) -> None:
+    import numpy as np
+
+    with tempfile.TemporaryDirectory() as td:
+        out = Path(td) / "output"
+        (out / "rectangleData").mkdir(parents=True)
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        cmd = [str(exe), *args, f"steps={steps}", f"diag_every={every}"]
+        subprocess.run(cmd, check=True, env=env, cwd=td, stdout=subprocess.DEVNULL)
+        files = {}
+        for f in sorted(out.rglob("*.txt")):
+            files[str(f.relative_to(out))] = np.frombuffer(f.read_bytes(), dtype=np.uint8)
+        np.savez_compressed(HERE / f"{name}_diag.npz", **files)
+
+
 def run_case(exe: Path, name: str, args: list[str], steps: int, keep: list[int]) -> None:
     with tempfile.TemporaryDirectory() as td:
         env = dict(os.environ, OMP_NUM_THREADS="4")
@@ -102,6 +126,11 @@ def main() -> None:
             continue
         run_regrid(exe, name, CASES[name][0], every)
         print("wrote", name, "regrid")
+    for name, (steps, every) in DIAG.items():
+        if a.only and name not in a.only:
+            continue
+        run_diag(exe, name, CASES[name][0], steps, every)
+        print("wrote", name, "diag")
 
 
 if __name__ == "__main__":

@@ -101,6 +101,8 @@ def _load() -> ctypes.CDLL:
         "vx_run_load_state": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "vx_run_save_state": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "vx_run_get_field": (ctypes.c_int, [vp, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_int64)]),
+        "vx_run_write_fields": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_double]),
+        "vx_run_write_rectangles": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_double]),
         "vx_ctx_timer_begin": (ctypes.c_int, [vp]),
         "vx_ctx_timer_end": (ctypes.c_int, [vp, P(ctypes.c_double)]),
         "vx_run_profile_kernels": (ctypes.c_int, [vp, ctypes.c_int, P(ctypes.c_double), ctypes.c_int, P(ctypes.c_int)]),
@@ -240,6 +242,10 @@ class Context:
             pass
 
 
+# Output flags of the reference (Settings.hpp:22-33) -> VX_OUT_* bits of vx.h.
+OUTPUT_BITS = {"charge": 0x01, "energy": 0x02, "potential": 0x04, "EFieldLongitudinal": 0x08,
+               "EFieldTransverse": 0x10, "BFieldTransverse": 0x20, "AFieldSquared": 0x40, "time": 0x80}
+
 FIELD_IDS = {"By": 0, "Bz": 1, "Ey": 2, "Ez": 3, "Ay": 4, "Az": 5, "a_squared": 6, "phi": 7, "charge": 8, "J": 9,
              "Ex": 10}
 
@@ -297,6 +303,17 @@ class SolverManager:
 
     def save_state(self, path: str | os.PathLike) -> None:
         _check(_lib.vx_run_save_state(self._h, str(path).encode()))
+
+    def fileOutput(self, t: float, directory: str | os.PathLike = "output", outputs=None, precision: int = 15) -> None:
+        """SolverManager::fileOutput(t) (SolverManager.cpp:102-159): appends one record to
+        each of the reference's text files under `directory` (created by the run's first
+        call).  `outputs`: names from OUTPUT_BITS (default: all, as Output's defaults)."""
+        mask = 0xFF if outputs is None else sum(OUTPUT_BITS[o] for o in set(outputs))
+        _check(_lib.vx_run_write_fields(self._h, str(directory).encode(), mask, precision, t))
+
+    def OutputRectangles(self, t: float, directory: str | os.PathLike = "output/rectangleData") -> None:
+        """SolverManager::OutputRectangles(t) / Mesh::outputRectangleData (Mesh.cpp:877-902)."""
+        _check(_lib.vx_run_write_rectangles(self._h, str(directory).encode(), t))
 
     def field(self, name: str) -> np.ndarray:
         n = ctypes.c_int64()

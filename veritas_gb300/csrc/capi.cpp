@@ -368,6 +368,18 @@ int vx_run_save_state(vx_run *run, const char *path) {
     return (rc == VX_ERR_STATE) ? VX_ERR_IO : rc;
 }
 
+int vx_run_write_fields(vx_run *run, const char *dir, uint32_t mask, int digits, double t) {
+    if (!run || !dir || digits < 0 || digits > 40 || (mask & ~(uint32_t)VX_OUT_ALL)) return VX_ERR_INVALID;
+    int rc = guard([&] { run->run->write_fields(dir, mask, digits, t); });
+    return (rc == VX_ERR_STATE) ? VX_ERR_IO : rc;
+}
+
+int vx_run_write_rectangles(vx_run *run, const char *dir, double t) {
+    if (!run || !dir) return VX_ERR_INVALID;
+    int rc = guard([&] { run->run->write_rectangles(dir, t); });
+    return (rc == VX_ERR_STATE) ? VX_ERR_IO : rc;
+}
+
 int vx_run_get_field(vx_run *run, int which, double *out, int64_t *len) {
     if (!run || !len) return VX_ERR_INVALID;
     return guard([&] {

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <fstream>
 #include <functional>
 #include <map>
 #include <memory>
@@ -167,6 +168,12 @@ public:
     int64_t state_size() const;
     void step_host(const double *in, double *out, double dt);
     void state_to_host(double *out);
+    // Diagnostics in the reference's text formats (output.cpp).
+    void write_fields(const std::string &dir, unsigned mask, int digits, double t);
+    void write_rectangles(const std::string &dir, double t);
+    std::map<std::string, std::unique_ptr<std::ofstream>> out_streams;  // files kept open, by path
+    std::ofstream &out_stream(const std::string &path, int digits);
+    std::vector<double> slot_to_host(const Rect &r, int slot);
 };
 
 // Clustering of one species' hierarchy (Mesh::updateHierarchy without the promotion)
