@@ -304,6 +304,16 @@ __device__ bool pois_stage_band(PoisBandChunk &B, const BandFactor &F, int a, in
         }
         if (F.take) B.take[k] = F.take[r];
     }
+    // buffer rows past n: neutral entries, so that a look-ahead read past the matrix's end
+    // finds a zero coefficient and no row index
+    for (int k = cnt + t; k < kPoisBuf; k += nt) {
+        B.c[0][k] = B.c[1][k] = B.c[2][k] = B.c[3][k] = 0.0;
+        for (int sl = 0; sl < 4; sl++) {  // every accumulator row of the buffer
+            B.slotc[sl][k] = 0.0;
+            B.sload[sl][k] = -1;
+        }
+        B.take[k] = -1;
+    }
     for (int k = t; k <= cnt; k += nt) B.fptr[k] = F.fptr[a + k] - f0;
     if (fits)
         for (int e = f0 + t; e < f1; e += nt) {
@@ -437,45 +447,54 @@ __device__ void pois_bwd_chunk(PoisBandChunk &B, const BandFactor &F, int r0, in
 // Steady-state forms of the two chunk loops (every far term handled by accumulator
 // lanes or by the parallel pass): each lane walks its own coefficient stream with a
 // pointer, the shift and the slot hand-over are one shuffle with a per-lane source, and
-// no branch depends on the lane, so a row costs about 25 warp instructions.
+// no branch depends on the lane.  The operands of the next row are loaded at the top of
+// each row, ahead of its multiply: the warp issues in order, and a load placed after the
+// previous row's shuffle-dependent store would add its shared-memory latency to every row
+// of the chain (forward 282 -> 242 cycles per row, step 28.4 -> 27.1 ms).  The look-ahead
+// reads at most two rows past the chunk: the staged look-ahead rows, or past n the
+// neutral entries pois_stage_band writes there (zero coefficients, no slot row).
 __device__ void pois_fwd_fast(const PoisBandChunk &B, const BandFactor &F, int r0, int cnt, int n, double *x,
                               double &V, double &w1) {
-    // Only lanes 0..7 (band lanes 0..3, accumulator lanes 4..7) run the recurrence: the
-    // dependent latency of an FP64 warp instruction grows with its active lanes on this
-    // part, so the chain's multiply-subtract runs on eight lanes, not 32.
+    // Only lanes 0..7 (band lanes 0..3, accumulator lanes 4..7) run the recurrence.
     constexpr unsigned act = 0xffu;
     const int lane = threadIdx.x & 31;
+    if (lane >= 8) return;
     const int slot = lane - 4;
     const bool is_slot = slot >= 0 && slot < F.nslots;
+    const bool has_coef = lane < 4 || is_slot;
     const int k0 = r0 - B.a;
-    // coefficient stream of this lane (zeros for lanes without a role)
-    __shared__ double zero_stream[1];
-    if (lane == 0) zero_stream[0] = 0.0;
-    __syncwarp();
-    if (lane >= 8) return;
-    const double *cp;
-    int cstep = 1;
-    if (lane < 4) cp = &B.c[lane][k0 + lane];
-    else if (is_slot) cp = &B.slotc[slot][k0];
-    else {
-        cp = zero_stream;
-        cstep = 0;
-    }
-    const int *lp = is_slot ? &B.sload[slot][k0] : nullptr;
+    // coefficient stream of this lane (lanes without a role read slot 0's and use zero)
+    const double *cp = lane < 4 ? &B.c[lane][k0 + lane] : &B.slotc[is_slot ? slot : 0][k0];
+    const int cstep = has_coef ? 1 : 0;
+    // row indices the slot takes up, read two rows ahead so that x[row] is one row ahead
+    const int *lp = &B.sload[is_slot ? slot : 0][k0];
+    const int lstep = is_slot ? 1 : 0;
     const int base_src = lane < 3 ? lane + 1 : lane;
     // rows past the end of the matrix get a zero coefficient
     const int lim = lane < 4 ? n - 1 - lane - r0 : cnt;  // q > lim: row i+lane >= n
+    double coef = (0 > lim || !has_coef) ? 0.0 : *cp;
+    cp += cstep;
+    int ld = is_slot ? *lp : -1;
+    lp += lstep;
+    int ldn = is_slot ? *lp : -1;
+    lp += lstep;
+    double vld = ld >= 0 ? x[ld] : 0.0;
+    int tk = B.take[k0];
+    double fb = (lane == 3 && r0 + 4 < n) ? x[r0 + 4] : 0.0;
     for (int q = 0; q < cnt; q++) {
         const int i = r0 + q;
-        double coef = *cp;
+        // row q+1's operands; a slot's row r >= step + 4 and the right-hand side x[i + 5]
+        // are not yet overwritten by the sweep.  Rows past the chunk read the staged
+        // look-ahead rows, or past n the neutral entries pois_stage_band leaves there.
+        double coef_n = *cp;
         cp += cstep;
-        if (q > lim) coef = 0.0;
-        if (lp) {
-            const int ld = *lp++;
-            if (ld >= 0) V = x[ld];
-        }
-        const int tk = B.take[k0 + q];
-        const double fb = (lane == 3 && i + 4 < n) ? x[i + 4] : 0.0;
+        if (q + 1 > lim || !has_coef) coef_n = 0.0;
+        const int tk_n = B.take[k0 + q + 1];
+        const double fb_n = (lane == 3 && i + 5 < n) ? x[i + 5] : 0.0;
+        const double vld_n = ldn >= 0 ? x[ldn] : 0.0;
+        const int ldnn = is_slot ? *lp : -1;
+        lp += lstep;
+        if (ld >= 0) V = vld;  // a slot takes up a new row's right-hand side
         const double nv = V - w1 * coef;
         const double xi = __shfl_sync(act, nv, 0, 8);
         const int src = (lane == 3 && tk >= 0) ? 4 + tk : base_src;  // tk < kMaxSlots = 4
@@ -483,12 +502,19 @@ __device__ void pois_fwd_fast(const PoisBandChunk &B, const BandFactor &F, int r
         V = (lane == 3 && tk < 0) ? fb : sh;
         if (lane == 0) x[i] = xi;
         w1 = xi;
+        coef = coef_n;
+        tk = tk_n;
+        fb = fb_n;
+        vld = vld_n;
+        ld = ldn;
+        ldn = ldnn;
     }
 }
 
 __device__ void pois_bwd_fast(PoisBandChunk &B, int r0, int cnt, double *x, double &V, double &w1) {
-    // Lanes 0..3 run the multiply-subtract and lane 0 alone the quotient (see
-    // pois_fwd_fast on active lanes); the other lanes leave V and w1 unused.
+    // Lanes 0..3 run the multiply-subtract and lane 0 alone the quotient (the same
+    // instructions on four lanes made the backward sweep 40 % slower); the other lanes
+    // leave V and w1 unused.
     constexpr unsigned act = 0xfu;
     const int lane = threadIdx.x & 31;
     if (lane >= 4) return;
@@ -497,12 +523,23 @@ __device__ void pois_bwd_fast(PoisBandChunk &B, int r0, int cnt, double *x, doub
     const double *cp = &B.c[L][kl - L];
     const double *yp = &B.rdiag[kl];
     const double *lp = &B.rdlo[kl];
+    const int ilast = r0 + cnt - 1;
+    double coef = (ilast - L < 0) ? 0.0 : cp[0];
+    double y = yp[0], ylo = lp[0];
+    cp--;
+    yp--;
+    lp--;
+    double fb = (lane == 3 && ilast - 4 >= 0) ? x[ilast - 4] : 0.0;
     for (int qq = cnt - 1; qq >= 0; qq--) {
         const int i = r0 + qq;
-        double coef = *cp--;
-        if (i - L < 0) coef = 0.0;
-        const double y = *yp--, ylo = *lp--;
-        const double fb = (lane == 3 && i - 4 >= 0) ? x[i - 4] : 0.0;
+        // row i-1's operands (kPoisLA rows are staged below the chunk); x[i - 5] is still
+        // the right-hand side
+        const double coef_n = (i - 1 - L >= 0) ? cp[0] : 0.0;
+        const double y_n = qq > 0 ? yp[0] : 0.0, ylo_n = qq > 0 ? lp[0] : 0.0;
+        const double fb_n = (lane == 3 && i - 5 >= 0) ? x[i - 5] : 0.0;
+        cp--;
+        yp--;
+        lp--;
         const double nv = V - w1 * coef;
         const double up = __shfl_down_sync(act, nv, 1, 4);
         // quotient from the reciprocal split into high and low parts: within 2^-105 of
@@ -516,6 +553,10 @@ __device__ void pois_bwd_fast(PoisBandChunk &B, int r0, int cnt, double *x, doub
         const double xi = __shfl_sync(act, q1, 0, 4);
         V = (lane == 3) ? fb : up;
         w1 = xi;
+        coef = coef_n;
+        y = y_n;
+        ylo = ylo_n;
+        fb = fb_n;
     }
 }
 
