@@ -237,8 +237,13 @@ __global__ void k64_limR(const P64 *patches, const TileRef *tiles) {
     double wMin = vmin(w1mi, vmin(w2mi, vmin(w3mi, vmin(w4mi, w5mi))));
     double Qm = -wMin + c2;
     double Qp = wMax - c2;
-    P.Rp[id] = Pp > 0.0 ? vmin(1.0, Qp / Pp) : 0.0;
-    P.Rm[id] = Pm > 0.0 ? vmin(1.0, Qm / Pm) : 0.0;
+    // min(1, Q/P) is 1 whenever Q >= P and P is finite: the quotient (Q infinite
+    // included) is then >= 1 however it rounds.  Every other case, NaN and infinite P
+    // among them, takes the division as written.  Most cells of a smooth solution take
+    // the first branch and skip the division (about ten FP64 instructions).
+    constexpr double kMaxFinite = 1.7976931348623157e308;
+    P.Rp[id] = Pp > 0.0 ? ((Qp >= Pp && Pp <= kMaxFinite) ? 1.0 : vmin(1.0, Qp / Pp)) : 0.0;
+    P.Rm[id] = Pm > 0.0 ? ((Qm >= Pm && Pm <= kMaxFinite) ? 1.0 : vmin(1.0, Qm / Pm)) : 0.0;
 }
 
 // Limiter coefficients on interior faces, 1 elsewhere (Rectangle.cpp:1581-1594).
