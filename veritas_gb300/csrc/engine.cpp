@@ -524,6 +524,7 @@ static void run_poisson(const LaunchSet &L, const PoissonLaunch &pl) {
         f.fcoef = pl.fcoef;
         f.nruns = pl.nruns;
         f.maxn = pl.maxn;
+        f.f32 = L.precision == kF32;
         f.stream = pl.stream;
         launch_poisson_fast(f);
     } else {
@@ -578,6 +579,7 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     ml.fields = L.dfields.as<RunFields>();
     ml.nruns = (int)L.runs.size();
     ml.maxnf = L.maxnf;
+    ml.acell = 0;  // as in a step's later stages: the Maxwell stage made the copy
     ml.stream = stream;
     time_it([&] { run_moments(L, ml); });
     AsmLaunch al{};
@@ -624,6 +626,7 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     mx.params = L.dparams.as<double>();
     mx.dxinv = L.ddxinv.as<double>();
     mx.step = 0;
+    mx.f32 = L.precision == kF32;
     mx.stream = stream;
     time_it([&] { launch_maxwell(mx); });
     // the AMR op batches of one stage (each entry: all batches of that kind)
@@ -942,11 +945,17 @@ void Engine::record_step(LaunchSet &L) {
     mx.maxnf = L.maxnf;
     mx.params = L.dparams.as<double>();
     mx.dxinv = L.ddxinv.as<double>();
+    mx.f32 = L.precision == kF32;
     mx.stream = stream;
     for (int s = 0; s < 6; s++) {
+        // FP32 copies of the fields: E_x's comes with each solve (k_efield), the per-cell
+        // A^2 the moments read with each Maxwell stage for the next one (the step's first
+        // stage makes its own).  a^2's is made at every stage: the Maxwell stage runs
+        // beside the face kernels that read it.
+        ml.acell = s == 0;
         run_moments(L, ml);
         launch_assemble(al);
-        launches += L.precision == kF32 ? 3 : 2;
+        launches += (L.precision == kF32 && s == 0) ? 3 : 2;
         // the Poisson solve (and E_x) runs beside the x-direction face work, which does
         // not read E_x; the p-direction faces wait for both
         VX_CUDA(cudaEventRecord(ev_fork, stream));
@@ -955,9 +964,8 @@ void Engine::record_step(LaunchSet &L) {
         run_poisson(L, pl);
         launches += L.poisson == kPoissonScan ? 2 : 1;
         if (L.precision == kF32) {
-            launch_fields_to_f32(L.dfields.as<RunFields>(), (int)L.runs.size(), L.maxn, 2, side);
             launch_fields_to_f32(L.dfields.as<RunFields>(), (int)L.runs.size(), L.maxn, 1, stream);
-            launches += 2;
+            launches += 1;
         }
         fl.step = s;
         // The Maxwell stage (EMFieldSolver::RGKStep) writes A and a^2, which the Vlasov
@@ -1126,7 +1134,7 @@ std::vector<double> Engine::calculate_dt(const std::vector<Run *> &set) {
 // E_x on the finest grid from the current phi and Ex0 (after a state was loaded).
 void Engine::refresh_efield(Run &run) {
     LaunchSet &L = get_set({&run});
-    launch_efield(L.dfields.as<RunFields>(), L.dfcoef.as<double>(), 1, L.maxn, stream);
+    launch_efield(L.dfields.as<RunFields>(), L.dfcoef.as<double>(), 1, L.maxn, L.precision == kF32, stream);
     kernel_launches += 1;
 }
 
@@ -1142,6 +1150,7 @@ void Engine::advance_fields(const std::vector<Run *> &set, const std::vector<dou
     mx.maxnf = L.maxnf;
     mx.params = L.dparams.as<double>();
     mx.dxinv = L.ddxinv.as<double>();
+    mx.f32 = L.precision == kF32;
     mx.stream = stream;
     for (int s = 0; s < 6; s++) {
         mx.step = s;

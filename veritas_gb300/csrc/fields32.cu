@@ -185,12 +185,13 @@ __global__ void k_acell32(const RunFields *fields, int nruns) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= F.nf) return;
     const double ay = F.Ay[F.nf + x], az = F.Az[F.nf + x];
-    F.acell32[x] = (float)((ay * ay) + (az * az));
+    // unfused, as the Maxwell update kernel forms the same copy (FP64 unit, no contraction)
+    F.acell32[x] = (float)__dadd_rn(__dmul_rn(ay, ay), __dmul_rn(az, az));
 }
 
 void launch_moments32(const MomLaunch &M) {
     if (M.ncols == 0) return;
-    vx_launch(k_acell32, dim3((M.maxnf + 255) / 256, M.nruns), 256, 0, M.stream, M.fields, M.nruns);
+    if (M.acell) vx_launch(k_acell32, dim3((M.maxnf + 255) / 256, M.nruns), 256, 0, M.stream, M.fields, M.nruns);
     const int threads = 256;
     const int blocks = (M.ncols * 32 + threads - 1) / threads;
     vx_launch(k32_moments, blocks, threads, 0, M.stream, M);

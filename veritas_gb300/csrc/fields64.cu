@@ -711,19 +711,21 @@ void launch_poisson(const PoissonLaunch &L) {
 
 // E_x on the finest grid from phi and Ex0 (EMSolver::GetEfield), for states loaded from
 // outside the step.
-__global__ void k_efield(RunFields *fields, const double *fcoef, int nruns) {
+__global__ void k_efield(RunFields *fields, const double *fcoef, int nruns, int f32) {
     VX_PDL_WAIT();
     const int run = blockIdx.y;
     if (run >= nruns) return;
     RunFields &F = fields[run];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n) return;
-    F.efin[i] = efield_at(F.phi, F.n, fcoef[run], *F.ex0, i);
+    const double e = efield_at(F.phi, F.n, fcoef[run], *F.ex0, i);
+    F.efin[i] = e;
+    if (f32) F.efin32[i] = (float)e;
 }
 
-void launch_efield(RunFields *fields, const double *fcoef, int nruns, int maxn, cudaStream_t s) {
+void launch_efield(RunFields *fields, const double *fcoef, int nruns, int maxn, int f32, cudaStream_t s) {
     dim3 g((maxn + 255) / 256, nruns);
-    vx_launch(k_efield, g, 256, 0, s, fields, fcoef, nruns);
+    vx_launch(k_efield, g, 256, 0, s, fields, fcoef, nruns, f32);
 }
 
 // ---------------------------------------------------------------- Maxwell
@@ -806,6 +808,10 @@ __global__ void k_mx_update(MaxwellLaunch L) {
     mx_combine(F.Ez, F.nf, i, L.step, c);
     mx_combine(F.Ay, F.nf, i, L.step, c);
     mx_combine(F.Az, F.nf, i, L.step, c);
+    if (L.f32) {  // the per-cell A^2 the next stage's FP32 moments read (as k_acell32)
+        const double ay = F.Ay[F.nf + i], az = F.Az[F.nf + i];
+        F.acell32[i] = (float)((ay * ay) + (az * az));
+    }
 }
 
 // WENO-weighted (unmapped) face value of A (EMSolver.cpp:555-619).

@@ -246,7 +246,7 @@ void launch_poisson_fast(const PoissonFastLaunch &L) {
     const size_t smem = poisson_scan_smem(L.maxn);
     cudaFuncSetAttribute(k_poisson_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     vx_launch(k_poisson_scan, L.nruns * kPsCluster, scan_threads(L.maxn), smem, L.stream, L);
-    launch_efield(L.fields, L.fcoef, L.nruns, L.maxn, L.stream);
+    launch_efield(L.fields, L.fcoef, L.nruns, L.maxn, L.f32, L.stream);
 }
 
 }  // namespace vx

@@ -90,6 +90,7 @@ struct MomLaunch {
     int maxnp;            // largest n_p over the patches
     const RunFields *fields;
     int nruns, maxnf;     // FP32: the per-cell A^2 copy covers every run's field grid
+    int acell = 1;        // FP32: refresh the per-cell A^2 copy first (else the Maxwell stage made it)
     cudaStream_t stream;
 };
 constexpr int kMomCols = 16;  // FP64 moment columns per block (padded per patch)
@@ -166,6 +167,7 @@ struct PoissonFastLaunch {
     const double *fcoef;       // per run: 1/(12 dx0)
     int nruns;
     int maxn;                  // largest n of the runs
+    int f32;                   // also write the FP32 copy of E_x (precision-32 sets)
     cudaStream_t stream;
 };
 void launch_poisson_fast(const PoissonFastLaunch &L);
@@ -173,7 +175,8 @@ size_t poisson_scan_smem(int maxn);  // dynamic shared memory of one block
 // FP32 copies of a^2 (which & 1) and E_x (which & 2) of every run of a set (the FP32 form
 // reads these).
 void launch_fields_to_f32(RunFields *fields, int nruns, int maxn, int which, cudaStream_t s);
-void launch_efield(RunFields *fields, const double *fcoef, int nruns, int maxn, cudaStream_t s);
+// E_x from phi; f32 != 0 also writes its FP32 copy (precision-32 sets).
+void launch_efield(RunFields *fields, const double *fcoef, int nruns, int maxn, int f32, cudaStream_t s);
 
 // Maxwell RK stage + face interpolation of A (EMSolver::RGKStep).
 struct MaxwellLaunch {
@@ -182,6 +185,7 @@ struct MaxwellLaunch {
     int step;
     const double *params;  // per-run stage parameter blocks
     const double *dxinv;   // per run: 1/dx0
+    int f32;               // precision-32 sets: also the FP32 per-cell A^2 (k_mx_update)
     cudaStream_t stream;
 };
 void launch_maxwell(const MaxwellLaunch &L);
