@@ -536,6 +536,17 @@ def main() -> None:
                               "rounding order: one thread's FP64 latency chain, not bandwidth, bounds it"
                               if dom == "poisson" else "FP64 issue rate is the binding roofline of the plain path"),
                      "kernel_ms": prof, "kernel_share": {k: share[k] / tot for k in share}})
+    if dom == "poisson":
+        # the solve's own bound: per row, forward one dependent multiply-subtract and the
+        # shuffle that hands x_{i-1} to the lanes, backward the multiply-subtract, the
+        # two-operation quotient and the shuffle; cycles measured live on one lane
+        ms_cyc, sh_cyc = ctx.measure_fp64_latency()
+        mhz = clk.summary().get("sm_mhz") or 2070.0
+        row_cyc = (ms_cyc + sh_cyc) + (2 * ms_cyc + sh_cyc)
+        min_ms = n_fine * row_cyc / (mhz * 1e3)
+        roofline["latency"] = {"bound": "FP64 dependent chain", "mul_sub_cycles": ms_cyc, "shuffle_cycles": sh_cyc,
+                               "cycles_per_row": row_cyc, "rows": n_fine, "sm_mhz": mhz, "min_ms": min_ms,
+                               "achieved_ms": prof["poisson"], "frac": min_ms / prof["poisson"]}
     stencil = max((k for k in share if k in KERNEL_BYTES and KERNEL_BYTES[k] > 0), key=share.get)
     roofline["stencil"] = kernel_roofline(stencil)
     roofline["stencil"]["kernel"] = KERNEL_NAMES.get(stencil, stencil)

@@ -200,6 +200,10 @@ int vx_ctx_flush_l2(vx_ctx *ctx);
 /* Measured FP64 FMA throughput of this GPU in GFLOP/s (2 flops per FMA): a register-
  * resident DFMA chain kernel timed with CUDA events on the context stream. */
 int vx_ctx_measure_fp64_peak(vx_ctx *ctx, double *gflops);
+/* Dependent-chain latency of one lane in SM clock cycles: a multiply followed by a
+ * subtract (the triangular solves' step) and the extra cost of a 64-bit shuffle in the
+ * chain.  With them the exact Poisson solve's latency bound is stated. */
+int vx_ctx_measure_fp64_latency(vx_ctx *ctx, double *mul_sub_cycles, double *shfl_cycles);
 
 /* Page-locked host memory for host-buffer calls. */
 int vx_host_alloc(size_t bytes, void **out);

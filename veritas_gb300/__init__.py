@@ -108,6 +108,7 @@ def _load() -> ctypes.CDLL:
         "vx_run_profile_kernels": (ctypes.c_int, [vp, ctypes.c_int, P(ctypes.c_double), ctypes.c_int, P(ctypes.c_int)]),
         "vx_ctx_flush_l2": (ctypes.c_int, [vp]),
         "vx_ctx_measure_fp64_peak": (ctypes.c_int, [vp, P(ctypes.c_double)]),
+        "vx_ctx_measure_fp64_latency": (ctypes.c_int, [vp, P(ctypes.c_double), P(ctypes.c_double)]),
         "vx_host_alloc": (ctypes.c_int, [ctypes.c_size_t, P(vp)]),
         "vx_host_free": (ctypes.c_int, [vp]),
         "vx_run_state_size": (ctypes.c_int, [vp, P(ctypes.c_int64)]),
@@ -221,6 +222,12 @@ class Context:
 
     def flush_l2(self) -> None:
         _check(_lib.vx_ctx_flush_l2(self._h))
+
+    def measure_fp64_latency(self) -> tuple[float, float]:
+        """(cycles of a dependent multiply + subtract, extra cycles of a 64-bit shuffle)."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(_lib.vx_ctx_measure_fp64_latency(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return float(a.value), float(b.value)
 
     def measure_fp64_peak(self) -> float:
         v = ctypes.c_double()

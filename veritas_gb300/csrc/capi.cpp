@@ -433,6 +433,11 @@ int vx_ctx_flush_l2(vx_ctx *ctx) {
     return guard([&] { ctx->eng->flush_l2(); });
 }
 
+int vx_ctx_measure_fp64_latency(vx_ctx *ctx, double *mul_sub_cycles, double *shfl_cycles) {
+    if (!ctx || !mul_sub_cycles || !shfl_cycles) return VX_ERR_INVALID;
+    return guard([&] { ctx->eng->measure_fp64_latency(mul_sub_cycles, shfl_cycles); });
+}
+
 int vx_ctx_measure_fp64_peak(vx_ctx *ctx, double *gflops) {
     if (!ctx || !gflops) return VX_ERR_INVALID;
     return guard([&] { *gflops = ctx->eng->measure_fp64_peak(); });

@@ -506,6 +506,21 @@ double Engine::measure_fp64_peak() {
     return flops / (ms * 1e-3) / 1e9;
 }
 
+void Engine::measure_fp64_latency(double *mul_sub_cycles, double *shfl_cycles) {
+    if (!flush_.p) flush_ = DevBuf((size_t)512 << 20);
+    const int iters = 4096;
+    long long *cyc = flush_.as<long long>();
+    double *val = flush_.as<double>() + 2;
+    launch_fp64_latency(cyc, val, iters, stream);  // warm-up
+    launch_fp64_latency(cyc, val, iters, stream);
+    kernel_launches += 2;
+    long long h[2];
+    VX_CUDA(cudaMemcpyAsync(h, cyc, sizeof h, cudaMemcpyDeviceToHost, stream));
+    VX_CUDA(cudaStreamSynchronize(stream));
+    *mul_sub_cycles = (double)h[0] / iters;
+    *shfl_cycles = (double)(h[1] - h[0]) / iters;
+}
+
 // Precision dispatch of the per-stage kernels of a launch set.
 static void fct_sub(const LaunchSet &L, const FctLaunch &fl, int sub) {
     if (L.precision == kF32) launch_fct32_substep(fl, sub);

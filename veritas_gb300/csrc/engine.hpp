@@ -234,6 +234,7 @@ public:
     double timer_end();
     void flush_l2();
     double measure_fp64_peak();
+    void measure_fp64_latency(double *mul_sub_cycles, double *shfl_cycles);
     void sync();
     void forget(Run *r);
     // Times the FCT sub-step kernels of the set for each candidate tile shape and keeps

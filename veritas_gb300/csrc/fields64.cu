@@ -933,4 +933,31 @@ __global__ void k_fp64_peak(double *out, int iters) {
 void launch_fp64_peak(double *out, int blocks, int threads, int iters, cudaStream_t s) {
     vx_launch(k_fp64_peak, blocks, threads, 0, s, out, iters);
 }
+
+// Dependent-chain latency on one lane: iters steps of the substitution's multiply-
+// subtract, then the same with a 64-bit shuffle in the chain (clock64 cycles, into
+// cyc[0] and cyc[1]; the chains' values into val so that they are not eliminated).
+__global__ void k_fp64_latency(long long *cyc, double *val, int iters) {
+    VX_PDL_WAIT();
+    double x = 1.0 + threadIdx.x * 1e-3;
+    const double c = 0.999999, v = 1e-7;
+    long long t0 = clock64();
+    for (int k = 0; k < iters; k++) x = v - x * c;
+    long long t1 = clock64();
+    double y = x;
+    for (int k = 0; k < iters; k++) {
+        y = v - y * c;
+        y = __shfl_sync(0xffffffffu, y, 0);
+    }
+    long long t2 = clock64();
+    if (threadIdx.x == 0) {
+        cyc[0] = t1 - t0;
+        cyc[1] = t2 - t1;
+        val[0] = x + y;
+    }
+}
+
+void launch_fp64_latency(long long *cyc, double *val, int iters, cudaStream_t s) {
+    vx_launch(k_fp64_latency, 1, 32, 0, s, cyc, val, iters);
+}
 }  // namespace vx

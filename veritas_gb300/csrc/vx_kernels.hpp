@@ -206,6 +206,8 @@ void launch_fill_separable(float *f0, float *f1, int pitch, int nx, int np, cons
                            const double *dp_sum, double inv, double fn, cudaStream_t s);
 // FP64 FMA throughput probe: blocks x threads threads, iters x 8 independent DFMA each.
 void launch_fp64_peak(double *out, int blocks, int threads, int iters, cudaStream_t s);
+// One warp: cycles of iters dependent (multiply, subtract) steps, then with a shuffle each.
+void launch_fp64_latency(long long *cyc, double *val, int iters, cudaStream_t s);
 
 // AMR op batches (amr.hpp, amr64.cu)
 struct GhostOp;
