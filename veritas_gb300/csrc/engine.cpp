@@ -965,8 +965,8 @@ void Engine::record_step(LaunchSet &L) {
     for (int s = 0; s < 6; s++) {
         // FP32 copies of the fields: E_x's comes with each solve (k_efield), the per-cell
         // A^2 the moments read with each Maxwell stage for the next one (the step's first
-        // stage makes its own).  a^2's is made at every stage: the Maxwell stage runs
-        // beside the face kernels that read it.
+        // stage makes its own), a^2's with the moments at every stage (the Maxwell stage
+        // runs beside the face kernels that read it, so it cannot write the copy).
         ml.acell = s == 0;
         run_moments(L, ml);
         launch_assemble(al);
@@ -978,10 +978,6 @@ void Engine::record_step(LaunchSet &L) {
         pl.stream = side;
         run_poisson(L, pl);
         launches += L.poisson == kPoissonScan ? 2 : 1;
-        if (L.precision == kF32) {
-            launch_fields_to_f32(L.dfields.as<RunFields>(), (int)L.runs.size(), L.maxn, 1, stream);
-            launches += 1;
-        }
         fl.step = s;
         // The Maxwell stage (EMFieldSolver::RGKStep) writes A and a^2, which the Vlasov
         // stage reads only in the gamma kernel (FP64) or the FP32 copy of a^2 made above;

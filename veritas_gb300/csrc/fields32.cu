@@ -165,6 +165,16 @@ __device__ __forceinline__ void moments_group(const P32 &P, const RunFields &F, 
 // assembly, which scales them in FP64.
 __global__ void k32_moments(MomLaunch M) {
     VX_PDL_WAIT();
+    if (M.asq32) {
+        // the FP32 copy of a^2 that this stage's face kernels read (the Maxwell stage,
+        // which rewrites a^2, starts only after this kernel)
+        const int per = M.maxnf + 1;
+        for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < M.nruns * per; e += gridDim.x * blockDim.x) {
+            const RunFields &F = M.fields[e / per];
+            const int x = e % per;
+            if (x <= F.n) F.asq32[x] = (float)F.asq[x];
+        }
+    }
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= M.ncols) return;
@@ -195,22 +205,6 @@ void launch_moments32(const MomLaunch &M) {
     const int threads = 256;
     const int blocks = (M.ncols * 32 + threads - 1) / threads;
     vx_launch(k32_moments, blocks, threads, 0, M.stream, M);
-}
-
-__global__ void k_fields_to_f32(RunFields *fields, int nruns, int which) {
-    VX_PDL_WAIT();
-    const int run = blockIdx.y;
-    if (run >= nruns) return;
-    RunFields &F = fields[run];
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if ((which & 1) && x <= F.n) F.asq32[x] = (float)F.asq[x];
-    if ((which & 2) && x < F.n) F.efin32[x] = (float)F.efin[x];
-}
-
-void launch_fields_to_f32(RunFields *fields, int nruns, int maxn, int which, cudaStream_t s) {
-    if (nruns == 0) return;
-    dim3 g((maxn + 1 + 255) / 256, nruns);
-    vx_launch(k_fields_to_f32, g, 256, 0, s, fields, nruns, which);
 }
 
 }  // namespace vx

@@ -91,6 +91,7 @@ struct MomLaunch {
     const RunFields *fields;
     int nruns, maxnf;     // FP32: the per-cell A^2 copy covers every run's field grid
     int acell = 1;        // FP32: refresh the per-cell A^2 copy first (else the Maxwell stage made it)
+    int asq32 = 1;        // FP32: the moments kernel also makes the FP32 copy of a^2
     cudaStream_t stream;
 };
 constexpr int kMomCols = 16;  // FP64 moment columns per block (padded per patch)
@@ -172,9 +173,6 @@ struct PoissonFastLaunch {
 };
 void launch_poisson_fast(const PoissonFastLaunch &L);
 size_t poisson_scan_smem(int maxn);  // dynamic shared memory of one block
-// FP32 copies of a^2 (which & 1) and E_x (which & 2) of every run of a set (the FP32 form
-// reads these).
-void launch_fields_to_f32(RunFields *fields, int nruns, int maxn, int which, cudaStream_t s);
 // E_x from phi; f32 != 0 also writes its FP32 copy (precision-32 sets).
 void launch_efield(RunFields *fields, const double *fcoef, int nruns, int maxn, int f32, cudaStream_t s);
 
