@@ -873,6 +873,32 @@ void Engine::build_set(LaunchSet &L) {
                [](Run &R) -> const std::vector<int> & { return R.csync_b.ptr; }, merge_csync_ops, L.dcsync,
                L.csync_ptr);
     }
+    // Moment work units (FP64: blocks of kMomCols columns of one patch; FP32: one column
+    // per warp) longest first: a unit's time grows with its patch's n_p and sub-columns,
+    // and the GPU schedules blocks in list order, so the short units of the fine levels
+    // fill the tail instead of leaving a last wave of long base-level blocks alone on a
+    // few SMs.  Each column's result is independent of the order.
+    {
+        const int unit = L.precision == kF64 ? kMomCols : 1;
+        const int nunits = (int)colpatch.size() / unit;
+        auto cost = [&](int u) {
+            const PatchT<double> &d = L.hpatch[colpatch[(size_t)u * unit]];
+            return (long long)(d.np + 2) * ((d.rtb + 1) / 2);
+        };
+        std::vector<int> order(nunits);
+        for (int u = 0; u < nunits; u++) order[u] = u;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+        std::vector<int> cp2, ci2;
+        cp2.reserve(colpatch.size());
+        ci2.reserve(colidx.size());
+        for (int u : order)
+            for (int k = 0; k < unit; k++) {
+                cp2.push_back(colpatch[(size_t)u * unit + k]);
+                ci2.push_back(colidx[(size_t)u * unit + k]);
+            }
+        colpatch.swap(cp2);
+        colidx.swap(ci2);
+    }
     L.ncols = (int)colpatch.size();
     // lvl_ptr is absolute; lvl_off points at each run's block.
     L.dpatch = upload(L.hpatch, stream);
