@@ -51,6 +51,10 @@ CASES = {
     # two-level hierarchy; moments, Poisson and CFL sum over both.
     "ions2": (["L=8", "nx=64", "np=32", "Te=50", "pmax=2", "x1=1.5", "x2=2", "x3=6", "x4=6.5", "pert_amp=0.2",
                "pert_k=2", "a0=2", "fwhm=2", "delay=1", "mi=4", "iTe=50", "ipmax=0.6", "levels=2"], 3, [0, 1, 3]),
+    # Ragged sizes: 50 x 38 base cells (n_p not a multiple of 8 or of the kernels' tiles,
+    # n_x not a multiple of 8), one fine patch of 68 x 64.
+    "ragged2": (["L=8", "nx=50", "np=38", "Te=50", "pmax=2", "x1=1.5", "x2=2", "x3=6", "x4=6.5", "pert_amp=0.2",
+                 "pert_k=2", "a0=2", "fwhm=2", "delay=1", "levels=2"], 3, [0, 1, 3]),
 }
 
 
@@ -58,6 +62,7 @@ CASES = {
 # SolverManager::reGrid ("_pre"), just after it ("_post") and one step later ("_post1").
 REGRID = {
     "amr2": 4,
+    "ragged2": 4,
     "ions2": 4,
     "beam2": 4,
     "beam3": 4,

@@ -80,7 +80,7 @@ def test_port_detects_planted_error(port, tmp_path):
     assert err["f"] > 0.0
 
 
-@pytest.mark.parametrize("name,k0,k1", [("amr2", 0, 3), ("beam2", 1, 3), ("beam3", 0, 3)])
+@pytest.mark.parametrize("name,k0,k1", [("amr2", 0, 3), ("beam2", 1, 3), ("beam3", 0, 3), ("ragged2", 0, 3)])
 def test_port_amr_steps_match_reference(port, tmp_path, name, k0, k1):
     """Multi-level step (ghost fills, interface fluxes, limiter exchange, nested moments)
     from a reference state with the port's own dt."""
@@ -95,7 +95,7 @@ def test_port_amr_steps_match_reference(port, tmp_path, name, k0, k1):
         assert max(err.values()) == 0.0, (k, err)
 
 
-@pytest.mark.parametrize("name", ["amr2", "beam2", "beam3"])
+@pytest.mark.parametrize("name", ["amr2", "beam2", "beam3", "ragged2"])
 def test_port_amr_step_after_regrid(port, tmp_path, name):
     from helpers import golden_named
 

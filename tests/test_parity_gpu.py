@@ -14,7 +14,7 @@ from helpers import compare_states, golden, golden_named, problem_for, total_mas
 
 TOL = 1e-10
 ONE_STEP = [("slab64", 0), ("slab64", 1), ("drift128", 0), ("edge64", 0),
-            ("amr2", 0), ("beam2", 0), ("beam3", 0), ("ions2", 0)]
+            ("amr2", 0), ("beam2", 0), ("beam3", 0), ("ions2", 0), ("ragged2", 0)]
 
 
 @pytest.fixture(scope="module")
@@ -51,7 +51,7 @@ def test_one_step_from_reference_state(ctx, tmp_path, name, k):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name,k0,k1", [("slab64", 0, 5), ("drift128", 1, 3), ("edge64", 1, 3), ("amr2", 1, 3),
-                                        ("ions2", 1, 3),
+                                        ("ions2", 1, 3), ("ragged2", 0, 3),
                                         ("beam2", 1, 3), ("beam3", 0, 3)])
 def test_multi_step_with_own_dt(ctx, tmp_path, name, k0, k1):
     s = _solver(ctx, name)
@@ -90,7 +90,7 @@ def _check(got, ref, label):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["amr2", "beam2", "beam3", "ions2"])
+@pytest.mark.parametrize("name", ["amr2", "beam2", "beam3", "ions2", "ragged2"])
 def test_initial_hierarchy_matches_reference(ctx, tmp_path, name):
     """Mesh::Mesh: base level, maxDepth rounds of flagging / clustering with every patch
     from the quadrature, then the ghost fill and the neutralising charge."""
@@ -101,7 +101,7 @@ def test_initial_hierarchy_matches_reference(ctx, tmp_path, name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["amr2", "beam2", "beam3", "ions2"])
+@pytest.mark.parametrize("name", ["amr2", "beam2", "beam3", "ions2", "ragged2"])
 def test_regrid_matches_reference(ctx, tmp_path, name):
     """SolverManager::reGrid on the reference's state: the new layout, the transferred
     f (slots 0 and 1, ghosts included), then one step on the new layout."""

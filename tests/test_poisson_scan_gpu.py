@@ -16,7 +16,7 @@ import vxstate
 from helpers import compare_states, golden, problem_for
 
 TOL = 1e-10
-ONE_STEP = [("slab64", 0), ("drift128", 0), ("edge64", 0), ("amr2", 0), ("beam2", 0), ("beam3", 0), ("ions2", 0)]
+ONE_STEP = [("slab64", 0), ("drift128", 0), ("edge64", 0), ("amr2", 0), ("beam2", 0), ("beam3", 0), ("ions2", 0), ("ragged2", 0)]
 
 
 @pytest.fixture(scope="module")

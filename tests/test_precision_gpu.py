@@ -84,7 +84,7 @@ def problem_for_precision(prob, precision):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name,k", [("slab64", 0), ("drift128", 0), ("amr2", 0), ("beam2", 0), ("beam3", 0),
-                                    ("ions2", 0)])
+                                    ("ions2", 0), ("ragged2", 0)])
 def test_fp32_form_error_vs_fp64(ctx, tmp_path, name, k):
     ef, errs = run_pair(ctx, tmp_path, problem_for(name), golden(name, k), steps=5)
     ew = max(e["W"] for e in errs)

@@ -12,7 +12,7 @@ import pytest
 
 from helpers import golden_named, problem_for
 
-CASES = ["amr2", "beam2", "beam3"]
+CASES = ["amr2", "beam2", "beam3", "ragged2"]
 
 
 def _flags(st, prob, maxdepth):
