@@ -190,6 +190,22 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def max_over_ranks(total_ms: float, dist, device: str) -> float:
+    """The job's timed-region length: the slowest rank's (all-reduce MAX), then a barrier
+    so that no rank starts the next phase while another is still timing."""
+    import torch
+
+    t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def job_value(cells_per_rank: int, world: int, steps: int, total_ms: float) -> float:
+    """Whole-job cell-updates/s: every rank advances its own replica of the workload."""
+    return cells_per_rank * world * steps / (total_ms * 1e-3)
+
+
 def dist_info():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -470,14 +486,9 @@ def main() -> None:
     launches = ctx.kernel_launches() - l0 - args.steps  # minus the flush memsets (not kernels of ours)
     total_ms = sum(times)
     if dist:
-        import torch
-
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        dist.barrier()
+        total_ms = max_over_ranks(total_ms, dist, f"cuda:{local}")
     ms_step = total_ms / args.steps
-    value = cells * world * args.steps / (total_ms * 1e-3)
+    value = job_value(cells, world, args.steps, total_ms)
     if args.lite:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms_step, "lite": True}))
