@@ -141,3 +141,16 @@ def test_file_output_selected_and_appended(ctx, tmp_path):
     assert sorted(p.name for p in out.iterdir()) == ["charge.txt", "time.txt"]
     assert len((out / "charge.txt").read_text().splitlines()) == 3
     assert (out / "time.txt").read_text().splitlines() == ["0.000000e+00"] * 3
+
+
+@pytest.mark.gpu
+def test_file_output_missing_directory_is_an_io_error(ctx, tmp_path):
+    from veritas_gb300 import SolverManager, VxError
+
+    s = SolverManager(ctx, problem_for("slab64"))
+    with pytest.raises(VxError) as e:
+        s.fileOutput(s.time, tmp_path / "absent")
+    assert e.value.code == -4  # VX_ERR_IO
+    with pytest.raises(VxError):
+        s.OutputRectangles(s.time, tmp_path / "absent")
+    s.close()
