@@ -1003,7 +1003,7 @@ void Engine::record_step(LaunchSet &L) {
         VX_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
         pl.stream = side;
         run_poisson(L, pl);
-        launches += L.poisson == kPoissonScan ? 2 : 1;
+        launches += 1;  // the scan solve forms E_x itself
         fl.step = s;
         // The Maxwell stage (EMFieldSolver::RGKStep) writes A and a^2, which the Vlasov
         // stage reads only in the gamma kernel (FP64) or the FP32 copy of a^2 made above;

@@ -220,8 +220,18 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsMaxThrea
         const double e_m1 = efield_at(phi, n, P.fcoef[run], ex0, -1);
         const double e_0 = efield_at(phi, n, P.fcoef[run], ex0, 0);
         *F.ex0 = ex0 + -(e_m1 + e_0) * 0.5;
+        __threadfence();
     }
-    // E_x on the finest grid follows in k_efield (all blocks of the device)
+    cl.sync();  // phi[0] and the new Ex0 are visible to every block of the cluster
+    // E_x on the finest grid (EMFieldSolver::GetEfield), each block a contiguous share
+    const double ex0 = __ldcg(F.ex0), fc = P.fcoef[run];
+    const int share = (n + kPsCluster - 1) / kPsCluster;
+    const int i1 = min(n, (rank + 1) * share);
+    for (int i = rank * share + threadIdx.x; i < i1; i += T) {
+        const double e = efield_at(F.phi, n, fc, ex0, i);
+        F.efin[i] = e;
+        if (P.f32) F.efin32[i] = (float)e;
+    }
 }
 
 // Threads per block: segments of about 8 elements (a decaying pass then gathers three
@@ -246,7 +256,6 @@ void launch_poisson_fast(const PoissonFastLaunch &L) {
     const size_t smem = poisson_scan_smem(L.maxn);
     cudaFuncSetAttribute(k_poisson_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     vx_launch(k_poisson_scan, L.nruns * kPsCluster, scan_threads(L.maxn), smem, L.stream, L);
-    launch_efield(L.fields, L.fcoef, L.nruns, L.maxn, L.f32, L.stream);
 }
 
 }  // namespace vx
