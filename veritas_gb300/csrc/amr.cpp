@@ -6,7 +6,6 @@
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
-#include <stdexcept>
 #include <unordered_map>
 
 #include "engine.hpp"
@@ -280,29 +279,6 @@ void Run::validate_ops() const {
              "limiter faces");
     }
     if (r > 8) throw std::invalid_argument("refinement ratio above 8 is not supported");
-}
-
-std::vector<GhostOpDev> pack_ghost_ops(const std::vector<GhostOp> &ops) {
-    std::vector<GhostOpDev> out(ops.size());
-    auto fit16 = [](int v) {
-        if (v < -32768 || v > 32767) throw std::invalid_argument("ghost op field out of the 16-bit range");
-        return (int16_t)v;
-    };
-    for (size_t k = 0; k < ops.size(); k++) {
-        const GhostOp &o = ops[k];
-        if (o.sub < 0 || o.sub > 255) throw std::invalid_argument("ghost op interpolation entry out of range");
-        GhostOpDev &d = out[k];
-        d.dst = fit16(o.dst);
-        d.src = fit16(o.src);
-        d.di = fit16(o.di);
-        d.dj = fit16(o.dj);
-        d.si = fit16(o.si);
-        d.sj = fit16(o.sj);
-        d.kind = (uint8_t)o.kind;
-        d.sub = (uint8_t)o.sub;
-        d.pad = 0;
-    }
-    return out;
 }
 
 void Run::build_amr() {
@@ -632,7 +608,7 @@ void Run::build_amr() {
     }
     sort_by_batch(csync_ops, cs.batch, cs.nbatches, csync_b);
     validate_ops();
-    dghost_ops = upload(pack_ghost_ops(ghost_ops), eng.stream);
+    dghost_ops = upload(ghost_ops, eng.stream);
     diface_ops = upload(iface_ops, eng.stream);
     dcsync_ops = upload(csync_ops, eng.stream);
     lap("csync ops");

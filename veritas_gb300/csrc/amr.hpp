@@ -31,18 +31,6 @@ struct GhostOp {
     int sub;
 };
 
-// The same record packed for the device: 16 bytes, read as one 128-bit load (patch ids
-// below 32768 in a launch set, cell indices within [-32768, 32767], sub < 256).
-struct alignas(16) GhostOpDev {
-    int16_t dst, src;
-    int16_t di, dj, si, sj;
-    uint8_t kind, sub;
-    int16_t pad;
-};
-static_assert(sizeof(GhostOpDev) == 16, "packed ghost op");
-// Packs ops for the device; throws std::invalid_argument when a field does not fit.
-std::vector<GhostOpDev> pack_ghost_ops(const std::vector<GhostOp> &ops);
-
 enum CSyncKind : int { kCSame = 0, kCDiff = 1, kCUpdate = 2 };
 
 // kCSame / kCUpdate: one face k of SetCFromSameLevel / UpdateCFromSameLevel: patch nb's

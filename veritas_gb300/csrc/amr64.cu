@@ -68,11 +68,11 @@ __device__ T coarse_interp(const PatchT<T> &C, const T *f, int ic, int jc, int s
 }
 
 template <class T>
-__global__ void k_ghost(const PatchT<T> *patches, const GhostOpDev *ops, int n, int slot) {
+__global__ void k_ghost(const PatchT<T> *patches, const GhostOp *ops, int n, int slot) {
     VX_PDL_WAIT();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const GhostOpDev op = ops[k];
+    const GhostOp op = ops[k];
     const PatchT<T> &D = patches[op.dst];
     T v = 0;
     if (op.kind == kGhostCopy) {
@@ -279,9 +279,9 @@ void launch_xfer(const void *patches, const XferOp *ops, int n, uint8_t *mask, i
 }
 
 // One block per segment: copy its ops and make their patch ids global to the set.
-__device__ __forceinline__ void rebase(GhostOpDev &op, int b) {  // b + id < 32768: build_set checks
-    op.dst = (int16_t)(op.dst + b);
-    if (op.src >= 0) op.src = (int16_t)(op.src + b);
+__device__ __forceinline__ void rebase(GhostOp &op, int b) {
+    op.dst += b;
+    if (op.src >= 0) op.src += b;
 }
 __device__ __forceinline__ void rebase(IfaceOp &op, int b) {
     op.coarse += b;
@@ -302,8 +302,8 @@ __global__ void k_merge_ops(const OpSegment *segs, Op *dst) {
         dst[sg.dst_off + k] = op;
     }
 }
-void merge_ghost_ops(const OpSegment *segs, int nseg, GhostOpDev *dst, cudaStream_t s) {
-    if (nseg > 0) vx_launch(k_merge_ops<GhostOpDev>, nseg, 256, 0, s, segs, dst);
+void merge_ghost_ops(const OpSegment *segs, int nseg, GhostOp *dst, cudaStream_t s) {
+    if (nseg > 0) vx_launch(k_merge_ops<GhostOp>, nseg, 256, 0, s, segs, dst);
 }
 void merge_iface_ops(const OpSegment *segs, int nseg, IfaceOp *dst, cudaStream_t s) {
     if (nseg > 0) vx_launch(k_merge_ops<IfaceOp>, nseg, 256, 0, s, segs, dst);
@@ -312,7 +312,7 @@ void merge_csync_ops(const OpSegment *segs, int nseg, CSyncOp *dst, cudaStream_t
     if (nseg > 0) vx_launch(k_merge_ops<CSyncOp>, nseg, 256, 0, s, segs, dst);
 }
 
-void launch_ghost(const void *patches, const GhostOpDev *ops, int n, int slot, int prec, cudaStream_t s) {
+void launch_ghost(const void *patches, const GhostOp *ops, int n, int slot, int prec, cudaStream_t s) {
     if (n <= 0) return;
     if (prec == kF32) vx_launch(k_ghost<float>, (n + 127) / 128, 128, 0, s, (const PatchT<float> *)patches, ops, n, slot);
     else vx_launch(k_ghost<double>, (n + 127) / 128, 128, 0, s, (const PatchT<double> *)patches, ops, n, slot);

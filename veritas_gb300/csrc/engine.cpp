@@ -647,7 +647,7 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     // the AMR op batches of one stage (each entry: all batches of that kind)
     time_it([&] {
         for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++)
-            launch_ghost(L.dpatch.p, L.dghost.as<GhostOpDev>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, L.precision, stream);
+            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, L.precision, stream);
     });
     time_it([&] {
         for (size_t b = 0; b + 1 < L.iface_ptr.size(); b++)
@@ -832,8 +832,6 @@ void Engine::build_set(LaunchSet &L) {
         sp[24] = dpsMax;
         spec.insert(spec.end(), sp.begin(), sp.end());
     }
-    // packed ghost ops address patches with 16-bit ids
-    if (L.hpatch.size() > 32767) throw std::invalid_argument("a launch set holds at most 32767 patches");
     // AMR op tables: batch b of the set = batch b of every run, patch ids made global.
     // Each run's sorted lists already sit on the device; the set's tables are gathered
     // there, one segment per (batch, run), so a new set costs no host-side op copies.
@@ -865,7 +863,7 @@ void Engine::build_set(LaunchSet &L) {
                 sync();  // dsegs is released at the end of this scope
             }
         };
-        gather(GhostOpDev{}, [](Run &R) -> DevBuf & { return R.dghost_ops; },
+        gather(GhostOp{}, [](Run &R) -> DevBuf & { return R.dghost_ops; },
                [](Run &R) -> const std::vector<int> & { return R.ghost_b.ptr; }, merge_ghost_ops, L.dghost,
                L.ghost_ptr);
         gather(IfaceOp{}, [](Run &R) -> DevBuf & { return R.diface_ops; },
@@ -1059,7 +1057,7 @@ void Engine::record_step(LaunchSet &L) {
         fct_sub(L, fl, kSubDsF2);
         launches += 1;
         for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
-            launch_ghost(L.dpatch.p, L.dghost.as<GhostOpDev>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 2, L.precision, stream);
+            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 2, L.precision, stream);
         fct_sub(L, fl, kSubLimR);
         fct_sub(L, fl, kSubLimC);
         launches += 2;
@@ -1068,7 +1066,7 @@ void Engine::record_step(LaunchSet &L) {
         fct_sub(L, fl, kSubUpdate);
         launches += 1;
         for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
-            launch_ghost(L.dpatch.p, L.dghost.as<GhostOpDev>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, L.precision, stream);
+            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, L.precision, stream);
         if (s == 5) {
             fct_sub(L, fl, kSubCopy10);
             launches += 1;

@@ -572,9 +572,9 @@ DevBuf Run::flat_descs() {
 // Mesh::PushData(val) (Mesh.cpp:91-106) for this run alone.
 void Run::push_data(int slot) {
     DevBuf dd = flat_descs();
-    DevBuf dops = upload(pack_ghost_ops(ghost_ops), eng.stream);
+    DevBuf dops = upload(ghost_ops, eng.stream);
     for (size_t b = 0; b + 1 < ghost_b.ptr.size(); b++)
-        launch_ghost(dd.p, dops.as<GhostOpDev>() + ghost_b.ptr[b], ghost_b.ptr[b + 1] - ghost_b.ptr[b], slot, precision,
+        launch_ghost(dd.p, dops.as<GhostOp>() + ghost_b.ptr[b], ghost_b.ptr[b + 1] - ghost_b.ptr[b], slot, precision,
                      eng.stream);
     eng.sync();
 }

@@ -208,11 +208,11 @@ void launch_fp64_peak(double *out, int blocks, int threads, int iters, cudaStrea
 void launch_fp64_latency(long long *cyc, double *val, int iters, cudaStream_t s);
 
 // AMR op batches (amr.hpp, amr64.cu)
-struct GhostOpDev;
+struct GhostOp;
 struct IfaceOp;
 struct CSyncOp;
 // `prec` selects the patch storage type (kF64 or kF32) of the descriptor array.
-void launch_ghost(const void *patches, const GhostOpDev *ops, int n, int slot, int prec, cudaStream_t s);
+void launch_ghost(const void *patches, const GhostOp *ops, int n, int slot, int prec, cudaStream_t s);
 void launch_iface(const void *patches, const IfaceOp *ops, int n, int step, int prec, cudaStream_t s);
 // Launch-set op tables gathered on the device: segment s copies count ops from src to
 // dst + dst_off and adds base to their patch ids (the run's first patch in the set).
@@ -221,7 +221,7 @@ struct OpSegment {
     long long dst_off;
     int count, base;
 };
-void merge_ghost_ops(const OpSegment *segs, int nseg, GhostOpDev *dst, cudaStream_t s);
+void merge_ghost_ops(const OpSegment *segs, int nseg, GhostOp *dst, cudaStream_t s);
 void merge_iface_ops(const OpSegment *segs, int nseg, IfaceOp *dst, cudaStream_t s);
 void merge_csync_ops(const OpSegment *segs, int nseg, CSyncOp *dst, cudaStream_t s);
 void launch_csync(const void *patches, const CSyncOp *ops, int n, int prec, cudaStream_t s);
