@@ -1,6 +1,7 @@
 """The three-level wakefield case (base 16384 x 1024, 36 M cells) builds and steps: its
 finest patch is 45888 cells wide (more than any 16-bit index holds), and its 65536
-finest cells take the scan Poisson solve to 64 unknowns per thread segment group."""
+finest cells take the scan Poisson solve to its largest blocks (512 threads per CTA,
+16 unknowns per thread)."""
 import dataclasses
 import sys
 from pathlib import Path
