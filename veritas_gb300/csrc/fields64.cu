@@ -62,25 +62,29 @@ __device__ __forceinline__ double cell_asq(const RunFields &F, int x) {
 //   L(j) = c2 * ln((g_{j+1} + c1 p_{j+1}) / (g_j + c1 p_j))
 // (the reference's gm; gm1 and gp1 are L(j-1) and L(j+1), the same expressions), the
 // interpolated f and the cell's charge/current contributions.  The window's 29
-// contributions per sub-column then go through shared memory to warp 0, whose lanes each
-// add one sub-column's in ascending j, which keeps the reference's accumulation order
-// (Rectangle.cpp:207-255) exactly.  The serial sums thus take one FP64 warp instruction
-// per cell for up to 32 sub-columns at once (an FP64 warp instruction occupies the
-// sub-partition's FP64 unit for tens of cycles whatever the number of active lanes).
+// contributions per sub-column then go through shared memory to the block's last warp,
+// whose lanes each add one sub-column's in ascending j, which keeps the reference's
+// accumulation order (Rectangle.cpp:207-255) exactly.  The serial sums thus take one
+// FP64 warp instruction per cell for up to 30 sub-columns at once (an FP64 warp
+// instruction occupies the sub-partition's FP64 unit for tens of cycles whatever the
+// number of active lanes), and with two window buffers they run while the column warps
+// form the next window.
 // The coarse-column list is padded per patch to a multiple of kMomCols (padding: patch
 // -1), so the warps of a block share n_p and rtb and step through the windows together.
 constexpr int kMomOut = 29;  // outputs per window: j0 .. j0+28
 
-__global__ void __launch_bounds__(kMomCols * 32) k64_moments(MomLaunch M) {
+__global__ void __launch_bounds__((kMomCols + 1) * 32) k64_moments(MomLaunch M) {
     VX_PDL_WAIT();
-    __shared__ double s_cc[kMomCols][2][32], s_cj[kMomCols][2][32];
-    __shared__ unsigned s_use[kMomCols];
+    // two window buffers: the column warps fill one while the summing warp adds the other
+    __shared__ double s_cc[2][kMomCols][2][32], s_cj[2][kMomCols][2][32];
+    __shared__ unsigned s_use[2][kMomCols];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool summer = wid == kMomCols;  // the last warp adds; warps 0..kMomCols-1 form columns
     const int col0 = blockIdx.x * kMomCols;
-    const bool real = M.colpatch[col0 + wid] >= 0;  // warp-uniform
+    const bool real = !summer && M.colpatch[col0 + wid] >= 0;  // warp-uniform
     const P64 &P = ((const P64 *)M.patches)[M.colpatch[col0]];  // the block's patch
     const int np = P.np, rtb = P.rtb, pit = P.pitch;
-    const int i = M.colidx[col0 + wid] / rtb;
+    const int i = summer ? 0 : M.colidx[col0 + wid] / rtb;
     const RunFields &F = M.fields[P.run];
     const double minv = 1 / P.mass;
     const double c1 = minv * kCInv;
@@ -93,72 +97,83 @@ __global__ void __launch_bounds__(kMomCols * 32) k64_moments(MomLaunch M) {
         double a[2] = {0.0, 0.0};
         for (int q = 0; q < kg; q++)
             if (real) a[q] = P.qq * cell_asq(F, (i + P.x_pos) * rtb + k0 + q);
-        double ch = 0.0, cu = 0.0;  // warp 0, lane t < kMomCols * kg: sub-column t % kg of column t / kg
-        for (int j0 = 0; j0 < np; j0 += kMomOut) {
-            const int j = j0 - 1 + lane;  // this lane's p index
-            double p = 0.0, f3 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0, cor = 0.0;
-            bool use = false;
-            if (real) {
-                p = P.pmin + P.dp * (double)(j + P.p_pos);
-                if (j <= np) {
-                    if (rtb == 1) f3 = f[pidx(i, j, pit)];
-                    else rel_shared(P, f, i, j, f3, a1, a2, a3, cor);
-                }
-                use = lane >= 1 && lane <= kMomOut && j < np && !(P.nested && P.nested[pidx(i, j, pit)]);
-            }
-            for (int q = 0; q < kg; q++) {
-                double cc = 0.0, cj = 0.0;
-                if (real) {
-                    double G = 0.0, V = 0.0;
-                    if (j <= np + 1) {
-                        double g = sqrt(1.0 + ((p * p) + a[q]) * P.g2);
-                        G = g + c1 * p;
-                    }
-                    if (j <= np) V = rtb == 1 ? f3 : rel_pick(P, k0 + q, a1, a2, a3, f3) + cor;
-                    const double Gn = __shfl_down_sync(full, G, 1);
-                    const double L = c2 * log(Gn / G);  // valid for lanes 0..30
-                    const double Lm = __shfl_up_sync(full, L, 1);
-                    const double Lp = __shfl_down_sync(full, L, 1);
-                    const double Vm = __shfl_up_sync(full, V, 1);
-                    const double Vp = __shfl_down_sync(full, V, 1);
-                    if (use) {
-                        cc = V;
-                        cj = V * L + c3 * (Lp - Lm) * (Vp - Vm);
-                    }
-                }
-                s_cc[wid][q][lane] = cc;
-                s_cj[wid][q][lane] = cj;
-            }
-            const unsigned usemask = __ballot_sync(full, use);
-            if (lane == 0) s_use[wid] = usemask;
-            __syncthreads();
-            if (wid == 0 && lane < kMomCols * kg) {
+        // summing warp, lane t < kMomCols * kg: sub-column t % kg of column t / kg
+        double ch = 0.0, cu = 0.0;
+        auto add_window = [&](int bf) {
+            if (lane < kMomCols * kg) {
                 const int w = lane / kg, q = lane - w * kg;
-                const unsigned um = s_use[w];
+                const unsigned um = s_use[bf][w];
                 for (int t = 1; t <= kMomOut; t++)
                     if ((um >> t) & 1u) {
-                        ch += s_cc[w][q][t];
-                        cu += s_cj[w][q][t];
+                        ch += s_cc[bf][w][q][t];
+                        cu += s_cj[bf][w][q][t];
                     }
+            }
+        };
+        int bf = 0;
+        for (int j0 = 0; j0 < np; j0 += kMomOut, bf ^= 1) {
+            if (!summer) {
+                const int j = j0 - 1 + lane;  // this lane's p index
+                double p = 0.0, f3 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0, cor = 0.0;
+                bool use = false;
+                if (real) {
+                    p = P.pmin + P.dp * (double)(j + P.p_pos);
+                    if (j <= np) {
+                        if (rtb == 1) f3 = f[pidx(i, j, pit)];
+                        else rel_shared(P, f, i, j, f3, a1, a2, a3, cor);
+                    }
+                    use = lane >= 1 && lane <= kMomOut && j < np && !(P.nested && P.nested[pidx(i, j, pit)]);
+                }
+                for (int q = 0; q < kg; q++) {
+                    double cc = 0.0, cj = 0.0;
+                    if (real) {
+                        double G = 0.0, V = 0.0;
+                        if (j <= np + 1) {
+                            double g = sqrt(1.0 + ((p * p) + a[q]) * P.g2);
+                            G = g + c1 * p;
+                        }
+                        if (j <= np) V = rtb == 1 ? f3 : rel_pick(P, k0 + q, a1, a2, a3, f3) + cor;
+                        const double Gn = __shfl_down_sync(full, G, 1);
+                        const double L = c2 * log(Gn / G);  // valid for lanes 0..30
+                        const double Lm = __shfl_up_sync(full, L, 1);
+                        const double Lp = __shfl_down_sync(full, L, 1);
+                        const double Vm = __shfl_up_sync(full, V, 1);
+                        const double Vp = __shfl_down_sync(full, V, 1);
+                        if (use) {
+                            cc = V;
+                            cj = V * L + c3 * (Lp - Lm) * (Vp - Vm);
+                        }
+                    }
+                    s_cc[bf][wid][q][lane] = cc;
+                    s_cj[bf][wid][q][lane] = cj;
+                }
+                const unsigned usemask = __ballot_sync(full, use);
+                if (lane == 0) s_use[bf][wid] = usemask;
+            } else if (j0 > 0) {
+                add_window(bf ^ 1);  // the previous window, in ascending j
             }
             __syncthreads();
         }
-        if (wid == 0 && lane < kMomCols * kg) {
-            const int w = lane / kg, q = lane - w * kg;
-            if (M.colpatch[col0 + w] >= 0) {
-                const int cl = M.colidx[col0 + w] + k0 + q;  // i_w * rtb + k
-                const double qc = P.q;
-                P.chargeR[cl] = ch * (P.dp * qc);
-                P.currentR[cl] = cu * (-qc * qc / P.mass);
+        if (summer) {
+            add_window(bf ^ 1);  // the last window
+            if (lane < kMomCols * kg) {
+                const int w = lane / kg, q = lane - w * kg;
+                if (M.colpatch[col0 + w] >= 0) {
+                    const int cl = M.colidx[col0 + w] + k0 + q;  // i_w * rtb + k
+                    const double qc = P.q;
+                    P.chargeR[cl] = ch * (P.dp * qc);
+                    P.currentR[cl] = cu * (-qc * qc / P.mass);
+                }
             }
         }
+        __syncthreads();  // the next pair's first window reuses the buffers
     }
 }
 
 void launch_moments64(const MomLaunch &M) {
     if (M.ncols == 0) return;
     // M.ncols is a multiple of kMomCols (the list is padded per patch)
-    vx_launch(k64_moments, M.ncols / kMomCols, kMomCols * 32, 0, M.stream, M);
+    vx_launch(k64_moments, M.ncols / kMomCols, (kMomCols + 1) * 32, 0, M.stream, M);
 }
 
 // ---------------------------------------------------------------- separable initial f

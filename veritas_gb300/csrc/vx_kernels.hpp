@@ -94,7 +94,7 @@ struct MomLaunch {
     int asq32 = 1;        // FP32: the moments kernel also makes the FP32 copy of a^2
     cudaStream_t stream;
 };
-constexpr int kMomCols = 16;  // FP64 moment columns per block (padded per patch)
+constexpr int kMomCols = 15;  // FP64 moment columns per block (padded per patch), plus a summing warp
 void launch_moments64(const MomLaunch &M);
 void launch_moments32(const MomLaunch &M);
 
