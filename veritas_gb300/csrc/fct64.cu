@@ -76,6 +76,19 @@ __device__ __forceinline__ void weno_face_both(double f1, double f2, double f3, 
 
 __device__ __forceinline__ double vmax(double a, double b) { return (a > b) ? a : b; }
 __device__ __forceinline__ double vmin(double a, double b) { return (a < b) ? a : b; }
+// vmax(0.0, x) and vmin(0.0, x) decided on the bit pattern with integer instructions (the
+// FP64 unit is the limiter's bottleneck): x < 0 exactly when the sign bit is set and x is
+// neither -0 nor NaN; x > 0 when the sign bit is clear and x is neither +0 nor NaN.
+__device__ __forceinline__ double vmax0(double x) {
+    const long long b = __double_as_longlong(x);
+    const long long m = b & 0x7FFFFFFFFFFFFFFFLL;
+    return (b < 0 && m != 0 && m <= 0x7FF0000000000000LL) ? 0.0 : x;
+}
+__device__ __forceinline__ double vmin0(double x) {
+    const long long b = __double_as_longlong(x);
+    return (b > 0 && b <= 0x7FF0000000000000LL) ? 0.0 : x;
+}
+
 
 // Rectangle::GetEfield (Rectangle.cpp:1055-1067): mean of the finest-grid E_x over the
 // rtb finest cells under coarse cell i; finest indices are periodic (EMSolver.cpp:137-154).
@@ -220,8 +233,8 @@ __global__ void k64_limR(const P64 *patches, const TileRef *tiles) {
     if (i < -1 || i > P.nx || j < -1 || j > P.np) return;
     const double *DX = P.FxDS, *DP = P.FpDS, *f0 = P.f0, *f2 = P.f2;
     double dxi = DX[id], dxn = DX[id + pit], dpi = DP[id], dpn = DP[id + 1];
-    double Pp = vmax(0.0, dxi) - vmin(0.0, dxn) + vmax(0.0, dpi) - vmin(0.0, dpn);
-    double Pm = vmax(0.0, dxn) - vmin(0.0, dxi) + vmax(0.0, dpn) - vmin(0.0, dpi);
+    double Pp = vmax0(dxi) - vmin0(dxn) + vmax0(dpi) - vmin0(dpn);
+    double Pm = vmax0(dxn) - vmin0(dxi) + vmax0(dpn) - vmin0(dpi);
     double c0 = f0[id], c2 = f2[id];
     double w1ma = vmax(c0, c2);
     double w2ma = vmax(f0[id + pit], f2[id + pit]);
