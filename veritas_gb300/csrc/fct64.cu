@@ -88,6 +88,11 @@ __device__ __forceinline__ double vmin0(double x) {
     const long long b = __double_as_longlong(x);
     return (b > 0 && b <= 0x7FF0000000000000LL) ? 0.0 : x;
 }
+// x > 0.0 (false for zeros and NaN) on the bit pattern
+__device__ __forceinline__ bool gt0(double x) {
+    const long long b = __double_as_longlong(x);
+    return b > 0 && b <= 0x7FF0000000000000LL;
+}
 
 
 // Rectangle::GetEfield (Rectangle.cpp:1055-1067): mean of the finest-grid E_x over the
@@ -141,14 +146,14 @@ __global__ void k64_faces(const P64 *patches, const TileRef *tiles, const RunFie
     if ((part & 1) && i >= 0 && i <= P.nx && j >= -1 && j <= P.np) {
         double am = P.dp_inv * P.cc * (g[pidx(i, j + 1, pit)] - g[id]);
         P.ex[id] = am;
-        P.fx[id] = weno_face(f[pidx(i - 2, j, pit)], f[pidx(i - 1, j, pit)], f[id], f[pidx(i + 1, j, pit)], am > 0.0);
+        P.fx[id] = weno_face(f[pidx(i - 2, j, pit)], f[pidx(i - 1, j, pit)], f[id], f[pidx(i + 1, j, pit)], gt0(am));
     }
     if ((part & 2) && i >= -1 && i <= P.nx && j >= 0 && j <= P.np) {
         const RunFields &F = fields[P.run];
         double Em = P.q * patch_efield(P, F, i);
         double am = Em - P.cc * P.dx_inv * (g[pidx(i + 1, j, pit)] - g[id]);
         P.ep[id] = am;
-        P.fp[id] = weno_face(f[pidx(i, j - 2, pit)], f[pidx(i, j - 1, pit)], f[id], f[pidx(i, j + 1, pit)], am > 0.0);
+        P.fp[id] = weno_face(f[pidx(i, j - 2, pit)], f[pidx(i, j - 1, pit)], f[id], f[pidx(i, j + 1, pit)], gt0(am));
     }
     // The p faces in two halves, so that the E_x-independent one runs beside the Poisson
     // solve: part 4 forms both upwind candidates (fp and, as scratch, Rp, which the
@@ -165,7 +170,7 @@ __global__ void k64_faces(const P64 *patches, const TileRef *tiles, const RunFie
         double Em = P.q * patch_efield(P, F, i);
         double am = Em - P.cc * P.dx_inv * (g[pidx(i + 1, j, pit)] - g[id]);
         P.ep[id] = am;
-        if (!(am > 0.0)) P.fp[id] = P.Rp[id];
+        if (!gt0(am)) P.fp[id] = P.Rp[id];
     }
 }
 
@@ -181,13 +186,13 @@ __global__ void k64_flux(const P64 *patches, const TileRef *tiles, int step, int
         double am = P.ex[id], ap1 = P.ex[id + 1], am1 = P.ex[id - 1];
         double fm = P.fx[id], fp1 = P.fx[id + 1], fm1 = P.fx[id - 1];
         P.FxH[step][id] = P.dx_inv * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
-        if (step == 0) P.FxL[id] = P.dx_inv * ((am > 0.0 ? f[id - pit] : f[id]) * am);
+        if (step == 0) P.FxL[id] = P.dx_inv * ((gt0(am) ? f[id - pit] : f[id]) * am);
     }
     if ((part & 2) && i >= -1 && i <= P.nx && j >= 0 && j <= P.np && !(P.ifp && P.ifp[id])) {
         double am = P.ep[id], ap1 = P.ep[id + pit], am1 = P.ep[id - pit];
         double fm = P.fp[id], fp1 = P.fp[id + pit], fm1 = P.fp[id - pit];
         P.FpH[step][id] = P.dp_inv * (fm * am + w3 * (fp1 - fm1) * (ap1 - am1));
-        if (step == 0) P.FpL[id] = P.dp_inv * ((am > 0.0 ? f[id - 1] : f[id]) * am);
+        if (step == 0) P.FpL[id] = P.dp_inv * ((gt0(am) ? f[id - 1] : f[id]) * am);
     }
 }
 
@@ -255,8 +260,8 @@ __global__ void k64_limR(const P64 *patches, const TileRef *tiles) {
     // among them, takes the division as written.  Most cells of a smooth solution take
     // the first branch and skip the division (about ten FP64 instructions).
     constexpr double kMaxFinite = 1.7976931348623157e308;
-    P.Rp[id] = Pp > 0.0 ? ((Qp >= Pp && Pp <= kMaxFinite) ? 1.0 : vmin(1.0, Qp / Pp)) : 0.0;
-    P.Rm[id] = Pm > 0.0 ? ((Qm >= Pm && Pm <= kMaxFinite) ? 1.0 : vmin(1.0, Qm / Pm)) : 0.0;
+    P.Rp[id] = gt0(Pp) ? ((Qp >= Pp && Pp <= kMaxFinite) ? 1.0 : vmin(1.0, Qp / Pp)) : 0.0;
+    P.Rm[id] = gt0(Pm) ? ((Qm >= Pm && Pm <= kMaxFinite) ? 1.0 : vmin(1.0, Qm / Pm)) : 0.0;
 }
 
 // Limiter coefficients on interior faces, 1 elsewhere (Rectangle.cpp:1581-1594).
@@ -267,8 +272,8 @@ __global__ void k64_limC(const P64 *patches, const TileRef *tiles) {
     double cx = 1.0, cp = 1.0;
     if (i >= 1 && i < P.nx && j >= 0 && j < P.np) {
         const double *Rp = P.Rp, *Rm = P.Rm;
-        cx = P.FxDS[id] > 0.0 ? vmin(Rp[id], Rm[id - pit]) : vmin(Rp[id - pit], Rm[id]);
-        cp = P.FpDS[id] > 0.0 ? vmin(Rp[id], Rm[id - 1]) : vmin(Rp[id - 1], Rm[id]);
+        cx = gt0(P.FxDS[id]) ? vmin(Rp[id], Rm[id - pit]) : vmin(Rp[id - pit], Rm[id]);
+        cp = gt0(P.FpDS[id]) ? vmin(Rp[id], Rm[id - 1]) : vmin(Rp[id - 1], Rm[id]);
     }
     P.Cx[id] = cx;
     P.Cp[id] = cp;
