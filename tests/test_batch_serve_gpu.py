@@ -31,7 +31,7 @@ def _bytes(s, path):
 def test_batched_equals_separate(ctx, tmp_path, precision):
     from veritas_gb300 import SolverManager, advance_many, calculate_dt_many
 
-    names = ["slab64", "amr2", "drift128", "beam2"]
+    names = ["slab64", "amr2", "drift128", "beam2", "ragged2", "ions2"]
     probs = [dataclasses.replace(problem_for(n), precision=precision) for n in names]
     alone = [SolverManager(ctx, p) for p in probs]
     mixed = [SolverManager(ctx, p) for p in probs]
