@@ -577,17 +577,18 @@ __device__ void pois_bwd_fast(PoisBandChunk &B, int r0, int cnt, double *x, doub
 
 constexpr int kPoisSmemMaxN = 16384;  // solution vector kept in shared memory up to this n
 
-__global__ void __launch_bounds__(1024, 1) k_poisson(PoissonLaunch L) {
-    VX_PDL_WAIT();
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+// The solve with the solution vector x in shared memory (XS) or in phi itself.  The two
+// instantiations let the compiler see x's address space: with one pointer chosen at run
+// time its loads and stores in the sweeps go through generic addressing.
+template <bool XS>
+__device__ __forceinline__ void poisson_solve(const PoissonLaunch &L, unsigned char *smem_raw, double *x) {
     PoisBandChunk *buf = (PoisBandChunk *)smem_raw;  // two chunk buffers, then the solution vector
     __shared__ int s_bad;
     const int run = blockIdx.x;
     RunFields &F = L.fields[run];
     const LUDev &lu = L.lu[run];
     const int n = F.n;
-    const bool in_smem = L.x_in_smem;
-    double *x = in_smem ? (double *)(smem_raw + 2 * sizeof(PoisBandChunk)) : F.phi;
+    constexpr bool in_smem = XS;
     double *tmp = F.efin;  // scratch until E_x is recomputed at the end
     const double te = kEps0Inv;
     const double w = L.w[run];
@@ -703,6 +704,13 @@ __global__ void __launch_bounds__(1024, 1) k_poisson(PoissonLaunch L) {
     __syncthreads();
     const double ex0 = *F.ex0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) F.efin[i] = efield_at(x, n, L.fcoef[run], ex0, i);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_poisson(PoissonLaunch L) {
+    VX_PDL_WAIT();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    if (L.x_in_smem) poisson_solve<true>(L, smem_raw, (double *)(smem_raw + 2 * sizeof(PoisBandChunk)));
+    else poisson_solve<false>(L, smem_raw, L.fields[blockIdx.x].phi);
 }
 
 void launch_poisson(const PoissonLaunch &L) {
