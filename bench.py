@@ -54,35 +54,40 @@ KERNEL_NAMES = {"gamma": "k64_gamma", "faces": "k64_faces", "flux": "k64_flux", 
 
 
 def problem_config1():
-    from veritas_gb300 import Problem
+    from veritas_gb300.workloads import laser_slab_2048x256
 
-    return Problem(L=100.0, nx=2048, np=256, Lfinest=1, pmax=2.0, dens=0.01, x1=15, x2=20, x3=80, x4=85, Te=1.0,
-                   a0=1.0, fwhm=10.0, delay=10.0, cfl=0.5, quadDepth=2, precision=64)
+    return laser_slab_2048x256()
 
 
 def problem_config3():
     """Larger wakefield case: base 16384 x 1024, three levels, 0.005 n_c, a0 = 2, 0.5 keV."""
-    p = problem_config1()
-    p.nx, p.np, p.Lfinest, p.r = 16384, 1024, 3, 2
-    p.dens, p.a0, p.Te = 0.005, 2.0, 0.5
-    p.crit, p.sizeWeight = 1e-6, 1.0
-    return p
+    from veritas_gb300.workloads import laser_wakefield_amr_16384x1024
+
+    return laser_wakefield_amr_16384x1024()
 
 
 def run_config3(args) -> None:
+    """--form config3: the larger three-level case alone, as one JSON line."""
+    from veritas_gb300 import Context
+
+    ctx = Context(0)
+    print(json.dumps(measure_config3(ctx, args.steps)))
+    ctx.close()
+
+
+def measure_config3(ctx, steps: int) -> dict:
     """The precision form on the larger case: FP32 throughput, and the error of f, E_x,
     E_y and the field energy against the FP64 path over the same steps from the same
-    initial hierarchy.  One JSON line."""
+    initial hierarchy."""
     import dataclasses
 
     import numpy as np
 
-    from veritas_gb300 import Context, SolverManager
+    from veritas_gb300 import SolverManager
 
     sys.path.insert(0, str(ROOT / "tests"))
     import vxstate
 
-    ctx = Context(0)
     t0 = time.perf_counter()
     s32 = SolverManager(ctx, dataclasses.replace(problem_config3(), precision=32))
     init32 = time.perf_counter() - t0
@@ -98,7 +103,7 @@ def run_config3(args) -> None:
         e0 = p.a0 * 9.10938291e-31 * 299792458.0 * (2 * np.pi * 299792458.0 / p.lambda_) / 1.60217657e-19
         ew = ee = ey = 0.0
         t64 = t32 = 0.0
-        for _ in range(args.steps):
+        for _ in range(steps):
             dt = s64.CalculateDt()
             ctx.timer_begin()
             s64.Advance(dt)
@@ -120,25 +125,23 @@ def run_config3(args) -> None:
             num = max(num, float(np.max(np.abs(fb - fa))))
             den = max(den, float(np.max(np.abs(fa))))
     line = {"form": "precision", "workload": "laser_wakefield_amr_Nx16384_Np1024_3level_r2",
-            "cells_per_step": cells, "patches": len(layout), "steps": args.steps,
-            "fp32": {"value": cells * args.steps / (t32 * 1e-3), "unit": UNIT, "ms_per_step": t32 / args.steps},
-            "fp64": {"value": cells * args.steps / (t64 * 1e-3), "unit": UNIT, "ms_per_step": t64 / args.steps},
+            "cells_per_step": cells, "patches": len(layout), "steps": steps,
+            "fp32": {"value": cells * steps / (t32 * 1e-3), "unit": UNIT, "ms_per_step": t32 / steps},
+            "fp64": {"value": cells * steps / (t64 * 1e-3), "unit": UNIT, "ms_per_step": t64 / steps},
             "init_s": {"fp32": init32, "fp64": init64},
             "error_vs_fp64": {"from": "the FP64 run's initial hierarchy (t = 0), same dt sequence",
                               "f_rel_linf": num / den, "field_energy_rel_max": ew,
                               "Ex_abs_max_over_laser_E0": ee, "Ey_abs_max_over_laser_E0": ey}}
-    print(json.dumps(line))
     s32.close()
     s64.close()
-    ctx.close()
+    return line
 
 
 def problem_config2():
     """Two-level AMR laser / slab case: base 4096 x 512, refinement ratio 2."""
-    p = problem_config1()
-    p.nx, p.np, p.Lfinest, p.r = 4096, 512, 2, 2
-    p.crit, p.sizeWeight = 1e-6, 1.0
-    return p
+    from veritas_gb300.workloads import laser_slab_amr_4096x512
+
+    return laser_slab_amr_4096x512()
 
 
 class ClockSampler:
@@ -570,7 +573,8 @@ def main() -> None:
                                                    "f64 (O(n) scan Poisson instead of the LU's rounding order)"),
                  "batched_fp32": measure_batched(ctx, 64, 5, 3, 32),
                  "served_fp32": measure_serving(ctx, 24, 16, 32),
-                 "served_fp64": measure_serving(ctx, 24, 16, 64)}
+                 "served_fp64": measure_serving(ctx, 24, 16, 64),
+                 "precision_wakefield_16384x1024": measure_config3(ctx, args.steps)}
         forms["fp32_speedup_vs_fp64"] = forms["fp32"]["value"] / value
         forms["fp64_scan_poisson_speedup_vs_fp64"] = forms["fp64_scan_poisson"]["value"] / value
         forms["batched_fp32_speedup_vs_fp64"] = forms["batched_fp32"]["value"] / value
@@ -584,6 +588,9 @@ def main() -> None:
                              "warm-up steps, from the same initial hierarchy"}
         else:
             cpu = {"value": None, "unavailable": rec["unavailable"]}
+    parity = None
+    if rank == 0 and not args.no_cpu_baseline:
+        parity = parity_vs_port(ctx, init_path, 2)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -592,7 +599,7 @@ def main() -> None:
                            "l2": "flushed before every timed step",
                            "parallelism": f"replicas{world}"},
                 "clocks": clk.summary(), "gpu_launches": launches, "e2e": e2e, "roofline": roofline,
-                "cpu_baseline": cpu, "forms": forms}
+                "cpu_baseline": cpu, "parity_vs_port": parity, "forms": forms}
         print(json.dumps(line))
     hin.close()
     hout.close()
@@ -602,6 +609,21 @@ def main() -> None:
         init_path.unlink()
     if dist:
         dist.destroy_process_group()
+
+
+def parity_vs_port(ctx, init_path: Path, steps: int) -> dict:
+    """The headline workload's parity: the GPU path and the oracle port (pinned bit-exact
+    to the reference build) advanced `steps` RK steps from the same initial hierarchy with
+    the same dt, compared array by array (relative L-inf; the bar is 1e-10)."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from helpers import gpu_vs_port
+
+    with tempfile.TemporaryDirectory() as td:
+        err = gpu_vs_port(ctx, problem_config2(), steps, Path(td), init_state=init_path)
+    return {"steps": steps, "from": "the workload's initial hierarchy (t = 0), same dt sequence",
+            "tolerance": 1e-10, "f_rel_linf": err["f"],
+            "fields_rel_linf": max(v for k, v in err.items() if k not in ("f", "time")),
+            "per_array": err}
 
 
 def _read_traffic(kernel: str):

@@ -229,8 +229,10 @@ int vx_run_step_host(vx_run *run, const double *state_in, double *state_out, dou
  * caller owns — Ay, Az, By, Bz (their first n entries, slot 0) and E_x (n) — with the
  * species' charge q, mass m and finest-level dp0 given on the host.  Its scratch is a
  * fixed device array of VX_CFL_NOALLOC_MAX_CELLS / 256 doubles, looked up on the first
- * call on each device (make that first call before any stream capture); larger n is
- * rejected with VX_ERR_INVALID.  Calls that overlap on the GPU share the scratch and race.
+ * call on each device (make that first call before any stream capture, and do not use the
+ * entry point on a device after cudaDeviceReset); larger n is rejected with
+ * VX_ERR_INVALID, as are non-positive or non-finite dp0 and m.  Calls that overlap on the
+ * GPU share the scratch and race.
  * `stream` is a cudaStream_t (NULL: the default stream); the call waits for its result. */
 #define VX_CFL_NOALLOC_MAX_CELLS (1 << 20)
 int vx_cfl_bound_noalloc(const double *Ay, const double *Az, const double *By, const double *Bz, const double *Ex,

@@ -8,10 +8,14 @@
 # mkl_shim.cpp (the four MKL routines, see shim/mkl.h).  USINGMKL/MKL_ILP64 select the
 # reference's default configuration (CMakeLists.txt:9,26).  -ffp-contract=off keeps
 # IEEE double arithmetic identical on x86-64 and aarch64.
-# Usage: build_ref.sh [reference_dir]   (default: the mounted reference tree)
+# Usage: build_ref.sh [reference_dir]   (default: $VERITAS_REFERENCE_DIR)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${VERITAS_REFERENCE_DIR:-}}"
+if [ -z "$REF" ]; then
+  echo "no reference tree given (argument or VERITAS_REFERENCE_DIR)" >&2
+  exit 3
+fi
 OUT="$HERE/../_ref"
 if [ ! -f "$REF/Rectangle.cpp" ]; then
   echo "reference sources not found at $REF" >&2

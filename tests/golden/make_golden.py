@@ -116,9 +116,12 @@ def run_regrid(exe: Path, name: str, args: list[str], every: int) -> None:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("VERITAS_REFERENCE_DIR"),
+                    help="the reference's source tree (default: $VERITAS_REFERENCE_DIR)")
     ap.add_argument("--only", action="append", default=[], help="regenerate only these cases")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give --ref or set VERITAS_REFERENCE_DIR to the reference's source tree")
     subprocess.run(["bash", str(REPO / "oracle" / "ref" / "build_ref.sh"), a.ref], check=True)
     exe = REPO / "oracle" / "_ref" / "veritas_ref"
     for name, (args, steps, keep) in CASES.items():

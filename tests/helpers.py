@@ -72,3 +72,52 @@ def total_mass(st: dict) -> float:
             for r in rects:
                 m += float(np.sum(r["f"][2:-2, 2:-2, 0]))
     return m
+
+
+ROOT = GOLDEN.parent.parent
+PORT = ROOT / "oracle" / "_port" / "veritas_port"
+
+
+def port_exe() -> Path:
+    """The oracle port (built by build(); built here if missing)."""
+    import subprocess
+
+    if not PORT.exists():
+        subprocess.run(["bash", str(ROOT / "oracle" / "port" / "build_port.sh")], check=True, capture_output=True)
+    return PORT
+
+
+def gpu_vs_port(ctx, problem, steps: int, workdir: Path, init_state: Path | None = None,
+                threads: int | None = None) -> dict:
+    """The GPU path and the oracle port advanced `steps` RK steps from the same state with
+    the GPU path's dt sequence; returns compare_states' relative L-inf errors (f slots 0
+    and 1, every field array, Ex0, time).  The start is `init_state`, or the GPU path's
+    own initial hierarchy when None."""
+    import os
+    import subprocess
+
+    from veritas_gb300 import SolverManager
+
+    workdir = Path(workdir)
+    s = SolverManager(ctx, problem)
+    if init_state is None:
+        init_state = workdir / "init.bin"
+        s.save_state(init_state)
+    else:
+        s.load_state(init_state)
+    dts = []
+    for _ in range(steps):
+        dt = s.CalculateDt()
+        dts.append(dt)
+        s.Advance(dt)
+    s.save_state(workdir / "gpu.bin")
+    s.close()
+    env = dict(os.environ)
+    if threads:
+        env["OMP_NUM_THREADS"] = str(threads)
+    subprocess.run([str(port_exe()), *problem.harness_args(), f"load={init_state}",
+                    "dts=" + ",".join(repr(d) for d in dts), f"steps={steps}", f"dump_every={steps}",
+                    f"dumpdir={workdir}"], check=True, capture_output=True, env=env)
+    ref = vxstate.read_state(workdir / f"state_{steps:05d}.bin")
+    got = vxstate.read_state(workdir / "gpu.bin")
+    return compare_states(got, ref, 0.0)

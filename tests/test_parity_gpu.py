@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import vxstate
-from helpers import compare_states, golden, golden_named, problem_for, total_mass
+from helpers import compare_states, golden, golden_named, gpu_vs_port, problem_for, total_mass
 
 TOL = 1e-10
 ONE_STEP = [("slab64", 0), ("slab64", 1), ("drift128", 0), ("edge64", 0),
@@ -185,3 +185,17 @@ def test_gpu_matches_port_at_512x128(tmp_path):
         assert v <= TOL, (k, v)
     s.close()
     c.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("workload", ["laser_slab_2048x256", "laser_slab_amr_4096x512"])
+def test_gpu_matches_port_at_benchmark_size(ctx, tmp_path, workload):
+    """The benchmarked workloads at full size (one level 2048 x 256; two levels on a
+    4096 x 512 base): the GPU path and the oracle port from the GPU path's initial
+    hierarchy, two RK steps with the same dt, every array within 1e-10."""
+    from veritas_gb300.workloads import WORKLOADS
+
+    err = gpu_vs_port(ctx, WORKLOADS[workload](), 2, tmp_path)
+    print(workload, "vs port", {k: f"{v:.2e}" for k, v in err.items()})
+    for k, v in err.items():
+        assert v <= TOL, (k, v)

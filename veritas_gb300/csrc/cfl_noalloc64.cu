@@ -90,7 +90,10 @@ __global__ void k_cfl_fold(double *partial, int blocks) {
 }
 
 // Device address of the scratch array, looked up once per device with that device
-// current (host code only sees a stand-in for the symbol, not a device address).
+// current (host code only sees a stand-in for the symbol, not a device address).  The
+// address is kept for the life of the process: after cudaDeviceReset the module is
+// loaded again and the array may move, so the entry point must not be used on a device
+// that has been reset.
 double *scratch_on_current_device(int *err) {
     static std::mutex mu;
     static double *addr[64] = {};
@@ -124,10 +127,24 @@ extern "C" int vx_cfl_bound_noalloc(const double *Ay, const double *Az, const do
         set_last_error("vx_cfl_bound_noalloc: bad argument");
         return VX_ERR_INVALID;
     }
+    for (int i = 0; i < nspecies; i++) {
+        if (!(std::isfinite(dp0[i]) && dp0[i] > 0) || !(std::isfinite(m[i]) && m[i] > 0) || !std::isfinite(q[i])) {
+            set_last_error("vx_cfl_bound_noalloc: species " + std::to_string(i) +
+                           " needs a finite positive dp0 and mass and a finite charge");
+            return VX_ERR_INVALID;
+        }
+    }
     if (n > VX_CFL_NOALLOC_MAX_CELLS) {
         set_last_error("vx_cfl_bound_noalloc: n = " + std::to_string(n) + " exceeds the limit of " +
                        std::to_string(VX_CFL_NOALLOC_MAX_CELLS) + " finest cells (its scratch is a fixed array)");
         return VX_ERR_INVALID;
+    }
+    // an error the caller left pending is reported as such, not blamed on this call
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_last_error(std::string("vx_cfl_bound_noalloc: a CUDA error was pending before the call: ") +
+                       cudaGetErrorString(e));
+        return VX_ERR_CUDA;
     }
     int err = 0;
     double *partial = scratch_on_current_device(&err);
@@ -151,11 +168,18 @@ extern "C" int vx_cfl_bound_noalloc(const double *Ay, const double *Az, const do
     cudaStream_t st = (cudaStream_t)stream;
     const int blocks = (n + kCflThreads - 1) / kCflThreads;
     k_cfl_partial<<<blocks, kCflThreads, 0, st>>>(Ay, Az, By, Bz, Ex, n, S, partial);
-    k_cfl_fold<<<1, kCflThreads, 0, st>>>(partial, blocks);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        k_cfl_fold<<<1, kCflThreads, 0, st>>>(partial, blocks);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        set_last_error(std::string("vx_cfl_bound_noalloc: launch failed: ") + cudaGetErrorString(e));
+        return VX_ERR_CUDA;
+    }
     double pc = 0.0;
-    cudaError_t e = cudaMemcpyAsync(&pc, partial, sizeof(double), cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(&pc, partial, sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_last_error(std::string("vx_cfl_bound_noalloc: ") + cudaGetErrorString(e));
         return VX_ERR_CUDA;
