@@ -2,8 +2,16 @@
 //
 // Not part of the product: tests compare the CUDA path against it, and bench.py times
 // it on the host cores as the CPU baseline ("kind": "port").  It restates, in plain
-// C++/OpenMP, the per-step algorithm of the reference for a mesh whose every species is
-// one patch covering the domain (the single-level case):
+// C++/OpenMP, the per-step algorithm of the reference for one species on its
+// block-structured AMR hierarchy, and the construction of that hierarchy at t = 0:
+//   SolverManager::SolverManager      SolverManager.cpp:8-26
+//   Mesh::Mesh, updateHierarchy(true)  Mesh.cpp:8-50, 132-210 (flagging, clustering by
+//                                      Mesh.cpp:298-792, promoteHierarchyToMesh :794-875)
+//   Rectangle::getError / weights      Rectangle.cpp:866-890, 68-74; Rectangle.hpp:128-130
+//   Settings::DetermineMaximum         Settings.cpp:181-194
+//   Mesh::PushData / PushBoundaryC     Mesh.cpp:91-106, 904-917 (ghost fills, coarse-fine
+//                                      fluxes, limiter exchange; Rectangle.cpp:307-614,
+//                                      1032-1253, 1625-1960)
 //   SolverManager::Advance            SolverManager.cpp:28-39
 //   EMFieldSolver::AssembleRhoAndJ     EMSolver.cpp:104-122
 //   Rectangle::CalculateRhoAndJ (MKL)  Rectangle.cpp:157-237, 276-281
@@ -30,6 +38,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <iterator>
+#include <limits>
 #include <map>
 #include <sstream>
 #include <string>
@@ -362,23 +372,11 @@ struct Solver {
         lu.factor_rows(rows);
     }
 
+    // SolverManager::SolverManager (SolverManager.cpp:8-26): the hierarchy (Mesh::Mesh),
+    // the ghost fill, then EMFieldSolver::EnforceChargeNeutralization (EMSolver.cpp:621-629).
     void init_distribution() {
-        for (auto &P : patches) {
-            const int nvals = std::pow(pr.r, P.depth + pr.quadDepth);
-#pragma omp parallel for schedule(guided)
-            for (int i = 0; i < P.nx; i++)
-                for (int j = 0; j < P.np; j++) {
-                    double temp = 0.0;
-                    for (int k = 0; k < nvals; k++)
-                        for (int l = 0; l < nvals; l++) {
-                            double xp = ((0.5 + k) / nvals + i + P.x_pos) * P.dx;
-                            double pp = P.pmin + P.dp * ((0.5 + l) / nvals + j + P.p_pos);
-                            temp += pr.init_f(xp, pp);
-                        }
-                    P.f[0][P.id(i, j)] = temp * (1 / std::pow(nvals, 2.0));
-                    P.f[1][P.id(i, j)] = temp * (1 / std::pow(nvals, 2.0));
-                }
-        }
+        build_hierarchy();
+        push_data(1);
         assemble();
         for (int i = 0; i < F.n; i++) F.neut[i] = -F.charge[i];
         std::fill(F.J.begin(), F.J.end(), 0.0);
@@ -482,6 +480,327 @@ struct Solver {
             for (int rl : lv[l])
                 for (int rr : lv[l])
                     if (rl != rr) connect_same(rl, rr);
+    }
+
+    // ---------------------------------------------------------------- initial hierarchy
+    // Mesh::Mesh (Mesh.cpp:8-50) in the reference's default configuration (MKLINIT 0):
+    // the initial getError(init) keeps its flags in a private list (Mesh.cpp:272-287),
+    // so the hierarchy starts as the base patch alone and gains its finer levels from
+    // maxDepth rounds of flagging on quadrature-initialised data, every round
+    // re-initialising every patch from the quadrature (promoteHierarchyToMesh(true)).
+    typedef std::pair<int, int> Cell;  // (i, j) in a level's global coordinates
+    struct Box {                       // Mesh's rect: lower-left and upper-right corners
+        int x0, p0, x1, p1;
+    };
+    std::vector<std::vector<Box>> H;  // H[0] = the base level, coarse to fine
+    double fmax = 0.0;
+
+    // Settings::DetermineMaximum (Settings.cpp:181-194): the peak of f on the finest x grid at p = 0.
+    void determine_maximum() {
+        const double dx0 = pr.GetDx(0);
+        double mv(0.0);
+        for (int i = 0; i < pr.GetXSize(0); i++) {
+            double t(pr.init_f((i + 0.5) * dx0, 0));
+            mv = t > mv ? t : mv;
+        }
+        fmax = mv;
+    }
+
+    // Rectangle::InitializeDistribution (Rectangle.cpp:616-665, non-MKL loop)
+    void quadrature(Patch &P) {
+        const int nvals = std::pow(pr.r, P.depth + pr.quadDepth);
+#pragma omp parallel for schedule(guided)
+        for (int i = 0; i < P.nx; i++)
+            for (int j = 0; j < P.np; j++) {
+                double temp = 0.0;
+                for (int k = 0; k < nvals; k++)
+                    for (int l = 0; l < nvals; l++) {
+                        double xp = ((0.5 + k) / nvals + i + P.x_pos) * P.dx;
+                        double pp = P.pmin + P.dp * ((0.5 + l) / nvals + j + P.p_pos);
+                        temp += pr.init_f(xp, pp);
+                    }
+                P.f[0][P.id(i, j)] = temp * (1 / std::pow(nvals, 2.0));
+                P.f[1][P.id(i, j)] = temp * (1 / std::pow(nvals, 2.0));
+            }
+    }
+
+    // Rectangle::getError (Rectangle.cpp:866-890) with ErrorEstimate (Rectangle.hpp:128-130)
+    // and the weights of the Rectangle constructor (Rectangle.cpp:68-74).  The problem's
+    // RefinementOverride is false.
+    void patch_flags(const Patch &P, std::vector<Cell> &out) const {
+        const double rr = pr.r;
+        double w[5];
+        w[0] = 0.5 / fmax * std::pow(rr, -0.5 * P.depth);
+        w[1] = 0.5 / fmax * std::pow(rr, -0.5 * P.depth);
+        w[2] = 0.5 / fmax * std::pow(rr, -2.0 * P.depth);
+        w[3] = 0.5 / fmax * std::pow(rr, -2.0 * P.depth);
+        w[4] = pr.P.sizeWeight / fmax * std::pow(rr, -pr.maxDepth + P.depth);
+        int band = 0;
+        for (int k = 0; k <= pr.maxDepth - P.depth; k++) band += std::pow(pr.r, k);
+        band *= 3;
+        const int ilo = std::max(P.x_pos, band), ihi = std::min(P.x_pos + P.nx, pr.GetXSize(P.depth) - band);
+        const int jlo = std::max(P.p_pos, band), jhi = std::min(P.p_pos + P.np, pr.GetPSize(P.depth) - band);
+        const double *f = P.f[1].data();
+        for (int i = ilo; i < ihi; i++)
+            for (int j = jlo; j < jhi; j++) {
+                const int a = i - P.x_pos, b = j - P.p_pos;
+                const double c = f[P.id(a, b)];
+                double e = w[0] * std::fabs(f[P.id(a + 1, b)] - f[P.id(a - 1, b)]) +
+                           w[1] * std::fabs(f[P.id(a, b + 1)] - f[P.id(a, b - 1)]) +
+                           w[2] * std::fabs(f[P.id(a + 1, b)] - 2 * c + f[P.id(a - 1, b)]) +
+                           w[3] * std::fabs(f[P.id(a, b + 1)] - 2 * c + f[P.id(a, b - 1)]) + w[4] * std::fabs(c);
+                if (e > pr.P.crit) out.push_back(Cell(i, j));
+            }
+    }
+    // Mesh::getError(lvl, false) (Mesh.cpp:289-294): hierarchy index -> depth maxDepth - lvl
+    void level_flags(int lvl, std::vector<Cell> &out) const {
+        for (int k : lv[pr.maxDepth - lvl]) patch_flags(patches[k], out);
+    }
+
+    // Mesh::interpRectanglesUp (Mesh.cpp:298-313): close the upper corner and scale the
+    // boxes found on hierarchy index lvl to the grid of lvl + 1 (int *= double truncates).
+    void boxes_up(std::vector<Box> &bs, int lvl) const {
+        const int n0 = pr.GetXSize(pr.maxDepth - lvl), m0 = pr.GetPSize(pr.maxDepth - lvl);
+        const int n1 = pr.GetXSize(pr.maxDepth - (lvl + 1)), m1 = pr.GetPSize(pr.maxDepth - (lvl + 1));
+        for (Box &b : bs) {
+            b.x1 += 1;
+            b.p1 += 1;
+            b.x0 *= (n1 / double(n0));
+            b.p0 *= (m1 / double(m0));
+            b.x1 *= (n1 / double(n0));
+            b.p1 *= (m1 / double(m0));
+        }
+    }
+    // Mesh::mergeDownFlaggedData (Mesh.cpp:315-339): the cells of hierarchy index lvl that
+    // lie under a box of index lvl + 2 widened by two ratios (upper x bound one further).
+    void merge_down(int lvl, const Box &b, std::vector<Cell> &out) const {
+        const int n0 = pr.GetXSize(pr.maxDepth - lvl), m0 = pr.GetPSize(pr.maxDepth - lvl);
+        const int n2 = pr.GetXSize(pr.maxDepth - (lvl + 2)), m2 = pr.GetPSize(pr.maxDepth - (lvl + 2));
+        const int w = 2 * (int)pr.r;
+        for (int i = b.x0 - w; i <= b.x1 + w + 1; i++)
+            for (int j = b.p0 - w; j <= b.p1 + w; j++) {
+                int ic = i * (n0 / double(n2));
+                int jc = j * (m0 / double(m2));
+                if (ic > -1 && ic < n0 && jc > -1 && jc < m0) out.push_back(Cell(ic, jc));
+            }
+        std::sort(out.begin(), out.end());
+        out.erase(std::unique(out.begin(), out.end()), out.end());
+    }
+
+    // Mesh::getExtrema (Mesh.cpp:626-642)
+    static Box extrema(const std::vector<Cell> &c) {
+        Box b{c[0].first, c[0].second, c[0].first, c[0].second};
+        for (const Cell &x : c) {
+            b.x0 = std::min(b.x0, x.first);
+            b.x1 = std::max(b.x1, x.first);
+            b.p0 = std::min(b.p0, x.second);
+            b.p1 = std::max(b.p1, x.second);
+        }
+        return b;
+    }
+    // Mesh::hasHole (Mesh.cpp:597-624): the first zero run of a signature.  Returns found
+    // and (start, finish): the entry before the run (or 0 at the edge) and the first entry
+    // after it (or the last entry).
+    static bool first_gap(const std::vector<int> &sig, int &start, int &finish) {
+        start = finish = 0;
+        size_t z = 0;
+        while (z < sig.size() && sig[z] != 0) z++;
+        if (z == sig.size()) return false;
+        start = z == 0 ? 0 : (int)z - 1;
+        size_t e = z;
+        while (e < sig.size() && sig[e] == 0) e++;
+        finish = e == sig.size() ? (int)e - 1 : (int)e;
+        return true;
+    }
+    // The sign-change search of Mesh::identifyInflection (Mesh.cpp:449-595) along one
+    // direction.  lap is the signature's discrete Laplacian.  Returns -1 when the
+    // signature is too short to look at, 0 when it has no sign change (bisect), 1 with
+    // (index, size) of the chosen change otherwise; `far` is the distance the reference
+    // starts its closest-to-centre search from (INT_MAX along x, 32767 along p).
+    static int best_inflection(const std::vector<int> &lap, int far, int &index, int &size) {
+        index = size = 0;
+        const int n = (int)lap.size();
+        if (n <= 2) return -1;
+        std::vector<int> at, mag;
+        for (int i = 0; i + 1 < n; i++) {
+            const int a = lap[i], b = lap[i + 1];
+            const int sa = (a > 0) - (a < 0), sb = (b > 0) - (b < 0);
+            if (a != 0 && b != 0 && sa != sb) {
+                at.push_back(i);
+                mag.push_back(std::abs(b - a));
+            }
+        }
+        if (at.empty()) return 0;
+        if (at.size() == 1) {
+            index = at[0];
+            size = mag[0];
+            return 1;
+        }
+        const int top = *std::max_element(mag.begin(), mag.end());
+        const int ties = (int)std::count(mag.begin(), mag.end(), top);
+        int pick = 0;
+        if (ties > 1) {
+            int best = far;
+            const int mid = n / 2;  // the reference's centre: the Laplacian's length / 2
+            for (size_t k = 0; k < at.size(); k++)
+                if (best > std::abs(at[k] - mid)) {
+                    best = std::abs(at[k] - mid);
+                    pick = (int)k;
+                }
+        } else {
+            pick = (int)(std::max_element(mag.begin(), mag.end()) - mag.begin());
+        }
+        index = at[pick];
+        size = mag[pick];
+        return 1;
+    }
+    static std::vector<int> laplacian(const std::vector<int> &sig) {
+        std::vector<int> d;
+        if (sig.size() >= 3) {
+            d.resize(sig.size() - 2);
+            for (size_t h = 1; h + 1 < sig.size(); h++) d[h - 1] = sig[h - 1] + sig[h + 1] - 2 * sig[h];
+        }
+        return d;
+    }
+    static bool inside(const Cell &c, const Box &b) {
+        return c.first >= b.x0 && c.first <= b.x1 && c.second >= b.p0 && c.second <= b.p1;
+    }
+    // Mesh::splitRectangle (Mesh.cpp:644-792): recursive cuts (holes first, the larger of
+    // the two when both directions have one; then the largest signature inflection;
+    // bisection of the long side last) until a box is efficient enough or too small.
+    std::vector<Box> split(const Box &b, const std::vector<Cell> &cells) const {
+        const double cellsIn = double((b.x1 - b.x0 + 1) * (b.p1 - b.p0 + 1));
+        if (cells.size() / cellsIn > pr.P.minEff) return {b};
+        std::vector<int> sx(b.x1 - b.x0 + 1, 0), sp(b.p1 - b.p0 + 1, 0);
+        for (const Cell &c : cells) {
+            sx.at(c.first - b.x0)++;
+            sp.at(c.second - b.p0)++;
+        }
+        int hx0, hx1, hp0, hp1;
+        const bool gx = first_gap(sx, hx0, hx1), gp = first_gap(sp, hp0, hp1);
+        hx0 += b.x0, hx1 += b.x0, hp0 += b.p0, hp1 += b.p0;
+        Box one, two;
+        bool cutx;
+        int cut_lo = 0, cut_hi = 0;  // one ends at cut_lo, two starts at cut_hi
+        if (gx || gp) {
+            cutx = gx && (!gp || std::abs(hx1 - hx0) > std::abs(hp1 - hp0));
+            cut_lo = cutx ? hx0 : hp0;
+            cut_hi = cutx ? hx1 : hp1;
+        } else {
+            // Mesh::computeSignatures builds the Laplacians only for boxes at least three
+            // cells long in that direction (Mesh.cpp:412-441)
+            const std::vector<int> lx = (b.x1 - b.x0 >= 2) ? laplacian(sx) : std::vector<int>();
+            const std::vector<int> lp = (b.p1 - b.p0 >= 2) ? laplacian(sp) : std::vector<int>();
+            int ix, mx, ip, mp;
+            const int kx = best_inflection(lx, std::numeric_limits<int>::max(), ix, mx);
+            const int kp = best_inflection(lp, 32767, ip, mp);
+            if (kx == 0 && kp == 0) {  // bisect the long side
+                const double lxd = b.x1 - b.x0, lpd = b.p1 - b.p0;
+                cutx = lxd > lpd;
+                const double at = cutx ? std::floor((lxd / 2) + b.x0) : std::floor((lpd / 2) + b.p0);
+                cut_lo = (int)at;
+                cut_hi = (int)at + 1;
+            } else if ((lx.size() <= 2 && lp.size() <= 2) || (mx == 0 && mp == 0)) {
+                return {b};
+            } else {
+                cutx = mx > mp;
+                cut_lo = cutx ? ix + b.x0 + 1 : ip + b.p0 + 1;
+                cut_hi = cut_lo + 1;
+            }
+        }
+        if (cutx) {
+            one = Box{b.x0, b.p0, cut_lo, b.p1};
+            two = Box{cut_hi, b.p0, b.x1, b.p1};
+        } else {
+            one = Box{b.x0, b.p0, b.x1, cut_lo};
+            two = Box{b.x0, cut_hi, b.x1, b.p1};
+        }
+        std::vector<Cell> c1, c2;
+        for (const Cell &c : cells) (inside(c, one) ? c1 : c2).push_back(c);
+        std::vector<Box> out;
+        if (!c1.empty()) out = split(one, c1);
+        if (!c2.empty()) {
+            auto more = split(two, c2);
+            out.insert(out.end(), more.begin(), more.end());
+        }
+        return out;
+    }
+
+    // Mesh::promoteHierarchyToMesh(true) (Mesh.cpp:794-875): patches for every box (depth 0
+    // the finest; a hierarchy shorter than maxDepth + 1 levels leaves the finest depths
+    // empty and compares its edges against the sizes of its own depth count), every patch
+    // from the quadrature, connectivity, the ghost fill and f0 = f1 (FCTTimeStep(0,-1,3)).
+    void promote() {
+        const int N = (int)H.size() - 1, empty = pr.maxDepth - N;
+        patches.clear();
+        lv.assign(pr.maxDepth + 1, {});
+        for (int l = N; l >= 0; l--) {
+            const int depth = N - l + empty;
+            const int xs = pr.GetXSize(N - l), ps = pr.GetPSize(N - l);
+            for (const Box &b : H[l]) {
+                Patch P = make_patch(depth, b.x0, b.p0, b.x1 - b.x0, b.p1 - b.p0);
+                P.up = b.p1 == ps;
+                P.down = b.p0 == 0;
+                P.left = b.x0 == 0;
+                P.right = b.x1 == xs;
+                lv[depth].push_back((int)patches.size());
+                patches.push_back(std::move(P));
+            }
+        }
+        for (auto &P : patches) quadrature(P);
+        connect_keep_f();
+        push_data(1);
+        for (auto &P : patches) P.f[0] = P.f[1];
+    }
+
+    // Mesh::updateHierarchy(true) (Mesh.cpp:132-210)
+    void update_hierarchy() {
+        const int top = (int)H.size() - 1;
+        std::vector<Cell> cells;
+        for (int l = top; l > -1; l--) {
+            if (l < (int)H.size() - 2) {
+                std::vector<Cell> own, under;
+                if (H.size() > 2)
+                    for (const Box &b : H.at(l + 2)) {
+                        std::vector<Cell> t;
+                        merge_down(l, b, t);
+                        under.insert(under.end(), t.begin(), t.end());
+                    }
+                level_flags(l, own);
+                std::sort(own.begin(), own.end());
+                // `under` is a concatenation of sorted runs, not sorted itself; the
+                // reference passes it to set_union as it is
+                std::set_union(own.begin(), own.end(), under.begin(), under.end(), std::back_inserter(cells));
+            } else {
+                level_flags(l, cells);
+            }
+            if (!cells.empty()) {
+                std::vector<Box> found = split(extrema(cells), cells);
+                if (l == top) {
+                    if (l < pr.maxDepth) {
+                        boxes_up(found, l);
+                        H.push_back(found);
+                    }
+                } else {
+                    boxes_up(found, l);
+                    H.at(l + 1) = found;
+                }
+            } else if (l < top) {
+                H.erase(H.begin() + l + 1);
+            }
+            cells.clear();
+        }
+        promote();
+    }
+
+    void build_hierarchy() {
+        determine_maximum();
+        H.assign(1, {Box{0, 0, pr.GetXSize(pr.maxDepth), pr.GetPSize(pr.maxDepth)}});
+        promote();
+        for (int i = 0; i < pr.maxDepth; i++) {
+            push_data(1);
+            update_hierarchy();
+        }
     }
 
     // ---------------------------------------------------------------- ghost fills
@@ -1315,11 +1634,6 @@ int main(int argc, char **argv) {
     P.bdens = getd("bdens", P.bdens);
     P.bp0 = getd("bp0", P.bp0);
     P.bTe = getd("bTe", P.bTe);
-    if (P.Lfinest != 1 && !kv.count("load")) {
-        fprintf(stderr, "multi-level runs start from a state file (load=): the port restates the step, not the\n"
-                        "hierarchy construction\n");
-        return 3;
-    }
     long long steps = geti("steps", 0), dump_every = geti("dump_every", 0), time_steps = geti("time_steps", 0);
     std::string dumpdir = kv.count("dumpdir") ? kv["dumpdir"] : "";
     std::vector<double> dts;
@@ -1360,8 +1674,9 @@ int main(int argc, char **argv) {
         std::sort(per.begin(), per.end());
         long long cells = 0;
         for (auto &p : S.patches) cells += (long long)p.nx * p.np;  // every level, covered cells included
-        printf("{\"cells\": %lld, \"steps\": %lld, \"best_s\": %.6f, \"median_s\": %.6f, \"threads\": %d, \"init_s\": %.3f}\n",
-               cells, time_steps, per.front(), per[per.size() / 2], omp_get_max_threads(),
+        printf("{\"cells\": %lld, \"patches\": %zu, \"steps\": %lld, \"best_s\": %.6f, \"median_s\": %.6f, "
+               "\"threads\": %d, \"init_s\": %.3f}\n",
+               cells, S.patches.size(), time_steps, per.front(), per[per.size() / 2], omp_get_max_threads(),
                std::chrono::duration<double>(t1 - t0).count());
     }
     return 0;

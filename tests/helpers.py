@@ -89,10 +89,11 @@ def port_exe() -> Path:
 
 def gpu_vs_port(ctx, problem, steps: int, workdir: Path, init_state: Path | None = None,
                 threads: int | None = None) -> dict:
-    """The GPU path and the oracle port advanced `steps` RK steps from the same state with
-    the GPU path's dt sequence; returns compare_states' relative L-inf errors (f slots 0
-    and 1, every field array, Ex0, time).  The start is `init_state`, or the GPU path's
-    own initial hierarchy when None."""
+    """The GPU path and the oracle port advanced `steps` RK steps with the GPU path's dt
+    sequence; returns compare_states' relative L-inf errors after the steps (f slots 0 and
+    1, every field array, Ex0, time).  Both start from `init_state` when given.  When None,
+    each builds the initial hierarchy itself (flagging, clustering, quadrature) and the
+    errors of the two initial states are returned too, under keys prefixed "init_"."""
     import os
     import subprocess
 
@@ -100,11 +101,10 @@ def gpu_vs_port(ctx, problem, steps: int, workdir: Path, init_state: Path | None
 
     workdir = Path(workdir)
     s = SolverManager(ctx, problem)
-    if init_state is None:
-        init_state = workdir / "init.bin"
-        s.save_state(init_state)
-    else:
+    if init_state is not None:
         s.load_state(init_state)
+    else:
+        s.save_state(workdir / "gpu_init.bin")
     dts = []
     for _ in range(steps):
         dt = s.CalculateDt()
@@ -115,9 +115,15 @@ def gpu_vs_port(ctx, problem, steps: int, workdir: Path, init_state: Path | None
     env = dict(os.environ)
     if threads:
         env["OMP_NUM_THREADS"] = str(threads)
-    subprocess.run([str(port_exe()), *problem.harness_args(), f"load={init_state}",
-                    "dts=" + ",".join(repr(d) for d in dts), f"steps={steps}", f"dump_every={steps}",
-                    f"dumpdir={workdir}"], check=True, capture_output=True, env=env)
-    ref = vxstate.read_state(workdir / f"state_{steps:05d}.bin")
-    got = vxstate.read_state(workdir / "gpu.bin")
-    return compare_states(got, ref, 0.0)
+    cmd = [str(port_exe()), *problem.harness_args(), "dts=" + ",".join(repr(d) for d in dts), f"steps={steps}",
+           f"dump_every={steps}", f"dumpdir={workdir}"]
+    if init_state is not None:
+        cmd.append(f"load={init_state}")
+    subprocess.run(cmd, check=True, capture_output=True, env=env)
+    err = compare_states(vxstate.read_state(workdir / "gpu.bin"), vxstate.read_state(workdir / f"state_{steps:05d}.bin"),
+                         0.0)
+    if init_state is None:
+        e0 = compare_states(vxstate.read_state(workdir / "gpu_init.bin"), vxstate.read_state(workdir / "state_00000.bin"),
+                            0.0)
+        err.update({"init_" + k: v for k, v in e0.items()})
+    return err

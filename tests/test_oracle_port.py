@@ -1,8 +1,9 @@
 """The oracle port (oracle/port, C++ restatement) is pinned to the reference build.
 
 The golden fixtures were dumped by the reference itself; the port, started from the same
-problem arguments (t=0, its own quadrature) or from a dumped state with the reference's
-dt sequence, must reproduce them bit for bit.
+problem arguments (t=0: its own initial hierarchy and quadrature, multi-level cases
+included) or from a dumped state with the reference's dt sequence, must reproduce them
+bit for bit.
 """
 import subprocess
 from pathlib import Path
@@ -15,7 +16,10 @@ from helpers import GOLDEN, case_args, compare_states, golden
 
 ROOT = Path(__file__).resolve().parent.parent
 PORT = ROOT / "oracle" / "_port" / "veritas_port"
-CASES = {"slab64": [0, 1, 2, 5], "drift128": [0, 1, 3], "edge64": [0, 1, 3]}
+# single-level cases, and the one-species AMR cases from t = 0: the port builds the
+# initial hierarchy itself (maxDepth rounds of flagging, clustering and quadrature)
+CASES = {"slab64": [0, 1, 2, 5], "drift128": [0, 1, 3], "edge64": [0, 1, 3],
+         "amr2": [0, 1, 3], "beam2": [0, 1, 3], "beam3": [0, 1, 3], "ragged2": [0, 1, 3]}
 
 
 @pytest.fixture(scope="module")

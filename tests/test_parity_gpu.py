@@ -191,8 +191,9 @@ def test_gpu_matches_port_at_512x128(tmp_path):
 @pytest.mark.parametrize("workload", ["laser_slab_2048x256", "laser_slab_amr_4096x512"])
 def test_gpu_matches_port_at_benchmark_size(ctx, tmp_path, workload):
     """The benchmarked workloads at full size (one level 2048 x 256; two levels on a
-    4096 x 512 base): the GPU path and the oracle port from the GPU path's initial
-    hierarchy, two RK steps with the same dt, every array within 1e-10."""
+    4096 x 512 base): the GPU path and the oracle port each build the initial hierarchy
+    (same patch layout, every array within 1e-10), then take two RK steps with the same
+    dt (every array within 1e-10)."""
     from veritas_gb300.workloads import WORKLOADS
 
     err = gpu_vs_port(ctx, WORKLOADS[workload](), 2, tmp_path)

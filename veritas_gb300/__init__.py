@@ -4,7 +4,7 @@ The classes follow the reference's driver interface: :class:`SolverManager` stan
 Veritas's ``SolverManager`` (SolverManager.hpp:5-19) with ``CalculateDt``, ``Advance``
 and the state exchange used for checkpoints and parity tests.  Every call goes through
 ``libvx_cuda.so`` (declared in ``include/vx.h``); there is no CPU fallback — if the
-library cannot be loaded, importing this module raises.
+library cannot be loaded, the first call into it raises.
 """
 from __future__ import annotations
 
@@ -122,11 +122,27 @@ def _load() -> ctypes.CDLL:
     return lib
 
 
-_lib = _load()
+_CDLL = None
 
 
 def lib() -> ctypes.CDLL:
-    return _lib
+    """The library, loaded on first use (raises if it is missing: there is no fallback)."""
+    global _CDLL
+    if _CDLL is None:
+        _CDLL = _load()
+    return _CDLL
+
+
+class _LazyLib:
+    """Forwards to the library, loading it on the first call: importing the package maps
+    nothing, so a process that only reads problem definitions (the CPU reference arm of
+    the benchmark) never loads the CUDA library."""
+
+    def __getattr__(self, name):
+        return getattr(lib(), name)
+
+
+_lib = _LazyLib()
 
 
 def _check(rc: int) -> None:
