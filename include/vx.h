@@ -73,6 +73,134 @@ typedef struct vx_problem {
 /* Fills *p with the defaults of the 2048 x 256 single-level laser/slab case. */
 void vx_problem_defaults(vx_problem *p);
 
+/* ---------------------------------------------------------------- user problems
+ * The reference's whole user surface is its problem file (veritas.cpp): the user fills
+ * the Input / Particles / Output structs (initialConditions, veritas.cpp:7), edits the
+ * Settings (Settings::settingsOverride, :36) and supplies InitialDistribution (:107),
+ * GetBY / GetBZ (:80, :93, the laser at x = 0) and RefinementOverride (:76), then
+ * recompiles.  Here the same hooks are C callbacks handed to vx_run_create_hooks: a
+ * custom problem needs no rebuild of the library.  The structs mirror the reference's
+ * (Settings.hpp:4-65) with fixed-size arrays for the per-species vectors. */
+#define VX_MAX_SPECIES 8
+#define VX_MAX_MISC 8
+
+/* Input (Settings.hpp:4-11). */
+typedef struct vx_input {
+    double minEfficiency, dx, k, refinementCriteria, cfl, sizeWeight, preLength, postLength;
+    uint32_t nx, r, Lfinest;
+    double plasma_xl_bound, plasma_xr_bound;
+    int32_t ntempEM;                 /* entries of tempEM in use */
+    double tempEM[VX_MAX_MISC];
+} vx_input;
+
+/* Particles (Settings.hpp:13-20): entry s of each array belongs to species s. */
+typedef struct vx_particles {
+    int32_t nspecies;
+    double mass[VX_MAX_SPECIES], charge[VX_MAX_SPECIES];
+    uint32_t np[VX_MAX_SPECIES];
+    double dp[VX_MAX_SPECIES], pmin[VX_MAX_SPECIES];
+    int32_t nmisc[VX_MAX_SPECIES];  /* entries of misc[s] in use */
+    double misc[VX_MAX_SPECIES][VX_MAX_MISC];
+} vx_particles;
+
+/* Output (Settings.hpp:22-33): nonzero = on. */
+typedef struct vx_output {
+    int32_t time, rectangleData, charge, energy, potential, EFieldLongitudinal, EFieldTransverse, BFieldTransverse,
+        AFieldSquared;
+    int32_t precision;
+} vx_output;
+
+/* Settings (Settings.hpp:35-65): what the hooks read, and what settings_override may
+ * change (the fields the reference's Settings::settingsOverride may assign: dx, dp,
+ * pmin, temp, tempEM, quadratureDepth, the grid scalars, ...).  temp[s] is the
+ * reference's temp[s] (Particles::misc on entry), ntemp[s] its length. */
+typedef struct vx_settings {
+    double dx, time, minEfficiency, preLength, postLength, refinementCriteria, cfl, sizeWeight, plasma_xl_bound,
+        plasma_xr_bound;
+    int32_t nspecies;
+    double m[VX_MAX_SPECIES], q[VX_MAX_SPECIES], m_inv[VX_MAX_SPECIES], dp[VX_MAX_SPECIES], fMax[VX_MAX_SPECIES],
+        pmin[VX_MAX_SPECIES];
+    int32_t ntemp[VX_MAX_SPECIES];
+    double temp[VX_MAX_SPECIES][VX_MAX_MISC];
+    int32_t ntempEM;
+    double tempEM[VX_MAX_MISC];
+    uint32_t x_size_finest, x_size, refinementRatio;
+    int32_t maxDepth, quadratureDepth;
+    uint32_t p_size[VX_MAX_SPECIES], p_size_finest[VX_MAX_SPECIES];
+} vx_settings;
+
+/* The problem hooks.  `user` is passed back to every callback.  The settings a callback
+ * sees are those after settings_override, with the derived sizes, m_inv and fMax filled
+ * in once the Settings are complete (the reference's DetermineMaximum calls
+ * initial_distribution before that); `time` is not kept current (the laser hooks get
+ * the time as an argument).  initial_distribution is called concurrently from several
+ * host threads and must be thread-safe; the others from the calling thread.  Units are
+ * SI, as in the reference. */
+typedef struct vx_hooks {
+    void *user;
+    /* initialConditions (veritas.cpp:7): fill the structs, which arrive holding the
+     * reference's defaults (Settings.hpp:4-33).  Required. */
+    void (*initial_conditions)(void *user, vx_input *grid, vx_particles *particles, vx_output *output);
+    /* Settings::settingsOverride (veritas.cpp:36).  Optional. */
+    void (*settings_override)(void *user, vx_settings *s);
+    /* Settings::InitialDistribution (veritas.cpp:107): f(x, p) of species at t = 0.  Required. */
+    double (*initial_distribution)(void *user, const vx_settings *s, double x, double p, int species);
+    /* Settings::GetBY / GetBZ (veritas.cpp:80, :93): the transverse B the laser imposes at
+     * x (the solver asks for x = 0) and time t.  Optional (NULL: 0). */
+    double (*get_by)(void *user, const vx_settings *s, double x, double t);
+    double (*get_bz)(void *user, const vx_settings *s, double x, double t);
+    /* Settings::RefinementOverride (veritas.cpp:76): nonzero refines the cell at cell
+     * centre x and lower p face p whatever its error estimate.  Optional (NULL: never). */
+    int (*refinement_override)(void *user, const vx_settings *s, double x, double p, int depth, int species);
+} vx_hooks;
+
+/* The reference's defaults of Input, Particles (one species) and Output (Settings.hpp:4-33). */
+void vx_input_defaults(vx_input *grid, vx_particles *particles, vx_output *output);
+
+/* SolverManager::SolverManager (SolverManager.cpp:8-26) for a problem given by hooks:
+ * the Settings from initial_conditions and settings_override (Settings.cpp:5-54,
+ * validation errors are VX_ERR_INVALID), the initial hierarchy from
+ * initial_distribution's quadrature and the error estimate with refinement_override
+ * (Mesh.cpp:8-50), the field solver and the neutralising charge.  precision 64 or 32 and
+ * poisson as in vx_problem.  The hooks are kept for the life of the run (the laser hooks
+ * are called every stage, refinement_override at every regrid). */
+int vx_run_create_hooks(vx_ctx *ctx, const vx_hooks *hooks, int precision, int poisson, vx_run **out);
+/* The run's Settings as the hooks see them (time current). */
+int vx_run_settings(vx_run *run, vx_settings *out);
+
+/* ---------------------------------------------------------------- per-class calls
+ * The steps SolverManager::Advance (SolverManager.cpp:28-39) takes per RK stage, one entry
+ * point each, for callers that drive the stages themselves.  Each launches on the
+ * context stream without a CUDA graph; called in the reference's order —
+ *   for stage in 0..5: vx_run_moments; vx_run_poisson; vx_run_vlasov_stage(stage, dt,
+ *   VX_SUB_ALL); vx_run_update_time(stage, dt); vx_run_maxwell_stage(stage, dt)
+ * — they give the same bits as vx_run_advance(dt). */
+/* EMFieldSolver::AssembleRhoAndJ (EMSolver.cpp:104-122): moments of every patch
+ * (Rectangle::CalculateRhoAndJ, Rectangle.cpp:157-282), interpolated to the finest grid
+ * and summed over levels and species (Level.cpp:19-62). */
+int vx_run_moments(vx_run *run);
+/* EMFieldSolver::UpdatePotential (EMSolver.cpp:156-192): phi, Ex0 and E_x on the finest grid. */
+int vx_run_poisson(vx_run *run);
+/* Mesh::Advance(dt, stage) (Mesh.cpp:64-89) for every species: sub_mask selects its parts.
+ * Level::FCTTimeStep sub-steps (Level.cpp:12-16 -> Rectangle::FCTTimeStep,
+ * Rectangle.cpp:1255-1623) and the exchanges between them. */
+#define VX_SUB_FLUX 0x1    /* sub-step 0: face values, fluxes (coarse/fine faces included), low-order f */
+#define VX_SUB_LIMIT 0x2   /* PushData(2), sub-step 1 (limiter R and C), PushBoundaryC */
+#define VX_SUB_UPDATE 0x4  /* sub-step 2 (antidiffusive update), PushData(1) */
+#define VX_SUB_COPY 0x8    /* sub-step 3 (f0 = f1): at stage 5 only, as Mesh::Advance */
+#define VX_SUB_ALL 0xf
+int vx_run_vlasov_stage(vx_run *run, int stage, double dt, unsigned sub_mask);
+/* Settings::UpdateTime (Settings.cpp:166-179). */
+int vx_run_update_time(vx_run *run, int stage, double dt);
+/* EMFieldSolver::RGKStep (EMSolver.cpp:194-202): the Maxwell stage with the laser of
+ * get_by/get_bz at the run's current time, then a^2 on the faces. */
+int vx_run_maxwell_stage(vx_run *run, int stage, double dt);
+/* Mesh::getError(lvl, false) (Mesh.cpp:289-294 -> Rectangle::getError,
+ * Rectangle.cpp:866-890): the flagged cells (i, j) of the patches of one species and
+ * depth (0 = finest), in the reference's patch and loop order, as pairs in ij_out (up to
+ * cap pairs); *count receives the total. */
+int vx_run_flag(vx_run *run, int species, int depth, int32_t *ij_out, int cap, int *count);
+
 const char *vx_last_error(void);
 
 /* Context: one GPU + one stream. */

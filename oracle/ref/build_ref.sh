@@ -32,6 +32,16 @@ for src in BoundaryCondition Level Rectangle SolverManager EMSolver Mesh Setting
 done
 "$CXX" "${FLAGS[@]}" -c "$HERE/harness.cpp" -o "$OUT/obj/harness.o" & pids+=($!)
 "$CXX" "${FLAGS[@]}" -c "$HERE/mkl_shim.cpp" -o "$OUT/obj/mkl_shim.o" & pids+=($!)
+# the same driver over a user problem written against the C hooks (tests/hooks)
+HOOKS="$HERE/../../tests/hooks"
+mkdir -p "$OUT/hobj"
+"$CXX" "${FLAGS[@]}" -DVX_HOOKS_PROBLEM -I"$HOOKS" -c "$HERE/harness.cpp" -o "$OUT/hobj/harness_hooks.o" & pids+=($!)
+"${CC:-gcc}" -O2 -ffp-contract=off -c "$HOOKS/sin2_problem.c" -o "$OUT/hobj/sin2_problem.o" & pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 "$CXX" -fopenmp "$OUT"/obj/*.o -o "$OUT/veritas_ref"
-echo "built $OUT/veritas_ref"
+REFOBJ=()
+for src in BoundaryCondition Level Rectangle SolverManager EMSolver Mesh Settings mkl_shim; do
+  REFOBJ+=("$OUT/obj/$src.o")
+done
+"$CXX" -fopenmp "${REFOBJ[@]}" "$OUT/hobj/harness_hooks.o" "$OUT/hobj/sin2_problem.o" -lm -o "$OUT/veritas_ref_hooks"
+echo "built $OUT/veritas_ref $OUT/veritas_ref_hooks"

@@ -19,6 +19,7 @@
 
 #include <chrono>
 #include <cstdio>
+#include <cstring>
 #include <map>
 #include <string>
 
@@ -69,6 +70,7 @@ VX_ROB(R_down, Rectangle, bool, down)
 VX_ROB(R_left, Rectangle, bool, left)
 VX_ROB(R_right, Rectangle, bool, right)
 
+#ifndef VX_HOOKS_PROBLEM
 // ---------------------------------------------------------------- problem parameters
 // Synthetic laser / plasma-slab problem (all lengths in laser wavelengths, momenta in
 // m_e c, temperatures in keV).  The product carries its own copy of these formulas.
@@ -200,6 +202,120 @@ double Settings::InitialDistribution(double x, double p, int particleType) {
     return v;
 }
 
+#else  // VX_HOOKS_PROBLEM
+// ---------------------------------------------------------------- C-hook problem
+// The reference's Settings hooks forwarded to a user problem written against the C
+// structs of include/vx.h (tests/hooks/sin2_problem.c), so that the reference build and
+// the GPU path (vx_run_create_hooks) run the same user code.  The hooks see the Settings
+// as vx.h describes: taken after settingsOverride and refreshed once the Settings are
+// complete (main, after the constructor).
+#include "sin2_problem.h"
+
+static sin2_params HP;
+static vx_settings VIEW;
+
+template <class V>
+static void put_vec(const V &v, int32_t *n, double *out) {
+    *n = (int32_t)v.size();
+    for (size_t i = 0; i < v.size(); i++) out[i] = v[i];
+}
+static void settings_to_c(const Settings &s, vx_settings &c) {
+    std::memset(&c, 0, sizeof c);
+    c.dx = s.dx, c.time = s.time, c.minEfficiency = s.minEfficiency, c.preLength = s.preLength;
+    c.postLength = s.postLength, c.refinementCriteria = s.refinementCriteria, c.cfl = s.cfl;
+    c.sizeWeight = s.sizeWeight, c.plasma_xl_bound = s.plasma_xl_bound, c.plasma_xr_bound = s.plasma_xr_bound;
+    c.nspecies = (int32_t)s.m.size();
+    for (size_t i = 0; i < s.m.size(); i++) {
+        c.m[i] = s.m[i];
+        c.q[i] = s.q[i];
+        c.m_inv[i] = i < s.m_inv.size() ? s.m_inv[i] : 0.0;
+        c.dp[i] = s.dp[i];
+        c.fMax[i] = i < s.fMax.size() ? s.fMax[i] : 0.0;
+        c.pmin[i] = s.pmin[i];
+        put_vec(s.temp[i], &c.ntemp[i], c.temp[i]);
+        c.p_size[i] = s.p_size[i];
+        c.p_size_finest[i] = i < s.p_size_finest.size() ? s.p_size_finest[i] : 0;
+    }
+    put_vec(s.tempEM, &c.ntempEM, c.tempEM);
+    c.x_size_finest = s.x_size_finest, c.x_size = s.x_size, c.refinementRatio = s.refinementRatio;
+    c.maxDepth = s.maxDepth, c.quadratureDepth = s.quadratureDepth;
+}
+
+void initialConditions(Input &grid, Particles &particles, Output &output) {
+    vx_input g;
+    vx_particles p;
+    vx_output o;
+    std::memset(&g, 0, sizeof g);
+    std::memset(&p, 0, sizeof p);
+    g.minEfficiency = grid.minEfficiency, g.dx = grid.dx, g.k = grid.k;
+    g.refinementCriteria = grid.refinementCriteria, g.cfl = grid.cfl, g.sizeWeight = grid.sizeWeight;
+    g.preLength = grid.preLength, g.postLength = grid.postLength;
+    g.nx = grid.nx, g.r = grid.r, g.Lfinest = grid.Lfinest;
+    g.plasma_xl_bound = grid.plasma_xl_bound, g.plasma_xr_bound = grid.plasma_xr_bound;
+    put_vec(grid.tempEM, &g.ntempEM, g.tempEM);
+    p.nspecies = (int32_t)particles.mass.size();
+    for (int s = 0; s < p.nspecies; s++) {
+        p.mass[s] = particles.mass[s], p.charge[s] = particles.charge[s], p.np[s] = particles.np[s];
+        p.dp[s] = particles.dp[s], p.pmin[s] = particles.pmin[s];
+        put_vec(particles.misc[s], &p.nmisc[s], p.misc[s]);
+    }
+    o.time = output.time, o.rectangleData = output.rectangleData, o.charge = output.charge;
+    o.energy = output.energy, o.potential = output.potential, o.EFieldLongitudinal = output.EFieldLongitudinal;
+    o.EFieldTransverse = output.EFieldTransverse, o.BFieldTransverse = output.BFieldTransverse;
+    o.AFieldSquared = output.AFieldSquared, o.precision = output.precision;
+    sin2_initial_conditions(&HP, &g, &p, &o);
+    grid.minEfficiency = g.minEfficiency, grid.dx = g.dx, grid.k = g.k;
+    grid.refinementCriteria = g.refinementCriteria, grid.cfl = g.cfl, grid.sizeWeight = g.sizeWeight;
+    grid.preLength = g.preLength, grid.postLength = g.postLength;
+    grid.nx = g.nx, grid.r = g.r, grid.Lfinest = g.Lfinest;
+    grid.plasma_xl_bound = g.plasma_xl_bound, grid.plasma_xr_bound = g.plasma_xr_bound;
+    grid.tempEM.assign(g.tempEM, g.tempEM + g.ntempEM);
+    particles.mass.clear(), particles.charge.clear(), particles.np.clear();
+    particles.dp.clear(), particles.pmin.clear(), particles.misc.clear();
+    for (int s = 0; s < p.nspecies; s++) {
+        particles.mass.push_back(p.mass[s]);
+        particles.charge.push_back(p.charge[s]);
+        particles.np.push_back(p.np[s]);
+        particles.dp.push_back(p.dp[s]);
+        particles.pmin.push_back(p.pmin[s]);
+        particles.misc.push_back(std::vector<double>(p.misc[s], p.misc[s] + p.nmisc[s]));
+    }
+    output.time = o.time, output.rectangleData = o.rectangleData, output.charge = o.charge;
+    output.energy = o.energy, output.potential = o.potential, output.EFieldLongitudinal = o.EFieldLongitudinal;
+    output.EFieldTransverse = o.EFieldTransverse, output.BFieldTransverse = o.BFieldTransverse;
+    output.AFieldSquared = o.AFieldSquared, output.precision = o.precision;
+}
+
+void Settings::settingsOverride() {
+    settings_to_c(*this, VIEW);
+    sin2_settings_override(&HP, &VIEW);
+    dx = VIEW.dx, time = VIEW.time, minEfficiency = VIEW.minEfficiency, preLength = VIEW.preLength;
+    postLength = VIEW.postLength, refinementCriteria = VIEW.refinementCriteria, cfl = VIEW.cfl;
+    sizeWeight = VIEW.sizeWeight, plasma_xl_bound = VIEW.plasma_xl_bound, plasma_xr_bound = VIEW.plasma_xr_bound;
+    for (int i = 0; i < VIEW.nspecies; i++) {
+        m[i] = VIEW.m[i], q[i] = VIEW.q[i], dp[i] = VIEW.dp[i], pmin[i] = VIEW.pmin[i];
+        temp[i].assign(VIEW.temp[i], VIEW.temp[i] + VIEW.ntemp[i]);
+        p_size[i] = VIEW.p_size[i];
+    }
+    tempEM.assign(VIEW.tempEM, VIEW.tempEM + VIEW.ntempEM);
+    x_size = VIEW.x_size, refinementRatio = VIEW.refinementRatio;
+    maxDepth = VIEW.maxDepth, quadratureDepth = VIEW.quadratureDepth;
+    settings_to_c(*this, VIEW);
+}
+
+bool Settings::RefinementOverride(double x, double p, int depth, int particleType) {
+    return sin2_refinement_override(&HP, &VIEW, x, p, depth, particleType) != 0;
+}
+
+double Settings::GetBY(double x, double t) { return sin2_get_by(&HP, &VIEW, x, t); }
+
+double Settings::GetBZ(double x, double t) { return sin2_get_bz(&HP, &VIEW, x, t); }
+
+double Settings::InitialDistribution(double x, double p, int particleType) {
+    return sin2_initial_distribution(&HP, &VIEW, x, p, particleType);
+}
+#endif  // VX_HOOKS_PROBLEM
+
 bool LOUD = false, NOISY = false;
 
 // ---------------------------------------------------------------- state dump
@@ -287,6 +403,7 @@ int main(int argc, char **argv) {
     auto kv = parse_args(argc, argv);
     auto getd = [&](const char *k, double d) { return kv.count(k) ? std::stod(kv[k]) : d; };
     auto geti = [&](const char *k, long long d) { return kv.count(k) ? std::stoll(kv[k]) : d; };
+#ifndef VX_HOOKS_PROBLEM
     P.L = getd("L", P.L);
     P.nx = (unsigned)geti("nx", P.nx);
     P.np = (unsigned)geti("np", P.np);
@@ -316,6 +433,18 @@ int main(int argc, char **argv) {
     P.mi = getd("mi", P.mi);
     P.iTe = getd("iTe", P.iTe);
     P.ipmax = getd("ipmax", P.ipmax);
+#else
+    sin2_defaults(&HP);
+    HP.nx = (uint32_t)geti("nx", HP.nx);
+    HP.np = (uint32_t)geti("np", HP.np);
+    HP.Lfinest = (uint32_t)geti("levels", HP.Lfinest);
+    HP.L = getd("L", HP.L);
+    HP.pad = getd("pad", HP.pad);
+    HP.a0 = getd("a0", HP.a0);
+    HP.ramp = getd("ramp", HP.ramp);
+    HP.crit = getd("crit", HP.crit);
+    HP.minEff = getd("minEff", HP.minEff);
+#endif
     long long steps = geti("steps", 0);
     long long dump_every = geti("dump_every", 0);
     long long regrid_every = geti("regrid_every", 0);
@@ -323,7 +452,9 @@ int main(int argc, char **argv) {
     // diag_every=K: SolverManager::fileOutput and OutputRectangles at t = 0 and after every
     // K-th step, into output/ and output/rectangleData/ of the working directory.
     long long diag_every = geti("diag_every", 0);
+#ifndef VX_HOOKS_PROBLEM
     P.diag = diag_every > 0;
+#endif
     std::string dumpdir = kv.count("dumpdir") ? kv["dumpdir"] : "";
 
     Input grid;
@@ -334,6 +465,9 @@ int main(int argc, char **argv) {
     std::ostringstream sink;
     std::cout.rdbuf(sink.rdbuf());  // silence the banner and level table
     Settings settings(grid, particles, output);
+#ifdef VX_HOOKS_PROBLEM
+    settings_to_c(settings, VIEW);  // the Settings are complete (sizes, fMax)
+#endif
     auto t_init0 = std::chrono::steady_clock::now();
     SolverManager SM(settings);
     auto t_init1 = std::chrono::steady_clock::now();

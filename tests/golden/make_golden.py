@@ -58,6 +58,17 @@ CASES = {
 }
 
 
+# Cases of a user problem given through the C hooks (tests/hooks/sin2_problem.c), run by
+# the reference build linked behind its Settings hooks (oracle/_ref/veritas_ref_hooks):
+# two mobile species, vacuum pads of 5 cells, a circularly polarised sin^2-ramped laser
+# (both GetBY and GetBZ), a refinement window from RefinementOverride; args are the
+# problem's own keys (sin2_params).
+HOOK_CASES = {
+    "sin2hooks": (["nx=64", "np=32", "levels=2"], 3, [0, 1, 3]),
+}
+HOOK_REGRID = {"sin2hooks": 4}
+
+
 # name -> regrid interval for the regrid fixtures of that case: the state just before
 # SolverManager::reGrid ("_pre"), just after it ("_post") and one step later ("_post1").
 REGRID = {
@@ -134,6 +145,14 @@ def main() -> None:
             continue
         run_regrid(exe, name, CASES[name][0], every)
         print("wrote", name, "regrid")
+    exe_hooks = REPO / "oracle" / "_ref" / "veritas_ref_hooks"
+    for name, (args, steps, keep) in HOOK_CASES.items():
+        if a.only and name not in a.only:
+            continue
+        run_case(exe_hooks, name, args, steps, keep)
+        if name in HOOK_REGRID:
+            run_regrid(exe_hooks, name, args, HOOK_REGRID[name])
+        print("wrote", name, "(C hooks)")
     for name, (steps, every) in DIAG.items():
         if a.only and name not in a.only:
             continue

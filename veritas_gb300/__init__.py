@@ -60,6 +60,56 @@ class _RequestResult(ctypes.Structure):
     ]
 
 
+MAX_SPECIES = 8
+MAX_MISC = 8
+_D = ctypes.c_double
+_I = ctypes.c_int32
+_U = ctypes.c_uint32
+
+
+class VxInput(ctypes.Structure):
+    """vx_input (the reference's Input, Settings.hpp:4-11)."""
+    _fields_ = [("minEfficiency", _D), ("dx", _D), ("k", _D), ("refinementCriteria", _D), ("cfl", _D),
+                ("sizeWeight", _D), ("preLength", _D), ("postLength", _D), ("nx", _U), ("r", _U), ("Lfinest", _U),
+                ("plasma_xl_bound", _D), ("plasma_xr_bound", _D), ("ntempEM", _I), ("tempEM", _D * MAX_MISC)]
+
+
+class VxParticles(ctypes.Structure):
+    """vx_particles (the reference's Particles, Settings.hpp:13-20)."""
+    _fields_ = [("nspecies", _I), ("mass", _D * MAX_SPECIES), ("charge", _D * MAX_SPECIES), ("np", _U * MAX_SPECIES),
+                ("dp", _D * MAX_SPECIES), ("pmin", _D * MAX_SPECIES), ("nmisc", _I * MAX_SPECIES),
+                ("misc", (_D * MAX_MISC) * MAX_SPECIES)]
+
+
+class VxOutput(ctypes.Structure):
+    """vx_output (the reference's Output, Settings.hpp:22-33)."""
+    _fields_ = [(n, _I) for n in ("time", "rectangleData", "charge", "energy", "potential", "EFieldLongitudinal",
+                                  "EFieldTransverse", "BFieldTransverse", "AFieldSquared", "precision")]
+
+
+class VxSettings(ctypes.Structure):
+    """vx_settings (the reference's Settings, Settings.hpp:35-65)."""
+    _fields_ = [(n, _D) for n in ("dx", "time", "minEfficiency", "preLength", "postLength", "refinementCriteria",
+                                  "cfl", "sizeWeight", "plasma_xl_bound", "plasma_xr_bound")] + [
+        ("nspecies", _I), ("m", _D * MAX_SPECIES), ("q", _D * MAX_SPECIES), ("m_inv", _D * MAX_SPECIES),
+        ("dp", _D * MAX_SPECIES), ("fMax", _D * MAX_SPECIES), ("pmin", _D * MAX_SPECIES),
+        ("ntemp", _I * MAX_SPECIES), ("temp", (_D * MAX_MISC) * MAX_SPECIES), ("ntempEM", _I),
+        ("tempEM", _D * MAX_MISC), ("x_size_finest", _U), ("x_size", _U), ("refinementRatio", _U),
+        ("maxDepth", _I), ("quadratureDepth", _I), ("p_size", _U * MAX_SPECIES),
+        ("p_size_finest", _U * MAX_SPECIES)]
+
+
+class VxHooks(ctypes.Structure):
+    """vx_hooks: the user problem's callbacks (function pointers as void*)."""
+    _fields_ = [("user", ctypes.c_void_p), ("initial_conditions", ctypes.c_void_p),
+                ("settings_override", ctypes.c_void_p), ("initial_distribution", ctypes.c_void_p),
+                ("get_by", ctypes.c_void_p), ("get_bz", ctypes.c_void_p), ("refinement_override", ctypes.c_void_p)]
+
+
+# sub-step selection of vx_run_vlasov_stage
+SUB_FLUX, SUB_LIMIT, SUB_UPDATE, SUB_COPY, SUB_ALL = 0x1, 0x2, 0x4, 0x8, 0xF
+
+
 def _load() -> ctypes.CDLL:
     if not LIB_PATH.exists():
         raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'` first")
@@ -114,6 +164,16 @@ def _load() -> ctypes.CDLL:
         "vx_run_state_size": (ctypes.c_int, [vp, P(ctypes.c_int64)]),
         "vx_run_step_host": (ctypes.c_int, [vp, P(ctypes.c_double), P(ctypes.c_double), ctypes.c_double]),
         "vx_run_state_to_host": (ctypes.c_int, [vp, P(ctypes.c_double)]),
+        "vx_input_defaults": (None, [P(VxInput), P(VxParticles), P(VxOutput)]),
+        "vx_run_create_hooks": (ctypes.c_int, [vp, P(VxHooks), ctypes.c_int, ctypes.c_int, P(vp)]),
+        "vx_run_settings": (ctypes.c_int, [vp, P(VxSettings)]),
+        "vx_run_moments": (ctypes.c_int, [vp]),
+        "vx_run_poisson": (ctypes.c_int, [vp]),
+        "vx_run_vlasov_stage": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double, ctypes.c_uint]),
+        "vx_run_update_time": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double]),
+        "vx_run_maxwell_stage": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double]),
+        "vx_run_flag": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, P(ctypes.c_int32), ctypes.c_int,
+                                        P(ctypes.c_int)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -276,13 +336,58 @@ FIELD_IDS = {"By": 0, "Bz": 1, "Ey": 2, "Ez": 3, "Ay": 4, "Az": 5, "a_squared": 
 class SolverManager:
     """One independent solve on a context (the reference's SolverManager)."""
 
-    def __init__(self, ctx: Context, problem: Problem):
+    def __init__(self, ctx: Context, problem: Problem | None, *, hooks: VxHooks | None = None, precision: int = 64,
+                 poisson: int = 0):
+        """`problem`: the built-in laser / plasma-slab problem; or problem=None and `hooks`
+        (a user problem as C callbacks, vx_run_create_hooks) with its precision and
+        Poisson solver.  The hooks struct and whatever its pointers reference must outlive
+        the run."""
         self.ctx = ctx
         self.problem = problem
         h = ctypes.c_void_p()
-        _check(_lib.vx_run_create(ctx.handle, ctypes.byref(problem.to_c()), ctypes.byref(h)))
+        if problem is not None:
+            _check(_lib.vx_run_create(ctx.handle, ctypes.byref(problem.to_c()), ctypes.byref(h)))
+        else:
+            if hooks is None:
+                raise ValueError("give a problem or hooks")
+            self._hooks = hooks
+            _check(_lib.vx_run_create_hooks(ctx.handle, ctypes.byref(hooks), precision, poisson, ctypes.byref(h)))
         self._h = h
         ctx._runs.add(self)
+
+    # ---- per-class calls (EMFieldSolver / Mesh / Settings steps of one RK stage)
+    def moments(self) -> None:
+        """EMFieldSolver::AssembleRhoAndJ."""
+        _check(_lib.vx_run_moments(self._h))
+
+    def poisson(self) -> None:
+        """EMFieldSolver::UpdatePotential (phi, Ex0, E_x)."""
+        _check(_lib.vx_run_poisson(self._h))
+
+    def vlasov_stage(self, stage: int, dt: float, sub_mask: int = SUB_ALL) -> None:
+        """Mesh::Advance(dt, stage) for every species (sub_mask: SUB_* bits)."""
+        _check(_lib.vx_run_vlasov_stage(self._h, stage, float(dt), sub_mask))
+
+    def update_time(self, stage: int, dt: float) -> None:
+        """Settings::UpdateTime."""
+        _check(_lib.vx_run_update_time(self._h, stage, float(dt)))
+
+    def maxwell_stage(self, stage: int, dt: float) -> None:
+        """EMFieldSolver::RGKStep."""
+        _check(_lib.vx_run_maxwell_stage(self._h, stage, float(dt)))
+
+    def flag(self, species: int, depth: int) -> list[tuple[int, int]]:
+        """Mesh::getError of one level: the flagged (i, j) in the reference's order."""
+        cnt = ctypes.c_int()
+        _check(_lib.vx_run_flag(self._h, species, depth, None, 0, ctypes.byref(cnt)))
+        buf = (ctypes.c_int32 * max(2, 2 * cnt.value))()
+        _check(_lib.vx_run_flag(self._h, species, depth, buf, cnt.value, ctypes.byref(cnt)))
+        return [(buf[2 * k], buf[2 * k + 1]) for k in range(cnt.value)]
+
+    def settings(self) -> VxSettings:
+        out = VxSettings()
+        _check(_lib.vx_run_settings(self._h, ctypes.byref(out)))
+        return out
 
     @property
     def handle(self) -> ctypes.c_void_p:

@@ -2,45 +2,11 @@
 #include <cstring>
 #include <string>
 
-#include "../../include/vx.h"
-#include "engine.hpp"
-#include "serve.hpp"
+#include "capi_internal.hpp"
 
-struct vx_ctx {
-    std::unique_ptr<vx::Engine> eng;
-};
-struct vx_run {
-    vx_ctx *ctx;
-    std::unique_ptr<vx::Run> run;
-};
-struct vx_server {
-    vx_ctx *ctx;
-    std::unique_ptr<vx::Server> srv;
-};
+using vx::guard;
 
 namespace {
-thread_local std::string g_err;
-
-template <class F>
-int guard(F &&f) {
-    try {
-        f();
-        return VX_OK;
-    } catch (const vx::CudaError &e) {
-        g_err = e.what();
-        return VX_ERR_CUDA;
-    } catch (const std::invalid_argument &e) {
-        g_err = e.what();
-        return VX_ERR_INVALID;
-    } catch (const std::bad_alloc &e) {
-        g_err = e.what();
-        return VX_ERR_NOMEM;
-    } catch (const std::exception &e) {
-        g_err = e.what();
-        return VX_ERR_STATE;
-    }
-}
-
 vx::LaserSlabParams to_params(const vx_problem &p) {
     vx::LaserSlabParams q;
     q.lambda = p.lambda;
@@ -87,6 +53,7 @@ std::unique_ptr<vx::Settings> host_settings(const vx_problem &p) {
 }  // namespace
 
 namespace vx {
+thread_local std::string g_err;
 // Error message for entry points defined outside this file.
 void set_last_error(const std::string &msg) { g_err = msg; }
 }  // namespace vx
@@ -131,7 +98,7 @@ void vx_problem_defaults(vx_problem *p) {
     p->ipmax = d.ipmax;
 }
 
-const char *vx_last_error(void) { return g_err.c_str(); }
+const char *vx_last_error(void) { return vx::g_err.c_str(); }
 
 int vx_ctx_create(int device, vx_ctx **out) {
     if (!out) return VX_ERR_INVALID;

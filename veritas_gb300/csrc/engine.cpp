@@ -930,11 +930,14 @@ void Engine::build_set(LaunchSet &L) {
     sync();
 }
 
-// The kernel sequence of one full RK step (SolverManager.cpp:28-39 -> Mesh.cpp:64-89,
-// EMSolver.cpp:104-202) for every run of the set.
-void Engine::record_step(LaunchSet &L) {
-    int launches = 0;
-    FctLaunch fl{};
+// Launch descriptors of a set's step kernels (tables, tiles, fields, parameter blocks).
+StageLaunches Engine::stage_launches(LaunchSet &L) {
+    StageLaunches K{};
+    FctLaunch &fl = K.fl;
+    MomLaunch &ml = K.ml;
+    AsmLaunch &al = K.al;
+    PoissonLaunch &pl = K.pl;
+    MaxwellLaunch &mx = K.mx;
     fl.patches = L.dpatch.p;
     fl.tiles = L.dtiles.as<TileRef>();
     fl.ntiles = L.ntiles;
@@ -949,7 +952,6 @@ void Engine::record_step(LaunchSet &L) {
     fl.params32 = L.dparams32.as<float>();
     fl.use_f0 = 0;
     fl.stream = stream;
-    MomLaunch ml{};
     ml.patches = L.dpatch.p;
     ml.colpatch = L.dcolpatch.as<int>();
     ml.colidx = L.dcolidx.as<int>();
@@ -959,7 +961,6 @@ void Engine::record_step(LaunchSet &L) {
     ml.nruns = (int)L.runs.size();
     ml.maxnf = L.maxnf;
     ml.stream = stream;
-    AsmLaunch al{};
     al.patches = L.dpatch.p;
     al.lvl_ptr = L.dlvl_ptr.as<int>();
     al.lvl_off = L.dlvl_off.as<int>();
@@ -972,7 +973,6 @@ void Engine::record_step(LaunchSet &L) {
     al.pairs = L.precision == kF32 ? 1 : 0;
     al.fields = L.dfields.as<RunFields>();
     al.stream = stream;
-    PoissonLaunch pl{};
     pl.lu = L.dlu.as<LUDev>();
     pl.fields = L.dfields.as<RunFields>();
     pl.w = L.dw.as<double>();
@@ -980,7 +980,6 @@ void Engine::record_step(LaunchSet &L) {
     pl.nruns = (int)L.runs.size();
     pl.maxn = L.maxn;
     pl.stream = stream;
-    MaxwellLaunch mx{};
     mx.fields = L.dfields.as<RunFields>();
     mx.nruns = (int)L.runs.size();
     mx.maxnf = L.maxnf;
@@ -988,6 +987,19 @@ void Engine::record_step(LaunchSet &L) {
     mx.dxinv = L.ddxinv.as<double>();
     mx.f32 = L.precision == kF32;
     mx.stream = stream;
+    return K;
+}
+
+// The kernel sequence of one full RK step (SolverManager.cpp:28-39 -> Mesh.cpp:64-89,
+// EMSolver.cpp:104-202) for every run of the set.
+void Engine::record_step(LaunchSet &L) {
+    int launches = 0;
+    StageLaunches K = stage_launches(L);
+    FctLaunch &fl = K.fl;
+    MomLaunch &ml = K.ml;
+    AsmLaunch &al = K.al;
+    PoissonLaunch &pl = K.pl;
+    MaxwellLaunch &mx = K.mx;
     for (int s = 0; s < 6; s++) {
         // FP32 copies of the fields: E_x's comes with each solve (k_efield), the per-cell
         // A^2 the moments read with each Maxwell stage for the next one (the step's first
@@ -1076,6 +1088,32 @@ void Engine::record_step(LaunchSet &L) {
     launches_per_step_ = launches;
 }
 
+// The dt-scaled weights of RK stage st: FCT [0..5] and their left-to-right sum [6] (as
+// Rectangle.cpp:1396-1517 forms aSum), Maxwell [8..13] (EMSolver.cpp:204-338, the last
+// stage with b - a_4).  The laser entries [16], [17] are left to the caller.
+static void stage_weights(double *p, int st, double timestep) {
+    for (int k = 0; k < kParamStride; k++) p[k] = 0.0;
+    if (st < 5) {
+        for (int k = 0; k <= st; k++) p[k] = kRK[st][k] * timestep;
+        double sum = p[0];
+        for (int k = 1; k <= st; k++) sum = sum + p[k];
+        p[6] = sum;
+    } else {
+        for (int k = 0; k < 6; k++) p[k] = kRK[5][k] * timestep;
+        double sum = p[0];
+        for (int k = 1; k < 6; k++) sum = sum + p[k];
+        p[6] = sum;
+    }
+    if (st < 5) {
+        for (int k = 0; k <= st; k++) p[8 + k] = kRK[st][k] * timestep;
+    } else {
+        double a[6];
+        for (int k = 0; k < 5; k++) a[k] = kRK[4][k] * timestep;
+        a[5] = 0;
+        for (int k = 0; k < 6; k++) p[8 + k] = kRK[5][k] * timestep - a[k];
+    }
+}
+
 // Host-side stage parameters (dt-scaled tableau, laser boundary values) of one step of
 // every run of the set; advances each run's time through Settings::UpdateTime.
 void Engine::fill_params(LaunchSet &L, const std::vector<Run *> &set, const std::vector<double> &dt) {
@@ -1085,31 +1123,7 @@ void Engine::fill_params(LaunchSet &L, const std::vector<Run *> &set, const std:
         double timestep = dt[ri];
         for (int st = 0; st < 6; st++) {
             double *p = &L.hparams[param_base((int)ri, st)];
-            for (int k = 0; k < kParamStride; k++) p[k] = 0.0;
-            if (st < 5) {
-                double sum = 0.0;
-                for (int k = 0; k <= st; k++) {
-                    p[k] = kRK[st][k] * timestep;
-                }
-                // aSum exactly as written in Rectangle.cpp (left-to-right sum of products)
-                sum = p[0];
-                for (int k = 1; k <= st; k++) sum = sum + p[k];
-                p[6] = sum;
-            } else {
-                for (int k = 0; k < 6; k++) p[k] = kRK[5][k] * timestep;
-                double sum = p[0];
-                for (int k = 1; k < 6; k++) sum = sum + p[k];
-                p[6] = sum;
-            }
-            // Maxwell weights (EMSolver.cpp:204-338)
-            if (st < 5) {
-                for (int k = 0; k <= st; k++) p[8 + k] = kRK[st][k] * timestep;
-            } else {
-                double a[6];
-                for (int k = 0; k < 5; k++) a[k] = kRK[4][k] * timestep;
-                a[5] = 0;
-                for (int k = 0; k < 6; k++) p[8 + k] = kRK[5][k] * timestep - a[k];
-            }
+            stage_weights(p, st, timestep);
             s.UpdateTime(st, timestep);
             p[16] = s.GetBY(0, s.time);
             p[17] = s.GetBZ(0, s.time);
@@ -1122,6 +1136,92 @@ void Engine::fill_params(LaunchSet &L, const std::vector<Run *> &set, const std:
         VX_CUDA(cudaMemcpyAsync(L.dparams32.p, L.hparams32.data(), L.hparams32.size() * sizeof(float),
                                 cudaMemcpyHostToDevice, stream));
     }
+}
+
+// Selected phases of RK stage s of one run, launched one after another on the context
+// stream (no graph, no side stream): the per-class entry points.  The kernels and their
+// order are those of record_step, so a step composed of these calls in the reference's
+// order (SolverManager.cpp:28-39) gives the same bits as Engine::advance.
+void Engine::run_phases(Run &run, int s, double dt, unsigned phases) {
+    if (s < 0 || s > 5) throw std::invalid_argument("stage must be in 0..5");
+    LaunchSet &L = get_set({&run});
+    if (phases & (kPhSub0 | kPhMaxwell)) {
+        double *p = &L.hparams[param_base(0, s)];
+        stage_weights(p, s, dt);
+        p[16] = run.S->GetBY(0, run.S->time);
+        p[17] = run.S->GetBZ(0, run.S->time);
+        VX_CUDA(cudaMemcpyAsync(L.dparams.as<double>() + param_base(0, s), p, kParamStride * sizeof(double),
+                                cudaMemcpyHostToDevice, stream));
+        if (L.precision == kF32) {
+            float *q = &L.hparams32[param_base(0, s)];
+            for (int k = 0; k < kParamStride; k++) q[k] = (float)p[k];
+            VX_CUDA(cudaMemcpyAsync(L.dparams32.as<float>() + param_base(0, s), q, kParamStride * sizeof(float),
+                                    cudaMemcpyHostToDevice, stream));
+        }
+        // the host copies are read by the asynchronous uploads; keep them until done
+        sync();
+    }
+    StageLaunches K = stage_launches(L);
+    FctLaunch &fl = K.fl;
+    fl.step = s;
+    int launches = 0;
+    if (phases & kPhMoments) {  // EMFieldSolver::AssembleRhoAndJ
+        K.ml.acell = 1;
+        run_moments(L, K.ml);
+        launch_assemble(K.al);
+        launches += (L.precision == kF32) ? 3 : 2;
+    }
+    if (phases & kPhPoisson) {  // EMFieldSolver::UpdatePotential and E_x
+        run_poisson(L, K.pl);
+        launches += 1;
+    }
+    if (phases & kPhSub0) {  // Level::FCTTimeStep(dt, s, 0) coarsest first, incl. interface fluxes
+        if (L.precision == kF32) {
+            fct_sub(L, fl, kSubXFlux);
+            fct_sub(L, fl, kSubPFlux);
+            launches += 2;
+        } else {
+            fct_sub(L, fl, kSubGamma);
+            fl.part = 0;
+            fct_sub(L, fl, kSubFaces);
+            fct_sub(L, fl, kSubFlux);
+            launches += 3;
+        }
+        for (size_t b = 0; b + 1 < L.iface_ptr.size(); b++, launches++)
+            launch_iface(L.dpatch.p, L.diface.as<IfaceOp>() + L.iface_ptr[b], L.iface_ptr[b + 1] - L.iface_ptr[b], s,
+                         L.precision, stream);
+        fct_sub(L, fl, kSubDsF2);
+        launches += 1;
+    }
+    if (phases & kPhSub1) {  // PushData(2), FCTTimeStep(.., 1), PushBoundaryC
+        for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
+            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 2,
+                         L.precision, stream);
+        fct_sub(L, fl, kSubLimR);
+        fct_sub(L, fl, kSubLimC);
+        launches += 2;
+        for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++, launches++)
+            launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b],
+                         L.precision, stream);
+    }
+    if (phases & kPhSub2) {  // FCTTimeStep(.., 2), PushData(1)
+        fct_sub(L, fl, kSubUpdate);
+        launches += 1;
+        for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
+            launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1,
+                         L.precision, stream);
+    }
+    if ((phases & kPhSub3) && s == 5) {  // FCTTimeStep(.., 3): Mesh::Advance runs it at the last stage only
+        fct_sub(L, fl, kSubCopy10);
+        launches += 1;
+    }
+    if (phases & kPhMaxwell) {  // EMFieldSolver::RGKStep
+        K.mx.step = s;
+        launch_maxwell(K.mx);
+        launches += 3;
+    }
+    kernel_launches += launches;
+    VX_CUDA(cudaGetLastError());
 }
 
 void Engine::advance(const std::vector<Run *> &set, const std::vector<double> &dt) {

@@ -209,6 +209,26 @@ struct LaunchSet {
     ~LaunchSet();
 };
 
+// Launch descriptors of one set's step kernels (Engine::stage_launches).
+struct StageLaunches {
+    FctLaunch fl;
+    MomLaunch ml;
+    AsmLaunch al;
+    PoissonLaunch pl;
+    MaxwellLaunch mx;
+};
+
+// Phases of one RK stage for Engine::run_phases (the per-class entry points).
+enum StagePhase : unsigned {
+    kPhMoments = 1u,   // EMFieldSolver::AssembleRhoAndJ
+    kPhPoisson = 2u,   // EMFieldSolver::UpdatePotential (+ E_x)
+    kPhSub0 = 4u,      // Mesh::Advance sub-step 0 (fluxes, interface fluxes, low-order f)
+    kPhSub1 = 8u,      // PushData(2), sub-step 1 (limiter), PushBoundaryC
+    kPhSub2 = 16u,     // sub-step 2 (antidiffusive update), PushData(1)
+    kPhSub3 = 32u,     // sub-step 3 (f0 = f1; stage 5 only)
+    kPhMaxwell = 64u,  // EMFieldSolver::RGKStep
+};
+
 class Engine {
 public:
     explicit Engine(int device);
@@ -225,6 +245,7 @@ public:
     void advance(const std::vector<Run *> &set, const std::vector<double> &dt);
     void advance_fields(const std::vector<Run *> &set, const std::vector<double> &dt);
     void fill_params(LaunchSet &L, const std::vector<Run *> &set, const std::vector<double> &dt);
+    void run_phases(Run &run, int stage, double dt, unsigned phases);
     std::vector<double> calculate_dt(const std::vector<Run *> &set);
     void moments_only(const std::vector<Run *> &set);
     void refresh_efield(Run &run);
@@ -254,6 +275,7 @@ private:
     void build_set(LaunchSet &L);
     void build_tiles(LaunchSet &L);
     void record_step(LaunchSet &L);
+    StageLaunches stage_launches(LaunchSet &L);
     int launches_per_step_ = 0;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
     DevBuf flush_;

@@ -46,6 +46,7 @@ Settings::Settings(const Input &grid, const Particles &particles, const Output &
     for (double mm : m) m_inv.push_back(1 / mm);
     fMax.resize(q.size(), 0.0);
     DetermineMaximum();
+    problem->settingsComplete(*this);
 }
 
 double Settings::GetDp(int level, int particleType) const {

@@ -50,6 +50,8 @@ public:
     virtual double GetBZ(const Settings &s, double x, double t) const = 0;
     virtual bool RefinementOverride(const Settings &s, double x, double p, int depth, int particleType) const = 0;
     virtual bool HasRefinementOverride() const { return true; }
+    // Called at the end of the Settings constructor (derived sizes and fMax known).
+    virtual void settingsComplete(const Settings &) {}
     // Optional: f(x, p) = density(x) * profile(p).  A problem that says so lets the FP32
     // form integrate the initial cell averages as a product of two 1-D quadratures.
     virtual bool Separable() const { return false; }
