@@ -370,18 +370,33 @@ int vx_cfl_bound_noalloc(const double *Ay, const double *Az, const double *By, c
 /* ---------------------------------------------------------------- serving loop
  * No reference counterpart (the reference runs one solve per process): continuous
  * batching of independent solves on one context under a device-memory budget.
- * submit() queues a solve of `steps` RK steps (arrival on the server's clock, seconds);
- * step() admits, in arrival order, the waiting solves that fit in the budget, advances
- * every live solve one step in one batched launch set and retires the finished ones
- * (writing their final state to state_path when one was given). */
+ * submit() queues a solve of `steps` RK steps (arrival on the server's clock, seconds;
+ * a request larger than the whole budget is refused with VX_ERR_INVALID); step() binds
+ * the runs its builder thread has finished, admits in arrival order the waiting solves
+ * that fit in the budget (their runs are built on that thread while the batch keeps
+ * stepping), advances every live solve one step in one batched launch set, regrids by
+ * the reference driver's rule, and retires the finished ones (writing their final state
+ * to state_path when one was given) and the failed ones: a solve whose CFL bound or E_x0
+ * is not finite after a step (something in it went non-finite) is retired alone with
+ * VX_REQ_FAILED. */
 typedef struct vx_server vx_server;
+#define VX_REQ_WAITING 0    /* queued for device memory */
+#define VX_REQ_BUILDING 1   /* admitted; its run is being built on the server's builder thread */
+#define VX_REQ_LIVE 2       /* stepping with the batch */
+#define VX_REQ_DONE 3       /* all steps taken (state written if asked) */
+#define VX_REQ_CANCELLED 4  /* withdrawn by vx_server_cancel */
+#define VX_REQ_FAILED 5     /* build failed, or its fields went non-finite (error says which) */
 typedef struct vx_request_result {
-    int32_t finished;
+    int32_t finished;                 /* 1 once the request is over (done, cancelled or failed) */
     int64_t steps_done;
     double arrival, admitted, finish; /* server clock, seconds; -1 until reached */
     double sim_time;                  /* simulated time at the end of the solve */
     int64_t cells;                    /* phase-space cells of the final hierarchy */
     uint64_t device_bytes;            /* device memory the solve held */
+    int32_t status;                   /* VX_REQ_* */
+    int32_t regrids;                  /* regrids taken during the solve */
+    double bound;                     /* server clock when its built run joined the batch; -1 until then */
+    char error[192];                  /* why it failed (empty otherwise) */
 } vx_request_result;
 int vx_server_create(vx_ctx *ctx, uint64_t hbm_budget_bytes, int max_live, vx_server **out);
 int vx_server_destroy(vx_server *s);
@@ -390,6 +405,15 @@ int vx_server_submit(vx_server *s, const vx_problem *p, int64_t steps, double ar
                      int64_t *id);
 int vx_server_step(vx_server *s, int *live, int *waiting);
 int vx_server_result(vx_server *s, int64_t id, vx_request_result *out);
+/* Withdraws a request that is not over: a waiting one leaves the queue, one being built is
+ * dropped when its build ends, a live one is retired at once (no state written). */
+int vx_server_cancel(vx_server *s, int64_t id);
+/* Regridding of served solves: enable != 0 applies the reference driver's rule
+ * (veritas.cpp:146-151: SolverManager::reGrid when more than 20 steps have passed since
+ * the last one, once the time before the step exceeds after_s seconds; the reference's
+ * demo switches its plasma on at 3 laser periods, served solves at t = 0, so the default
+ * is 0).  On by default. */
+int vx_server_set_regrid(vx_server *s, int enable, double after_s);
 
 #ifdef __cplusplus
 }

@@ -64,7 +64,8 @@ def test_served_result_same_alone_and_in_mix(ctx, tmp_path, precision):
 
     srv = Server(ctx, 8 << 30)
     ry = srv.submit(Y, 4)
-    srv.step()  # Y runs alone for one step
+    while srv.result(ry)["steps_done"] == 0:  # Y runs alone for a step
+        srv.step()
     rx = srv.submit(X, 3, state_path=tmp_path / "mix.bin")  # joins while Y is live
     rz = srv.submit(Z, 2)
     while srv.step() != (0, 0):
@@ -84,7 +85,8 @@ def test_server_admits_by_memory_budget(ctx):
     P = problem_for("slab64")
     srv = Server(ctx, 1 << 30)
     a = srv.submit(P, 2)
-    srv.step()
+    while srv.result(a)["device_bytes"] == 0:  # built on the server's thread, then bound
+        srv.step()
     used = srv.result(a)["device_bytes"]
     srv.close()
     srv = Server(ctx, int(used * 1.5))
@@ -136,3 +138,118 @@ def test_launch_mode_changes_nothing(ctx, tmp_path, precision):
         s.close()
     ctx.set_launch_mode(graphs=True, pdl=True)
     assert out[0] == out[1] == out[2]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [64, 32])
+def test_served_solve_regrids_and_is_the_same_alone_and_in_mix(ctx, tmp_path, precision):
+    """A served solve of 25 steps regrids after step 22 (the reference driver's rule:
+    more than 20 steps since the last regrid); its final state is the same alone as in a
+    mix with solves that join, regrid and retire around it, and equals a plain run that
+    regrids at the same step."""
+    from veritas_gb300 import Server, SolverManager
+
+    X = dataclasses.replace(problem_for("beam2"), precision=precision)
+    Y = dataclasses.replace(problem_for("amr2"), precision=precision)
+    Z = dataclasses.replace(problem_for("ions2"), precision=precision)
+    srv = Server(ctx, 8 << 30)
+    rid = srv.submit(X, 25, state_path=tmp_path / "alone.bin")
+    while srv.step() != (0, 0):
+        pass
+    r = srv.result(rid)
+    assert r["status"] == 3 and r["regrids"] == 1 and r["steps_done"] == 25
+    srv.close()
+
+    srv = Server(ctx, 8 << 30)
+    ry = srv.submit(Y, 30)
+    while srv.result(ry)["steps_done"] < 5:
+        srv.step()
+    rx = srv.submit(X, 25, state_path=tmp_path / "mix.bin")
+    rz = srv.submit(Z, 12)
+    while srv.step() != (0, 0):
+        pass
+    assert [srv.result(k)["status"] for k in (rx, ry, rz)] == [3, 3, 3]
+    assert srv.result(ry)["regrids"] == 1
+    assert (tmp_path / "alone.bin").read_bytes() == (tmp_path / "mix.bin").read_bytes()
+    srv.close()
+
+    s = SolverManager(ctx, X)
+    for k in range(25):
+        s.Advance(s.CalculateDt())
+        if k + 1 == 22:
+            s.reGrid()
+    assert _bytes(s, tmp_path / "plain.bin") == (tmp_path / "alone.bin").read_bytes()
+    s.close()
+
+
+@pytest.mark.gpu
+def test_server_cancels_waiting_and_live_requests(ctx, tmp_path):
+    """Cancelling a waiting request removes it from the queue; cancelling a live one
+    retires it at once without writing its state; the others finish unaffected."""
+    from veritas_gb300 import REQ_CANCELLED, REQ_DONE, Server
+
+    P = problem_for("amr2")
+    srv = Server(ctx, 8 << 30)
+    keep = srv.submit(P, 6, state_path=tmp_path / "keep_alone.bin")
+    while srv.step() != (0, 0):
+        pass
+    srv.close()
+
+    srv = Server(ctx, 8 << 30, max_live=2)
+    a = srv.submit(P, 6, state_path=tmp_path / "keep_mix.bin")
+    b = srv.submit(problem_for("drift128"), 50, state_path=tmp_path / "never.bin")
+    c = srv.submit(problem_for("slab64"), 4)  # waits: max_live is 2
+    while srv.result(b)["steps_done"] < 2:
+        srv.step()
+    assert srv.result(c)["status"] == 0
+    srv.cancel(c)
+    srv.cancel(b)
+    while srv.step() != (0, 0):
+        pass
+    ra, rb, rc = srv.result(a), srv.result(b), srv.result(c)
+    assert ra["status"] == REQ_DONE and rb["status"] == REQ_CANCELLED and rc["status"] == REQ_CANCELLED
+    assert rb["finished"] == 1 and 2 <= rb["steps_done"] < 50 and rc["steps_done"] == 0
+    assert not (tmp_path / "never.bin").exists()
+    assert (tmp_path / "keep_alone.bin").read_bytes() == (tmp_path / "keep_mix.bin").read_bytes()
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_server_retires_a_solve_gone_non_finite_alone(ctx, tmp_path):
+    """A request whose laser amplitude is NaN (a bad host-side input) fails its health
+    check after its first step and is retired alone; the solve stepping beside it in the
+    same launches finishes with the same bits as alone."""
+    from veritas_gb300 import REQ_DONE, REQ_FAILED, Server
+
+    P = problem_for("amr2")
+    bad = dataclasses.replace(problem_for("slab64"), a0=float("nan"))
+    srv = Server(ctx, 8 << 30)
+    srv.submit(P, 4, state_path=tmp_path / "alone.bin")
+    while srv.step() != (0, 0):
+        pass
+    srv.close()
+    srv = Server(ctx, 8 << 30)
+    g = srv.submit(P, 4, state_path=tmp_path / "mix.bin")
+    b = srv.submit(bad, 4)
+    while srv.step() != (0, 0):
+        pass
+    rg, rb = srv.result(g), srv.result(b)
+    assert rg["status"] == REQ_DONE
+    assert rb["status"] == REQ_FAILED and "not finite" in rb["error"] and rb["steps_done"] <= 1
+    assert (tmp_path / "alone.bin").read_bytes() == (tmp_path / "mix.bin").read_bytes()
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_server_refuses_a_request_larger_than_its_budget(ctx):
+    from veritas_gb300 import Problem, Server, VxError
+
+    srv = Server(ctx, 64 << 20)
+    with pytest.raises(VxError) as e:
+        srv.submit(Problem(nx=16384, np=1024, Lfinest=3), 10)
+    assert e.value.code == -1 and "larger than the whole memory budget" in str(e.value)
+    ok = srv.submit(problem_for("slab64"), 1)
+    while srv.step() != (0, 0):
+        pass
+    assert srv.result(ok)["status"] == 3
+    srv.close()

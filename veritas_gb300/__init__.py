@@ -56,8 +56,13 @@ class _RequestResult(ctypes.Structure):
     _fields_ = [
         ("finished", ctypes.c_int32), ("steps_done", ctypes.c_int64), ("arrival", ctypes.c_double),
         ("admitted", ctypes.c_double), ("finish", ctypes.c_double), ("sim_time", ctypes.c_double),
-        ("cells", ctypes.c_int64), ("device_bytes", ctypes.c_uint64),
+        ("cells", ctypes.c_int64), ("device_bytes", ctypes.c_uint64), ("status", ctypes.c_int32),
+        ("regrids", ctypes.c_int32), ("bound", ctypes.c_double), ("error", ctypes.c_char * 192),
     ]
+
+
+# request states of the serving loop (VX_REQ_*)
+REQ_WAITING, REQ_BUILDING, REQ_LIVE, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(6)
 
 
 MAX_SPECIES = 8
@@ -138,6 +143,8 @@ def _load() -> ctypes.CDLL:
                                              P(ctypes.c_int64)]),
         "vx_server_step": (ctypes.c_int, [vp, P(ctypes.c_int), P(ctypes.c_int)]),
         "vx_server_result": (ctypes.c_int, [vp, ctypes.c_int64, P(_RequestResult)]),
+        "vx_server_cancel": (ctypes.c_int, [vp, ctypes.c_int64]),
+        "vx_server_set_regrid": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double]),
         "vx_run_advance_fields": (ctypes.c_int, [vp, ctypes.c_double]),
         "vx_run_regrid": (ctypes.c_int, [vp]),
         "vx_error_weights": (ctypes.c_int, [P(_Problem), ctypes.c_int, ctypes.c_int, P(ctypes.c_double),
@@ -581,7 +588,16 @@ class Server:
     def result(self, rid: int) -> dict:
         r = _RequestResult()
         _check(_lib.vx_server_result(self._h, rid, ctypes.byref(r)))
-        return {k: getattr(r, k) for k, _ in r._fields_}
+        out = {k: getattr(r, k) for k, _ in r._fields_}
+        out["error"] = r.error.decode()
+        return out
+
+    def cancel(self, rid: int) -> None:
+        _check(_lib.vx_server_cancel(self._h, rid))
+
+    def set_regrid(self, enable: bool = True, after_s: float = 0.0) -> None:
+        """The reference driver's regrid rule for every solve (on by default)."""
+        _check(_lib.vx_server_set_regrid(self._h, int(enable), float(after_s)))
 
     def close(self) -> None:
         if self._h:

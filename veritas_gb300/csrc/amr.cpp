@@ -608,9 +608,9 @@ void Run::build_amr() {
     }
     sort_by_batch(csync_ops, cs.batch, cs.nbatches, csync_b);
     validate_ops();
-    dghost_ops = upload(ghost_ops, eng.stream);
-    diface_ops = upload(iface_ops, eng.stream);
-    dcsync_ops = upload(csync_ops, eng.stream);
+    dghost_ops = upload(ghost_ops, eng->stream);
+    diface_ops = upload(iface_ops, eng->stream);
+    dcsync_ops = upload(csync_ops, eng->stream);
     lap("csync ops");
 
     // ------------------------------------------------------------ device masks, weights

@@ -369,7 +369,7 @@ int vx_run_get_field(vx_run *run, int which, double *out, int64_t *len) {
         }
         *len = n;
         if (out) {
-            R.eng.sync();
+            R.eng->sync();
             VX_CUDA(cudaMemcpy(out, src, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
         }
     });
@@ -478,7 +478,10 @@ int vx_server_result(vx_server *s, int64_t id, vx_request_result *out) {
     if (!s || !out) return VX_ERR_INVALID;
     return guard([&] {
         const auto &r = s->srv->request(id);
-        out->finished = r.finished ? 1 : 0;
+        std::memset(out, 0, sizeof *out);
+        const bool over = r.status == vx::Server::kDone || r.status == vx::Server::kCancelled ||
+                          r.status == vx::Server::kFailed;
+        out->finished = over ? 1 : 0;
         out->steps_done = r.done_steps;
         out->arrival = r.arrival;
         out->admitted = r.admitted;
@@ -486,7 +489,23 @@ int vx_server_result(vx_server *s, int64_t id, vx_request_result *out) {
         out->sim_time = r.sim_time;
         out->cells = r.cells;
         out->device_bytes = r.bytes;
+        out->status = (int32_t)r.status;
+        out->regrids = r.regrids;
+        out->bound = r.bound;
+        std::strncpy(out->error, r.error.c_str(), sizeof out->error - 1);
     });
+}
+
+int vx_server_cancel(vx_server *s, int64_t id) {
+    if (!s) return VX_ERR_INVALID;
+    return guard([&] { s->srv->cancel(id); });
+}
+
+int vx_server_set_regrid(vx_server *s, int enable, double after_s) {
+    if (!s || !(after_s >= 0)) return VX_ERR_INVALID;
+    s->srv->regrid_enabled = enable != 0;
+    s->srv->regrid_after = after_s;
+    return VX_OK;
 }
 
 }  // extern "C"

@@ -20,10 +20,11 @@ void cuda_check(cudaError_t e, const char *what) {
 DevBuf::DevBuf(size_t b) : bytes(b) {
     if (b) {
         VX_CUDA(cudaMalloc(&p, b));
-        // Zero-fill and wait: later uploads run on a non-blocking stream that is not
-        // ordered after work on the legacy default stream.
-        VX_CUDA(cudaMemset(p, 0, b));
-        VX_CUDA(cudaDeviceSynchronize());
+        // Zero-fill and wait for it: later uploads run on a non-blocking stream that is
+        // not ordered after the legacy default stream.  Only the legacy stream is waited
+        // for, so a run built on one thread does not wait for steps running on another.
+        VX_CUDA(cudaMemsetAsync(p, 0, b, cudaStreamLegacy));
+        VX_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
     }
 }
 DevBuf::~DevBuf() {
@@ -43,7 +44,7 @@ DevBuf &DevBuf::operator=(DevBuf &&o) noexcept {
 // ---------------------------------------------------------------- Run
 static_assert(sizeof(PatchT<float>) == sizeof(PatchT<double>), "descriptor layouts must match");
 
-Run::Run(Engine &e, std::shared_ptr<Problem> prob, int prec) : eng(e), precision(prec) {
+Run::Run(Engine &e, std::shared_ptr<Problem> prob, int prec) : eng(&e), precision(prec) {
     if (prec != kF64 && prec != kF32) throw std::invalid_argument("precision must be 64 or 32");
     Input grid;
     Particles particles;
@@ -72,9 +73,17 @@ Run::Run(Engine &e, std::shared_ptr<Problem> prob, int prec) : eng(e), precision
 }
 
 Run::~Run() {
-    auto &v = eng.runs;
+    auto &v = eng->runs;
     v.erase(std::remove(v.begin(), v.end(), this), v.end());
-    eng.forget(this);
+    eng->forget(this);
+}
+
+void Run::migrate(Engine &to) {
+    if (to.device != eng->device) throw std::invalid_argument("a run moves only between engines of one device");
+    eng->forget(this);
+    auto &v = eng->runs;
+    v.erase(std::remove(v.begin(), v.end(), this), v.end());
+    eng = &to;
 }
 
 long long Run::cell_count() const {
@@ -208,10 +217,31 @@ void Run::init_rect_distribution(Rect &r) {
                 dp_sum[j] += s.problem->Profile(s, pmin + dp * ((0.5 + l) / nvals + j + r.p_pos), r.species);
         // the product on the device (the planes of a new patch are zero: ghosts stay 0)
         const double inv = 1 / std::pow(nvals, 2.0);
-        DevBuf dxs = upload(dx_sum, eng.stream), dps = upload(dp_sum, eng.stream);
+        DevBuf dxs = upload(dx_sum, eng->stream), dps = upload(dp_sum, eng->stream);
         launch_fill_separable((float *)r.desc.f0, (float *)r.desc.f1, r.pitch, r.n_x, r.n_p, dxs.as<double>(),
-                              dps.as<double>(), inv, fnorm[r.species], eng.stream);
-        VX_CUDA(cudaStreamSynchronize(eng.stream));
+                              dps.as<double>(), inv, fnorm[r.species], eng->stream);
+        VX_CUDA(cudaStreamSynchronize(eng->stream));
+        return;
+    }
+    const int terms = precision == kF64 ? s.problem->ProductTerms(r.species) : 0;
+    if (terms > 0) {
+        // the hook's factors at every sample point on the host, the double sum on the device
+        std::vector<double> X((size_t)terms * r.n_x * nvals), Pf((size_t)terms * r.n_p * nvals), C(terms);
+        for (int t = 0; t < terms; t++) {
+            C[t] = s.problem->Divisor(s, t, r.species);
+            for (int i = 0; i < r.n_x; i++)
+                for (int k = 0; k < nvals; k++)
+                    X[((size_t)t * r.n_x + i) * nvals + k] =
+                        s.problem->XFactor(s, t, ((0.5 + k) / nvals + i + r.x_pos) * dx, r.species);
+            for (int j = 0; j < r.n_p; j++)
+                for (int l = 0; l < nvals; l++)
+                    Pf[((size_t)t * r.n_p + j) * nvals + l] =
+                        s.problem->PFactor(s, t, pmin + dp * ((0.5 + l) / nvals + j + r.p_pos), r.species);
+        }
+        DevBuf dX = upload(X, eng->stream), dP = upload(Pf, eng->stream), dC = upload(C, eng->stream);
+        launch_quadrature64((double *)r.desc.f0, (double *)r.desc.f1, r.pitch, r.n_x, r.n_p, nvals, terms,
+                            dX.as<double>(), dP.as<double>(), dC.as<double>(), 1 / std::pow(nvals, 2.0), eng->stream);
+        VX_CUDA(cudaStreamSynchronize(eng->stream));
         return;
     }
     std::vector<double> host((size_t)(r.n_x + 4) * r.pitch, 0.0);
@@ -239,15 +269,15 @@ void Run::init_rect_distribution(Rect &r) {
         std::vector<float> h32(host.size());
         const double fn = fnorm[r.species];
         for (size_t q = 0; q < host.size(); q++) h32[q] = (float)(host[q] * fn);
-        VX_CUDA(cudaMemcpyAsync(r.desc.f0, h32.data(), r.plane_bytes(), cudaMemcpyHostToDevice, eng.stream));
-        VX_CUDA(cudaMemcpyAsync(r.desc.f1, h32.data(), r.plane_bytes(), cudaMemcpyHostToDevice, eng.stream));
-        VX_CUDA(cudaStreamSynchronize(eng.stream));
+        VX_CUDA(cudaMemcpyAsync(r.desc.f0, h32.data(), r.plane_bytes(), cudaMemcpyHostToDevice, eng->stream));
+        VX_CUDA(cudaMemcpyAsync(r.desc.f1, h32.data(), r.plane_bytes(), cudaMemcpyHostToDevice, eng->stream));
+        VX_CUDA(cudaStreamSynchronize(eng->stream));
         return;
     }
     size_t bytes = host.size() * sizeof(double);
-    VX_CUDA(cudaMemcpyAsync(r.desc.f0, host.data(), bytes, cudaMemcpyHostToDevice, eng.stream));
-    VX_CUDA(cudaMemcpyAsync(r.desc.f1, host.data(), bytes, cudaMemcpyHostToDevice, eng.stream));
-    VX_CUDA(cudaStreamSynchronize(eng.stream));
+    VX_CUDA(cudaMemcpyAsync(r.desc.f0, host.data(), bytes, cudaMemcpyHostToDevice, eng->stream));
+    VX_CUDA(cudaMemcpyAsync(r.desc.f1, host.data(), bytes, cudaMemcpyHostToDevice, eng->stream));
+    VX_CUDA(cudaStreamSynchronize(eng->stream));
 }
 
 void Run::alloc_fields() {
@@ -298,7 +328,7 @@ void Run::alloc_fields() {
 }
 
 void Run::upload_lu() {
-    cudaStream_t st = eng.stream;
+    cudaStream_t st = eng->stream;
     auto Lb = lu.lower_band();
     auto Ub = lu.upper_band();
     dlu_perm = upload(lu.perm, st);
@@ -316,7 +346,7 @@ void Run::upload_lu() {
     dub_fptr = upload(Ub.fptr, st);
     dub_fcol = upload(Ub.fcol, st);
     dub_fval = upload(Ub.fval, st);
-    eng.sync();
+    eng->sync();
     ludev.n = lu.n;
     ludev.perm = dlu_perm.as<int>();
     ludev.L = BandFactor{dlb_band.as<double>(), nullptr, nullptr, nullptr, dlb_fptr.as<int>(), dlb_fcol.as<int>(),
@@ -338,7 +368,7 @@ void Run::init() {
     auto t0 = std::chrono::steady_clock::now();
     auto lap = [&](const char *what) {
         if (!trace) return;
-        eng.sync();
+        eng->sync();
         auto t1 = std::chrono::steady_clock::now();
         std::fprintf(stderr, "vx init %-14s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(t1 - t0).count());
         t0 = t1;
@@ -373,10 +403,10 @@ void Run::init() {
 // EMFieldSolver::EnforceChargeNeutralization (EMSolver.cpp:621-629):
 // neutralizationCharge = -rho(t=0), J = 0.
 void Run::enforce_neutralization() {
-    eng.moments_only({this});
-    launch_negate(F.neut, F.charge, n, eng.stream);
-    VX_CUDA(cudaMemsetAsync(F.J, 0, (size_t)n * sizeof(double), eng.stream));
-    eng.sync();
+    eng->moments_only({this});
+    launch_negate(F.neut, F.charge, n, eng->stream);
+    VX_CUDA(cudaMemsetAsync(F.J, 0, (size_t)n * sizeof(double), eng->stream));
+    eng->sync();
 }
 
 int64_t Run::state_size() const {
@@ -389,7 +419,7 @@ int64_t Run::state_size() const {
 
 // Host-buffer step: H2D of the packed state, one RK step, D2H of the new state.
 void Run::step_host(const double *in, double *out, double dt) {
-    cudaStream_t st = eng.stream;
+    cudaStream_t st = eng->stream;
     const double *p = in;
     for (auto &sp : rects)
         for (auto &lvl : sp)
@@ -410,13 +440,13 @@ void Run::step_host(const double *in, double *out, double dt) {
     VX_CUDA(cudaMemcpyAsync(F.phi, p, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st));
     p += n;
     VX_CUDA(cudaMemcpyAsync(F.ex0, p, sizeof(double), cudaMemcpyHostToDevice, st));
-    eng.refresh_efield(*this);
+    eng->refresh_efield(*this);
     advance(dt);
     state_to_host(out);
 }
 
 void Run::state_to_host(double *out) {
-    cudaStream_t st = eng.stream;
+    cudaStream_t st = eng->stream;
     double *q = out;
     for (auto &sp : rects)
         for (auto &lvl : sp)
@@ -433,14 +463,14 @@ void Run::state_to_host(double *out) {
     VX_CUDA(cudaMemcpyAsync(q, F.phi, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
     q += n;
     VX_CUDA(cudaMemcpyAsync(q, F.ex0, sizeof(double), cudaMemcpyDeviceToHost, st));
-    eng.sync();
+    eng->sync();
 }
 
-double Run::calculate_dt() { return eng.calculate_dt({this})[0]; }
+double Run::calculate_dt() { return eng->calculate_dt({this})[0]; }
 
-void Run::advance(double dt) { eng.advance({this}, {dt}); }
+void Run::advance(double dt) { eng->advance({this}, {dt}); }
 
-void Run::advance_fields(double dt) { eng.advance_fields({this}, {dt}); }
+void Run::advance_fields(double dt) { eng->advance_fields({this}, {dt}); }
 
 // ---------------------------------------------------------------- LaunchSet / Engine
 LaunchSet::~LaunchSet() {

@@ -95,7 +95,10 @@ class Run {
 public:
     Run(Engine &eng, std::shared_ptr<Problem> prob, int precision = kF64);
     ~Run();
-    Engine &eng;
+    Engine *eng;  // the engine whose stream runs this run's work (a serving loop builds on its own)
+    // Hands the run to another engine of the same device: the old engine drops its cached
+    // launch sets (call on the thread that drives the old engine, with its work done).
+    void migrate(Engine &to);
     std::unique_ptr<Settings> S;
     // rects[species][depth] -> patches of that level, in the reference's order.
     std::vector<std::vector<std::vector<std::unique_ptr<Rect>>>> rects;

@@ -196,6 +196,39 @@ void launch_fill_separable(float *f0, float *f1, int pitch, int nx, int np, cons
     vx_launch(k_fill_separable, dim3((np + 255) / 256, nx), 256, 0, s, f0, f1, pitch, nx, np, dx_sum, dp_sum, inv, fn);
 }
 
+// Rectangle::InitializeDistribution (Rectangle.cpp:616-665) for a problem whose
+// InitialDistribution is a sum of product terms, f(x, p) = sum_t (X_t(x) * P_t(p)) / C_t.
+// The host evaluates the hook's factors at every sample point (X over the patch's n_x *
+// nvals x samples, P over its n_p * nvals p samples, with its own exp / sin); each
+// thread forms one cell's nvals^2 samples in the reference's loop order and operation
+// order (--fmad=false: no contraction), so the cell averages equal the host loop's bits.
+__global__ void k64_quadrature(double *f0, double *f1, int pitch, int nx, int np, int nvals, int terms,
+                               const double *X, const double *Pf, const double *C, double scale) {
+    VX_PDL_WAIT();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (j >= np || i >= nx) return;
+    const double *xr = X + (size_t)i * nvals, *pr = Pf + (size_t)j * nvals;
+    const size_t xstride = (size_t)nx * nvals, pstride = (size_t)np * nvals;
+    double temp = 0.0;
+    for (int k = 0; k < nvals; k++) {
+        for (int l = 0; l < nvals; l++) {
+            double v = (xr[k] * pr[l]) / C[0];
+            for (int t = 1; t < terms; t++) v = v + (xr[t * xstride + k] * pr[t * pstride + l]) / C[t];
+            temp = temp + v;
+        }
+    }
+    const double f = temp * scale;
+    const int id = pidx(i, j, pitch);
+    f0[id] = f;
+    f1[id] = f;
+}
+
+void launch_quadrature64(double *f0, double *f1, int pitch, int nx, int np, int nvals, int terms, const double *X,
+                         const double *Pf, const double *C, double scale, cudaStream_t s) {
+    vx_launch(k64_quadrature, dim3((np + 127) / 128, nx), 128, 0, s, f0, f1, pitch, nx, np, nvals, terms, X, Pf, C,
+              scale);
+}
+
 // ---------------------------------------------------------------- assembly
 // Level::CollectRhoAndJ + EMFieldSolver::AssembleRhoAndJ (Level.cpp:19-62,
 // EMSolver.cpp:104-122): per level, chargeL[x] = 0 + (patch values in patch order);
@@ -715,12 +748,9 @@ __global__ void __launch_bounds__(1024, 1) k_poisson(PoissonLaunch L) {
 
 void launch_poisson(const PoissonLaunch &L) {
     PoissonLaunch P = L;
-    static int max_smem = 0;
-    if (!max_smem) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    }
+    int max_smem = 0, dev = 0;  // per call: engines on several host threads may launch
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     // the solution vector joins the two chunk buffers in shared memory when it fits
     const int base = 2 * (int)sizeof(PoisBandChunk);
     P.x_in_smem = (L.maxn <= kPoisSmemMaxN && base + 8 * L.maxn <= max_smem) ? 1 : 0;

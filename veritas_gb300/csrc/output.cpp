@@ -64,10 +64,10 @@ std::vector<double> Run::slot_to_host(const Rect &r, int slot) {
     const void *src = slot == 0 ? r.desc.f0 : r.desc.f1;
     std::vector<double> h(pe);
     if (r.esize == 8) {
-        VX_CUDA(cudaMemcpyAsync(h.data(), src, pe * sizeof(double), cudaMemcpyDeviceToHost, eng.stream));
-        VX_CUDA(cudaStreamSynchronize(eng.stream));
+        VX_CUDA(cudaMemcpyAsync(h.data(), src, pe * sizeof(double), cudaMemcpyDeviceToHost, eng->stream));
+        VX_CUDA(cudaStreamSynchronize(eng->stream));
     } else {
-        auto f = to_host((const float *)src, pe, eng.stream);
+        auto f = to_host((const float *)src, pe, eng->stream);
         const double inv = 1.0 / fnorm[r.species];
         for (size_t q = 0; q < pe; q++) h[q] = (double)f[q] * inv;
     }
@@ -76,7 +76,7 @@ std::vector<double> Run::slot_to_host(const Rect &r, int slot) {
 
 void Run::write_fields(const std::string &dir, unsigned mask, int digits, double t) {
     const Settings &s = *S;
-    eng.sync();
+    eng->sync();
     const std::string d = dir.empty() ? std::string(".") : dir;
     auto line = [](std::ofstream &o, const double *v, size_t n) {
         for (size_t i = 0; i < n; i++) o << v[i] << " ";
@@ -94,11 +94,11 @@ void Run::write_fields(const std::string &dir, unsigned mask, int digits, double
                     const size_t nc = (size_t)r.n_x * rtb;
                     std::vector<double> col(nc);
                     if (precision == kF32) {  // FP32 pairs of the column sums, then their scale
-                        auto pr = to_host((const float *)r.desc.chargeR, 2 * nc, eng.stream);
+                        auto pr = to_host((const float *)r.desc.chargeR, 2 * nc, eng->stream);
                         for (size_t c = 0; c < nc; c++)
                             col[c] = ((double)pr[2 * c] + (double)pr[2 * c + 1]) * r.desc.msc_rho;
                     } else {
-                        col = to_host(r.desc.chargeR, nc, eng.stream);
+                        col = to_host(r.desc.chargeR, nc, eng->stream);
                     }
                     const size_t shift = (size_t)r.x_pos * rtb;
                     for (size_t c = 0; c < nc; c++) chargeL[shift + c] += col[c];
@@ -154,27 +154,27 @@ void Run::write_fields(const std::string &dir, unsigned mask, int digits, double
         }
     }
     if (mask & VX_OUT_POTENTIAL) {  // potential.txt (EMSolver.cpp:417-430)
-        auto phi = to_host(F.phi, (size_t)n, eng.stream);
+        auto phi = to_host(F.phi, (size_t)n, eng->stream);
         line(out_stream(d + "/potential.txt", digits), phi.data(), phi.size());
     }
     if (mask & VX_OUT_EFIELD_LONG) {  // EFieldLong.txt: GetEfield(i) (EMSolver.cpp:381-394)
-        auto ex = to_host(F.efin, (size_t)n, eng.stream);
+        auto ex = to_host(F.efin, (size_t)n, eng->stream);
         line(out_stream(d + "/EFieldLong.txt", digits), ex.data(), ex.size());
     }
     if (mask & VX_OUT_EFIELD_TRANS) {  // EFieldTrans.txt: E_y then E_z (EMSolver.cpp:396-415)
         std::ofstream &o = out_stream(d + "/EFieldTrans.txt", digits);
-        auto ey = to_host(F.Ey, (size_t)nf, eng.stream), ez = to_host(F.Ez, (size_t)nf, eng.stream);
+        auto ey = to_host(F.Ey, (size_t)nf, eng->stream), ez = to_host(F.Ez, (size_t)nf, eng->stream);
         line(o, ey.data(), ey.size());
         line(o, ez.data(), ez.size());
     }
     if (mask & VX_OUT_BFIELD_TRANS) {  // BFieldTrans.txt: B_y then B_z (EMSolver.cpp:432-451)
         std::ofstream &o = out_stream(d + "/BFieldTrans.txt", digits);
-        auto by = to_host(F.By, (size_t)nf, eng.stream), bz = to_host(F.Bz, (size_t)nf, eng.stream);
+        auto by = to_host(F.By, (size_t)nf, eng->stream), bz = to_host(F.Bz, (size_t)nf, eng->stream);
         line(o, by.data(), by.size());
         line(o, bz.data(), bz.size());
     }
     if (mask & VX_OUT_ASQUARED) {  // ASquared.txt: GetASquared(i), i < x_size (EMSolver.cpp:453-466)
-        auto a = to_host(F.asq, (size_t)n, eng.stream);
+        auto a = to_host(F.asq, (size_t)n, eng->stream);
         line(out_stream(d + "/ASquared.txt", digits), a.data(), a.size());
     }
     if (mask & VX_OUT_TIME) {  // time.txt: the caller's clock (EMSolver.cpp:468-477)
@@ -186,7 +186,7 @@ void Run::write_fields(const std::string &dir, unsigned mask, int digits, double
 // every patch as "r x_pos p_pos n_x n_p" and then "x p  f" per cell (f of slot 0, four
 // significant digits).
 void Run::write_rectangles(const std::string &dir, double t) {
-    eng.sync();
+    eng->sync();
     const std::string d = dir.empty() ? std::string(".") : dir;
     for (size_t sp = 0; sp < rects.size(); sp++)
         for (size_t l = 0; l < rects[sp].size(); l++) {

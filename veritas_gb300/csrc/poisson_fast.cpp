@@ -74,8 +74,8 @@ void Run::build_poisson_fast() {
     }
     for (int r = 0; r < 3; r++)
         for (int q = 0; q < 3; q++) pfdev.K[3 * r + q] = A[r][3 + q] / A[r][r];
-    dpf_Y = upload(pf_Y, eng.stream);
-    eng.sync();
+    dpf_Y = upload(pf_Y, eng->stream);
+    eng->sync();
     pfdev.Y = dpf_Y.as<double>();
     pfdev.rho = rho;
     pfdev.c_inv = 1.0 / c;

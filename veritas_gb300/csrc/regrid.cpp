@@ -267,12 +267,12 @@ std::vector<std::vector<std::pair<int, int>>> Run::flag_cells() {
     if (total) {
         std::vector<PatchT<double>> descs;
         for (Rect *R : flat) descs.push_back(R->desc);
-        DevBuf dd = upload(descs, eng.stream);
-        DevBuf dfp = upload(fp, eng.stream);
+        DevBuf dd = upload(descs, eng->stream);
+        DevBuf dfp = upload(fp, eng->stream);
         DevBuf dout(total);
-        launch_flags(dd.p, dfp.as<FlagPatch>(), (int)fp.size(), dout.as<uint8_t>(), precision, eng.stream);
-        VX_CUDA(cudaMemcpyAsync(flags.data(), dout.p, total, cudaMemcpyDeviceToHost, eng.stream));
-        eng.sync();
+        launch_flags(dd.p, dfp.as<FlagPatch>(), (int)fp.size(), dout.as<uint8_t>(), precision, eng->stream);
+        VX_CUDA(cudaMemcpyAsync(flags.data(), dout.p, total, cudaMemcpyDeviceToHost, eng->stream));
+        eng->sync();
     }
     std::vector<std::vector<std::pair<int, int>>> out(flat.size());
     for (size_t k = 0; k < flat.size(); k++) {
@@ -410,7 +410,7 @@ void Run::promote(const std::vector<std::vector<BoxList>> &hier, bool init) {
     auto t0 = std::chrono::steady_clock::now();
     auto lap = [&](const char *what) {
         if (!trace) return;
-        eng.sync();
+        eng->sync();
         auto t1 = std::chrono::steady_clock::now();
         std::fprintf(stderr, "vx promote %-11s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(t1 - t0).count());
         t0 = t1;
@@ -483,8 +483,8 @@ void Run::transfer_from(std::vector<std::vector<std::vector<std::unique_ptr<Rect
         mtotal += (long long)(R->n_x + 4) * (R->n_p + 4);
     }
     DevBuf dmask((size_t)std::max<long long>(mtotal, 1));
-    VX_CUDA(cudaMemsetAsync(dmask.p, 0, dmask.bytes, eng.stream));
-    DevBuf dd = upload(descs, eng.stream);
+    VX_CUDA(cudaMemsetAsync(dmask.p, 0, dmask.bytes, eng->stream));
+    DevBuf dd = upload(descs, eng->stream);
 
     auto bounds = [&](const Rect &R, int i, int j) { return i >= -2 && i < R.n_x + 2 && j >= -2 && j < R.n_p + 2; };
     auto need = [](bool ok) {
@@ -529,9 +529,9 @@ void Run::transfer_from(std::vector<std::vector<std::vector<std::unique_ptr<Rect
     };
     auto run_ops = [&](const std::vector<XferOp> &ops) {
         if (ops.empty()) return;
-        DevBuf d = upload(ops, eng.stream);
-        launch_xfer(dd.p, d.as<XferOp>(), (int)ops.size(), dmask.as<uint8_t>(), precision, eng.stream);
-        eng.sync();
+        DevBuf d = upload(ops, eng->stream);
+        launch_xfer(dd.p, d.as<XferOp>(), (int)ops.size(), dmask.as<uint8_t>(), precision, eng->stream);
+        eng->sync();
     };
     for (size_t sp = 0; sp < old.size(); sp++) {
         auto &nl = rects[sp];
@@ -566,17 +566,17 @@ void Run::transfer_from(std::vector<std::vector<std::vector<std::unique_ptr<Rect
 DevBuf Run::flat_descs() {
     std::vector<PatchT<double>> descs;
     for (Rect *R : flat) descs.push_back(R->desc);
-    return upload(descs, eng.stream);
+    return upload(descs, eng->stream);
 }
 
 // Mesh::PushData(val) (Mesh.cpp:91-106) for this run alone.
 void Run::push_data(int slot) {
     DevBuf dd = flat_descs();
-    DevBuf dops = upload(ghost_ops, eng.stream);
+    DevBuf dops = upload(ghost_ops, eng->stream);
     for (size_t b = 0; b + 1 < ghost_b.ptr.size(); b++)
         launch_ghost(dd.p, dops.as<GhostOp>() + ghost_b.ptr[b], ghost_b.ptr[b + 1] - ghost_b.ptr[b], slot, precision,
-                     eng.stream);
-    eng.sync();
+                     eng->stream);
+    eng->sync();
 }
 
 // FCTTimeStep sub-step 3 (Rectangle.cpp:1614-1621) over every patch: f[to] = f[from].
@@ -584,9 +584,9 @@ void Run::copy_slot(int from, int to) {
     for (Rect *R : flat) {
         const double *src = from == 0 ? R->desc.f0 : (from == 1 ? R->desc.f1 : R->desc.f2);
         double *dst = to == 0 ? R->desc.f0 : (to == 1 ? R->desc.f1 : R->desc.f2);
-        VX_CUDA(cudaMemcpyAsync(dst, src, R->plane_bytes(), cudaMemcpyDeviceToDevice, eng.stream));
+        VX_CUDA(cudaMemcpyAsync(dst, src, R->plane_bytes(), cudaMemcpyDeviceToDevice, eng->stream));
     }
-    eng.sync();
+    eng->sync();
 }
 
 }  // namespace vx

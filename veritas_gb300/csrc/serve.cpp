@@ -1,13 +1,19 @@
 // Serving loop: continuous batching of independent solves on one context.
 //
-// Requests queue in arrival order.  Each call of step() first admits, in order, every
-// waiting request whose device-memory estimate fits in what the budget has left (the
-// estimate is replaced by the run's real footprint once it exists), then advances every
-// live solve by one full RK step in one batched launch set (one launch per sub-step for
-// all of them), and retires the solves that reached their step count: their final
-// state is written where the request asked and their memory is released before the
-// next admission.  A request that arrives while others run joins at the next step;
-// nothing waits for the batch to drain.
+// Requests queue in arrival order.  Each call of step() first binds the runs the builder
+// thread has finished, then admits, in order, the waiting requests whose device-memory
+// estimate fits in what the budget has left and hands them to the builder thread, which
+// constructs each run (host quadrature, clustering, Poisson factors, uploads) on its own
+// engine and streams while the loop keeps stepping; the estimate is replaced by the
+// run's real footprint when it is bound.  Then every live solve advances by one full RK
+// step in one batched launch set per precision (one launch per sub-step for all of
+// them), and each solve regrids by the reference driver's rule (veritas.cpp:146-151: a
+// counter of steps since the last regrid; at a count above 20, once the plasma is on,
+// SolverManager::reGrid and the counter restarts).  A solve whose CFL bound or
+// E_x0 is not finite after its step (something in it went non-finite) fails and is
+// retired alone; the others in the batch are unaffected (runs share launches, never data).  Finished solves
+// write their final state where the request asked and release their memory before the
+// next admission.
 #include <algorithm>
 #include <cmath>
 
@@ -41,12 +47,53 @@ size_t Server::estimate_bytes(const LaserSlabParams &p, int precision) {
     return (size_t)(cells * planes * esize * levels + fields);
 }
 
-Server::Server(Engine &e, size_t budget, int max_live) : eng(e), budget_(budget), max_live_(max_live) {}
+Server::Server(Engine &e, size_t budget, int max_live) : eng(e), budget_(budget), max_live_(max_live) {
+    builder_eng_.reset(new Engine(e.device));
+    VX_CUDA(cudaSetDevice(e.device));  // the builder engine's constructor made it current too
+    builder_ = std::thread([this] { builder_loop(); });
+}
 
-Server::~Server() = default;
+Server::~Server() {
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        stop_ = true;
+    }
+    cv_.notify_all();
+    if (builder_.joinable()) builder_.join();
+    built_.clear();  // runs built but never bound
+    for (auto &kv : reqs_) kv.second.run.reset();
+}
+
+void Server::builder_loop() {
+    cudaSetDevice(builder_eng_->device);
+    for (;;) {
+        Build b;
+        {
+            std::unique_lock<std::mutex> lk(mu_);
+            cv_.wait(lk, [&] { return stop_ || !todo_.empty(); });
+            if (stop_) return;
+            b = std::move(todo_.front());
+            todo_.pop_front();
+        }
+        try {
+            b.run.reset(new Run(*builder_eng_, std::make_shared<LaserSlab>(b.params), b.precision));
+            b.run->poisson = b.poisson;
+            b.run->init();
+            b.run->migrate(eng);  // drops the builder engine's sets; the loop's engine runs it from now on
+        } catch (const std::exception &e) {
+            b.run.reset();
+            b.error = e.what();
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            built_.push_back(std::move(b));
+        }
+        built_cv_.notify_all();
+    }
+}
 
 int64_t Server::submit(const LaserSlabParams &p, int precision, int64_t steps, double arrival,
-                       const std::string &state_path, int poisson) {
+                       const std::string &state_path, int poisson, int regrid) {
     if (steps <= 0) throw std::invalid_argument("a request needs at least one step");
     if (precision != kF64 && precision != kF32) throw std::invalid_argument("precision must be 64 or 32");
     if (poisson != kPoissonLU && poisson != kPoissonScan) throw std::invalid_argument("poisson must be 0 or 1");
@@ -55,39 +102,130 @@ int64_t Server::submit(const LaserSlabParams &p, int precision, int64_t steps, d
     r.params = p;
     r.precision = precision;
     r.poisson = precision == kF32 ? kPoissonScan : poisson;
+    r.regrid = regrid ? 1 : 0;
     r.steps = steps;
     r.arrival = arrival;
     r.state_path = state_path;
     r.estimate = estimate_bytes(p, precision);
-    if (r.estimate > budget_) throw std::invalid_argument("request larger than the whole memory budget");
+    if (r.estimate > budget_)
+        throw std::invalid_argument("request of about " + std::to_string(r.estimate >> 20) +
+                                    " MiB is larger than the whole memory budget");
     waiting_.push_back(r.id);
     reqs_.emplace(r.id, std::move(r));
     return next_id_ - 1;
 }
 
+int Server::waiting() const { return (int)waiting_.size() + building_; }
+
 void Server::admit(double now) {
-    while (!waiting_.empty() && (int)live_.size() < max_live_) {
+    std::vector<Build> go;
+    while (!waiting_.empty() && (int)live_.size() + building_ + (int)go.size() < max_live_) {
         Request &r = reqs_.at(waiting_.front());
         if (used_ + r.estimate > budget_) break;  // in order: the head blocks the queue
         waiting_.pop_front();
         r.admitted = now;
-        r.run.reset(new Run(eng, std::make_shared<LaserSlab>(r.params), r.precision));
-        r.run->poisson = r.poisson;
-        r.run->init();
+        r.status = kBuilding;
+        used_ += r.estimate;
+        Build b;
+        b.id = r.id;
+        b.params = r.params;
+        b.precision = r.precision;
+        b.poisson = r.poisson;
+        go.push_back(std::move(b));
+    }
+    if (go.empty()) return;
+    building_ += (int)go.size();
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        for (auto &b : go) todo_.push_back(std::move(b));
+    }
+    cv_.notify_one();
+}
+
+void Server::bind_built(double now) {
+    std::vector<Build> done;
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        done.swap(built_);
+    }
+    for (auto &b : done) {
+        building_--;
+        Request &r = reqs_.at(b.id);
+        used_ -= r.estimate;
+        if (r.status == kCancelled) continue;  // withdrawn while building: the run goes
+        if (!b.run) {
+            r.error = b.error;
+            r.status = kFailed;
+            r.finish = clock();
+            finished_order_.push_back(r.id);
+            continue;
+        }
+        r.run = std::move(b.run);
         r.bytes = r.run->device_bytes();
         used_ += r.bytes;
+        r.bound = now;
+        r.status = kLive;
         live_.push_back(r.id);
     }
 }
 
+void Server::retire(Request &r, Status st, double now) {
+    r.finish = now;
+    r.status = st;
+    if (r.run) {
+        r.sim_time = r.run->S->time;
+        if (st == kDone && !r.state_path.empty()) r.run->save_state(r.state_path);
+        r.cells = r.run->cell_count();
+        used_ -= r.bytes;
+        r.run.reset();
+    }
+    finished_order_.push_back(r.id);
+}
+
+void Server::cancel(int64_t id) {
+    auto it = reqs_.find(id);
+    if (it == reqs_.end()) throw std::invalid_argument("unknown request id");
+    Request &r = it->second;
+    switch (r.status) {
+        case kWaiting:
+            waiting_.erase(std::find(waiting_.begin(), waiting_.end(), id));
+            r.status = kCancelled;
+            r.finish = clock();
+            finished_order_.push_back(id);
+            break;
+        case kBuilding:
+            r.status = kCancelled;  // bind_built drops the run when its build ends
+            r.finish = clock();
+            break;
+        case kLive:
+            eng.sync();
+            live_.erase(std::find(live_.begin(), live_.end(), id));
+            retire(r, kCancelled, clock());
+            break;
+        default:
+            break;  // already over
+    }
+}
+
 int Server::step(double now) {
+    bind_built(now);
     admit(now);
+    if (live_.empty() && building_ > 0) {
+        // nothing to step: wait (a little) for a build to end rather than spin
+        {
+            std::unique_lock<std::mutex> lk(mu_);
+            built_cv_.wait_for(lk, std::chrono::milliseconds(50), [&] { return !built_.empty(); });
+        }
+        bind_built(clock());
+    }
     if (live_.empty()) return 0;
     std::vector<Run *> set;
     for (int64_t id : live_) set.push_back(reqs_.at(id).run.get());
     // one launch set per precision and Poisson solver (different kernels); the sets of
     // earlier mixes are dropped, so cached tables do not pile up beside the budget
     std::vector<std::vector<Run *>> used;
+    std::map<Run *, double> t_before, dt_of;
+    for (Run *r : set) t_before[r] = r->S->time;
     for (int prec : {kF64, kF32})
         for (int pois : {kPoissonLU, kPoissonScan}) {
             std::vector<Run *> part;
@@ -95,27 +233,48 @@ int Server::step(double now) {
                 if (r->precision == prec && r->poisson == pois) part.push_back(r);
             if (part.empty()) continue;
             auto dt = eng.calculate_dt(part);
+            for (size_t k = 0; k < part.size(); k++) dt_of[part[k]] = dt[k];
             eng.advance(part, dt);
             used.push_back(part);
         }
     eng.retain_sets(used);
+    // health: E_x0 (updated every stage from phi, which the solve makes depend on every
+    // cell's charge) turns non-finite within a step once any f, charge or field value has
+    std::vector<double> ex0(set.size(), 0.0);
+    for (size_t k = 0; k < set.size(); k++)
+        VX_CUDA(cudaMemcpyAsync(&ex0[k], set[k]->F.ex0, sizeof(double), cudaMemcpyDeviceToHost, eng.stream));
     eng.sync();
+    std::map<Run *, double> ex0_of;
+    for (size_t k = 0; k < set.size(); k++) ex0_of[set[k]] = ex0[k];
+    const double tnow = clock();
     std::vector<int64_t> still;
     for (int64_t id : live_) {
         Request &r = reqs_.at(id);
-        r.done_steps++;
-        if (r.done_steps < r.steps) {
-            still.push_back(id);
+        Run *run = r.run.get();
+        // health: the step's CFL bound (from the fields it started from) and E_x0 after it
+        const double dt = dt_of[run];
+        if (!(std::isfinite(dt) && dt > 0) || !std::isfinite(ex0_of[run])) {
+            r.error = "the solve is not finite any more (CFL bound or E_x0 after step " +
+                      std::to_string(r.done_steps + 1) + ")";
+            retire(r, kFailed, tnow);
             continue;
         }
-        r.finish = clock();
-        r.sim_time = r.run->S->time;
-        if (!r.state_path.empty()) r.run->save_state(r.state_path);
-        used_ -= r.bytes;
-        r.cells = r.run->cell_count();
-        r.run.reset();
-        r.finished = true;
-        finished_order_.push_back(id);
+        r.done_steps++;
+        if (r.done_steps >= r.steps) {
+            retire(r, kDone, tnow);
+            continue;
+        }
+        // the reference driver's regrid rule, with the time before the step (veritas.cpp:146-151)
+        if (r.regrid && regrid_enabled && run->S->maxDepth > 0) {
+            if (r.regrid_counter > 20 && t_before[run] > regrid_after) {
+                run->regrid(false);
+                r.regrids++;
+                r.regrid_counter = 0;
+            } else {
+                r.regrid_counter++;
+            }
+        }
+        still.push_back(id);
     }
     live_ = still;
     return (int)live_.size();

@@ -1,10 +1,13 @@
 // Serving loop: continuous batching of independent solves under an HBM budget (serve.cpp).
 #pragma once
 #include <chrono>
+#include <condition_variable>
 #include <deque>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "engine.hpp"
@@ -13,17 +16,21 @@ namespace vx {
 
 class Server {
 public:
+    enum Status { kWaiting = 0, kBuilding, kLive, kDone, kCancelled, kFailed };
     struct Request {
         int64_t id = 0;
         LaserSlabParams params;
         int precision = kF64;
         int poisson = kPoissonLU;
+        int regrid = 1;  // 1: the reference driver's regrid rule (veritas.cpp:146-151); 0: none
         int64_t steps = 0, done_steps = 0;
-        double arrival = 0, admitted = -1, finish = -1, sim_time = 0;
+        int regrid_counter = 0;
+        int regrids = 0;
+        double arrival = 0, admitted = -1, bound = -1, finish = -1, sim_time = 0;
         size_t estimate = 0, bytes = 0;
         long long cells = 0;
-        bool finished = false;
-        std::string state_path;
+        Status status = kWaiting;
+        std::string state_path, error;
         std::unique_ptr<Run> run;
     };
 
@@ -31,30 +38,60 @@ public:
     ~Server();
     // Queue a solve of `steps` RK steps that arrived at `arrival` (seconds on clock()).
     int64_t submit(const LaserSlabParams &p, int precision, int64_t steps, double arrival,
-                   const std::string &state_path, int poisson = kPoissonLU);
-    // Admit what fits, advance every live solve one step, retire the finished ones.
-    // Returns the number of solves still live.
+                   const std::string &state_path, int poisson = kPoissonLU, int regrid = 1);
+    // Bind the runs built since the last call, admit what fits (its runs are built on
+    // the builder thread), advance every live solve one step, regrid those whose counter
+    // says so, retire the finished, failed and cancelled ones.  Returns the live count.
     int step(double now);
+    // Withdraws a request that has not finished: a waiting one leaves the queue, one being
+    // built is dropped when its build ends, a live one is retired now (no state written).
+    void cancel(int64_t id);
     const Request &request(int64_t id) const;
     double clock() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0_).count();
     }
     size_t used_bytes() const { return used_; }
     int live() const { return (int)live_.size(); }
-    int waiting() const { return (int)waiting_.size(); }
+    // Requests not yet live: waiting for memory, or admitted and being built.
+    int waiting() const;
     static size_t estimate_bytes(const LaserSlabParams &p, int precision);
+    // The regrid rule's time threshold [s]: the reference's driver regrids only once its
+    // plasma is switched on (t > 3 laser periods in its demo, veritas.cpp:139-151); served
+    // solves couple the plasma from t = 0, so the default is 0.  regrid_enabled = false
+    // turns regridding off for every request.
+    double regrid_after = 0;
+    bool regrid_enabled = true;
 
 private:
+    struct Build {  // one admitted request on its way through the builder thread
+        int64_t id;
+        LaserSlabParams params;
+        int precision, poisson;
+        std::unique_ptr<Run> run;
+        std::string error;
+    };
     void admit(double now);
+    void bind_built(double now);
+    void retire(Request &r, Status st, double now);
+    void builder_loop();
     Engine &eng;
+    std::unique_ptr<Engine> builder_eng_;  // the builder thread's engine (own streams, same device)
     size_t budget_, used_ = 0;
     int max_live_;
     int64_t next_id_ = 1;
     std::map<int64_t, Request> reqs_;
     std::deque<int64_t> waiting_;
     std::vector<int64_t> live_;
+    int building_ = 0;
     std::vector<int64_t> finished_order_;
     std::chrono::steady_clock::time_point t0_ = std::chrono::steady_clock::now();
+    // builder thread: admitted requests in, built runs out
+    std::mutex mu_;
+    std::condition_variable cv_, built_cv_;
+    std::deque<Build> todo_;
+    std::vector<Build> built_;
+    bool stop_ = false;
+    std::thread builder_;
 };
 
 }  // namespace vx

@@ -158,6 +158,26 @@ double LaserSlab::InitialDistribution(const Settings &s, double x, double p, int
     return v;
 }
 
+// InitialDistribution's terms: (ne * exp) / sqrt for the plasma, ((bdens * ne) * exp) /
+// sqrt for the electron beam (the operations of InitialDistribution above).
+double LaserSlab::XFactor(const Settings &s, int term, double x, int particleType) const {
+    double ne = s.temp[particleType][0] * slab_density(x / P.lambda);
+    return term == 0 ? ne : P.bdens * ne;
+}
+
+double LaserSlab::PFactor(const Settings &s, int term, double p, int particleType) const {
+    if (term == 0) {
+        double dpv = p - s.temp[particleType][2];
+        return std::exp(-(dpv * dpv) / (2.0 * s.temp[particleType][1]));
+    }
+    double dbv = p - beam_p;
+    return std::exp(-(dbv * dbv) / (2.0 * beam_T));
+}
+
+double LaserSlab::Divisor(const Settings &s, int term, int particleType) const {
+    return term == 0 ? std::sqrt(kDPI * s.temp[particleType][1]) : std::sqrt(kDPI * beam_T);
+}
+
 double LaserSlab::Density(const Settings &s, double x, int particleType) const {
     return s.temp[particleType][0] * slab_density(x / P.lambda);
 }

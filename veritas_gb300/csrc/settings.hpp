@@ -57,6 +57,15 @@ public:
     virtual bool Separable() const { return false; }
     virtual double Density(const Settings &, double, int) const { return 0.0; }
     virtual double Profile(const Settings &, double, int) const { return 0.0; }
+    // Optional, exact product form: InitialDistribution(x, p) computes
+    //   v = (X_0(x) * P_0(p)) / C_0;  v = v + (X_t(x) * P_t(p)) / C_t  (t = 1 .. terms-1)
+    // in exactly these IEEE double operations.  A problem that says so (ProductTerms > 0)
+    // has its FP64 quadrature formed on the device from the host-evaluated factors, with
+    // the same bits as the host loop.
+    virtual int ProductTerms(int) const { return 0; }
+    virtual double XFactor(const Settings &, int, double, int) const { return 0.0; }
+    virtual double PFactor(const Settings &, int, double, int) const { return 0.0; }
+    virtual double Divisor(const Settings &, int, int) const { return 1.0; }
 };
 
 // Parameters of the built-in laser / plasma-slab problem (lengths in laser wavelengths,
@@ -95,6 +104,10 @@ public:
     bool Separable() const override { return true; }
     double Density(const Settings &s, double x, int particleType) const override;
     double Profile(const Settings &s, double p, int particleType) const override;
+    int ProductTerms(int particleType) const override { return (P.bdens != 0.0 && particleType == 0) ? 2 : 1; }
+    double XFactor(const Settings &s, int term, double x, int particleType) const override;
+    double PFactor(const Settings &s, int term, double p, int particleType) const override;
+    double Divisor(const Settings &s, int term, int particleType) const override;
     double slab_density(double xl) const;
     LaserSlabParams P;
     double beam_T = 0.0, beam_p = 0.0;  // beam temperature [J] and drift [kg m/s]

@@ -93,12 +93,12 @@ void Run::load_state(const std::string &path) {
     double ex0 = f.rdd();
     long long fn = f.ri(), fpre = f.ri(), fpost = f.ri();
     if (fn != n || fpre != pre || fpost != post) throw std::invalid_argument("state file grid does not match the run");
-    cudaStream_t st = eng.stream;
+    cudaStream_t st = eng->stream;
     auto put = [&](double *d, size_t expect) {
         auto v = f.rv();
         if (v.size() != expect) throw std::invalid_argument("state file array size mismatch");
         h2d(d, v, st);
-        eng.sync();
+        eng->sync();
     };
     size_t fb = (size_t)nf * 8;
     put(F.By, fb);
@@ -170,8 +170,8 @@ void Run::load_state(const std::string &path) {
     layout_version++;
     // a state written by an FP32 run holds FP32-form values already: nothing to rebase
     if (precision == kF32 && !fp32_exact) rebase_neutralization(f1_host);
-    eng.refresh_efield(*this);
-    eng.sync();
+    eng->refresh_efield(*this);
+    eng->sync();
 }
 
 // The FP32 form represents f rounded to FP32, whose charge density differs from the
@@ -242,21 +242,21 @@ void Run::rebase_neutralization(const std::vector<std::vector<double>> &f1) {
         }
         q64[x] = charge;
     }
-    cudaStream_t st = eng.stream;
+    cudaStream_t st = eng->stream;
     auto keep_charge = d2h(F.charge, (size_t)n, st);
     auto keep_J = d2h(F.J, (size_t)n, st);
     auto neut = d2h(F.neut, (size_t)n, st);
-    eng.moments_only({this});
+    eng->moments_only({this});
     auto q32 = d2h(F.charge, (size_t)n, st);
     for (int x = 0; x < n; x++) neut[x] += q64[x] - q32[x];
     h2d(F.neut, neut, st);
     h2d(F.charge, keep_charge, st);
     h2d(F.J, keep_J, st);
-    eng.sync();
+    eng->sync();
 }
 
 void Run::save_state(const std::string &path) {
-    eng.sync();
+    eng->sync();
     File f(path, "wb");
     f.wr("VXST0001", 8);
     f.wi(0);
@@ -268,7 +268,7 @@ void Run::save_state(const std::string &path) {
     f.wi(n);
     f.wi(pre);
     f.wi(post);
-    cudaStream_t st = eng.stream;
+    cudaStream_t st = eng->stream;
     size_t fb = (size_t)nf * 8;
     f.wv(d2h(F.By, fb, st));
     f.wv(d2h(F.Bz, fb, st));

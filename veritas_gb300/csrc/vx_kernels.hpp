@@ -202,6 +202,10 @@ void launch_cfl(const CflLaunch &L);
 // Interior of a fresh (zeroed) FP32 patch from the separable quadrature's 1-D sums.
 void launch_fill_separable(float *f0, float *f1, int pitch, int nx, int np, const double *dx_sum,
                            const double *dp_sum, double inv, double fn, cudaStream_t s);
+// FP64 initial cell averages of a product-form problem (see k64_quadrature): X[t][i*nvals
+// + k], Pf[t][j*nvals + l] the factors at the sample points, C[t] the divisors.
+void launch_quadrature64(double *f0, double *f1, int pitch, int nx, int np, int nvals, int terms, const double *X,
+                         const double *Pf, const double *C, double scale, cudaStream_t s);
 // FP64 FMA throughput probe: blocks x threads threads, iters x 8 independent DFMA each.
 void launch_fp64_peak(double *out, int blocks, int threads, int iters, cudaStream_t s);
 // One warp: cycles of iters dependent (multiply, subtract) steps, then with a shuffle each.
