@@ -439,8 +439,11 @@ def main() -> None:
                     help="Poisson solver of the headline run: 0 the LU's rounding order, 1 the O(n) scan solve")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32],
                     help="precision of the headline workload (64, the plain path, unless profiling the FP32 form)")
-    ap.add_argument("--form", default="", choices=["", "config3"],
-                    help="config3: the precision form on the larger three-level case (its own JSON line)")
+    ap.add_argument("--form", default="", choices=["", "config3", "batched", "served"],
+                    help="config3: the precision form on the larger three-level case; batched: the 64-run "
+                         "ensemble alone; served: the serving loop alone (each its own JSON line; --precision "
+                         "selects the form's precision)")
+    ap.add_argument("--runs", type=int, default=64, help="ensemble size of --form batched / solves of --form served")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the FP32 / batched / served forms (FP64 headline line only)")
     ap.add_argument("--lite", action="store_true",
@@ -451,6 +454,17 @@ def main() -> None:
         return
     if args.form == "config3":
         run_config3(args)
+        return
+    if args.form in ("batched", "served"):
+        from veritas_gb300 import Context
+
+        ctx = Context(0)
+        if args.form == "batched":
+            out = measure_batched(ctx, args.runs, args.steps, max(1, args.warmup), args.precision)
+        else:
+            out = measure_serving(ctx, args.runs, args.steps, args.precision)
+        print(json.dumps({"form": args.form, **out}))
+        ctx.close()
         return
     world, rank, local = dist_info()
     dist = None

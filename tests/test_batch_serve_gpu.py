@@ -190,18 +190,18 @@ def test_server_cancels_waiting_and_live_requests(ctx, tmp_path):
 
     P = problem_for("amr2")
     srv = Server(ctx, 8 << 30)
-    keep = srv.submit(P, 6, state_path=tmp_path / "keep_alone.bin")
+    keep = srv.submit(P, 40, state_path=tmp_path / "keep_alone.bin")
     while srv.step() != (0, 0):
         pass
     srv.close()
 
     srv = Server(ctx, 8 << 30, max_live=2)
-    a = srv.submit(P, 6, state_path=tmp_path / "keep_mix.bin")
+    a = srv.submit(P, 40, state_path=tmp_path / "keep_mix.bin")
     b = srv.submit(problem_for("drift128"), 50, state_path=tmp_path / "never.bin")
-    c = srv.submit(problem_for("slab64"), 4)  # waits: max_live is 2
+    c = srv.submit(problem_for("slab64"), 4)  # waits while a and b hold both slots
     while srv.result(b)["steps_done"] < 2:
         srv.step()
-    assert srv.result(c)["status"] == 0
+    assert srv.result(a)["status"] == 2 and srv.result(c)["status"] == 0
     srv.cancel(c)
     srv.cancel(b)
     while srv.step() != (0, 0):
