@@ -274,7 +274,7 @@ struct LuRow {  // one row at the lane's column: f0, f2, both antidiffusive flux
     float f0, f2, dx, dp, s0, s2, sdp;
 };
 
-__global__ void __launch_bounds__(128, 6) k32_limupd(const P32 *patches, const TileRef *tiles, int ntiles) {
+__global__ void __launch_bounds__(128) k32_limupd(const P32 *patches, const TileRef *tiles, int ntiles) {
     VX_PDL_WAIT();
     const int wt = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (wt >= ntiles) return;
@@ -282,12 +282,7 @@ __global__ void __launch_bounds__(128, 6) k32_limupd(const P32 *patches, const T
     const unsigned full = 0xffffffffu;
     const TileRef t = tiles[wt];
     const P32 &P = patches[t.patch];
-    // the descriptor fields in registers: the loop's stores to f1 / R / C would otherwise
-    // make the compiler reload them from the descriptor after every store
     const int pit = P.pitch, nx = P.nx, np = P.np, i0 = t.i0, j0 = t.j0;
-    const int axm = P.xm, axp = P.xp, apm = P.pm, app = P.pp;
-    float *const F1 = P.f1, *const Rpw = P.Rp, *const Rmw = P.Rm, *const Cxw = P.Cx, *const Cpw = P.Cp;
-    auto active = [&](int i, int j) { return i >= axm && i < axp && j >= apm && j < app; };
     const int jj = j0 - 1 + lane;
     const int js = lane == 0 ? jj - 1 : jj + 1;  // the cell beyond the warp
     const bool edge = lane == 0 || lane == 31;
@@ -346,8 +341,8 @@ __global__ void __launch_bounds__(128, 6) k32_limupd(const P32 *patches, const T
         if (lm && own_col && r >= qlo && r < qhi) {
             const int id = pidx(r, jj, pit);
             if (lm[id] & 1) {
-                Rpw[id] = rpC;
-                Rmw[id] = rmC;
+                P.Rp[id] = rpC;
+                P.Rm[id] = rmC;
             }
         }
         // C and the update of row q = r - 1 (k32_limC, k32_update): R of rows q-1, q, q+1
@@ -369,17 +364,17 @@ __global__ void __launch_bounds__(128, 6) k32_limupd(const P32 *patches, const T
             const uint8_t m = lm ? lm[id] : 0;
             if (q >= 0 && q < nx && in0 && !(m & 2)) {
                 float v = A.f2;
-                if (active(q, jj)) v += cxq * dA;
-                if (active(q, jj)) v += cpq * pA;
-                if (active(q, jj + 1)) v -= cpq1 * pAr;
-                if (active(q + 1, jj)) v -= cxq1 * dB;
-                F1[id] = v;
+                if (active32(P, q, jj)) v += cxq * dA;
+                if (active32(P, q, jj)) v += cpq * pA;
+                if (active32(P, q, jj + 1)) v -= cpq1 * pAr;
+                if (active32(P, q + 1, jj)) v -= cxq1 * dB;
+                P.f1[id] = v;
             }
             if (m & 2) {
-                Cxw[id] = cxq;
-                Cxw[id + pit] = cxq1;
-                Cpw[id] = cpq;
-                Cpw[id + 1] = cpq1;
+                P.Cx[id] = cxq;
+                P.Cx[id + pit] = cxq1;
+                P.Cp[id] = cpq;
+                P.Cp[id + 1] = cpq1;
             }
         }
         A = B;
