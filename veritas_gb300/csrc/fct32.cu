@@ -492,22 +492,29 @@ __global__ void k32_xflux(const P32 *patches, const TileRef *tiles, int ntiles, 
     const float p0 = mom32(P, jj), p1 = mom32(P, jj + 1);
     const float w3 = 1.0f / 48.0f;
     const unsigned full = 0xffffffffu;
-    // f at rows i-2, i-1, i of the first row (i0 >= 0, so all inside the padded block)
-    float fa = 0.0f, fb = 0.0f, fc = 0.0f;
+    // f at rows i-2, i-1, i of the first row (i0 >= 0, so all inside the padded block),
+    // and row i+1 and the first row's a^2 already in flight: each row's loads are issued
+    // one row ahead of their use
+    float fa = 0.0f, fb = 0.0f, fc = 0.0f, fnext = 0.0f;
     if (col_ok) {
         const int id = pidx(t.i0, jj, pit);
         fa = f[id - 2 * pit];
         fb = f[id - pit];
         fc = f[id];
+        fnext = f[id + pit];  // row i0+1 <= nx+1
     }
+    float anext = asq32(P, F, t.i0);
     for (int r = 0; r < kStripRows; r++) {
         const int i = t.i0 + r;
         if (i > P.nx) break;  // warp-uniform
         const int id = pidx(i, jj, pit);
-        float am = 0.0f, fv = 0.0f, fd = 0.0f;
+        const float fd = fnext, a = anext;
+        if (i + 1 <= P.nx) {  // the next row's loads (row i+2 <= nx+1)
+            if (col_ok) fnext = f[id + 2 * pit];
+            anext = asq32(P, F, i + 1);
+        }
+        float am = 0.0f, fv = 0.0f;
         if (col_ok) {
-            fd = f[id + pit];  // row i+1 <= nx+1
-            const float a = asq32(P, F, i);
             const float g0 = sqrt_ge1(1.0f + p0 * p0 + a), g1 = sqrt_ge1(1.0f + p1 * p1 + a);
             am = P.kxf * __fdividef(P.dpnf * (p1 + p0), g1 + g0);
             fv = weno32(fa, fb, fc, fd, am > 0.0f, P.weno_eps);
@@ -534,15 +541,30 @@ __device__ __forceinline__ PRow prow32(const FluxView &V, int i, float p) {
     const float a = V.asq_at(i);
     return {a, sqrt_ge1(1.0f + p * p + a)};
 }
-__device__ __forceinline__ void pface32(const FluxView &V, int i, int j, bool col_ok, const PRow &lo,
-                                        const PRow &hi, float &am, float &fv) {
+// The memory inputs of p-face row i at the lane's column j: a^2 at x-face i+1 (for the
+// row's upper gamma), q E_x of the row, and f at j-2 .. j+1 (zero where the face is
+// outside the reference's range).  Loaded one row ahead of their use.
+struct PIn {
+    float a_hi, qe, f0, f1, f2, f3;
+};
+__device__ __forceinline__ PIn pload32(const FluxView &V, int i, int j, bool col_ok) {
+    PIn L{V.asq_at(i + 1), 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    if (!col_ok || i < -1 || i > V.nx) return L;
+    L.qe = V.qe_at(i);
+    const int id = pidx(i, j, V.pit);
+    L.f0 = V.f[id - 2];
+    L.f1 = V.f[id - 1];
+    L.f2 = V.f[id];
+    L.f3 = V.f[id + 1];
+    return L;
+}
+__device__ __forceinline__ void pface32(const FluxView &V, int i, bool col_ok, const PRow &lo, const PRow &hi,
+                                        const PIn &L, float &am, float &fv) {
     am = 0.0f;
     fv = 0.0f;
     if (!col_ok || i < -1 || i > V.nx) return;
-    am = V.qe_at(i) - V.kpf * __fdividef(hi.a - lo.a, hi.g + lo.g);
-    const int id = pidx(i, j, V.pit);
-    const float *f = V.f;
-    fv = weno32(f[id - 2], f[id - 1], f[id], f[id + 1], am > 0.0f, V.weno_eps);
+    am = L.qe - V.kpf * __fdividef(hi.a - lo.a, hi.g + lo.g);
+    fv = weno32(L.f0, L.f1, L.f2, L.f3, am > 0.0f, V.weno_eps);
 }
 
 __global__ void k32_pflux(const P32 *patches, const TileRef *tiles, int ntiles, const RunFields *fields, int step,
@@ -558,16 +580,22 @@ __global__ void k32_pflux(const P32 *patches, const TileRef *tiles, int ntiles, 
     const bool col_ok = j >= 0 && j <= V.np;
     const float p = V.mom(j + P.p_pos);
     const float w3 = 1.0f / 48.0f;
-    PRow r0 = prow32(V, t.i0 - 1, p), r1 = prow32(V, t.i0, p), r2 = prow32(V, t.i0 + 1, p);
+    auto prow = [&](float a) -> PRow { return {a, sqrt_ge1(1.0f + p * p + a)}; };
+    const PIn L0 = pload32(V, t.i0 - 1, j, col_ok), L1 = pload32(V, t.i0, j, col_ok);
+    PIn Lnext = pload32(V, t.i0 + 1, j, col_ok);  // face row i+1 of the first row, in flight
+    const PRow r0 = prow(V.asq_at(t.i0 - 1)), r1 = prow(L0.a_hi);
+    PRow r2 = prow(L1.a_hi);
     float amA, fvA, amB, fvB;  // rows i-1 and i
-    pface32(V, t.i0 - 1, j, col_ok, r0, r1, amA, fvA);
-    pface32(V, t.i0, j, col_ok, r1, r2, amB, fvB);
+    pface32(V, t.i0 - 1, col_ok, r0, r1, L0, amA, fvA);
+    pface32(V, t.i0, col_ok, r1, r2, L1, amB, fvB);
     const int rows = min(kStripRows, V.nx + 1 - t.i0);
     for (int r = 0; r < rows; r++) {
         const int i = t.i0 + r;
-        const PRow r3 = prow32(V, i + 2, p);
+        const PIn Lc = Lnext;
+        if (r + 1 < rows) Lnext = pload32(V, i + 2, j, col_ok);  // the next row's inputs
+        const PRow r3 = prow(Lc.a_hi);
         float amC, fvC;  // row i+1
-        pface32(V, i + 1, j, col_ok, r2, r3, amC, fvC);
+        pface32(V, i + 1, col_ok, r2, r3, Lc, amC, fvC);
         const int id = pidx(i, j, V.pit);
         if (col_ok && !(V.ifp && V.ifp[id])) {
             V.FH[id] = V.dpif * (fvB * amB + w3 * (fvC - fvA) * (amC - amA));
