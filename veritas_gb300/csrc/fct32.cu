@@ -269,9 +269,8 @@ __global__ void k32_update(const P32 *patches, const TileRef *tiles) {
 // k32_limR, k32_limC and k32_update.
 constexpr int kLuOut = 30;  // output columns per strip (lanes 1 .. 30)
 
-struct LuRow {  // one row at the lane's column: f0, f2, both antidiffusive fluxes, and on
-               // lanes 0 / 31 f0, f2 (and on lane 31 the p flux) of the cell beyond the warp
-    float f0, f2, dx, dp, s0, s2, sdp;
+struct LuRow {  // one row of the window at the lane's column (and, on lanes 0 / 31, beyond it)
+    float f0, f2, s0, s2;
 };
 
 __global__ void __launch_bounds__(128) k32_limupd(const P32 *patches, const TileRef *tiles, int ntiles) {
@@ -284,26 +283,18 @@ __global__ void __launch_bounds__(128) k32_limupd(const P32 *patches, const Tile
     const P32 &P = patches[t.patch];
     const int pit = P.pitch, nx = P.nx, np = P.np, i0 = t.i0, j0 = t.j0;
     const int jj = j0 - 1 + lane;
-    const int js = lane == 0 ? jj - 1 : jj + 1;  // the cell beyond the warp
-    const bool edge = lane == 0 || lane == 31;
-    const bool colv = jj >= -2 && jj <= np + 1, sidev = edge && js >= -2 && js <= np + 1;
-    const float *F0 = P.f0, *F2 = P.f2, *DX = P.FxDS, *DP = P.FpDS;
+    // the cell beyond the warp: left of lane 0, right of lane 31
+    const int js = lane == 0 ? jj - 1 : jj + 1;
+    auto ld = [&](const float *a, int i, int j) -> float {
+        return (i >= -2 && i <= nx + 1 && j >= -2 && j <= np + 1) ? a[pidx(i, j, pit)] : 0.0f;
+    };
     auto row = [&](int i) -> LuRow {
-        LuRow w{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-        if (i < -2 || i > nx + 1) return w;
-        const int id = pidx(i, jj, pit);
-        if (colv) {
-            w.f0 = F0[id];
-            w.f2 = F2[id];
-            w.dx = DX[id];
-            w.dp = DP[id];
-        }
-        if (sidev) {
-            const int is = pidx(i, js, pit);
-            w.s0 = F0[is];
-            w.s2 = F2[is];
-            w.sdp = DP[is];
-        }
+        LuRow w;
+        w.f0 = ld(P.f0, i, jj);
+        w.f2 = ld(P.f2, i, jj);
+        const bool edge = lane == 0 || lane == 31;
+        w.s0 = edge ? ld(P.f0, i, js) : 0.0f;
+        w.s2 = edge ? ld(P.f2, i, js) : 0.0f;
         return w;
     };
     const uint8_t *lm = P.lmask;
@@ -311,23 +302,24 @@ __global__ void __launch_bounds__(128) k32_limupd(const P32 *patches, const Tile
     // rows and lanes 1..30, plus the ghost ring at the patch's edges
     const int qlo = i0 == 0 ? -1 : i0, qhi = min(i0 + kLuRows, nx + 1);
     const bool own_col = ((lane >= 1 && lane <= kLuOut) || (lane == 0 && j0 == 0)) && jj >= -1 && jj <= np;
-    // window: A = row r-1, B = row r, C = row r+1; N1, N2 = rows r+2, r+3 in flight
-    LuRow A = row(i0 - 2), B = row(i0 - 1), N1 = row(i0), N2 = row(i0 + 1);
+    LuRow A = row(i0 - 2), B = row(i0 - 1);
+    float dA = 0.0f, dB = ld(P.FxDS, i0 - 1, jj);
+    float pA = 0.0f, spA = 0.0f;
     float rpA = 0.0f, rmA = 0.0f, rpB = 0.0f, rmB = 0.0f;
     const int rend = min(i0 + kLuRows, nx + 1);
     for (int r = i0 - 1; r <= rend; r++) {  // warp-uniform
-        const LuRow C = N1;
-        N1 = N2;
-        N2 = row(r + 3);
+        const LuRow C = row(r + 1);
+        const float dC = ld(P.FxDS, r + 1, jj);
+        const float pB = ld(P.FpDS, r, jj);
+        const float spB = lane == 31 ? ld(P.FpDS, r, jj + 1) : 0.0f;
         // R+ / R- of row r (k32_limR), cells i in [-1, nx], j in [-1, np]
         float fl0 = __shfl_up_sync(full, B.f0, 1), fl2 = __shfl_up_sync(full, B.f2, 1);
         float fr0 = __shfl_down_sync(full, B.f0, 1), fr2 = __shfl_down_sync(full, B.f2, 1);
-        float dpn = __shfl_down_sync(full, B.dp, 1);
+        float dpn = __shfl_down_sync(full, pB, 1);
         if (lane == 0) fl0 = B.s0, fl2 = B.s2;
-        if (lane == 31) fr0 = B.s0, fr2 = B.s2, dpn = B.sdp;
+        if (lane == 31) fr0 = B.s0, fr2 = B.s2, dpn = spB;
         float rpC = 0.0f, rmC = 0.0f;
         if (r >= -1 && r <= nx && jj >= -1 && jj <= np) {
-            const float dB = B.dx, dC = C.dx, pB = B.dp;
             const float Pp = fmaxf(0.0f, dB) - fminf(0.0f, dC) + fmaxf(0.0f, pB) - fminf(0.0f, dpn);
             const float Pm = fmaxf(0.0f, dC) - fminf(0.0f, dB) + fmaxf(0.0f, dpn) - fminf(0.0f, pB);
             const float c0 = B.f0, c2 = B.f2;
@@ -338,7 +330,7 @@ __global__ void __launch_bounds__(128) k32_limupd(const P32 *patches, const Tile
             rpC = limiter_ratio(wMax - c2, Pp);
             rmC = limiter_ratio(-wMin + c2, Pm);
         }
-        if (lm && own_col && r >= qlo && r < qhi) {
+        if (lm && own_col && r >= qlo && r < qhi && r <= nx) {
             const int id = pidx(r, jj, pit);
             if (lm[id] & 1) {
                 P.Rp[id] = rpC;
@@ -346,13 +338,12 @@ __global__ void __launch_bounds__(128) k32_limupd(const P32 *patches, const Tile
             }
         }
         // C and the update of row q = r - 1 (k32_limC, k32_update): R of rows q-1, q, q+1
-        // are rpA/rmA, rpB/rmB, rpC/rmC; the fluxes of row q are A's, of row q+1 B's
+        // are rpA/rmA, rpB/rmB, rpC/rmC
         const int q = r - 1;
         const float rpBl = __shfl_up_sync(full, rpB, 1), rmBl = __shfl_up_sync(full, rmB, 1);
         const float rpBr = __shfl_down_sync(full, rpB, 1), rmBr = __shfl_down_sync(full, rmB, 1);
-        const float pAr = __shfl_down_sync(full, A.dp, 1);
+        const float pAr = __shfl_down_sync(full, pA, 1);
         if (own_col && q >= qlo && q < qhi) {
-            const float dA = A.dx, dB = B.dx, pA = A.dp;
             const bool rowin = q >= 1 && q < nx;
             const bool in0 = jj >= 0 && jj < np, in1 = jj + 1 >= 0 && jj + 1 < np;
             const float cxq = (rowin && in0) ? (dA > 0.0f ? fminf(rpB, rmA) : fminf(rpA, rmB)) : 1.0f;
@@ -379,11 +370,16 @@ __global__ void __launch_bounds__(128) k32_limupd(const P32 *patches, const Tile
         }
         A = B;
         B = C;
+        dA = dB;
+        dB = dC;
+        pA = pB;
+        spA = spB;
         rpA = rpB;
         rmA = rmB;
         rpB = rpC;
         rmB = rmC;
     }
+    (void)spA;
 }
 
 // The update of the cells whose faces the limiter exchange rewrote (k32_update's
@@ -492,29 +488,22 @@ __global__ void k32_xflux(const P32 *patches, const TileRef *tiles, int ntiles, 
     const float p0 = mom32(P, jj), p1 = mom32(P, jj + 1);
     const float w3 = 1.0f / 48.0f;
     const unsigned full = 0xffffffffu;
-    // f at rows i-2, i-1, i of the first row (i0 >= 0, so all inside the padded block),
-    // and row i+1 and the first row's a^2 already in flight: each row's loads are issued
-    // one row ahead of their use
-    float fa = 0.0f, fb = 0.0f, fc = 0.0f, fnext = 0.0f;
+    // f at rows i-2, i-1, i of the first row (i0 >= 0, so all inside the padded block)
+    float fa = 0.0f, fb = 0.0f, fc = 0.0f;
     if (col_ok) {
         const int id = pidx(t.i0, jj, pit);
         fa = f[id - 2 * pit];
         fb = f[id - pit];
         fc = f[id];
-        fnext = f[id + pit];  // row i0+1 <= nx+1
     }
-    float anext = asq32(P, F, t.i0);
     for (int r = 0; r < kStripRows; r++) {
         const int i = t.i0 + r;
         if (i > P.nx) break;  // warp-uniform
         const int id = pidx(i, jj, pit);
-        const float fd = fnext, a = anext;
-        if (i + 1 <= P.nx) {  // the next row's loads (row i+2 <= nx+1)
-            if (col_ok) fnext = f[id + 2 * pit];
-            anext = asq32(P, F, i + 1);
-        }
-        float am = 0.0f, fv = 0.0f;
+        float am = 0.0f, fv = 0.0f, fd = 0.0f;
         if (col_ok) {
+            fd = f[id + pit];  // row i+1 <= nx+1
+            const float a = asq32(P, F, i);
             const float g0 = sqrt_ge1(1.0f + p0 * p0 + a), g1 = sqrt_ge1(1.0f + p1 * p1 + a);
             am = P.kxf * __fdividef(P.dpnf * (p1 + p0), g1 + g0);
             fv = weno32(fa, fb, fc, fd, am > 0.0f, P.weno_eps);
@@ -541,30 +530,15 @@ __device__ __forceinline__ PRow prow32(const FluxView &V, int i, float p) {
     const float a = V.asq_at(i);
     return {a, sqrt_ge1(1.0f + p * p + a)};
 }
-// The memory inputs of p-face row i at the lane's column j: a^2 at x-face i+1 (for the
-// row's upper gamma), q E_x of the row, and f at j-2 .. j+1 (zero where the face is
-// outside the reference's range).  Loaded one row ahead of their use.
-struct PIn {
-    float a_hi, qe, f0, f1, f2, f3;
-};
-__device__ __forceinline__ PIn pload32(const FluxView &V, int i, int j, bool col_ok) {
-    PIn L{V.asq_at(i + 1), 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    if (!col_ok || i < -1 || i > V.nx) return L;
-    L.qe = V.qe_at(i);
-    const int id = pidx(i, j, V.pit);
-    L.f0 = V.f[id - 2];
-    L.f1 = V.f[id - 1];
-    L.f2 = V.f[id];
-    L.f3 = V.f[id + 1];
-    return L;
-}
-__device__ __forceinline__ void pface32(const FluxView &V, int i, bool col_ok, const PRow &lo, const PRow &hi,
-                                        const PIn &L, float &am, float &fv) {
+__device__ __forceinline__ void pface32(const FluxView &V, int i, int j, bool col_ok, const PRow &lo,
+                                        const PRow &hi, float &am, float &fv) {
     am = 0.0f;
     fv = 0.0f;
     if (!col_ok || i < -1 || i > V.nx) return;
-    am = L.qe - V.kpf * __fdividef(hi.a - lo.a, hi.g + lo.g);
-    fv = weno32(L.f0, L.f1, L.f2, L.f3, am > 0.0f, V.weno_eps);
+    am = V.qe_at(i) - V.kpf * __fdividef(hi.a - lo.a, hi.g + lo.g);
+    const int id = pidx(i, j, V.pit);
+    const float *f = V.f;
+    fv = weno32(f[id - 2], f[id - 1], f[id], f[id + 1], am > 0.0f, V.weno_eps);
 }
 
 __global__ void k32_pflux(const P32 *patches, const TileRef *tiles, int ntiles, const RunFields *fields, int step,
@@ -580,22 +554,16 @@ __global__ void k32_pflux(const P32 *patches, const TileRef *tiles, int ntiles, 
     const bool col_ok = j >= 0 && j <= V.np;
     const float p = V.mom(j + P.p_pos);
     const float w3 = 1.0f / 48.0f;
-    auto prow = [&](float a) -> PRow { return {a, sqrt_ge1(1.0f + p * p + a)}; };
-    const PIn L0 = pload32(V, t.i0 - 1, j, col_ok), L1 = pload32(V, t.i0, j, col_ok);
-    PIn Lnext = pload32(V, t.i0 + 1, j, col_ok);  // face row i+1 of the first row, in flight
-    const PRow r0 = prow(V.asq_at(t.i0 - 1)), r1 = prow(L0.a_hi);
-    PRow r2 = prow(L1.a_hi);
+    PRow r0 = prow32(V, t.i0 - 1, p), r1 = prow32(V, t.i0, p), r2 = prow32(V, t.i0 + 1, p);
     float amA, fvA, amB, fvB;  // rows i-1 and i
-    pface32(V, t.i0 - 1, col_ok, r0, r1, L0, amA, fvA);
-    pface32(V, t.i0, col_ok, r1, r2, L1, amB, fvB);
+    pface32(V, t.i0 - 1, j, col_ok, r0, r1, amA, fvA);
+    pface32(V, t.i0, j, col_ok, r1, r2, amB, fvB);
     const int rows = min(kStripRows, V.nx + 1 - t.i0);
     for (int r = 0; r < rows; r++) {
         const int i = t.i0 + r;
-        const PIn Lc = Lnext;
-        if (r + 1 < rows) Lnext = pload32(V, i + 2, j, col_ok);  // the next row's inputs
-        const PRow r3 = prow(Lc.a_hi);
+        const PRow r3 = prow32(V, i + 2, p);
         float amC, fvC;  // row i+1
-        pface32(V, i + 1, col_ok, r2, r3, Lc, amC, fvC);
+        pface32(V, i + 1, j, col_ok, r2, r3, amC, fvC);
         const int id = pidx(i, j, V.pit);
         if (col_ok && !(V.ifp && V.ifp[id])) {
             V.FH[id] = V.dpif * (fvB * amB + w3 * (fvC - fvA) * (amC - amA));

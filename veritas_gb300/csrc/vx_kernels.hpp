@@ -63,7 +63,7 @@ enum FctSub : int {
     kSubLimUpd,
     kSubLateUpd,
 };
-constexpr int kLuRows = 16;  // rows per strip of the fused FP32 limiter + update kernel (30 p cells wide)
+constexpr int kLuRows = 32;  // rows per strip of the fused FP32 limiter + update kernel (30 p cells wide)
 
 struct FctLaunch {
     const void *patches;  // device array of PatchT<T>
