@@ -784,7 +784,7 @@ void Engine::build_tiles(LaunchSet &L) {
         L.nptiles = (int)pt.size();
         L.dxtiles = upload(xt, stream);
         L.dptiles = upload(pt, stream);
-        // fused limiter + update: strips, and the set's late-update cells
+        // fused limiter + update: interior tiles, and the set's late-update cells
         std::vector<TileRef> lu, late;
         pi = 0;
         for (Run *R : L.runs) {
@@ -792,9 +792,8 @@ void Engine::build_tiles(LaunchSet &L) {
             for (auto &sp : R->rects)
                 for (auto &lvl : sp)
                     for (auto &rp : lvl) {
-                        // strips up to row nx and column np: the last ones own the ghost ring
-                        for (int i0 = 0; i0 <= rp->n_x; i0 += kLuRows)
-                            for (int j0 = 0; j0 <= rp->n_p; j0 += 30) lu.push_back({pi, i0, j0});
+                        for (int i0 = 0; i0 < rp->n_x; i0 += kLuRows)
+                            for (int j0 = 0; j0 < rp->n_p; j0 += kLuCols) lu.push_back({pi, i0, j0});
                         pi++;
                     }
             for (const TileRef &c : R->late_cells) late.push_back({base + c.patch, c.i0, c.j0});

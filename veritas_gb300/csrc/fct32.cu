@@ -256,130 +256,133 @@ __global__ void k32_update(const P32 *patches, const TileRef *tiles) {
 }
 
 // ---------------------------------------------------------------- fused limiter + update
-// Sub-steps 1 and 2 of Rectangle::FCTTimeStep (Rectangle.cpp:1536-1612) in one pass.  A
-// warp owns a strip of kLuRows rows by 30 p cells: lane l holds column j0-1+l and walks
-// down the strip with a sliding window of rows in registers (f0 and f2 of three rows,
-// the x-direction antidiffusive fluxes of three, the p-direction ones of two, R+ / R- of
-// three), its p neighbours through shuffles (lanes 0 and 31 load the cell beyond the
-// warp themselves).  Per row it forms R+ / R- of row r, then C and the update of row
-// r-1, so every plane is read once and only f1 is written; the R and C planes are
-// written only where the limiter exchange between patches (PushBoundaryC) needs them
-// (the patch's lmask), and the update of a cell beside a face the exchange rewrites is
-// left to k32_late_update, which runs after the exchange.  The arithmetic is that of
-// k32_limR, k32_limC and k32_update.
-constexpr int kLuOut = 30;  // output columns per strip (lanes 1 .. 30)
+// Sub-steps 1 and 2 of Rectangle::FCTTimeStep (Rectangle.cpp:1536-1612) in one pass: a
+// block stages f0, f2 and the antidiffusive fluxes of a kLuRows x kLuCols tile and its
+// halo in shared memory (aligned 128-bit loads), forms R+ / R- on the tile and a one-cell
+// ring, the face coefficients C from them, and the update of the tile's cells; the R and
+// C planes are not written, except where the limiter exchange between patches
+// (PushBoundaryC) needs them (the patch's lmask): there R and the cell's face C go to
+// memory and the cell's update is left to k32_late_update, which runs after the
+// exchange.  The arithmetic is that of k32_limR, k32_limC and k32_update.
+constexpr int kLuW = kLuCols + 4;  // shared row: p cells j0-2 .. j0+kLuCols+1
 
-struct LuRow {  // one row of the window at the lane's column (and, on lanes 0 / 31, beyond it)
-    float f0, f2, s0, s2;
+size_t limupd_smem_bytes() { return sizeof(float) * (size_t)kLuW * (6 * kLuRows + 17); }
+
+struct LuTile {
+    const float *sf0, *sf2, *sdx, *sdp, *srp, *srm;
+    int i0, j0, nx, np;
+    // element (i, j) of an array whose first shared row is row `r0`
+    __device__ __forceinline__ int at(int i, int j, int r0) const { return (i - r0) * kLuW + (j - (j0 - 2)); }
+    __device__ __forceinline__ float F0(int i, int j) const { return sf0[at(i, j, i0 - 2)]; }
+    __device__ __forceinline__ float F2(int i, int j) const { return sf2[at(i, j, i0 - 2)]; }
+    __device__ __forceinline__ float DX(int i, int j) const { return sdx[at(i, j, i0 - 1)]; }
+    __device__ __forceinline__ float DP(int i, int j) const { return sdp[at(i, j, i0 - 1)]; }
+    __device__ __forceinline__ float RP(int i, int j) const { return srp[at(i, j, i0 - 1)]; }
+    __device__ __forceinline__ float RM(int i, int j) const { return srm[at(i, j, i0 - 1)]; }
+    // C of x-face i / p-face j (k32_limC: 1 outside i in [1, nx), j in [0, np))
+    __device__ __forceinline__ float cx(int i, int j) const {
+        if (!(i >= 1 && i < nx && j >= 0 && j < np)) return 1.0f;
+        return DX(i, j) > 0.0f ? fminf(RP(i, j), RM(i - 1, j)) : fminf(RP(i - 1, j), RM(i, j));
+    }
+    __device__ __forceinline__ float cp(int i, int j) const {
+        if (!(i >= 1 && i < nx && j >= 0 && j < np)) return 1.0f;
+        return DP(i, j) > 0.0f ? fminf(RP(i, j), RM(i, j - 1)) : fminf(RP(i, j - 1), RM(i, j));
+    }
 };
 
-__global__ void __launch_bounds__(128) k32_limupd(const P32 *patches, const TileRef *tiles, int ntiles) {
+__global__ void __launch_bounds__(256) k32_limupd(const P32 *patches, const TileRef *tiles) {
     VX_PDL_WAIT();
-    const int wt = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (wt >= ntiles) return;
-    const int lane = threadIdx.x & 31;
-    const unsigned full = 0xffffffffu;
-    const TileRef t = tiles[wt];
+    extern __shared__ __align__(16) float lu_sm[];
+    const TileRef t = tiles[blockIdx.x];
     const P32 &P = patches[t.patch];
-    const int pit = P.pitch, nx = P.nx, np = P.np, i0 = t.i0, j0 = t.j0;
-    const int jj = j0 - 1 + lane;
-    // the cell beyond the warp: left of lane 0, right of lane 31
-    const int js = lane == 0 ? jj - 1 : jj + 1;
-    auto ld = [&](const float *a, int i, int j) -> float {
-        return (i >= -2 && i <= nx + 1 && j >= -2 && j <= np + 1) ? a[pidx(i, j, pit)] : 0.0f;
+    const int pit = P.pitch;
+    LuTile T;
+    T.i0 = t.i0;
+    T.j0 = t.j0;
+    T.nx = P.nx;
+    T.np = P.np;
+    float *sf0 = lu_sm, *sf2 = sf0 + (kLuRows + 4) * kLuW, *sdx = sf2 + (kLuRows + 4) * kLuW;
+    float *sdp = sdx + (kLuRows + 3) * kLuW, *srp = sdp + (kLuRows + 2) * kLuW, *srm = srp + (kLuRows + 2) * kLuW;
+    T.sf0 = sf0, T.sf2 = sf2, T.sdx = sdx, T.sdp = sdp, T.srp = srp, T.srm = srm;
+    // rows [r0, r0 + nrows) of a plane, p cells j0-2 .. j0+kLuCols+1 as aligned float4
+    // (their first cell j0-2 sits at column j0 of the pitched row, a multiple of 4); rows
+    // outside the padded block and segments past the row's pitch are not read
+    auto load = [&](float *dst, const float *src, int r0, int nrows) {
+        constexpr int nch = kLuW / 4;
+        for (int q = threadIdx.x; q < nrows * nch; q += blockDim.x) {
+            const int rr = q / nch, c = q - rr * nch;
+            const int i = r0 + rr, col = T.j0 + 4 * c;
+            if (i < -2 || i > T.nx + 1 || col >= pit) continue;
+            *reinterpret_cast<float4 *>(dst + rr * kLuW + 4 * c) =
+                *reinterpret_cast<const float4 *>(src + (size_t)(i + 2) * pit + col);
+        }
     };
-    auto row = [&](int i) -> LuRow {
-        LuRow w;
-        w.f0 = ld(P.f0, i, jj);
-        w.f2 = ld(P.f2, i, jj);
-        const bool edge = lane == 0 || lane == 31;
-        w.s0 = edge ? ld(P.f0, i, js) : 0.0f;
-        w.s2 = edge ? ld(P.f2, i, js) : 0.0f;
-        return w;
-    };
-    const uint8_t *lm = P.lmask;
-    // rows and columns this strip owns (outputs, and the R / C the exchange reads): its
-    // rows and lanes 1..30, plus the ghost ring at the patch's edges
-    const int qlo = i0 == 0 ? -1 : i0, qhi = min(i0 + kLuRows, nx + 1);
-    const bool own_col = ((lane >= 1 && lane <= kLuOut) || (lane == 0 && j0 == 0)) && jj >= -1 && jj <= np;
-    LuRow A = row(i0 - 2), B = row(i0 - 1);
-    float dA = 0.0f, dB = ld(P.FxDS, i0 - 1, jj);
-    float pA = 0.0f, spA = 0.0f;
-    float rpA = 0.0f, rmA = 0.0f, rpB = 0.0f, rmB = 0.0f;
-    const int rend = min(i0 + kLuRows, nx + 1);
-    for (int r = i0 - 1; r <= rend; r++) {  // warp-uniform
-        const LuRow C = row(r + 1);
-        const float dC = ld(P.FxDS, r + 1, jj);
-        const float pB = ld(P.FpDS, r, jj);
-        const float spB = lane == 31 ? ld(P.FpDS, r, jj + 1) : 0.0f;
-        // R+ / R- of row r (k32_limR), cells i in [-1, nx], j in [-1, np]
-        float fl0 = __shfl_up_sync(full, B.f0, 1), fl2 = __shfl_up_sync(full, B.f2, 1);
-        float fr0 = __shfl_down_sync(full, B.f0, 1), fr2 = __shfl_down_sync(full, B.f2, 1);
-        float dpn = __shfl_down_sync(full, pB, 1);
-        if (lane == 0) fl0 = B.s0, fl2 = B.s2;
-        if (lane == 31) fr0 = B.s0, fr2 = B.s2, dpn = spB;
-        float rpC = 0.0f, rmC = 0.0f;
-        if (r >= -1 && r <= nx && jj >= -1 && jj <= np) {
-            const float Pp = fmaxf(0.0f, dB) - fminf(0.0f, dC) + fmaxf(0.0f, pB) - fminf(0.0f, dpn);
-            const float Pm = fmaxf(0.0f, dC) - fminf(0.0f, dB) + fmaxf(0.0f, dpn) - fminf(0.0f, pB);
-            const float c0 = B.f0, c2 = B.f2;
-            const float wMax = fmaxf(fmaxf(c0, c2), fmaxf(fmaxf(C.f0, C.f2), fmaxf(fmaxf(A.f0, A.f2),
-                               fmaxf(fmaxf(fr0, fr2), fmaxf(fl0, fl2)))));
-            const float wMin = fminf(fminf(c0, c2), fminf(fminf(C.f0, C.f2), fminf(fminf(A.f0, A.f2),
-                               fminf(fminf(fr0, fr2), fminf(fl0, fl2)))));
-            rpC = limiter_ratio(wMax - c2, Pp);
-            rmC = limiter_ratio(-wMin + c2, Pm);
+    load(sf0, P.f0, T.i0 - 2, kLuRows + 4);
+    load(sf2, P.f2, T.i0 - 2, kLuRows + 4);
+    load(sdx, P.FxDS, T.i0 - 1, kLuRows + 3);
+    load(sdp, P.FpDS, T.i0 - 1, kLuRows + 2);
+    __syncthreads();
+    // R+ and R- (k32_limR) on rows i0-1 .. i0+kLuRows, cells j0-1 .. j0+kLuCols, inside
+    // the limiter's cell range i in [-1, nx], j in [-1, np]
+    constexpr int rcols = kLuCols + 2;
+    for (int q = threadIdx.x; q < (kLuRows + 2) * rcols; q += blockDim.x) {
+        const int rr = q / rcols, cc = q - rr * rcols;
+        const int i = T.i0 - 1 + rr, j = T.j0 - 1 + cc;
+        const int o = T.at(i, j, T.i0 - 1);
+        if (i < -1 || i > T.nx || j < -1 || j > T.np) {
+            srp[o] = 0.0f;
+            srm[o] = 0.0f;
+            continue;
         }
-        if (lm && own_col && r >= qlo && r < qhi && r <= nx) {
-            const int id = pidx(r, jj, pit);
-            if (lm[id] & 1) {
-                P.Rp[id] = rpC;
-                P.Rm[id] = rmC;
-            }
-        }
-        // C and the update of row q = r - 1 (k32_limC, k32_update): R of rows q-1, q, q+1
-        // are rpA/rmA, rpB/rmB, rpC/rmC
-        const int q = r - 1;
-        const float rpBl = __shfl_up_sync(full, rpB, 1), rmBl = __shfl_up_sync(full, rmB, 1);
-        const float rpBr = __shfl_down_sync(full, rpB, 1), rmBr = __shfl_down_sync(full, rmB, 1);
-        const float pAr = __shfl_down_sync(full, pA, 1);
-        if (own_col && q >= qlo && q < qhi) {
-            const bool rowin = q >= 1 && q < nx;
-            const bool in0 = jj >= 0 && jj < np, in1 = jj + 1 >= 0 && jj + 1 < np;
-            const float cxq = (rowin && in0) ? (dA > 0.0f ? fminf(rpB, rmA) : fminf(rpA, rmB)) : 1.0f;
-            const bool rowin1 = q + 1 >= 1 && q + 1 < nx;
-            const float cxq1 = (rowin1 && in0) ? (dB > 0.0f ? fminf(rpC, rmB) : fminf(rpB, rmC)) : 1.0f;
-            const float cpq = (rowin && in0) ? (pA > 0.0f ? fminf(rpB, rmBl) : fminf(rpBl, rmB)) : 1.0f;
-            const float cpq1 = (rowin && in1) ? (pAr > 0.0f ? fminf(rpBr, rmB) : fminf(rpB, rmBr)) : 1.0f;
-            const int id = pidx(q, jj, pit);
-            const uint8_t m = lm ? lm[id] : 0;
-            if (q >= 0 && q < nx && in0 && !(m & 2)) {
-                float v = A.f2;
-                if (active32(P, q, jj)) v += cxq * dA;
-                if (active32(P, q, jj)) v += cpq * pA;
-                if (active32(P, q, jj + 1)) v -= cpq1 * pAr;
-                if (active32(P, q + 1, jj)) v -= cxq1 * dB;
-                P.f1[id] = v;
-            }
-            if (m & 2) {
-                P.Cx[id] = cxq;
-                P.Cx[id + pit] = cxq1;
-                P.Cp[id] = cpq;
-                P.Cp[id + 1] = cpq1;
-            }
-        }
-        A = B;
-        B = C;
-        dA = dB;
-        dB = dC;
-        pA = pB;
-        spA = spB;
-        rpA = rpB;
-        rmA = rmB;
-        rpB = rpC;
-        rmB = rmC;
+        const float dxi = T.DX(i, j), dxn = T.DX(i + 1, j), dpi = T.DP(i, j), dpn = T.DP(i, j + 1);
+        const float Pp = fmaxf(0.0f, dxi) - fminf(0.0f, dxn) + fmaxf(0.0f, dpi) - fminf(0.0f, dpn);
+        const float Pm = fmaxf(0.0f, dxn) - fminf(0.0f, dxi) + fmaxf(0.0f, dpn) - fminf(0.0f, dpi);
+        const float c0 = T.F0(i, j), c2 = T.F2(i, j);
+        const float u0 = T.F0(i + 1, j), u2 = T.F2(i + 1, j), d0 = T.F0(i - 1, j), d2 = T.F2(i - 1, j);
+        const float rf0 = T.F0(i, j + 1), rf2 = T.F2(i, j + 1), lf0 = T.F0(i, j - 1), lf2 = T.F2(i, j - 1);
+        const float wMax = fmaxf(fmaxf(c0, c2), fmaxf(fmaxf(u0, u2), fmaxf(fmaxf(d0, d2), fmaxf(fmaxf(rf0, rf2), fmaxf(lf0, lf2)))));
+        const float wMin = fminf(fminf(c0, c2), fminf(fminf(u0, u2), fminf(fminf(d0, d2), fminf(fminf(rf0, rf2), fminf(lf0, lf2)))));
+        srp[o] = limiter_ratio(wMax - c2, Pp);
+        srm[o] = limiter_ratio(-wMin + c2, Pm);
     }
-    (void)spA;
+    __syncthreads();
+    // the antidiffusive update (k32_update) of the tile's interior cells
+    for (int q = threadIdx.x; q < kLuRows * kLuCols; q += blockDim.x) {
+        const int rr = q / kLuCols, cc = q - rr * kLuCols;
+        const int i = T.i0 + rr, j = T.j0 + cc;
+        if (i >= T.nx || j >= T.np) continue;
+        const int id = pidx(i, j, pit);
+        if (P.lmask && (P.lmask[id] & 2)) continue;  // after the exchange (k32_late_update)
+        float v = T.F2(i, j);
+        if (active32(P, i, j)) v += T.cx(i, j) * T.DX(i, j);
+        if (active32(P, i, j)) v += T.cp(i, j) * T.DP(i, j);
+        if (active32(P, i, j + 1)) v -= T.cp(i, j + 1) * T.DP(i, j + 1);
+        if (active32(P, i + 1, j)) v -= T.cx(i + 1, j) * T.DX(i + 1, j);
+        P.f1[id] = v;
+    }
+    if (!P.lmask) return;
+    // what the limiter exchange reads: R of the cells it compares, C of the faces it
+    // rewrites (both faces of each such cell in each direction); a tile owns its cells
+    // plus, at the patch's edges, the ghost ring the exchange reaches
+    const int ilo = T.i0 == 0 ? -1 : T.i0, ihi = T.i0 + kLuRows >= T.nx ? T.nx + 1 : T.i0 + kLuRows;
+    const int jlo = T.j0 == 0 ? -1 : T.j0, jhi = T.j0 + kLuCols >= T.np ? T.np + 1 : T.j0 + kLuCols;
+    const int ow = jhi - jlo;
+    for (int q = threadIdx.x; q < (ihi - ilo) * ow; q += blockDim.x) {
+        const int rr = q / ow;
+        const int i = ilo + rr, j = jlo + (q - rr * ow);
+        const int id = pidx(i, j, pit);
+        const uint8_t m = P.lmask[id];
+        if (m & 1) {
+            P.Rp[id] = T.RP(i, j);
+            P.Rm[id] = T.RM(i, j);
+        }
+        if (m & 2) {
+            P.Cx[id] = T.cx(i, j);
+            P.Cx[id + pit] = T.cx(i + 1, j);
+            P.Cp[id] = T.cp(i, j);
+            P.Cp[id + 1] = T.cp(i, j + 1);
+        }
+    }
 }
 
 // The update of the cells whose faces the limiter exchange rewrote (k32_update's
@@ -605,7 +608,11 @@ void launch_fct32_substep(const FctLaunch &L, int sub) {
             if (L.nptiles) vx_launch(k32_pflux, (L.nptiles + 3) / 4, 128, 0, L.stream, pp, L.ptiles, L.nptiles, L.fields, L.step, L.use_f0);
             break;
         case kSubLimUpd:
-            if (L.nlutiles) vx_launch(k32_limupd, (L.nlutiles + 3) / 4, 128, 0, L.stream, pp, L.lutiles, L.nlutiles);
+            if (L.nlutiles) {
+                const size_t sm = limupd_smem_bytes();
+                cudaFuncSetAttribute(k32_limupd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                vx_launch(k32_limupd, L.nlutiles, 256, sm, L.stream, pp, L.lutiles);
+            }
             break;
         case kSubLateUpd:
             if (L.nlate) vx_launch(k32_late_update, (L.nlate + 127) / 128, 128, 0, L.stream, pp, L.late, L.nlate);

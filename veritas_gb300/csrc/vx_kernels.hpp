@@ -63,7 +63,8 @@ enum FctSub : int {
     kSubLimUpd,
     kSubLateUpd,
 };
-constexpr int kLuRows = 32;  // rows per strip of the fused FP32 limiter + update kernel (30 p cells wide)
+constexpr int kLuRows = 16;   // tile rows of the fused FP32 limiter + update kernel
+constexpr int kLuCols = 128;  // tile p cells (one float4-aligned row segment + halo)
 
 struct FctLaunch {
     const void *patches;  // device array of PatchT<T>
@@ -79,9 +80,8 @@ struct FctLaunch {
     // FP32 fused face + flux kernels: one warp per strip tile
     const TileRef *xtiles, *ptiles;
     int nxtiles, nptiles;
-    // FP32 fused limiter + update: strips of kLuRows x 30 cells (one warp each; i0 in
-    // [0, nx], j0 in [0, np]) and the cells whose update waits for the limiter exchange
-    // (i0, j0 = the cell)
+    // FP32 fused limiter + update: interior tiles (i0, j0 multiples of kLuRows, kLuCols)
+    // and the cells whose update waits for the limiter exchange (i0, j0 = the cell)
     const TileRef *lutiles, *late;
     int nlutiles, nlate;
     cudaStream_t stream;
