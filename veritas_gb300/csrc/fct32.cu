@@ -255,153 +255,6 @@ __global__ void k32_update(const P32 *patches, const TileRef *tiles) {
     st4(P.f1 + id, out, j, 0, P.np);
 }
 
-// ---------------------------------------------------------------- fused limiter + update
-// Sub-steps 1 and 2 of Rectangle::FCTTimeStep (Rectangle.cpp:1536-1612) in one pass: a
-// block stages f0, f2 and the antidiffusive fluxes of a kLuRows x kLuCols tile and its
-// halo in shared memory (aligned 128-bit loads), forms R+ / R- on the tile and a one-cell
-// ring, the face coefficients C from them, and the update of the tile's cells; the R and
-// C planes are not written, except where the limiter exchange between patches
-// (PushBoundaryC) needs them (the patch's lmask): there R and the cell's face C go to
-// memory and the cell's update is left to k32_late_update, which runs after the
-// exchange.  The arithmetic is that of k32_limR, k32_limC and k32_update.
-constexpr int kLuW = kLuCols + 4;  // shared row: p cells j0-2 .. j0+kLuCols+1
-
-size_t limupd_smem_bytes() { return sizeof(float) * (size_t)kLuW * (6 * kLuRows + 17); }
-
-struct LuTile {
-    const float *sf0, *sf2, *sdx, *sdp, *srp, *srm;
-    int i0, j0, nx, np;
-    // element (i, j) of an array whose first shared row is row `r0`
-    __device__ __forceinline__ int at(int i, int j, int r0) const { return (i - r0) * kLuW + (j - (j0 - 2)); }
-    __device__ __forceinline__ float F0(int i, int j) const { return sf0[at(i, j, i0 - 2)]; }
-    __device__ __forceinline__ float F2(int i, int j) const { return sf2[at(i, j, i0 - 2)]; }
-    __device__ __forceinline__ float DX(int i, int j) const { return sdx[at(i, j, i0 - 1)]; }
-    __device__ __forceinline__ float DP(int i, int j) const { return sdp[at(i, j, i0 - 1)]; }
-    __device__ __forceinline__ float RP(int i, int j) const { return srp[at(i, j, i0 - 1)]; }
-    __device__ __forceinline__ float RM(int i, int j) const { return srm[at(i, j, i0 - 1)]; }
-    // C of x-face i / p-face j (k32_limC: 1 outside i in [1, nx), j in [0, np))
-    __device__ __forceinline__ float cx(int i, int j) const {
-        if (!(i >= 1 && i < nx && j >= 0 && j < np)) return 1.0f;
-        return DX(i, j) > 0.0f ? fminf(RP(i, j), RM(i - 1, j)) : fminf(RP(i - 1, j), RM(i, j));
-    }
-    __device__ __forceinline__ float cp(int i, int j) const {
-        if (!(i >= 1 && i < nx && j >= 0 && j < np)) return 1.0f;
-        return DP(i, j) > 0.0f ? fminf(RP(i, j), RM(i, j - 1)) : fminf(RP(i, j - 1), RM(i, j));
-    }
-};
-
-__global__ void __launch_bounds__(256) k32_limupd(const P32 *patches, const TileRef *tiles) {
-    VX_PDL_WAIT();
-    extern __shared__ __align__(16) float lu_sm[];
-    const TileRef t = tiles[blockIdx.x];
-    const P32 &P = patches[t.patch];
-    const int pit = P.pitch;
-    LuTile T;
-    T.i0 = t.i0;
-    T.j0 = t.j0;
-    T.nx = P.nx;
-    T.np = P.np;
-    float *sf0 = lu_sm, *sf2 = sf0 + (kLuRows + 4) * kLuW, *sdx = sf2 + (kLuRows + 4) * kLuW;
-    float *sdp = sdx + (kLuRows + 3) * kLuW, *srp = sdp + (kLuRows + 2) * kLuW, *srm = srp + (kLuRows + 2) * kLuW;
-    T.sf0 = sf0, T.sf2 = sf2, T.sdx = sdx, T.sdp = sdp, T.srp = srp, T.srm = srm;
-    // rows [r0, r0 + nrows) of a plane, p cells j0-2 .. j0+kLuCols+1 as aligned float4
-    // (their first cell j0-2 sits at column j0 of the pitched row, a multiple of 4); rows
-    // outside the padded block and segments past the row's pitch are not read
-    auto load = [&](float *dst, const float *src, int r0, int nrows) {
-        constexpr int nch = kLuW / 4;
-        for (int q = threadIdx.x; q < nrows * nch; q += blockDim.x) {
-            const int rr = q / nch, c = q - rr * nch;
-            const int i = r0 + rr, col = T.j0 + 4 * c;
-            if (i < -2 || i > T.nx + 1 || col >= pit) continue;
-            *reinterpret_cast<float4 *>(dst + rr * kLuW + 4 * c) =
-                *reinterpret_cast<const float4 *>(src + (size_t)(i + 2) * pit + col);
-        }
-    };
-    load(sf0, P.f0, T.i0 - 2, kLuRows + 4);
-    load(sf2, P.f2, T.i0 - 2, kLuRows + 4);
-    load(sdx, P.FxDS, T.i0 - 1, kLuRows + 3);
-    load(sdp, P.FpDS, T.i0 - 1, kLuRows + 2);
-    __syncthreads();
-    // R+ and R- (k32_limR) on rows i0-1 .. i0+kLuRows, cells j0-1 .. j0+kLuCols, inside
-    // the limiter's cell range i in [-1, nx], j in [-1, np]
-    constexpr int rcols = kLuCols + 2;
-    for (int q = threadIdx.x; q < (kLuRows + 2) * rcols; q += blockDim.x) {
-        const int rr = q / rcols, cc = q - rr * rcols;
-        const int i = T.i0 - 1 + rr, j = T.j0 - 1 + cc;
-        const int o = T.at(i, j, T.i0 - 1);
-        if (i < -1 || i > T.nx || j < -1 || j > T.np) {
-            srp[o] = 0.0f;
-            srm[o] = 0.0f;
-            continue;
-        }
-        const float dxi = T.DX(i, j), dxn = T.DX(i + 1, j), dpi = T.DP(i, j), dpn = T.DP(i, j + 1);
-        const float Pp = fmaxf(0.0f, dxi) - fminf(0.0f, dxn) + fmaxf(0.0f, dpi) - fminf(0.0f, dpn);
-        const float Pm = fmaxf(0.0f, dxn) - fminf(0.0f, dxi) + fmaxf(0.0f, dpn) - fminf(0.0f, dpi);
-        const float c0 = T.F0(i, j), c2 = T.F2(i, j);
-        const float u0 = T.F0(i + 1, j), u2 = T.F2(i + 1, j), d0 = T.F0(i - 1, j), d2 = T.F2(i - 1, j);
-        const float rf0 = T.F0(i, j + 1), rf2 = T.F2(i, j + 1), lf0 = T.F0(i, j - 1), lf2 = T.F2(i, j - 1);
-        const float wMax = fmaxf(fmaxf(c0, c2), fmaxf(fmaxf(u0, u2), fmaxf(fmaxf(d0, d2), fmaxf(fmaxf(rf0, rf2), fmaxf(lf0, lf2)))));
-        const float wMin = fminf(fminf(c0, c2), fminf(fminf(u0, u2), fminf(fminf(d0, d2), fminf(fminf(rf0, rf2), fminf(lf0, lf2)))));
-        srp[o] = limiter_ratio(wMax - c2, Pp);
-        srm[o] = limiter_ratio(-wMin + c2, Pm);
-    }
-    __syncthreads();
-    // the antidiffusive update (k32_update) of the tile's interior cells
-    for (int q = threadIdx.x; q < kLuRows * kLuCols; q += blockDim.x) {
-        const int rr = q / kLuCols, cc = q - rr * kLuCols;
-        const int i = T.i0 + rr, j = T.j0 + cc;
-        if (i >= T.nx || j >= T.np) continue;
-        const int id = pidx(i, j, pit);
-        if (P.lmask && (P.lmask[id] & 2)) continue;  // after the exchange (k32_late_update)
-        float v = T.F2(i, j);
-        if (active32(P, i, j)) v += T.cx(i, j) * T.DX(i, j);
-        if (active32(P, i, j)) v += T.cp(i, j) * T.DP(i, j);
-        if (active32(P, i, j + 1)) v -= T.cp(i, j + 1) * T.DP(i, j + 1);
-        if (active32(P, i + 1, j)) v -= T.cx(i + 1, j) * T.DX(i + 1, j);
-        P.f1[id] = v;
-    }
-    if (!P.lmask) return;
-    // what the limiter exchange reads: R of the cells it compares, C of the faces it
-    // rewrites (both faces of each such cell in each direction); a tile owns its cells
-    // plus, at the patch's edges, the ghost ring the exchange reaches
-    const int ilo = T.i0 == 0 ? -1 : T.i0, ihi = T.i0 + kLuRows >= T.nx ? T.nx + 1 : T.i0 + kLuRows;
-    const int jlo = T.j0 == 0 ? -1 : T.j0, jhi = T.j0 + kLuCols >= T.np ? T.np + 1 : T.j0 + kLuCols;
-    const int ow = jhi - jlo;
-    for (int q = threadIdx.x; q < (ihi - ilo) * ow; q += blockDim.x) {
-        const int rr = q / ow;
-        const int i = ilo + rr, j = jlo + (q - rr * ow);
-        const int id = pidx(i, j, pit);
-        const uint8_t m = P.lmask[id];
-        if (m & 1) {
-            P.Rp[id] = T.RP(i, j);
-            P.Rm[id] = T.RM(i, j);
-        }
-        if (m & 2) {
-            P.Cx[id] = T.cx(i, j);
-            P.Cx[id + pit] = T.cx(i + 1, j);
-            P.Cp[id] = T.cp(i, j);
-            P.Cp[id + 1] = T.cp(i, j + 1);
-        }
-    }
-}
-
-// The update of the cells whose faces the limiter exchange rewrote (k32_update's
-// arithmetic on the C planes).
-__global__ void k32_late_update(const P32 *patches, const TileRef *cells, int n) {
-    VX_PDL_WAIT();
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const TileRef c = cells[k];
-    const P32 &P = patches[c.patch];
-    const int i = c.i0, j = c.j0, pit = P.pitch, id = pidx(i, j, pit);
-    float v = P.f2[id];
-    if (active32(P, i, j)) v += P.Cx[id] * P.FxDS[id];
-    if (active32(P, i, j)) v += P.Cp[id] * P.FpDS[id];
-    if (active32(P, i, j + 1)) v -= P.Cp[id + 1] * P.FpDS[id + 1];
-    if (active32(P, i + 1, j)) v -= P.Cx[id + pit] * P.FxDS[id + pit];
-    P.f1[id] = v;
-}
-
 // f0 = f1 over the padded block (Rectangle.cpp:1614-1621).
 __global__ void k32_copy10(const P32 *patches, const TileRef *tiles) {
     VX_PDL_WAIT();
@@ -606,16 +459,6 @@ void launch_fct32_substep(const FctLaunch &L, int sub) {
             break;
         case kSubPFlux:
             if (L.nptiles) vx_launch(k32_pflux, (L.nptiles + 3) / 4, 128, 0, L.stream, pp, L.ptiles, L.nptiles, L.fields, L.step, L.use_f0);
-            break;
-        case kSubLimUpd:
-            if (L.nlutiles) {
-                const size_t sm = limupd_smem_bytes();
-                cudaFuncSetAttribute(k32_limupd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-                vx_launch(k32_limupd, L.nlutiles, 256, sm, L.stream, pp, L.lutiles);
-            }
-            break;
-        case kSubLateUpd:
-            if (L.nlate) vx_launch(k32_late_update, (L.nlate + 127) / 128, 128, 0, L.stream, pp, L.late, L.nlate);
             break;
         default:  // the FP32 form has no separate gamma / face / flux sub-steps (fused above)
             break;
