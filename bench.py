@@ -321,7 +321,7 @@ def measure_form(ctx, init_path: Path, steps: int, warmup: int, variant: dict, d
     # E_x is normalised by the laser's field amplitude a0 m c omega / |q| (near t = 0 the
     # plasma is neutral and E_x itself is rounding noise, so a relative error means nothing)
     e0 = p32.a0 * 9.10938291e-31 * 299792458.0 * (2 * np.pi * 299792458.0 / p32.lambda_) / 1.60217657e-19
-    ew = ee = ey = 0.0
+    ew = ee = ey = exr = 0.0
     for _ in range(steps):
         dt = a.CalculateDt()
         a.Advance(dt)
@@ -330,6 +330,7 @@ def measure_form(ctx, init_path: Path, steps: int, warmup: int, variant: dict, d
         ew = max(ew, abs(wb - wa) / max(abs(wa), 1e-300))
         xa, xb = a.field("Ex"), b.field("Ex")
         ee = max(ee, float(np.max(np.abs(xb - xa))) / e0)
+        exr = max(exr, float(np.max(np.abs(xb - xa))) / max(float(np.max(np.abs(xa))), 1e-300))
         ya, yb = a.field("Ey"), b.field("Ey")
         ey = max(ey, float(np.max(np.abs(yb - ya))) / e0)
     with tempfile.TemporaryDirectory() as td:
@@ -347,7 +348,7 @@ def measure_form(ctx, init_path: Path, steps: int, warmup: int, variant: dict, d
     return {"value": cells / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "dtype": dtype,
             "variant": variant, "tile_p_x": list(tile),
             "error_vs_fp64": {"steps": steps, "from": "the FP64 run's initial hierarchy (t = 0), same dt sequence",
-                              "f_rel_linf": num / den, "field_energy_rel_max": ew,
+                              "f_rel_linf": num / den, "field_energy_rel_max": ew, "Ex_rel_linf_max": exr,
                               "Ex_abs_max_over_laser_E0": ee, "Ey_abs_max_over_laser_E0": ey},
             "kernel_ms": prof}
 
@@ -589,6 +590,10 @@ def main() -> None:
                                       "f32 (moments, fields, Poisson f64)"),
                  "fp64_scan_poisson": measure_form(ctx, init_path, args.steps, warmup, {"poisson": 1},
                                                    "f64 (O(n) scan Poisson instead of the LU's rounding order)"),
+                 "fp64_fast": measure_form(ctx, init_path, args.steps, warmup, {"fast": 1},
+                                           "f64 (FCT kernels with fused multiply-add; the LU's rounding order)"),
+                 "fp64_fast_scan_poisson": measure_form(ctx, init_path, args.steps, warmup, {"fast": 1, "poisson": 1},
+                                                        "f64 (fused multiply-add FCT kernels, O(n) scan Poisson)"),
                  "batched_fp32": measure_batched(ctx, 64, 20, 3, 32),
                  "batched_fp64": measure_batched(ctx, 64, 20, 3, 64),
                  "served_fp32": measure_serving(ctx, 200, 48, 32),
@@ -596,6 +601,8 @@ def main() -> None:
                  "precision_wakefield_16384x1024": measure_config3(ctx, args.steps)}
         forms["fp32_speedup_vs_fp64"] = forms["fp32"]["value"] / value
         forms["fp64_scan_poisson_speedup_vs_fp64"] = forms["fp64_scan_poisson"]["value"] / value
+        forms["fp64_fast_speedup_vs_fp64"] = forms["fp64_fast"]["value"] / value
+        forms["fp64_fast_scan_poisson_speedup_vs_fp64"] = forms["fp64_fast_scan_poisson"]["value"] / value
         forms["batched_fp32_speedup_vs_fp64"] = forms["batched_fp32"]["value"] / value
         forms["batched_fp32_speedup_vs_batched_fp64"] = forms["batched_fp32"]["value"] / forms["batched_fp64"]["value"]
         forms["served_fp32_speedup_vs_fp64"] = forms["served_fp32"]["cell_updates_per_s"] / value

@@ -68,6 +68,12 @@ typedef struct vx_problem {
     double mi, iTe, ipmax; /* mobile ions (second species) when mi > 0: mass mi m_e, charge
                             * +e, the electrons' density, temperature iTe [keV], momenta in
                             * [-ipmax, ipmax] m_i c */
+    int32_t fast;      /* precision-64 runs: 0 (default) the FCT kernels in the reference's
+                        * operations and order (bit-exact); 1 the same kernels with fused
+                        * multiply-add and the WENO weights from one ratio (fewer FP64
+                        * instructions; results differ from the exact form at rounding
+                        * level, about 1e-15 relative in f per step).  Runs advanced
+                        * together share it. */
 } vx_problem;
 
 /* Fills *p with the defaults of the 2048 x 256 single-level laser/slab case. */

@@ -68,14 +68,15 @@ def test_hooks_struct_layouts_match_the_header():
     import subprocess
     import tempfile
 
-    from veritas_gb300 import VxHooks, VxInput, VxOutput, VxParticles, VxSettings
+    from veritas_gb300 import VxHooks, VxInput, VxOutput, VxParticles, VxSettings, _Problem, _RequestResult
 
-    src = ('#include <stdio.h>\n#include "vx.h"\nint main(void){printf("%zu %zu %zu %zu %zu",sizeof(vx_input),'
-           'sizeof(vx_particles),sizeof(vx_output),sizeof(vx_settings),sizeof(vx_hooks));return 0;}\n')
+    src = ('#include <stdio.h>\n#include "vx.h"\nint main(void){printf("%zu %zu %zu %zu %zu %zu %zu",'
+           'sizeof(vx_input),sizeof(vx_particles),sizeof(vx_output),sizeof(vx_settings),sizeof(vx_hooks),'
+           'sizeof(vx_problem),sizeof(vx_request_result));return 0;}\n')
     with tempfile.TemporaryDirectory() as td:
         (Path(td) / "s.c").write_text(src)
         subprocess.run(["gcc", "-I", str(ROOT / "include"), "-o", str(Path(td) / "s"), str(Path(td) / "s.c")],
                        check=True)
         got = subprocess.run([str(Path(td) / "s")], capture_output=True, text=True, check=True).stdout.split()
-    want = [ctypes.sizeof(t) for t in (VxInput, VxParticles, VxOutput, VxSettings, VxHooks)]
+    want = [ctypes.sizeof(t) for t in (VxInput, VxParticles, VxOutput, VxSettings, VxHooks, _Problem, _RequestResult)]
     assert [int(x) for x in got] == want

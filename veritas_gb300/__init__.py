@@ -49,6 +49,7 @@ class _Problem(ctypes.Structure):
         ("bdens", ctypes.c_double), ("bp0", ctypes.c_double), ("bTe", ctypes.c_double),
         ("poisson", ctypes.c_int32),
         ("mi", ctypes.c_double), ("iTe", ctypes.c_double), ("ipmax", ctypes.c_double),
+        ("fast", ctypes.c_int32),
     ]
 
 
@@ -253,6 +254,7 @@ class Problem:
     mi: float = 0.0     # mobile ions (second species) when > 0: mass / m_e
     iTe: float = 1.0    # ion temperature [keV]
     ipmax: float = 0.1  # ion momenta in [-ipmax, ipmax] m_i c
+    fast: int = 0       # precision-64 runs: 1 = contracted FCT kernels (not the reference's rounding)
 
     def to_c(self) -> _Problem:
         p = _Problem()

@@ -56,6 +56,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
                    "-I", str(CSRC), "-c", str(s), "-o", str(obj)]
             if s.stem.endswith("64"):
                 cmd.insert(1, "--fmad=false")
+            if s.name == "fct64.cu":  # the FP64 FCT kernels once more, contracted (fast form)
+                fast = BUILD / "fct64_fast.cu.o"
+                jobs.append(([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-DVX_FP64_FAST", "-Xcompiler",
+                              "-fPIC", "-I", str(CSRC), "-c", str(s), "-o", str(fast)], fast))
         else:
             cmd = [nvcc, "-x", "cu", *ARCH, "-O3", "-std=c++17", "-Xcompiler", ",".join(host_flags),
                    "-I", str(CSRC), "-c", str(s), "-o", str(obj)]

@@ -93,6 +93,7 @@ void vx_problem_defaults(vx_problem *p) {
     p->bp0 = d.bp0;
     p->bTe = d.bTe;
     p->poisson = 0;
+    p->fast = 0;
     p->mi = d.mi;
     p->iTe = d.iTe;
     p->ipmax = d.ipmax;
@@ -148,8 +149,10 @@ int vx_run_create(vx_ctx *ctx, const vx_problem *prob, vx_run **out) {
         r->ctx = ctx;
         if (prob->poisson != vx::kPoissonLU && prob->poisson != vx::kPoissonScan)
             throw std::invalid_argument("poisson must be 0 (LU) or 1 (scan)");
+        if (prob->fast != 0 && prob->fast != 1) throw std::invalid_argument("fast must be 0 or 1");
         r->run.reset(new vx::Run(*ctx->eng, std::make_shared<vx::LaserSlab>(to_params(*prob)), prob->precision));
         r->run->poisson = prob->poisson;
+        r->run->fast64 = prob->precision == 64 ? prob->fast : 0;
         r->run->init();
         ctx->eng->runs.push_back(r->run.get());
         *out = r.release();
@@ -462,7 +465,10 @@ int vx_server_clock(vx_server *s, double *now) {
 int vx_server_submit(vx_server *s, const vx_problem *p, int64_t steps, double arrival, const char *state_path,
                      int64_t *id) {
     if (!s || !p || !id) return VX_ERR_INVALID;
-    return guard([&] { *id = s->srv->submit(to_params(*p), p->precision, steps, arrival, state_path ? state_path : "", p->poisson); });
+    return guard([&] {
+        *id = s->srv->submit(to_params(*p), p->precision, steps, arrival, state_path ? state_path : "", p->poisson, 1,
+                             p->precision == 64 ? p->fast : 0);
+    });
 }
 
 int vx_server_step(vx_server *s, int *live, int *waiting) {

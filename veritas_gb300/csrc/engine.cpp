@@ -554,6 +554,7 @@ void Engine::measure_fp64_latency(double *mul_sub_cycles, double *shfl_cycles) {
 // Precision dispatch of the per-stage kernels of a launch set.
 static void fct_sub(const LaunchSet &L, const FctLaunch &fl, int sub) {
     if (L.precision == kF32) launch_fct32_substep(fl, sub);
+    else if (L.fast64) launch_fct64_substep_fast(fl, sub);
     else launch_fct64_substep(fl, sub);
 }
 static void run_moments(const LaunchSet &L, const MomLaunch &ml) {
@@ -787,11 +788,14 @@ void Engine::build_set(LaunchSet &L) {
     L.tile_j = tile_pref[L.precision == kF32][0];
     L.tile_i = tile_pref[L.precision == kF32][1];
     L.poisson = L.runs.empty() ? kPoissonLU : L.runs[0]->poisson;
+    L.fast64 = L.runs.empty() ? 0 : L.runs[0]->fast64;
     for (Run *R : L.runs) {
         if (R->precision != L.precision)
             throw std::invalid_argument("runs advanced together must share one precision");
         if (R->poisson != L.poisson)
             throw std::invalid_argument("runs advanced together must share one Poisson solver");
+        if (R->fast64 != L.fast64)
+            throw std::invalid_argument("runs advanced together must share one FP64 kernel form");
     }
     std::vector<PoissonFastDev> pfs;
     for (Run *R : L.runs) pfs.push_back(R->pfdev);

@@ -115,6 +115,7 @@ public:
     int id = 0;
     int precision = kF64;            // kF64: plain path; kF32: precision form
     int poisson = kPoissonLU;        // Poisson solver (kF32 runs always use kPoissonScan)
+    int fast64 = 0;                  // FP64 runs: 1 = the contracted FCT kernels (not the reference's rounding)
     std::vector<double> fnorm;       // per species: scale of the stored FP32 f (1 for FP64)
     // fast Poisson of the precision form (Woodbury columns and capacitance)
     std::vector<double> pf_Y;
@@ -206,6 +207,7 @@ struct LaunchSet {
     DevBuf dxtiles, dptiles;      // FP32: strip tiles of the fused face + flux kernels
     int nxtiles = 0, nptiles = 0;
     int poisson = kPoissonLU;
+    int fast64 = 0;  // FP64 sets: contracted FCT kernels
     DevBuf dpf;  // per-run PoissonFastDev (scan Poisson sets)
     std::vector<int> ghost_ptr, iface_ptr, csync_ptr;
     cudaGraphExec_t graph = nullptr;

@@ -10,10 +10,24 @@
 // Work decomposition: every kernel walks a list of 32(p) x 8(x) tiles that covers the
 // padded block of every patch of every run in the launch, so one launch per sub-step
 // serves a single patch, all patches of an AMR hierarchy, or a batch of independent runs.
+//
+// Compiled a second time with -DVX_FP64_FAST and contraction allowed: the FP64 form that
+// trades the reference's rounding for fewer FP64 instructions (fused multiply-add, and
+// WENO weights from one ratio: 3 divisions per face value instead of 5).  Its kernels
+// live in namespace vx::fast64 and its launcher is launch_fct64_substep_fast.
 #include <cuda_runtime.h>
 #include "vx_kernels.hpp"
 
+#ifdef VX_FP64_FAST
+#define VX_FCT64_NS fast64
+#define VX_FCT64_LAUNCH launch_fct64_substep_fast
+#else
+#define VX_FCT64_NS exact64
+#define VX_FCT64_LAUNCH launch_fct64_substep
+#endif
+
 namespace vx {
+namespace VX_FCT64_NS {
 
 using P64 = PatchT<double>;
 
@@ -31,10 +45,17 @@ __device__ __forceinline__ double weno_face(double f1, double f2, double f3, dou
     double bL = c43 * (AL * AL) + 0.5 * AL * BL + 0.25 * (BL * BL);
     double bR = c43 * (AR * AR) - 0.5 * AR * BR + 0.25 * (BR * BR);
     const double mm = 1.0e-10;
+#ifdef VX_FP64_FAST
+    // oL / (oL + oR) with o = 0.5 / (mm + b)^2, from the ratio rr = (mm + bL) / (mm + bR)
+    const double rr = (mm + bL) / (mm + bR);
+    double wL = 1.0 / (1.0 + rr * rr);  // rr^2 = inf gives 0, the limit
+    double wR = 1.0 - wL;
+#else
     double oL = 0.5 / ((mm + bL) * (mm + bL));
     double oR = 0.5 / ((mm + bR) * (mm + bR));
     double wL = oL / (oL + oR);
     double wR = oR / (oL + oR);
+#endif
     double wL0 = wL * (0.75 + wL * (wL - 0.5));
     double wR0 = wR * (0.75 + wR * (wR - 0.5));
     double pick;
@@ -61,10 +82,16 @@ __device__ __forceinline__ void weno_face_both(double f1, double f2, double f3, 
     double bL = c43 * (AL * AL) + 0.5 * AL * BL + 0.25 * (BL * BL);
     double bR = c43 * (AR * AR) - 0.5 * AR * BR + 0.25 * (BR * BR);
     const double mm = 1.0e-10;
+#ifdef VX_FP64_FAST
+    const double rr = (mm + bL) / (mm + bR);
+    double wL = 1.0 / (1.0 + rr * rr);
+    double wR = 1.0 - wL;
+#else
     double oL = 0.5 / ((mm + bL) * (mm + bL));
     double oR = 0.5 / ((mm + bR) * (mm + bR));
     double wL = oL / (oL + oR);
     double wR = oR / (oL + oR);
+#endif
     double wL0 = wL * (0.75 + wL * (wL - 0.5));
     double wR0 = wR * (0.75 + wR * (wR - 0.5));
     const double pr = (wL0 > wR0) ? wL0 : wR0, pl = (wL0 < wR0) ? wL0 : wR0;
@@ -300,8 +327,11 @@ __global__ void k64_copy10(const P64 *patches, const TileRef *tiles) {
     P.f0[id] = P.f1[id];
 }
 
+}  // namespace VX_FCT64_NS
+
 // --------------------------------------------------------------------------------
-void launch_fct64_substep(const FctLaunch &L, int sub) {
+void VX_FCT64_LAUNCH(const FctLaunch &L, int sub) {
+    using namespace VX_FCT64_NS;
     dim3 blk(L.tile_j ? L.tile_j : 32, L.tile_i ? L.tile_i : 8);
     const P64 *pp = (const P64 *)L.patches;
     if (L.ntiles == 0) return;

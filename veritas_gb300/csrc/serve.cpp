@@ -78,6 +78,7 @@ void Server::builder_loop() {
         try {
             b.run.reset(new Run(*builder_eng_, std::make_shared<LaserSlab>(b.params), b.precision));
             b.run->poisson = b.poisson;
+            b.run->fast64 = b.fast64;
             b.run->init();
             b.run->migrate(eng);  // drops the builder engine's sets; the loop's engine runs it from now on
         } catch (const std::exception &e) {
@@ -93,7 +94,7 @@ void Server::builder_loop() {
 }
 
 int64_t Server::submit(const LaserSlabParams &p, int precision, int64_t steps, double arrival,
-                       const std::string &state_path, int poisson, int regrid) {
+                       const std::string &state_path, int poisson, int regrid, int fast64) {
     if (steps <= 0) throw std::invalid_argument("a request needs at least one step");
     if (precision != kF64 && precision != kF32) throw std::invalid_argument("precision must be 64 or 32");
     if (poisson != kPoissonLU && poisson != kPoissonScan) throw std::invalid_argument("poisson must be 0 or 1");
@@ -103,6 +104,7 @@ int64_t Server::submit(const LaserSlabParams &p, int precision, int64_t steps, d
     r.precision = precision;
     r.poisson = precision == kF32 ? kPoissonScan : poisson;
     r.regrid = regrid ? 1 : 0;
+    r.fast64 = precision == kF64 ? (fast64 ? 1 : 0) : 0;
     r.steps = steps;
     r.arrival = arrival;
     r.state_path = state_path;
@@ -131,6 +133,7 @@ void Server::admit(double now) {
         b.params = r.params;
         b.precision = r.precision;
         b.poisson = r.poisson;
+        b.fast64 = r.fast64;
         go.push_back(std::move(b));
     }
     if (go.empty()) return;
@@ -227,16 +230,17 @@ int Server::step(double now) {
     std::map<Run *, double> t_before, dt_of;
     for (Run *r : set) t_before[r] = r->S->time;
     for (int prec : {kF64, kF32})
-        for (int pois : {kPoissonLU, kPoissonScan}) {
-            std::vector<Run *> part;
-            for (Run *r : set)
-                if (r->precision == prec && r->poisson == pois) part.push_back(r);
-            if (part.empty()) continue;
-            auto dt = eng.calculate_dt(part);
-            for (size_t k = 0; k < part.size(); k++) dt_of[part[k]] = dt[k];
-            eng.advance(part, dt);
-            used.push_back(part);
-        }
+        for (int pois : {kPoissonLU, kPoissonScan})
+            for (int fast : {0, 1}) {
+                std::vector<Run *> part;
+                for (Run *r : set)
+                    if (r->precision == prec && r->poisson == pois && r->fast64 == fast) part.push_back(r);
+                if (part.empty()) continue;
+                auto dt = eng.calculate_dt(part);
+                for (size_t k = 0; k < part.size(); k++) dt_of[part[k]] = dt[k];
+                eng.advance(part, dt);
+                used.push_back(part);
+            }
     eng.retain_sets(used);
     // health: E_x0 (updated every stage from phi, which the solve makes depend on every
     // cell's charge) turns non-finite within a step once any f, charge or field value has

@@ -23,6 +23,7 @@ public:
         int precision = kF64;
         int poisson = kPoissonLU;
         int regrid = 1;  // 1: the reference driver's regrid rule (veritas.cpp:146-151); 0: none
+        int fast64 = 0;  // FP64 requests: the contracted FCT kernels
         int64_t steps = 0, done_steps = 0;
         int regrid_counter = 0;
         int regrids = 0;
@@ -38,7 +39,7 @@ public:
     ~Server();
     // Queue a solve of `steps` RK steps that arrived at `arrival` (seconds on clock()).
     int64_t submit(const LaserSlabParams &p, int precision, int64_t steps, double arrival,
-                   const std::string &state_path, int poisson = kPoissonLU, int regrid = 1);
+                   const std::string &state_path, int poisson = kPoissonLU, int regrid = 1, int fast64 = 0);
     // Bind the runs built since the last call, admit what fits (its runs are built on
     // the builder thread), advance every live solve one step, regrid those whose counter
     // says so, retire the finished, failed and cancelled ones.  Returns the live count.
@@ -66,7 +67,7 @@ private:
     struct Build {  // one admitted request on its way through the builder thread
         int64_t id;
         LaserSlabParams params;
-        int precision, poisson;
+        int precision, poisson, fast64;
         std::unique_ptr<Run> run;
         std::string error;
     };

@@ -79,6 +79,8 @@ constexpr int kStripRows = 16;  // rows per strip tile of the fused FP32 face + 
 constexpr int kXCols = 30;      // output columns per x strip (32 lanes hold j0-1 .. j0+30)
 
 void launch_fct64_substep(const FctLaunch &L, int sub);
+// The FP64 kernels compiled with contraction and the 3-division WENO weights (fast form).
+void launch_fct64_substep_fast(const FctLaunch &L, int sub);
 void launch_fct32_substep(const FctLaunch &L, int sub);
 
 // ---------------------------------------------------------------- moments
