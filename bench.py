@@ -353,14 +353,18 @@ def measure_form(ctx, init_path: Path, steps: int, warmup: int, variant: dict, d
             "kernel_ms": prof}
 
 
-def measure_batched(ctx, count: int, steps: int, warmup: int, precision: int) -> dict:
+def measure_batched(ctx, count: int, steps: int, warmup: int, precision: int, fast: int = 0) -> dict:
     """The seeded ensemble of `count` independent runs advanced together: one launch per
-    sub-step for all runs (captured in one CUDA graph per step)."""
+    sub-step for all runs (captured in one CUDA graph per step).  fast = 1: FP64 runs with
+    the contracted FCT kernels."""
+    import dataclasses
+
     from veritas_gb300 import SolverManager, advance_many, calculate_dt_many
     from veritas_gb300.ensemble import ensemble_problems
 
     t0 = time.perf_counter()
-    runs = [SolverManager(ctx, p) for p in ensemble_problems(count, precision=precision)]
+    runs = [SolverManager(ctx, dataclasses.replace(p, fast=fast))
+            for p in ensemble_problems(count, precision=precision)]
     init_s = time.perf_counter() - t0
     cells = sum(r.cell_count() for r in runs)
     from veritas_gb300 import autotune_many
@@ -378,7 +382,7 @@ def measure_batched(ctx, count: int, steps: int, warmup: int, precision: int) ->
         r.close()
     ms = sum(times) / len(times)
     return {"value": cells / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "runs": count, "cells_per_step": cells,
-            "init_s": init_s, "precision": precision, "tile_p_x": list(tile),
+            "init_s": init_s, "precision": precision, "fast": fast, "tile_p_x": list(tile),
             "sampler": "splitmix64 seed 0x5EED0004, stream r = run r (veritas_gb300/ensemble.py)"}
 
 
@@ -596,6 +600,7 @@ def main() -> None:
                                                         "f64 (fused multiply-add FCT kernels, O(n) scan Poisson)"),
                  "batched_fp32": measure_batched(ctx, 64, 20, 3, 32),
                  "batched_fp64": measure_batched(ctx, 64, 20, 3, 64),
+                 "batched_fp64_fast": measure_batched(ctx, 64, 20, 3, 64, fast=1),
                  "served_fp32": measure_serving(ctx, 200, 48, 32),
                  "served_fp64": measure_serving(ctx, 24, 24, 64),
                  "precision_wakefield_16384x1024": measure_config3(ctx, args.steps)}
