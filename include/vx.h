@@ -195,9 +195,6 @@ int vx_run_poisson(vx_run *run);
 #define VX_SUB_UPDATE 0x4  /* sub-step 2 (antidiffusive update), PushData(1) */
 #define VX_SUB_COPY 0x8    /* sub-step 3 (f0 = f1): at stage 5 only, as Mesh::Advance */
 #define VX_SUB_ALL 0xf
-/* (Precision-32 runs given VX_SUB_LIMIT and VX_SUB_UPDATE in one call take the step's
- * fused limiter + update pass, as vx_run_advance does; given one alone, the separate
- * kernels, whose FP32 results may differ from the fused pass in the last bit.) */
 int vx_run_vlasov_stage(vx_run *run, int stage, double dt, unsigned sub_mask);
 /* Settings::UpdateTime (Settings.cpp:166-179). */
 int vx_run_update_time(vx_run *run, int stage, double dt);
@@ -326,10 +323,8 @@ int vx_ctx_timer_end(vx_ctx *ctx, double *ms);
 /* Time the run's Vlasov kernels in isolation: reps back-to-back launches per kernel on
  * the context stream (after one untimed launch).  out_ms[k] receives the mean launch
  * time of kernel k in the order gamma, faces, flux, ds_f2, limR, limC, update,
- * moments (log table + ordered sums), assemble, poisson, maxwell, ghost, iface, csync and
- * (precision-32 runs; 0 otherwise) the fused limiter + update pass that replaces limR,
- * limC and update in their steps; *count is set to the number of entries written
- * (<= cap).  Each timed kernel is idempotent, so the run's state is unchanged. */
+ * moments (log table + ordered sums), assemble; *count is set to the number of entries
+ * written (<= cap).  Each timed kernel is idempotent, so the run's state is unchanged. */
 int vx_run_profile_kernels(vx_run *run, int reps, double *out_ms, int cap, int *count);
 
 /* Overwrite a device buffer larger than the L2 cache on the context stream, so the next

@@ -461,7 +461,7 @@ class SolverManager:
         return out
 
     PROFILE_KERNELS = ["gamma", "faces", "flux", "ds_f2", "limR", "limC", "update", "moments", "assemble", "poisson",
-                       "maxwell", "ghost", "iface", "csync", "limupd"]
+                       "maxwell", "ghost", "iface", "csync"]
 
     def profile_kernels(self, reps: int = 5) -> dict:
         buf = (ctypes.c_double * 16)()

@@ -613,56 +613,10 @@ void Run::build_amr() {
     dcsync_ops = upload(csync_ops, eng->stream);
     lap("csync ops");
 
-    // ------------------------------------------------------------ limiter-exchange masks
-    // (FP32 fused limiter + update): per patch, bit 0 on the cells whose R+ / R- an
-    // exchange op compares, bit 1 on the cells beside a face an op rewrites (their update
-    // waits for the exchange); the waiting interior cells are listed for the late update
-    std::vector<std::vector<uint8_t>> lm(flat.size());
-    for (size_t k = 0; k < flat.size(); k++) lm[k].assign(flat[k]->plane_elems(), 0);
-    auto mark = [&](int patch, int i, int j, uint8_t bits) {
-        const Rect &R = *flat[patch];
-        if (i < -2 || i > R.n_x + 1 || j < -2 || j > R.n_p + 1)
-            throw std::logic_error("limiter exchange op outside its patch");
-        lm[patch][(size_t)pidx(i, j, R.pitch)] |= bits;
-    };
-    for (const CSyncOp &op : csync_ops) {
-        const bool xf = op.t < 2;
-        // the two cells beside face (i, j) of a patch: (i-1, j) and (i, j) for an x face,
-        // (i, j-1) and (i, j) for a p face
-        auto both = [&](int patch, int i, int j, uint8_t bits) {
-            mark(patch, i, j, bits);
-            mark(patch, xf ? i - 1 : i, xf ? j : j - 1, bits);
-        };
-        if (op.kind == kCDiff) {
-            both(op.nb, op.ni, op.nj, 3);
-            for (int q = 0; q < r; q++) both(op.caller, xf ? op.ci : op.ci + q, xf ? op.cj + q : op.cj, 3);
-        } else {
-            const uint8_t bits = op.kind == kCSame ? 3 : 2;
-            both(op.nb, op.ni, op.nj, bits);
-            both(op.caller, op.ci, op.cj, bits);
-        }
-    }
-    late_cells.clear();
-    for (size_t k = 0; k < flat.size(); k++) {
-        Rect &R = *flat[k];
-        R.has_lmask = false;
-        for (int i = 0; i < R.n_x; i++)
-            for (int j = 0; j < R.n_p; j++)
-                if (lm[k][(size_t)pidx(i, j, R.pitch)] & 2) late_cells.push_back({(int)k, i, j});
-        for (uint8_t v : lm[k])
-            if (v) {
-                R.has_lmask = true;
-                break;
-            }
-    }
-    lap("limiter masks");
-
     // ------------------------------------------------------------ device masks, weights
-    for (size_t k = 0; k < flat.size(); k++) {
-        Rect *R = flat[k];
+    for (Rect *R : flat) {
         const size_t pe = R->plane_elems();
-        std::vector<uint8_t> m(4 * pe, 0);
-        std::memcpy(&m[3 * pe], lm[k].data(), pe);
+        std::vector<uint8_t> m(3 * pe, 0);
         // rows of (n_p + 4) cells in the reference's index order become pitched rows
         const size_t w = (size_t)R->n_p + 4;
         for (int i = -2; i < R->n_x + 2; i++) {

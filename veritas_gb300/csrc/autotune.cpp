@@ -28,7 +28,7 @@ std::pair<int, int> Engine::autotune(const std::vector<Run *> &set, int reps) {
     fl.stream = stream;
     auto run_subs = [&]() {
         if (L.precision == kF32)
-            for (int sub : {kSubXFlux, kSubPFlux, kSubDsF2, kSubLimUpd}) launch_fct32_substep(fl, sub);
+            for (int sub : {kSubXFlux, kSubPFlux, kSubDsF2, kSubLimR, kSubLimC}) launch_fct32_substep(fl, sub);
         else
             for (int sub : {kSubGamma, kSubFaces, kSubFlux, kSubDsF2, kSubLimR, kSubLimC}) launch_fct64_substep(fl, sub);
     };

@@ -193,11 +193,9 @@ void Run::upload_rect_desc(Rect &r, int run_index) {
         d.nested = m;
         d.ifx = m + pe;
         d.ifp = m + 2 * pe;
-        d.lmask = r.has_lmask ? m + 3 * pe : nullptr;
         d.has_iface = 1;
     } else {
         d.nested = d.ifx = d.ifp = nullptr;
-        d.lmask = nullptr;
         d.has_iface = 0;
     }
 }
@@ -690,9 +688,6 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
         for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++)
             launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], L.precision, stream);
     });
-    // FP32: the fused limiter + update pass the step runs in place of limR, limC, update
-    if (L.precision == kF32) time_it([&] { fct_sub(L, fl, kSubLimUpd); });
-    else out.push_back(0.0);
     return out;
 }
 
@@ -785,25 +780,6 @@ void Engine::build_tiles(LaunchSet &L) {
         L.nptiles = (int)pt.size();
         L.dxtiles = upload(xt, stream);
         L.dptiles = upload(pt, stream);
-        // fused limiter + update: tiles, and the set's late-update cells
-        std::vector<TileRef> lu, late;
-        pi = 0;
-        for (Run *R : L.runs) {
-            const int base = pi;
-            for (auto &sp : R->rects)
-                for (auto &lvl : sp)
-                    for (auto &rp : lvl) {
-                        // rows up to nx and columns up to np + 1: the last tiles own the ghost ring
-                        for (int i0 = 0; i0 <= rp->n_x; i0 += kLuRows)
-                            for (int j0 = -2; j0 <= rp->n_p + 1; j0 += 128) lu.push_back({pi, i0, j0});
-                        pi++;
-                    }
-            for (const TileRef &c : R->late_cells) late.push_back({base + c.patch, c.i0, c.j0});
-        }
-        L.nlutiles = (int)lu.size();
-        L.nlate = (int)late.size();
-        L.dlutiles = upload(lu, stream);
-        L.dlate = upload(late, stream);
     }
 }
 
@@ -1005,10 +981,6 @@ StageLaunches Engine::stage_launches(LaunchSet &L) {
     fl.ptiles = L.dptiles.as<TileRef>();
     fl.nxtiles = L.nxtiles;
     fl.nptiles = L.nptiles;
-    fl.lutiles = L.dlutiles.as<TileRef>();
-    fl.nlutiles = L.nlutiles;
-    fl.late = L.dlate.as<TileRef>();
-    fl.nlate = L.nlate;
     fl.fields = L.dfields.as<RunFields>();
     fl.params = L.dparams.as<double>();
     fl.params32 = L.dparams32.as<float>();
@@ -1132,24 +1104,13 @@ void Engine::record_step(LaunchSet &L) {
         launches += 1;
         for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
             launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 2, L.precision, stream);
-        if (L.precision == kF32) {  // limiter and update in one pass; exchanged cells after the exchange
-            fct_sub(L, fl, kSubLimUpd);
-            launches += 1;
-            for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++, launches++)
-                launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], L.precision, stream);
-            if (L.nlate) {
-                fct_sub(L, fl, kSubLateUpd);
-                launches += 1;
-            }
-        } else {
-            fct_sub(L, fl, kSubLimR);
-            fct_sub(L, fl, kSubLimC);
-            launches += 2;
-            for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++, launches++)
-                launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], L.precision, stream);
-            fct_sub(L, fl, kSubUpdate);
-            launches += 1;
-        }
+        fct_sub(L, fl, kSubLimR);
+        fct_sub(L, fl, kSubLimC);
+        launches += 2;
+        for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++, launches++)
+            launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], L.precision, stream);
+        fct_sub(L, fl, kSubUpdate);
+        launches += 1;
         for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
             launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, L.precision, stream);
         if (s == 5) {
@@ -1266,28 +1227,19 @@ void Engine::run_phases(Run &run, int s, double dt, unsigned phases) {
         fct_sub(L, fl, kSubDsF2);
         launches += 1;
     }
-    // FP32 runs given sub-steps 1 and 2 together take the step's fused pass (limiter and
-    // the update of the cells the exchange does not touch, then the rest after it); given
-    // one of them alone, the separate limiter / update kernels
-    const bool fused = L.precision == kF32 && (phases & kPhSub1) && (phases & kPhSub2);
     if (phases & kPhSub1) {  // PushData(2), FCTTimeStep(.., 1), PushBoundaryC
         for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
             launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 2,
                          L.precision, stream);
-        if (fused) {
-            fct_sub(L, fl, kSubLimUpd);
-            launches += 1;
-        } else {
-            fct_sub(L, fl, kSubLimR);
-            fct_sub(L, fl, kSubLimC);
-            launches += 2;
-        }
+        fct_sub(L, fl, kSubLimR);
+        fct_sub(L, fl, kSubLimC);
+        launches += 2;
         for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++, launches++)
             launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b],
                          L.precision, stream);
     }
     if (phases & kPhSub2) {  // FCTTimeStep(.., 2), PushData(1)
-        fct_sub(L, fl, fused ? kSubLateUpd : kSubUpdate);
+        fct_sub(L, fl, kSubUpdate);
         launches += 1;
         for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
             launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1,

@@ -62,8 +62,7 @@ struct Rect {
     int pitch = 0;
     DevBuf slab;   // all per-patch planes
     DevBuf cols;   // chargeR, currentR
-    DevBuf masks;  // nested, ifx, ifp, lmask (AMR only)
-    bool has_lmask = false;  // any cell of this patch in the limiter exchange
+    DevBuf masks;  // nested, ifx, ifp (AMR only)
     // Device descriptor.  For FP32 runs the plane pointers address float planes: the
     // layout of PatchT<float> is identical (see the static_assert in engine.cpp), and the
     // host never dereferences them.
@@ -152,7 +151,6 @@ public:
     std::vector<IfaceOp> iface_ops;
     Batched iface_b;
     DevBuf dghost_ops, dcsync_ops, diface_ops;  // the op lists on the device (set tables gather them)
-    std::vector<TileRef> late_cells;  // (flat patch, i, j) updated after the limiter exchange (FP32 form)
     DevBuf drelc;                   // sub-cell interpolation weights per depth
     DevBuf drefc;                   // coarse-to-fine interpolation weights (refinement ratio)
     std::vector<int> relc_off;      // offset of depth d's weights in drelc
@@ -208,8 +206,6 @@ struct LaunchSet {
     int tile_j = 32, tile_i = 8;  // FCT tile (p x x) = thread block of the sub-step kernels
     DevBuf dxtiles, dptiles;      // FP32: strip tiles of the fused face + flux kernels
     int nxtiles = 0, nptiles = 0;
-    DevBuf dlutiles, dlate;       // FP32: fused limiter + update tiles, cells updated after the exchange
-    int nlutiles = 0, nlate = 0;
     int poisson = kPoissonLU;
     int fast64 = 0;  // FP64 sets: contracted FCT kernels
     DevBuf dpf;  // per-run PoissonFastDev (scan Poisson sets)

@@ -255,186 +255,6 @@ __global__ void k32_update(const P32 *patches, const TileRef *tiles) {
     st4(P.f1 + id, out, j, 0, P.np);
 }
 
-// ---------------------------------------------------------------- fused limiter + update
-// Sub-steps 1 and 2 of Rectangle::FCTTimeStep (Rectangle.cpp:1536-1612) in one pass over
-// tiles of kLuRows rows by 128 p cells, four cells per thread as aligned float4 (the
-// streaming kernels' layout, j0 = -2 + 128 k).  The block first forms R+ / R- of its rows
-// and a one-cell ring (k32_limR's arithmetic) into shared memory, then each thread forms
-// the face coefficients C of its four cells from them (k32_limC) and the antidiffusive
-// update (k32_update), so f0, f2 and the antidiffusive fluxes are read and only f1 is
-// written.  Where the limiter exchange between patches (PushBoundaryC) needs them (the
-// patch's lmask), R and the cell's face C go to memory too, and the update of a cell
-// beside a face the exchange rewrites is left to k32_late_update after the exchange.
-constexpr int kLuSW = 136;  // shared row: p cells j0-4 .. j0+131 (column c <-> j = j0 - 4 + c)
-constexpr int kLuSR = kLuRows + 2;  // shared rows: i0-1 .. i0+kLuRows
-
-// R+ and R- of cells (i, j .. j+3) (k32_limR), zero outside i in [-1, nx], j in [-1, np];
-// j + 2 is a multiple of 4 and j <= np + 1, i in [-1, nx].
-__device__ __forceinline__ void limR4(const P32 &P, int i, int j, V4 &rp, V4 &rm) {
-    const int pit = P.pitch, id = pidx(i, j, pit);
-    const float *DX = P.FxDS, *DP = P.FpDS, *f0 = P.f0, *f2 = P.f2;
-    const V4 dxi = ld4(DX + id), dxn = ld4(DX + id + pit), dpi = ld4(DP + id);
-    const V4 a0 = ld4(f0 + id), a2 = ld4(f2 + id);
-    const V4 u0 = ld4(f0 + id + pit), u2 = ld4(f2 + id + pit);
-    const V4 d0 = ld4(f0 + id - pit), d2 = ld4(f2 + id - pit);
-    const bool lo_ok = j >= -1, hi_ok = j + 3 <= P.np;
-    const float l0 = lo_ok ? f0[id - 1] : 0.0f, l2 = lo_ok ? f2[id - 1] : 0.0f;
-    const float r0 = hi_ok ? f0[id + 4] : 0.0f, r2 = hi_ok ? f2[id + 4] : 0.0f;
-    const float dp4 = hi_ok ? DP[id + 4] : 0.0f;
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-        const float dpn = e < 3 ? dpi.v[e + 1] : dp4;
-        const float Pp = fmaxf(0.0f, dxi.v[e]) - fminf(0.0f, dxn.v[e]) + fmaxf(0.0f, dpi.v[e]) - fminf(0.0f, dpn);
-        const float Pm = fmaxf(0.0f, dxn.v[e]) - fminf(0.0f, dxi.v[e]) + fmaxf(0.0f, dpn) - fminf(0.0f, dpi.v[e]);
-        const float c0 = a0.v[e], c2 = a2.v[e];
-        const float lf0 = e > 0 ? a0.v[e - 1] : l0, lf2 = e > 0 ? a2.v[e - 1] : l2;
-        const float rf0 = e < 3 ? a0.v[e + 1] : r0, rf2 = e < 3 ? a2.v[e + 1] : r2;
-        const float wMax = fmaxf(fmaxf(c0, c2), fmaxf(fmaxf(u0.v[e], u2.v[e]),
-                           fmaxf(fmaxf(d0.v[e], d2.v[e]), fmaxf(fmaxf(rf0, rf2), fmaxf(lf0, lf2)))));
-        const float wMin = fminf(fminf(c0, c2), fminf(fminf(u0.v[e], u2.v[e]),
-                           fminf(fminf(d0.v[e], d2.v[e]), fminf(fminf(rf0, rf2), fminf(lf0, lf2)))));
-        const bool in = j + e >= -1 && j + e <= P.np;
-        rp.v[e] = in ? limiter_ratio(wMax - c2, Pp) : 0.0f;
-        rm.v[e] = in ? limiter_ratio(-wMin + c2, Pm) : 0.0f;
-    }
-}
-// The same for one cell (the tile's ring columns j0-1 and j0+128).
-__device__ __forceinline__ void limR1(const P32 &P, int i, int j, float &rp, float &rm) {
-    rp = rm = 0.0f;
-    if (i < -1 || i > P.nx || j < -1 || j > P.np) return;
-    const int pit = P.pitch, id = pidx(i, j, pit);
-    const float *DX = P.FxDS, *DP = P.FpDS, *f0 = P.f0, *f2 = P.f2;
-    const float dxi = DX[id], dxn = DX[id + pit], dpi = DP[id], dpn = DP[id + 1];
-    const float Pp = fmaxf(0.0f, dxi) - fminf(0.0f, dxn) + fmaxf(0.0f, dpi) - fminf(0.0f, dpn);
-    const float Pm = fmaxf(0.0f, dxn) - fminf(0.0f, dxi) + fmaxf(0.0f, dpn) - fminf(0.0f, dpi);
-    const float c0 = f0[id], c2 = f2[id];
-    const float wMax = fmaxf(fmaxf(c0, c2), fmaxf(fmaxf(f0[id + pit], f2[id + pit]),
-                       fmaxf(fmaxf(f0[id - pit], f2[id - pit]), fmaxf(fmaxf(f0[id + 1], f2[id + 1]),
-                                                                      fmaxf(f0[id - 1], f2[id - 1])))));
-    const float wMin = fminf(fminf(c0, c2), fminf(fminf(f0[id + pit], f2[id + pit]),
-                       fminf(fminf(f0[id - pit], f2[id - pit]), fminf(fminf(f0[id + 1], f2[id + 1]),
-                                                                      fminf(f0[id - 1], f2[id - 1])))));
-    rp = limiter_ratio(wMax - c2, Pp);
-    rm = limiter_ratio(-wMin + c2, Pm);
-}
-
-struct LuShared {
-    float rp[kLuSR][kLuSW], rm[kLuSR][kLuSW];
-};
-
-// C of x-face i and p-face j from the shared R (k32_limC: 1 outside i in [1, nx), j in
-// [0, np)); the tile's shared row of cell row i is i - (i0 - 1), column j - (j0 - 4).
-__device__ __forceinline__ float lu_cx(const LuShared &S, const P32 &P, int i0, int j0, int i, int j, float dx) {
-    if (!(i >= 1 && i < P.nx && j >= 0 && j < P.np)) return 1.0f;
-    const int a = i - i0 + 1, c = j - j0 + 4;
-    return dx > 0.0f ? fminf(S.rp[a][c], S.rm[a - 1][c]) : fminf(S.rp[a - 1][c], S.rm[a][c]);
-}
-__device__ __forceinline__ float lu_cp(const LuShared &S, const P32 &P, int i0, int j0, int i, int j, float dp) {
-    if (!(i >= 1 && i < P.nx && j >= 0 && j < P.np)) return 1.0f;
-    const int a = i - i0 + 1, c = j - j0 + 4;
-    return dp > 0.0f ? fminf(S.rp[a][c], S.rm[a][c - 1]) : fminf(S.rp[a][c - 1], S.rm[a][c]);
-}
-
-__global__ void __launch_bounds__(32 * kLuRows) k32_limupd(const P32 *patches, const TileRef *tiles) {
-    VX_PDL_WAIT();
-    __shared__ __align__(16) LuShared S;
-    const TileRef t = tiles[blockIdx.x];
-    const P32 &P = patches[t.patch];
-    const int i0 = t.i0, j0 = t.j0, tx = threadIdx.x, ty = threadIdx.y;
-    const int j = j0 + 4 * tx;
-    // R on rows i0-1 .. i0+kLuRows: thread row ty takes row i0-1+ty, rows 0 and 1 also
-    // the last two; lanes 0 / 31 also the ring columns j0-1 / j0+128
-    for (int rr = ty; rr < kLuSR; rr += kLuRows) {
-        const int i = i0 - 1 + rr;
-        V4 rp{{0.0f, 0.0f, 0.0f, 0.0f}}, rm{{0.0f, 0.0f, 0.0f, 0.0f}};
-        if (i >= -1 && i <= P.nx && j <= P.np + 1) limR4(P, i, j, rp, rm);
-        *reinterpret_cast<float4 *>(&S.rp[rr][4 + 4 * tx]) = make_float4(rp.v[0], rp.v[1], rp.v[2], rp.v[3]);
-        *reinterpret_cast<float4 *>(&S.rm[rr][4 + 4 * tx]) = make_float4(rm.v[0], rm.v[1], rm.v[2], rm.v[3]);
-        if (tx == 0) limR1(P, i, j0 - 1, S.rp[rr][3], S.rm[rr][3]);
-        if (tx == 31) limR1(P, i, j0 + 128, S.rp[rr][132], S.rm[rr][132]);
-    }
-    __syncthreads();
-    const int i = i0 + ty;
-    const int pit = P.pitch;
-    const uint8_t *lm = P.lmask;
-    // C and the update of the thread's four cells (interior cells only)
-    if (i >= 0 && i < P.nx && j + 3 >= 0 && j < P.np) {
-        const int id = pidx(i, j, pit);
-        const V4 f2 = ld4(P.f2 + id), dx = ld4(P.FxDS + id), dxn = ld4(P.FxDS + id + pit), dp = ld4(P.FpDS + id);
-        const bool hi_ok = j + 3 < P.np;  // element 3 has a p neighbour j + 4 <= np
-        const float dp4 = hi_ok ? P.FpDS[id + 4] : 0.0f;
-        V4 out;
-        bool wait[4] = {false, false, false, false};
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-            const int je = j + e;
-            const float dpn = e < 3 ? dp.v[e + 1] : dp4;
-            const float cxi = lu_cx(S, P, i0, j0, i, je, dx.v[e]);
-            const float cxn = lu_cx(S, P, i0, j0, i + 1, je, dxn.v[e]);
-            const float cpi = lu_cp(S, P, i0, j0, i, je, dp.v[e]);
-            const float cpn = lu_cp(S, P, i0, j0, i, je + 1, dpn);
-            float v = f2.v[e];
-            if (active32(P, i, je)) v += cxi * dx.v[e];
-            if (active32(P, i, je)) v += cpi * dp.v[e];
-            if (active32(P, i, je + 1)) v -= cpn * dpn;
-            if (active32(P, i + 1, je)) v -= cxn * dxn.v[e];
-            out.v[e] = v;
-            if (lm && je >= 0 && je < P.np) wait[e] = (lm[id + e] & 2) != 0;
-        }
-        if (!(wait[0] || wait[1] || wait[2] || wait[3])) {
-            st4(P.f1 + id, out, j, 0, P.np);
-        } else {
-#pragma unroll
-            for (int e = 0; e < 4; e++)
-                if (!wait[e] && j + e >= 0 && j + e < P.np) P.f1[id + e] = out.v[e];
-        }
-    }
-    if (!lm) return;
-    // what the limiter exchange reads: R of the cells it compares, C of both faces in each
-    // direction of the cells beside a face it rewrites; a tile owns its rows (row -1 with
-    // the first row of tiles) and its 128 columns, clipped to i in [-1, nx], j in [-1, np]
-    for (int pass = 0; pass < 2; pass++) {
-        const int ii = pass == 0 ? i : -1;
-        if (pass == 1 && !(i0 == 0 && ty == 0)) break;
-        if (ii < -1 || ii > P.nx) continue;
-        for (int e = 0; e < 4; e++) {
-            const int je = j + e;
-            if (je < -1 || je > P.np) continue;
-            const int id = pidx(ii, je, pit);
-            const uint8_t m = lm[id];
-            if (!m) continue;
-            const int a = ii - i0 + 1, c = je - j0 + 4;
-            if (m & 1) {
-                P.Rp[id] = S.rp[a][c];
-                P.Rm[id] = S.rm[a][c];
-            }
-            if (m & 2) {
-                P.Cx[id] = lu_cx(S, P, i0, j0, ii, je, P.FxDS[id]);
-                P.Cx[id + pit] = lu_cx(S, P, i0, j0, ii + 1, je, P.FxDS[id + pit]);
-                P.Cp[id] = lu_cp(S, P, i0, j0, ii, je, P.FpDS[id]);
-                P.Cp[id + 1] = lu_cp(S, P, i0, j0, ii, je + 1, P.FpDS[id + 1]);
-            }
-        }
-    }
-}
-
-// The update of the cells whose faces the limiter exchange rewrote (k32_update's
-// arithmetic on the C planes).
-__global__ void k32_late_update(const P32 *patches, const TileRef *cells, int n) {
-    VX_PDL_WAIT();
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const TileRef c = cells[k];
-    const P32 &P = patches[c.patch];
-    const int i = c.i0, j = c.j0, pit = P.pitch, id = pidx(i, j, pit);
-    float v = P.f2[id];
-    if (active32(P, i, j)) v += P.Cx[id] * P.FxDS[id];
-    if (active32(P, i, j)) v += P.Cp[id] * P.FpDS[id];
-    if (active32(P, i, j + 1)) v -= P.Cp[id + 1] * P.FpDS[id + 1];
-    if (active32(P, i + 1, j)) v -= P.Cx[id + pit] * P.FxDS[id + pit];
-    P.f1[id] = v;
-}
-
 // f0 = f1 over the padded block (Rectangle.cpp:1614-1621).
 __global__ void k32_copy10(const P32 *patches, const TileRef *tiles) {
     VX_PDL_WAIT();
@@ -639,12 +459,6 @@ void launch_fct32_substep(const FctLaunch &L, int sub) {
             break;
         case kSubPFlux:
             if (L.nptiles) vx_launch(k32_pflux, (L.nptiles + 3) / 4, 128, 0, L.stream, pp, L.ptiles, L.nptiles, L.fields, L.step, L.use_f0);
-            break;
-        case kSubLimUpd:
-            if (L.nlutiles) vx_launch(k32_limupd, L.nlutiles, dim3(32, kLuRows), 0, L.stream, pp, L.lutiles);
-            break;
-        case kSubLateUpd:
-            if (L.nlate) vx_launch(k32_late_update, (L.nlate + 127) / 128, 128, 0, L.stream, pp, L.late, L.nlate);
             break;
         default:  // the FP32 form has no separate gamma / face / flux sub-steps (fused above)
             break;

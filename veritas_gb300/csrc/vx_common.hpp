@@ -74,10 +74,6 @@ struct PatchT {
     T *Rp, *Rm, *Cx, *Cp;   // Zalesak limiter
     uint8_t *nested;        // is_nested (cells covered by a finer patch)
     uint8_t *ifx, *ifp;     // is_interrior_level_boundary_x / _p
-    // FP32 fused limiter + update: per cell, bit 0 = the limiter exchange (PushBoundaryC)
-    // reads its R+/R-, bit 1 = the exchange rewrites one of its faces' C, so its update
-    // waits for the exchange; null when the patch takes no part in the exchange
-    const uint8_t *lmask;
     double *chargeR, *currentR;  // per finest column of this patch (n_x * rtb)
     const double *relc;     // interpolation weights onto the rtb finest sub-cells, 3*rtb
     const double *refc;     // interpolation weights onto the r sub-cells of a coarse cell, 3*r

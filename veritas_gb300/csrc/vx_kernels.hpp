@@ -57,13 +57,7 @@ enum FctSub : int {
     // FP32 form only: gamma + x faces + x fluxes, and p faces + p fluxes, each fused
     kSubXFlux,
     kSubPFlux,
-    // FP32 form only: limiter R and C and the antidiffusive update in one pass over
-    // shared-memory tiles (cells the limiter exchange touches wait), and the update of
-    // those waiting cells after the exchange
-    kSubLimUpd,
-    kSubLateUpd,
 };
-constexpr int kLuRows = 8;  // tile rows (thread rows) of the fused FP32 limiter + update kernel
 
 struct FctLaunch {
     const void *patches;  // device array of PatchT<T>
@@ -79,11 +73,6 @@ struct FctLaunch {
     // FP32 fused face + flux kernels: one warp per strip tile
     const TileRef *xtiles, *ptiles;
     int nxtiles, nptiles;
-    // FP32 fused limiter + update: tiles of kLuRows rows (i0 = 0, 8, .. <= nx) by 128 p
-    // cells (j0 = -2 + 128 k <= np + 1), and the cells whose update waits for the limiter
-    // exchange (i0, j0 = the cell)
-    const TileRef *lutiles, *late;
-    int nlutiles, nlate;
     cudaStream_t stream;
 };
 constexpr int kStripRows = 16;  // rows per strip tile of the fused FP32 face + flux kernels
