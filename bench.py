@@ -282,7 +282,8 @@ def field_energy(s):
         0.5 / MU0 * float(np.sum(By * By) + np.sum(Bz * Bz))
 
 
-def measure_form(ctx, init_path: Path, steps: int, warmup: int, variant: dict, dtype: str) -> dict:
+def measure_form(ctx, init_path: Path, steps: int, warmup: int, variant: dict, dtype: str,
+                 persistent: int = 0) -> dict:
     """A variant of the plain path (`variant` overrides Problem fields: the FP32 precision
     form, or FP64 with the scan Poisson solve) on the same workload: throughput, and its
     error against the plain FP64 path over `steps` steps from the same state with the same
@@ -302,6 +303,7 @@ def measure_form(ctx, init_path: Path, steps: int, warmup: int, variant: dict, d
     from veritas_gb300 import autotune_many
 
     tile = autotune_many([s])
+    ctx.set_persistent(bool(persistent))  # FP32: the persistent stage kernels
     for _ in range(warmup):
         s.Advance(s.CalculateDt())
     ctx.sync()
@@ -311,6 +313,7 @@ def measure_form(ctx, init_path: Path, steps: int, warmup: int, variant: dict, d
         ctx.timer_begin()
         s.Advance(s.CalculateDt())
         times.append(ctx.timer_end())
+    ctx.set_persistent(False)
     prof = s.profile_kernels(reps=5)
     s.close()
     ms = sum(times) / len(times)
@@ -346,17 +349,19 @@ def measure_form(ctx, init_path: Path, steps: int, warmup: int, variant: dict, d
     a.close()
     b.close()
     return {"value": cells / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "dtype": dtype,
-            "variant": variant, "tile_p_x": list(tile),
+            "variant": variant, "persistent": persistent, "tile_p_x": list(tile),
             "error_vs_fp64": {"steps": steps, "from": "the FP64 run's initial hierarchy (t = 0), same dt sequence",
                               "f_rel_linf": num / den, "field_energy_rel_max": ew, "Ex_rel_linf_max": exr,
                               "Ex_abs_max_over_laser_E0": ee, "Ey_abs_max_over_laser_E0": ey},
             "kernel_ms": prof}
 
 
-def measure_batched(ctx, count: int, steps: int, warmup: int, precision: int, fast: int = 0) -> dict:
+def measure_batched(ctx, count: int, steps: int, warmup: int, precision: int, fast: int = 0,
+                    persistent: int = 0) -> dict:
     """The seeded ensemble of `count` independent runs advanced together: one launch per
-    sub-step for all runs (captured in one CUDA graph per step).  fast = 1: FP64 runs with
-    the contracted FCT kernels."""
+    sub-step for all runs (captured in one CUDA graph per step), or with persistent = 1
+    (FP32) three launches per RK stage, two of them persistent cooperative stage kernels.
+    fast = 1: FP64 runs with the contracted FCT kernels."""
     import dataclasses
 
     from veritas_gb300 import SolverManager, advance_many, calculate_dt_many
@@ -370,19 +375,25 @@ def measure_batched(ctx, count: int, steps: int, warmup: int, precision: int, fa
     from veritas_gb300 import autotune_many
 
     tile = autotune_many(runs)
+    ctx.set_persistent(bool(persistent))
     for _ in range(warmup):
         advance_many(runs, calculate_dt_many(runs))
     ctx.sync()
     times = []
+    l0 = ctx.kernel_launches()
     for _ in range(steps):
         ctx.timer_begin()
         advance_many(runs, calculate_dt_many(runs))
         times.append(ctx.timer_end())
+    ctx.sync()
+    launches = (ctx.kernel_launches() - l0) / steps - 1  # minus the CFL kernel of each step
+    ctx.set_persistent(False)
     for r in runs:
         r.close()
     ms = sum(times) / len(times)
     return {"value": cells / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "runs": count, "cells_per_step": cells,
-            "init_s": init_s, "precision": precision, "fast": fast, "tile_p_x": list(tile),
+            "init_s": init_s, "precision": precision, "fast": fast, "persistent": persistent,
+            "launches_per_rk_stage": launches / 6, "tile_p_x": list(tile),
             "sampler": "splitmix64 seed 0x5EED0004, stream r = run r (veritas_gb300/ensemble.py)"}
 
 
@@ -453,6 +464,8 @@ def main() -> None:
     ap.add_argument("--runs", type=int, default=64, help="ensemble size of --form batched / solves of --form served")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the FP32 / batched / served forms (FP64 headline line only)")
+    ap.add_argument("--persistent", action="store_true",
+                    help="FP32 runs (--form batched, or --precision 32): the persistent stage kernels")
     ap.add_argument("--lite", action="store_true",
                     help="only the warm-up and timed steps (used under ncu); no e2e, kernel timing or CPU baseline")
     args = ap.parse_args()
@@ -467,7 +480,8 @@ def main() -> None:
 
         ctx = Context(0)
         if args.form == "batched":
-            out = measure_batched(ctx, args.runs, args.steps, max(1, args.warmup), args.precision)
+            out = measure_batched(ctx, args.runs, args.steps, max(1, args.warmup), args.precision,
+                                  persistent=int(args.persistent))
         else:
             out = measure_serving(ctx, args.runs, args.steps, args.precision)
         print(json.dumps({"form": args.form, **out}))
@@ -491,6 +505,8 @@ def main() -> None:
 
     s = SolverManager(ctx, dataclasses.replace(problem_config2(), precision=args.precision, poisson=args.poisson))
     cells = s.cell_count()
+    if args.persistent:
+        ctx.set_persistent(True)
     init_path = Path(tempfile.mkdtemp()) / "init.bin"
     if rank == 0 and not args.lite and not (args.no_cpu_baseline and args.no_forms):
         s.save_state(init_path)  # the CPU baseline and the FP32 error check start from it
@@ -600,7 +616,11 @@ def main() -> None:
                                            "f64 (FCT kernels with fused multiply-add; the LU's rounding order)"),
                  "fp64_fast_scan_poisson": measure_form(ctx, init_path, args.steps, warmup, {"fast": 1, "poisson": 1},
                                                         "f64 (fused multiply-add FCT kernels, O(n) scan Poisson)"),
+                 "fp32_persistent": measure_form(ctx, init_path, args.steps, warmup, {"precision": 32},
+                                                 "f32, persistent stage kernels (3 launches per RK stage)",
+                                                 persistent=1),
                  "batched_fp32": measure_batched(ctx, 64, 20, 3, 32),
+                 "batched_fp32_persistent": measure_batched(ctx, 64, 20, 3, 32, persistent=1),
                  "batched_fp64": measure_batched(ctx, 64, 20, 3, 64),
                  "batched_fp64_fast": measure_batched(ctx, 64, 20, 3, 64, fast=1),
                  "served_fp32": measure_serving(ctx, 200, 48, 32),

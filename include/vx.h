@@ -218,6 +218,20 @@ int vx_ctx_destroy(vx_ctx *ctx);
  * dependent launch (process-wide).  For debugging and timing; results do not depend on
  * it. */
 int vx_ctx_set_launch_mode(vx_ctx *ctx, int graphs, int pdl);
+/* Persistent stage form (no reference counterpart; off by default): on != 0 advances the
+ * context's FP32 runs (alone or batched) with three launches per RK stage — one
+ * cooperative kernel for the moments and rho/J assembly, the Poisson solve, and one
+ * cooperative kernel for the whole FCT stage of every patch of every run with the
+ * Maxwell stage beside it — instead of one launch per sub-step (FP64 runs are unaffected).
+ * Same bits as the per-sub-step form.  The kernels' grid barriers wait a bounded time; a
+ * wait that runs out is reported by the next call that synchronises the context
+ * (vx_ctx_sync, vx_run_calculate_dt, state reads) as VX_ERR_TIMEOUT, after which that
+ * step's results are not valid and the context stays usable. */
+int vx_ctx_set_persistent(vx_ctx *ctx, int on);
+/* Wait limit of those barriers in ns (default 2e9) and a count of arrivals each barrier
+ * waits for beyond the launch's own blocks (default 0; any phantom > 0 makes every wait
+ * run out — the failure path's test). */
+int vx_ctx_set_persistent_limit(vx_ctx *ctx, uint64_t limit_ns, int phantom);
 int vx_ctx_sync(vx_ctx *ctx);
 /* Kernels launched by this context so far (graph replays count their nodes). */
 int vx_ctx_kernel_launches(vx_ctx *ctx, uint64_t *out);

@@ -129,6 +129,8 @@ def _load() -> ctypes.CDLL:
         "vx_ctx_destroy": (ctypes.c_int, [vp]),
         "vx_ctx_sync": (ctypes.c_int, [vp]),
         "vx_ctx_set_launch_mode": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
+        "vx_ctx_set_persistent": (ctypes.c_int, [vp, ctypes.c_int]),
+        "vx_ctx_set_persistent_limit": (ctypes.c_int, [vp, ctypes.c_uint64, ctypes.c_int]),
         "vx_ctx_kernel_launches": (ctypes.c_int, [vp, P(ctypes.c_uint64)]),
         "vx_run_create": (ctypes.c_int, [vp, P(_Problem), P(vp)]),
         "vx_run_destroy": (ctypes.c_int, [vp]),
@@ -291,6 +293,16 @@ class Context:
     def set_launch_mode(self, graphs: bool = True, pdl: bool = True) -> None:
         """CUDA graph per step and programmatic dependent launch (both on by default)."""
         _check(_lib.vx_ctx_set_launch_mode(self._h, int(graphs), int(pdl)))
+
+    def set_persistent(self, on: bool = True) -> None:
+        """FP32 runs: three launches per RK stage (two persistent cooperative stage kernels
+        around the Poisson solve) instead of one per sub-step; same bits."""
+        _check(_lib.vx_ctx_set_persistent(self._h, int(on)))
+
+    def set_persistent_limit(self, limit_ns: int = 2_000_000_000, phantom: int = 0) -> None:
+        """Wait limit of the persistent kernels' grid barriers; phantom > 0 makes every wait
+        run out (failure-path test)."""
+        _check(_lib.vx_ctx_set_persistent_limit(self._h, int(limit_ns), int(phantom)))
 
     def kernel_launches(self) -> int:
         v = ctypes.c_uint64()

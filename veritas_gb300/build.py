@@ -39,7 +39,7 @@ def sources() -> list[Path]:
 
 def build(force: bool = False, verbose: bool = False) -> Path:
     srcs = sources()
-    deps = srcs + list(CSRC.glob("*.hpp")) + [HERE.parent / "include" / "vx.h", HERE.parent / "include" / "veritas_gb300.hpp",
+    deps = srcs + list(CSRC.glob("*.hpp")) + list(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "vx.h", HERE.parent / "include" / "veritas_gb300.hpp",
                                               HERE / "driver" / "veritas_gb300_run.cpp", Path(__file__)]
     if LIB.exists() and (HERE / "veritas_gb300_run").exists() and not force:
         t = LIB.stat().st_mtime

@@ -135,6 +135,16 @@ int vx_ctx_set_launch_mode(vx_ctx *ctx, int graphs, int pdl) {
     return guard([&] { ctx->eng->set_launch_mode(graphs != 0, pdl != 0); });
 }
 
+int vx_ctx_set_persistent(vx_ctx *ctx, int on) {
+    if (!ctx) return VX_ERR_INVALID;
+    return guard([&] { ctx->eng->set_persistent(on != 0); });
+}
+
+int vx_ctx_set_persistent_limit(vx_ctx *ctx, uint64_t limit_ns, int phantom) {
+    if (!ctx) return VX_ERR_INVALID;
+    return guard([&] { ctx->eng->set_persistent_limit(limit_ns, phantom); });
+}
+
 int vx_ctx_kernel_launches(vx_ctx *ctx, uint64_t *out) {
     if (!ctx || !out) return VX_ERR_INVALID;
     *out = ctx->eng->kernel_launches;

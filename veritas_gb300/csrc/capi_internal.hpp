@@ -33,6 +33,9 @@ int guard(F &&f) {
     } catch (const CudaError &e) {
         g_err = e.what();
         return VX_ERR_CUDA;
+    } catch (const TimeoutError &e) {
+        g_err = e.what();
+        return VX_ERR_TIMEOUT;
     } catch (const std::invalid_argument &e) {
         g_err = e.what();
         return VX_ERR_INVALID;

@@ -691,7 +691,10 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     return out;
 }
 
-void Engine::sync() { VX_CUDA(cudaStreamSynchronize(stream)); }
+void Engine::sync() {
+    VX_CUDA(cudaStreamSynchronize(stream));
+    check_device_errors();
+}
 
 // Drop every cached launch set that refers to a run being destroyed.
 void Engine::forget(Run *r) {
@@ -906,6 +909,12 @@ void Engine::build_set(LaunchSet &L) {
         gather(CSyncOp{}, [](Run &R) -> DevBuf & { return R.dcsync_ops; },
                [](Run &R) -> const std::vector<int> & { return R.csync_b.ptr; }, merge_csync_ops, L.dcsync,
                L.csync_ptr);
+        L.max_batch = 0;
+        for (const std::vector<int> *p : {&L.ghost_ptr, &L.iface_ptr, &L.csync_ptr})
+            for (size_t b = 0; b + 1 < p->size(); b++) L.max_batch = std::max(L.max_batch, (*p)[b + 1] - (*p)[b]);
+        L.dghost_ptr = upload(L.ghost_ptr, stream);
+        L.diface_ptr = upload(L.iface_ptr, stream);
+        L.dcsync_ptr = upload(L.csync_ptr, stream);
     }
     // Moment work units (FP64: blocks of kMomCols columns of one patch; FP32: one column
     // per warp) longest first: a unit's time grows with its patch's n_p and sub-columns,
@@ -1027,6 +1036,10 @@ StageLaunches Engine::stage_launches(LaunchSet &L) {
 // The kernel sequence of one full RK step (SolverManager.cpp:28-39 -> Mesh.cpp:64-89,
 // EMSolver.cpp:104-202) for every run of the set.
 void Engine::record_step(LaunchSet &L) {
+    if (persistent && L.precision == kF32) {
+        record_step_persistent32(L);
+        return;
+    }
     int launches = 0;
     StageLaunches K = stage_launches(L);
     FctLaunch &fl = K.fl;
@@ -1119,7 +1132,103 @@ void Engine::record_step(LaunchSet &L) {
         }
         VX_CUDA(cudaStreamWaitEvent(stream, ev_mx, 0));
     }
-    launches_per_step_ = launches;
+    L.launches_per_step = launches;
+}
+
+// The persistent form of an FP32 set's step: per RK stage the moments and assembly in
+// one cooperative launch, the Poisson solve, then the FCT stage with the Maxwell stage
+// beside it in a second cooperative launch (stage32.cu) — three launches per stage, in
+// stream order (the solve no longer overlaps the x-direction fluxes: they share the
+// second launch with the p-direction ones).
+void Engine::record_step_persistent32(LaunchSet &L) {
+    if (!gsync_.p) throw std::logic_error("persistent form recorded without its barrier state");
+    StageLaunches K = stage_launches(L);
+    Stage32Launch S{};
+    S.fl = K.fl;
+    S.ml = K.ml;
+    S.al = K.al;
+    S.mx = K.mx;
+    S.mx.asq32_out = 1;  // the next stage's x fluxes run beside its moments (see launch_stage32_pre)
+    S.ghost = L.dghost.as<GhostOp>();
+    S.ghost_ptr = L.dghost_ptr.as<int>();
+    S.nghost_b = L.ghost_ptr.empty() ? 0 : (int)L.ghost_ptr.size() - 1;
+    S.iface = L.diface.as<IfaceOp>();
+    S.iface_ptr = L.diface_ptr.as<int>();
+    S.niface_b = L.iface_ptr.empty() ? 0 : (int)L.iface_ptr.size() - 1;
+    S.csync = L.dcsync.as<CSyncOp>();
+    S.csync_ptr = L.dcsync_ptr.as<int>();
+    S.ncsync_b = L.csync_ptr.empty() ? 0 : (int)L.csync_ptr.size() - 1;
+    S.max_batch = L.max_batch;
+    S.sync = gsync_.as<GridSyncState>();
+    S.limit_ns = persist_limit_ns;
+    S.phantom = persist_phantom;
+    S.stream = stream;
+    PoissonLaunch pl = K.pl;
+    pl.stream = stream;
+    unsigned long long *tr = stage_trace_.as<unsigned long long>();
+    for (int s = 0; s < 6; s++) {
+        S.step = s;
+        S.fl.step = s;
+        S.mx.step = s;
+        S.ml.acell = s == 0;
+        S.trace = tr ? tr + (2 * s) * kStageTraceSlots : nullptr;
+        launch_stage32_pre(S);
+        run_poisson(L, pl);
+        S.trace = tr ? tr + (2 * s + 1) * kStageTraceSlots : nullptr;
+        launch_stage32_fct(S);
+    }
+    L.launches_per_step = 18;
+    gsync_pending_ = true;
+}
+
+void Engine::set_persistent(bool on) {
+    sync();
+    if (on && !gsync_.p) gsync_ = DevBuf(sizeof(GridSyncState));  // zeroed; not during a capture
+    if (on && !stage_trace_.p && std::getenv("VX_TRACE_STAGE"))
+        stage_trace_ = DevBuf(12 * kStageTraceSlots * sizeof(unsigned long long));
+    persistent = on;
+    for (auto &kv : sets_)
+        if (kv.second->graph) {
+            cudaGraphExecDestroy(kv.second->graph);
+            kv.second->graph = nullptr;
+        }
+}
+
+void Engine::set_persistent_limit(unsigned long long limit_ns, int phantom) {
+    if (limit_ns == 0 || phantom < 0) throw std::invalid_argument("persistent barrier limit must be > 0, phantom >= 0");
+    set_persistent(persistent);  // the captured graphs hold the old values
+    persist_limit_ns = limit_ns;
+    persist_phantom = phantom;
+}
+
+void Engine::check_device_errors() {
+    if (!gsync_pending_ || !gsync_.p) return;
+    gsync_pending_ = false;
+    if (stage_trace_.p) {  // per launch: each phase's work (to its last arrival) and the barrier's release
+        std::vector<unsigned long long> t(12 * kStageTraceSlots);
+        VX_CUDA(cudaMemcpy(t.data(), stage_trace_.p, t.size() * sizeof(t[0]), cudaMemcpyDeviceToHost));
+        for (int l = 0; l < 12; l++) {
+            const unsigned long long *q = &t[(size_t)l * kStageTraceSlots];
+            std::fprintf(stderr, "vx stage %d %s:", l / 2, l % 2 ? "fct" : "pre");
+            unsigned long long prev = q[0];
+            for (int k = 1; 2 * k < kStageTraceSlots; k++) {
+                const unsigned long long arr = q[2 * k - 1], ex = q[2 * k];
+                if (arr < prev || arr == 0) break;
+                std::fprintf(stderr, " %.1f", (arr - prev) * 1e-3);
+                if (ex < arr) break;  // the launch's end (no barrier after its last phase)
+                std::fprintf(stderr, "+%.1f", (ex - arr) * 1e-3);
+                prev = ex;
+            }
+            std::fprintf(stderr, " us\n");
+        }
+    }
+    GridSyncState h{};
+    VX_CUDA(cudaMemcpy(&h, gsync_.p, sizeof h, cudaMemcpyDeviceToHost));
+    if (h.err != 0) {
+        VX_CUDA(cudaMemset(gsync_.p, 0, sizeof(GridSyncState)));
+        throw TimeoutError("persistent stage kernel: the wait at grid barrier " + std::to_string(h.err) +
+                           " ran out (the step's results are not valid)");
+    }
 }
 
 // The dt-scaled weights of RK stage st: FCT [0..5] and their left-to-right sum [6] (as
@@ -1274,7 +1383,7 @@ void Engine::advance(const std::vector<Run *> &set, const std::vector<double> &d
     } else {
         record_step(L);
     }
-    kernel_launches += launches_per_step_;
+    kernel_launches += L.launches_per_step;
     VX_CUDA(cudaGetLastError());
 }
 

@@ -23,6 +23,10 @@ namespace vx {
 struct CudaError : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
+// A bounded device wait ran out (a persistent stage kernel's grid barrier).
+struct TimeoutError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
 void cuda_check(cudaError_t e, const char *what);
 #define VX_CUDA(x) ::vx::cuda_check((x), #x)
 
@@ -210,6 +214,9 @@ struct LaunchSet {
     int fast64 = 0;  // FP64 sets: contracted FCT kernels
     DevBuf dpf;  // per-run PoissonFastDev (scan Poisson sets)
     std::vector<int> ghost_ptr, iface_ptr, csync_ptr;
+    DevBuf dghost_ptr, diface_ptr, dcsync_ptr;  // the batch offsets on the device (persistent form)
+    int max_batch = 0;                          // largest op batch
+    int launches_per_step = 0;                  // kernels of one recorded step
     cudaGraphExec_t graph = nullptr;
     ~LaunchSet();
 };
@@ -269,6 +276,18 @@ public:
     // CUDA graph per step and programmatic dependent launch on or off; drops the
     // captured graphs (they hold the old launch attributes).
     void set_launch_mode(bool graphs, bool pdl);
+    // FP32 sets: each RK stage as the persistent stage kernels (stage32.cu) instead of one
+    // launch per sub-step; drops the captured graphs.
+    void set_persistent(bool on);
+    bool persistent = false;
+    // Wait limit of the persistent kernels' grid barriers, and arrivals each barrier waits
+    // for beyond the grid's (0; the failure test makes every wait run out with it).
+    void set_persistent_limit(unsigned long long limit_ns, int phantom);
+    unsigned long long persist_limit_ns = 2000000000ull;
+    int persist_phantom = 0;
+    // Throws TimeoutError if a persistent kernel's barrier wait ran out since the last
+    // check (called by sync(), once the stream is idle), clearing the record.
+    void check_device_errors();
     // Drops every cached launch set but the listed ones (their tables and graphs hold
     // device memory; a serving loop keeps only the sets of its current step).
     void retain_sets(const std::vector<std::vector<Run *>> &keep);
@@ -280,8 +299,11 @@ private:
     void build_set(LaunchSet &L);
     void build_tiles(LaunchSet &L);
     void record_step(LaunchSet &L);
+    void record_step_persistent32(LaunchSet &L);
     StageLaunches stage_launches(LaunchSet &L);
-    int launches_per_step_ = 0;
+    DevBuf gsync_;               // GridSyncState of the persistent kernels
+    DevBuf stage_trace_;         // VX_TRACE_STAGE=1: clock trace of the persistent kernels of a step
+    bool gsync_pending_ = false;  // persistent kernels ran since the last check
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
     DevBuf flush_;
 };

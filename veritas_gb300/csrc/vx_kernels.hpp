@@ -186,6 +186,8 @@ struct MaxwellLaunch {
     const double *params;  // per-run stage parameter blocks
     const double *dxinv;   // per run: 1/dx0
     int f32;               // precision-32 sets: also the FP32 per-cell A^2 (k_mx_update)
+    int asq32_out = 0;     // the face a^2 step also writes the FP32 copy of a^2 (persistent form:
+                           // nothing reads that copy between this step and the next stage)
     cudaStream_t stream;
 };
 void launch_maxwell(const MaxwellLaunch &L);
@@ -238,5 +240,69 @@ void launch_xfer(const void *patches, const XferOp *ops, int n, uint8_t *mask, i
 
 // dst[i] = -src[i]
 void launch_negate(double *dst, const double *src, int n, cudaStream_t s);
+
+// ---------------------------------------------------------------- FP32 launch sets (stage32.cu)
+// The op batches, assembly and Maxwell stage of FP32 launch sets, as kernels over the same
+// bodies as the persistent stage kernels below (one compilation, so the per-sub-step and
+// the persistent forms give the same bits).
+void launch_ghost32(const void *patches, const GhostOp *ops, int n, int slot, cudaStream_t s);
+void launch_iface32(const void *patches, const IfaceOp *ops, int n, int step, cudaStream_t s);
+void launch_csync32(const void *patches, const CSyncOp *ops, int n, cudaStream_t s);
+void launch_assemble32(const AsmLaunch &A);
+void launch_maxwell32(const MaxwellLaunch &L);
+
+// Persistent form of an FP32 launch set's RK stage: two cooperative launches per stage
+// around the Poisson solve, each running its phases over every patch of every run, the
+// phases separated by grid-wide barriers.  A barrier waits at most limit_ns (and a fixed
+// number of polls); a wait that runs out records 1 + its barrier index in err, and every
+// later barrier of that and following launches passes without waiting until the host has
+// read and cleared it, so a lost block can only cost time, never hang the stream.
+struct GridSyncState {
+    unsigned arrive;      // barrier arrivals of the running launch (the last block out resets it)
+    unsigned pad0[31];
+    unsigned released;    // barriers of the running launch whose last arrival has come
+    unsigned pad1[31];    // (its own 128-byte line: the waiting blocks poll it, the arrivals add elsewhere)
+    unsigned leave;       // blocks that finished the running launch
+    int err;              // 0, or the index (from 1) of the first barrier whose wait ran out
+    unsigned pad2[30];
+    unsigned next;        // work counter of the running phase (reset by each barrier's release)
+    unsigned pad3[31];
+};
+struct Stage32Launch {
+    FctLaunch fl;      // patches, tile and strip lists, fields, FP32 stage weights
+    MomLaunch ml;      // moments (acell: refresh the per-cell A^2 copy first)
+    AsmLaunch al;      // assembly of rho and J
+    MaxwellLaunch mx;  // Maxwell stage
+    const GhostOp *ghost;  // op tables and their batch offsets (device arrays)
+    const int *ghost_ptr;
+    int nghost_b;
+    const IfaceOp *iface;
+    const int *iface_ptr;
+    int niface_b;
+    const CSyncOp *csync;
+    const int *csync_ptr;
+    int ncsync_b;
+    int max_batch;     // largest op batch (grid sizing)
+    int step;          // RK stage 0..5
+    GridSyncState *sync;
+    unsigned long long limit_ns;
+    int phantom;       // arrivals each barrier waits for beyond the grid's (0; > 0 makes every wait run out)
+    // Optional clock trace (kStageTraceSlots per launch, ns): [0] the launch's start on
+    // block 0, [2k - 1] the last arrival at barrier k, [2k] block 0 leaving it.
+    unsigned long long *trace;
+    cudaStream_t stream;
+};
+constexpr int kStageTraceSlots = 128;
+// [per-cell A^2 and a^2 copies] | moments + x fluxes | assembly: the x fluxes need neither
+// E_x nor rho, so they run beside the moments, before the Poisson solve that separates the
+// two launches; the FP32 a^2 copy they read comes from the previous stage's Maxwell step
+// (MaxwellLaunch::asq32_out), or at stage 0 from the copy phase
+void launch_stage32_pre(const Stage32Launch &L);
+// p fluxes + Maxwell right-hand side | interface flux batches | ds/f2 + Maxwell update |
+// ghost batches (f2) | limiter R + face a^2 | limiter C | C exchange batches | update |
+// ghost batches (f1) | [f0 = f1]
+void launch_stage32_fct(const Stage32Launch &L);
+// Blocks of each persistent kernel one launch may use (co-resident on every SM).
+int stage32_grid_limit(int which_fct);
 
 }  // namespace vx
