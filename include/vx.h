@@ -232,6 +232,15 @@ int vx_ctx_set_persistent(vx_ctx *ctx, int on);
  * waits for beyond the launch's own blocks (default 0; any phantom > 0 makes every wait
  * run out — the failure path's test). */
 int vx_ctx_set_persistent_limit(vx_ctx *ctx, uint64_t limit_ns, int phantom);
+/* Pipelined moments and exact Poisson solve (no reference counterpart; on by default):
+ * on != 0 runs, for FP64 runs with the exact solve advanced alone or in sets of up to four,
+ * EMFieldSolver::AssembleRhoAndJ and UpdatePotential of each RK stage as one launch in
+ * which the solve's forward sweep follows the moment columns as they are completed (the
+ * columns go out in the order the sweep needs them) instead of starting after all of them.
+ * Same bits as the separate kernels (on == 0).  Its waits are bounded by the limit and
+ * phantom count of vx_ctx_set_persistent_limit; a wait that runs out is reported as
+ * VX_ERR_TIMEOUT by the next call that synchronises the context. */
+int vx_ctx_set_pipelined(vx_ctx *ctx, int on);
 int vx_ctx_sync(vx_ctx *ctx);
 /* Kernels launched by this context so far (graph replays count their nodes). */
 int vx_ctx_kernel_launches(vx_ctx *ctx, uint64_t *out);
@@ -337,7 +346,9 @@ int vx_ctx_timer_end(vx_ctx *ctx, double *ms);
 /* Time the run's Vlasov kernels in isolation: reps back-to-back launches per kernel on
  * the context stream (after one untimed launch).  out_ms[k] receives the mean launch
  * time of kernel k in the order gamma, faces, flux, ds_f2, limR, limC, update,
- * moments (log table + ordered sums), assemble; *count is set to the number of entries
+ * moments (log table + ordered sums), assemble, poisson, maxwell, ghost, iface, csync
+ * (all batches of each kind), moments_poisson (the pipelined moments + assembly + exact
+ * solve launch; 0 where the run does not use it); *count is set to the number of entries
  * written (<= cap).  Each timed kernel is idempotent, so the run's state is unchanged. */
 int vx_run_profile_kernels(vx_run *run, int reps, double *out_ms, int cap, int *count);
 

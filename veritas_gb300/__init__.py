@@ -131,6 +131,7 @@ def _load() -> ctypes.CDLL:
         "vx_ctx_set_launch_mode": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
         "vx_ctx_set_persistent": (ctypes.c_int, [vp, ctypes.c_int]),
         "vx_ctx_set_persistent_limit": (ctypes.c_int, [vp, ctypes.c_uint64, ctypes.c_int]),
+        "vx_ctx_set_pipelined": (ctypes.c_int, [vp, ctypes.c_int]),
         "vx_ctx_kernel_launches": (ctypes.c_int, [vp, P(ctypes.c_uint64)]),
         "vx_run_create": (ctypes.c_int, [vp, P(_Problem), P(vp)]),
         "vx_run_destroy": (ctypes.c_int, [vp]),
@@ -304,6 +305,12 @@ class Context:
         run out (failure-path test)."""
         _check(_lib.vx_ctx_set_persistent_limit(self._h, int(limit_ns), int(phantom)))
 
+    def set_pipelined(self, on: bool = True) -> None:
+        """FP64 runs with the exact solve (alone or up to four together): moments, assembly
+        and solve of each RK stage in one launch whose solve follows the moments as they
+        finish (on by default); off runs the three kernels one after another.  Same bits."""
+        _check(_lib.vx_ctx_set_pipelined(self._h, int(on)))
+
     def kernel_launches(self) -> int:
         v = ctypes.c_uint64()
         _check(_lib.vx_ctx_kernel_launches(self._h, ctypes.byref(v)))
@@ -473,7 +480,7 @@ class SolverManager:
         return out
 
     PROFILE_KERNELS = ["gamma", "faces", "flux", "ds_f2", "limR", "limC", "update", "moments", "assemble", "poisson",
-                       "maxwell", "ghost", "iface", "csync"]
+                       "maxwell", "ghost", "iface", "csync", "moments_poisson"]
 
     def profile_kernels(self, reps: int = 5) -> dict:
         buf = (ctypes.c_double * 16)()

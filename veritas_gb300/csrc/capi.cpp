@@ -145,6 +145,11 @@ int vx_ctx_set_persistent_limit(vx_ctx *ctx, uint64_t limit_ns, int phantom) {
     return guard([&] { ctx->eng->set_persistent_limit(limit_ns, phantom); });
 }
 
+int vx_ctx_set_pipelined(vx_ctx *ctx, int on) {
+    if (!ctx) return VX_ERR_INVALID;
+    return guard([&] { ctx->eng->set_pipelined(on != 0); });
+}
+
 int vx_ctx_kernel_launches(vx_ctx *ctx, uint64_t *out) {
     if (!ctx || !out) return VX_ERR_INVALID;
     *out = ctx->eng->kernel_launches;

@@ -331,6 +331,7 @@ void Run::upload_lu() {
     cudaStream_t st = eng->stream;
     auto Lb = lu.lower_band();
     auto Ub = lu.upper_band();
+    pipe_rfc = lu.first_read_chunk(Lb, kPoisRowsHost);
     dlu_perm = upload(lu.perm, st);
     dlb_band = upload(Lb.band, st);
     dlb_fptr = upload(Lb.fptr, st);
@@ -485,6 +486,10 @@ Engine::Engine(int dev) : device(dev) {
     VX_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     VX_CUDA(cudaEventCreateWithFlags(&ev_gamma, cudaEventDisableTiming));
     VX_CUDA(cudaEventCreateWithFlags(&ev_mx, cudaEventDisableTiming));
+    int lo = 0, hi = 0;
+    VX_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    prio_hi_ = hi;
+    VX_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
 }
 
 Engine::~Engine() {
@@ -688,6 +693,39 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
         for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++)
             launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], L.precision, stream);
     });
+    // FP64 exact-solve runs: the pipelined moments + assembly + solve launch (alone here,
+    // without the face kernels that share the GPU with it inside a step)
+    if (L.pipe) {
+        StageLaunches K = stage_launches(L);
+        K.ml.acell = 0;
+        PipeLaunch P = pipe_launch(L, K);
+        time_it([&] { launch_moments_poisson64(P); });
+        pipe_pending_ = true;
+        // VX_TRACE_PIPE=1: when each forward chunk's rows were ready, when the sweeps ended
+        // and when each chunk's last moment unit finished (ns from the solve's start)
+        if (std::getenv("VX_TRACE_PIPE")) {
+            const int nch = (L.runs[0]->n + kPoisRowsHost - 1) / kPoisRowsHost;
+            DevBuf tr((size_t)(1 + 2 * nch) * sizeof(unsigned long long));
+            DevBuf tp((size_t)(2 * nch + 2) * sizeof(unsigned long long));
+            P.trace = tr.as<unsigned long long>();
+            P.trace_nch = nch;
+            P.P.trace = tp.as<unsigned long long>();
+            launch_moments_poisson64(P);
+            sync();
+            std::vector<unsigned long long> a(1 + 2 * nch), b(2 * nch + 1);
+            VX_CUDA(cudaMemcpy(a.data(), tr.p, a.size() * sizeof(a[0]), cudaMemcpyDeviceToHost));
+            VX_CUDA(cudaMemcpy(b.data(), tp.p, b.size() * sizeof(b[0]), cudaMemcpyDeviceToHost));
+            const double t0 = (double)a[0];
+            std::fprintf(stderr, "vx pipe n=%d chunks=%d units=%d (us from the solve's start)\n", L.runs[0]->n, nch,
+                         L.pipe_nunits);
+            for (int c = 0; c < nch; c++)
+                std::fprintf(stderr, "  chunk %2d: units done %8.1f rows ready %8.1f forward end %8.1f backward end %8.1f\n",
+                             c, a[1 + nch + c] ? (a[1 + nch + c] - t0) * 1e-3 : -1.0, (a[1 + c] - t0) * 1e-3,
+                             (b[1 + c] - t0) * 1e-3, (b[1 + nch + (nch - 1 - c)] - t0) * 1e-3);
+        }
+    } else {
+        out.push_back(0.0);
+    }
     return out;
 }
 
@@ -943,6 +981,7 @@ void Engine::build_set(LaunchSet &L) {
         colidx.swap(ci2);
     }
     L.ncols = (int)colpatch.size();
+    build_pipe_tables(L, colpatch, colidx);
     // lvl_ptr is absolute; lvl_off points at each run's block.
     L.dpatch = upload(L.hpatch, stream);
     build_tiles(L);
@@ -971,6 +1010,102 @@ void Engine::build_set(LaunchSet &L) {
         L.graph = nullptr;
     }
     sync();
+}
+
+// Tables of the pipelined moments + solve launch (k64_moments_poisson) for an FP64 set
+// with the exact solve: the moment units in the order the forward sweeps first need their
+// columns, the done counter each unit adds to, and per run and forward chunk the rows
+// whose right-hand side the chunk reads first.  A unit covers finest x positions
+// [(x_pos * rtb) + c, ... + rtb) for each of its columns c = i * rtb; row k's right-hand
+// side comes from position perm[k].
+void Engine::build_pipe_tables(LaunchSet &L, const std::vector<int> &colpatch, const std::vector<int> &colidx) {
+    L.pipe = false;
+    if (L.precision != kF64 || L.poisson != kPoissonLU || L.runs.empty() || (int)L.runs.size() > kPipeMaxRuns) return;
+    for (Run *R : L.runs)
+        if (R->pipe_rfc.empty() || (int)R->pipe_rfc.size() != R->n) return;
+    const int R = kPoisRowsHost;
+    std::vector<int> run_ctr, run_gptr, gptr, grow, need;
+    std::vector<std::vector<int>> xfc(L.runs.size());  // per run and x position: first chunk needing it
+    for (size_t ri = 0; ri < L.runs.size(); ri++) {
+        const Run &Rn = *L.runs[ri];
+        const int n = Rn.n, nch = (n + R - 1) / R;
+        run_ctr.push_back((int)need.size());
+        need.resize(need.size() + nch, 0);
+        xfc[ri].assign(n, 0);
+        for (int k = 0; k < n; k++) xfc[ri][Rn.lu.perm[k]] = Rn.pipe_rfc[k];
+        // rows grouped by the chunk that reads them first, ascending within a chunk
+        run_gptr.push_back((int)gptr.size());
+        std::vector<int> cnt(nch + 1, 0);
+        for (int k = 0; k < n; k++) cnt[Rn.pipe_rfc[k] + 1]++;
+        for (int c = 0; c < nch; c++) cnt[c + 1] += cnt[c];
+        const int base = (int)grow.size();
+        for (int c = 0; c <= nch; c++) gptr.push_back(base + cnt[c]);
+        grow.resize(base + n);
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+        for (int k = 0; k < n; k++) grow[base + fill[Rn.pipe_rfc[k]]++] = k;
+    }
+    const int nunits = (int)colpatch.size() / kMomCols;
+    std::vector<int> ufc(nunits, 0), urun(nunits, 0);
+    for (int u = 0; u < nunits; u++) {
+        const PatchT<double> &P = L.hpatch[colpatch[(size_t)u * kMomCols]];
+        const int ri = P.run;
+        const std::vector<int> &xf = xfc[ri];
+        int fc = INT32_MAX;
+        for (int w = 0; w < kMomCols; w++) {
+            if (colpatch[(size_t)u * kMomCols + w] < 0) continue;
+            const int x0 = P.x_pos * P.rtb + colidx[(size_t)u * kMomCols + w];
+            for (int k = 0; k < P.rtb; k++) {
+                const int x = x0 + k;
+                if (x < 0 || x >= (int)xf.size()) return;  // not a layout the pipelined form covers
+                fc = std::min(fc, xf[x]);
+            }
+        }
+        if (fc == INT32_MAX) return;
+        ufc[u] = fc;
+        urun[u] = ri;
+    }
+    // units by first needed chunk (then the longest-first order they already have); a
+    // unit's items (p windows of each sub-column pair) are consecutive tickets
+    std::vector<int> order(nunits);
+    for (int u = 0; u < nunits; u++) order[u] = u;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ufc[a] < ufc[b]; });
+    std::vector<int> col0(nunits), sig(nunits), item0(nunits + 1, 0), nwin(nunits), item_unit;
+    std::vector<double2> c12(nunits);
+    for (int t = 0; t < nunits; t++) {
+        const int u = order[t];
+        const PatchT<double> &P = L.hpatch[colpatch[(size_t)u * kMomCols]];
+        col0[t] = u * kMomCols;
+        sig[t] = run_ctr[urun[u]] + ufc[u];
+        need[sig[t]]++;
+        nwin[t] = (P.np + kMomWindow - 1) / kMomWindow;
+        const int items = (P.rtb + 1) / 2 * nwin[t];
+        item0[t + 1] = item0[t] + items;
+        item_unit.insert(item_unit.end(), items, t);
+        // the moments' (1 / m) / c and its reciprocal, in their operations
+        const double minv = 1 / P.mass;
+        const double c1 = minv * kCInv;
+        c12[t] = make_double2(c1, 1 / c1);
+    }
+    const int nitems = item0[nunits];
+    if ((size_t)nitems * kPipeItemDoubles * sizeof(double) > kPipeMaxScratch) return;
+    L.pipe_nunits = nunits;
+    L.pipe_nitems = nitems;
+    L.pipe_ndone = (int)need.size();
+    L.dpipe_col0 = upload(col0, stream);
+    L.dpipe_sig = upload(sig, stream);
+    L.dpipe_item0 = upload(item0, stream);
+    L.dpipe_nwin = upload(nwin, stream);
+    L.dpipe_c12 = upload(c12, stream);
+    L.dpipe_items = upload(item_unit, stream);
+    L.dpipe_need = upload(need, stream);
+    L.dpipe_runctr = upload(run_ctr, stream);
+    L.dpipe_rungptr = upload(run_gptr, stream);
+    L.dpipe_gptr = upload(gptr, stream);
+    L.dpipe_grow = upload(grow, stream);
+    L.dpipe_scratch = DevBuf((size_t)nitems * kPipeItemDoubles * sizeof(double));
+    L.dpipe_state = DevBuf((size_t)(kPipeDone + L.pipe_ndone + nunits) * sizeof(unsigned));  // zeroed
+    if (!pipe_err_.p) pipe_err_ = DevBuf(sizeof(int));
+    L.pipe = true;
 }
 
 // Launch descriptors of a set's step kernels (tables, tiles, fields, parameter blocks).
@@ -1047,7 +1182,12 @@ void Engine::record_step(LaunchSet &L) {
     AsmLaunch &al = K.al;
     PoissonLaunch &pl = K.pl;
     MaxwellLaunch &mx = K.mx;
+    const bool pipe = pipelined && L.pipe;
     for (int s = 0; s < 6; s++) {
+        if (pipe) {
+            record_pipe_stage(L, K, s, launches);
+            continue;
+        }
         // FP32 copies of the fields: E_x's comes with each solve (k_efield), the per-cell
         // A^2 the moments read with each Maxwell stage for the next one (the step's first
         // stage makes its own), a^2's with the moments at every stage (the Maxwell stage
@@ -1133,6 +1273,108 @@ void Engine::record_step(LaunchSet &L) {
         VX_CUDA(cudaStreamWaitEvent(stream, ev_mx, 0));
     }
     L.launches_per_step = launches;
+    if (pipe) pipe_pending_ = true;
+}
+
+// One RK stage of an FP64 exact-solve set in the pipelined form.  Main stream: the
+// moments + solve launch, then (once the faces beside it are done) the E_x-dependent half
+// of the p faces and the rest of the FCT chain.  Side stream, beside the launch: gamma, the
+// x faces and fluxes and the E_x-independent half of the p faces (none reads rho, J or
+// E_x), then the Maxwell stage after the launch (it reads J and rewrites A, which gamma
+// reads).  The launch carries the highest stream priority, so its moment blocks go ahead
+// of the face blocks and the solve's inputs arrive as early as possible.
+PipeLaunch Engine::pipe_launch(LaunchSet &L, const StageLaunches &K) {
+    PipeLaunch P{};
+    P.M = K.ml;
+    P.A = K.al;
+    P.P = K.pl;
+    P.P.stream = stream;
+    P.unit_col0 = L.dpipe_col0.as<int>();
+    P.unit_sig = L.dpipe_sig.as<int>();
+    P.unit_item0 = L.dpipe_item0.as<int>();
+    P.unit_nwin = L.dpipe_nwin.as<int>();
+    P.unit_c12 = L.dpipe_c12.as<double2>();
+    P.nunits = L.pipe_nunits;
+    P.item_unit = L.dpipe_items.as<int>();
+    P.nitems = L.pipe_nitems;
+    P.scratch = L.dpipe_scratch.as<double>();
+    P.workers = std::max(1, std::min(num_sms_ - (int)L.runs.size(), (L.pipe_nitems + 1) / 2));
+    P.need = L.dpipe_need.as<int>();
+    P.ndone = L.pipe_ndone;
+    P.run_ctr = L.dpipe_runctr.as<int>();
+    P.run_gptr = L.dpipe_rungptr.as<int>();
+    P.gptr = L.dpipe_gptr.as<int>();
+    P.grow = L.dpipe_grow.as<int>();
+    P.state = L.dpipe_state.as<unsigned>();
+    P.err = pipe_err_.as<int>();
+    P.limit_ns = persist_limit_ns;
+    P.phantom = persist_phantom;
+    P.priority = prio_hi_;
+    P.stream = stream;
+    return P;
+}
+
+void Engine::record_pipe_stage(LaunchSet &L, StageLaunches &K, int s, int &launches) {
+    FctLaunch &fl = K.fl;
+    MaxwellLaunch &mx = K.mx;
+    const PipeLaunch P = pipe_launch(L, K);
+    VX_CUDA(cudaEventRecord(ev_fork, stream));
+    VX_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+    launch_moments_poisson64(P);
+    VX_CUDA(cudaEventRecord(ev_join, stream));
+    fl.step = s;
+    fl.stream = side;
+    fct_sub(L, fl, kSubGamma);
+    fl.part = 1;
+    fct_sub(L, fl, kSubFaces);
+    fct_sub(L, fl, kSubFlux);
+    fl.part = 4;
+    fct_sub(L, fl, kSubFaces);
+    VX_CUDA(cudaEventRecord(ev_gamma, side));
+    VX_CUDA(cudaStreamWaitEvent(side, ev_join, 0));
+    mx.step = s;
+    mx.stream = side;
+    launch_maxwell(mx);
+    VX_CUDA(cudaEventRecord(ev_mx, side));
+    launches += 1 + 4 + 3;
+    fl.stream = stream;
+    VX_CUDA(cudaStreamWaitEvent(stream, ev_gamma, 0));
+    fl.part = 8;
+    fct_sub(L, fl, kSubFaces);
+    fl.part = 2;
+    fct_sub(L, fl, kSubFlux);
+    fl.part = 0;
+    launches += 2;
+    for (size_t b = 0; b + 1 < L.iface_ptr.size(); b++, launches++)
+        launch_iface(L.dpatch.p, L.diface.as<IfaceOp>() + L.iface_ptr[b], L.iface_ptr[b + 1] - L.iface_ptr[b], s, L.precision, stream);
+    fct_sub(L, fl, kSubDsF2);
+    launches += 1;
+    for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
+        launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 2, L.precision, stream);
+    fct_sub(L, fl, kSubLimR);
+    fct_sub(L, fl, kSubLimC);
+    launches += 2;
+    for (size_t b = 0; b + 1 < L.csync_ptr.size(); b++, launches++)
+        launch_csync(L.dpatch.p, L.dcsync.as<CSyncOp>() + L.csync_ptr[b], L.csync_ptr[b + 1] - L.csync_ptr[b], L.precision, stream);
+    fct_sub(L, fl, kSubUpdate);
+    launches += 1;
+    for (size_t b = 0; b + 1 < L.ghost_ptr.size(); b++, launches++)
+        launch_ghost(L.dpatch.p, L.dghost.as<GhostOp>() + L.ghost_ptr[b], L.ghost_ptr[b + 1] - L.ghost_ptr[b], 1, L.precision, stream);
+    if (s == 5) {
+        fct_sub(L, fl, kSubCopy10);
+        launches += 1;
+    }
+    VX_CUDA(cudaStreamWaitEvent(stream, ev_mx, 0));
+}
+
+void Engine::set_pipelined(bool on) {
+    sync();
+    pipelined = on;
+    for (auto &kv : sets_)
+        if (kv.second->graph) {
+            cudaGraphExecDestroy(kv.second->graph);
+            kv.second->graph = nullptr;
+        }
 }
 
 // The persistent form of an FP32 set's step: per RK stage the moments and assembly in
@@ -1202,6 +1444,16 @@ void Engine::set_persistent_limit(unsigned long long limit_ns, int phantom) {
 }
 
 void Engine::check_device_errors() {
+    if (pipe_pending_ && pipe_err_.p) {
+        pipe_pending_ = false;
+        int e = 0;
+        VX_CUDA(cudaMemcpy(&e, pipe_err_.p, sizeof e, cudaMemcpyDeviceToHost));
+        if (e != 0) {
+            VX_CUDA(cudaMemset(pipe_err_.p, 0, sizeof(int)));
+            throw TimeoutError("pipelined moments + Poisson solve: the wait for the moments of done counter " +
+                               std::to_string(e - 1) + " ran out (the step's results are not valid)");
+        }
+    }
     if (!gsync_pending_ || !gsync_.p) return;
     gsync_pending_ = false;
     if (stage_trace_.p) {  // per launch: each phase's work (to its last arrival) and the barrier's release

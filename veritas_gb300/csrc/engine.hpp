@@ -115,6 +115,7 @@ public:
     DevBuf dlu_perm, dlb_band, dlb_fptr, dlb_fcol, dlb_fval, dlb_slot, dlb_sload, dlb_take, dub_band, dub_diag, dub_rdiag, dub_rdlo, dub_fptr, dub_fcol,
         dub_fval;
     LUDev ludev{};
+    std::vector<int> pipe_rfc;  // per row: first forward chunk reading it (empty: no pipelined solve)
     uint64_t layout_version = 0;
     int id = 0;
     int precision = kF64;            // kF64: plain path; kF32: precision form
@@ -217,6 +218,12 @@ struct LaunchSet {
     DevBuf dghost_ptr, diface_ptr, dcsync_ptr;  // the batch offsets on the device (persistent form)
     int max_batch = 0;                          // largest op batch
     int launches_per_step = 0;                  // kernels of one recorded step
+    // FP64 exact-solve sets of up to kPipeMaxRuns runs: tables of the pipelined moments +
+    // solve launch (k64_moments_poisson)
+    bool pipe = false;
+    int pipe_nunits = 0, pipe_nitems = 0, pipe_ndone = 0;
+    DevBuf dpipe_col0, dpipe_sig, dpipe_item0, dpipe_nwin, dpipe_c12, dpipe_items, dpipe_need, dpipe_runctr,
+        dpipe_rungptr, dpipe_gptr, dpipe_grow, dpipe_scratch, dpipe_state;
     cudaGraphExec_t graph = nullptr;
     ~LaunchSet();
 };
@@ -285,6 +292,11 @@ public:
     void set_persistent_limit(unsigned long long limit_ns, int phantom);
     unsigned long long persist_limit_ns = 2000000000ull;
     int persist_phantom = 0;
+    // FP64 exact-solve sets: moments, assembly and solve in one launch whose solve follows
+    // the moments as they finish (on by default; off: the three separate kernels, same bits).
+    // Its waits use the persistent form's limit and phantom count.  Drops the captured graphs.
+    void set_pipelined(bool on);
+    bool pipelined = true;
     // Throws TimeoutError if a persistent kernel's barrier wait ran out since the last
     // check (called by sync(), once the stream is idle), clearing the record.
     void check_device_errors();
@@ -298,12 +310,19 @@ private:
     LaunchSet &get_set(const std::vector<Run *> &set);
     void build_set(LaunchSet &L);
     void build_tiles(LaunchSet &L);
+    void build_pipe_tables(LaunchSet &L, const std::vector<int> &colpatch, const std::vector<int> &colidx);
     void record_step(LaunchSet &L);
     void record_step_persistent32(LaunchSet &L);
     StageLaunches stage_launches(LaunchSet &L);
     DevBuf gsync_;               // GridSyncState of the persistent kernels
     DevBuf stage_trace_;         // VX_TRACE_STAGE=1: clock trace of the persistent kernels of a step
     bool gsync_pending_ = false;  // persistent kernels ran since the last check
+    DevBuf pipe_err_;             // the pipelined solve's wait record (PipeLaunch::err)
+    bool pipe_pending_ = false;   // pipelined launches ran since the last check
+    int prio_hi_ = 0;             // greatest stream priority of the device
+    int num_sms_ = 1;
+    PipeLaunch pipe_launch(LaunchSet &L, const StageLaunches &K);
+    void record_pipe_stage(LaunchSet &L, StageLaunches &K, int s, int &launches);
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
     DevBuf flush_;
 };

@@ -13,7 +13,10 @@ namespace vx {
 // Level::CollectRhoAndJ + EMFieldSolver::AssembleRhoAndJ (Level.cpp:19-62,
 // EMSolver.cpp:104-122): per level, chargeL[x] = 0 + (patch values in patch order);
 // charges_s[x] = 0 + level sums finest->coarsest; J sums species then levels;
-// charge[x] = 0 + species sums.
+// charge[x] = 0 + species sums.  CG: the column sums are read through L2 only (the
+// pipelined solve reads them while the moment blocks that write them still run; see
+// k64_moments_poisson).
+template <bool CG = false>
 __device__ __forceinline__ void assemble_cell(const AsmLaunch &A, int run, int x) {
     const int n = A.run_n[run];
     if (x >= n) return;
@@ -34,6 +37,9 @@ __device__ __forceinline__ void assemble_cell(const AsmLaunch &A, int run, int x
                         const float2 qj = reinterpret_cast<const float2 *>(P.currentR)[c];
                         lc += ((double)qc.x + (double)qc.y) * P.msc_rho;
                         lj += ((double)qj.x + (double)qj.y) * P.msc_j;
+                    } else if (CG) {
+                        lc += __ldcg(P.chargeR + c);
+                        lj += __ldcg(P.currentR + c);
                     } else {
                         lc += P.chargeR[c];
                         lj += P.currentR[c];

@@ -72,28 +72,81 @@ __device__ __forceinline__ double cell_asq(const RunFields &F, int x) {
 // form the next window.
 // The coarse-column list is padded per patch to a multiple of kMomCols (padding: patch
 // -1), so the warps of a block share n_p and rtb and step through the windows together.
-constexpr int kMomOut = 29;  // outputs per window: j0 .. j0+28
+constexpr int kMomOut = kMomWindow;  // outputs per window: j0 .. j0+28
+constexpr int kMomThreads = (kMomCols + 1) * 32;
 
-__global__ void __launch_bounds__((kMomCols + 1) * 32) k64_moments(MomLaunch M) {
-    VX_PDL_WAIT();
-    // two window buffers: the column warps fill one while the summing warp adds the other
-    __shared__ double s_cc[2][kMomCols][2][32], s_cj[2][kMomCols][2][32];
-    __shared__ unsigned s_use[2][kMomCols];
-    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const bool summer = wid == kMomCols;  // the last warp adds; warps 0..kMomCols-1 form columns
-    const int col0 = blockIdx.x * kMomCols;
-    const bool real = !summer && M.colpatch[col0 + wid] >= 0;  // warp-uniform
-    const P64 &P = ((const P64 *)M.patches)[M.colpatch[col0]];  // the block's patch
+// Two window buffers: the column warps fill one while the summing warp adds the other.
+struct MomSmem {
+    double cc[2][kMomCols][2][32], cj[2][kMomCols][2][32];
+    unsigned use[2][kMomCols];
+};
+
+// Barrier of one moment unit's kMomThreads threads: barrier 0 in k64_moments (the whole
+// block), named barriers 1 and 2 for the two units a pipelined block carries.
+__device__ __forceinline__ void mom_sync(int bar) {
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(kMomThreads) : "memory");
+}
+
+// One window of column i's sub-columns k0 .. k0+kg-1 (kg <= 2): lane L covers the p index
+// j = j0 - 1 + L; lanes 1 .. kMomOut return the charge and current contributions cc[q],
+// cj[q] of their cell (zero where the cell is not used) and set `use`.  All 32 lanes
+// take part (shuffles).  a[q]: q^2 A^2 of sub-column k0+q.
+__device__ __forceinline__ void mom_window(const P64 &P, const double *f, bool real, int i, int j0, int k0, int kg,
+                                           const double a[2], double c1, double c2, int lane, double cc[2],
+                                           double cj[2], bool &use) {
+    const unsigned full = 0xffffffffu;
+    const double c3 = 1 / 48.0;
     const int np = P.np, rtb = P.rtb, pit = P.pitch;
+    const int j = j0 - 1 + lane;  // this lane's p index
+    double p = 0.0, f3 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0, cor = 0.0;
+    use = false;
+    if (real) {
+        p = P.pmin + P.dp * (double)(j + P.p_pos);
+        if (j <= np) {
+            if (rtb == 1) f3 = f[pidx(i, j, pit)];
+            else rel_shared(P, f, i, j, f3, a1, a2, a3, cor);
+        }
+        use = lane >= 1 && lane <= kMomOut && j < np && !(P.nested && P.nested[pidx(i, j, pit)]);
+    }
+    for (int q = 0; q < kg; q++) {
+        cc[q] = 0.0;
+        cj[q] = 0.0;
+        if (real) {
+            double G = 0.0, V = 0.0;
+            if (j <= np + 1) {
+                double g = sqrt(1.0 + ((p * p) + a[q]) * P.g2);
+                G = g + c1 * p;
+            }
+            if (j <= np) V = rtb == 1 ? f3 : rel_pick(P, k0 + q, a1, a2, a3, f3) + cor;
+            const double Gn = __shfl_down_sync(full, G, 1);
+            const double L = c2 * log(Gn / G);  // valid for lanes 0..30
+            const double Lm = __shfl_up_sync(full, L, 1);
+            const double Lp = __shfl_down_sync(full, L, 1);
+            const double Vm = __shfl_up_sync(full, V, 1);
+            const double Vp = __shfl_down_sync(full, V, 1);
+            if (use) {
+                cc[q] = V;
+                cj[q] = V * L + c3 * (Lp - Lm) * (Vp - Vm);
+            }
+        }
+    }
+}
+
+// One unit: the kMomCols columns col0 .. col0 + kMomCols - 1 of the padded column list,
+// formed by warps 0 .. kMomCols - 1 and summed by warp kMomCols (wid: warp within the unit).
+__device__ __forceinline__ void moments_unit(const MomLaunch &M, int col0, int wid, int lane, MomSmem &S, int bar) {
+    const bool summer = wid == kMomCols;  // the last warp adds; warps 0..kMomCols-1 form columns
+    const bool real = !summer && M.colpatch[col0 + wid] >= 0;  // warp-uniform
+    const P64 &P = ((const P64 *)M.patches)[M.colpatch[col0]];  // the unit's patch
+    const int np = P.np, rtb = P.rtb;
     const int i = summer ? 0 : M.colidx[col0 + wid] / rtb;
     const RunFields &F = M.fields[P.run];
     const double minv = 1 / P.mass;
     const double c1 = minv * kCInv;
     const double c2 = 1 / c1;
-    const double c3 = 1 / 48.0;
     const double *f = P.f1;
     const unsigned full = 0xffffffffu;
-    for (int k0 = 0; k0 < rtb; k0 += 2) {  // block-uniform
+    for (int k0 = 0; k0 < rtb; k0 += 2) {  // unit-uniform
         const int kg = rtb - k0 < 2 ? rtb - k0 : 2;
         double a[2] = {0.0, 0.0};
         for (int q = 0; q < kg; q++)
@@ -103,57 +156,30 @@ __global__ void __launch_bounds__((kMomCols + 1) * 32) k64_moments(MomLaunch M) 
         auto add_window = [&](int bf) {
             if (lane < kMomCols * kg) {
                 const int w = lane / kg, q = lane - w * kg;
-                const unsigned um = s_use[bf][w];
+                const unsigned um = S.use[bf][w];
                 for (int t = 1; t <= kMomOut; t++)
                     if ((um >> t) & 1u) {
-                        ch += s_cc[bf][w][q][t];
-                        cu += s_cj[bf][w][q][t];
+                        ch += S.cc[bf][w][q][t];
+                        cu += S.cj[bf][w][q][t];
                     }
             }
         };
         int bf = 0;
         for (int j0 = 0; j0 < np; j0 += kMomOut, bf ^= 1) {
             if (!summer) {
-                const int j = j0 - 1 + lane;  // this lane's p index
-                double p = 0.0, f3 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0, cor = 0.0;
-                bool use = false;
-                if (real) {
-                    p = P.pmin + P.dp * (double)(j + P.p_pos);
-                    if (j <= np) {
-                        if (rtb == 1) f3 = f[pidx(i, j, pit)];
-                        else rel_shared(P, f, i, j, f3, a1, a2, a3, cor);
-                    }
-                    use = lane >= 1 && lane <= kMomOut && j < np && !(P.nested && P.nested[pidx(i, j, pit)]);
-                }
+                double cc[2], cj[2];
+                bool use;
+                mom_window(P, f, real, i, j0, k0, kg, a, c1, c2, lane, cc, cj, use);
                 for (int q = 0; q < kg; q++) {
-                    double cc = 0.0, cj = 0.0;
-                    if (real) {
-                        double G = 0.0, V = 0.0;
-                        if (j <= np + 1) {
-                            double g = sqrt(1.0 + ((p * p) + a[q]) * P.g2);
-                            G = g + c1 * p;
-                        }
-                        if (j <= np) V = rtb == 1 ? f3 : rel_pick(P, k0 + q, a1, a2, a3, f3) + cor;
-                        const double Gn = __shfl_down_sync(full, G, 1);
-                        const double L = c2 * log(Gn / G);  // valid for lanes 0..30
-                        const double Lm = __shfl_up_sync(full, L, 1);
-                        const double Lp = __shfl_down_sync(full, L, 1);
-                        const double Vm = __shfl_up_sync(full, V, 1);
-                        const double Vp = __shfl_down_sync(full, V, 1);
-                        if (use) {
-                            cc = V;
-                            cj = V * L + c3 * (Lp - Lm) * (Vp - Vm);
-                        }
-                    }
-                    s_cc[bf][wid][q][lane] = cc;
-                    s_cj[bf][wid][q][lane] = cj;
+                    S.cc[bf][wid][q][lane] = cc[q];
+                    S.cj[bf][wid][q][lane] = cj[q];
                 }
                 const unsigned usemask = __ballot_sync(full, use);
-                if (lane == 0) s_use[bf][wid] = usemask;
+                if (lane == 0) S.use[bf][wid] = usemask;
             } else if (j0 > 0) {
                 add_window(bf ^ 1);  // the previous window, in ascending j
             }
-            __syncthreads();
+            mom_sync(bar);
         }
         if (summer) {
             add_window(bf ^ 1);  // the last window
@@ -167,14 +193,20 @@ __global__ void __launch_bounds__((kMomCols + 1) * 32) k64_moments(MomLaunch M) 
                 }
             }
         }
-        __syncthreads();  // the next pair's first window reuses the buffers
+        mom_sync(bar);  // the next pair's first window reuses the buffers
     }
+}
+
+__global__ void __launch_bounds__(kMomThreads) k64_moments(MomLaunch M) {
+    VX_PDL_WAIT();
+    __shared__ MomSmem S;
+    moments_unit(M, blockIdx.x * kMomCols, threadIdx.x >> 5, threadIdx.x & 31, S, 0);
 }
 
 void launch_moments64(const MomLaunch &M) {
     if (M.ncols == 0) return;
     // M.ncols is a multiple of kMomCols (the list is padded per patch)
-    vx_launch(k64_moments, M.ncols / kMomCols, (kMomCols + 1) * 32, 0, M.stream, M);
+    vx_launch(k64_moments, M.ncols / kMomCols, kMomThreads, 0, M.stream, M);
 }
 
 // ---------------------------------------------------------------- separable initial f
@@ -580,11 +612,88 @@ __device__ void pois_bwd_fast(PoisBandChunk &B, int r0, int cnt, double *x, doub
 
 constexpr int kPoisSmemMaxN = 16384;  // solution vector kept in shared memory up to this n
 
+// ---- pipelined form: the solve follows the moment units of its run (k64_moments_poisson)
+constexpr unsigned kPipeMaxPolls = 1u << 25;  // second bound of a wait (>= 64 ns per poll)
+
+__device__ __forceinline__ unsigned long long pipe_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ unsigned pipe_ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int pipe_ld_relaxed(const int *p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void pipe_bar(int bar, int nt) {
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nt) : "memory");
+}
+
+// Waits until done counter ci has every unit it expects.  A wait that runs out records
+// itself in *err and returns; so does every later wait at once (the step's values are
+// then not valid, but every index stays what the host tables say: nothing goes out of
+// bounds).
+__device__ void pipe_wait(const PipeLaunch &K, int ci) {
+    const unsigned need = (unsigned)K.need[ci] + (unsigned)K.phantom;
+    const unsigned *p = K.state + kPipeDone + ci;
+    if (pipe_ld_acquire(p) >= need) return;
+    if (pipe_ld_relaxed(K.err) != 0) return;
+    const unsigned long long t0 = pipe_ns();
+    for (unsigned poll = 0;; poll++) {
+        __nanosleep(32);
+        if (pipe_ld_acquire(p) >= need) break;
+        if ((poll & 63u) == 63u && pipe_ld_relaxed(K.err) != 0) break;
+        if (poll >= kPipeMaxPolls || pipe_ns() - t0 > K.limit_ns) {
+            atomicCAS(K.err, 0, 1 + ci);
+            break;
+        }
+    }
+    __threadfence();
+}
+
+// Rows that forward chunk c reads first: one thread waits for the chunk's moment units,
+// then threads t = 0 .. nt-1 (barrier bar) assemble rho and J at each row's x position
+// perm[k] and form its right-hand side as the unpipelined solve does
+// (tmp[i] = (te * (charge[i] + neut[i])) * w, then x[k] = tmp[perm[k]]).  off_sp0: while
+// warp 0 runs the sweep, the FP64 work stays off its sub-partition (warps 4m), whose FP64
+// unit the sweep's dependent chain needs.
+__device__ void pipe_rows(const PipeLaunch &K, int run, int c, double *x, int t, int nt, int bar, bool off_sp0) {
+    if (t == 0) {
+        if (K.trace && run == 0 && c == 0) K.trace[0] = pipe_ns();
+        pipe_wait(K, K.run_ctr[run] + c);
+        if (K.trace && run == 0) K.trace[1 + c] = pipe_ns();
+    }
+    pipe_bar(bar, nt);
+    const int *gp = K.gptr + K.run_gptr[run];
+    RunFields &F = K.P.fields[run];
+    const int *perm = K.P.lu[run].perm;
+    const double te = kEps0Inv;
+    const double w = K.P.w[run];
+    if (off_sp0) {  // warps 1..31 of the block: the 24 that are not 4m
+        const int wg = (int)threadIdx.x >> 5;
+        if ((wg & 3) == 0) return;
+        t = ((wg >> 2) * 3 + (wg & 3) - 1) * 32 + ((int)threadIdx.x & 31);
+        nt = 24 * 32;
+    }
+    for (int e = gp[c] + t; e < gp[c + 1]; e += nt) {
+        const int k = K.grow[e], i = perm[k];
+        assemble_cell<true>(K.A, run, i);
+        const double v = te * (F.charge[i] + F.neut[i]);
+        x[k] = v * w;
+    }
+}
+
 // The solve with the solution vector x in shared memory (XS) or in phi itself.  The two
 // instantiations let the compiler see x's address space: with one pointer chosen at run
 // time its loads and stores in the sweeps go through generic addressing.
-template <bool XS>
-__device__ __forceinline__ void poisson_solve(const PoissonLaunch &L, unsigned char *smem_raw, double *x) {
+template <bool XS, bool PIPE>
+__device__ __forceinline__ void poisson_solve(const PoissonLaunch &L, unsigned char *smem_raw, double *x,
+                                              const PipeLaunch *K) {
     PoisBandChunk *buf = (PoisBandChunk *)smem_raw;  // two chunk buffers, then the solution vector
     __shared__ int s_bad;
     const int run = blockIdx.x;
@@ -595,16 +704,22 @@ __device__ __forceinline__ void poisson_solve(const PoissonLaunch &L, unsigned c
     double *tmp = F.efin;  // scratch until E_x is recomputed at the end
     const double te = kEps0Inv;
     const double w = L.w[run];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double v = te * (F.charge[i] + F.neut[i]);
-        tmp[i] = v * w;
+    if (PIPE) {
+        pipe_rows(*K, run, 0, x, threadIdx.x, blockDim.x, 0, false);  // chunk 0's rows, all threads
+    } else {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            double v = te * (F.charge[i] + F.neut[i]);
+            tmp[i] = v * w;
+        }
+        __syncthreads();
+        // Row interchanges of dgetrs applied as one gather: b'[k] = b[perm[k]].
+        for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = tmp[lu.perm[k]];
     }
-    __syncthreads();
-    // Row interchanges of dgetrs applied as one gather: b'[k] = b[perm[k]].
-    for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = tmp[lu.perm[k]];
     const int nchunks = (n + kPoisRows - 1) / kPoisRows;
     unsigned long long *trace = (L.trace && run == 0 && threadIdx.x == 0) ? L.trace : nullptr;
-    if (trace) trace[0] = clock64();
+    // clock64 (cycles) alone; globaltimer (ns) when pipelined, to compare with the moment units
+    auto tick = [] { return PIPE ? pipe_ns() : (unsigned long long)clock64(); };
+    if (trace) trace[0] = tick();
     const int lane = threadIdx.x & 31;
     // ---- forward: rows ascending; chunk c stages rows [c*R, c*R + R + LA)
     {
@@ -620,9 +735,12 @@ __device__ __forceinline__ void poisson_solve(const PoissonLaunch &L, unsigned c
             bool fit_next = false;
             if (c + 1 < nchunks) {
                 const int r1 = r0 + kPoisRows;
-                if (threadIdx.x >= 32)
+                if (threadIdx.x >= 32) {
                     fit_next = pois_stage_band(buf[(c + 1) & 1], lu.L, r1, r1 + kPoisBuf, n, 32, blockDim.x - 32, false);
-                else
+                    // the rows chunk c+1 reads first, while warp 0 sweeps chunk c (it reads
+                    // and writes only rows first read by chunks up to c)
+                    if (PIPE) pipe_rows(*K, run, c + 1, x, threadIdx.x - 32, blockDim.x - 32, 1, true);
+                } else
                     fit_next = (lu.L.fptr[min(r1 + kPoisBuf, n)] - lu.L.fptr[r1]) <= kPoisFar;
             }
             if (threadIdx.x < 32) {
@@ -632,7 +750,7 @@ __device__ __forceinline__ void poisson_solve(const PoissonLaunch &L, unsigned c
             }
             fit_cur = fit_next;
             __syncthreads();
-            if (trace) trace[1 + c] = clock64();
+            if (trace) trace[1 + c] = tick();
         }
     }
     // ---- backward: rows descending; chunk c stages rows [c*R - LA, c*R + R)
@@ -693,7 +811,7 @@ __device__ __forceinline__ void poisson_solve(const PoissonLaunch &L, unsigned c
             fit_cur = fit_next;
             parity ^= 1;
             __syncthreads();
-            if (trace) trace[1 + nchunks + (clast - c)] = clock64();
+            if (trace) trace[1 + nchunks + (clast - c)] = tick();
         }
     }
     if (in_smem)
@@ -712,8 +830,203 @@ __device__ __forceinline__ void poisson_solve(const PoissonLaunch &L, unsigned c
 __global__ void __launch_bounds__(1024, 1) k_poisson(PoissonLaunch L) {
     VX_PDL_WAIT();
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    if (L.x_in_smem) poisson_solve<true>(L, smem_raw, (double *)(smem_raw + 2 * sizeof(PoisBandChunk)));
-    else poisson_solve<false>(L, smem_raw, L.fields[blockIdx.x].phi);
+    if (L.x_in_smem) poisson_solve<true, false>(L, smem_raw, (double *)(smem_raw + 2 * sizeof(PoisBandChunk)), nullptr);
+    else poisson_solve<false, false>(L, smem_raw, L.fields[blockIdx.x].phi, nullptr);
+}
+
+// ---- workers of the pipelined launch
+constexpr int kPipeRing = 16;  // units waiting for a group's summing warp
+struct PipeGroup {
+    int ticket[2];  // the column warps' current item (two slots: one is read while the next is taken)
+    int ring[kPipeRing];
+    int head, tail;  // units handed to the summing warp / summed
+};
+__device__ __forceinline__ int pipe_vld(const int *p) { return *(const volatile int *)p; }
+__device__ __forceinline__ void pipe_vst(int *p, int v) { *(volatile int *)p = v; }
+
+// One item: column warp wid forms window j0 of its column's sub-columns k0, k0+1 (those
+// the patch has) and writes the contributions of lanes 1 .. kMomOut to `out`.
+__device__ __forceinline__ void mom_item(const PipeLaunch &K, int u, int k0, int j0, int wid, int lane, double *out) {
+    const MomLaunch &M = K.M;
+    const int col0 = K.unit_col0[u];
+    const bool real = M.colpatch[col0 + wid] >= 0;  // warp-uniform
+    const P64 &P = ((const P64 *)M.patches)[M.colpatch[col0]];
+    const int rtb = P.rtb;
+    const int i = M.colidx[col0 + wid] / rtb;
+    const RunFields &F = M.fields[P.run];
+    const double2 c12 = K.unit_c12[u];
+    const int kg = rtb - k0 < 2 ? rtb - k0 : 2;
+    double a[2] = {0.0, 0.0};
+    for (int q = 0; q < kg; q++)
+        if (real) a[q] = P.qq * cell_asq(F, (i + P.x_pos) * rtb + k0 + q);
+    double cc[2], cj[2];
+    bool use;
+    mom_window(P, P.f1, real, i, j0, k0, kg, a, c12.x, c12.y, lane, cc, cj, use);
+    if (lane >= 1 && lane <= kMomOut)
+        for (int q = 0; q < kg; q++) {
+            out[lane * 30 + wid * 2 + q] = cc[q];
+            out[960 + lane * 30 + wid * 2 + q] = cj[q];
+        }
+}
+
+// The column sums of unit u (one warp, lane = sub-column as in k64_moments): every window's
+// contributions in ascending p.  A cell that is not used contributes +0.0, which leaves a
+// sum that starts at +0.0 unchanged bit for bit (such a sum never becomes -0.0), so these
+// are the sums of the used cells alone.  Then the unit counts as done for its chunk.
+__device__ void mom_sum_unit(const PipeLaunch &K, int u, int lane) {
+    const MomLaunch &M = K.M;
+    const int col0 = K.unit_col0[u];
+    const P64 &P = ((const P64 *)M.patches)[M.colpatch[col0]];
+    const int rtb = P.rtb, nw = K.unit_nwin[u];
+    for (int k0 = 0; k0 < rtb; k0 += 2) {
+        const int kg = rtb - k0 < 2 ? rtb - k0 : 2;
+        if (lane < kMomCols * kg) {
+            const int w = lane / kg, q = lane - w * kg;
+            const double *src = K.scratch + (size_t)(K.unit_item0[u] + (k0 / 2) * nw) * kPipeItemDoubles + w * 2 + q;
+            double ch = 0.0, cu = 0.0;
+            for (int win = 0; win < nw; win++, src += kPipeItemDoubles) {
+#pragma unroll
+                for (int t = 1; t <= kMomOut; t++) {
+                    ch += __ldcg(src + t * 30);
+                    cu += __ldcg(src + 960 + t * 30);
+                }
+            }
+            if (M.colpatch[col0 + w] >= 0) {
+                const int cl = M.colidx[col0 + w] + k0 + q;  // i_w * rtb + k
+                const double qc = P.q;
+                P.chargeR[cl] = ch * (P.dp * qc);
+                P.currentR[cl] = cu * (-qc * qc / P.mass);
+            }
+        }
+    }
+    __threadfence();  // the column sums, device-wide, before the count
+    __syncwarp();
+    if (lane == 0) {
+        atomicAdd(K.state + kPipeDone + K.unit_sig[u], 1u);
+        if (K.trace && K.unit_sig[u] < K.trace_nch) atomicMax(K.trace + 1 + K.trace_nch + K.unit_sig[u], pipe_ns());
+    }
+}
+
+// A group of a worker block: column warps 0 .. kMomCols-1 take items until none are left;
+// the warp that completes a unit (the unit's item count reaches its total) hands it to the
+// group's summing warp (warp kMomCols) through a ring in shared memory, or sums it itself
+// when the ring is full.  The column warps never wait for the summing warp except to hand
+// over their end mark, and the summing warp waits only for its own group: every wait ends.
+__device__ void pipe_worker(const PipeLaunch &K, PipeGroup &G, int g) {
+    const unsigned full = 0xffffffffu;
+    const int tid = (int)threadIdx.x - g * kMomThreads, wid = tid >> 5, lane = tid & 31;
+    const int bar = 1 + g, ncol = kMomCols * 32;
+    unsigned *items_done = K.state + kPipeDone + K.ndone;  // per unit
+    if (wid < kMomCols) {
+        for (int it = 0;; it++) {
+            if (tid == 0) G.ticket[it & 1] = (int)atomicAdd(K.state + kPipeTicket, 1u);
+            pipe_bar(bar, ncol);
+            const int t = G.ticket[it & 1];
+            if (t >= K.nitems) break;
+            const int u = K.item_unit[t];
+            const int loc = t - K.unit_item0[u], nw = K.unit_nwin[u];
+            const int kp = loc / nw;
+            mom_item(K, u, 2 * kp, (loc - kp * nw) * kMomOut, wid, lane, K.scratch + (size_t)t * kPipeItemDoubles);
+            __threadfence();  // this warp's contributions, device-wide, before the item counts
+            pipe_bar(bar, ncol);
+            if (wid == 0) {
+                int self = 0;
+                if (lane == 0) {
+                    const unsigned total = (unsigned)(K.unit_item0[u + 1] - K.unit_item0[u]);
+                    if (atomicAdd(items_done + u, 1u) + 1 == total) {
+                        __threadfence();  // every item's contributions before the sums read them
+                        const int h = pipe_vld(&G.head);
+                        if (h - pipe_vld(&G.tail) < kPipeRing) {
+                            pipe_vst(&G.ring[h % kPipeRing], u);
+                            __threadfence_block();
+                            pipe_vst(&G.head, h + 1);
+                        } else {
+                            self = 1;
+                        }
+                    }
+                }
+                if (__shfl_sync(full, self, 0)) mom_sum_unit(K, u, lane);
+            }
+        }
+        if (tid == 0) {  // no items left: the end mark, after the units handed over before it
+            const unsigned long long t0 = pipe_ns();
+            for (unsigned poll = 0;; poll++) {
+                const int h = pipe_vld(&G.head);
+                if (h - pipe_vld(&G.tail) < kPipeRing) {
+                    pipe_vst(&G.ring[h % kPipeRing], -1);
+                    __threadfence_block();
+                    pipe_vst(&G.head, h + 1);
+                    break;
+                }
+                if (poll >= kPipeMaxPolls || pipe_ns() - t0 > K.limit_ns) {
+                    atomicCAS(K.err, 0, 1 + K.ndone);
+                    break;
+                }
+                __nanosleep(256);
+            }
+        }
+    } else if (wid == kMomCols) {  // the summing warp
+        int tail = 0;
+        const unsigned long long t0 = pipe_ns();
+        for (unsigned poll = 0;;) {
+            int u = 0, ready = 0;
+            if (lane == 0) {
+                ready = pipe_vld(&G.head) > tail;
+                if (ready) u = pipe_vld(&G.ring[tail % kPipeRing]);
+            }
+            ready = __shfl_sync(full, ready, 0);
+            if (ready) {
+                u = __shfl_sync(full, u, 0);
+                if (u < 0) break;
+                __threadfence();
+                mom_sum_unit(K, u, lane);
+                tail++;
+                if (lane == 0) pipe_vst(&G.tail, tail);
+                continue;
+            }
+            if (++poll >= kPipeMaxPolls || pipe_ns() - t0 > K.limit_ns) {
+                if (lane == 0) atomicCAS(K.err, 0, 1 + K.ndone);
+                break;
+            }
+            __nanosleep(256);
+        }
+    }
+}
+
+// Moments, assembly and the exact solve in one launch.  Block r < nruns solves run r (its
+// forward sweep starts as soon as the moments of its first rows are summed, instead of
+// after the whole moments kernel); every other block is a worker (pipe_worker).  Only
+// the solve waits on other blocks, and only on work the workers always finish, whatever
+// order the blocks are scheduled in.  Same arithmetic as k64_moments + k_assemble +
+// k_poisson.
+__global__ void __launch_bounds__(1024, 1) k64_moments_poisson(PipeLaunch K) {
+    VX_PDL_WAIT();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    if ((int)blockIdx.x < K.P.nruns) {
+        if (K.P.x_in_smem)
+            poisson_solve<true, true>(K.P, smem_raw, (double *)(smem_raw + 2 * sizeof(PoisBandChunk)), &K);
+        else poisson_solve<false, true>(K.P, smem_raw, K.P.fields[blockIdx.x].phi, &K);
+    } else {
+        PipeGroup *G = reinterpret_cast<PipeGroup *>(smem_raw);
+        if (threadIdx.x < 2) {
+            G[threadIdx.x].head = 0;
+            G[threadIdx.x].tail = 0;
+        }
+        __syncthreads();
+        const int g = (int)threadIdx.x / kMomThreads;
+        pipe_worker(K, G[g], g);
+    }
+    // the last block out zeroes the tickets, done and item counters for the next launch
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(K.state + kPipeLeave, 1u) + 1 == gridDim.x) {
+            atomicExch(K.state + kPipeTicket, 0u);
+            for (int i = 0; i < K.ndone + K.nunits; i++) atomicExch(K.state + kPipeDone + i, 0u);
+            atomicExch(K.state + kPipeLeave, 0u);
+            __threadfence();
+        }
+    }
 }
 
 void launch_poisson(const PoissonLaunch &L) {
@@ -730,6 +1043,31 @@ void launch_poisson(const PoissonLaunch &L) {
     // face kernels that run beside the solve shares the SM, whose FP64 unit would
     // otherwise delay the solve's dependent chain (step 32.4 -> 28.1 ms on 4096 x 512)
     vx_launch(k_poisson, L.nruns, 1024, smem, L.stream, P);
+}
+
+void launch_moments_poisson64(const PipeLaunch &K0) {
+    PipeLaunch K = K0;
+    int max_smem = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const int base = 2 * (int)sizeof(PoisBandChunk);
+    K.P.x_in_smem = (K.P.maxn <= kPoisSmemMaxN && base + 8 * K.P.maxn <= max_smem) ? 1 : 0;
+    const int smem_solve = base + (K.P.x_in_smem ? 8 * K.P.maxn : 0);
+    const int smem = std::max(smem_solve, 2 * (int)sizeof(PipeGroup));
+    cudaFuncSetAttribute(k64_moments_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(K.P.nruns + K.workers);
+    cfg.blockDim = dim3(1024);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = K.stream;
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = K.priority;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = g_launch_pdl ? 2 : 1;
+    cudaLaunchKernelEx(&cfg, k64_moments_poisson, K);  // errors surface through cudaGetLastError
 }
 
 // E_x on the finest grid from phi and Ex0 (EMSolver::GetEfield), for states loaded from

@@ -246,6 +246,30 @@ PoissonLU::Band PoissonLU::upper_band() const {
     return B;
 }
 
+std::vector<int> PoissonLU::first_read_chunk(const Band &Lb, int rows_per_chunk) const {
+    std::vector<int> fc;
+    if (Lb.nslots < 0 || n < 5 || rows_per_chunk <= 0) return fc;  // the device sweep's other form
+    const int R = rows_per_chunk;
+    fc.assign(n, -1);
+    auto mark = [&](int k, int c) {
+        if (k >= 0 && k < n && (fc[k] < 0 || c < fc[k])) fc[k] = c;
+    };
+    const int nch = (n + R - 1) / R;
+    for (int c = 0; c < nch; c++) {
+        const int r0 = c * R, cnt = std::min(R, n - r0);
+        if (c == 0)
+            for (int k = 0; k < 4; k++) mark(k, 0);  // the four band lanes' first rows
+        // the band's last lane: x[i + 4] at the chunk's start, x[i + 5] one row ahead
+        for (int k = r0 + 4; k <= r0 + cnt + 4; k++) mark(k, c);
+        // the accumulator lanes: the row taken up at step i, read one step ahead
+        for (int s = 0; s < Lb.nslots; s++)
+            for (int i = r0; i <= r0 + cnt && i < n; i++) mark(Lb.slot_load[(size_t)s * n + i], c);
+    }
+    for (int k = 0; k < n; k++)
+        if (fc[k] < 0) return {};
+    return fc;
+}
+
 void PoissonLU::solve(double *b) const {
     for (int k = 0; k < n; k++)
         if (ipiv[k] != k) std::swap(b[k], b[ipiv[k]]);

@@ -49,6 +49,11 @@ struct PoissonLU {
     };
     Band lower_band() const;
     Band upper_band() const;
+    // For each row k, the first chunk of rows_per_chunk steps of the device's forward sweep
+    // (fields64.cu, pois_fwd_fast) that reads x[k]: the band lanes read rows 0..3 before
+    // the first step and row i+5 at step i, the accumulator lanes the row they take up one
+    // step ahead.  Empty when the sweep runs in its other form (nslots < 0).
+    std::vector<int> first_read_chunk(const Band &Lb, int rows_per_chunk) const;
 };
 
 }  // namespace vx

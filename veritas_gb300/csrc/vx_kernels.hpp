@@ -97,6 +97,7 @@ struct MomLaunch {
     cudaStream_t stream;
 };
 constexpr int kMomCols = 15;  // FP64 moment columns per block (padded per patch), plus a summing warp
+constexpr int kMomWindow = 29;  // p cells per window of the FP64 moments (a warp's lanes 1..29)
 void launch_moments64(const MomLaunch &M);
 void launch_moments32(const MomLaunch &M);
 
@@ -152,6 +153,55 @@ struct PoissonLaunch {
 };
 void launch_poisson(const PoissonLaunch &L);
 constexpr int kPoisRowsHost = 256;  // rows per chunk of k_poisson (fields64.cu kPoisRows)
+
+// Moments, assembly and exact Poisson solve of an FP64 set in one launch
+// (k64_moments_poisson): blocks 0 .. nruns-1 solve, each following its run's moments as
+// they are completed; every other block is a persistent worker of two groups.  A group's
+// 15 column warps take items — one p window of one moment unit's 15 columns (one pair of
+// sub-columns) — by ticket in the order the forward sweeps first need the units' columns,
+// and write each cell's charge and current contributions to `scratch`; the group that
+// completes a unit's last item hands the unit to its summing warp, which adds the
+// contributions in ascending p (the reference's order) and adds one to the done counter of
+// the chunk that needs the unit first.  The solve waits (bounded) for a chunk's counter
+// before it assembles rho and J at the x positions whose right-hand sides the chunk reads
+// first.
+constexpr int kPipeErr = 0, kPipeTicket = 32, kPipeLeave = 64, kPipeDone = 96;  // words of the state
+constexpr int kPipeMaxRuns = 4;  // sets of more runs keep separate launches (each solve holds an SM)
+constexpr int kPipeItemDoubles = 2 * 32 * 30;  // per item: [cc, cj][lane t][column w][sub-column q]
+constexpr size_t kPipeMaxScratch = (size_t)2 << 30;  // larger sets keep separate launches
+struct PipeLaunch {
+    MomLaunch M;             // moment columns (padded per patch into units of kMomCols)
+    AsmLaunch A;             // assembly tables
+    PoissonLaunch P;         // solve (x_in_smem set by the launcher)
+    const int *unit_col0;    // per unit: its first column in M's column list
+    const int *unit_sig;     // per unit: done counter it adds to
+    const int *unit_item0;   // per unit: its first item (a unit's items are consecutive tickets)
+    const int *unit_nwin;    // per unit: p windows per sub-column pair
+    const double2 *unit_c12; // per unit: (1 / m) / c and its reciprocal, as the moments form them
+    int nunits;
+    const int *item_unit;    // per item: its unit
+    int nitems;
+    double *scratch;         // kPipeItemDoubles per item
+    const int *need;         // per done counter: units that add to it
+    int ndone;               // done counters; the units' item counters follow them
+    const int *run_ctr;      // per run: its chunk-0 done counter
+    const int *run_gptr;     // per run: offset of its (nchunks + 1) row pointers in gptr
+    const int *gptr;         // rows first read by each forward chunk: grow[gptr[c] .. gptr[c+1])
+    const int *grow;
+    unsigned *state;         // kPipe* words, done and item counters from kPipeDone (the last block out zeroes them)
+    int *err;                // 0, or 1 + the done counter whose wait ran out (or 1 + ndone: a worker's wait)
+    unsigned long long limit_ns;
+    int phantom;             // units each wait expects beyond the real ones (> 0: every wait runs out)
+    int priority;            // launch priority (the moments go ahead of the face kernels beside them)
+    int workers;             // worker blocks
+    // Optional globaltimer trace (ns) of run 0: [0] the solve's start, [1 + c] chunk c's rows
+    // ready, [1 + trace_nch + k] the last unit of done counter k summed; the solve's own
+    // chunk ends go to P.trace.
+    unsigned long long *trace;
+    int trace_nch;
+    cudaStream_t stream;
+};
+void launch_moments_poisson64(const PipeLaunch &K);
 
 // O(n) Poisson solve by prefix scans, one thread-block cluster per run (poisson_scan.cu).
 // Y holds the m x 3 Woodbury columns (row-major), K the 3x3 capacitance factor.
