@@ -705,19 +705,21 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
         // and when each chunk's last moment unit finished (ns from the solve's start)
         if (std::getenv("VX_TRACE_PIPE")) {
             const int nch = (L.runs[0]->n + kPoisRowsHost - 1) / kPoisRowsHost;
-            DevBuf tr((size_t)(1 + 2 * nch) * sizeof(unsigned long long));
+            DevBuf tr((size_t)(3 + 2 * nch) * sizeof(unsigned long long));
             DevBuf tp((size_t)(2 * nch + 2) * sizeof(unsigned long long));
             P.trace = tr.as<unsigned long long>();
             P.trace_nch = nch;
             P.P.trace = tp.as<unsigned long long>();
             launch_moments_poisson64(P);
             sync();
-            std::vector<unsigned long long> a(1 + 2 * nch), b(2 * nch + 1);
+            std::vector<unsigned long long> a(3 + 2 * nch), b(2 * nch + 1);
             VX_CUDA(cudaMemcpy(a.data(), tr.p, a.size() * sizeof(a[0]), cudaMemcpyDeviceToHost));
             VX_CUDA(cudaMemcpy(b.data(), tp.p, b.size() * sizeof(b[0]), cudaMemcpyDeviceToHost));
             const double t0 = (double)a[0];
             std::fprintf(stderr, "vx pipe n=%d chunks=%d units=%d (us from the solve's start)\n", L.runs[0]->n, nch,
                          L.pipe_nunits);
+            std::fprintf(stderr, "  forward sweep: %llu cycles in %.1f us\n", a[2 + 2 * nch] - a[1 + 2 * nch],
+                         (b[nch] - b[0]) * 1e-3);
             for (int c = 0; c < nch; c++)
                 std::fprintf(stderr, "  chunk %2d: units done %8.1f rows ready %8.1f forward end %8.1f backward end %8.1f\n",
                              c, a[1 + nch + c] ? (a[1 + nch + c] - t0) * 1e-3 : -1.0, (a[1 + c] - t0) * 1e-3,
@@ -1103,7 +1105,12 @@ void Engine::build_pipe_tables(LaunchSet &L, const std::vector<int> &colpatch, c
     L.dpipe_gptr = upload(gptr, stream);
     L.dpipe_grow = upload(grow, stream);
     L.dpipe_scratch = DevBuf((size_t)nitems * kPipeItemDoubles * sizeof(double));
-    L.dpipe_state = DevBuf((size_t)(kPipeDone + L.pipe_ndone + nunits) * sizeof(unsigned));  // zeroed
+    L.dpipe_state = DevBuf((size_t)(kPipeDone + L.pipe_ndone + 2 * nunits) * sizeof(unsigned));  // zeroed
+    // summing warps, four per block: each unit's sums take about 64 cycles per FP64 add on
+    // their sub-partition; enough blocks that they keep up with the column warps
+    long long adds = 0;
+    for (int t = 0; t < nunits; t++) adds += (long long)(item0[t + 1] - item0[t]) * 2 * kMomWindow;
+    L.pipe_summers = (int)std::min<long long>(8, std::max<long long>(1, (adds * 64 / 4 + 1200000 - 1) / 1200000));
     if (!pipe_err_.p) pipe_err_ = DevBuf(sizeof(int));
     L.pipe = true;
 }
@@ -1298,7 +1305,8 @@ PipeLaunch Engine::pipe_launch(LaunchSet &L, const StageLaunches &K) {
     P.item_unit = L.dpipe_items.as<int>();
     P.nitems = L.pipe_nitems;
     P.scratch = L.dpipe_scratch.as<double>();
-    P.workers = std::max(1, std::min(num_sms_ - (int)L.runs.size(), (L.pipe_nitems + 1) / 2));
+    P.summers = L.pipe_summers;
+    P.workers = std::max(1, std::min(num_sms_ - (int)L.runs.size() - P.summers, (L.pipe_nitems + 1) / 2));
     P.need = L.dpipe_need.as<int>();
     P.ndone = L.pipe_ndone;
     P.run_ctr = L.dpipe_runctr.as<int>();

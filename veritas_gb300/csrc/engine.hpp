@@ -221,7 +221,7 @@ struct LaunchSet {
     // FP64 exact-solve sets of up to kPipeMaxRuns runs: tables of the pipelined moments +
     // solve launch (k64_moments_poisson)
     bool pipe = false;
-    int pipe_nunits = 0, pipe_nitems = 0, pipe_ndone = 0;
+    int pipe_nunits = 0, pipe_nitems = 0, pipe_ndone = 0, pipe_summers = 1;
     DevBuf dpipe_col0, dpipe_sig, dpipe_item0, dpipe_nwin, dpipe_c12, dpipe_items, dpipe_need, dpipe_runctr,
         dpipe_rungptr, dpipe_gptr, dpipe_grow, dpipe_scratch, dpipe_state;
     cudaGraphExec_t graph = nullptr;

@@ -720,6 +720,7 @@ __device__ __forceinline__ void poisson_solve(const PoissonLaunch &L, unsigned c
     // clock64 (cycles) alone; globaltimer (ns) when pipelined, to compare with the moment units
     auto tick = [] { return PIPE ? pipe_ns() : (unsigned long long)clock64(); };
     if (trace) trace[0] = tick();
+    if (PIPE && K->trace && run == 0 && threadIdx.x == 0) K->trace[1 + 2 * K->trace_nch] = clock64();
     const int lane = threadIdx.x & 31;
     // ---- forward: rows ascending; chunk c stages rows [c*R, c*R + R + LA)
     {
@@ -753,6 +754,7 @@ __device__ __forceinline__ void poisson_solve(const PoissonLaunch &L, unsigned c
             if (trace) trace[1 + c] = tick();
         }
     }
+    if (PIPE && K->trace && run == 0 && threadIdx.x == 0) K->trace[2 + 2 * K->trace_nch] = clock64();
     // ---- backward: rows descending; chunk c stages rows [c*R - LA, c*R + R)
     {
         double V = 0.0, w1 = 0.0;
@@ -835,15 +837,6 @@ __global__ void __launch_bounds__(1024, 1) k_poisson(PoissonLaunch L) {
 }
 
 // ---- workers of the pipelined launch
-constexpr int kPipeRing = 16;  // units waiting for a group's summing warp
-struct PipeGroup {
-    int ticket[2];  // the column warps' current item (two slots: one is read while the next is taken)
-    int ring[kPipeRing];
-    int head, tail;  // units handed to the summing warp / summed
-};
-__device__ __forceinline__ int pipe_vld(const int *p) { return *(const volatile int *)p; }
-__device__ __forceinline__ void pipe_vst(int *p, int v) { *(volatile int *)p = v; }
-
 // One item: column warp wid forms window j0 of its column's sub-columns k0, k0+1 (those
 // the patch has) and writes the contributions of lanes 1 .. kMomOut to `out`.
 __device__ __forceinline__ void mom_item(const PipeLaunch &K, int u, int k0, int j0, int wid, int lane, double *out) {
@@ -908,97 +901,78 @@ __device__ void mom_sum_unit(const PipeLaunch &K, int u, int lane) {
 }
 
 // A group of a worker block: column warps 0 .. kMomCols-1 take items until none are left;
-// the warp that completes a unit (the unit's item count reaches its total) hands it to the
-// group's summing warp (warp kMomCols) through a ring in shared memory, or sums it itself
-// when the ring is full.  The column warps never wait for the summing warp except to hand
-// over their end mark, and the summing warp waits only for its own group: every wait ends.
-__device__ void pipe_worker(const PipeLaunch &K, PipeGroup &G, int g) {
-    const unsigned full = 0xffffffffu;
+// the warp that completes a unit (the unit's item count reaches its total) appends the
+// unit to the queue of completed units.  They never wait for anything but each other.
+__device__ void pipe_columns(const PipeLaunch &K, int *ticket, int g) {
     const int tid = (int)threadIdx.x - g * kMomThreads, wid = tid >> 5, lane = tid & 31;
     const int bar = 1 + g, ncol = kMomCols * 32;
-    unsigned *items_done = K.state + kPipeDone + K.ndone;  // per unit
-    if (wid < kMomCols) {
-        for (int it = 0;; it++) {
-            if (tid == 0) G.ticket[it & 1] = (int)atomicAdd(K.state + kPipeTicket, 1u);
-            pipe_bar(bar, ncol);
-            const int t = G.ticket[it & 1];
-            if (t >= K.nitems) break;
-            const int u = K.item_unit[t];
-            const int loc = t - K.unit_item0[u], nw = K.unit_nwin[u];
-            const int kp = loc / nw;
-            mom_item(K, u, 2 * kp, (loc - kp * nw) * kMomOut, wid, lane, K.scratch + (size_t)t * kPipeItemDoubles);
-            __threadfence();  // this warp's contributions, device-wide, before the item counts
-            pipe_bar(bar, ncol);
-            if (wid == 0) {
-                int self = 0;
-                if (lane == 0) {
-                    const unsigned total = (unsigned)(K.unit_item0[u + 1] - K.unit_item0[u]);
-                    if (atomicAdd(items_done + u, 1u) + 1 == total) {
-                        __threadfence();  // every item's contributions before the sums read them
-                        const int h = pipe_vld(&G.head);
-                        if (h - pipe_vld(&G.tail) < kPipeRing) {
-                            pipe_vst(&G.ring[h % kPipeRing], u);
-                            __threadfence_block();
-                            pipe_vst(&G.head, h + 1);
-                        } else {
-                            self = 1;
-                        }
+    unsigned *items_done = K.state + kPipeDone + K.ndone;      // per unit
+    unsigned *queue = items_done + K.nunits;                    // completed units (u + 1), in order
+    for (int it = 0;; it++) {
+        if (tid == 0) ticket[it & 1] = (int)atomicAdd(K.state + kPipeTicket, 1u);
+        pipe_bar(bar, ncol);
+        const int t = ticket[it & 1];
+        if (t >= K.nitems) break;
+        const int u = K.item_unit[t];
+        const int loc = t - K.unit_item0[u], nw = K.unit_nwin[u];
+        const int kp = loc / nw;
+        mom_item(K, u, 2 * kp, (loc - kp * nw) * kMomOut, wid, lane, K.scratch + (size_t)t * kPipeItemDoubles);
+        __threadfence();  // this warp's contributions, device-wide, before the item counts
+        pipe_bar(bar, ncol);
+        if (tid == 0) {
+            const unsigned total = (unsigned)(K.unit_item0[u + 1] - K.unit_item0[u]);
+            if (atomicAdd(items_done + u, 1u) + 1 == total) {
+                __threadfence();  // every item's contributions before a summing warp reads them
+                const unsigned slot = atomicAdd(K.state + kPipeQHead, 1u);
+                atomicExch(queue + slot, (unsigned)u + 1);
+            }
+        }
+    }
+}
+
+// A summing warp (one per sub-partition of a summing block, so that its serial adds have
+// the sub-partition's FP64 unit to themselves): takes completed units from the queue in
+// order and forms their column sums.  It waits only for units, which the column warps
+// always complete; a wait that runs out records itself and ends the warp.
+__device__ void pipe_summer(const PipeLaunch &K, int lane) {
+    const unsigned full = 0xffffffffu;
+    unsigned *queue = K.state + kPipeDone + K.ndone + K.nunits;
+    for (;;) {
+        int slot = 0;
+        if (lane == 0) slot = (int)atomicAdd(K.state + kPipeQTail, 1u);
+        slot = __shfl_sync(full, slot, 0);
+        if (slot >= K.nunits) break;
+        unsigned v = 0;
+        if (lane == 0) {
+            v = pipe_ld_acquire(queue + slot);
+            if (!v) {
+                const unsigned long long t0 = pipe_ns();
+                for (unsigned poll = 0;; poll++) {
+                    __nanosleep(64);
+                    v = pipe_ld_acquire(queue + slot);
+                    if (v) break;
+                    if ((poll & 63u) == 63u && pipe_ld_relaxed(K.err) != 0) break;
+                    if (poll >= kPipeMaxPolls || pipe_ns() - t0 > K.limit_ns) {
+                        atomicCAS(K.err, 0, 1 + K.ndone);
+                        break;
                     }
                 }
-                if (__shfl_sync(full, self, 0)) mom_sum_unit(K, u, lane);
             }
         }
-        if (tid == 0) {  // no items left: the end mark, after the units handed over before it
-            const unsigned long long t0 = pipe_ns();
-            for (unsigned poll = 0;; poll++) {
-                const int h = pipe_vld(&G.head);
-                if (h - pipe_vld(&G.tail) < kPipeRing) {
-                    pipe_vst(&G.ring[h % kPipeRing], -1);
-                    __threadfence_block();
-                    pipe_vst(&G.head, h + 1);
-                    break;
-                }
-                if (poll >= kPipeMaxPolls || pipe_ns() - t0 > K.limit_ns) {
-                    atomicCAS(K.err, 0, 1 + K.ndone);
-                    break;
-                }
-                __nanosleep(256);
-            }
-        }
-    } else if (wid == kMomCols) {  // the summing warp
-        int tail = 0;
-        const unsigned long long t0 = pipe_ns();
-        for (unsigned poll = 0;;) {
-            int u = 0, ready = 0;
-            if (lane == 0) {
-                ready = pipe_vld(&G.head) > tail;
-                if (ready) u = pipe_vld(&G.ring[tail % kPipeRing]);
-            }
-            ready = __shfl_sync(full, ready, 0);
-            if (ready) {
-                u = __shfl_sync(full, u, 0);
-                if (u < 0) break;
-                __threadfence();
-                mom_sum_unit(K, u, lane);
-                tail++;
-                if (lane == 0) pipe_vst(&G.tail, tail);
-                continue;
-            }
-            if (++poll >= kPipeMaxPolls || pipe_ns() - t0 > K.limit_ns) {
-                if (lane == 0) atomicCAS(K.err, 0, 1 + K.ndone);
-                break;
-            }
-            __nanosleep(256);
-        }
+        v = __shfl_sync(full, v, 0);
+        if (!v) break;
+        __threadfence();
+        mom_sum_unit(K, (int)v - 1, lane);
     }
 }
 
 // Moments, assembly and the exact solve in one launch.  Block r < nruns solves run r (its
 // forward sweep starts as soon as the moments of its first rows are summed, instead of
-// after the whole moments kernel); every other block is a worker (pipe_worker).  Only
-// the solve waits on other blocks, and only on work the workers always finish, whatever
-// order the blocks are scheduled in.  Same arithmetic as k64_moments + k_assemble +
-// k_poisson.
+// after the whole moments kernel); the next K.summers blocks carry four summing warps each
+// (pipe_summer); every other block carries two groups of column warps (pipe_columns).
+// Column warps wait for nothing outside their group, summing warps only for column
+// warps, the solve only for summing warps: every wait ends whatever order the blocks are
+// scheduled in.  Same arithmetic as k64_moments + k_assemble + k_poisson.
 __global__ void __launch_bounds__(1024, 1) k64_moments_poisson(PipeLaunch K) {
     VX_PDL_WAIT();
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1006,23 +980,22 @@ __global__ void __launch_bounds__(1024, 1) k64_moments_poisson(PipeLaunch K) {
         if (K.P.x_in_smem)
             poisson_solve<true, true>(K.P, smem_raw, (double *)(smem_raw + 2 * sizeof(PoisBandChunk)), &K);
         else poisson_solve<false, true>(K.P, smem_raw, K.P.fields[blockIdx.x].phi, &K);
+    } else if ((int)blockIdx.x < K.P.nruns + K.summers) {
+        if (threadIdx.x < 4 * 32) pipe_summer(K, (int)threadIdx.x & 31);  // warps 0..3: one per sub-partition
     } else {
-        PipeGroup *G = reinterpret_cast<PipeGroup *>(smem_raw);
-        if (threadIdx.x < 2) {
-            G[threadIdx.x].head = 0;
-            G[threadIdx.x].tail = 0;
-        }
-        __syncthreads();
+        int *ticket = reinterpret_cast<int *>(smem_raw);
         const int g = (int)threadIdx.x / kMomThreads;
-        pipe_worker(K, G[g], g);
+        if (((int)threadIdx.x & (kMomThreads - 1)) < kMomCols * 32) pipe_columns(K, ticket + 2 * g, g);
     }
-    // the last block out zeroes the tickets, done and item counters for the next launch
+    // the last block out zeroes the tickets, the queue, done and item counters for the next launch
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
         if (atomicAdd(K.state + kPipeLeave, 1u) + 1 == gridDim.x) {
             atomicExch(K.state + kPipeTicket, 0u);
-            for (int i = 0; i < K.ndone + K.nunits; i++) atomicExch(K.state + kPipeDone + i, 0u);
+            atomicExch(K.state + kPipeQHead, 0u);
+            atomicExch(K.state + kPipeQTail, 0u);
+            for (int i = 0; i < K.ndone + 2 * K.nunits; i++) atomicExch(K.state + kPipeDone + i, 0u);
             atomicExch(K.state + kPipeLeave, 0u);
             __threadfence();
         }
@@ -1053,10 +1026,10 @@ void launch_moments_poisson64(const PipeLaunch &K0) {
     const int base = 2 * (int)sizeof(PoisBandChunk);
     K.P.x_in_smem = (K.P.maxn <= kPoisSmemMaxN && base + 8 * K.P.maxn <= max_smem) ? 1 : 0;
     const int smem_solve = base + (K.P.x_in_smem ? 8 * K.P.maxn : 0);
-    const int smem = std::max(smem_solve, 2 * (int)sizeof(PipeGroup));
+    const int smem = std::max(smem_solve, 16);
     cudaFuncSetAttribute(k64_moments_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(K.P.nruns + K.workers);
+    cfg.gridDim = dim3(K.P.nruns + K.summers + K.workers);
     cfg.blockDim = dim3(1024);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = K.stream;

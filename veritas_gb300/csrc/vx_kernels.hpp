@@ -156,16 +156,17 @@ constexpr int kPoisRowsHost = 256;  // rows per chunk of k_poisson (fields64.cu 
 
 // Moments, assembly and exact Poisson solve of an FP64 set in one launch
 // (k64_moments_poisson): blocks 0 .. nruns-1 solve, each following its run's moments as
-// they are completed; every other block is a persistent worker of two groups.  A group's
-// 15 column warps take items — one p window of one moment unit's 15 columns (one pair of
-// sub-columns) — by ticket in the order the forward sweeps first need the units' columns,
-// and write each cell's charge and current contributions to `scratch`; the group that
-// completes a unit's last item hands the unit to its summing warp, which adds the
-// contributions in ascending p (the reference's order) and adds one to the done counter of
-// the chunk that needs the unit first.  The solve waits (bounded) for a chunk's counter
-// before it assembles rho and J at the x positions whose right-hand sides the chunk reads
-// first.
-constexpr int kPipeErr = 0, kPipeTicket = 32, kPipeLeave = 64, kPipeDone = 96;  // words of the state
+// they are completed; the other blocks are persistent workers.  Column warps (two groups
+// of 15 per worker block) take items — one p window of one moment unit's 15 columns (one
+// pair of sub-columns) — by ticket in the order the forward sweeps first need the units'
+// columns, and write each cell's charge and current contributions to `scratch`; the warp
+// that completes a unit's last item queues the unit.  Summing warps (four per summing
+// block, one per sub-partition) take queued units in order, add their contributions in
+// ascending p (the reference's order) and add one to the done counter of the chunk that
+// needs the unit first.  The solve waits (bounded) for a chunk's counter before it
+// assembles rho and J at the x positions whose right-hand sides the chunk reads first.
+constexpr int kPipeErr = 0, kPipeTicket = 32, kPipeLeave = 64, kPipeQHead = 96, kPipeQTail = 128,
+              kPipeDone = 160;  // words of the state (each on its own 128-byte line)
 constexpr int kPipeMaxRuns = 4;  // sets of more runs keep separate launches (each solve holds an SM)
 constexpr int kPipeItemDoubles = 2 * 32 * 30;  // per item: [cc, cj][lane t][column w][sub-column q]
 constexpr size_t kPipeMaxScratch = (size_t)2 << 30;  // larger sets keep separate launches
@@ -188,12 +189,13 @@ struct PipeLaunch {
     const int *run_gptr;     // per run: offset of its (nchunks + 1) row pointers in gptr
     const int *gptr;         // rows first read by each forward chunk: grow[gptr[c] .. gptr[c+1])
     const int *grow;
-    unsigned *state;         // kPipe* words, done and item counters from kPipeDone (the last block out zeroes them)
-    int *err;                // 0, or 1 + the done counter whose wait ran out (or 1 + ndone: a worker's wait)
+    unsigned *state;         // kPipe* words; from kPipeDone: done counters, item counters, queue (zeroed by the last block out)
+    int *err;                // 0, or 1 + the done counter whose wait ran out (or 1 + ndone: a summing warp's wait)
     unsigned long long limit_ns;
     int phantom;             // units each wait expects beyond the real ones (> 0: every wait runs out)
     int priority;            // launch priority (the moments go ahead of the face kernels beside them)
-    int workers;             // worker blocks
+    int summers;             // summing blocks
+    int workers;             // column-warp blocks
     // Optional globaltimer trace (ns) of run 0: [0] the solve's start, [1 + c] chunk c's rows
     // ready, [1 + trace_nch + k] the last unit of done counter k summed; the solve's own
     // chunk ends go to P.trace.
