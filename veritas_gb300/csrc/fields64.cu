@@ -730,18 +730,39 @@ __device__ __forceinline__ void poisson_solve(const PoissonLaunch &L, unsigned c
         if (threadIdx.x < 32 && lane < 4 && lane < n)
             V = fit_cur ? pois_far<true>(buf[0], lu.L, x, lane) : pois_far<false>(buf[0], lu.L, x, lane);
 
-        for (int c = 0; c < nchunks; c++) {
+        if (PIPE) {
+            // warp 0 sweeps, the others stage the next chunk and gather its rows: two
+            // loops with one block barrier per chunk each, so that the sweep's loop holds
+            // only the sweep's values (the accumulator-lane form: the host pipelines only
+            // factors that have it)
+            if (threadIdx.x < 32) {
+                for (int c = 0; c < nchunks; c++) {
+                    const int r0 = c * kPoisRows;
+                    pois_fwd_fast(buf[c & 1], lu.L, r0, min(kPoisRows, n - r0), n, x, V, w1);
+                    __syncthreads();
+                    if (trace) trace[1 + c] = tick();
+                }
+            } else {
+                for (int c = 0; c + 1 < nchunks; c++) {
+                    const int r1 = (c + 1) * kPoisRows;
+                    pois_stage_band(buf[(c + 1) & 1], lu.L, r1, r1 + kPoisBuf, n, 32, blockDim.x - 32, false);
+                    // the rows chunk c+1 reads first, while warp 0 sweeps chunk c (it reads
+                    // and writes only rows first read by chunks up to c)
+                    pipe_rows(*K, run, c + 1, x, threadIdx.x - 32, blockDim.x - 32, 1, true);
+                    __syncthreads();
+                }
+                __syncthreads();  // the last chunk's
+            }
+        }
+        for (int c = 0; !PIPE && c < nchunks; c++) {
             const int r0 = c * kPoisRows, cnt = min(kPoisRows, n - r0);
             PoisBandChunk &B = buf[c & 1];
             bool fit_next = false;
             if (c + 1 < nchunks) {
                 const int r1 = r0 + kPoisRows;
-                if (threadIdx.x >= 32) {
+                if (threadIdx.x >= 32)
                     fit_next = pois_stage_band(buf[(c + 1) & 1], lu.L, r1, r1 + kPoisBuf, n, 32, blockDim.x - 32, false);
-                    // the rows chunk c+1 reads first, while warp 0 sweeps chunk c (it reads
-                    // and writes only rows first read by chunks up to c)
-                    if (PIPE) pipe_rows(*K, run, c + 1, x, threadIdx.x - 32, blockDim.x - 32, 1, true);
-                } else
+                else
                     fit_next = (lu.L.fptr[min(r1 + kPoisBuf, n)] - lu.L.fptr[r1]) <= kPoisFar;
             }
             if (threadIdx.x < 32) {
