@@ -338,14 +338,16 @@ __device__ __forceinline__ void xflux32(const P32 *patches, const TileRef t, int
         fb = f[id - pit];
         fc = f[id];
     }
+    // q^2 A^2 / (m c)^2 of row i0 + k, formed once by lane k and taken by shuffle
+    const float a_l = asq32(P, F, t.i0 + lane);
     for (int r = 0; r < kStripRows; r++) {
         const int i = t.i0 + r;
         if (i > P.nx) break;  // warp-uniform
         const int id = pidx(i, jj, pit);
         float am = 0.0f, fv = 0.0f, fd = 0.0f;
+        const float a = __shfl_sync(full, a_l, r);
         if (col_ok) {
             fd = f[id + pit];  // row i+1 <= nx+1
-            const float a = asq32(P, F, i);
             const float g0 = sqrt_ge1(1.0f + p0 * p0 + a), g1 = sqrt_ge1(1.0f + p1 * p1 + a);
             am = P.kxf * __fdividef(P.dpnf * (p1 + p0), g1 + g0);
             fv = weno32(fa, fb, fc, fd, am > 0.0f, P.weno_eps);
@@ -368,39 +370,49 @@ __device__ __forceinline__ void xflux32(const P32 *patches, const TileRef t, int
 struct PRow {
     float a, g;  // q^2 A^2 / (m c)^2 and gamma at the row's lower x-face
 };
-__device__ __forceinline__ PRow prow32(const FluxView &V, int i, float p) {
-    const float a = V.asq_at(i);
-    return {a, sqrt_ge1(1.0f + p * p + a)};
-}
 __device__ __forceinline__ void pface32(const FluxView &V, int i, int j, bool col_ok, const PRow &lo,
-                                        const PRow &hi, float &am, float &fv) {
+                                        const PRow &hi, float qe, float &am, float &fv) {
     am = 0.0f;
     fv = 0.0f;
     if (!col_ok || i < -1 || i > V.nx) return;
-    am = V.qe_at(i) - V.kpf * __fdividef(hi.a - lo.a, hi.g + lo.g);
+    am = qe - V.kpf * __fdividef(hi.a - lo.a, hi.g + lo.g);
     const int id = pidx(i, j, V.pit);
     const float *f = V.f;
     fv = weno32(f[id - 2], f[id - 1], f[id], f[id + 1], am > 0.0f, V.weno_eps);
 }
 
+// The row quantities — q^2 A^2 / (m c)^2 at x-faces i0-1 .. i0+rows+1 and q<E_x> of rows
+// i0-1 .. i0+rows — are the same for every lane: lane k forms those of row i0-1+k once
+// (k <= kStripRows + 2 < 32) and each row takes them by shuffle, instead of every lane
+// forming every row's (their index clamping and the periodic E_x average were most of the
+// kernel's integer instructions).
 __device__ __forceinline__ void pflux32(const P32 *patches, const TileRef t, int lane, const RunFields *fields,
                                        int step, int use_f0) {
+    const unsigned full = 0xffffffffu;
     const P32 &P = patches[t.patch];
     const FluxView V(P, fields[P.run], step, use_f0);
     const int j = t.j0 + lane;
     const bool col_ok = j >= 0 && j <= V.np;
     const float p = V.mom(j + P.p_pos);
     const float w3 = 1.0f / 48.0f;
-    PRow r0 = prow32(V, t.i0 - 1, p), r1 = prow32(V, t.i0, p), r2 = prow32(V, t.i0 + 1, p);
+    const int ir = t.i0 - 1 + lane;
+    const float a_l = V.asq_at(ir);
+    const float qe_l = (ir >= -1 && ir <= V.nx) ? V.qe_at(ir) : 0.0f;
+    auto prow = [&](int i) {  // i - (i0 - 1) in 0 .. kStripRows + 2
+        const float a = __shfl_sync(full, a_l, i - (t.i0 - 1));
+        return PRow{a, sqrt_ge1(1.0f + p * p + a)};
+    };
+    auto qe = [&](int i) { return __shfl_sync(full, qe_l, i - (t.i0 - 1)); };
+    PRow r0 = prow(t.i0 - 1), r1 = prow(t.i0), r2 = prow(t.i0 + 1);
     float amA, fvA, amB, fvB;  // rows i-1 and i
-    pface32(V, t.i0 - 1, j, col_ok, r0, r1, amA, fvA);
-    pface32(V, t.i0, j, col_ok, r1, r2, amB, fvB);
+    pface32(V, t.i0 - 1, j, col_ok, r0, r1, qe(t.i0 - 1), amA, fvA);
+    pface32(V, t.i0, j, col_ok, r1, r2, qe(t.i0), amB, fvB);
     const int rows = min(kStripRows, V.nx + 1 - t.i0);
     for (int r = 0; r < rows; r++) {
         const int i = t.i0 + r;
-        const PRow r3 = prow32(V, i + 2, p);
+        const PRow r3 = prow(i + 2);
         float amC, fvC;  // row i+1
-        pface32(V, i + 1, j, col_ok, r2, r3, amC, fvC);
+        pface32(V, i + 1, j, col_ok, r2, r3, qe(i + 1), amC, fvC);
         const int id = pidx(i, j, V.pit);
         if (col_ok && !(V.ifp && V.ifp[id])) {
             V.FH[id] = V.dpif * (fvB * amB + w3 * (fvC - fvA) * (amC - amA));
