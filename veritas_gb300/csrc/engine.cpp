@@ -630,6 +630,7 @@ std::vector<double> Engine::profile_kernels(Run &run, int reps) {
     ml.fields = L.dfields.as<RunFields>();
     ml.nruns = (int)L.runs.size();
     ml.maxnf = L.maxnf;
+    ml.fast = L.precision == kF64 ? L.fast64 : 0;
     ml.acell = 0;  // as in a step's later stages: the Maxwell stage made the copy
     ml.stream = stream;
     time_it([&] { run_moments(L, ml); });
@@ -1145,6 +1146,7 @@ StageLaunches Engine::stage_launches(LaunchSet &L) {
     ml.fields = L.dfields.as<RunFields>();
     ml.nruns = (int)L.runs.size();
     ml.maxnf = L.maxnf;
+    ml.fast = L.precision == kF64 ? L.fast64 : 0;
     ml.stream = stream;
     al.patches = L.dpatch.p;
     al.lvl_ptr = L.dlvl_ptr.as<int>();
@@ -1711,6 +1713,7 @@ void Engine::moments_only(const std::vector<Run *> &set) {
     ml.fields = L.dfields.as<RunFields>();
     ml.nruns = (int)L.runs.size();
     ml.maxnf = L.maxnf;
+    ml.fast = L.precision == kF64 ? L.fast64 : 0;
     ml.stream = stream;
     run_moments(L, ml);
     AsmLaunch al{};

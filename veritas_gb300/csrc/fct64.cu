@@ -12,10 +12,12 @@
 // serves a single patch, all patches of an AMR hierarchy, or a batch of independent runs.
 //
 // Compiled a second time with -DVX_FP64_FAST and contraction allowed: the FP64 form that
-// trades the reference's rounding for fewer FP64 instructions (fused multiply-add, and
-// WENO weights from one ratio: 3 divisions per face value instead of 5).  Its kernels
+// trades the reference's rounding for fewer FP64 instructions (fused multiply-add, the
+// WENO weights as one quotient, and the two quotients of a face value through a
+// Newton-refined hardware reciprocal instead of five IEEE divisions).  Its kernels
 // live in namespace vx::fast64 and its launcher is launch_fct64_substep_fast.
 #include <cuda_runtime.h>
+#include "fast64.cuh"
 #include "vx_kernels.hpp"
 
 #ifdef VX_FP64_FAST
@@ -46,9 +48,9 @@ __device__ __forceinline__ double weno_face(double f1, double f2, double f3, dou
     double bR = c43 * (AR * AR) - 0.5 * AR * BR + 0.25 * (BR * BR);
     const double mm = 1.0e-10;
 #ifdef VX_FP64_FAST
-    // oL / (oL + oR) with o = 0.5 / (mm + b)^2, from the ratio rr = (mm + bL) / (mm + bR)
-    const double rr = (mm + bL) / (mm + bR);
-    double wL = 1.0 / (1.0 + rr * rr);  // rr^2 = inf gives 0, the limit
+    // oL / (oL + oR) with o = 0.5 / (mm + b)^2 is dR^2 / (dL^2 + dR^2), d = mm + b
+    const double dL = mm + bL, dR = mm + bR;
+    double wL = (dR * dR) * rcp_nr(dL * dL + dR * dR);
     double wR = 1.0 - wL;
 #else
     double oL = 0.5 / ((mm + bL) * (mm + bL));
@@ -61,7 +63,11 @@ __device__ __forceinline__ double weno_face(double f1, double f2, double f3, dou
     double pick;
     if (right) pick = (wL0 > wR0) ? wL0 : wR0;
     else pick = (wL0 < wR0) ? wL0 : wR0;
+#ifdef VX_FP64_FAST
+    double fwl = pick * rcp_nr(wL0 + wR0);
+#else
     double fwl = pick / (wL0 + wR0);
+#endif
     double fwr = 1 - fwl;
     return fwl * fL + fwr * fR;
 }
@@ -83,8 +89,8 @@ __device__ __forceinline__ void weno_face_both(double f1, double f2, double f3, 
     double bR = c43 * (AR * AR) - 0.5 * AR * BR + 0.25 * (BR * BR);
     const double mm = 1.0e-10;
 #ifdef VX_FP64_FAST
-    const double rr = (mm + bL) / (mm + bR);
-    double wL = 1.0 / (1.0 + rr * rr);
+    const double dL = mm + bL, dR = mm + bR;
+    double wL = (dR * dR) * rcp_nr(dL * dL + dR * dR);
     double wR = 1.0 - wL;
 #else
     double oL = 0.5 / ((mm + bL) * (mm + bL));
@@ -95,10 +101,18 @@ __device__ __forceinline__ void weno_face_both(double f1, double f2, double f3, 
     double wL0 = wL * (0.75 + wL * (wL - 0.5));
     double wR0 = wR * (0.75 + wR * (wR - 0.5));
     const double pr = (wL0 > wR0) ? wL0 : wR0, pl = (wL0 < wR0) ? wL0 : wR0;
+#ifdef VX_FP64_FAST
+    const double inv = rcp_nr(wL0 + wR0);  // one reciprocal for both choices
+    double fwl = pr * inv;
+    out_right = fwl * fL + (1 - fwl) * fR;
+    fwl = pl * inv;
+    out_left = fwl * fL + (1 - fwl) * fR;
+#else
     double fwl = pr / (wL0 + wR0);
     out_right = fwl * fL + (1 - fwl) * fR;
     fwl = pl / (wL0 + wR0);
     out_left = fwl * fL + (1 - fwl) * fR;
+#endif
 }
 
 __device__ __forceinline__ double vmax(double a, double b) { return (a > b) ? a : b; }

@@ -8,6 +8,7 @@
 // and evaluation order.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include "fast64.cuh"
 #include "field_ops.cuh"
 #include "vx_kernels.hpp"
 
@@ -44,6 +45,28 @@ __device__ __forceinline__ void rel_shared(const P64 &P, const double *f, int i,
 }
 __device__ __forceinline__ double rel_pick(const P64 &P, int k, double a1, double a2, double a3, double f3) {
     return P.relc[3 * k] * a1 + P.relc[3 * k + 1] * a2 + P.relc[3 * k + 2] * a3 + f3;
+}
+// The same two for the fast FP64 form: multiply-adds fused (this file is otherwise
+// compiled without contraction).
+__device__ __forceinline__ void rel_shared_fma(const P64 &P, const double *f, int i, int j, double &f3, double &a1,
+                                               double &a2, double &a3, double &cor) {
+    const int pit = P.pitch;
+    f3 = f[pidx(i, j, pit)];
+    const double m0 = 0.104166666666667, m1 = -0.708333333333334, m2 = 0.708333333333334, m3 = -0.104166666666667;
+    const double m4 = 0.117647058823529, m5 = 0.029411764705882, m6 = 0.029411764705882, m7 = 0.117647058823529;
+    const double m8 = -0.083333333333333, m9 = 0.166666666666667, m10 = -0.166666666666667, m11 = 0.083333333333334;
+    const double g1 = f[pidx(i - 2, j, pit)] - f3, g2 = f[pidx(i - 1, j, pit)] - f3;
+    const double g4 = f[pidx(i + 1, j, pit)] - f3, g5 = f[pidx(i + 2, j, pit)] - f3;
+    a1 = __fma_rn(m3, g5, __fma_rn(m2, g4, __fma_rn(m1, g2, m0 * g1)));
+    a2 = __fma_rn(m7, g5, __fma_rn(m6, g4, __fma_rn(m5, g2, m4 * g1)));
+    a3 = __fma_rn(m11, g5, __fma_rn(m10, g4, __fma_rn(m9, g2, m8 * g1)));
+    double te = 0.0;
+    for (int q = 0; q < P.rtb; q++)
+        te += __fma_rn(P.relc[3 * q + 2], a3, __fma_rn(P.relc[3 * q + 1], a2, __fma_rn(P.relc[3 * q], a1, f3)));
+    cor = __fma_rn(-1.0 / (double)P.rtb, te, f3);
+}
+__device__ __forceinline__ double rel_pick_fma(const P64 &P, int k, double a1, double a2, double a3, double f3) {
+    return __fma_rn(P.relc[3 * k + 2], a3, __fma_rn(P.relc[3 * k + 1], a2, __fma_rn(P.relc[3 * k], a1, f3)));
 }
 
 __device__ __forceinline__ double cell_asq(const RunFields &F, int x) {
@@ -91,6 +114,28 @@ __device__ __forceinline__ void mom_sync(int bar) {
 // j = j0 - 1 + L; lanes 1 .. kMomOut return the charge and current contributions cc[q],
 // cj[q] of their cell (zero where the cell is not used) and set `use`.  All 32 lanes
 // take part (shuffles).  a[q]: q^2 A^2 of sub-column k0+q.
+// ln(Gn / G) for the fast FP64 form.  Neighbouring nodes of a p grid differ by a factor
+// 1 + dp / gamma, so z = (Gn - G) / (Gn + G) is small and ln(Gn / G) = 2 atanh(z) =
+// 2 z (1 + z^2/3 + z^4/5 + z^6/7) to within z^8 / 9 < 1.2e-17 relative for |z| <= 0.01;
+// otherwise (and for G = 0 past the window's end, whose value is not used) the logarithm
+// of the quotient.
+__device__ __forceinline__ double fast_log_ratio(double Gn, double G) {
+    const double s = Gn + G;
+    if (G != 0.0 && s != 0.0) {
+        const double z = (Gn - G) * rcp_nr(s);
+        if (fabs(z) <= 0.01) {
+            const double z2 = z * z;
+            const double poly = __fma_rn(z2, __fma_rn(z2, __fma_rn(z2, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
+            return (2.0 * z) * poly;
+        }
+        return log(Gn * rcp_nr(G));
+    }
+    return log(Gn / G);
+}
+
+// FAST (the fast FP64 form): multiply-adds fused and the node ratio's logarithm as above;
+// the same formulas, not the reference's rounding.
+template <bool FAST>
 __device__ __forceinline__ void mom_window(const P64 &P, const double *f, bool real, int i, int j0, int k0, int kg,
                                            const double a[2], double c1, double c2, int lane, double cc[2],
                                            double cj[2], bool &use) {
@@ -101,9 +146,10 @@ __device__ __forceinline__ void mom_window(const P64 &P, const double *f, bool r
     double p = 0.0, f3 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0, cor = 0.0;
     use = false;
     if (real) {
-        p = P.pmin + P.dp * (double)(j + P.p_pos);
+        p = FAST ? __fma_rn(P.dp, (double)(j + P.p_pos), P.pmin) : P.pmin + P.dp * (double)(j + P.p_pos);
         if (j <= np) {
             if (rtb == 1) f3 = f[pidx(i, j, pit)];
+            else if (FAST) rel_shared_fma(P, f, i, j, f3, a1, a2, a3, cor);
             else rel_shared(P, f, i, j, f3, a1, a2, a3, cor);
         }
         use = lane >= 1 && lane <= kMomOut && j < np && !(P.nested && P.nested[pidx(i, j, pit)]);
@@ -114,19 +160,25 @@ __device__ __forceinline__ void mom_window(const P64 &P, const double *f, bool r
         if (real) {
             double G = 0.0, V = 0.0;
             if (j <= np + 1) {
-                double g = sqrt(1.0 + ((p * p) + a[q]) * P.g2);
-                G = g + c1 * p;
+                if (FAST) {
+                    const double g = sqrt(__fma_rn(__fma_rn(p, p, a[q]), P.g2, 1.0));
+                    G = __fma_rn(c1, p, g);
+                } else {
+                    double g = sqrt(1.0 + ((p * p) + a[q]) * P.g2);
+                    G = g + c1 * p;
+                }
             }
-            if (j <= np) V = rtb == 1 ? f3 : rel_pick(P, k0 + q, a1, a2, a3, f3) + cor;
+            if (j <= np) V = rtb == 1 ? f3 : (FAST ? rel_pick_fma(P, k0 + q, a1, a2, a3, f3) : rel_pick(P, k0 + q, a1, a2, a3, f3)) + cor;
             const double Gn = __shfl_down_sync(full, G, 1);
-            const double L = c2 * log(Gn / G);  // valid for lanes 0..30
+            // valid for lanes 0..30 (lane 31's Gn is its own G; beyond n_p + 1, G = 0)
+            const double L = FAST ? c2 * fast_log_ratio(Gn, G) : c2 * log(Gn / G);
             const double Lm = __shfl_up_sync(full, L, 1);
             const double Lp = __shfl_down_sync(full, L, 1);
             const double Vm = __shfl_up_sync(full, V, 1);
             const double Vp = __shfl_down_sync(full, V, 1);
             if (use) {
                 cc[q] = V;
-                cj[q] = V * L + c3 * (Lp - Lm) * (Vp - Vm);
+                cj[q] = FAST ? __fma_rn(V, L, c3 * (Lp - Lm) * (Vp - Vm)) : V * L + c3 * (Lp - Lm) * (Vp - Vm);
             }
         }
     }
@@ -134,6 +186,7 @@ __device__ __forceinline__ void mom_window(const P64 &P, const double *f, bool r
 
 // One unit: the kMomCols columns col0 .. col0 + kMomCols - 1 of the padded column list,
 // formed by warps 0 .. kMomCols - 1 and summed by warp kMomCols (wid: warp within the unit).
+template <bool FAST>
 __device__ __forceinline__ void moments_unit(const MomLaunch &M, int col0, int wid, int lane, MomSmem &S, int bar) {
     const bool summer = wid == kMomCols;  // the last warp adds; warps 0..kMomCols-1 form columns
     const bool real = !summer && M.colpatch[col0 + wid] >= 0;  // warp-uniform
@@ -169,7 +222,7 @@ __device__ __forceinline__ void moments_unit(const MomLaunch &M, int col0, int w
             if (!summer) {
                 double cc[2], cj[2];
                 bool use;
-                mom_window(P, f, real, i, j0, k0, kg, a, c1, c2, lane, cc, cj, use);
+                mom_window<FAST>(P, f, real, i, j0, k0, kg, a, c1, c2, lane, cc, cj, use);
                 for (int q = 0; q < kg; q++) {
                     S.cc[bf][wid][q][lane] = cc[q];
                     S.cj[bf][wid][q][lane] = cj[q];
@@ -197,16 +250,18 @@ __device__ __forceinline__ void moments_unit(const MomLaunch &M, int col0, int w
     }
 }
 
-__global__ void __launch_bounds__(kMomThreads) k64_moments(MomLaunch M) {
+template <bool FAST>
+__global__ void __launch_bounds__(kMomThreads, 2) k64_moments(MomLaunch M) {
     VX_PDL_WAIT();
     __shared__ MomSmem S;
-    moments_unit(M, blockIdx.x * kMomCols, threadIdx.x >> 5, threadIdx.x & 31, S, 0);
+    moments_unit<FAST>(M, blockIdx.x * kMomCols, threadIdx.x >> 5, threadIdx.x & 31, S, 0);
 }
 
 void launch_moments64(const MomLaunch &M) {
     if (M.ncols == 0) return;
     // M.ncols is a multiple of kMomCols (the list is padded per patch)
-    vx_launch(k64_moments, M.ncols / kMomCols, kMomThreads, 0, M.stream, M);
+    if (M.fast) vx_launch(k64_moments<true>, M.ncols / kMomCols, kMomThreads, 0, M.stream, M);
+    else vx_launch(k64_moments<false>, M.ncols / kMomCols, kMomThreads, 0, M.stream, M);
 }
 
 // ---------------------------------------------------------------- separable initial f
@@ -860,6 +915,7 @@ __global__ void __launch_bounds__(1024, 1) k_poisson(PoissonLaunch L) {
 // ---- workers of the pipelined launch
 // One item: column warp wid forms window j0 of its column's sub-columns k0, k0+1 (those
 // the patch has) and writes the contributions of lanes 1 .. kMomOut to `out`.
+template <bool FAST>
 __device__ __forceinline__ void mom_item(const PipeLaunch &K, int u, int k0, int j0, int wid, int lane, double *out) {
     const MomLaunch &M = K.M;
     const int col0 = K.unit_col0[u];
@@ -875,7 +931,7 @@ __device__ __forceinline__ void mom_item(const PipeLaunch &K, int u, int k0, int
         if (real) a[q] = P.qq * cell_asq(F, (i + P.x_pos) * rtb + k0 + q);
     double cc[2], cj[2];
     bool use;
-    mom_window(P, P.f1, real, i, j0, k0, kg, a, c12.x, c12.y, lane, cc, cj, use);
+    mom_window<FAST>(P, P.f1, real, i, j0, k0, kg, a, c12.x, c12.y, lane, cc, cj, use);
     if (lane >= 1 && lane <= kMomOut)
         for (int q = 0; q < kg; q++) {
             out[lane * 30 + wid * 2 + q] = cc[q];
@@ -924,6 +980,7 @@ __device__ void mom_sum_unit(const PipeLaunch &K, int u, int lane) {
 // A group of a worker block: column warps 0 .. kMomCols-1 take items until none are left;
 // the warp that completes a unit (the unit's item count reaches its total) appends the
 // unit to the queue of completed units.  They never wait for anything but each other.
+template <bool FAST>
 __device__ void pipe_columns(const PipeLaunch &K, int *ticket, int g) {
     const int tid = (int)threadIdx.x - g * kMomThreads, wid = tid >> 5, lane = tid & 31;
     const int bar = 1 + g, ncol = kMomCols * 32;
@@ -937,7 +994,7 @@ __device__ void pipe_columns(const PipeLaunch &K, int *ticket, int g) {
         const int u = K.item_unit[t];
         const int loc = t - K.unit_item0[u], nw = K.unit_nwin[u];
         const int kp = loc / nw;
-        mom_item(K, u, 2 * kp, (loc - kp * nw) * kMomOut, wid, lane, K.scratch + (size_t)t * kPipeItemDoubles);
+        mom_item<FAST>(K, u, 2 * kp, (loc - kp * nw) * kMomOut, wid, lane, K.scratch + (size_t)t * kPipeItemDoubles);
         __threadfence();  // this warp's contributions, device-wide, before the item counts
         pipe_bar(bar, ncol);
         if (tid == 0) {
@@ -994,6 +1051,7 @@ __device__ void pipe_summer(const PipeLaunch &K, int lane) {
 // Column warps wait for nothing outside their group, summing warps only for column
 // warps, the solve only for summing warps: every wait ends whatever order the blocks are
 // scheduled in.  Same arithmetic as k64_moments + k_assemble + k_poisson.
+template <bool FAST>
 __global__ void __launch_bounds__(1024, 1) k64_moments_poisson(PipeLaunch K) {
     VX_PDL_WAIT();
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1006,7 +1064,7 @@ __global__ void __launch_bounds__(1024, 1) k64_moments_poisson(PipeLaunch K) {
     } else {
         int *ticket = reinterpret_cast<int *>(smem_raw);
         const int g = (int)threadIdx.x / kMomThreads;
-        if (((int)threadIdx.x & (kMomThreads - 1)) < kMomCols * 32) pipe_columns(K, ticket + 2 * g, g);
+        if (((int)threadIdx.x & (kMomThreads - 1)) < kMomCols * 32) pipe_columns<FAST>(K, ticket + 2 * g, g);
     }
     // the last block out zeroes the tickets, the queue, done and item counters for the next launch
     __syncthreads();
@@ -1048,7 +1106,8 @@ void launch_moments_poisson64(const PipeLaunch &K0) {
     K.P.x_in_smem = (K.P.maxn <= kPoisSmemMaxN && base + 8 * K.P.maxn <= max_smem) ? 1 : 0;
     const int smem_solve = base + (K.P.x_in_smem ? 8 * K.P.maxn : 0);
     const int smem = std::max(smem_solve, 16);
-    cudaFuncSetAttribute(k64_moments_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    auto kern = K.M.fast ? k64_moments_poisson<true> : k64_moments_poisson<false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(K.P.nruns + K.summers + K.workers);
     cfg.blockDim = dim3(1024);
@@ -1061,7 +1120,7 @@ void launch_moments_poisson64(const PipeLaunch &K0) {
     attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = g_launch_pdl ? 2 : 1;
-    cudaLaunchKernelEx(&cfg, k64_moments_poisson, K);  // errors surface through cudaGetLastError
+    cudaLaunchKernelEx(&cfg, kern, K);  // errors surface through cudaGetLastError
 }
 
 // E_x on the finest grid from phi and Ex0 (EMSolver::GetEfield), for states loaded from

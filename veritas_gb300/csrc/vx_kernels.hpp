@@ -94,6 +94,7 @@ struct MomLaunch {
     int nruns, maxnf;     // FP32: the per-cell A^2 copy covers every run's field grid
     int acell = 1;        // FP32: refresh the per-cell A^2 copy first (else the Maxwell stage made it)
     int asq32 = 1;        // FP32: the moments kernel also makes the FP32 copy of a^2
+    int fast = 0;         // FP64: the fast form's moments (fused multiply-adds, Newton reciprocal)
     cudaStream_t stream;
 };
 constexpr int kMomCols = 15;  // FP64 moment columns per block (padded per patch), plus a summing warp
