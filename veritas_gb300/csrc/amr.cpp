@@ -6,7 +6,6 @@
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
-#include <unordered_map>
 
 #include "engine.hpp"
 
@@ -125,45 +124,18 @@ void conn_same(Rect &a, const Rect &b, int r) {
     }
 }
 
-// Assigns each op of an ordered list the smallest batch that keeps the list's
-// read/write orders (RAW, WAR, WAW) on the cells it touches.
-struct Scheduler {
-    std::unordered_map<uint64_t, int> last_w, last_r;
-    std::vector<int> batch;
-    int nbatches = 0;
-    static uint64_t key(int patch, int plane, int i, int j) {
-        return ((uint64_t)(uint32_t)patch << 36) ^ ((uint64_t)plane << 32) ^ ((uint64_t)(uint32_t)(i + 4) << 16) ^
-               (uint64_t)(uint32_t)(j + 4);
-    }
-    void add(const std::vector<uint64_t> &reads, const std::vector<uint64_t> &writes) {
-        int b = 0;
-        for (auto c : reads) {
-            auto it = last_w.find(c);
-            if (it != last_w.end()) b = std::max(b, it->second + 1);
-        }
-        for (auto c : writes) {
-            auto it = last_w.find(c);
-            if (it != last_w.end()) b = std::max(b, it->second + 1);
-            auto jt = last_r.find(c);
-            if (jt != last_r.end()) b = std::max(b, jt->second + 1);
-        }
-        for (auto c : reads) {
-            auto &v = last_r[c];
-            v = std::max(v, b);
-        }
-        for (auto c : writes) last_w[c] = b;
-        batch.push_back(b);
-        nbatches = std::max(nbatches, b + 1);
-    }
-};
+constexpr int kMaxRatio = 8;  // refinement ratios above it are refused (build_amr)
+constexpr int kMaxBatches = 255;  // op batches per list (the fills and exchanges take a few)
 
-// The same schedule for ghost-fill ops, with the last write / read batch of each cell
-// kept in dense per-patch planes (allocated when a patch is first touched) instead of a
-// hash map: the restriction ops of large nested regions number in the millions.
+// Assigns each op of an ordered list the smallest batch that keeps the list's read /
+// write orders (RAW, WAR, WAW) on the cells it touches, with the last write / read batch
+// of each cell kept in dense per-patch byte planes (batch + 1, 0 for none; allocated when
+// a patch is first touched): the restriction ops of large nested regions number in the
+// millions.
 struct PlaneScheduler {
     explicit PlaneScheduler(const std::vector<Rect *> &patches) : flat(patches), last_w(patches.size()), last_r(patches.size()) {}
     const std::vector<Rect *> &flat;
-    std::vector<std::vector<int16_t>> last_w, last_r;
+    std::vector<std::vector<uint8_t>> last_w, last_r;  // batch + 1, 0 = none
     std::vector<int> batch;
     int nbatches = 0;
     size_t slot(int patch, int i, int j) {
@@ -173,8 +145,8 @@ struct PlaneScheduler {
             throw std::invalid_argument("AMR layout: ghost op cell outside its patch");
         if (last_w[patch].empty()) {
             const size_t cells = (size_t)(R.n_x + 4) * (R.n_p + 4);
-            last_w[patch].assign(cells, (int16_t)-1);
-            last_r[patch].assign(cells, (int16_t)-1);
+            last_w[patch].assign(cells, 0);
+            last_r[patch].assign(cells, 0);
         }
         return (size_t)(i + 2) * (R.n_p + 4) + (j + 2);
     }
@@ -183,60 +155,65 @@ struct PlaneScheduler {
         int b = 0;
         for (int q = 0; q < nr; q++) {
             const size_t c = slot(reads[q][0], reads[q][1], reads[q][2]);
-            b = std::max(b, last_w[reads[q][0]][c] + 1);
+            b = std::max<int>(b, last_w[reads[q][0]][c]);
         }
         for (int q = 0; q < nw; q++) {
             const size_t c = slot(writes[q][0], writes[q][1], writes[q][2]);
-            b = std::max(b, last_w[writes[q][0]][c] + 1);
-            b = std::max(b, last_r[writes[q][0]][c] + 1);
+            b = std::max<int>(b, last_w[writes[q][0]][c]);
+            b = std::max<int>(b, last_r[writes[q][0]][c]);
         }
-        if (b > 32000) throw std::runtime_error("ghost-fill schedule too deep");
+        if (b >= kMaxBatches) throw std::runtime_error("AMR op schedule too deep");
         for (int q = 0; q < nr; q++) {
-            int16_t &v = last_r[reads[q][0]][slot(reads[q][0], reads[q][1], reads[q][2])];
-            v = (int16_t)std::max<int>(v, b);
+            uint8_t &v = last_r[reads[q][0]][slot(reads[q][0], reads[q][1], reads[q][2])];
+            v = (uint8_t)std::max<int>(v, b + 1);
         }
-        for (int q = 0; q < nw; q++) last_w[writes[q][0]][slot(writes[q][0], writes[q][1], writes[q][2])] = (int16_t)b;
+        for (int q = 0; q < nw; q++) last_w[writes[q][0]][slot(writes[q][0], writes[q][1], writes[q][2])] = (uint8_t)(b + 1);
         batch.push_back(b);
         nbatches = std::max(nbatches, b + 1);
     }
-    // add() for a restriction: reads the r x r block at (si, sj) of patch src, writes
-    // (di, dj) of patch dst; the same batch, with the block's bounds checked once.
-    void add_restrict(int dst, int di, int dj, int src, int si, int sj, int r) {
+    // Restrictions of `len` consecutive cells (di, dj + k) of patch dst from the r x r
+    // blocks at (si, sj + r k) of patch src, scheduled as one unit: every cell takes the
+    // largest batch any of them needs, which keeps each cell's read / write orders (a
+    // later batch than a cell's own minimum never runs before an op it must follow, and
+    // the ops emitted after see the batch in the planes).  Bounds are checked once for
+    // the row; one batch entry per cell op.
+    void add_restrict_row(int dst, int di, int dj, int src, int si, int sj, int r, int len) {
         slot(src, si, sj);
-        slot(src, si + r - 1, sj + r - 1);  // bounds of the whole block
-        const size_t cw = slot(dst, di, dj);
+        slot(src, si + r - 1, sj + r * len - 1);  // bounds of the row's blocks
+        slot(dst, di, dj);
+        const size_t cw = slot(dst, di, dj + len - 1) - (size_t)(len - 1);
         const int wp = flat[src]->n_p + 4;
         const size_t s0 = slot(src, si, sj);
-        const int16_t *lw = last_w[src].data();
+        const uint8_t *lw = last_w[src].data();
+        const uint8_t *dw = last_w[dst].data() + cw, *dr = last_r[dst].data() + cw;
         int b = 0;
-        for (int a = 0; a < r; a++)
-            for (int q = 0; q < r; q++) b = std::max(b, lw[s0 + (size_t)a * wp + q] + 1);
-        b = std::max(b, last_w[dst][cw] + 1);
-        b = std::max(b, last_r[dst][cw] + 1);
-        if (b > 32000) throw std::runtime_error("ghost-fill schedule too deep");
-        int16_t *lr = last_r[src].data();
-        for (int a = 0; a < r; a++)
-            for (int q = 0; q < r; q++) {
-                int16_t &v = lr[s0 + (size_t)a * wp + q];
-                v = (int16_t)std::max<int>(v, b);
-            }
-        last_w[dst][cw] = (int16_t)b;
-        batch.push_back(b);
+        for (int a = 0; a < r; a++) {
+            const uint8_t *row = lw + s0 + (size_t)a * wp;
+            for (int q = 0; q < r * len; q++) b = std::max<int>(b, row[q]);
+        }
+        for (int k = 0; k < len; k++) b = std::max<int>(b, std::max(dw[k], dr[k]));
+        if (b >= kMaxBatches) throw std::runtime_error("AMR op schedule too deep");
+        uint8_t *lr = last_r[src].data();
+        for (int a = 0; a < r; a++) {
+            uint8_t *row = lr + s0 + (size_t)a * wp;
+            for (int q = 0; q < r * len; q++) row[q] = std::max<uint8_t>(row[q], (uint8_t)(b + 1));
+        }
+        uint8_t *dwm = last_w[dst].data() + cw;
+        for (int k = 0; k < len; k++) dwm[k] = (uint8_t)(b + 1);
+        batch.insert(batch.end(), (size_t)len, b);
         nbatches = std::max(nbatches, b + 1);
     }
 };
 
+// Stable counting sort of the ops by batch; out.ptr gets the batch offsets.
 template <class Op>
 void sort_by_batch(std::vector<Op> &ops, const std::vector<int> &batch, int nb, Batched &out) {
-    std::vector<Op> sorted;
-    sorted.reserve(ops.size());
-    out.ptr.assign(1, 0);
-    std::vector<std::vector<Op>> buckets(nb);
-    for (size_t k = 0; k < ops.size(); k++) buckets[batch[k]].push_back(ops[k]);
-    for (auto &b : buckets) {
-        sorted.insert(sorted.end(), b.begin(), b.end());
-        out.ptr.push_back((int)sorted.size());
-    }
+    out.ptr.assign((size_t)nb + 1, 0);
+    for (size_t k = 0; k < ops.size(); k++) out.ptr[batch[k] + 1]++;
+    for (int b = 0; b < nb; b++) out.ptr[b + 1] += out.ptr[b];
+    std::vector<int> fill(out.ptr.begin(), out.ptr.end() - 1);
+    std::vector<Op> sorted(ops.size());
+    for (size_t k = 0; k < ops.size(); k++) sorted[fill[batch[k]]++] = ops[k];
     ops.swap(sorted);
 }
 
@@ -419,14 +396,24 @@ void Run::build_amr() {
         for (auto &rp : lvl) {
             Rect &R = *rp;
             for (int i = 0; i < R.n_x; i++)
-                for (int j = 0; j < R.n_p; j++)
-                    if (R.nested[R.ns(i, j)]) {
-                        const Rect &F = *flat[R.finer[R.ns(i, j)]];
-                        const GhostOp op{kGhostRestrict, R.id, i, j, F.id, (R.x_pos + i) * r - F.x_pos,
-                                         (R.p_pos + j) * r - F.p_pos, 0};
-                        gs.add_restrict(op.dst, op.di, op.dj, op.src, op.si, op.sj, r);
-                        ghost_ops.push_back(op);
+                for (int j = 0; j < R.n_p;) {
+                    if (!R.nested[R.ns(i, j)]) {  // skip to the row's next nested cell
+                        const uint8_t *row = &R.nested[R.ns(i, 0)];
+                        const void *hit = std::memchr(row + j, 1, (size_t)(R.n_p - j));
+                        if (!hit) break;
+                        j = (int)((const uint8_t *)hit - row);
                     }
+                    // a run of nested cells over the same finer patch, in the loop's order
+                    const int fid = R.finer[R.ns(i, j)];
+                    int j1 = j + 1;
+                    while (j1 < R.n_p && R.nested[R.ns(i, j1)] && R.finer[R.ns(i, j1)] == fid) j1++;
+                    const Rect &F = *flat[fid];
+                    const int si = (R.x_pos + i) * r - F.x_pos;
+                    gs.add_restrict_row(R.id, i, j, F.id, si, (R.p_pos + j) * r - F.p_pos, r, j1 - j);
+                    for (int k = j; k < j1; k++)
+                        ghost_ops.push_back({kGhostRestrict, R.id, i, k, F.id, si, (R.p_pos + k) * r - F.p_pos, 0});
+                    j = j1;
+                }
         }
     };
     auto type1 = [&](std::vector<std::unique_ptr<Rect>> &lvl) {  // UpdateSameLevelBoundaries
@@ -545,23 +532,35 @@ void Run::build_amr() {
 
     // ------------------------------------------------------------ limiter C exchange
     csync_ops.clear();
-    Scheduler cs;
-    auto ckey = [&](int patch, int plane, int i, int j) { return Scheduler::key(patch, plane, i, j); };
+    // the Cx and Cp planes of every patch as 2 x flat scheduler planes (Cp of patch k at k + nflat)
+    std::vector<Rect *> cplanes(flat);
+    cplanes.insert(cplanes.end(), flat.begin(), flat.end());
+    const int nflat = (int)flat.size();
+    PlaneScheduler cs(cplanes);
     auto emit_c = [&](const CSyncOp &op) {
-        const int plane = op.t < 2 ? 0 : 1;
-        std::vector<uint64_t> reads, writes;
+        const int off = op.t < 2 ? 0 : nflat;
+        int reads[2][3], writes[2 + kMaxRatio][3];
+        int nr = 0, nw = 0;
+        auto cell = [&](int (*a)[3], int &n, int patch, int i, int j) {
+            a[n][0] = patch + off, a[n][1] = i, a[n][2] = j, n++;
+        };
         if (op.kind == kCSame) {
-            writes = {ckey(op.nb, plane, op.ni, op.nj), ckey(op.caller, plane, op.ci, op.cj)};
+            cell(writes, nw, op.nb, op.ni, op.nj);
+            cell(writes, nw, op.caller, op.ci, op.cj);
         } else if (op.kind == kCUpdate) {
-            reads = {ckey(op.nb, plane, op.ni, op.nj), ckey(op.caller, plane, op.ci, op.cj)};
-            writes = reads;
+            cell(reads, nr, op.nb, op.ni, op.nj);
+            cell(reads, nr, op.caller, op.ci, op.cj);
+            cell(writes, nw, op.nb, op.ni, op.nj);
+            cell(writes, nw, op.caller, op.ci, op.cj);
         } else {
-            reads = {ckey(op.nb, plane, op.ni, op.nj)};
-            writes = {ckey(op.nb, plane, op.ni, op.nj)};
-            for (int k = 0; k < r; k++)
-                writes.push_back(plane == 0 ? ckey(op.caller, 0, op.ci, op.cj + k) : ckey(op.caller, 1, op.ci + k, op.cj));
+            cell(reads, nr, op.nb, op.ni, op.nj);
+            cell(writes, nw, op.nb, op.ni, op.nj);
+            for (int k = 0; k < r; k++) {
+                if (off == 0) cell(writes, nw, op.caller, op.ci, op.cj + k);
+                else cell(writes, nw, op.caller, op.ci + k, op.cj);
+            }
         }
-        cs.add(reads, writes);
+        cs.add(reads, nr, writes, nw);
         csync_ops.push_back(op);
     };
     // same-level exchange on every face of every patch edge; the domain boundary's
@@ -607,11 +606,13 @@ void Run::build_amr() {
             for (auto &rp : sp[l]) same_calls(*rp, kCUpdate);
     }
     sort_by_batch(csync_ops, cs.batch, cs.nbatches, csync_b);
+    lap("csync ops");
     validate_ops();
+    lap("validate");
     dghost_ops = upload(ghost_ops, eng->stream);
     diface_ops = upload(iface_ops, eng->stream);
     dcsync_ops = upload(csync_ops, eng->stream);
-    lap("csync ops");
+    lap("op upload");
 
     // ------------------------------------------------------------ device masks, weights
     for (Rect *R : flat) {

@@ -27,6 +27,9 @@ DevBuf::DevBuf(size_t b) : bytes(b) {
         VX_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
     }
 }
+DevBuf::DevBuf(size_t b, Uninit) : bytes(b) {
+    if (b) VX_CUDA(cudaMalloc(&p, b));
+}
 DevBuf::~DevBuf() {
     if (p) cudaFree(p);
 }

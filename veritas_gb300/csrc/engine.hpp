@@ -35,7 +35,9 @@ struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
     DevBuf() = default;
-    explicit DevBuf(size_t b);
+    explicit DevBuf(size_t b);  // zero-filled
+    struct Uninit {};
+    DevBuf(size_t b, Uninit);   // contents undefined: for buffers the caller fills at once
     ~DevBuf();
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
@@ -53,8 +55,9 @@ struct DevBuf {
 // Device copy of a host vector (at least one element's worth of storage).
 template <class T>
 DevBuf upload(const std::vector<T> &v, cudaStream_t s) {
-    DevBuf b(std::max<size_t>(v.size() * sizeof(T), sizeof(T)));
-    if (!v.empty()) VX_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    if (v.empty()) return DevBuf(sizeof(T));
+    DevBuf b(v.size() * sizeof(T), DevBuf::Uninit{});
+    VX_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
     return b;
 }
 
