@@ -831,6 +831,16 @@ void Engine::build_tiles(LaunchSet &L) {
 }
 
 void Engine::build_set(LaunchSet &L) {
+    // VX_TRACE_INIT=1: wall time of each phase on stderr
+    static const bool trace = std::getenv("VX_TRACE_INIT") != nullptr;
+    auto t0 = std::chrono::steady_clock::now();
+    auto lap = [&](const char *what) {
+        if (!trace) return;
+        sync();
+        auto t1 = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "vx set %-12s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(t1 - t0).count());
+        t0 = t1;
+    };
     L.precision = L.runs.empty() ? kF64 : L.runs[0]->precision;
     L.tile_j = tile_pref[L.precision == kF32][0];
     L.tile_i = tile_pref[L.precision == kF32][1];
@@ -913,6 +923,7 @@ void Engine::build_set(LaunchSet &L) {
         sp[24] = dpsMax;
         spec.insert(spec.end(), sp.begin(), sp.end());
     }
+    lap("runs");
     // AMR op tables: batch b of the set = batch b of every run, patch ids made global.
     // Each run's sorted lists already sit on the device; the set's tables are gathered
     // there, one segment per (batch, run), so a new set costs no host-side op copies.
@@ -960,37 +971,49 @@ void Engine::build_set(LaunchSet &L) {
         L.diface_ptr = upload(L.iface_ptr, stream);
         L.dcsync_ptr = upload(L.csync_ptr, stream);
     }
+    lap("op tables");
     // Moment work units (FP64: blocks of kMomCols columns of one patch; FP32: one column
     // per warp) longest first: a unit's time grows with its patch's n_p and sub-columns,
     // and the GPU schedules blocks in list order, so the short units of the fine levels
     // fill the tail instead of leaving a last wave of long base-level blocks alone on a
     // few SMs.  Each column's result is independent of the order.
     {
+        // A unit's cost depends on its patch alone and a patch's units are consecutive in
+        // the list, so a stable sort of the patches' unit ranges by cost gives the stable
+        // sort of the units (in O(units) instead of sorting every unit).
         const int unit = L.precision == kF64 ? kMomCols : 1;
         const int nunits = (int)colpatch.size() / unit;
-        auto cost = [&](int u) {
-            const PatchT<double> &d = L.hpatch[colpatch[(size_t)u * unit]];
-            return (long long)(d.np + 2) * ((d.rtb + 1) / 2);
+        struct Range {
+            int u0, u1;
+            long long cost;
         };
-        std::vector<int> order(nunits);
-        for (int u = 0; u < nunits; u++) order[u] = u;
-        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+        std::vector<Range> ranges;
+        for (int u = 0; u < nunits;) {
+            const int pi = colpatch[(size_t)u * unit];
+            int u1 = u + 1;
+            while (u1 < nunits && colpatch[(size_t)u1 * unit] == pi) u1++;
+            const PatchT<double> &d = L.hpatch[pi];
+            ranges.push_back({u, u1, (long long)(d.np + 2) * ((d.rtb + 1) / 2)});
+            u = u1;
+        }
+        std::stable_sort(ranges.begin(), ranges.end(), [](const Range &a, const Range &b) { return a.cost > b.cost; });
         std::vector<int> cp2, ci2;
         cp2.reserve(colpatch.size());
         ci2.reserve(colidx.size());
-        for (int u : order)
-            for (int k = 0; k < unit; k++) {
-                cp2.push_back(colpatch[(size_t)u * unit + k]);
-                ci2.push_back(colidx[(size_t)u * unit + k]);
-            }
+        for (const Range &rg : ranges) {
+            cp2.insert(cp2.end(), colpatch.begin() + (size_t)rg.u0 * unit, colpatch.begin() + (size_t)rg.u1 * unit);
+            ci2.insert(ci2.end(), colidx.begin() + (size_t)rg.u0 * unit, colidx.begin() + (size_t)rg.u1 * unit);
+        }
         colpatch.swap(cp2);
         colidx.swap(ci2);
     }
     L.ncols = (int)colpatch.size();
     build_pipe_tables(L, colpatch, colidx);
+    lap("units");
     // lvl_ptr is absolute; lvl_off points at each run's block.
     L.dpatch = upload(L.hpatch, stream);
     build_tiles(L);
+    lap("tiles");
     L.dfields = upload(fields, stream);
     L.dcolpatch = upload(colpatch, stream);
     L.dcolidx = upload(colidx, stream);
@@ -1016,6 +1039,7 @@ void Engine::build_set(LaunchSet &L) {
         L.graph = nullptr;
     }
     sync();
+    lap("uploads");
 }
 
 // Tables of the pipelined moments + solve launch (k64_moments_poisson) for an FP64 set
@@ -1637,12 +1661,17 @@ void Engine::advance(const std::vector<Run *> &set, const std::vector<double> &d
     fill_params(L, set, dt);
     if (use_graphs) {
         if (!L.graph) {
+            static const bool trace = std::getenv("VX_TRACE_INIT") != nullptr;
+            const auto t0 = std::chrono::steady_clock::now();
             cudaGraph_t g;
             VX_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
             record_step(L);
             VX_CUDA(cudaStreamEndCapture(stream, &g));
             VX_CUDA(cudaGraphInstantiate(&L.graph, g, 0));
             cudaGraphDestroy(g);
+            if (trace)
+                std::fprintf(stderr, "vx set capture      %8.2f ms\n",
+                             std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
         }
         VX_CUDA(cudaGraphLaunch(L.graph, stream));
     } else {
