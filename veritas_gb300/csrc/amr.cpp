@@ -626,7 +626,7 @@ void Run::build_amr() {
             std::memcpy(&m[pe + d], &R->ifx[q], w);
             std::memcpy(&m[2 * pe + d], &R->ifp[q], w);
         }
-        R->masks = DevBuf(m.size());
+        R->masks = DevBuf(m.size(), DevBuf::Uninit{});  // the blocking copy below fills it
         VX_CUDA(cudaMemcpy(R->masks.p, m.data(), m.size(), cudaMemcpyHostToDevice));
     }
     lap("masks");

@@ -396,6 +396,25 @@ void Run::regrid(bool init) {
         hier[sp] = update_hierarchy(s, (int)sp, hierarchy_of((int)sp), level_flags);
     }
     lap("clustering");
+    bool kept = !init;
+    for (size_t sp = 0; kept && sp < rects.size(); sp++) kept = hier[sp] == hierarchy_of((int)sp);
+    if (kept) {
+        // The clustering returned the current boxes in the current order: the promotion
+        // would build the same patches (fresh storage, all zero), the same tables, copy
+        // every f1 value across unchanged, refill the slot-1 ghosts and set f0 = f1.  Its
+        // result, in place: every plane but f0 and f1 (and the moment columns) zeroed, the
+        // ghosts refilled from the same values, f0 = f1.  The layout version stays, so the
+        // launch sets and graphs that hold this run stay valid.
+        for (Rect *R : flat) {
+            const size_t keep = 2 * R->plane_bytes();  // f0 and f1 lead the slab
+            VX_CUDA(cudaMemsetAsync(R->slab.as<char>() + keep, 0, R->slab.bytes - keep, eng->stream));
+            VX_CUDA(cudaMemsetAsync(R->cols.p, 0, R->cols.bytes, eng->stream));
+        }
+        push_data(1);
+        copy_slot(1, 0);
+        lap("kept layout");
+        return;
+    }
     promote(hier, init);
     lap("promote");
 }
