@@ -445,7 +445,7 @@ def measure_serving(ctx, count: int, steps: int, precision: int, budget_gb: floa
             "arrivals": "Poisson, 20 solves/s, splitmix64 seed 0x5EED0005", "hbm_budget_gb": budget_gb,
             "note": "each solve is scaled to a fixed step count (the full 50-period solves of this size mix "
                     "exceed one GPU's throughput at this arrival rate by two orders of magnitude); runs are built "
-                    "on the server's builder thread while the batch steps; regrid after every 21 steps"}
+                    "and regridded on the server's worker threads while the batch steps; regrid after every 21 steps"}
 
 
 def main() -> None:

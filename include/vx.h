@@ -403,16 +403,17 @@ int vx_cfl_bound_noalloc(const double *Ay, const double *Az, const double *By, c
  * batching of independent solves on one context under a device-memory budget.
  * submit() queues a solve of `steps` RK steps (arrival on the server's clock, seconds;
  * a request larger than the whole budget is refused with VX_ERR_INVALID); step() binds
- * the runs its builder thread has finished, admits in arrival order the waiting solves
- * that fit in the budget (their runs are built on that thread while the batch keeps
+ * the runs its worker threads have finished, admits in arrival order the waiting solves
+ * that fit in the budget (their runs are built on those threads while the batch keeps
  * stepping), advances every live solve one step in one batched launch set, regrids by
- * the reference driver's rule, and retires the finished ones (writing their final state
+ * the reference driver's rule (on a worker thread, the solve out of the batch until its
+ * new hierarchy is in place; it stays VX_REQ_LIVE), and retires the finished ones (writing their final state
  * to state_path when one was given) and the failed ones: a solve whose CFL bound or E_x0
  * is not finite after a step (something in it went non-finite) is retired alone with
  * VX_REQ_FAILED. */
 typedef struct vx_server vx_server;
 #define VX_REQ_WAITING 0    /* queued for device memory */
-#define VX_REQ_BUILDING 1   /* admitted; its run is being built on the server's builder thread */
+#define VX_REQ_BUILDING 1   /* admitted; its run is being built on a server worker thread */
 #define VX_REQ_LIVE 2       /* stepping with the batch */
 #define VX_REQ_DONE 3       /* all steps taken (state written if asked) */
 #define VX_REQ_CANCELLED 4  /* withdrawn by vx_server_cancel */

@@ -215,6 +215,35 @@ def test_server_cancels_waiting_and_live_requests(ctx, tmp_path):
 
 
 @pytest.mark.gpu
+def test_server_cancels_a_solve_out_for_regrid(ctx, tmp_path):
+    """A solve regrids on a worker thread, out of the batch; cancelled meanwhile, it is
+    dropped when the regrid ends (the regrid not counted), and the solve beside it
+    finishes with the same bits as alone."""
+    from veritas_gb300 import REQ_CANCELLED, REQ_DONE, Server
+
+    srv = Server(ctx, 8 << 30)
+    srv.submit(problem_for("beam2"), 30, state_path=tmp_path / "alone.bin")
+    while srv.step() != (0, 0):
+        pass
+    srv.close()
+
+    srv = Server(ctx, 8 << 30)
+    a = srv.submit(problem_for("amr2"), 40)
+    k = srv.submit(problem_for("beam2"), 30, state_path=tmp_path / "mix.bin")
+    while srv.result(a)["steps_done"] < 22:
+        srv.step()
+    srv.cancel(a)  # its regrid, due after step 22, was handed to a worker by that step
+    while srv.step() != (0, 0):
+        pass
+    ra, rk = srv.result(a), srv.result(k)
+    assert ra["status"] == REQ_CANCELLED and ra["finished"] == 1
+    assert ra["steps_done"] == 22 and ra["regrids"] == 0
+    assert rk["status"] == REQ_DONE and rk["regrids"] == 1
+    assert (tmp_path / "alone.bin").read_bytes() == (tmp_path / "mix.bin").read_bytes()
+    srv.close()
+
+
+@pytest.mark.gpu
 def test_server_retires_a_solve_gone_non_finite_alone(ctx, tmp_path):
     """A request whose laser amplitude is NaN (a bad host-side input) fails its health
     check after its first step and is retired alone; the solve stepping beside it in the

@@ -106,6 +106,9 @@ public:
     // Hands the run to another engine of the same device: the old engine drops its cached
     // launch sets (call on the thread that drives the old engine, with its work done).
     void migrate(Engine &to);
+    // Points the run at `to` when its engine has already dropped it (Engine::forget, called
+    // on that engine's own thread): a thread that cannot touch the old engine takes it over.
+    void adopt(Engine &to) { eng = &to; }
     std::unique_ptr<Settings> S;
     // rects[species][depth] -> patches of that level, in the reference's order.
     std::vector<std::vector<std::vector<std::unique_ptr<Rect>>>> rects;

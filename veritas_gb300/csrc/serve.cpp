@@ -1,15 +1,16 @@
 // Serving loop: continuous batching of independent solves on one context.
 //
-// Requests queue in arrival order.  Each call of step() first binds the runs the builder
-// thread has finished, then admits, in order, the waiting requests whose device-memory
-// estimate fits in what the budget has left and hands them to the builder thread, which
-// constructs each run (host quadrature, clustering, Poisson factors, uploads) on its own
-// engine and streams while the loop keeps stepping; the estimate is replaced by the
+// Requests queue in arrival order.  Each call of step() first binds the runs the worker
+// threads have finished, then admits, in order, the waiting requests whose device-memory
+// estimate fits in what the budget has left and hands them to the workers, which
+// construct each run (host quadrature, clustering, Poisson factors, uploads) on their own
+// engines and streams while the loop keeps stepping; the estimate is replaced by the
 // run's real footprint when it is bound.  Then every live solve advances by one full RK
 // step in one batched launch set per precision (one launch per sub-step for all of
 // them), and each solve regrids by the reference driver's rule (veritas.cpp:146-151: a
 // counter of steps since the last regrid; at a count above 20, once the plasma is on,
-// SolverManager::reGrid and the counter restarts).  A solve whose CFL bound or
+// SolverManager::reGrid and the counter restarts) — on a worker thread, the solve out of
+// the batch until its new hierarchy is in place.  A solve whose CFL bound or
 // E_x0 is not finite after its step (something in it went non-finite) fails and is
 // retired alone; the others in the batch are unaffected (runs share launches, never data).  Finished solves
 // write their final state where the request asked and release their memory before the
@@ -48,9 +49,9 @@ size_t Server::estimate_bytes(const LaserSlabParams &p, int precision) {
 }
 
 Server::Server(Engine &e, size_t budget, int max_live) : eng(e), budget_(budget), max_live_(max_live) {
-    builder_eng_.reset(new Engine(e.device));
-    VX_CUDA(cudaSetDevice(e.device));  // the builder engine's constructor made it current too
-    builder_ = std::thread([this] { builder_loop(); });
+    for (int w = 0; w < kWorkers; w++) worker_eng_.emplace_back(new Engine(e.device));
+    VX_CUDA(cudaSetDevice(e.device));  // the worker engines' constructors made it current too
+    for (int w = 0; w < kWorkers; w++) workers_.emplace_back([this, w] { worker_loop(worker_eng_[w].get()); });
 }
 
 Server::~Server() {
@@ -59,13 +60,17 @@ Server::~Server() {
         stop_ = true;
     }
     cv_.notify_all();
-    if (builder_.joinable()) builder_.join();
-    built_.clear();  // runs built but never bound
+    for (auto &t : workers_)
+        if (t.joinable()) t.join();
+    // runs still queued for a regrid point at the loop's engine; finished ones were handed
+    // back to it: all go before the worker engines
+    todo_.clear();
+    built_.clear();
     for (auto &kv : reqs_) kv.second.run.reset();
 }
 
-void Server::builder_loop() {
-    cudaSetDevice(builder_eng_->device);
+void Server::worker_loop(Engine *weng) {
+    cudaSetDevice(weng->device);
     for (;;) {
         Build b;
         {
@@ -76,13 +81,23 @@ void Server::builder_loop() {
             todo_.pop_front();
         }
         try {
-            b.run.reset(new Run(*builder_eng_, std::make_shared<LaserSlab>(b.params), b.precision));
-            b.run->poisson = b.poisson;
-            b.run->fast64 = b.fast64;
-            b.run->init();
-            b.run->migrate(eng);  // drops the builder engine's sets; the loop's engine runs it from now on
+            if (b.regrid) {
+                // the loop synchronised the solve's last step and dropped its launch sets:
+                // SolverManager::reGrid on this thread's streams while the batch steps on
+                b.run->adopt(*weng);
+                b.run->regrid(false);
+                weng->sync();
+            } else {
+                b.run.reset(new Run(*weng, std::make_shared<LaserSlab>(b.params), b.precision));
+                b.run->poisson = b.poisson;
+                b.run->fast64 = b.fast64;
+                b.run->init();
+            }
+            b.run->migrate(eng);  // drops this engine's sets; the loop's engine runs it from now on
         } catch (const std::exception &e) {
-            b.run.reset();
+            cudaStreamSynchronize(weng->stream);
+            if (b.regrid) b.run->migrate(eng);  // the loop retires it as failed
+            else b.run.reset();
             b.error = e.what();
         }
         {
@@ -121,7 +136,7 @@ int Server::waiting() const { return (int)waiting_.size() + building_; }
 
 void Server::admit(double now) {
     std::vector<Build> go;
-    while (!waiting_.empty() && (int)live_.size() + building_ + (int)go.size() < max_live_) {
+    while (!waiting_.empty() && (int)live_.size() + regridding_ + building_ + (int)go.size() < max_live_) {
         Request &r = reqs_.at(waiting_.front());
         if (used_ + r.estimate > budget_) break;  // in order: the head blocks the queue
         waiting_.pop_front();
@@ -151,9 +166,30 @@ void Server::bind_built(double now) {
         std::lock_guard<std::mutex> lk(mu_);
         done.swap(built_);
     }
+    if (done.empty()) return;
     for (auto &b : done) {
-        building_--;
         Request &r = reqs_.at(b.id);
+        if (b.regrid) {
+            regridding_--;
+            r.out = false;
+            const size_t bytes = b.run->device_bytes();
+            used_ += bytes - r.bytes;
+            r.bytes = bytes;
+            if (r.status == kCancelled) {  // withdrawn while regridding
+                used_ -= r.bytes;
+                continue;
+            }
+            r.run = std::move(b.run);
+            if (!b.error.empty()) {
+                r.error = "regrid failed: " + b.error;
+                retire(r, kFailed, clock());
+                continue;
+            }
+            r.regrids++;
+            live_.push_back(r.id);
+            continue;
+        }
+        building_--;
         used_ -= r.estimate;
         if (r.status == kCancelled) continue;  // withdrawn while building: the run goes
         if (!b.run) {
@@ -170,6 +206,7 @@ void Server::bind_built(double now) {
         r.status = kLive;
         live_.push_back(r.id);
     }
+    std::sort(live_.begin(), live_.end());  // arrival order, whatever came back when
 }
 
 void Server::retire(Request &r, Status st, double now) {
@@ -201,6 +238,12 @@ void Server::cancel(int64_t id) {
             r.finish = clock();
             break;
         case kLive:
+            if (r.out) {  // bind_built drops the run when its regrid ends
+                r.status = kCancelled;
+                r.finish = clock();
+                finished_order_.push_back(id);
+                break;
+            }
             eng.sync();
             live_.erase(std::find(live_.begin(), live_.end(), id));
             retire(r, kCancelled, clock());
@@ -213,15 +256,15 @@ void Server::cancel(int64_t id) {
 int Server::step(double now) {
     bind_built(now);
     admit(now);
-    if (live_.empty() && building_ > 0) {
-        // nothing to step: wait (a little) for a build to end rather than spin
+    if (live_.empty() && building_ + regridding_ > 0) {
+        // nothing to step: wait (a little) for a build or a regrid to end rather than spin
         {
             std::unique_lock<std::mutex> lk(mu_);
             built_cv_.wait_for(lk, std::chrono::milliseconds(50), [&] { return !built_.empty(); });
         }
         bind_built(clock());
     }
-    if (live_.empty()) return 0;
+    if (live_.empty()) return regridding_;
     std::vector<Run *> set;
     for (int64_t id : live_) set.push_back(reqs_.at(id).run.get());
     // one launch set per precision and Poisson solver (different kernels); the sets of
@@ -252,6 +295,7 @@ int Server::step(double now) {
     for (size_t k = 0; k < set.size(); k++) ex0_of[set[k]] = ex0[k];
     const double tnow = clock();
     std::vector<int64_t> still;
+    std::vector<Build> regrids;
     for (int64_t id : live_) {
         Request &r = reqs_.at(id);
         Run *run = r.run.get();
@@ -269,19 +313,35 @@ int Server::step(double now) {
             continue;
         }
         // the reference driver's regrid rule, with the time before the step (veritas.cpp:146-151)
+        // The regrid runs on a worker thread while the others step on; the solve sits out
+        // of the batch until it is back, so its own sequence (step, regrid, step) and bits
+        // are those of a plain run.
         if (r.regrid && regrid_enabled && run->S->maxDepth > 0) {
             if (r.regrid_counter > 20 && t_before[run] > regrid_after) {
-                run->regrid(false);
-                r.regrids++;
                 r.regrid_counter = 0;
-            } else {
-                r.regrid_counter++;
+                eng.forget(run);  // the step is synchronised above
+                Build b;
+                b.id = id;
+                b.regrid = true;
+                b.run = std::move(r.run);
+                r.out = true;
+                regridding_++;
+                regrids.push_back(std::move(b));
+                continue;
             }
+            r.regrid_counter++;
         }
         still.push_back(id);
     }
     live_ = still;
-    return (int)live_.size();
+    if (!regrids.empty()) {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            for (auto it = regrids.rbegin(); it != regrids.rend(); ++it) todo_.push_front(std::move(*it));
+        }
+        cv_.notify_all();
+    }
+    return (int)live_.size() + regridding_;
 }
 
 const Server::Request &Server::request(int64_t id) const {

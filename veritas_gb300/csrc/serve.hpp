@@ -27,6 +27,7 @@ public:
         int64_t steps = 0, done_steps = 0;
         int regrid_counter = 0;
         int regrids = 0;
+        bool out = false;  // live, its run with a worker thread for a regrid
         double arrival = 0, admitted = -1, bound = -1, finish = -1, sim_time = 0;
         size_t estimate = 0, bytes = 0;
         long long cells = 0;
@@ -52,7 +53,8 @@ public:
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0_).count();
     }
     size_t used_bytes() const { return used_; }
-    int live() const { return (int)live_.size(); }
+    // Live solves, those out for a regrid included.
+    int live() const { return (int)live_.size() + regridding_; }
     // Requests not yet live: waiting for memory, or admitted and being built.
     int waiting() const;
     static size_t estimate_bytes(const LaserSlabParams &p, int precision);
@@ -64,35 +66,39 @@ public:
     bool regrid_enabled = true;
 
 private:
-    struct Build {  // one admitted request on its way through the builder thread
+    // One job of a worker thread: an admitted request's run to build, or a live solve's
+    // run to regrid (it sits out of the batch meanwhile).
+    struct Build {
         int64_t id;
+        bool regrid = false;
         LaserSlabParams params;
         int precision, poisson, fast64;
         std::unique_ptr<Run> run;
         std::string error;
     };
+    static constexpr int kWorkers = 4;
     void admit(double now);
     void bind_built(double now);
     void retire(Request &r, Status st, double now);
-    void builder_loop();
+    void worker_loop(Engine *weng);
     Engine &eng;
-    std::unique_ptr<Engine> builder_eng_;  // the builder thread's engine (own streams, same device)
+    std::vector<std::unique_ptr<Engine>> worker_eng_;  // one per worker thread (own streams, same device)
     size_t budget_, used_ = 0;
     int max_live_;
     int64_t next_id_ = 1;
     std::map<int64_t, Request> reqs_;
     std::deque<int64_t> waiting_;
     std::vector<int64_t> live_;
-    int building_ = 0;
+    int building_ = 0, regridding_ = 0;
     std::vector<int64_t> finished_order_;
     std::chrono::steady_clock::time_point t0_ = std::chrono::steady_clock::now();
-    // builder thread: admitted requests in, built runs out
+    // worker threads: builds and regrids in (regrids first), finished runs out
     std::mutex mu_;
     std::condition_variable cv_, built_cv_;
     std::deque<Build> todo_;
     std::vector<Build> built_;
     bool stop_ = false;
-    std::thread builder_;
+    std::vector<std::thread> workers_;
 };
 
 }  // namespace vx
