@@ -117,25 +117,42 @@ __device__ __forceinline__ void rebase(CSyncOp &op, int b) {
     op.nb += b;
     op.caller += b;
 }
+// Blocks (segment, part): part y of gridDim.y copies every gridDim.y-th stretch of 256 ops,
+// so that a long segment is not left to one block.
 template <class Op>
 __global__ void k_merge_ops(const OpSegment *segs, Op *dst) {
     VX_PDL_WAIT();
     const OpSegment sg = segs[blockIdx.x];
     const Op *src = (const Op *)sg.src;
-    for (int k = threadIdx.x; k < sg.count; k += blockDim.x) {
+    for (int k = blockIdx.y * blockDim.x + threadIdx.x; k < sg.count; k += gridDim.y * blockDim.x) {
         Op op = src[k];
         rebase(op, sg.base);
         dst[sg.dst_off + k] = op;
     }
 }
+constexpr int kMergeParts = 8;
 void merge_ghost_ops(const OpSegment *segs, int nseg, GhostOp *dst, cudaStream_t s) {
-    if (nseg > 0) vx_launch(k_merge_ops<GhostOp>, nseg, 256, 0, s, segs, dst);
+    if (nseg > 0) vx_launch_plain(k_merge_ops<GhostOp>, dim3(nseg, kMergeParts), 256, 0, s, segs, dst);
 }
 void merge_iface_ops(const OpSegment *segs, int nseg, IfaceOp *dst, cudaStream_t s) {
-    if (nseg > 0) vx_launch(k_merge_ops<IfaceOp>, nseg, 256, 0, s, segs, dst);
+    if (nseg > 0) vx_launch_plain(k_merge_ops<IfaceOp>, dim3(nseg, kMergeParts), 256, 0, s, segs, dst);
 }
 void merge_csync_ops(const OpSegment *segs, int nseg, CSyncOp *dst, cudaStream_t s) {
-    if (nseg > 0) vx_launch(k_merge_ops<CSyncOp>, nseg, 256, 0, s, segs, dst);
+    if (nseg > 0) vx_launch_plain(k_merge_ops<CSyncOp>, dim3(nseg, kMergeParts), 256, 0, s, segs, dst);
+}
+
+// Host tables to the device through the SMs: page-locked host memory read over the
+// host link, so the copy does not queue on a copy engine behind other threads' transfers.
+__global__ void k_copy_from_host(const uint4 *src, uint4 *dst, size_t n16) {
+    VX_PDL_WAIT();
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+void copy_from_host(const void *src_dev, void *dst, size_t bytes, cudaStream_t s) {
+    const size_t n16 = bytes / 16;
+    if (n16 == 0) return;
+    const int blocks = (int)std::min<size_t>((n16 + 255) / 256, 1024);
+    vx_launch_plain(k_copy_from_host, blocks, 256, 0, s, (const uint4 *)src_dev, (uint4 *)dst, n16);
 }
 
 void launch_ghost(const void *patches, const GhostOp *ops, int n, int slot, int prec, cudaStream_t s) {

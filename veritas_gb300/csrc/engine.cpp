@@ -31,17 +31,35 @@ DevBuf::DevBuf(size_t b, Uninit) : bytes(b) {
     if (b) VX_CUDA(cudaMalloc(&p, b));
 }
 DevBuf::~DevBuf() {
-    if (p) cudaFree(p);
+    if (p && own) cudaFree(p);
 }
 DevBuf &DevBuf::operator=(DevBuf &&o) noexcept {
     if (this != &o) {
-        if (p) cudaFree(p);
+        if (p && own) cudaFree(p);
         p = o.p;
         bytes = o.bytes;
+        own = o.own;
         o.p = nullptr;
         o.bytes = 0;
     }
     return *this;
+}
+
+void TablePack::place(const DevBuf &arena) {
+    if (arena.bytes < bytes()) throw std::logic_error("table storage smaller than its tables");
+    base_ = arena.as<char>();
+    for (const Item &it : items_)
+        *it.view = DevBuf::view(base_ + (it.staged ? it.off : host_.size() + it.off), it.bytes);
+}
+
+void TablePack::copy(cudaStream_t s, void *pinned_host, void *pinned_dev) {
+    if (host_.empty()) return;
+    if (pinned_host && pinned_dev) {
+        std::memcpy(pinned_host, host_.data(), host_.size());
+        copy_from_host(pinned_dev, base_, host_.size(), s);  // host_.size() is a multiple of 256
+    } else {
+        VX_CUDA(cudaMemcpyAsync(base_, host_.data(), host_.size(), cudaMemcpyHostToDevice, s));
+    }
 }
 
 // ---------------------------------------------------------------- Run
@@ -485,6 +503,7 @@ Engine::Engine(int dev) : device(dev) {
     VX_CUDA(cudaSetDevice(dev));
     VX_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     VX_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    VX_CUDA(cudaEventCreateWithFlags(&ev_pinned_, cudaEventDisableTiming));
     VX_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     VX_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     VX_CUDA(cudaEventCreateWithFlags(&ev_gamma, cudaEventDisableTiming));
@@ -497,12 +516,15 @@ Engine::Engine(int dev) : device(dev) {
 
 Engine::~Engine() {
     sets_.clear();
+    arena_cache_.clear();
+    if (pinned_) cudaFreeHost(pinned_);
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     if (ev_gamma) cudaEventDestroy(ev_gamma);
     if (ev_mx) cudaEventDestroy(ev_mx);
+    if (ev_pinned_) cudaEventDestroy(ev_pinned_);
     if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
 }
@@ -740,12 +762,58 @@ void Engine::sync() {
     check_device_errors();
 }
 
+DevBuf Engine::take_arena(size_t bytes) {
+    // a cached block of at least `bytes` and at most twice that (plus 1 MiB)
+    auto it = arena_cache_.lower_bound(bytes);
+    if (it != arena_cache_.end() && it->first <= 2 * bytes + ((size_t)1 << 20)) {
+        DevBuf b = std::move(it->second);
+        arena_cache_bytes_ -= it->first;
+        arena_cache_.erase(it);
+        return b;
+    }
+    // new storage rounded up (1/8 and to 256 KiB) so that later sets of a similar mix fit
+    const size_t cap = (bytes + bytes / 8 + ((size_t)256 << 10) - 1) / ((size_t)256 << 10) * ((size_t)256 << 10);
+    return DevBuf(cap, DevBuf::Uninit{});
+}
+
+void *Engine::pinned_staging(size_t bytes) {
+    if (bytes > pinned_bytes_) {
+        if (pinned_) cudaFreeHost(pinned_);
+        pinned_ = pinned_dev_ = nullptr;
+        pinned_bytes_ = 0;
+        const size_t cap = std::max(bytes + bytes / 2, (size_t)4 << 20);
+        VX_CUDA(cudaHostAlloc(&pinned_, cap, cudaHostAllocMapped));
+        VX_CUDA(cudaHostGetDevicePointer(&pinned_dev_, pinned_, 0));
+        pinned_bytes_ = cap;
+    }
+    return pinned_;
+}
+
+void Engine::drop_idle(std::unique_ptr<LaunchSet> &L) {
+    DevBuf a = std::move(L->arena);
+    L.reset();
+    if (!a.p || !a.own) return;
+    if (a.bytes > kArenaCacheBytes) return;  // freed
+    while (arena_cache_bytes_ + a.bytes > kArenaCacheBytes && !arena_cache_.empty()) {
+        auto it = arena_cache_.begin();  // the smallest goes first
+        arena_cache_bytes_ -= it->first;
+        arena_cache_.erase(it);
+    }
+    arena_cache_bytes_ += a.bytes;
+    const size_t cap = a.bytes;
+    arena_cache_.emplace(cap, std::move(a));
+}
+
 // Drop every cached launch set that refers to a run being destroyed.
 void Engine::forget(Run *r) {
     cudaStreamSynchronize(stream);
     for (auto it = sets_.begin(); it != sets_.end();) {
-        if (std::find(it->first.begin(), it->first.end(), r) != it->first.end()) it = sets_.erase(it);
-        else ++it;
+        if (std::find(it->first.begin(), it->first.end(), r) != it->first.end()) {
+            drop_idle(it->second);
+            it = sets_.erase(it);
+        } else {
+            ++it;
+        }
     }
 }
 
@@ -767,24 +835,31 @@ void Engine::retain_sets(const std::vector<std::vector<Run *>> &keep) {
     if (!drop) return;
     sync();  // a dropped set's buffers may still be in use by queued work
     for (auto it = sets_.begin(); it != sets_.end();) {
-        if (std::find(keep.begin(), keep.end(), it->first) == keep.end()) it = sets_.erase(it);
-        else ++it;
+        if (std::find(keep.begin(), keep.end(), it->first) == keep.end()) {
+            drop_idle(it->second);  // synchronised above
+            it = sets_.erase(it);
+        } else {
+            ++it;
+        }
     }
 }
 
-LaunchSet &Engine::get_set(const std::vector<Run *> &set) {
+LaunchSet &Engine::get_set(const std::vector<Run *> &set, bool defer) {
     auto it = sets_.find(set);
     uint64_t ver = 0;
     for (Run *r : set) ver = ver * 1000003ull + r->layout_version;
-    if (it != sets_.end() && it->second->key_version == ver) return *it->second;
+    if (it != sets_.end() && it->second->key_version == ver) {
+        if (!defer) flush_set(*it->second);
+        return *it->second;
+    }
     auto L = std::make_unique<LaunchSet>();
     L->runs = set;
     L->key_version = ver;
     static const bool trace = std::getenv("VX_TRACE_INIT") != nullptr;
     const auto t0 = std::chrono::steady_clock::now();
     build_set(*L);
+    if (!defer) flush_set(*L);
     if (trace) {
-        sync();
         std::fprintf(stderr, "vx launch set of %zu runs: %8.2f ms\n", set.size(),
                      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
     }
@@ -794,7 +869,9 @@ LaunchSet &Engine::get_set(const std::vector<Run *> &set) {
 }
 
 // Tile list covering every patch's padded block with tile_j (p) x tile_i (x) tiles.
-void Engine::build_tiles(LaunchSet &L) {
+void Engine::build_tiles(LaunchSet &L, TablePack *pk) {
+    TablePack alone;
+    TablePack &P = pk ? *pk : alone;
     // FP32 streaming kernels own four p cells per thread: 128-cell tiles starting at
     // j0 = -2 + 128 k keep every thread's cells one aligned float4
     if (L.precision == kF32) L.tile_j = 128;
@@ -809,7 +886,7 @@ void Engine::build_tiles(LaunchSet &L) {
                     pi++;
                 }
     L.ntiles = (int)tiles.size();
-    L.dtiles = upload(tiles, stream);
+    P.put(L.dtiles, tiles);
     if (L.precision == kF32) {  // strip tiles of the fused face + flux kernels
         std::vector<TileRef> xt, pt;
         pi = 0;
@@ -825,18 +902,33 @@ void Engine::build_tiles(LaunchSet &L) {
                     }
         L.nxtiles = (int)xt.size();
         L.nptiles = (int)pt.size();
-        L.dxtiles = upload(xt, stream);
-        L.dptiles = upload(pt, stream);
+        P.put(L.dxtiles, xt);
+        P.put(L.dptiles, pt);
+    }
+    if (!pk) {  // rebuilt alone (the autotuner's trial shapes)
+        L.tile_arena = DevBuf(alone.bytes(), DevBuf::Uninit{});
+        alone.place(L.tile_arena);
+        alone.copy(stream);
     }
 }
 
+// The set's host tables are packed into one allocation and copied, and its op tables
+// gathered from the runs' own lists, by kernels queued on `stream`: ordered after the
+// work already there (which may still be writing the runs' lists) and before any use, and
+// never waited for on the host — a serving loop builds the next step's set while the
+// current step runs.
+// The set's host tables are packed into one allocation; flush_set then copies them and
+// gathers its op tables from the runs' own lists, by kernels queued on `stream` — after
+// the work already there (which may still be writing the runs' lists) and before any use.
+// A serving loop builds the next step's set on the host while the current step runs and
+// queues the copies once it is done (a launch queued behind a running step's graph holds
+// the host up).
 void Engine::build_set(LaunchSet &L) {
-    // VX_TRACE_INIT=1: wall time of each phase on stderr
+    // VX_TRACE_INIT=1: host time of each phase on stderr
     static const bool trace = std::getenv("VX_TRACE_INIT") != nullptr;
     auto t0 = std::chrono::steady_clock::now();
     auto lap = [&](const char *what) {
         if (!trace) return;
-        sync();
         auto t1 = std::chrono::steady_clock::now();
         std::fprintf(stderr, "vx set %-12s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(t1 - t0).count());
         t0 = t1;
@@ -854,9 +946,11 @@ void Engine::build_set(LaunchSet &L) {
         if (R->fast64 != L.fast64)
             throw std::invalid_argument("runs advanced together must share one FP64 kernel form");
     }
+    L.pending_pack.reset(new TablePack);  // every table below: one allocation, one copy
+    TablePack &pk = *L.pending_pack;
     std::vector<PoissonFastDev> pfs;
     for (Run *R : L.runs) pfs.push_back(R->pfdev);
-    L.dpf = upload(pfs, stream);
+    pk.put(L.dpf, pfs);
     std::vector<int> colpatch, colidx, lvl_ptr, lvl_off, lvl_patch, run_n, run_ns, run_nl;
     std::vector<RunFields> fields;
     std::vector<LUDev> lus;
@@ -927,7 +1021,12 @@ void Engine::build_set(LaunchSet &L) {
     // AMR op tables: batch b of the set = batch b of every run, patch ids made global.
     // Each run's sorted lists already sit on the device; the set's tables are gathered
     // there, one segment per (batch, run), so a new set costs no host-side op copies.
+    // The segment lists go into the pack; the gathers run once it is on the device.
+    std::vector<std::function<void()>> &gathers = L.pending_gathers;
+    gathers.clear();
+    DevBuf *dsegs = L.dsegs;
     {
+        int which = 0;
         auto gather = [&](auto dummy, auto table_of, auto ptr_of, auto merge, DevBuf &out, std::vector<int> &optr) {
             using Op = decltype(dummy);
             size_t nb = 0;
@@ -948,11 +1047,12 @@ void Engine::build_set(LaunchSet &L) {
                 }
                 optr.push_back((int)total);
             }
-            out = DevBuf((size_t)std::max<long long>(total, 1) * sizeof(Op));
-            if (!segs.empty()) {
-                DevBuf dsegs = upload(segs, stream);
-                merge(dsegs.as<OpSegment>(), (int)segs.size(), out.as<Op>(), stream);
-                sync();  // dsegs is released at the end of this scope
+            pk.reserve(out, (size_t)std::max<long long>(total, 1) * sizeof(Op));
+            DevBuf &ds = dsegs[which++];
+            const int nseg = (int)segs.size();
+            if (nseg) {
+                pk.put(ds, segs);
+                gathers.push_back([&ds, &out, nseg, merge, this] { merge(ds.as<OpSegment>(), nseg, out.as<Op>(), stream); });
             }
         };
         gather(GhostOp{}, [](Run &R) -> DevBuf & { return R.dghost_ops; },
@@ -967,9 +1067,9 @@ void Engine::build_set(LaunchSet &L) {
         L.max_batch = 0;
         for (const std::vector<int> *p : {&L.ghost_ptr, &L.iface_ptr, &L.csync_ptr})
             for (size_t b = 0; b + 1 < p->size(); b++) L.max_batch = std::max(L.max_batch, (*p)[b + 1] - (*p)[b]);
-        L.dghost_ptr = upload(L.ghost_ptr, stream);
-        L.diface_ptr = upload(L.iface_ptr, stream);
-        L.dcsync_ptr = upload(L.csync_ptr, stream);
+        pk.put(L.dghost_ptr, L.ghost_ptr);
+        pk.put(L.diface_ptr, L.iface_ptr);
+        pk.put(L.dcsync_ptr, L.csync_ptr);
     }
     lap("op tables");
     // Moment work units (FP64: blocks of kMomCols columns of one patch; FP32: one column
@@ -1008,38 +1108,57 @@ void Engine::build_set(LaunchSet &L) {
         colidx.swap(ci2);
     }
     L.ncols = (int)colpatch.size();
-    build_pipe_tables(L, colpatch, colidx);
+    build_pipe_tables(L, colpatch, colidx, pk);
     lap("units");
     // lvl_ptr is absolute; lvl_off points at each run's block.
-    L.dpatch = upload(L.hpatch, stream);
-    build_tiles(L);
+    pk.put(L.dpatch, L.hpatch);
+    build_tiles(L, &pk);
     lap("tiles");
-    L.dfields = upload(fields, stream);
-    L.dcolpatch = upload(colpatch, stream);
-    L.dcolidx = upload(colidx, stream);
-    L.dlvl_ptr = upload(lvl_ptr, stream);
-    L.dlvl_off = upload(lvl_off, stream);
-    L.dlvl_patch = upload(lvl_patch, stream);
-    L.drun_n = upload(run_n, stream);
-    L.drun_ns = upload(run_ns, stream);
-    L.drun_nl = upload(run_nl, stream);
-    L.dlu = upload(lus, stream);
-    L.dw = upload(L.w, stream);
-    L.dfcoef = upload(L.fcoef, stream);
-    L.ddxinv = upload(dxinv, stream);
-    L.dcfl_spec = upload(spec, stream);
-    L.dns = upload(run_ns, stream);
-    L.dcfl_out = DevBuf(L.runs.size() * sizeof(double));
+    pk.put(L.dfields, fields);
+    pk.put(L.dcolpatch, colpatch);
+    pk.put(L.dcolidx, colidx);
+    pk.put(L.dlvl_ptr, lvl_ptr);
+    pk.put(L.dlvl_off, lvl_off);
+    pk.put(L.dlvl_patch, lvl_patch);
+    pk.put(L.drun_n, run_n);
+    pk.put(L.drun_ns, run_ns);
+    pk.put(L.drun_nl, run_nl);
+    pk.put(L.dlu, lus);
+    pk.put(L.dw, L.w);
+    pk.put(L.dfcoef, L.fcoef);
+    pk.put(L.ddxinv, dxinv);
+    pk.put(L.dcfl_spec, spec);
+    pk.put(L.dns, run_ns);
+    pk.put(L.dcfl_out, std::vector<double>(L.runs.size(), 0.0));
     L.hparams.assign(L.runs.size() * 6 * kParamStride, 0.0);
-    L.dparams = DevBuf(L.hparams.size() * sizeof(double));
+    pk.put(L.dparams, L.hparams);
     L.hparams32.assign(L.hparams.size(), 0.0f);
-    L.dparams32 = DevBuf(L.hparams32.size() * sizeof(float));
+    pk.put(L.dparams32, L.hparams32);
+    lap("tables");
+    L.arena = take_arena(pk.bytes());
+    pk.place(L.arena);  // the views are final: a graph can be captured from here on
     if (L.graph) {
         cudaGraphExecDestroy(L.graph);
         L.graph = nullptr;
     }
-    sync();
-    lap("uploads");
+    lap("arena");
+}
+
+// The set's table copy and op gathers, queued on `stream` (once).
+void Engine::flush_set(LaunchSet &L) {
+    if (!L.pending_pack) return;
+    // the staging is reused once the previous set's copy has run
+    VX_CUDA(cudaEventSynchronize(ev_pinned_));
+    TablePack &pk = *L.pending_pack;
+    pk.copy(stream, pinned_staging(pk.staged_bytes()), pinned_dev_);
+    VX_CUDA(cudaEventRecord(ev_pinned_, stream));
+    for (auto &g : L.pending_gathers) g();
+    L.pending_gathers.clear();
+    L.pending_pack.reset();
+}
+
+void Engine::flush_prepared() {
+    for (auto &kv : sets_) flush_set(*kv.second);
 }
 
 // Tables of the pipelined moments + solve launch (k64_moments_poisson) for an FP64 set
@@ -1048,7 +1167,8 @@ void Engine::build_set(LaunchSet &L) {
 // whose right-hand side the chunk reads first.  A unit covers finest x positions
 // [(x_pos * rtb) + c, ... + rtb) for each of its columns c = i * rtb; row k's right-hand
 // side comes from position perm[k].
-void Engine::build_pipe_tables(LaunchSet &L, const std::vector<int> &colpatch, const std::vector<int> &colidx) {
+void Engine::build_pipe_tables(LaunchSet &L, const std::vector<int> &colpatch, const std::vector<int> &colidx,
+                               TablePack &pk) {
     L.pipe = false;
     if (L.precision != kF64 || L.poisson != kPoissonLU || L.runs.empty() || (int)L.runs.size() > kPipeMaxRuns) return;
     for (Run *R : L.runs)
@@ -1121,17 +1241,17 @@ void Engine::build_pipe_tables(LaunchSet &L, const std::vector<int> &colpatch, c
     L.pipe_nunits = nunits;
     L.pipe_nitems = nitems;
     L.pipe_ndone = (int)need.size();
-    L.dpipe_col0 = upload(col0, stream);
-    L.dpipe_sig = upload(sig, stream);
-    L.dpipe_item0 = upload(item0, stream);
-    L.dpipe_nwin = upload(nwin, stream);
-    L.dpipe_c12 = upload(c12, stream);
-    L.dpipe_items = upload(item_unit, stream);
-    L.dpipe_need = upload(need, stream);
-    L.dpipe_runctr = upload(run_ctr, stream);
-    L.dpipe_rungptr = upload(run_gptr, stream);
-    L.dpipe_gptr = upload(gptr, stream);
-    L.dpipe_grow = upload(grow, stream);
+    pk.put(L.dpipe_col0, col0);
+    pk.put(L.dpipe_sig, sig);
+    pk.put(L.dpipe_item0, item0);
+    pk.put(L.dpipe_nwin, nwin);
+    pk.put(L.dpipe_c12, c12);
+    pk.put(L.dpipe_items, item_unit);
+    pk.put(L.dpipe_need, need);
+    pk.put(L.dpipe_runctr, run_ctr);
+    pk.put(L.dpipe_rungptr, run_gptr);
+    pk.put(L.dpipe_gptr, gptr);
+    pk.put(L.dpipe_grow, grow);
     L.dpipe_scratch = DevBuf((size_t)nitems * kPipeItemDoubles * sizeof(double));
     L.dpipe_state = DevBuf((size_t)(kPipeDone + L.pipe_ndone + 2 * nunits) * sizeof(unsigned));  // zeroed
     // summing warps, four per block: each unit's sums take about 64 cycles per FP64 add on
@@ -1656,23 +1776,36 @@ void Engine::run_phases(Run &run, int s, double dt, unsigned phases) {
     VX_CUDA(cudaGetLastError());
 }
 
+// The step of a set as one CUDA graph (its kernels read dt and the stage weights from the
+// set's parameter block, so the graph serves every step).  Capturing only records: work
+// already queued on the stream keeps running meanwhile.
+void Engine::capture_graph(LaunchSet &L) {
+    if (L.graph) return;
+    static const bool trace = std::getenv("VX_TRACE_INIT") != nullptr;
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaGraph_t g;
+    VX_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    record_step(L);
+    VX_CUDA(cudaStreamEndCapture(stream, &g));
+    const auto t1 = std::chrono::steady_clock::now();
+    VX_CUDA(cudaGraphInstantiate(&L.graph, g, 0));
+    cudaGraphDestroy(g);
+    if (trace)
+        std::fprintf(stderr, "vx set capture      %8.2f ms (instantiate %.2f ms)\n",
+                     std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(),
+                     std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count());
+}
+
+void Engine::prepare(const std::vector<Run *> &set) { get_set(set, true); }
+
 void Engine::advance(const std::vector<Run *> &set, const std::vector<double> &dt) {
     LaunchSet &L = get_set(set);
     fill_params(L, set, dt);
-    if (use_graphs) {
-        if (!L.graph) {
-            static const bool trace = std::getenv("VX_TRACE_INIT") != nullptr;
-            const auto t0 = std::chrono::steady_clock::now();
-            cudaGraph_t g;
-            VX_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-            record_step(L);
-            VX_CUDA(cudaStreamEndCapture(stream, &g));
-            VX_CUDA(cudaGraphInstantiate(&L.graph, g, 0));
-            cudaGraphDestroy(g);
-            if (trace)
-                std::fprintf(stderr, "vx set capture      %8.2f ms\n",
-                             std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
-        }
+    // A set's first step is launched kernel by kernel, its graph captured from its second
+    // on: a serving loop's mix changes almost every step, and capturing and instantiating
+    // a graph for one step costs more than the launches it saves.
+    if (use_graphs && L.steps++ > 0) {
+        capture_graph(L);
         VX_CUDA(cudaGraphLaunch(L.graph, stream));
     } else {
         record_step(L);

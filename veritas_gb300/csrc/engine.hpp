@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstring>
 #include <fstream>
 #include <functional>
 #include <map>
@@ -34,14 +35,22 @@ void cuda_check(cudaError_t e, const char *what);
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
+    bool own = true;  // false: a view into storage another DevBuf owns
     DevBuf() = default;
     explicit DevBuf(size_t b);  // zero-filled
     struct Uninit {};
     DevBuf(size_t b, Uninit);   // contents undefined: for buffers the caller fills at once
+    static DevBuf view(void *p, size_t b) {
+        DevBuf d;
+        d.p = p;
+        d.bytes = b;
+        d.own = false;
+        return d;
+    }
     ~DevBuf();
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
-    DevBuf(DevBuf &&o) noexcept : p(o.p), bytes(o.bytes) {
+    DevBuf(DevBuf &&o) noexcept : p(o.p), bytes(o.bytes), own(o.own) {
         o.p = nullptr;
         o.bytes = 0;
     }
@@ -60,6 +69,51 @@ DevBuf upload(const std::vector<T> &v, cudaStream_t s) {
     VX_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
     return b;
 }
+
+// Device tables packed into one allocation: host tables are staged back to back
+// (256-byte aligned) and copied in one transfer, device-only regions reserved beside
+// them; the DevBufs handed in become views of the allocation once allocate() has run.  A
+// launch set's two dozen tables then cost one allocation and one copy instead of two
+// dozen of each (and one free when the set goes).
+class TablePack {
+public:
+    template <class T>
+    void put(DevBuf &view, const std::vector<T> &v) {
+        const size_t b = std::max<size_t>(v.size(), 1) * sizeof(T);
+        const size_t off = host_.size();
+        host_.resize(off + align(b), 0);  // an empty table: one zero element, as upload() gives
+        if (!v.empty()) std::memcpy(host_.data() + off, v.data(), v.size() * sizeof(T));
+        items_.push_back({&view, off, b, true});
+    }
+    // device-only region, contents undefined until a kernel writes it
+    void reserve(DevBuf &view, size_t bytes) {
+        bytes = std::max<size_t>(bytes, 1);
+        items_.push_back({&view, dev_, bytes, false});
+        dev_ += align(bytes);
+    }
+    // Bytes the tables take in one allocation.
+    size_t bytes() const { return host_.size() + dev_; }
+    // Points the views into `arena` (at least bytes() long); copy() then moves the staged
+    // tables on `s` — when given page-locked staging (host and device addresses, at least
+    // staged_bytes() long, not reused before `s` has run the copy), by a kernel reading it:
+    // a transfer from pageable memory, or any copy-engine transfer, queues behind the
+    // large uploads of other threads building runs.
+    void place(const DevBuf &arena);
+    size_t staged_bytes() const { return host_.size(); }
+    void copy(cudaStream_t s, void *pinned_host = nullptr, void *pinned_dev = nullptr);
+
+private:
+    static size_t align(size_t b) { return (b + 255) / 256 * 256; }
+    struct Item {
+        DevBuf *view;
+        size_t off, bytes;
+        bool staged;
+    };
+    std::vector<char> host_;
+    std::vector<Item> items_;
+    size_t dev_ = 0;
+    char *base_ = nullptr;
+};
 
 // Geometry of one Rectangle (Rectangle.hpp:20-23) plus its device storage.
 struct Rect {
@@ -230,7 +284,14 @@ struct LaunchSet {
     int pipe_nunits = 0, pipe_nitems = 0, pipe_ndone = 0, pipe_summers = 1;
     DevBuf dpipe_col0, dpipe_sig, dpipe_item0, dpipe_nwin, dpipe_c12, dpipe_items, dpipe_need, dpipe_runctr,
         dpipe_rungptr, dpipe_gptr, dpipe_grow, dpipe_scratch, dpipe_state;
+    DevBuf arena, tile_arena;  // the storage of the tables above (TablePack), tiles rebuilt alone
+    // built but not yet on the device (Engine::flush_set): the staged tables, the op
+    // gathers, their segment lists
+    std::unique_ptr<TablePack> pending_pack;
+    std::vector<std::function<void()>> pending_gathers;
+    DevBuf dsegs[3];
     cudaGraphExec_t graph = nullptr;
+    int steps = 0;  // steps advanced with this set (its graph is captured at the second)
     ~LaunchSet();
 };
 
@@ -309,15 +370,42 @@ public:
     // Drops every cached launch set but the listed ones (their tables and graphs hold
     // device memory; a serving loop keeps only the sets of its current step).
     void retain_sets(const std::vector<std::vector<Run *>> &keep);
+    // Table storage of dropped launch sets, kept for the next sets (a serving loop builds
+    // one almost every step, and cudaMalloc beside running kernels and other threads'
+    // allocations costs milliseconds: a set's gathered op tables can take hundreds of MB);
+    // bounded by kArenaCacheBytes.
+    DevBuf take_arena(size_t bytes);
+    // Page-locked staging of at least `bytes` for the set tables' copy (grown as needed);
+    // its device address in pinned_dev_.
+    void *pinned_staging(size_t bytes);
+    static constexpr size_t kArenaCacheBytes = (size_t)2 << 30;
+    // Builds (or finds) the launch set of `set`, host work only: a serving loop prepares
+    // the next step's sets while the current step runs.  The sets' table copies are
+    // queued by flush_prepared() (or their first use).
+    void prepare(const std::vector<Run *> &set);
+    void flush_prepared();
     int tile_pref[2][2] = {{32, 8}, {128, 8}};  // [precision 64, 32] -> (tile_j, tile_i)
 
 private:
     std::map<std::vector<Run *>, std::unique_ptr<LaunchSet>> sets_;
-    LaunchSet &get_set(const std::vector<Run *> &set);
+    std::multimap<size_t, DevBuf> arena_cache_;  // idle table storage by size
+    void *pinned_ = nullptr, *pinned_dev_ = nullptr;
+    size_t pinned_bytes_ = 0;
+    cudaEvent_t ev_pinned_ = nullptr;  // after the last copy out of pinned_
+    size_t arena_cache_bytes_ = 0;
+    // Drops a launch set whose work has finished (the engine's stream synchronised): its
+    // table storage goes to the cache.
+    void drop_idle(std::unique_ptr<LaunchSet> &L);
+    // defer: the set's table copy and gathers wait for flush_set / flush_prepared
+    LaunchSet &get_set(const std::vector<Run *> &set, bool defer = false);
     void build_set(LaunchSet &L);
-    void build_tiles(LaunchSet &L);
-    void build_pipe_tables(LaunchSet &L, const std::vector<int> &colpatch, const std::vector<int> &colidx);
+    void flush_set(LaunchSet &L);
+    // pk: the set's table pack; none: the tiles are rebuilt alone (their own allocation)
+    void build_tiles(LaunchSet &L, TablePack *pk = nullptr);
+    void build_pipe_tables(LaunchSet &L, const std::vector<int> &colpatch, const std::vector<int> &colidx,
+                           TablePack &pk);
     void record_step(LaunchSet &L);
+    void capture_graph(LaunchSet &L);
     void record_step_persistent32(LaunchSet &L);
     StageLaunches stage_launches(LaunchSet &L);
     DevBuf gsync_;               // GridSyncState of the persistent kernels

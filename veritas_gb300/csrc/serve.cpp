@@ -1,13 +1,13 @@
 // Serving loop: continuous batching of independent solves on one context.
 //
-// Requests queue in arrival order.  Each call of step() first binds the runs the worker
-// threads have finished, then admits, in order, the waiting requests whose device-memory
-// estimate fits in what the budget has left and hands them to the workers, which
-// construct each run (host quadrature, clustering, Poisson factors, uploads) on their own
-// engines and streams while the loop keeps stepping; the estimate is replaced by the
-// run's real footprint when it is bound.  Then every live solve advances by one full RK
-// step in one batched launch set per precision (one launch per sub-step for all of
-// them), and each solve regrids by the reference driver's rule (veritas.cpp:146-151: a
+// Requests queue in arrival order.  Each call of step() advances every live solve by one
+// full RK step in one batched launch set per precision (one launch per sub-step for all
+// of them).  While that step runs on the GPU, the loop binds the runs the worker threads
+// have finished, admits, in order, the waiting requests whose device-memory estimate fits
+// in what the budget has left and hands them to the workers, which construct each run
+// (host quadrature, clustering, Poisson factors, uploads) on their own engines and
+// streams, and builds the launch sets of the next step's mix; the estimate is replaced by
+// the run's real footprint when it is bound.  After the step each solve regrids by the reference driver's rule (veritas.cpp:146-151: a
 // counter of steps since the last regrid; at a count above 20, once the plasma is on,
 // SolverManager::reGrid and the counter restarts) — on a worker thread, the solve out of
 // the batch until its new hierarchy is in place.  A solve whose CFL bound or
@@ -17,6 +17,8 @@
 // next admission.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 
 #include "serve.hpp"
 
@@ -67,6 +69,11 @@ Server::~Server() {
     todo_.clear();
     built_.clear();
     for (auto &kv : reqs_) kv.second.run.reset();
+    if (std::getenv("VX_TRACE_SERVE"))
+        std::fprintf(stderr,
+                     "vx serve loop [s]: idle bind %.3f, dt + launch %.3f, bind + admit %.3f, next sets %.3f, "
+                     "step wait %.3f, retire + regrid hand-off %.3f; next mix predicted %d, missed %d\n",
+                     phase_s_[0], phase_s_[1], phase_s_[2], phase_s_[3], phase_s_[4], phase_s_[5], hits_, misses_);
 }
 
 void Server::worker_loop(Engine *weng) {
@@ -134,9 +141,10 @@ int64_t Server::submit(const LaserSlabParams &p, int precision, int64_t steps, d
 
 int Server::waiting() const { return (int)waiting_.size() + building_; }
 
-void Server::admit(double now) {
+void Server::admit(double now, int bound_meanwhile) {
     std::vector<Build> go;
-    while (!waiting_.empty() && (int)live_.size() + regridding_ + building_ + (int)go.size() < max_live_) {
+    while (!waiting_.empty() &&
+           (int)live_.size() + bound_meanwhile + regridding_ + building_ + (int)go.size() < max_live_) {
         Request &r = reqs_.at(waiting_.front());
         if (used_ + r.estimate > budget_) break;  // in order: the head blocks the queue
         waiting_.pop_front();
@@ -160,7 +168,7 @@ void Server::admit(double now) {
     cv_.notify_one();
 }
 
-void Server::bind_built(double now) {
+void Server::bind_built(double now, std::vector<int64_t> &into) {
     std::vector<Build> done;
     {
         std::lock_guard<std::mutex> lk(mu_);
@@ -186,7 +194,7 @@ void Server::bind_built(double now) {
                 continue;
             }
             r.regrids++;
-            live_.push_back(r.id);
+            into.push_back(r.id);
             continue;
         }
         building_--;
@@ -204,9 +212,9 @@ void Server::bind_built(double now) {
         used_ += r.bytes;
         r.bound = now;
         r.status = kLive;
-        live_.push_back(r.id);
+        into.push_back(r.id);
     }
-    std::sort(live_.begin(), live_.end());  // arrival order, whatever came back when
+    std::sort(into.begin(), into.end());  // arrival order, whatever came back when
 }
 
 void Server::retire(Request &r, Status st, double now) {
@@ -253,44 +261,97 @@ void Server::cancel(int64_t id) {
     }
 }
 
-int Server::step(double now) {
-    bind_built(now);
-    admit(now);
-    if (live_.empty() && building_ + regridding_ > 0) {
-        // nothing to step: wait (a little) for a build or a regrid to end rather than spin
-        {
-            std::unique_lock<std::mutex> lk(mu_);
-            built_cv_.wait_for(lk, std::chrono::milliseconds(50), [&] { return !built_.empty(); });
-        }
-        bind_built(clock());
-    }
-    if (live_.empty()) return regridding_;
-    std::vector<Run *> set;
-    for (int64_t id : live_) set.push_back(reqs_.at(id).run.get());
-    // one launch set per precision and Poisson solver (different kernels); the sets of
-    // earlier mixes are dropped, so cached tables do not pile up beside the budget
-    std::vector<std::vector<Run *>> used;
-    std::map<Run *, double> t_before, dt_of;
-    for (Run *r : set) t_before[r] = r->S->time;
+// One launch set per precision, Poisson solver and FP64 kernel form (different kernels).
+static std::vector<std::vector<Run *>> partition(const std::vector<Run *> &set) {
+    std::vector<std::vector<Run *>> parts;
     for (int prec : {kF64, kF32})
         for (int pois : {kPoissonLU, kPoissonScan})
             for (int fast : {0, 1}) {
                 std::vector<Run *> part;
                 for (Run *r : set)
                     if (r->precision == prec && r->poisson == pois && r->fast64 == fast) part.push_back(r);
-                if (part.empty()) continue;
-                auto dt = eng.calculate_dt(part);
-                for (size_t k = 0; k < part.size(); k++) dt_of[part[k]] = dt[k];
-                eng.advance(part, dt);
-                used.push_back(part);
+                if (!part.empty()) parts.push_back(part);
             }
-    eng.retain_sets(used);
+    return parts;
+}
+
+bool Server::regrid_due(const Request &r, double t_before) const {
+    // the reference driver's rule, with the time before the step (veritas.cpp:146-151)
+    return r.regrid && regrid_enabled && r.run->S->maxDepth > 0 && r.regrid_counter > 20 && t_before > regrid_after;
+}
+
+int Server::step(double now) {
+    // VX_TRACE_SERVE=1: wall time of the loop's phases, summed over steps, on stderr at the end
+    static const bool trace = std::getenv("VX_TRACE_SERVE") != nullptr;
+    double tp = clock();
+    auto phase = [&](int k) {
+        if (!trace) return;
+        const double t = clock();
+        phase_s_[k] += t - tp;
+        tp = t;
+    };
+    if (live_.empty()) {  // otherwise the previous step bound and admitted while it ran
+        bind_built(now, live_);
+        admit(now);
+        if (live_.empty() && building_ + regridding_ > 0) {
+            // nothing to step: wait (a little) for a build or a regrid to end rather than spin
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                built_cv_.wait_for(lk, std::chrono::milliseconds(50), [&] { return !built_.empty(); });
+            }
+            bind_built(clock(), live_);
+        }
+        phase(0);
+        if (live_.empty()) return regridding_;
+    }
+    if (trace) (live_ == predicted_ ? hits_ : misses_)++;
+    std::vector<Run *> set;
+    for (int64_t id : live_) set.push_back(reqs_.at(id).run.get());
+    std::vector<std::vector<Run *>> used = partition(set);
+    std::map<Run *, double> t_before, dt_of;
+    for (Run *r : set) t_before[r] = r->S->time;
+    for (auto &part : used) {
+        auto dt = eng.calculate_dt(part);
+        for (size_t k = 0; k < part.size(); k++) dt_of[part[k]] = dt[k];
+        eng.advance(part, dt);
+    }
+    phase(1);
+    // While the step runs: bind what the workers finished, admit, and build the launch
+    // sets (tables and graphs) of the next step's mix as far as it is known now — the
+    // solves that neither finish nor regrid after this step, and the runs just bound.  A
+    // solve that fails or is cancelled meanwhile changes the mix; its sets are then built
+    // at the next step as before.
+    std::vector<int64_t> fresh;
+    bind_built(clock(), fresh);
+    admit(clock(), (int)fresh.size());
+    std::vector<Run *> next;
+    {
+        std::vector<int64_t> ids;
+        for (int64_t id : live_) {
+            const Request &r = reqs_.at(id);
+            if (r.done_steps + 1 < r.steps && !regrid_due(r, t_before[r.run.get()])) ids.push_back(id);
+        }
+        ids.insert(ids.end(), fresh.begin(), fresh.end());
+        std::sort(ids.begin(), ids.end());
+        for (int64_t id : ids) next.push_back(reqs_.at(id).run.get());
+        if (trace) predicted_ = ids;
+    }
+    phase(2);
+    auto next_parts = partition(next);
+    for (auto &part : next_parts) eng.prepare(part);
+    phase(3);
+    // the sets of earlier mixes are dropped, so cached tables do not pile up beside the budget
+    std::vector<std::vector<Run *>> keep = used;
+    keep.insert(keep.end(), next_parts.begin(), next_parts.end());
+    eng.retain_sets(keep);
     // health: E_x0 (updated every stage from phi, which the solve makes depend on every
     // cell's charge) turns non-finite within a step once any f, charge or field value has
     std::vector<double> ex0(set.size(), 0.0);
     for (size_t k = 0; k < set.size(); k++)
         VX_CUDA(cudaMemcpyAsync(&ex0[k], set[k]->F.ex0, sizeof(double), cudaMemcpyDeviceToHost, eng.stream));
     eng.sync();
+    eng.flush_prepared();  // the next sets' table copies, queued now that the stream is idle
+    phase(4);
     std::map<Run *, double> ex0_of;
     for (size_t k = 0; k < set.size(); k++) ex0_of[set[k]] = ex0[k];
     const double tnow = clock();
@@ -312,27 +373,26 @@ int Server::step(double now) {
             retire(r, kDone, tnow);
             continue;
         }
-        // the reference driver's regrid rule, with the time before the step (veritas.cpp:146-151)
         // The regrid runs on a worker thread while the others step on; the solve sits out
         // of the batch until it is back, so its own sequence (step, regrid, step) and bits
         // are those of a plain run.
-        if (r.regrid && regrid_enabled && run->S->maxDepth > 0) {
-            if (r.regrid_counter > 20 && t_before[run] > regrid_after) {
-                r.regrid_counter = 0;
-                eng.forget(run);  // the step is synchronised above
-                Build b;
-                b.id = id;
-                b.regrid = true;
-                b.run = std::move(r.run);
-                r.out = true;
-                regridding_++;
-                regrids.push_back(std::move(b));
-                continue;
-            }
-            r.regrid_counter++;
+        if (regrid_due(r, t_before[run])) {
+            r.regrid_counter = 0;
+            eng.forget(run);  // the step is synchronised above
+            Build b;
+            b.id = id;
+            b.regrid = true;
+            b.run = std::move(r.run);
+            r.out = true;
+            regridding_++;
+            regrids.push_back(std::move(b));
+            continue;
         }
+        if (r.regrid && regrid_enabled && run->S->maxDepth > 0) r.regrid_counter++;
         still.push_back(id);
     }
+    still.insert(still.end(), fresh.begin(), fresh.end());
+    std::sort(still.begin(), still.end());  // arrival order
     live_ = still;
     if (!regrids.empty()) {
         {
@@ -341,6 +401,7 @@ int Server::step(double now) {
         }
         cv_.notify_all();
     }
+    phase(5);
     return (int)live_.size() + regridding_;
 }
 

@@ -77,8 +77,12 @@ private:
         std::string error;
     };
     static constexpr int kWorkers = 4;
-    void admit(double now);
-    void bind_built(double now);
+    // Admits waiting requests in order while slots and budget allow (bound_meanwhile: runs
+    // bound during the current step, not yet in live_).
+    void admit(double now, int bound_meanwhile = 0);
+    // Moves the runs the workers finished to `into` (live from then on).
+    void bind_built(double now, std::vector<int64_t> &into);
+    bool regrid_due(const Request &r, double t_before) const;
     void retire(Request &r, Status st, double now);
     void worker_loop(Engine *weng);
     Engine &eng;
@@ -92,6 +96,9 @@ private:
     int building_ = 0, regridding_ = 0;
     std::vector<int64_t> finished_order_;
     std::chrono::steady_clock::time_point t0_ = std::chrono::steady_clock::now();
+    double phase_s_[6] = {};  // VX_TRACE_SERVE: the loop's time per phase
+    int hits_ = 0, misses_ = 0;
+    std::vector<int64_t> predicted_;
     // worker threads: builds and regrids in (regrids first), finished runs out
     std::mutex mu_;
     std::condition_variable cv_, built_cv_;

@@ -31,6 +31,18 @@ inline void vx_launch(void (*kernel)(KP...), dim3 grid, dim3 block, size_t smem,
     cfg.numAttrs = g_launch_pdl ? 1 : 0;
     cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);  // errors surface through cudaGetLastError
 }
+// Without the attribute: for the launch-set table kernels, queued from the host behind a
+// running step's graph (nothing to overlap with there).
+template <typename... KP, typename... A>
+inline void vx_launch_plain(void (*kernel)(KP...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                            A &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
 
 // One 32(p) x 8(x) tile of a patch's padded block; (i0, j0) is its lower corner in
 // reference indices (>= -2).
@@ -283,6 +295,9 @@ struct OpSegment {
     int count, base;
 };
 void merge_ghost_ops(const OpSegment *segs, int nseg, GhostOp *dst, cudaStream_t s);
+// bytes (a multiple of 16) from page-locked host memory, given by its device address, to
+// device memory, copied by a kernel
+void copy_from_host(const void *src_dev, void *dst, size_t bytes, cudaStream_t s);
 void merge_iface_ops(const OpSegment *segs, int nseg, IfaceOp *dst, cudaStream_t s);
 void merge_csync_ops(const OpSegment *segs, int nseg, CSyncOp *dst, cudaStream_t s);
 void launch_csync(const void *patches, const CSyncOp *ops, int n, int prec, cudaStream_t s);
