@@ -41,9 +41,11 @@ public:
     // Queue a solve of `steps` RK steps that arrived at `arrival` (seconds on clock()).
     int64_t submit(const LaserSlabParams &p, int precision, int64_t steps, double arrival,
                    const std::string &state_path, int poisson = kPoissonLU, int regrid = 1, int fast64 = 0);
-    // Bind the runs built since the last call, admit what fits (its runs are built on
-    // the builder thread), advance every live solve one step, regrid those whose counter
-    // says so, retire the finished, failed and cancelled ones.  Returns the live count.
+    // Advance every live solve one step; meanwhile bind the runs the workers finished,
+    // admit what fits (its runs are built on the worker threads) and build the next
+    // step's launch sets; then hand the solves whose counter says so to the workers for
+    // their regrid and retire the finished, failed and cancelled ones.  Returns the live
+    // count (solves out for a regrid included).
     int step(double now);
     // Withdraws a request that has not finished: a waiting one leaves the queue, one being
     // built is dropped when its build ends, a live one is retired now (no state written).
