@@ -1801,10 +1801,7 @@ void Engine::prepare(const std::vector<Run *> &set) { get_set(set, true); }
 void Engine::advance(const std::vector<Run *> &set, const std::vector<double> &dt) {
     LaunchSet &L = get_set(set);
     fill_params(L, set, dt);
-    // A set's first step is launched kernel by kernel, its graph captured from its second
-    // on: a serving loop's mix changes almost every step, and capturing and instantiating
-    // a graph for one step costs more than the launches it saves.
-    if (use_graphs && L.steps++ > 0) {
+    if (use_graphs) {
         capture_graph(L);
         VX_CUDA(cudaGraphLaunch(L.graph, stream));
     } else {

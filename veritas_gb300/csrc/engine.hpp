@@ -291,7 +291,6 @@ struct LaunchSet {
     std::vector<std::function<void()>> pending_gathers;
     DevBuf dsegs[3];
     cudaGraphExec_t graph = nullptr;
-    int steps = 0;  // steps advanced with this set (its graph is captured at the second)
     ~LaunchSet();
 };
 
