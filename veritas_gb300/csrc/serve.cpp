@@ -316,8 +316,8 @@ int Server::step(double now) {
         eng.advance(part, dt);
     }
     phase(1);
-    // While the step runs: bind what the workers finished, admit, and build the launch
-    // sets (tables and graphs) of the next step's mix as far as it is known now — the
+    // While the step runs: bind what the workers finished, admit, and build the host
+    // tables of the launch sets of the next step's mix as far as it is known now — the
     // solves that neither finish nor regrid after this step, and the runs just bound.  A
     // solve that fails or is cancelled meanwhile changes the mix; its sets are then built
     // at the next step as before.
@@ -346,6 +346,7 @@ int Server::step(double now) {
     eng.retain_sets(keep);
     // health: E_x0 (updated every stage from phi, which the solve makes depend on every
     // cell's charge) turns non-finite within a step once any f, charge or field value has
+    // gone non-finite
     std::vector<double> ex0(set.size(), 0.0);
     for (size_t k = 0; k < set.size(); k++)
         VX_CUDA(cudaMemcpyAsync(&ex0[k], set[k]->F.ex0, sizeof(double), cudaMemcpyDeviceToHost, eng.stream));
