@@ -793,8 +793,8 @@ void Engine::drop_idle(std::unique_ptr<LaunchSet> &L) {
     DevBuf a = std::move(L->arena);
     L.reset();
     if (!a.p || !a.own) return;
-    if (a.bytes > kArenaCacheBytes) return;  // freed
-    while (arena_cache_bytes_ + a.bytes > kArenaCacheBytes && !arena_cache_.empty()) {
+    if (a.bytes > arena_cache_limit) return;  // freed
+    while (arena_cache_bytes_ + a.bytes > arena_cache_limit && !arena_cache_.empty()) {
         auto it = arena_cache_.begin();  // the smallest goes first
         arena_cache_bytes_ -= it->first;
         arena_cache_.erase(it);

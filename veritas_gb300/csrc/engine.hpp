@@ -372,12 +372,12 @@ public:
     // Table storage of dropped launch sets, kept for the next sets (a serving loop builds
     // one almost every step, and cudaMalloc beside running kernels and other threads'
     // allocations costs milliseconds: a set's gathered op tables can take hundreds of MB);
-    // bounded by kArenaCacheBytes.
+    // at most arena_cache_limit bytes are kept.
     DevBuf take_arena(size_t bytes);
+    size_t arena_cache_limit = (size_t)2 << 30;
     // Page-locked staging of at least `bytes` for the set tables' copy (grown as needed);
     // its device address in pinned_dev_.
     void *pinned_staging(size_t bytes);
-    static constexpr size_t kArenaCacheBytes = (size_t)2 << 30;
     // Builds (or finds) the launch set of `set`, host work only: a serving loop prepares
     // the next step's sets while the current step runs.  The sets' table copies are
     // queued by flush_prepared() (or their first use).

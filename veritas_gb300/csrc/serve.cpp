@@ -51,7 +51,10 @@ size_t Server::estimate_bytes(const LaserSlabParams &p, int precision) {
 }
 
 Server::Server(Engine &e, size_t budget, int max_live) : eng(e), budget_(budget), max_live_(max_live) {
-    for (int w = 0; w < kWorkers; w++) worker_eng_.emplace_back(new Engine(e.device));
+    for (int w = 0; w < kWorkers; w++) {
+        worker_eng_.emplace_back(new Engine(e.device));
+        worker_eng_.back()->arena_cache_limit = (size_t)256 << 20;  // single-run sets only
+    }
     VX_CUDA(cudaSetDevice(e.device));  // the worker engines' constructors made it current too
     for (int w = 0; w < kWorkers; w++) workers_.emplace_back([this, w] { worker_loop(worker_eng_[w].get()); });
 }
